@@ -33,6 +33,8 @@ typedef struct {
   uint64_t drawn;     /* number of 24-bit outputs delivered so far */
 } oracle_ranlux;
 
+/* 0: C library log in the ziggurat tail (as GSL on glibc); 1: correctly rounded log. */
+void oracle_rng_set_cr_log(int on);
 void oracle_ranlux_seed(oracle_ranlux *r, unsigned long seed, unsigned lux);
 uint32_t oracle_ranlux_next(oracle_ranlux *r);       /* integer in [0, 2^24) */
 double oracle_ranlux_uniform(oracle_ranlux *r);      /* next / 2^24 */
