@@ -1,0 +1,95 @@
+"""ctypes binding of libgicgpu.so (include/gicgpu.h).
+
+The CUDA library is the only implementation of the field-realisation path: if
+it is missing, loading fails loudly instead of falling back to anything else.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, 'libgicgpu.so')
+
+GIC_OK = 0
+GIC_ERR_INVALID_ARG = -1
+GIC_ERR_OOM = -2
+GIC_ERR_CUDA = -3
+GIC_ERR_TIMEOUT = -4
+GIC_ERR_NOT_READY = -5
+GIC_ERR_INTERNAL = -6
+
+GIC_FP64 = 0
+GIC_MIXED = 1
+
+GIC_SEED_REAL_SPACE = 0
+GIC_SEED_FOURIER_SERIAL = 1
+GIC_SEED_FOURIER_PARALLEL = 2
+GIC_SEED_FOURIER_REVERSE = 3
+
+GIC_FIELD_NOISE = 0
+GIC_FIELD_DELTA = 1
+GIC_FIELD_PSI_X = 2
+GIC_FIELD_PSI_Y = 3
+GIC_FIELD_PSI_Z = 4
+
+
+class GicDeviceOpts(ctypes.Structure):
+    _fields_ = [('precision', ctypes.c_int), ('device', ctypes.c_int), ('mem_limit', ctypes.c_size_t)]
+
+
+class GicCosmo(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_double) for name in
+                ('omega_m', 'omega_lambda', 'omega_b', 'hubble', 'sigma8', 'ns', 'redshift')]
+
+
+_P = ctypes.c_void_p
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.c_int
+# symbol -> argument types (all return int unless noted)
+SIGNATURES = {
+    'gic_create': [ctypes.POINTER(_P), ctypes.POINTER(GicDeviceOpts)],
+    'gic_destroy': [_P],
+    'gic_last_error': [_P],
+    'gic_level_add': [_P, ctypes.c_double, _I, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                      ctypes.POINTER(_I)],
+    'gic_set_cosmology': [_P, ctypes.POINTER(GicCosmo)],
+    'gic_set_transfer': [_P, _D, _I, _I],
+    'gic_get_normalisation': [_P, _D, _D],
+    'gic_draw_noise': [_P, ctypes.c_ulong, _I],
+    'gic_gaussian_stream': [_P, ctypes.c_ulong, ctypes.c_size_t, _D],
+    'gic_set_noise': [_P, _I, _D],
+    'gic_zeldovich': [_P, _I],
+    'gic_fetch_level': [_P, _I, _I, _D],
+    'gic_fetch_particles': [_P, _I, _D, _D],
+    'gic_fft': [_P, _I, _I, _I],
+    'gic_chi2': [_P, _D],
+}
+
+_lib = None
+
+
+def load():
+    """Load libgicgpu.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError('libgicgpu.so is not built (run genetic_gb300/build.py): %s' % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, args in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_char_p if name == 'gic_last_error' else ctypes.c_int
+    _lib = lib
+    return lib
+
+
+class GicError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__('%s (status %d)' % (message, code))
+        self.code = code
+
+
+def check(ctx, status):
+    if status != GIC_OK:
+        msg = load().gic_last_error(ctx)
+        raise GicError(status, msg.decode() if msg else 'error')

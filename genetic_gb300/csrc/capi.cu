@@ -1,0 +1,365 @@
+// C ABI entry points (include/gicgpu.h).  Each call validates its arguments,
+// runs on the context's CUDA stream, synchronises before returning and turns
+// every failure into a status code plus a message.
+#include "gic_internal.h"
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <new>
+
+struct gic_ctx {
+  gic::Context impl;
+};
+
+namespace gic {
+
+[[noreturn]] void fail(int code, const std::string &msg) { throw Error{code, msg}; }
+
+void cuda_check(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    fail(e == cudaErrorMemoryAllocation ? GIC_ERR_OOM : GIC_ERR_CUDA,
+         std::string(what) + ": " + cudaGetErrorString(e));
+  }
+}
+
+double velocity_to_offset_ratio(const Cosmo &c);
+
+namespace {
+
+template <typename T>
+__global__ void k_unpad_real(const T *src, double *dst, int n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t m = (size_t)n * n * n;
+  if (i >= m) return;
+  size_t row = i / n, z = i % n;
+  dst[i] = (double)src[row * (size_t)(2 * (n / 2 + 1)) + z];
+}
+
+template <typename T>
+__global__ void k_to_double(const T *src, double *dst, size_t count) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) dst[i] = (double)src[i];
+}
+
+template <typename T>
+__global__ void k_from_double(const double *src, T *dst, size_t count) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) dst[i] = (T)src[i];
+}
+
+// sum over the half spectrum of w |c|^2, w = 1 on the kz = 0, N/2 planes, else 2
+template <typename T>
+__global__ void k_chi2_partial(const T *c, int n, double *partial) {
+  __shared__ double red[256];
+  const int H = n / 2, S = H + 1;
+  size_t nc = (size_t)n * n * S;
+  double acc = 0;
+  for (size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x; id < nc; id += (size_t)gridDim.x * blockDim.x) {
+    int kz = (int)(id % S);
+    double re = (double)c[2 * id], im = (double)c[2 * id + 1];
+    double w = (kz == 0 || kz == H) ? 1.0 : 2.0;
+    acc += w * (re * re + im * im);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+Level &level_at(Context &c, int level) {
+  if (level < 0 || level >= (int)c.levels.size()) fail(GIC_ERR_INVALID_ARG, "no such level");
+  return *c.levels[level];
+}
+
+void use_device(Context &c) { GIC_CUDA(cudaSetDevice(c.device)); }
+
+template <typename T>
+void fetch_typed(Context &c, Level &L, int what, double *host) {
+  cudaStream_t s = c.stream;
+  static thread_local DevBuf *unused = nullptr;
+  (void)unused;
+  if (what == GIC_FIELD_NOISE) {
+    if (!L.have_noise) fail(GIC_ERR_NOT_READY, "white noise has not been drawn");
+    size_t count = 2 * L.ncomplex();
+    if (sizeof(T) == 8) {
+      GIC_CUDA(cudaMemcpyAsync(host, L.noise.ptr, count * sizeof(double), cudaMemcpyDeviceToHost, s));
+    } else {
+      c.reduce.ensure(count * sizeof(double));
+      k_to_double<T><<<(unsigned)((count + 255) / 256), 256, 0, s>>>(L.noise.as<T>(), c.reduce.as<double>(), count);
+      GIC_CUDA(cudaGetLastError());
+      GIC_CUDA(cudaMemcpyAsync(host, c.reduce.ptr, count * sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
+  } else {
+    if (!L.have_fields) fail(GIC_ERR_NOT_READY, "fields have not been computed");
+    int f = what - GIC_FIELD_DELTA;
+    size_t m = L.ncells();
+    c.reduce.ensure(m * sizeof(double));
+    k_unpad_real<T><<<(unsigned)((m + 255) / 256), 256, 0, s>>>(L.field[f].as<T>(), c.reduce.as<double>(), L.n);
+    GIC_CUDA(cudaGetLastError());
+    GIC_CUDA(cudaMemcpyAsync(host, c.reduce.ptr, m * sizeof(double), cudaMemcpyDeviceToHost, s));
+  }
+  GIC_CUDA(cudaStreamSynchronize(s));
+}
+
+template <typename T>
+void set_noise_typed(Context &c, Level &L, const double *host) {
+  cudaStream_t s = c.stream;
+  size_t count = 2 * L.ncomplex();
+  L.noise.ensure(count * sizeof(T));
+  if (sizeof(T) == 8) {
+    GIC_CUDA(cudaMemcpyAsync(L.noise.ptr, host, count * sizeof(double), cudaMemcpyHostToDevice, s));
+  } else {
+    c.reduce.ensure(count * sizeof(double));
+    GIC_CUDA(cudaMemcpyAsync(c.reduce.ptr, host, count * sizeof(double), cudaMemcpyHostToDevice, s));
+    k_from_double<T><<<(unsigned)((count + 255) / 256), 256, 0, s>>>(c.reduce.as<double>(), L.noise.as<T>(), count);
+    GIC_CUDA(cudaGetLastError());
+  }
+  GIC_CUDA(cudaStreamSynchronize(s));
+  L.have_noise = true;
+  L.have_fields = false;
+}
+
+template <typename T>
+double chi2_typed(Context &c, Level &L) {
+  const int blocks = 256;
+  DevBuf partial;
+  partial.ensure(blocks * sizeof(double));
+  k_chi2_partial<T><<<blocks, 256, 0, c.stream>>>(L.noise.as<T>(), L.n, partial.as<double>());
+  GIC_CUDA(cudaGetLastError());
+  std::vector<double> h(blocks);
+  GIC_CUDA(cudaMemcpyAsync(h.data(), partial.ptr, blocks * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  GIC_CUDA(cudaStreamSynchronize(c.stream));
+  double s = 0;
+  for (double v : h) s += v;
+  return s;
+}
+
+thread_local std::string g_create_error;
+
+}  // namespace
+}  // namespace gic
+
+using gic::Error;
+
+#define API_BEGIN(ctxp)                                    \
+  if (!(ctxp)) return GIC_ERR_INVALID_ARG;                 \
+  gic::Context &C = (ctxp)->impl;                          \
+  try {                                                    \
+    gic::use_device(C);
+#define API_END                                            \
+  }                                                        \
+  catch (const Error &e) {                                 \
+    C.last_error = e.msg;                                  \
+    return e.code;                                         \
+  }                                                        \
+  catch (const std::bad_alloc &) {                         \
+    C.last_error = "host allocation failed";               \
+    return GIC_ERR_OOM;                                    \
+  }                                                        \
+  catch (const std::exception &e) {                        \
+    C.last_error = e.what();                               \
+    return GIC_ERR_INTERNAL;                               \
+  }                                                        \
+  C.last_error.clear();                                    \
+  return GIC_OK;
+
+extern "C" {
+
+int gic_create(gic_ctx **out, const gic_device_opts *opts) {
+  if (!out) return GIC_ERR_INVALID_ARG;
+  *out = nullptr;
+  int precision = opts ? opts->precision : GIC_FP64;
+  int device = opts ? opts->device : 0;
+  if (precision != GIC_FP64 && precision != GIC_MIXED) {
+    gic::g_create_error = "unknown precision form";
+    return GIC_ERR_INVALID_ARG;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    gic::g_create_error = "no CUDA device available";
+    return GIC_ERR_CUDA;
+  }
+  if (device < 0 || device >= ndev) {
+    gic::g_create_error = "device ordinal out of range";
+    return GIC_ERR_INVALID_ARG;
+  }
+  gic_ctx *c = new (std::nothrow) gic_ctx;
+  if (!c) return GIC_ERR_OOM;
+  c->impl.device = device;
+  c->impl.precision = precision;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->impl.stream, cudaStreamNonBlocking) != cudaSuccess) {
+    gic::g_create_error = cudaGetErrorString(cudaGetLastError());
+    delete c;
+    return GIC_ERR_CUDA;
+  }
+  *out = c;
+  return GIC_OK;
+}
+
+int gic_destroy(gic_ctx *ctx) {
+  if (!ctx) return GIC_OK;
+  cudaSetDevice(ctx->impl.device);
+  cudaStreamSynchronize(ctx->impl.stream);
+  cudaStream_t s = ctx->impl.stream;
+  delete ctx;  // frees device buffers
+  cudaStreamDestroy(s);
+  return GIC_OK;
+}
+
+const char *gic_last_error(const gic_ctx *ctx) {
+  if (!ctx) return gic::g_create_error.c_str();
+  return ctx->impl.last_error.c_str();
+}
+
+int gic_level_add(gic_ctx *ctx, double box, int n, double x0, double y0, double z0, int *level_id) {
+  API_BEGIN(ctx)
+  if (!(box > 0) || n < 2 || n % 2 || n > 2048) gic::fail(GIC_ERR_INVALID_ARG, "level needs box > 0 and an even n <= 2048");
+  for (auto &L : C.levels)
+    if (L->have_noise) gic::fail(GIC_ERR_NOT_READY, "Trying to initialize a grid after the random field was already drawn");
+  auto L = std::make_unique<gic::Level>();
+  L->n = n;
+  L->box = box;
+  L->x0[0] = x0;
+  L->x0[1] = y0;
+  L->x0[2] = z0;
+  L->dx = box / n;
+  L->periodic = C.levels.empty() ? box : C.levels[0]->periodic;
+  C.levels.push_back(std::move(L));
+  if (level_id) *level_id = (int)C.levels.size() - 1;
+  API_END
+}
+
+int gic_set_cosmology(gic_ctx *ctx, const gic_cosmo *cosmo) {
+  API_BEGIN(ctx)
+  if (!cosmo) gic::fail(GIC_ERR_INVALID_ARG, "null cosmology");
+  C.cosmo.om = cosmo->omega_m;
+  C.cosmo.ol = cosmo->omega_lambda;
+  C.cosmo.ob = cosmo->omega_b;
+  C.cosmo.h = cosmo->hubble;
+  C.cosmo.s8 = cosmo->sigma8;
+  C.cosmo.ns = cosmo->ns;
+  C.cosmo.z = cosmo->redshift;
+  C.cosmo.a = 1. / (cosmo->redshift + 1.);
+  C.have_cosmo = true;
+  API_END
+}
+
+int gic_set_transfer(gic_ctx *ctx, const double *table, int nrows, int ncols) {
+  API_BEGIN(ctx)
+  if (!table) gic::fail(GIC_ERR_INVALID_ARG, "null table");
+  gic::transfer_setup(C, table, nrows, ncols);
+  API_END
+}
+
+int gic_get_normalisation(gic_ctx *ctx, double *amplitude, double *sigma8_unnormalised) {
+  API_BEGIN(ctx)
+  if (!C.transfer.ready) gic::fail(GIC_ERR_NOT_READY, "no transfer function");
+  if (amplitude) *amplitude = C.transfer.amplitude;
+  if (sigma8_unnormalised) *sigma8_unnormalised = C.transfer.sigma8_pre;
+  API_END
+}
+
+int gic_draw_noise(gic_ctx *ctx, unsigned long seed, int mode) {
+  API_BEGIN(ctx)
+  if (C.levels.empty()) gic::fail(GIC_ERR_NOT_READY, "no grid levels");
+  for (auto &L : C.levels) {
+    gic::draw_noise_level(C, *L, seed, mode);
+    L->have_fields = false;
+  }
+  API_END
+}
+
+int gic_gaussian_stream(gic_ctx *ctx, unsigned long seed, size_t n, double *host_dst) {
+  API_BEGIN(ctx)
+  if (!host_dst && n) gic::fail(GIC_ERR_INVALID_ARG, "null buffer");
+  if (n) gic::gaussian_stream(C, seed, n, host_dst);
+  API_END
+}
+
+int gic_set_noise(gic_ctx *ctx, int level, const double *host_src) {
+  API_BEGIN(ctx)
+  if (!host_src) gic::fail(GIC_ERR_INVALID_ARG, "null buffer");
+  gic::Level &L = gic::level_at(C, level);
+  if (C.dbl()) gic::set_noise_typed<double>(C, L, host_src);
+  else gic::set_noise_typed<float>(C, L, host_src);
+  API_END
+}
+
+int gic_zeldovich(gic_ctx *ctx, int order) {
+  API_BEGIN(ctx)
+  if (order != 1) gic::fail(GIC_ERR_INVALID_ARG, "only order 1 (Zel'dovich) is available");
+  if (C.levels.empty()) gic::fail(GIC_ERR_NOT_READY, "no grid levels");
+  if (C.levels.size() > 1) gic::fail(GIC_ERR_INVALID_ARG, "zoom levels are not supported yet");
+  for (auto &L : C.levels) {
+    gic::za_fields(C, *L);
+    gic::make_particles(C, *L);
+  }
+  GIC_CUDA(cudaStreamSynchronize(C.stream));
+  API_END
+}
+
+int gic_fetch_level(gic_ctx *ctx, int level, int what, double *host_dst) {
+  API_BEGIN(ctx)
+  if (!host_dst) gic::fail(GIC_ERR_INVALID_ARG, "null buffer");
+  if (what < GIC_FIELD_NOISE || what > GIC_FIELD_PSI_Z) gic::fail(GIC_ERR_INVALID_ARG, "unknown field");
+  gic::Level &L = gic::level_at(C, level);
+  if (C.dbl()) gic::fetch_typed<double>(C, L, what, host_dst);
+  else gic::fetch_typed<float>(C, L, what, host_dst);
+  API_END
+}
+
+int gic_fetch_particles(gic_ctx *ctx, int level, double *pos, double *vel) {
+  API_BEGIN(ctx)
+  gic::Level &L = gic::level_at(C, level);
+  if (!L.pos.ptr) gic::fail(GIC_ERR_NOT_READY, "particles have not been generated");
+  size_t m = L.ncells();
+  if (pos) GIC_CUDA(cudaMemcpyAsync(pos, L.pos.ptr, 3 * m * sizeof(double), cudaMemcpyDeviceToHost, C.stream));
+  if (vel) {
+    if (C.dbl()) {
+      GIC_CUDA(cudaMemcpyAsync(vel, L.vel.ptr, 3 * m * sizeof(double), cudaMemcpyDeviceToHost, C.stream));
+    } else {
+      C.reduce.ensure(3 * m * sizeof(double));
+      gic::k_to_double<float><<<(unsigned)((3 * m + 255) / 256), 256, 0, C.stream>>>(L.vel.as<float>(),
+                                                                                   C.reduce.as<double>(), 3 * m);
+      GIC_CUDA(cudaGetLastError());
+      GIC_CUDA(cudaMemcpyAsync(vel, C.reduce.ptr, 3 * m * sizeof(double), cudaMemcpyDeviceToHost, C.stream));
+    }
+  }
+  GIC_CUDA(cudaStreamSynchronize(C.stream));
+  API_END
+}
+
+int gic_fft(gic_ctx *ctx, int level, int what, int dir) {
+  API_BEGIN(ctx)
+  gic::Level &L = gic::level_at(C, level);
+  if (dir != -1 && dir != 1) gic::fail(GIC_ERR_INVALID_ARG, "dir must be -1 (forward) or +1 (inverse)");
+  gic::DevBuf *buf = what == GIC_FIELD_NOISE ? &L.noise : (what >= GIC_FIELD_DELTA && what <= GIC_FIELD_PSI_Z ? &L.field[what - 1] : nullptr);
+  if (!buf || !buf->ptr) gic::fail(GIC_ERR_NOT_READY, "field not allocated");
+  double scale = 1.0 / std::pow((double)L.n, 1.5);
+  if (C.dbl()) {
+    if (dir < 0) gic::fft_r2c_3d<double>(C, buf->as<double>(), L.n, scale);
+    else gic::fft_c2r_3d<double>(C, buf->as<double>(), L.n, scale);
+  } else {
+    if (dir < 0) gic::fft_r2c_3d<float>(C, buf->as<float>(), L.n, scale);
+    else gic::fft_c2r_3d<float>(C, buf->as<float>(), L.n, scale);
+  }
+  GIC_CUDA(cudaStreamSynchronize(C.stream));
+  API_END
+}
+
+int gic_chi2(gic_ctx *ctx, double *chi2) {
+  API_BEGIN(ctx)
+  if (!chi2) gic::fail(GIC_ERR_INVALID_ARG, "null output");
+  if (C.levels.size() != 1) gic::fail(GIC_ERR_INVALID_ARG, "chi^2 over several levels is not supported yet");
+  gic::Level &L = gic::level_at(C, 0);
+  if (!L.have_noise) gic::fail(GIC_ERR_NOT_READY, "white noise has not been drawn");
+  *chi2 = C.dbl() ? gic::chi2_typed<double>(C, L) : gic::chi2_typed<float>(C, L);
+  API_END
+}
+
+}  // extern "C"

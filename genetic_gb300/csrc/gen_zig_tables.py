@@ -40,7 +40,7 @@ if __name__ == '__main__':
     k = [0] + [int(mp.floor(s * xs[i] / xs[i + 1])) for i in range(1, 127)] + [int(mp.floor(s * R / (R + 1 / R)))]
     out = ['// Generated by gen_zig_tables.py; do not edit.', '#pragma once',
            '#define GIC_ZIG_PARAM_R %r' % g12(R),
-           'static const double kZigY[128] = {' + ', '.join(float.hex(g12(t)) for t in y) + '};',
-           'static const double kZigW[128] = {' + ', '.join(float.hex(g12(t)) for t in w) + '};',
-           'static const unsigned int kZigK[128] = {' + ', '.join('%du' % v for v in k) + '};']
+           '#define GIC_ZIG_Y_INIT {' + ', '.join(float.hex(g12(t)) for t in y) + '}',
+           '#define GIC_ZIG_W_INIT {' + ', '.join(float.hex(g12(t)) for t in w) + '}',
+           '#define GIC_ZIG_K_INIT {' + ', '.join('%du' % v for v in k) + '}']
     print('\n'.join(out))

@@ -1,0 +1,129 @@
+// Internal declarations of the GB300 field-realisation library (not part of the C-ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+#include <memory>
+#include "../../include/gicgpu.h"
+
+namespace gic {
+
+struct Error {
+  int code;
+  std::string msg;
+};
+
+[[noreturn]] void fail(int code, const std::string &msg);
+void cuda_check(cudaError_t e, const char *what);
+#define GIC_CUDA(call) ::gic::cuda_check((call), #call)
+
+// Owning device allocation.
+struct DevBuf {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+  }
+  void ensure(size_t nbytes) {  // grow-only
+    if (nbytes <= bytes && ptr) return;
+    release();
+    if (nbytes == 0) return;
+    cudaError_t e = cudaMalloc(&ptr, nbytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      ptr = nullptr;
+      fail(GIC_ERR_OOM, "cudaMalloc of " + std::to_string(nbytes) + " bytes failed");
+    }
+    bytes = nbytes;
+  }
+  template <typename T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+// One grid level: N^3 cells of a cube of side `box` whose lower corner is x0.
+struct Level {
+  int n = 0;
+  double box = 0, x0[3] = {0, 0, 0}, dx = 0;
+  double periodic = 0;  // size of the periodic simulation domain (box of level 0)
+  size_t ncomplex() const { return (size_t)n * n * (n / 2 + 1); }
+  size_t ncells() const { return (size_t)n * n * n; }
+  double kmin() const;
+  // half-spectrum (complex) fields, element type by precision; in place with the
+  // padded real layout of an r2c transform (row stride 2(n/2+1) reals)
+  DevBuf noise;          // white noise (unit variance per real d.o.f.)
+  DevBuf field[4];       // delta, psi_x, psi_y, psi_z
+  DevBuf sqrtp;          // double sqrt(P_grid) per integer |k|^2
+  DevBuf pos, vel;       // particles: pos double[3M], vel (precision)[3M]
+  bool have_noise = false;
+  bool have_fields = false;
+};
+
+struct Cosmo {
+  double om, ol, ob, h, s8, ns, z, a;
+};
+
+// Device-resident transfer function: natural cubic spline of ln T vs ln k.
+struct Transfer {
+  int nrows = 0;
+  DevBuf lnk, lnT_all, c_all, lnT_dm, c_dm;  // doubles
+  double lnk_min = 0, lnk_max = 0;
+  double amplitude = 0;  // (sigma8/sigma8_pre * D(a)/D(1))^2
+  double sigma8_pre = 0;
+  bool ready = false;
+};
+
+struct FftTables {
+  // twiddles w^m = exp(-2 pi i m / n), m < n, per size and precision
+  struct Entry {
+    int n;
+    DevBuf f32, f64;
+  };
+  std::vector<std::unique_ptr<Entry>> entries;
+  const void *get(int n, bool dbl, cudaStream_t s);
+};
+
+struct RngScratch {
+  DevBuf raw, gauss, owner, segtab, segentry, segbase, streams, chunkmul, flags;
+  int chunkmul_count = 0;
+};
+
+struct Context {
+  int device = 0;
+  int precision = GIC_FP64;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  std::vector<std::unique_ptr<Level>> levels;
+  Cosmo cosmo{};
+  bool have_cosmo = false;
+  Transfer transfer;
+  FftTables fft;
+  RngScratch rng;
+  DevBuf reduce;  // small scratch for reductions
+  bool dbl() const { return precision == GIC_FP64; }
+};
+
+// fft.cu
+template <typename T>
+void fft_c2r_3d(Context &ctx, T *data, int n, double scale);
+template <typename T>
+void fft_r2c_3d(Context &ctx, T *data, int n, double scale);
+
+// rng.cu
+void draw_noise_level(Context &ctx, Level &L, unsigned long long seed, int mode);
+void gaussian_stream(Context &ctx, unsigned long long seed, size_t n, double *host);
+
+// kspace.cu
+void transfer_setup(Context &ctx, const double *table, int nrows, int ncols);
+void build_sqrtp_table(Context &ctx, Level &L);
+void za_fields(Context &ctx, Level &L);
+
+// particles.cu
+void make_particles(Context &ctx, Level &L);
+
+}  // namespace gic

@@ -1,0 +1,295 @@
+// Power spectrum and fused k-space kernels.
+//
+// Transfer function: genetIC reads a CAMB table, normalises each species column
+// by the first row's column 1 and interpolates ln T against ln k with a natural
+// cubic spline, returning 0 outside the table
+// (genetIC/src/cosmology/camb.hpp:224-268, genetIC/src/tools/numerics/interpolation.hpp:81-110).
+// P(k) = A k^ns T(k)^2 with A = (sigma8 / sigma8_pre * D(a)/D(1))^2, sigma8_pre
+// from a 50 000-step Riemann sum over a top-hat window of radius 8 Mpc/h
+// (camb.hpp:289-328).  On a grid: P_grid = P(k) (2 pi / L)^3 / (2 pi)^3 N^3
+// (camb.hpp:101-139) and the field is multiplied by P_grid^0.5 (field.hpp:394-412).
+//
+// GB300 layout choice: P_grid depends on k only through the integer
+// q = kx^2 + ky^2 + kz^2 <= 3 (N/2)^2, so sqrt(P_grid) is tabulated once per
+// grid by q (196 609 doubles at N = 512, resident in L2) and every k-space
+// kernel reads it with one lookup instead of evaluating the spline per cell.
+#include "gic_internal.h"
+#include <cmath>
+#include <vector>
+
+namespace gic {
+namespace {
+
+// natural cubic spline (second-derivative form) solved by one thread; n ~ 10^3
+__global__ void k_spline_solve(const double *x, const double *y, double *c, int n, double *work) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  for (int i = 0; i < n; ++i) c[i] = 0.0;
+  if (n < 3) return;
+  int m = n - 2;
+  double *diag = work, *off = work + m, *rhs = work + 2 * m;
+  for (int i = 0; i < m; ++i) {
+    double h0 = x[i + 1] - x[i], h1 = x[i + 2] - x[i + 1];
+    double g0 = h0 != 0.0 ? 1.0 / h0 : 0.0, g1 = h1 != 0.0 ? 1.0 / h1 : 0.0;
+    off[i] = h1;
+    diag[i] = 2.0 * (h0 + h1);
+    rhs[i] = 3.0 * ((y[i + 2] - y[i + 1]) * g1 - (y[i + 1] - y[i]) * g0);
+  }
+  for (int i = 1; i < m; ++i) {
+    double w = off[i - 1] / diag[i - 1];
+    diag[i] -= w * off[i - 1];
+    rhs[i] -= w * rhs[i - 1];
+  }
+  c[m] = rhs[m - 1] / diag[m - 1];
+  for (int i = m - 1; i-- > 0;) c[i + 1] = (rhs[i] - off[i] * c[i + 2]) / diag[i];
+}
+
+__device__ double spline_eval(const double *x, const double *y, const double *c, int n, double v) {
+  if (v < x[0] || v > x[n - 1]) return 0.0;
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) {
+    int mid = (lo + hi) >> 1;
+    if (x[mid] > v) hi = mid; else lo = mid;
+  }
+  double h = x[lo + 1] - x[lo];
+  double dx = v - x[lo];
+  double dy = y[lo + 1] - y[lo];
+  double ci = c[lo], ci1 = c[lo + 1];
+  double b = dy / h - h * (ci1 + 2.0 * ci) / 3.0;
+  double d = (ci1 - ci) / (3.0 * h);
+  return y[lo] + dx * (b + dx * (ci + dx * d));
+}
+
+// T(k) from the log-log spline, zero outside the table
+__device__ double transfer_at(const double *lx, const double *ly, const double *c, int n, double k) {
+  double l = log(k);
+  if (l < lx[0] || l > lx[n - 1]) return 0.0;
+  return exp(spline_eval(lx, ly, c, n, l));
+}
+
+// k_i of `for (k = kmin; k < kmax; k += dk)`, accumulated exactly as written
+__global__ void k_sigma8_ks(double kmin, double kmax, double dk, double *ks, int cap, int *count) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  int i = 0;
+  for (double k = kmin; k < kmax && i < cap; k += dk) ks[i++] = k;
+  *count = i;
+}
+
+__global__ void k_sigma8_terms(const double *ks, const int *count, double ns, double radius, const double *lx,
+                               const double *ly, const double *c, int n, double *partial) {
+  __shared__ double red[256];
+  int cnt = *count;
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+    double k = ks[i];
+    double t = transfer_at(lx, ly, c, n, k);
+    double kr = k * radius;
+    double w = (sin(kr) - kr * cos(kr)) / (kr * kr * kr);
+    acc += pow(k, ns + 2.) * w * w * t * t;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+__global__ void k_sqrtp_table(double *tab, long long nq, double kmin, double amplitude, double ns, double norm,
+                              const double *lx, const double *ly, const double *c, int n) {
+  long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  double k = sqrt((double)q) * kmin;
+  double p = 0.0;
+  if (k != 0.0) {
+    double t = transfer_at(lx, ly, c, n, k);
+    p = amplitude * pow(k, ns) * t * t;
+  }
+  double spec = p * norm;
+  if (spec != 0.0) spec = pow(spec, 0.5);
+  tab[q] = spec;
+}
+
+template <typename T> struct V2;
+template <> struct V2<float> { using type = float2; };
+template <> struct V2<double> { using type = double2; };
+
+// delta = w sqrt(P); psi_i = i k_i delta / k^2, zero at k = 0 and at the
+// positive Nyquist component (zeldovich.hpp:155-181)
+template <typename T>
+__global__ void k_za_fields(const typename V2<T>::type *noise, const double *sqrtp, int n, T kmin,
+                            typename V2<T>::type *delta, typename V2<T>::type *px, typename V2<T>::type *py,
+                            typename V2<T>::type *pz) {
+  using C = typename V2<T>::type;
+  const int H = n / 2, S = H + 1;
+  size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t nc = (size_t)n * n * S;
+  if (id >= nc) return;
+  int iz = (int)(id % S);
+  size_t r = id / S;
+  int iy = (int)(r % n), ix = (int)(r / n);
+  int kx = ix > H ? ix - n : ix;
+  int ky = iy > H ? iy - n : iy;
+  int kz = iz;
+  long long q = (long long)kx * kx + (long long)ky * ky + (long long)kz * kz;
+  T s = (T)sqrtp[q];
+  C w = noise[id];
+  C d;
+  d.x = w.x * s;
+  d.y = w.y * s;
+  delta[id] = d;
+  T fx = (T)kx * kmin, fy = (T)ky * kmin, fz = (T)kz * kmin;
+  T kk = fx * fx + fy * fy + fz * fz;
+  C base;
+  base.x = -d.y / kk;
+  base.y = d.x / kk;
+  C z;
+  z.x = 0;
+  z.y = 0;
+  C rx = z, ry = z, rz = z;
+  if (q != 0) {
+    if (kx != H) { rx.x = base.x * fx; rx.y = base.y * fx; }
+    if (ky != H) { ry.x = base.x * fy; ry.y = base.y * fy; }
+    if (kz != H) { rz.x = base.x * fz; rz.y = base.y * fz; }
+  }
+  px[id] = rx;
+  py[id] = ry;
+  pz[id] = rz;
+}
+
+// Carroll, Press & Turner growth-factor fit, as genetIC evaluates it
+// (genetIC/src/cosmology/parameters.hpp:55-70), on the host: a scalar.
+double growth_factor(double a, double Om, double Ol) {
+  double Hsq = Om / powf((float)a, 3.0f) + (1. - Om - Ol) / a / a + Ol;
+  double d = 2.5 * a * Om / pow(a, 3.0) / Hsq /
+             (pow(Om / Hsq / a / a / a, 4.f / 7.f) - Ol / Hsq + (1. + 0.5 * Om / pow(a, 3.0) / Hsq) * (1. + 1. / 70. * Ol / Hsq));
+  return d;
+}
+
+}  // namespace
+
+double Level::kmin() const { return 2. * M_PI / box; }
+
+void transfer_setup(Context &ctx, const double *table, int nrows, int ncols) {
+  if (!ctx.have_cosmo) fail(GIC_ERR_NOT_READY, "set the cosmology before the transfer function");
+  if (ncols != 7 && ncols != 13) fail(GIC_ERR_INVALID_ARG, "CAMB transfer file doesn't have a sensible number of columns");
+  if (nrows < 2) fail(GIC_ERR_INVALID_ARG, "transfer table too short");
+  // species columns: dm -> 1, all -> 6; normalised by the first row's column 1
+  double tnorm = table[1];
+  std::vector<double> k, tall, tdm;
+  for (int j = 0; j < nrows; ++j) {
+    if (table[(size_t)ncols * j] > 0) {
+      k.push_back(table[(size_t)ncols * j]);
+      tdm.push_back(table[(size_t)ncols * j + 1] / tnorm);
+      tall.push_back(table[(size_t)ncols * j + 6] / tnorm);
+    }
+  }
+  auto logs = [](const std::vector<double> &x, const std::vector<double> &y, std::vector<double> &lx,
+                 std::vector<double> &ly) {
+    for (size_t i = 0; i < x.size(); ++i) {
+      double a = std::log(x[i]), b = std::log(y[i]);
+      if (std::isfinite(a) && std::isfinite(b)) {
+        lx.push_back(a);
+        ly.push_back(b);
+      }
+    }
+  };
+  std::vector<double> lx_all, ly_all, lx_dm, ly_dm;
+  logs(k, tall, lx_all, ly_all);
+  logs(k, tdm, lx_dm, ly_dm);
+  if (lx_all.size() < 2 || lx_dm.size() < 2)
+    fail(GIC_ERR_INVALID_ARG, "Could not find enough valid values in the transfer function");
+  if (lx_all.size() != lx_dm.size()) fail(GIC_ERR_INVALID_ARG, "transfer columns with invalid entries are not supported");
+  Transfer &T = ctx.transfer;
+  int n = (int)lx_all.size();
+  T.nrows = n;
+  cudaStream_t s = ctx.stream;
+  T.lnk.ensure(n * sizeof(double));
+  T.lnT_all.ensure(n * sizeof(double));
+  T.c_all.ensure(n * sizeof(double));
+  T.lnT_dm.ensure(n * sizeof(double));
+  T.c_dm.ensure(n * sizeof(double));
+  GIC_CUDA(cudaMemcpyAsync(T.lnk.ptr, lx_all.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+  GIC_CUDA(cudaMemcpyAsync(T.lnT_all.ptr, ly_all.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+  GIC_CUDA(cudaMemcpyAsync(T.lnT_dm.ptr, ly_dm.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+  DevBuf work;
+  work.ensure(3 * (size_t)n * sizeof(double));
+  k_spline_solve<<<1, 1, 0, s>>>(T.lnk.as<double>(), T.lnT_all.as<double>(), T.c_all.as<double>(), n,
+                                 work.as<double>());
+  k_spline_solve<<<1, 1, 0, s>>>(T.lnk.as<double>(), T.lnT_dm.as<double>(), T.c_dm.as<double>(), n,
+                                 work.as<double>());
+  GIC_CUDA(cudaGetLastError());
+
+  // sigma8 before normalisation, radius 8 Mpc/h, species "all"
+  const double radius = 8.0;
+  double kmax = std::min(k.back(), 200.0 / radius) * 0.999999;
+  double kmin = k[0] * 1.000001;
+  double dk = (kmax - kmin) / 50000.;
+  const int cap = 50100;
+  DevBuf ks, cnt, partial;
+  ks.ensure(cap * sizeof(double));
+  cnt.ensure(sizeof(int));
+  const int blocks = 64;
+  partial.ensure(blocks * sizeof(double));
+  k_sigma8_ks<<<1, 1, 0, s>>>(kmin, kmax, dk, ks.as<double>(), cap, cnt.as<int>());
+  k_sigma8_terms<<<blocks, 256, 0, s>>>(ks.as<double>(), cnt.as<int>(), ctx.cosmo.ns, radius, T.lnk.as<double>(),
+                                        T.lnT_all.as<double>(), T.c_all.as<double>(), n, partial.as<double>());
+  GIC_CUDA(cudaGetLastError());
+  std::vector<double> hp(blocks);
+  GIC_CUDA(cudaMemcpyAsync(hp.data(), partial.ptr, blocks * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GIC_CUDA(cudaStreamSynchronize(s));
+  double sum = 0;
+  for (double v : hp) sum += v;
+  double amp = 9. / 2. / M_PI / M_PI;
+  double sigma8_pre = std::sqrt(sum * amp * dk);
+  const Cosmo &c = ctx.cosmo;
+  double d_here = growth_factor(c.a, c.om, c.ol);
+  double d_today = growth_factor(1. / (1. + (double)(float)0), c.om, c.ol);
+  double renorm = (c.s8 / sigma8_pre) * (d_here / d_today);
+  T.sigma8_pre = sigma8_pre;
+  T.amplitude = renorm * renorm;
+  T.lnk_min = lx_all.front();
+  T.lnk_max = lx_all.back();
+  T.ready = true;
+  for (auto &L : ctx.levels) L->sqrtp.release();
+}
+
+void build_sqrtp_table(Context &ctx, Level &L) {
+  if (!ctx.transfer.ready) fail(GIC_ERR_NOT_READY, "no transfer function");
+  if (L.sqrtp.ptr) return;
+  long long half = L.n / 2;
+  long long nq = 3 * half * half + 1;
+  L.sqrtp.ensure(nq * sizeof(double));
+  double kw = 2. * M_PI / L.box;
+  double norm = kw * kw * kw / pow(2.f * M_PI, 3.f) * (double)L.ncells();
+  k_sqrtp_table<<<(unsigned)((nq + 255) / 256), 256, 0, ctx.stream>>>(
+      L.sqrtp.as<double>(), nq, L.kmin(), ctx.transfer.amplitude, ctx.cosmo.ns, norm, ctx.transfer.lnk.as<double>(),
+      ctx.transfer.lnT_all.as<double>(), ctx.transfer.c_all.as<double>(), ctx.transfer.nrows);
+  GIC_CUDA(cudaGetLastError());
+}
+
+template <typename T>
+static void za_fields_typed(Context &ctx, Level &L) {
+  using C = typename V2<T>::type;
+  size_t nc = L.ncomplex();
+  for (int f = 0; f < 4; ++f) L.field[f].ensure(nc * sizeof(C));
+  build_sqrtp_table(ctx, L);
+  unsigned blocks = (unsigned)((nc + 255) / 256);
+  k_za_fields<T><<<blocks, 256, 0, ctx.stream>>>(L.noise.as<C>(), L.sqrtp.as<double>(), L.n, (T)L.kmin(),
+                                                 L.field[0].as<C>(), L.field[1].as<C>(), L.field[2].as<C>(),
+                                                 L.field[3].as<C>());
+  GIC_CUDA(cudaGetLastError());
+  double scale = 1.0 / std::pow((double)L.n, 1.5);
+  for (int f = 0; f < 4; ++f) fft_c2r_3d<T>(ctx, L.field[f].as<T>(), L.n, scale);
+  L.have_fields = true;
+}
+
+void za_fields(Context &ctx, Level &L) {
+  if (!L.have_noise) fail(GIC_ERR_NOT_READY, "white noise has not been drawn");
+  if (ctx.dbl())
+    za_fields_typed<double>(ctx, L);
+  else
+    za_fields_typed<float>(ctx, L);
+}
+
+}  // namespace gic

@@ -1,0 +1,73 @@
+// Zel'dovich particles of one level: position = cell centroid + psi, wrapped
+// into the periodic domain, velocity = psi * 100 sqrt(Om/a^3 + OL) sqrt(a)
+// (f = 1), as ZeldovichParticleEvaluator evaluates them one index at a time
+// (genetIC/src/simulation/particles/zeldovich.hpp:87-124,
+//  genetIC/src/cosmology/parameters.hpp:84-106, generator.hpp:49-53,
+//  grid.hpp:659-669 centroid, grid.hpp:519-531 wrap).
+// Here every cell of the level is evaluated in one pass over the three
+// real-space displacement fields: positions in double, velocities in the
+// working precision.
+#include "gic_internal.h"
+#include <cmath>
+
+namespace gic {
+namespace {
+
+__device__ __forceinline__ double wrap_coord(double x, double period) {
+  x = fmod(x, period);
+  if (x < 0) x += period;
+  return x;
+}
+
+template <typename T>
+__global__ void k_particles(const T *px, const T *py, const T *pz, int n, double dx, double x0, double y0,
+                            double z0, double period, T ratio, double *pos, T *vel) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t m = (size_t)n * n * n;
+  if (i >= m) return;
+  size_t row = i / n;
+  int z = (int)(i % n);
+  int y = (int)(row % n);
+  int x = (int)(row / n);
+  size_t src = row * (size_t)(2 * (n / 2 + 1)) + z;
+  T sx = px[src], sy = py[src], sz = pz[src];
+  vel[3 * i + 0] = sx * ratio;
+  vel[3 * i + 1] = sy * ratio;
+  vel[3 * i + 2] = sz * ratio;
+  // centroid = coord * dx + offset + dx/2
+  double cx = (double)x * dx + x0 + dx / 2;
+  double cy = (double)y * dx + y0 + dx / 2;
+  double cz = (double)z * dx + z0 + dx / 2;
+  pos[3 * i + 0] = wrap_coord((double)sx + cx, period);
+  pos[3 * i + 1] = wrap_coord((double)sy + cy, period);
+  pos[3 * i + 2] = wrap_coord((double)sz + cz, period);
+}
+
+}  // namespace
+
+double velocity_to_offset_ratio(const Cosmo &c) {
+  double f = 1.0;
+  return f * 100. * std::sqrt(c.om / (c.a * c.a * c.a) + c.ol) * std::sqrt(c.a);
+}
+
+template <typename T>
+static void particles_typed(Context &ctx, Level &L) {
+  size_t m = L.ncells();
+  L.pos.ensure(3 * m * sizeof(double));
+  L.vel.ensure(3 * m * sizeof(T));
+  T ratio = (T)velocity_to_offset_ratio(ctx.cosmo);
+  k_particles<T><<<(unsigned)((m + 255) / 256), 256, 0, ctx.stream>>>(
+      L.field[1].as<T>(), L.field[2].as<T>(), L.field[3].as<T>(), L.n, L.dx, L.x0[0], L.x0[1], L.x0[2], L.periodic,
+      ratio, L.pos.as<double>(), L.vel.as<T>());
+  GIC_CUDA(cudaGetLastError());
+}
+
+void make_particles(Context &ctx, Level &L) {
+  if (!L.have_fields) fail(GIC_ERR_NOT_READY, "displacement fields not computed");
+  if (ctx.dbl())
+    particles_typed<double>(ctx, L);
+  else
+    particles_typed<float>(ctx, L);
+}
+
+}  // namespace gic

@@ -1,0 +1,532 @@
+// White-noise drawing on the device, reproducing genetIC's RandomFieldGenerator
+// (genetIC/src/simulation/field/randomfieldgenerator.hpp:122-260) bit for bit:
+//
+//  1. one RANLUX stream per seed (ranlxs2: luxury 794 subtract-with-borrow steps
+//     of base 2^24 per block of 24 delivered numbers, Luescher's seeding), split
+//     into chunks of kChunkBlocks blocks; each chunk's start state comes from the
+//     576-bit LCG jump (bigint576.h), then the thread steps the recurrence in
+//     registers;
+//  2. the ziggurat consumes 2, 3 or 4 numbers per attempt depending on the data,
+//     so gaussian positions in the stream are found with speculative segment
+//     walks: every segment of kSegLen numbers is walked from entry offsets
+//     0..kSpec-1 in parallel, one thread per stream chains the segments
+//     (entry of segment g+1 = exit of segment g), and a final walk writes each
+//     gaussian at its index;
+//  3. gaussian pairs are placed on Fourier modes in the reference's k-shell
+//     order; where two draws hit one stored coefficient (Hermitian folding of
+//     kz<0 and of modes with a zero component) the later draw wins, found with
+//     an atomicMax over draw indices, then one write per winning draw.
+#include "gic_internal.h"
+#include "bigint576.h"
+#include "ddlog.h"
+#include "zig_tables.h"
+#include <algorithm>
+#include <cmath>
+
+namespace gic {
+namespace {
+
+constexpr int kLux = 794;          // 24-bit steps per delivered block
+constexpr int kChunkBlocks = 16;   // blocks per generator thread
+constexpr int kSegLen = 2048;      // stream numbers per ziggurat segment
+constexpr int kSpec = 4;           // speculative entry offsets per segment
+constexpr uint32_t kUnderrun = 0xFFFFFFFFu;
+
+__constant__ double dZigY[128] = GIC_ZIG_Y_INIT;
+__constant__ double dZigW[128] = GIC_ZIG_W_INIT;
+__constant__ unsigned int dZigK[128] = GIC_ZIG_K_INIT;
+
+struct Stream {
+  unsigned long long seed;
+  unsigned long long raw_off, raw_count;      // numbers generated for this stream
+  unsigned long long gauss_off, gauss_count;  // gaussians required
+  unsigned long long seg_off;                 // first global segment
+  unsigned long long chunk_off;               // first global generator chunk
+  unsigned int nseg, nchunk;
+  U576 y0;
+};
+
+// ---- stream generation ------------------------------------------------------
+
+__global__ void k_seed(Stream *st, int nstreams) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nstreams) return;
+  uint32_t y[24];
+  ranlux_seed_state(y, st[s].seed);
+  u576_from_state(st[s].y0, y, 0);
+}
+
+// chunk multipliers a^(794 * kChunkBlocks * t) mod m, from the table of
+// a^(794 * kChunkBlocks * 2^i)
+__global__ void k_chunk_multipliers(U576 *out, int count, const U576 *pow2, int npow2) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  U576 acc;
+  u576_zero(acc);
+  acc.w[0] = 1;
+  for (int i = 0; i < npow2; ++i)
+    if ((t >> i) & 1) u576_mulmod(acc, acc, pow2[i]);
+  out[t] = acc;
+}
+
+__device__ __forceinline__ int find_stream_by_chunk(const Stream *st, int nstreams, unsigned long long c) {
+  int lo = 0, hi = nstreams - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (st[mid].chunk_off <= c) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int find_stream_by_segment(const Stream *st, int nstreams, unsigned long long g) {
+  int lo = 0, hi = nstreams - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (st[mid].seg_off <= g) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <int K>
+__device__ __forceinline__ void swb_group(uint32_t (&y)[24], uint32_t &c) {
+  // one step replacing slot K (the oldest word) by y_{n-10} - y_{n-24} - c
+  int32_t d = (int32_t)y[(K + 14) % 24] - (int32_t)y[K] - (int32_t)c;
+  c = (uint32_t)d >> 31;
+  y[K] = (uint32_t)d & 0xFFFFFFu;
+}
+
+__device__ __forceinline__ void swb_24(uint32_t (&y)[24], uint32_t &c) {
+  swb_group<0>(y, c);  swb_group<1>(y, c);  swb_group<2>(y, c);  swb_group<3>(y, c);
+  swb_group<4>(y, c);  swb_group<5>(y, c);  swb_group<6>(y, c);  swb_group<7>(y, c);
+  swb_group<8>(y, c);  swb_group<9>(y, c);  swb_group<10>(y, c); swb_group<11>(y, c);
+  swb_group<12>(y, c); swb_group<13>(y, c); swb_group<14>(y, c); swb_group<15>(y, c);
+  swb_group<16>(y, c); swb_group<17>(y, c); swb_group<18>(y, c); swb_group<19>(y, c);
+  swb_group<20>(y, c); swb_group<21>(y, c); swb_group<22>(y, c); swb_group<23>(y, c);
+}
+
+__global__ void __launch_bounds__(128) k_generate(const Stream *st, int nstreams, unsigned long long nchunks,
+                                                  const U576 *chunkmul, uint32_t *raw) {
+  unsigned long long gc = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gc >= nchunks) return;
+  int s = find_stream_by_chunk(st, nstreams, gc);
+  unsigned long long t = gc - st[s].chunk_off;
+  if (t >= st[s].nchunk) return;
+  U576 Y;
+  u576_mulmod(Y, st[s].y0, chunkmul[t]);
+  uint32_t y[24];
+  u576_to_state(y, Y);
+  uint32_t c = 0;
+  unsigned long long first = t * (unsigned long long)kChunkBlocks * 24ull;
+  unsigned long long count = st[s].raw_count;
+  uint32_t *dst = raw + st[s].raw_off;
+  for (int b = 0; b < kChunkBlocks; ++b) {
+    unsigned long long base = first + (unsigned long long)b * 24ull;
+    if (base >= count) break;
+#pragma unroll 1
+    for (int g = 0; g < kLux / 24; ++g) swb_24(y, c);
+    swb_group<0>(y, c);
+    swb_group<1>(y, c);
+    // oldest word now in slot 2: rotate so that slot 0 is the oldest again
+    uint32_t t0 = y[0], t1 = y[1];
+#pragma unroll
+    for (int k = 0; k < 22; ++k) y[k] = y[k + 2];
+    y[22] = t0;
+    y[23] = t1;
+#pragma unroll
+    for (int k = 0; k < 24; ++k)
+      if (base + k < count) dst[base + k] = y[k];
+  }
+}
+
+// ---- ziggurat ---------------------------------------------------------------
+
+// One gaussian starting at stream position *p; returns false on running past n.
+__device__ __forceinline__ bool zig_gaussian(const uint32_t *r, unsigned long long n, unsigned long long &p,
+                                             double &g) {
+  const double R = GIC_ZIG_PARAM_R;
+  for (int guard = 0; guard < 1 << 20; ++guard) {
+    if (p + 2 > n) return false;
+    uint32_t k1 = __ldg(r + p), k2 = __ldg(r + p + 1);
+    unsigned i = k1 & 0xFFu;
+    uint32_t j = k2 & 0xFFFFFFu;
+    double sign = (i & 0x80u) ? 1.0 : -1.0;
+    i &= 0x7Fu;
+    double x = __dmul_rn((double)j, dZigW[i]);
+    if (j < dZigK[i]) {
+      g = __dmul_rn(sign, x);
+      p += 2;
+      return true;
+    }
+    double y;
+    if (i < 127) {
+      if (p + 3 > n) return false;
+      double u1 = __dmul_rn((double)__ldg(r + p + 2), 1.0 / 16777216.0);
+      y = __dadd_rn(dZigY[i + 1], __dmul_rn(__dsub_rn(dZigY[i], dZigY[i + 1]), u1));
+      p += 3;
+    } else {
+      if (p + 4 > n) return false;
+      uint32_t kk = __ldg(r + p + 2);
+      double u2 = __dmul_rn((double)__ldg(r + p + 3), 1.0 / 16777216.0);
+      double lg = gic_log_k24(16777216u - kk);  // log(1 - kk/2^24), correctly rounded
+      x = __dsub_rn(R, __ddiv_rn(lg, R));
+      y = __dmul_rn(exp(__dmul_rn(-R, __dsub_rn(x, __dmul_rn(0.5, R)))), u2);
+      p += 4;
+    }
+    if (y < exp(__dmul_rn(__dmul_rn(-0.5, x), x))) {
+      g = __dmul_rn(sign, x);
+      return true;
+    }
+  }
+  return false;
+}
+
+// Walk one segment from `entry`; counts gaussians that start inside it.
+__device__ void walk_segment(const uint32_t *r, unsigned long long n, unsigned long long seg_start,
+                             unsigned long long seg_end, unsigned long long entry, uint32_t &count,
+                             uint32_t &exit_off, double *out, unsigned long long out_limit) {
+  unsigned long long p = seg_start + entry;
+  uint32_t cnt = 0;
+  while (p < seg_end) {
+    double g;
+    if (!zig_gaussian(r, n, p, g)) {
+      count = cnt;
+      exit_off = kUnderrun;
+      return;
+    }
+    if (out) {
+      if (cnt >= out_limit) break;
+      out[cnt] = g;
+    }
+    ++cnt;
+  }
+  count = cnt;
+  exit_off = (uint32_t)(p > seg_end ? p - seg_end : 0);
+}
+
+__global__ void k_walk_speculative(const Stream *st, int nstreams, unsigned long long nseg_total,
+                                   const uint32_t *raw, uint2 *tab) {
+  unsigned long long id = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= nseg_total * kSpec) return;
+  unsigned long long gseg = id / kSpec;
+  int e = (int)(id % kSpec);
+  int s = find_stream_by_segment(st, nstreams, gseg);
+  unsigned long long lseg = gseg - st[s].seg_off;
+  const uint32_t *r = raw + st[s].raw_off;
+  unsigned long long n = st[s].raw_count;
+  unsigned long long a = lseg * kSegLen, b = a + kSegLen;
+  if (b > n) b = n;
+  uint32_t cnt = 0, ex = 0;
+  walk_segment(r, n, a, b, (unsigned long long)e, cnt, ex, nullptr, 0);
+  tab[id] = make_uint2(cnt, ex);
+}
+
+// One thread per stream chains the segments.  flags[0] is set on underrun.
+__global__ void k_resolve(const Stream *st, int nstreams, const uint32_t *raw, const uint2 *tab,
+                          uint32_t *seg_entry, unsigned long long *seg_base, int *flags) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nstreams) return;
+  const uint32_t *r = raw + st[s].raw_off;
+  unsigned long long n = st[s].raw_count;
+  unsigned long long need = st[s].gauss_count;
+  unsigned long long base = 0;
+  uint32_t e = 0;
+  for (unsigned int g = 0; g < st[s].nseg; ++g) {
+    unsigned long long gseg = st[s].seg_off + g;
+    seg_entry[gseg] = e;
+    seg_base[gseg] = base;
+    if (base >= need) continue;
+    uint32_t cnt, ex;
+    if (e < kSpec) {
+      uint2 v = tab[gseg * kSpec + e];
+      cnt = v.x;
+      ex = v.y;
+    } else {
+      unsigned long long a = (unsigned long long)g * kSegLen, b = a + kSegLen;
+      if (b > n) b = n;
+      walk_segment(r, n, a, b, e, cnt, ex, nullptr, 0);
+    }
+    base += cnt;
+    if (ex == kUnderrun) {
+      if (base < need) atomicExch(flags, 1);
+      e = 0;
+      continue;
+    }
+    e = ex;
+  }
+  if (base < need) atomicExch(flags, 1);
+}
+
+__global__ void k_walk_final(const Stream *st, int nstreams, unsigned long long nseg_total, const uint32_t *raw,
+                             const uint32_t *seg_entry, const unsigned long long *seg_base, double *gauss,
+                             int *flags) {
+  unsigned long long gseg = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gseg >= nseg_total) return;
+  int s = find_stream_by_segment(st, nstreams, gseg);
+  unsigned long long base = seg_base[gseg];
+  unsigned long long need = st[s].gauss_count;
+  if (base >= need) return;
+  unsigned long long lseg = gseg - st[s].seg_off;
+  const uint32_t *r = raw + st[s].raw_off;
+  unsigned long long n = st[s].raw_count;
+  unsigned long long a = lseg * kSegLen, b = a + kSegLen;
+  if (b > n) b = n;
+  uint32_t cnt, ex;
+  walk_segment(r, n, a, b, seg_entry[gseg], cnt, ex, gauss + st[s].gauss_off + base, need - base);
+  if (ex == kUnderrun && base + cnt < need) atomicExch(flags, 1);
+}
+
+// ---- placement ----------------------------------------------------------------
+
+// modes drawn before shell ks: sum_{j<ks} 3 (2j)^2
+__host__ __device__ __forceinline__ unsigned long long shell_offset(long long ks) {
+  return ks <= 1 ? 0ull : (unsigned long long)(2 * (ks - 1) * ks * (2 * ks - 1));
+}
+
+__device__ __forceinline__ void decode_mode(unsigned long long Q, int half, int &k1, int &k2, int &k3) {
+  int lo = 1, hi = half - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (shell_offset(mid) <= Q) lo = mid; else hi = mid - 1;
+  }
+  int ks = lo;
+  unsigned long long q = Q - shell_offset(ks);
+  int which = (int)(q % 3ull);
+  unsigned long long t = q / 3ull;
+  int a = (int)(t / (unsigned long long)(2 * ks)) - ks;
+  int b = (int)(t % (unsigned long long)(2 * ks)) - ks;
+  if (which == 0) { k1 = ks; k2 = a; k3 = b; }
+  else if (which == 1) { k1 = a; k2 = ks; k3 = b; }
+  else { k1 = a; k2 = b; k3 = ks; }
+}
+
+// storage index of mode (kx,ky,kz) of a real field's half spectrum; conj = folded
+__device__ __forceinline__ size_t coeff_index(int n, int kx, int ky, int kz, bool &conj) {
+  conj = false;
+  if (kz < 0) { kx = -kx; ky = -ky; kz = -kz; conj = true; }
+  if (ky < 0) ky += n;
+  if (kx < 0) kx += n;
+  return (size_t)kz + (size_t)(n / 2 + 1) * ((size_t)ky + (size_t)n * (size_t)kx);
+}
+
+__device__ __forceinline__ bool needs_partner(int n, int k1, int k2, int k3) {
+  int nyq = n / 2;
+  return k1 == 0 || k1 == nyq || k2 == 0 || k2 == nyq || k3 == 0 || k3 == nyq;
+}
+
+__global__ void k_place_owner(int n, unsigned long long nmodes, int *owner) {
+  unsigned long long Q = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (Q >= nmodes) return;
+  int k1, k2, k3;
+  decode_mode(Q, n / 2, k1, k2, k3);
+  bool cj;
+  atomicMax(owner + coeff_index(n, k1, k2, k3, cj), (int)Q);
+  if (needs_partner(n, k1, k2, k3)) atomicMax(owner + coeff_index(n, -k1, -k2, -k3, cj), (int)Q);
+}
+
+template <typename T>
+__global__ void k_place_write(int n, unsigned long long nmodes, const int *owner, const double *gauss, T norm,
+                              int reverse, T *out /* interleaved complex */) {
+  unsigned long long Q = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (Q >= nmodes) return;
+  int k1, k2, k3;
+  decode_mode(Q, n / 2, k1, k2, k3);
+  // FloatType a = norm * gaussian  (double gaussian, promoted product, rounded to T)
+  T a = (T)((double)norm * gauss[2 * Q]);
+  T b = (T)((double)norm * gauss[2 * Q + 1]);
+  T re = reverse ? b : a, im = reverse ? a : b;
+  bool cj;
+  size_t c1 = coeff_index(n, k1, k2, k3, cj);
+  if (owner[c1] == (int)Q) {
+    out[2 * c1] = re;
+    out[2 * c1 + 1] = cj ? -im : im;
+  }
+  if (needs_partner(n, k1, k2, k3)) {
+    size_t c2 = coeff_index(n, -k1, -k2, -k3, cj);
+    if (owner[c2] == (int)Q) {
+      out[2 * c2] = re;
+      out[2 * c2 + 1] = cj ? im : -im;
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_place_real(int n, const double *gauss, T *out) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t m = (size_t)n * n * n;
+  if (i >= m) return;
+  size_t row = i / n, z = i % n;
+  out[row * (size_t)(2 * (n / 2 + 1)) + z] = (T)gauss[i];
+}
+
+template <typename T>
+__global__ void k_zero_first(T *out) {
+  out[0] = (T)0;
+}
+
+unsigned long long raw_needed(unsigned long long g) {
+  // mean 2.0534 numbers per gaussian, generous margin
+  double m = 2.0534 * (double)g + 12.0 * std::sqrt((double)g + 1.0) + 512.0;
+  return (unsigned long long)m;
+}
+
+}  // namespace
+
+// Generate `streams` gaussians into ctx.rng.gauss (layout given by gauss_off).
+static void generate_gaussians(Context &ctx, std::vector<Stream> &streams, unsigned long long total_gauss,
+                               double margin) {
+  cudaStream_t cs = ctx.stream;
+  int ns = (int)streams.size();
+  unsigned long long raw_total = 0, seg_total = 0, chunk_total = 0, max_chunks = 0;
+  for (auto &s : streams) {
+    s.raw_off = raw_total;
+    s.raw_count = (unsigned long long)(raw_needed(s.gauss_count) * margin);
+    s.raw_count = (s.raw_count + 23) / 24 * 24;
+    raw_total += s.raw_count;
+    s.nseg = (unsigned int)((s.raw_count + kSegLen - 1) / kSegLen);
+    s.seg_off = seg_total;
+    seg_total += s.nseg;
+    unsigned long long blocks = s.raw_count / 24;
+    s.nchunk = (unsigned int)((blocks + kChunkBlocks - 1) / kChunkBlocks);
+    s.chunk_off = chunk_total;
+    chunk_total += s.nchunk;
+    max_chunks = std::max<unsigned long long>(max_chunks, s.nchunk);
+  }
+  RngScratch &R = ctx.rng;
+  R.raw.ensure(raw_total * sizeof(uint32_t));
+  R.gauss.ensure(total_gauss * sizeof(double));
+  R.segtab.ensure(seg_total * kSpec * sizeof(uint2));
+  R.segentry.ensure(seg_total * sizeof(uint32_t));
+  R.segbase.ensure(seg_total * sizeof(unsigned long long));
+  R.streams.ensure(streams.size() * sizeof(Stream));
+  R.flags.ensure(sizeof(int) * 4);
+
+  // chunk multipliers (seed independent; computed once for the largest stream)
+  if ((unsigned long long)R.chunkmul_count < max_chunks) {
+    int count = (int)std::max<unsigned long long>(max_chunks, 1024);
+    std::vector<U576> pow2;
+    U576 a, step;
+    u576_ranlux_multiplier(a);
+    u576_powmod(step, a, (uint64_t)kLux * kChunkBlocks);
+    int npow = 0;
+    while ((1 << npow) < count) ++npow;
+    pow2.resize(std::max(npow, 1));
+    pow2[0] = step;
+    for (int i = 1; i < npow; ++i) u576_mulmod(pow2[i], pow2[i - 1], pow2[i - 1]);
+    DevBuf dpow;
+    dpow.ensure(pow2.size() * sizeof(U576));
+    GIC_CUDA(cudaMemcpyAsync(dpow.ptr, pow2.data(), pow2.size() * sizeof(U576), cudaMemcpyHostToDevice, cs));
+    R.chunkmul.ensure((size_t)count * sizeof(U576));
+    k_chunk_multipliers<<<(count + 127) / 128, 128, 0, cs>>>(R.chunkmul.as<U576>(), count, dpow.as<U576>(), npow);
+    GIC_CUDA(cudaGetLastError());
+    GIC_CUDA(cudaStreamSynchronize(cs));
+    R.chunkmul_count = count;
+  }
+
+  Stream *dst = R.streams.as<Stream>();
+  GIC_CUDA(cudaMemcpyAsync(dst, streams.data(), streams.size() * sizeof(Stream), cudaMemcpyHostToDevice, cs));
+  GIC_CUDA(cudaMemsetAsync(R.flags.ptr, 0, sizeof(int) * 4, cs));
+  k_seed<<<(ns + 127) / 128, 128, 0, cs>>>(dst, ns);
+  GIC_CUDA(cudaGetLastError());
+  k_generate<<<(unsigned)((chunk_total + 127) / 128), 128, 0, cs>>>(dst, ns, chunk_total, R.chunkmul.as<U576>(),
+                                                                   R.raw.as<uint32_t>());
+  GIC_CUDA(cudaGetLastError());
+  unsigned long long nspec = seg_total * kSpec;
+  k_walk_speculative<<<(unsigned)((nspec + 127) / 128), 128, 0, cs>>>(dst, ns, seg_total, R.raw.as<uint32_t>(),
+                                                                     R.segtab.as<uint2>());
+  GIC_CUDA(cudaGetLastError());
+  k_resolve<<<(ns + 63) / 64, 64, 0, cs>>>(dst, ns, R.raw.as<uint32_t>(), R.segtab.as<uint2>(),
+                                          R.segentry.as<uint32_t>(), R.segbase.as<unsigned long long>(),
+                                          R.flags.as<int>());
+  GIC_CUDA(cudaGetLastError());
+  k_walk_final<<<(unsigned)((seg_total + 127) / 128), 128, 0, cs>>>(
+      dst, ns, seg_total, R.raw.as<uint32_t>(), R.segentry.as<uint32_t>(), R.segbase.as<unsigned long long>(),
+      R.gauss.as<double>(), R.flags.as<int>());
+  GIC_CUDA(cudaGetLastError());
+  int flag = 0;
+  GIC_CUDA(cudaMemcpyAsync(&flag, R.flags.ptr, sizeof(int), cudaMemcpyDeviceToHost, cs));
+  GIC_CUDA(cudaStreamSynchronize(cs));
+  if (flag) {
+    if (margin > 4.0) fail(GIC_ERR_INTERNAL, "random stream shorter than the gaussians it must supply");
+    generate_gaussians(ctx, streams, total_gauss, margin * 1.5);
+  }
+}
+
+template <typename T>
+static void draw_level_typed(Context &ctx, Level &L, unsigned long long seed, int mode) {
+  cudaStream_t cs = ctx.stream;
+  int n = L.n;
+  size_t nc = L.ncomplex();
+  L.noise.ensure(nc * 2 * sizeof(T));
+  T *out = L.noise.as<T>();
+  std::vector<Stream> streams;
+  if (mode == GIC_SEED_REAL_SPACE) {
+    unsigned long long m = L.ncells();
+    Stream s{};
+    s.seed = seed;
+    s.gauss_off = 0;
+    s.gauss_count = m;
+    streams.push_back(s);
+    generate_gaussians(ctx, streams, m, 1.0);
+    GIC_CUDA(cudaMemsetAsync(out, 0, nc * 2 * sizeof(T), cs));
+    k_place_real<T><<<(unsigned)((m + 255) / 256), 256, 0, cs>>>(n, ctx.rng.gauss.as<double>(), out);
+    GIC_CUDA(cudaGetLastError());
+    fft_r2c_3d<T>(ctx, out, n, 1.0 / std::pow((double)n, 1.5));
+    k_zero_first<T><<<1, 1, 0, cs>>>(out);
+    GIC_CUDA(cudaGetLastError());
+  } else {
+    int half = n / 2;
+    unsigned long long nmodes = shell_offset(half);
+    if (mode == GIC_SEED_FOURIER_PARALLEL) {
+      for (int ks = 1; ks < half; ++ks) {
+        Stream s{};
+        s.seed = seed + (unsigned long long)ks;
+        s.gauss_off = 2 * shell_offset(ks);
+        s.gauss_count = 2 * (shell_offset(ks + 1) - shell_offset(ks));
+        streams.push_back(s);
+      }
+    } else {
+      Stream s{};
+      s.seed = seed;
+      s.gauss_off = 0;
+      s.gauss_count = 2 * nmodes;
+      streams.push_back(s);
+    }
+    GIC_CUDA(cudaMemsetAsync(out, 0, nc * 2 * sizeof(T), cs));
+    if (nmodes > 0) {
+      generate_gaussians(ctx, streams, 2 * nmodes, 1.0);
+      ctx.rng.owner.ensure(nc * sizeof(int));
+      GIC_CUDA(cudaMemsetAsync(ctx.rng.owner.ptr, 0xFF, nc * sizeof(int), cs));
+      unsigned blocks = (unsigned)((nmodes + 255) / 256);
+      k_place_owner<<<blocks, 256, 0, cs>>>(n, nmodes, ctx.rng.owner.as<int>());
+      GIC_CUDA(cudaGetLastError());
+      T norm = (T)(1.0 / std::sqrt(2.0));
+      k_place_write<T><<<blocks, 256, 0, cs>>>(n, nmodes, ctx.rng.owner.as<int>(), ctx.rng.gauss.as<double>(),
+                                               norm, mode == GIC_SEED_FOURIER_REVERSE ? 1 : 0, out);
+      GIC_CUDA(cudaGetLastError());
+    }
+  }
+  GIC_CUDA(cudaStreamSynchronize(cs));
+  L.have_noise = true;
+}
+
+void gaussian_stream(Context &ctx, unsigned long long seed, size_t n, double *host) {
+  std::vector<Stream> streams(1);
+  streams[0] = Stream{};
+  streams[0].seed = seed;
+  streams[0].gauss_count = n;
+  generate_gaussians(ctx, streams, n, 1.0);
+  GIC_CUDA(cudaMemcpyAsync(host, ctx.rng.gauss.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+  GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+}
+
+void draw_noise_level(Context &ctx, Level &L, unsigned long long seed, int mode) {
+  if (mode < 0 || mode > 3) fail(GIC_ERR_INVALID_ARG, "unknown seeding mode");
+  if ((long long)L.n * L.n * (L.n / 2 + 1) >= (1ll << 31))
+    fail(GIC_ERR_INVALID_ARG, "grid too large for 32-bit mode indices");
+  if (ctx.dbl())
+    draw_level_typed<double>(ctx, L, seed, mode);
+  else
+    draw_level_typed<float>(ctx, L, seed, mode);
+}
+
+}  // namespace gic

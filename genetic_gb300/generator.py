@@ -1,0 +1,234 @@
+"""Host-side driver of the GPU realisation path, mirroring genetIC's ICGenerator.
+
+Method names are genetIC's paramfile commands (genetIC/src/main.cpp:22-172) and
+their arguments mean the same; `run_paramfile` dispatches a paramfile line by
+line like genetIC's parser (genetIC/src/tools/parser.hpp:193-211).  Geometry
+and bookkeeping stay on the host; every field operation goes through the C ABI
+of libgicgpu.so.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+from .transfer import read_camb
+
+_DP = ctypes.POINTER(ctypes.c_double)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_DP)
+
+
+class ICGenerator:
+    """The realisation state of one set of initial conditions on one GPU."""
+
+    def __init__(self, precision='fp64', device=0):
+        lib = _lib.load()
+        self._lib = lib
+        opts = _lib.GicDeviceOpts(_lib.GIC_FP64 if precision == 'fp64' else _lib.GIC_MIXED, device, 0)
+        ctx = ctypes.c_void_p()
+        st = lib.gic_create(ctypes.byref(ctx), ctypes.byref(opts))
+        if st != _lib.GIC_OK:
+            raise _lib.GicError(st, lib.gic_last_error(None).decode())
+        self._ctx = ctx
+        self.precision = precision
+        # genetIC's defaults (genetIC/src/ic.hpp:200-210)
+        self.cosmo = dict(omega_m=0.3, omega_lambda=0.7, omega_b=0.0, hubble=0.701, sigma8=0.8, ns=0.96,
+                          redshift=0.0)
+        self.levels = []  # (box, n, offset)
+        self.seed = None
+        self.seed_mode = None
+        self.base_dir = '.'
+        self._drawn = False
+        self._done = False
+
+    # -- lifetime --------------------------------------------------------------
+    def close(self):
+        if self._ctx:
+            self._lib.gic_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _call(self, name, *args):
+        check(self._ctx, getattr(self._lib, name)(self._ctx, *args))
+
+    # -- cosmology (main.cpp:31-37) ------------------------------------------------
+    def Om(self, v):
+        self.cosmo['omega_m'] = float(v)
+
+    def Ol(self, v):
+        self.cosmo['omega_lambda'] = float(v)
+
+    def Ob(self, v):
+        self.cosmo['omega_b'] = float(v)
+
+    def hubble(self, v):
+        self.cosmo['hubble'] = float(v)
+
+    def s8(self, v):
+        self.cosmo['sigma8'] = float(v)
+
+    def ns(self, v):
+        self.cosmo['ns'] = float(v)
+
+    def zin(self, v):
+        self.cosmo['redshift'] = float(v)
+
+    def _push_cosmology(self):
+        c = _lib.GicCosmo(**self.cosmo)
+        self._call('gic_set_cosmology', ctypes.byref(c))
+
+    def camb(self, path_or_table):
+        """Load a CAMB transfer table (path, or an (nrows, ncols) array) with the current cosmology."""
+        if isinstance(path_or_table, str):
+            path = path_or_table if os.path.isabs(path_or_table) else os.path.join(self.base_dir, path_or_table)
+            table = read_camb(path)
+        else:
+            table = np.asarray(path_or_table, dtype=np.float64)
+        table = np.ascontiguousarray(table, dtype=np.float64)
+        self._push_cosmology()
+        self._call('gic_set_transfer', _ptr(table), table.shape[0], table.shape[1])
+
+    def normalisation(self):
+        a, s = ctypes.c_double(), ctypes.c_double()
+        self._call('gic_get_normalisation', ctypes.byref(a), ctypes.byref(s))
+        return a.value, s.value
+
+    # -- grids (main.cpp:92-94, ic.hpp:365-598) ------------------------------------
+    def base_grid(self, box, n):
+        self._add_level(float(box), int(n), (0.0, 0.0, 0.0))
+
+    basegrid = base_grid
+
+    def zoom_grid_with_origin_at(self, x0, y0, z0, zoomfac, n):
+        box0, n0, off0 = self.levels[-1]
+        dx0 = box0 / n0
+        if int(x0) < 0 or int(y0) < 0 or int(z0) < 0:
+            raise ValueError('The newly initialised zoom level is not fully contained within the previous level')
+        offset = tuple(off0[i] + int(c) * dx0 for i, c in enumerate((x0, y0, z0)))
+        self._add_level(box0 / int(zoomfac), int(n), offset)
+
+    zoomgrid_with_origin_at = zoom_grid_with_origin_at
+
+    def _add_level(self, box, n, offset):
+        lid = ctypes.c_int()
+        self._call('gic_level_add', box, n, offset[0], offset[1], offset[2], ctypes.byref(lid))
+        self.levels.append((box, n, offset))
+
+    # -- seeding (main.cpp:44-52) ----------------------------------------------------
+    def _seed(self, seed, mode):
+        if self.seed is not None:
+            raise RuntimeError('The random number generator has already been seeded')
+        self.seed, self.seed_mode = int(seed), mode
+
+    def random_seed(self, seed):
+        self._seed(seed, _lib.GIC_SEED_FOURIER_PARALLEL)
+
+    seedfourier_parallel = random_seed
+
+    def random_seed_serial(self, seed):
+        self._seed(seed, _lib.GIC_SEED_FOURIER_SERIAL)
+
+    seedfourier = random_seed_serial
+
+    def random_seed_real_space(self, seed):
+        self._seed(seed, _lib.GIC_SEED_REAL_SPACE)
+
+    seed_ = random_seed_real_space
+
+    def seedfourier_reverse(self, seed):
+        self._seed(seed, _lib.GIC_SEED_FOURIER_REVERSE)
+
+    # -- realisation -------------------------------------------------------------
+    def draw(self):
+        if self._drawn:
+            return
+        if self.seed is None:
+            raise RuntimeError('The random number generator has not been seeded')
+        self._call('gic_draw_noise', self.seed, self.seed_mode)
+        self._drawn = True
+
+    def done(self):
+        """Draw the noise if needed, apply P(k), build the Zel'dovich fields and particles."""
+        self.draw()
+        self._call('gic_zeldovich', 1)
+        self._done = True
+
+    def chi2(self):
+        self.draw()
+        v = ctypes.c_double()
+        self._call('gic_chi2', ctypes.byref(v))
+        return v.value
+
+    # -- results -----------------------------------------------------------------
+    def noise(self, level=0):
+        n = self.levels[level][1]
+        out = np.empty((n, n, n // 2 + 1, 2), dtype=np.float64)
+        self._call('gic_fetch_level', level, _lib.GIC_FIELD_NOISE, _ptr(out))
+        return out[..., 0] + 1j * out[..., 1]
+
+    def field(self, level=0, name='delta'):
+        what = {'delta': _lib.GIC_FIELD_DELTA, 'psi_x': _lib.GIC_FIELD_PSI_X, 'psi_y': _lib.GIC_FIELD_PSI_Y,
+                'psi_z': _lib.GIC_FIELD_PSI_Z}[name]
+        n = self.levels[level][1]
+        out = np.empty((n, n, n), dtype=np.float64)
+        self._call('gic_fetch_level', level, what, _ptr(out))
+        return out
+
+    def particles(self, level=0):
+        n = self.levels[level][1]
+        pos = np.empty((n ** 3, 3), dtype=np.float64)
+        vel = np.empty((n ** 3, 3), dtype=np.float64)
+        self._call('gic_fetch_particles', level, _ptr(pos), _ptr(vel))
+        return pos, vel
+
+    def gaussian_stream(self, seed, count):
+        out = np.empty(int(count), dtype=np.float64)
+        self._call('gic_gaussian_stream', int(seed), int(count), _ptr(out))
+        return out
+
+
+_COMMANDS = {
+    'Om': 'Om', 'Ol': 'Ol', 'Ob': 'Ob', 'hubble': 'hubble', 's8': 's8', 'ns': 'ns', 'zin': 'zin',
+    'camb': 'camb', 'basegrid': 'base_grid', 'base_grid': 'base_grid',
+    'zoomgrid_with_origin_at': 'zoom_grid_with_origin_at', 'zoom_grid_with_origin_at': 'zoom_grid_with_origin_at',
+    'random_seed': 'random_seed', 'seedfourier_parallel': 'random_seed',
+    'random_seed_serial': 'random_seed_serial', 'seedfourier': 'random_seed_serial',
+    'random_seed_real_space': 'random_seed_real_space', 'seed': 'random_seed_real_space',
+    'seedfourier_reverse': 'seedfourier_reverse', 'done': 'done', 'chi2': 'chi2',
+}
+# output-side commands handled by genetIC's own writers; accepted and ignored here
+_IGNORED = {'outname', 'outdir', 'outformat', 'dump_grid', 'dump_ps', 'idfile', 'dump_idfile'}
+
+
+def run_paramfile(path, precision='fp64', device=0):
+    """Run a genetIC paramfile's realisation commands on the GPU; returns the ICGenerator."""
+    gen = ICGenerator(precision=precision, device=device)
+    gen.base_dir = os.path.dirname(os.path.abspath(path))
+    with open(path) as f:
+        for lineno, line in enumerate(f, 1):
+            line = line.split('#')[0].strip()
+            if not line:
+                continue
+            parts = line.split()
+            cmd, args = parts[0], parts[1:]
+            if cmd in _IGNORED:
+                continue
+            if cmd not in _COMMANDS:
+                raise ValueError('%s:%d: command %r is not on the GPU realisation path' % (path, lineno, cmd))
+            getattr(gen, _COMMANDS[cmd])(*args)
+    return gen

@@ -1,0 +1,142 @@
+/* gicgpu.h -- C ABI of the GB300 field-realisation library (libgicgpu.so).
+ *
+ * The library replaces genetIC's field-realisation hot path: white-noise drawing,
+ * multiplication by sqrt(P(k)), inter-level filtering and zoom combination, the
+ * modification (constraint) projections and Zel'dovich displacements/velocities.
+ * genetIC's host (paramfile parser, grid geometry, particle mappers and the
+ * Gadget/grafIC/tipsy writers) stays as it is and calls these entry points.
+ *
+ * Conventions (same as genetIC):
+ *   - real-space index (x*N + y)*N + z, z fastest (genetIC/src/simulation/grid/grid.hpp:610-626);
+ *   - Fourier fields are half spectra of N*N*(N/2+1) complex values, kz fastest,
+ *     kx, ky wrapped to [0,N) (genetIC/src/tools/numerics/fourier.hpp:300-319);
+ *   - both FFT directions are normalised by N^-1.5 (fourier.hpp:479-518).
+ * Every call returns GIC_OK (0) or a negative status; gic_last_error() gives the
+ * message.  Nothing aborts the process and no C++ exception crosses the ABI.
+ * Host buffers are borrowed for the duration of a call; the context owns all
+ * device memory.  Calls on one context are serialised on the context's stream
+ * and have completed when they return.
+ */
+#ifndef GICGPU_H
+#define GICGPU_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GIC_OK 0
+#define GIC_ERR_INVALID_ARG (-1)
+#define GIC_ERR_OOM (-2)
+#define GIC_ERR_CUDA (-3)
+#define GIC_ERR_TIMEOUT (-4)
+#define GIC_ERR_NOT_READY (-5)
+#define GIC_ERR_INTERNAL (-6)
+
+/* precision forms */
+#define GIC_FP64 0   /* every field operation in double */
+#define GIC_MIXED 1  /* FFTs and spectral multiplies in float; normalisation integral,
+                        modification algebra and particle positions in double */
+
+/* white-noise drawing modes (genetIC/src/main.cpp:44-52, ic.hpp:620-666) */
+#define GIC_SEED_REAL_SPACE 0      /* random_seed_real_space / seed */
+#define GIC_SEED_FOURIER_SERIAL 1  /* random_seed_serial / seedfourier */
+#define GIC_SEED_FOURIER_PARALLEL 2/* random_seed / seedfourier_parallel */
+#define GIC_SEED_FOURIER_REVERSE 3 /* seedfourier_reverse */
+
+/* field selectors for gic_fetch_level / gic_fft */
+#define GIC_FIELD_NOISE 0
+#define GIC_FIELD_DELTA 1
+#define GIC_FIELD_PSI_X 2
+#define GIC_FIELD_PSI_Y 3
+#define GIC_FIELD_PSI_Z 4
+
+#if defined(__GNUC__)
+#define GIC_API __attribute__((visibility("default")))
+#else
+#define GIC_API
+#endif
+
+typedef struct gic_ctx gic_ctx;
+
+typedef struct {
+  int precision;     /* GIC_FP64 or GIC_MIXED */
+  int device;        /* CUDA device ordinal */
+  size_t mem_limit;  /* 0 = no limit */
+} gic_device_opts;
+
+/* Cosmological parameters, as set by the paramfile commands Om, Ol, Ob, hubble,
+ * s8, ns, zin (genetIC/src/main.cpp:31-37; genetIC/src/cosmology/parameters.hpp:19-32). */
+typedef struct {
+  double omega_m, omega_lambda, omega_b, hubble, sigma8, ns, redshift;
+} gic_cosmo;
+
+/* Context lifetime.  Replaces the state genetIC keeps in ICGenerator
+ * (genetIC/src/ic.hpp:50-200). */
+GIC_API int gic_create(gic_ctx **ctx, const gic_device_opts *opts);
+GIC_API int gic_destroy(gic_ctx *ctx);
+GIC_API const char *gic_last_error(const gic_ctx *ctx);
+
+/* Add a grid level of n^3 cells and side `box`, lower corner (x0,y0,z0).
+ * Level 0 is the periodic base grid.  Replaces MultiLevelGrid::addLevel
+ * (genetIC/src/simulation/multilevelgrid/multilevelgrid.hpp:97-140) as called by
+ * ICGenerator::initBaseGrid / initZoomGridWithLowLeftCornerAt (ic.hpp:502-598). */
+GIC_API int gic_level_add(gic_ctx *ctx, double box, int n, double x0, double y0, double z0, int *level_id);
+
+/* Cosmology and transfer table.  `table` is the CAMB transfer file as genetIC
+ * reads it (nrows x ncols doubles, ncols 7 or 13; genetIC/src/cosmology/camb.hpp:224-268).
+ * Computes the sigma8 normalisation on the device (camb.hpp:289-328).
+ * Replaces CAMB<T>::CAMB (camb.hpp:195-202). */
+GIC_API int gic_set_cosmology(gic_ctx *ctx, const gic_cosmo *cosmo);
+GIC_API int gic_set_transfer(gic_ctx *ctx, const double *table, int nrows, int ncols);
+GIC_API int gic_get_normalisation(gic_ctx *ctx, double *amplitude, double *sigma8_unnormalised);
+
+/* Draw white noise on every level.  Reproduces RandomFieldGenerator::draw
+ * (genetIC/src/simulation/field/randomfieldgenerator.hpp:122-260): GSL ranlxs2 +
+ * gsl_ran_gaussian_ziggurat streams, k-shell draw order, last-write-wins folding. */
+GIC_API int gic_draw_noise(gic_ctx *ctx, unsigned long seed, int mode);
+
+/* The first n unit gaussians of the stream genetIC draws for `seed`
+ * (gsl_ran_gaussian_ziggurat on a gsl_rng_ranlxs2 seeded with `seed`,
+ * randomfieldgenerator.hpp:191), written to host memory.  Testing and
+ * diagnostics. */
+GIC_API int gic_gaussian_stream(gic_ctx *ctx, unsigned long seed, size_t n, double *host_dst);
+
+/* Upload / download a level's white noise as a half spectrum of interleaved
+ * (re,im) doubles.  Replaces Field data access for import_level / dump_grid_fourier. */
+GIC_API int gic_set_noise(gic_ctx *ctx, int level, const double *host_src);
+
+/* delta_k = w_k sqrt(P_grid(k)) and the Zel'dovich displacement spectra
+ * psi_k = i k delta_k / k^2 on every level, then zoom combination (high-pass on
+ * level l, low-passed level l-1 interpolated in) and inverse FFTs to real space.
+ * Replaces ICGenerator::applyPowerSpec (ic.hpp:825-843) + OutputField::applyPowerSpectrumFor
+ * (genetIC/src/simulation/field/multilevelfield.hpp:410-454) +
+ * ZeldovichParticleGenerator::calculateOffsetFields (genetIC/src/simulation/particles/zeldovich.hpp:152-253)
+ * + initialiseParticleGeneratorBasedOnTemplate (multilevelgenerator.hpp:78-128).
+ * order: 1 = Zel'dovich (the reference's only option). */
+GIC_API int gic_zeldovich(gic_ctx *ctx, int order);
+
+/* Copy a level's field to the host.  Real-space fields (after gic_zeldovich)
+ * are written as n^3 doubles in genetIC's (x*N+y)*N+z order; Fourier fields
+ * (GIC_FIELD_NOISE) as n*n*(n/2+1) interleaved complex doubles. */
+GIC_API int gic_fetch_level(gic_ctx *ctx, int level, int what, double *host_dst);
+
+/* Particles of a level (every cell, before mapper selection): positions
+ * (x,y,z interleaved, Mpc/h, wrapped into the periodic box) and velocities
+ * (km/s a^1/2), as ZeldovichParticleEvaluator::getParticle evaluates them
+ * (zeldovich.hpp:87-124, genetIC/src/simulation/particles/generator.hpp:49-53). */
+GIC_API int gic_fetch_particles(gic_ctx *ctx, int level, double *pos, double *vel);
+
+/* Forward (dir=-1) or inverse (dir=+1) normalised 3-D real FFT of a level field
+ * in place on the device (testing).  Replaces FieldFourierManager<T,T>::performTransform
+ * (fourier.hpp:479-518). */
+GIC_API int gic_fft(gic_ctx *ctx, int level, int what, int dir);
+
+/* chi^2 of the white noise: sum over modes of |w_k|^2 with Hermitian weights
+ * (MultiLevelField::getChi2, multilevelfield.hpp:461-487). */
+GIC_API int gic_chi2(gic_ctx *ctx, double *chi2);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

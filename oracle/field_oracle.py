@@ -1,0 +1,279 @@
+"""Oracle (test infrastructure only): numpy restatement of genetIC's
+single-level field-realisation path, used to check the GPU library.
+
+Every function cites the genetIC code it restates.  Nothing in the shipped
+library imports this module; only tests/, the smoke check and the benchmark's
+CPU-baseline leg do.  White noise comes from the C restatement of the RANLUX +
+ziggurat stream in rng/oracle_rng.c (liboracle.so), whose outputs are pinned to
+the reference's golden chi^2 values and tipsy files.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBORACLE = os.path.join(HERE, '_ref', 'liboracle.so')
+
+_lib = None
+
+
+def build():
+    """Build liboracle.so (no reference sources needed)."""
+    subprocess.run(['make', '-s', '-C', HERE, '_ref/liboracle.so'], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIBORACLE):
+            build()
+        L = ctypes.CDLL(LIBORACLE)
+        L.oracle_draw_white_noise.argtypes = [ctypes.c_int, ctypes.c_ulong, ctypes.c_int,
+                                              ctypes.POINTER(ctypes.c_double)]
+        L.oracle_gaussian_stream.argtypes = [ctypes.c_ulong, ctypes.POINTER(ctypes.c_double), ctypes.c_uint64]
+        L.oracle_gaussian_stream.restype = ctypes.c_uint64
+        L.oracle_ranlux_stream.argtypes = [ctypes.c_ulong, ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint64]
+        L.oracle_rng_set_cr_log.argtypes = [ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def set_cr_log(on):
+    """Ziggurat tail log: C library (as GSL on glibc) or correctly rounded."""
+    lib().oracle_rng_set_cr_log(1 if on else 0)
+
+
+def gaussian_stream(seed, n):
+    out = np.empty(int(n), dtype=np.float64)
+    used = lib().oracle_gaussian_stream(int(seed), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), int(n))
+    return out, int(used)
+
+
+def ranlux_stream(seed, n):
+    out = np.empty(int(n), dtype=np.uint32)
+    lib().oracle_ranlux_stream(int(seed), out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), int(n))
+    return out
+
+
+# --- white noise (randomfieldgenerator.hpp:122-260) ---------------------------
+
+def fft_r2c(real):
+    """Unitary forward transform, N^-1.5 (fourier.hpp:479-518)."""
+    n = real.shape[0]
+    return np.fft.rfftn(real) / n ** 1.5
+
+
+def mirror(c):
+    """Hermitian mirroring of the kz = 0 and N/2 planes before c2r (fourier.hpp:331-357)."""
+    c = c.copy()
+    n = c.shape[0]
+    h = n // 2
+    for kz in (0, h):
+        p = c[:, :, kz]
+        src = p.copy()
+        for kx in range(h + 1, n):
+            p[kx, :] = np.conj(src[n - kx, (-np.arange(n)) % n])
+        for kx in (0, h):
+            ky = np.arange(h + 1, n)
+            p[kx, ky] = np.conj(src[kx, n - ky])
+    return c
+
+
+def fft_c2r(c):
+    """Unitary inverse transform of a half spectrum, N^-1.5, after mirroring."""
+    n = c.shape[0]
+    return np.fft.irfftn(mirror(c), s=(n, n, n)) * n ** 1.5
+
+
+def white_noise(n, seed, mode):
+    """Half spectrum (n, n, n/2+1) of the white noise genetIC draws (modes as in gicgpu.h)."""
+    if mode == 0:
+        real = np.empty(n ** 3, dtype=np.float64)
+        lib().oracle_draw_white_noise(n, int(seed), 0, real.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        c = fft_r2c(real.reshape(n, n, n))
+        c[0, 0, 0] = 0.0 + 1j * c[0, 0, 0].imag
+        return c
+    out = np.empty(n * n * (n // 2 + 1) * 2, dtype=np.float64)
+    rc = lib().oracle_draw_white_noise(n, int(seed), int(mode), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    assert rc == 0
+    out = out.reshape(n, n, n // 2 + 1, 2)
+    return out[..., 0] + 1j * out[..., 1]
+
+
+def chi2(noise):
+    """Hermitian-weighted sum of |w_k|^2 (multilevelfield.hpp:461-487, fourier.hpp:110-151)."""
+    n = noise.shape[0]
+    w = np.full(noise.shape[2], 2.0)
+    w[0] = 1.0
+    w[n // 2] = 1.0
+    return float(np.sum(np.abs(noise) ** 2 * w[None, None, :]))
+
+
+# --- power spectrum (camb.hpp, interpolation.hpp, parameters.hpp) -------------
+
+class NaturalSpline:
+    """Natural cubic spline in GSL's second-derivative form (interpolation.hpp:46-76)."""
+
+    def __init__(self, x, y):
+        x = np.asarray(x, float)
+        y = np.asarray(y, float)
+        n = len(x)
+        c = np.zeros(n)
+        if n >= 3:
+            m = n - 2
+            h0 = x[1:-1] - x[:-2]
+            h1 = x[2:] - x[1:-1]
+            diag = 2.0 * (h0 + h1)
+            off = h1.copy()
+            rhs = 3.0 * ((y[2:] - y[1:-1]) / h1 - (y[1:-1] - y[:-2]) / h0)
+            for i in range(1, m):
+                w = off[i - 1] / diag[i - 1]
+                diag[i] -= w * off[i - 1]
+                rhs[i] -= w * rhs[i - 1]
+            c[m] = rhs[m - 1] / diag[m - 1]
+            for i in range(m - 2, -1, -1):
+                c[i + 1] = (rhs[i] - off[i] * c[i + 2]) / diag[i]
+        self.x, self.y, self.c = x, y, c
+
+    def __call__(self, v):
+        v = np.asarray(v, float)
+        x, y, c = self.x, self.y, self.c
+        lo = np.clip(np.searchsorted(x, v, side='right') - 1, 0, len(x) - 2)
+        h = x[lo + 1] - x[lo]
+        dx = v - x[lo]
+        dy = y[lo + 1] - y[lo]
+        b = dy / h - h * (c[lo + 1] + 2.0 * c[lo]) / 3.0
+        d = (c[lo + 1] - c[lo]) / (3.0 * h)
+        out = y[lo] + dx * (b + dx * (c[lo] + dx * d))
+        return np.where((v < x[0]) | (v > x[-1]), 0.0, out)
+
+
+def growth_factor(a, om, ol):
+    """Carroll, Press & Turner fit (parameters.hpp:55-70), including its single-precision a^3."""
+    a3f = float(np.power(np.float32(a), np.float32(3.0)))
+    hsq = om / a3f + (1. - om - ol) / a / a + ol
+    return 2.5 * a * om / a ** 3.0 / hsq / (
+        (om / hsq / a / a / a) ** float(np.float32(4.0) / np.float32(7.0)) - ol / hsq
+        + (1. + 0.5 * om / a ** 3.0 / hsq) * (1. + 1. / 70. * ol / hsq))
+
+
+class CambPower:
+    """P(k) = A k^ns T(k)^2 from a CAMB table (camb.hpp:173-328)."""
+
+    def __init__(self, table, cosmo, column=6):
+        table = np.asarray(table, float)
+        ncols = table.shape[1]
+        assert ncols in (7, 13)
+        tnorm = table[0, 1]
+        keep = table[:, 0] > 0
+        k = table[keep, 0]
+        t = table[keep, column] / tnorm
+        with np.errstate(divide='ignore', invalid='ignore'):
+            lx, ly = np.log(k), np.log(t)
+        ok = np.isfinite(lx) & np.isfinite(ly)
+        self.spline = NaturalSpline(lx[ok], ly[ok])
+        self.kpoints = k
+        self.ns = cosmo['ns']
+        a = 1.0 / (cosmo['redshift'] + 1.0)
+        d = growth_factor(a, cosmo['omega_m'], cosmo['omega_lambda'])
+        d0 = growth_factor(1.0, cosmo['omega_m'], cosmo['omega_lambda'])
+        self.sigma8_pre = self.sigma_in_sphere(8.0)
+        renorm = (cosmo['sigma8'] / self.sigma8_pre) * (d / d0)
+        self.amplitude = renorm * renorm
+
+    def transfer(self, k):
+        k = np.asarray(k, float)
+        with np.errstate(divide='ignore'):
+            lk = np.log(k)
+        inside = (lk >= self.spline.x[0]) & (lk <= self.spline.x[-1])
+        return np.where(inside, np.exp(self.spline(np.where(inside, lk, self.spline.x[0]))), 0.0)
+
+    def sigma_in_sphere(self, radius):
+        """camb.hpp:300-328: Riemann sum, k accumulated by repeated addition."""
+        kmax = min(self.kpoints[-1], 200.0 / radius) * 0.999999
+        kmin = self.kpoints[0] * 1.000001
+        dk = (kmax - kmin) / 50000.
+        ks = []
+        k = kmin
+        while k < kmax:
+            ks.append(k)
+            k += dk
+        ks = np.array(ks)
+        t = self.transfer(ks)
+        kr = ks * radius
+        w = (np.sin(kr) - kr * np.cos(kr)) / (kr * kr * kr)
+        s = float(np.sum(ks ** (self.ns + 2.) * w * w * t * t))
+        return np.sqrt(s * 9. / 2. / np.pi / np.pi * dk)
+
+    def __call__(self, k):
+        k = np.asarray(k, float)
+        t = np.where(k != 0, self.transfer(np.where(k != 0, k, 1.0)), 0.0)
+        return self.amplitude * np.where(k != 0, k, 1.0) ** self.ns * t * t
+
+
+def kgrid(n, box):
+    """Integer and physical wavenumbers of the (n, n, n/2+1) half spectrum."""
+    i = np.arange(n)
+    ki = np.where(i > n // 2, i - n, i)
+    kz = np.arange(n // 2 + 1)
+    kmin = 2. * np.pi / box
+    return ki, kz, kmin
+
+
+def sqrt_power_grid(power, n, box):
+    """sqrt(P_grid) on every stored mode (camb.hpp:101-139, field.hpp:394-412)."""
+    ki, kz, kmin = kgrid(n, box)
+    kx = (ki * kmin)[:, None, None]
+    ky = (ki * kmin)[None, :, None]
+    kzz = (kz * kmin)[None, None, :]
+    k = np.sqrt(kx * kx + ky * ky + kzz * kzz)
+    kw = 2. * np.pi / box
+    norm = kw ** 3 / (2. * np.pi) ** 3 * n ** 3
+    spec = power(k) * norm
+    return np.sqrt(spec)
+
+
+def zeldovich_fields(noise, power, box):
+    """delta, psi_x, psi_y, psi_z in real space for one level (zeldovich.hpp:152-253)."""
+    n = noise.shape[0]
+    delta_k = noise * sqrt_power_grid(power, n, box)
+    ki, kz, kmin = kgrid(n, box)
+    kx = (ki * kmin)[:, None, None]
+    ky = (ki * kmin)[None, :, None]
+    kzz = (kz * kmin)[None, None, :]
+    kk = kx * kx + ky * ky + kzz * kzz
+    with np.errstate(divide='ignore', invalid='ignore'):
+        base = 1j * delta_k / kk
+    base[0, 0, 0] = 0
+    nyq = n // 2
+    out = [fft_c2r(delta_k)]
+    for comp, kc, ic in ((0, kx, ki[:, None, None]), (1, ky, ki[None, :, None]), (2, kzz, kz[None, None, :])):
+        psi_k = base * kc
+        psi_k = np.where(ic == nyq, 0.0, psi_k)
+        psi_k[0, 0, 0] = 0
+        out.append(fft_c2r(psi_k))
+    return out
+
+
+def velocity_to_offset_ratio(cosmo):
+    """parameters.hpp:84-106 (f = 1)."""
+    a = 1.0 / (cosmo['redshift'] + 1.0)
+    return 100. * np.sqrt(cosmo['omega_m'] / (a * a * a) + cosmo['omega_lambda']) * np.sqrt(a)
+
+
+def particles(psi, box, offset, periodic, ratio):
+    """Positions (wrapped) and velocities of every cell (zeldovich.hpp:87-124, generator.hpp:49-53)."""
+    n = psi[0].shape[0]
+    dx = box / n
+    idx = np.arange(n, dtype=np.float64)
+    cx = idx * dx + offset[0] + dx / 2
+    cy = idx * dx + offset[1] + dx / 2
+    cz = idx * dx + offset[2] + dx / 2
+    X, Y, Z = np.meshgrid(cx, cy, cz, indexing='ij')
+    pos = np.stack([psi[0] + X, psi[1] + Y, psi[2] + Z], axis=-1).reshape(-1, 3)
+    pos = np.fmod(pos, periodic)
+    pos = np.where(pos < 0, pos + periodic, pos)
+    vel = np.stack([p * ratio for p in psi], axis=-1).reshape(-1, 3)
+    return pos, vel

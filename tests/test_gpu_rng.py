@@ -1,0 +1,61 @@
+"""White noise on the GPU against the oracle's RANLUX + ziggurat restatement."""
+import numpy as np
+import pytest
+
+import field_oracle as fo
+from conftest import make_generator
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(autouse=True)
+def _cr_log():
+    # the device evaluates the tail log correctly rounded; the oracle matches in this mode
+    fo.set_cr_log(True)
+    yield
+    fo.set_cr_log(False)
+
+
+@pytest.mark.parametrize('seed,count', [(1, 10), (8896131, 100000), (13842314, 262144), (42, 3000001)])
+def test_gaussian_stream_bit_exact(built, seed, count):
+    import genetic_gb300 as g
+    with g.ICGenerator() as gen:
+        got = gen.gaussian_stream(seed, count)
+    want, _ = fo.gaussian_stream(seed, count)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize('n', [8, 16, 32, 64])
+@pytest.mark.parametrize('cmd,mode', [('random_seed_serial', 1), ('random_seed', 2), ('seedfourier_reverse', 3)])
+def test_fourier_white_noise_bit_exact(built, bbks, n, cmd, mode):
+    gen = make_generator('fp64', bbks, [('base', 50.0, n)], 8896131, cmd)
+    gen.draw()
+    got = gen.noise(0)
+    gen.close()
+    want = fo.white_noise(n, 8896131, mode)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize('n', [16, 64])
+def test_real_space_white_noise(built, bbks, n):
+    gen = make_generator('fp64', bbks, [('base', 50.0, n)], 13842314, 'random_seed_real_space')
+    gen.draw()
+    got = gen.noise(0)
+    chi2 = gen.chi2()
+    gen.close()
+    want = fo.white_noise(n, 13842314, 0)
+    # same gaussians, transformed by the device FFT instead of numpy's
+    assert np.abs(got - want).max() < 1e-12
+    if n == 64:
+        # genetIC/tests/test_02k_chisquare_onelevel/reference.txt
+        assert '%.10g' % chi2 == '261733.3011'
+
+
+def test_mixed_precision_noise_is_rounded_oracle(built, bbks):
+    gen = make_generator('mixed', bbks, [('base', 50.0, 32)], 8896131, 'random_seed')
+    gen.draw()
+    got = gen.noise(0)
+    gen.close()
+    w = fo.white_noise(32, 8896131, 2)
+    # float(norm * g) with norm the float 1/sqrt(2): within one float ulp of the double value
+    assert np.abs(got - w).max() <= 1.2e-7 * np.abs(w).max()

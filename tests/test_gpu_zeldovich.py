@@ -1,0 +1,69 @@
+"""Single-level Zel'dovich realisations on the GPU against the oracle."""
+import numpy as np
+import pytest
+
+import field_oracle as fo
+from conftest import COSMO, make_generator
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ('delta', 'psi_x', 'psi_y', 'psi_z')
+
+
+def _run(precision, bbks, n, box, cmd, seed=8896131):
+    gen = make_generator(precision, bbks, [('base', box, n)], seed, cmd)
+    gen.done()
+    out = {f: gen.field(0, f) for f in FIELDS}
+    out['pos'], out['vel'] = gen.particles(0)
+    out['norm'] = gen.normalisation()
+    gen.close()
+    return out
+
+
+def _oracle(bbks, n, box, mode, seed=8896131):
+    fo.set_cr_log(True)
+    w = fo.white_noise(n, seed, mode)
+    fo.set_cr_log(False)
+    power = fo.CambPower(bbks, COSMO)
+    d = fo.zeldovich_fields(w, power, box)
+    pos, vel = fo.particles(d[1:], box, (0, 0, 0), box, fo.velocity_to_offset_ratio(COSMO))
+    return dict(zip(FIELDS, d), pos=pos, vel=vel, power=power)
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+@pytest.mark.parametrize('n,box,cmd,mode', [(64, 50.0, 'random_seed_serial', 1), (32, 50.0, 'random_seed', 2),
+                                            (64, 100.0, 'random_seed_real_space', 0)])
+def test_fp64_matches_oracle(built, bbks, n, box, cmd, mode):
+    got = _run('fp64', bbks, n, box, cmd)
+    want = _oracle(bbks, n, box, mode)
+    amp, s8pre = got['norm']
+    assert abs(amp / want['power'].amplitude - 1) < 1e-12
+    assert abs(s8pre / want['power'].sigma8_pre - 1) < 1e-12
+    for f in FIELDS:
+        assert _rel(got[f], want[f]) < 1e-10, f
+    disp = (got['pos'] - want['pos'] + box / 2) % box - box / 2
+    assert np.abs(disp).max() < 1e-10 * np.abs(want['psi_x']).max() + 1e-12 * box
+    assert _rel(got['vel'], want['vel']) < 1e-10
+
+
+def test_mixed_matches_oracle_within_stated_error(built, bbks):
+    n, box = 64, 50.0
+    got = _run('mixed', bbks, n, box, 'random_seed_serial')
+    want = _oracle(bbks, n, box, 1)
+    for f in FIELDS:
+        assert _rel(got[f], want[f]) < 1e-5, f
+    disp_err = np.abs((got['pos'] - want['pos'] + box / 2) % box - box / 2).max()
+    assert disp_err < 1e-5 * np.abs(want['psi_x']).max()
+
+
+def test_grid_fixture_from_reference(built, bbks):
+    """Golden delta written by the reference build (tests/golden/make_golden.py)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'bbks32_serial.npz'))
+    got = _run('fp64', bbks, 32, 50.0, 'random_seed_serial')
+    assert _rel(got['delta'], g['delta']) < 1e-10
+    disp = (got['pos'] - g['pos'].astype(np.float64) + 25.0) % 50.0 - 25.0
+    assert np.abs(disp).max() < 5e-6

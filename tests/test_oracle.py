@@ -1,0 +1,106 @@
+"""The oracle against the reference's own known answers (CPU)."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import field_oracle as fo
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF_TESTS = '/root/reference/genetIC/tests'
+REF_BIN = os.path.join(ROOT, 'oracle', '_ref', 'genetIC')
+GOLDEN = os.path.join(ROOT, 'tests', 'golden')
+
+
+def test_chi2_real_space_seed_matches_reference_fixture():
+    # genetIC/tests/test_02k_chisquare_onelevel/reference.txt: random_seed_real_space 13842314, 64^3
+    fo.set_cr_log(False)
+    w = fo.white_noise(64, 13842314, 0)
+    assert '%.10g' % fo.chi2(w) == '261733.3011'
+
+
+def test_cr_log_mode_changes_nothing_at_this_size():
+    fo.set_cr_log(True)
+    a, _ = fo.gaussian_stream(13842314, 200000)
+    fo.set_cr_log(False)
+    b, _ = fo.gaussian_stream(13842314, 200000)
+    assert np.max(np.abs(a - b)) <= 2e-16 * np.max(np.abs(a))
+
+
+def test_ranlux_stream_first_values_stable():
+    s = fo.ranlux_stream(1, 48)
+    assert s.dtype == np.uint32 and s.max() < 2 ** 24
+    # stream is a pure function of the seed
+    assert np.array_equal(s, fo.ranlux_stream(1, 48))
+    assert not np.array_equal(s, fo.ranlux_stream(2, 48))
+
+
+def _load_golden(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+@pytest.mark.parametrize('mode', ['serial', 'parallel', 'real'])
+def test_field_oracle_matches_reference_delta(mode, bbks):
+    """Golden delta grids written by the reference build (tests/golden/make_golden.py)."""
+    from conftest import COSMO
+    g = _load_golden('bbks32_%s.npz' % mode)
+    fo.set_cr_log(False)
+    w = fo.white_noise(32, 8896131, {'serial': 1, 'parallel': 2, 'real': 0}[mode])
+    power = fo.CambPower(bbks, COSMO)
+    d, px, py, pz = fo.zeldovich_fields(w, power, 50.0)
+    ref = g['delta']
+    assert np.abs(d - ref).max() <= 1e-12 * np.abs(ref).max()
+    if 'pos' not in g:
+        return
+    pos, vel = fo.particles([px, py, pz], 50.0, (0, 0, 0), 50.0, fo.velocity_to_offset_ratio(COSMO))
+    # tipsy stores float32 positions in box units: compare to float32 resolution
+    dp = pos - g['pos'].astype(np.float64)
+    dp = (dp + 25.0) % 50.0 - 25.0
+    assert np.abs(dp).max() < 5e-6
+
+
+def _run_reference(tmp_path, name):
+    src = os.path.join(REF_TESTS, name)
+    dst = tmp_path / name
+    shutil.copytree(src, dst)
+    for dat in ('camb_transfer_kmax40_z0.dat', 'camb_transfer_kmax40_z0_post2015.dat'):
+        shutil.copy(os.path.join(REF_TESTS, dat), tmp_path / dat)
+    r = subprocess.run([REF_BIN, 'paramfile.txt'], cwd=dst, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return dst, r.stdout + r.stderr
+
+
+needs_reference = pytest.mark.skipif(not (os.path.isdir(REF_TESTS) and os.path.exists(REF_BIN)),
+                                     reason='reference sources / build not present')
+
+
+@needs_reference
+@pytest.mark.parametrize('name', ['test_02k_chisquare_onelevel', 'test_02m_chisquare_twolevels',
+                                  'test_02l_chisquare_modification', 'test_02f_onelevelvariance'])
+def test_reference_build_log_fixtures(tmp_path, name):
+    import re
+    d, out = _run_reference(tmp_path, name)
+    lines = [re.sub(r'^ [0-9]{4}-[0-9]{2}-[0-9]{2} [0-9]{2}:[0-9]{2}:[0-9]{2}   ', '', l) for l in out.splitlines()]
+    for want in open(d / 'reference.txt').read().splitlines():
+        if want.strip():
+            assert want in lines, want
+
+
+@needs_reference
+@pytest.mark.parametrize('name', ['test_13_parallel_seed', 'test_05a_seed_old'])
+def test_reference_build_tipsy_fixtures(tmp_path, name):
+    from tipsy_reader import read_tipsy
+    d, _ = _run_reference(tmp_path, name)
+    out = [f for f in os.listdir(d) if f.endswith('.tipsy')][0]
+    _, _, a = read_tipsy(d / out)
+    _, _, b = read_tipsy(d / 'reference_output')
+    assert np.array_equal(a, b)
+
+
+@needs_reference
+def test_reference_build_grid_fixture(tmp_path):
+    d, _ = _run_reference(tmp_path, 'test_01c_zoom_grid')
+    for g in ('grid-0.npy', 'grid-1.npy'):
+        np.testing.assert_almost_equal(np.load(d / g), np.load(d / 'reference_grid' / g), decimal=4)
