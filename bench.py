@@ -1,0 +1,315 @@
+"""Throughput of the GB300 field-realisation path (Mparticles/s).
+
+One step = one complete Zel'dovich realisation of the workload: white noise
+drawn from the seed, multiplied by sqrt(P(k)), displacement spectra, inverse
+FFTs, zoom combination where the workload has zoom levels, and particle
+positions/velocities -- with the transfer table already on the device
+(`value`), or end to end through the C ABI from host memory (`e2e`: the
+transfer table uploaded and the sigma8 normalisation recomputed every step,
+particles copied back to pinned host memory every step).
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+Under torchrun each rank runs an independent replica on its own GPU
+(realisations do not share data): value = all particles / max-over-ranks time.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # 512^3 single level, 100 Mpc/h box (the single-level configuration at 512^3)
+    'za512': dict(levels=[('base', 100.0, 512)], seed_cmd='random_seed', precision='mixed'),
+    'za512_fp64': dict(levels=[('base', 100.0, 512)], seed_cmd='random_seed', precision='fp64'),
+    'za256': dict(levels=[('base', 100.0, 256)], seed_cmd='random_seed', precision='mixed'),
+}
+DEFAULT_WORKLOAD = 'za512'
+COSMO = dict(omega_m=0.31, omega_lambda=0.69, omega_b=0.0, hubble=0.68, sigma8=0.81, ns=0.965, redshift=99.0)
+SEED = 8896131
+METRIC = "Mparticles/s, 512³ 2-level Zel'dovich IC: FP32+FP64 vs plain FP64 at ≤1e-5 err"
+
+
+def dist_env():
+    rank = int(os.environ.get('RANK', 0))
+    world = int(os.environ.get('WORLD_SIZE', 1))
+    local = int(os.environ.get('LOCAL_RANK', 0))
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_gen(wl, table, device):
+    import genetic_gb300 as g
+    gen = g.ICGenerator(precision=wl['precision'], device=device)
+    for k, v in (('Om', COSMO['omega_m']), ('Ol', COSMO['omega_lambda']), ('Ob', 0.0), ('hubble', COSMO['hubble']),
+                 ('s8', COSMO['sigma8']), ('ns', COSMO['ns']), ('zin', COSMO['redshift'])):
+        getattr(gen, k)(v)
+    gen.camb(table)
+    for lev in wl['levels']:
+        if lev[0] == 'base':
+            gen.base_grid(lev[1], lev[2])
+        else:
+            gen.zoom_grid_with_origin_at(*lev[1:])
+    return gen
+
+
+def n_particles(wl):
+    return sum(lev[2] ** 3 if lev[0] == 'base' else lev[5] ** 3 for lev in wl['levels'])
+
+
+class Clocks:
+    """nvidia-smi samples while the timed region runs."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, 'gpurun_out', 'bench_clocks.csv')
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, 'w')
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.index),
+                 '--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,'
+                 'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+                 'clocks_event_reasons.sw_power_cap', '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(',')]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[3:7]):
+                if v.lower() == 'active':
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {'sm_mhz': float(np.median(sm)), 'sm_max_mhz': max(mx), 'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
+        return float(peaks['hbm_gbs']), 'measured'
+    except (OSError, KeyError, ValueError):
+        return 6800.0, 'fallback'
+
+
+def fft_roofline(gen, wl, stream, reps=20):
+    """Average device time of one inverse 3-D FFT of the finest level's delta field."""
+    import torch
+    from genetic_gb300 import _lib
+    level = len(wl['levels']) - 1
+    n = gen.levels[level][1]
+    s = 4 if wl['precision'] == 'mixed' else 8
+    nc = n * n * (n // 2 + 1)
+    # the field is in real space after a realisation: forward then inverse keeps it meaningful
+    for _ in range(3):
+        gen._call('gic_fft', level, _lib.GIC_FIELD_DELTA, -1)
+        gen._call('gic_fft', level, _lib.GIC_FIELD_DELTA, +1)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * reps + 1)]
+    times = []
+    for r in range(reps):
+        gen._call('gic_fft', level, _lib.GIC_FIELD_DELTA, -1)
+        ev[2 * r].record(stream)
+        gen._call('gic_fft', level, _lib.GIC_FIELD_DELTA, +1)
+        ev[2 * r + 1].record(stream)
+    torch.cuda.synchronize()
+    for r in range(reps):
+        times.append(ev[2 * r].elapsed_time(ev[2 * r + 1]) * 1e-3)
+    t = float(np.mean(times))
+    algorithmic = 6.0 * (2 * s) * nc  # 3 passes, read + write of the half spectrum
+    peak, kind = measured_peak_hbm()
+    achieved = algorithmic / t / 1e9
+    return {'bound': 'hbm', 'achieved': round(achieved, 1), 'peak': peak, 'unit': 'GB/s',
+            'frac': round(achieved / peak, 4), 'traffic': None, 'kernel': 'fft_c2r_3d (%d^3, %s)' % (
+                n, 'fp32' if s == 4 else 'fp64'), 'ms_per_launch': round(t * 1e3, 4), 'peak_source': kind}
+
+
+def cpu_baseline_port(n=192, box=75.0, threads=None):
+    """The oracle's restatement of the path on the host: one single-level realisation."""
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import field_oracle as fo
+    from genetic_gb300.transfer import bbks_table
+    table = bbks_table()
+    t0 = time.perf_counter()
+    w = fo.white_noise(n, SEED, 2)
+    power = fo.CambPower(table, COSMO)
+    d = fo.zeldovich_fields(w, power, box)
+    fo.particles(d[1:], box, (0, 0, 0), box, fo.velocity_to_offset_ratio(COSMO))
+    dt = time.perf_counter() - t0
+    return n ** 3 / dt / 1e6, dt
+
+
+def run_reference(args, wl, rank, world):
+    if rank != 0:
+        return
+    n = 192
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline_port(n)
+    for _ in range(args.steps):
+        v, dt = cpu_baseline_port(n)
+        vals.append(dt)
+    t = float(np.mean(vals))
+    value = n ** 3 / t / 1e6
+    line = {'impl': 'reference', 'metric': METRIC, 'value': round(value, 4), 'unit': 'Mparticles/s',
+            'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(t * 1e3, 2),
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+            'config': {'workload': args.workload, 'sample': 'single-level %d^3 realisation (same cosmology, seed, '
+                                                            'seeding mode) per step' % n},
+            'cpu_baseline': {'value': round(value, 4), 'unit': 'Mparticles/s', 'cores': 1, 'kind': 'port',
+                             'sample': 'oracle restatement (C RANLUX+ziggurat, numpy FFT), %d^3 single level' % n},
+            'e2e': {'value': round(value, 4), 'unit': 'Mparticles/s', 'h2d_bytes_per_step': 0,
+                    'd2h_bytes_per_step': 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=5)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--workload', default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('gloo')
+    wl = WORKLOADS[args.workload]
+    if args.impl == 'reference':
+        run_reference(args, wl, rank, world)
+        return
+
+    import torch
+    from genetic_gb300 import _lib
+    from genetic_gb300.transfer import bbks_table
+    torch.cuda.set_device(local)
+    table = np.ascontiguousarray(bbks_table())
+    gen = make_gen(wl, table, local)
+    sptr = ctypes.c_void_p()
+    _lib.check(gen._ctx, gen._lib.gic_get_stream(gen._ctx, ctypes.byref(sptr)))
+    stream = torch.cuda.ExternalStream(sptr.value, device=torch.device('cuda', local))
+    mode = {'random_seed': _lib.GIC_SEED_FOURIER_PARALLEL, 'random_seed_serial': _lib.GIC_SEED_FOURIER_SERIAL,
+            'random_seed_real_space': _lib.GIC_SEED_REAL_SPACE}[wl['seed_cmd']]
+    npart = n_particles(wl)
+
+    def step(i):
+        gen._call('gic_draw_noise', SEED + i, mode)
+        gen._call('gic_zeldovich', 1)
+
+    for i in range(args.warmup):
+        step(i)
+    launches0 = ctypes.c_ulonglong()
+    gen._lib.gic_launch_count(ctypes.byref(launches0))
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        start.record(stream)
+        for i in range(args.steps):
+            step(args.warmup + i)
+        end.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    launches1 = ctypes.c_ulonglong()
+    gen._lib.gic_launch_count(ctypes.byref(launches1))
+    t = max_over_ranks(start.elapsed_time(end) * 1e-3 / args.steps, world)
+    value = npart * world / t / 1e6
+
+    # end to end through the C ABI, host buffers (pinned), copies inside the timed region
+    pinned = []
+    for lev in range(len(wl['levels'])):
+        n = gen.levels[lev][1]
+        pos = torch.empty((n ** 3, 3), dtype=torch.float64, pin_memory=True).numpy()
+        vel = torch.empty((n ** 3, 3), dtype=torch.float64, pin_memory=True).numpy()
+        pinned.append((pos, vel))
+    table_pinned = torch.empty(table.shape, dtype=torch.float64, pin_memory=True).numpy()
+    table_pinned[...] = table
+    from genetic_gb300.generator import _ptr
+
+    def e2e_step(i):
+        gen._call('gic_set_transfer', _ptr(table_pinned), table.shape[0], table.shape[1])
+        step(i)
+        for lev, (pos, vel) in enumerate(pinned):
+            gen._call('gic_fetch_particles', lev, _ptr(pos), _ptr(vel))
+
+    e2e_step(0)
+    barrier(world)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        e2e_step(i)
+    t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
+    d2h = sum(p.nbytes + v.nbytes for p, v in pinned)
+    roof = fft_roofline(gen, wl, stream)
+    gen.close()
+
+    if rank != 0:
+        return
+    line = {
+        'metric': METRIC, 'value': round(value, 3), 'unit': 'Mparticles/s', 'n_gpus': world, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': round(t * 1e3, 3), 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f32+f64' if wl['precision'] == 'mixed' else 'f64', 'data': 'synthetic',
+        'config': {'workload': args.workload, 'levels': [list(l) for l in wl['levels']],
+                   'precision': wl['precision'], 'seeding': wl['seed_cmd'], 'transfer': 'BBKS table, 2000 rows',
+                   'particles_per_step': npart, 'l2': 'inputs larger than L2 (fields >= 0.5 GB)',
+                   'parallelism': 'replicas' if world > 1 else 'single GPU'},
+        'e2e': {'value': round(npart * world / t_e2e / 1e6, 3), 'unit': 'Mparticles/s',
+                'h2d_bytes_per_step': int(table.nbytes), 'd2h_bytes_per_step': int(d2h)},
+        'gpu_launches': int(launches1.value - launches0.value),
+        'roofline': roof,
+        'clocks': clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        v, dt = cpu_baseline_port(256, 100.0)
+        line['cpu_baseline'] = {'value': round(v, 4), 'unit': 'Mparticles/s', 'cores': 1, 'kind': 'port',
+                                'sample': 'oracle restatement, one single-level 256^3 realisation (%.1f s)' % dt}
+    print(json.dumps(line))
+
+
+if __name__ == '__main__':
+    main()

@@ -62,6 +62,8 @@ SIGNATURES = {
     'gic_fetch_particles': [_P, _I, _D, _D],
     'gic_fft': [_P, _I, _I, _I],
     'gic_chi2': [_P, _D],
+    'gic_launch_count': [ctypes.POINTER(ctypes.c_ulonglong)],
+    'gic_get_stream': [_P, ctypes.POINTER(_P)],
 }
 
 _lib = None

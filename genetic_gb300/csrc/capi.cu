@@ -6,6 +6,7 @@
 #include <cstring>
 #include <exception>
 #include <new>
+#include <atomic>
 
 struct gic_ctx {
   gic::Context impl;
@@ -24,6 +25,13 @@ void cuda_check(cudaError_t e, const char *what) {
 }
 
 double velocity_to_offset_ratio(const Cosmo &c);
+
+static std::atomic<unsigned long long> g_launches{0};
+
+void launched(int kernels) {
+  cuda_check(cudaGetLastError(), "kernel launch");
+  g_launches.fetch_add((unsigned long long)kernels, std::memory_order_relaxed);
+}
 
 namespace {
 
@@ -90,7 +98,7 @@ void fetch_typed(Context &c, Level &L, int what, double *host) {
     } else {
       c.reduce.ensure(count * sizeof(double));
       k_to_double<T><<<(unsigned)((count + 255) / 256), 256, 0, s>>>(L.noise.as<T>(), c.reduce.as<double>(), count);
-      GIC_CUDA(cudaGetLastError());
+      launched();
       GIC_CUDA(cudaMemcpyAsync(host, c.reduce.ptr, count * sizeof(double), cudaMemcpyDeviceToHost, s));
     }
   } else {
@@ -99,7 +107,7 @@ void fetch_typed(Context &c, Level &L, int what, double *host) {
     size_t m = L.ncells();
     c.reduce.ensure(m * sizeof(double));
     k_unpad_real<T><<<(unsigned)((m + 255) / 256), 256, 0, s>>>(L.field[f].as<T>(), c.reduce.as<double>(), L.n);
-    GIC_CUDA(cudaGetLastError());
+    launched();
     GIC_CUDA(cudaMemcpyAsync(host, c.reduce.ptr, m * sizeof(double), cudaMemcpyDeviceToHost, s));
   }
   GIC_CUDA(cudaStreamSynchronize(s));
@@ -116,7 +124,7 @@ void set_noise_typed(Context &c, Level &L, const double *host) {
     c.reduce.ensure(count * sizeof(double));
     GIC_CUDA(cudaMemcpyAsync(c.reduce.ptr, host, count * sizeof(double), cudaMemcpyHostToDevice, s));
     k_from_double<T><<<(unsigned)((count + 255) / 256), 256, 0, s>>>(c.reduce.as<double>(), L.noise.as<T>(), count);
-    GIC_CUDA(cudaGetLastError());
+    launched();
   }
   GIC_CUDA(cudaStreamSynchronize(s));
   L.have_noise = true;
@@ -129,7 +137,7 @@ double chi2_typed(Context &c, Level &L) {
   DevBuf partial;
   partial.ensure(blocks * sizeof(double));
   k_chi2_partial<T><<<blocks, 256, 0, c.stream>>>(L.noise.as<T>(), L.n, partial.as<double>());
-  GIC_CUDA(cudaGetLastError());
+  launched();
   std::vector<double> h(blocks);
   GIC_CUDA(cudaMemcpyAsync(h.data(), partial.ptr, blocks * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
   GIC_CUDA(cudaStreamSynchronize(c.stream));
@@ -198,6 +206,18 @@ int gic_create(gic_ctx **out, const gic_device_opts *opts) {
     return GIC_ERR_CUDA;
   }
   *out = c;
+  return GIC_OK;
+}
+
+int gic_launch_count(unsigned long long *count) {
+  if (!count) return GIC_ERR_INVALID_ARG;
+  *count = gic::g_launches.load();
+  return GIC_OK;
+}
+
+int gic_get_stream(gic_ctx *ctx, void **stream) {
+  if (!ctx || !stream) return GIC_ERR_INVALID_ARG;
+  *stream = (void *)ctx->impl.stream;
   return GIC_OK;
 }
 
@@ -326,7 +346,7 @@ int gic_fetch_particles(gic_ctx *ctx, int level, double *pos, double *vel) {
       C.reduce.ensure(3 * m * sizeof(double));
       gic::k_to_double<float><<<(unsigned)((3 * m + 255) / 256), 256, 0, C.stream>>>(L.vel.as<float>(),
                                                                                    C.reduce.as<double>(), 3 * m);
-      GIC_CUDA(cudaGetLastError());
+      gic::launched();
       GIC_CUDA(cudaMemcpyAsync(vel, C.reduce.ptr, 3 * m * sizeof(double), cudaMemcpyDeviceToHost, C.stream));
     }
   }

@@ -357,7 +357,7 @@ void strided_pass(Context &ctx, typename Cx<T>::type *data, int A, int L, long l
   set_smem<T>((const void *)k_fft_strided<T>, smem);
   dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)A);
   k_fft_strided<T><<<grid, 256, smem, ctx.stream>>>(data, L, B, TC, plan, sign, tw, scale);
-  GIC_CUDA(cudaGetLastError());
+  launched();
 }
 
 template <typename T>
@@ -401,7 +401,7 @@ void fft_c2r_3d(Context &ctx, T *data, int n, double scale) {
   long long S = n / 2 + 1;
   long long mirror_threads = 2ll * n * n;
   k_mirror<T><<<(unsigned)((mirror_threads + 255) / 256), 256, 0, ctx.stream>>>(c, n);
-  GIC_CUDA(cudaGetLastError());
+  launched();
   strided_pass<T>(ctx, c, 1, n, (long long)n * S, +1, (T)1, tw);
   strided_pass<T>(ctx, c, n, n, S, +1, (T)1, tw);
   int rpc = rows_per_cta<T>(n);
@@ -411,7 +411,7 @@ void fft_c2r_3d(Context &ctx, T *data, int n, double scale) {
   long long nrows = (long long)n * n;
   k_fft_rows_c2r<T><<<(unsigned)((nrows + rpc - 1) / rpc), 256, smem, ctx.stream>>>(c, nrows, n, rpc, plan, tw,
                                                                                    (T)scale);
-  GIC_CUDA(cudaGetLastError());
+  launched();
 }
 
 template <typename T>
@@ -428,7 +428,7 @@ void fft_r2c_3d(Context &ctx, T *data, int n, double scale) {
   long long nrows = (long long)n * n;
   k_fft_rows_r2c<T><<<(unsigned)((nrows + rpc - 1) / rpc), 256, smem, ctx.stream>>>(c, nrows, n, rpc, plan, tw,
                                                                                    (T)1);
-  GIC_CUDA(cudaGetLastError());
+  launched();
   strided_pass<T>(ctx, c, n, n, S, -1, (T)1, tw);
   strided_pass<T>(ctx, c, 1, n, (long long)n * S, -1, (T)scale, tw);
 }

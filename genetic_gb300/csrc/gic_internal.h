@@ -15,6 +15,8 @@ struct Error {
 };
 
 [[noreturn]] void fail(int code, const std::string &msg);
+// check the last launch and count it (gic_launch_count)
+void launched(int kernels = 1);
 void cuda_check(cudaError_t e, const char *what);
 #define GIC_CUDA(call) ::gic::cuda_check((call), #call)
 

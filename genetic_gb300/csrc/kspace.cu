@@ -218,7 +218,7 @@ void transfer_setup(Context &ctx, const double *table, int nrows, int ncols) {
                                  work.as<double>());
   k_spline_solve<<<1, 1, 0, s>>>(T.lnk.as<double>(), T.lnT_dm.as<double>(), T.c_dm.as<double>(), n,
                                  work.as<double>());
-  GIC_CUDA(cudaGetLastError());
+  launched(2);
 
   // sigma8 before normalisation, radius 8 Mpc/h, species "all"
   const double radius = 8.0;
@@ -234,7 +234,7 @@ void transfer_setup(Context &ctx, const double *table, int nrows, int ncols) {
   k_sigma8_ks<<<1, 1, 0, s>>>(kmin, kmax, dk, ks.as<double>(), cap, cnt.as<int>());
   k_sigma8_terms<<<blocks, 256, 0, s>>>(ks.as<double>(), cnt.as<int>(), ctx.cosmo.ns, radius, T.lnk.as<double>(),
                                         T.lnT_all.as<double>(), T.c_all.as<double>(), n, partial.as<double>());
-  GIC_CUDA(cudaGetLastError());
+  launched(2);
   std::vector<double> hp(blocks);
   GIC_CUDA(cudaMemcpyAsync(hp.data(), partial.ptr, blocks * sizeof(double), cudaMemcpyDeviceToHost, s));
   GIC_CUDA(cudaStreamSynchronize(s));
@@ -265,7 +265,7 @@ void build_sqrtp_table(Context &ctx, Level &L) {
   k_sqrtp_table<<<(unsigned)((nq + 255) / 256), 256, 0, ctx.stream>>>(
       L.sqrtp.as<double>(), nq, L.kmin(), ctx.transfer.amplitude, ctx.cosmo.ns, norm, ctx.transfer.lnk.as<double>(),
       ctx.transfer.lnT_all.as<double>(), ctx.transfer.c_all.as<double>(), ctx.transfer.nrows);
-  GIC_CUDA(cudaGetLastError());
+  launched();
 }
 
 template <typename T>
@@ -278,7 +278,7 @@ static void za_fields_typed(Context &ctx, Level &L) {
   k_za_fields<T><<<blocks, 256, 0, ctx.stream>>>(L.noise.as<C>(), L.sqrtp.as<double>(), L.n, (T)L.kmin(),
                                                  L.field[0].as<C>(), L.field[1].as<C>(), L.field[2].as<C>(),
                                                  L.field[3].as<C>());
-  GIC_CUDA(cudaGetLastError());
+  launched();
   double scale = 1.0 / std::pow((double)L.n, 1.5);
   for (int f = 0; f < 4; ++f) fft_c2r_3d<T>(ctx, L.field[f].as<T>(), L.n, scale);
   L.have_fields = true;

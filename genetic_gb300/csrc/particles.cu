@@ -59,7 +59,7 @@ static void particles_typed(Context &ctx, Level &L) {
   k_particles<T><<<(unsigned)((m + 255) / 256), 256, 0, ctx.stream>>>(
       L.field[1].as<T>(), L.field[2].as<T>(), L.field[3].as<T>(), L.n, L.dx, L.x0[0], L.x0[1], L.x0[2], L.periodic,
       ratio, L.pos.as<double>(), L.vel.as<T>());
-  GIC_CUDA(cudaGetLastError());
+  launched();
 }
 
 void make_particles(Context &ctx, Level &L) {

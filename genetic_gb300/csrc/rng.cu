@@ -417,7 +417,7 @@ static void generate_gaussians(Context &ctx, std::vector<Stream> &streams, unsig
     GIC_CUDA(cudaMemcpyAsync(dpow.ptr, pow2.data(), pow2.size() * sizeof(U576), cudaMemcpyHostToDevice, cs));
     R.chunkmul.ensure((size_t)count * sizeof(U576));
     k_chunk_multipliers<<<(count + 127) / 128, 128, 0, cs>>>(R.chunkmul.as<U576>(), count, dpow.as<U576>(), npow);
-    GIC_CUDA(cudaGetLastError());
+    launched();
     GIC_CUDA(cudaStreamSynchronize(cs));
     R.chunkmul_count = count;
   }
@@ -426,22 +426,22 @@ static void generate_gaussians(Context &ctx, std::vector<Stream> &streams, unsig
   GIC_CUDA(cudaMemcpyAsync(dst, streams.data(), streams.size() * sizeof(Stream), cudaMemcpyHostToDevice, cs));
   GIC_CUDA(cudaMemsetAsync(R.flags.ptr, 0, sizeof(int) * 4, cs));
   k_seed<<<(ns + 127) / 128, 128, 0, cs>>>(dst, ns);
-  GIC_CUDA(cudaGetLastError());
+  launched();
   k_generate<<<(unsigned)((chunk_total + 127) / 128), 128, 0, cs>>>(dst, ns, chunk_total, R.chunkmul.as<U576>(),
                                                                    R.raw.as<uint32_t>());
-  GIC_CUDA(cudaGetLastError());
+  launched();
   unsigned long long nspec = seg_total * kSpec;
   k_walk_speculative<<<(unsigned)((nspec + 127) / 128), 128, 0, cs>>>(dst, ns, seg_total, R.raw.as<uint32_t>(),
                                                                      R.segtab.as<uint2>());
-  GIC_CUDA(cudaGetLastError());
+  launched();
   k_resolve<<<(ns + 63) / 64, 64, 0, cs>>>(dst, ns, R.raw.as<uint32_t>(), R.segtab.as<uint2>(),
                                           R.segentry.as<uint32_t>(), R.segbase.as<unsigned long long>(),
                                           R.flags.as<int>());
-  GIC_CUDA(cudaGetLastError());
+  launched();
   k_walk_final<<<(unsigned)((seg_total + 127) / 128), 128, 0, cs>>>(
       dst, ns, seg_total, R.raw.as<uint32_t>(), R.segentry.as<uint32_t>(), R.segbase.as<unsigned long long>(),
       R.gauss.as<double>(), R.flags.as<int>());
-  GIC_CUDA(cudaGetLastError());
+  launched();
   int flag = 0;
   GIC_CUDA(cudaMemcpyAsync(&flag, R.flags.ptr, sizeof(int), cudaMemcpyDeviceToHost, cs));
   GIC_CUDA(cudaStreamSynchronize(cs));
@@ -469,10 +469,10 @@ static void draw_level_typed(Context &ctx, Level &L, unsigned long long seed, in
     generate_gaussians(ctx, streams, m, 1.0);
     GIC_CUDA(cudaMemsetAsync(out, 0, nc * 2 * sizeof(T), cs));
     k_place_real<T><<<(unsigned)((m + 255) / 256), 256, 0, cs>>>(n, ctx.rng.gauss.as<double>(), out);
-    GIC_CUDA(cudaGetLastError());
+    launched();
     fft_r2c_3d<T>(ctx, out, n, 1.0 / std::pow((double)n, 1.5));
     k_zero_first<T><<<1, 1, 0, cs>>>(out);
-    GIC_CUDA(cudaGetLastError());
+    launched();
   } else {
     int half = n / 2;
     unsigned long long nmodes = shell_offset(half);
@@ -498,11 +498,11 @@ static void draw_level_typed(Context &ctx, Level &L, unsigned long long seed, in
       GIC_CUDA(cudaMemsetAsync(ctx.rng.owner.ptr, 0xFF, nc * sizeof(int), cs));
       unsigned blocks = (unsigned)((nmodes + 255) / 256);
       k_place_owner<<<blocks, 256, 0, cs>>>(n, nmodes, ctx.rng.owner.as<int>());
-      GIC_CUDA(cudaGetLastError());
+      launched();
       T norm = (T)(1.0 / std::sqrt(2.0));
       k_place_write<T><<<blocks, 256, 0, cs>>>(n, nmodes, ctx.rng.owner.as<int>(), ctx.rng.gauss.as<double>(),
                                                norm, mode == GIC_SEED_FOURIER_REVERSE ? 1 : 0, out);
-      GIC_CUDA(cudaGetLastError());
+      launched();
     }
   }
   GIC_CUDA(cudaStreamSynchronize(cs));

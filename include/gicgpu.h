@@ -136,6 +136,13 @@ GIC_API int gic_fft(gic_ctx *ctx, int level, int what, int dir);
  * (MultiLevelField::getChi2, multilevelfield.hpp:461-487). */
 GIC_API int gic_chi2(gic_ctx *ctx, double *chi2);
 
+/* Number of kernels this library has launched in the process so far. */
+GIC_API int gic_launch_count(unsigned long long *count);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that order their own
+ * work or timing events after the library's. */
+GIC_API int gic_get_stream(gic_ctx *ctx, void **stream);
+
 #ifdef __cplusplus
 }
 #endif
