@@ -91,7 +91,7 @@ struct FftTables {
 };
 
 struct RngScratch {
-  DevBuf raw, gauss, owner, segtab, segentry, segbase, streams, chunkmul, flags;
+  DevBuf raw, gauss, owner, segtab, segentry, segbase, blkmap, blkentry, blkbase, streams, chunkmul, flags;
   int chunkmul_count = 0;
 };
 

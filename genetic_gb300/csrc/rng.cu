@@ -28,8 +28,11 @@ namespace {
 
 constexpr int kLux = 794;          // 24-bit steps per delivered block
 constexpr int kChunkBlocks = 16;   // blocks per generator thread
-constexpr int kSegLen = 2048;      // stream numbers per ziggurat segment
-constexpr int kSpec = 4;           // speculative entry offsets per segment
+constexpr int kSegLen = 1024;      // stream numbers per ziggurat segment
+constexpr int kSpec = 8;           // speculative entry offsets per segment
+constexpr int kTileSegs = 8;       // segments staged together in shared memory
+constexpr int kOverhang = 256;     // numbers staged past the tile end
+constexpr int kBlockSegs = 64;     // segments per block of the two-level chain
 constexpr uint32_t kUnderrun = 0xFFFFFFFFu;
 
 __constant__ double dZigY[128] = GIC_ZIG_Y_INIT;
@@ -42,7 +45,8 @@ struct Stream {
   unsigned long long gauss_off, gauss_count;  // gaussians required
   unsigned long long seg_off;                 // first global segment
   unsigned long long chunk_off;               // first global generator chunk
-  unsigned int nseg, nchunk;
+  unsigned long long blk_off;                 // first global chain block
+  unsigned int nseg, nchunk, nblk;
   U576 y0;
 };
 
@@ -74,6 +78,15 @@ __device__ __forceinline__ int find_stream_by_chunk(const Stream *st, int nstrea
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
     if (st[mid].chunk_off <= c) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int find_stream_by_block(const Stream *st, int nstreams, unsigned long long b) {
+  int lo = 0, hi = nstreams - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (st[mid].blk_off <= b) lo = mid; else hi = mid - 1;
   }
   return lo;
 }
@@ -139,114 +152,204 @@ __global__ void __launch_bounds__(128) k_generate(const Stream *st, int nstreams
 }
 
 // ---- ziggurat ---------------------------------------------------------------
+//
+// A gaussian starting at stream position p consumes 2 numbers when the first
+// attempt is accepted on the integer test j < ktab[i] (97.2% of attempts);
+// otherwise 3 (layer < 127) or 4 (base strip) numbers plus, if rejected,
+// further attempts.  Consumption is found with integer work alone on the fast
+// path; doubles are only used on the slow path and for the final values.
 
-// One gaussian starting at stream position *p; returns false on running past n.
-__device__ __forceinline__ bool zig_gaussian(const uint32_t *r, unsigned long long n, unsigned long long &p,
+// Stream numbers come from a shared-memory copy of the tile when the index is
+// inside it, else from global memory.
+struct Reader {
+  const uint32_t *g;       // raw buffer (absolute indices)
+  const uint32_t *sm;      // shared copy of [lo, hi)
+  unsigned long long lo, hi;
+  __device__ __forceinline__ uint32_t operator()(unsigned long long p) const {
+    return (p >= lo && p < hi) ? sm[p - lo] : __ldg(g + p);
+  }
+};
+
+// Advance p past one gaussian of the stream ending at `end`; optionally return
+// its value.  Returns false when the stream runs out.
+template <bool VALUE>
+__device__ __forceinline__ bool zig_gaussian(const Reader &rd, unsigned long long end, unsigned long long &p,
                                              double &g) {
   const double R = GIC_ZIG_PARAM_R;
   for (int guard = 0; guard < 1 << 20; ++guard) {
-    if (p + 2 > n) return false;
-    uint32_t k1 = __ldg(r + p), k2 = __ldg(r + p + 1);
+    if (p + 2 > end) return false;
+    uint32_t k1 = rd(p), k2 = rd(p + 1);
     unsigned i = k1 & 0xFFu;
     uint32_t j = k2 & 0xFFFFFFu;
-    double sign = (i & 0x80u) ? 1.0 : -1.0;
-    i &= 0x7Fu;
-    double x = __dmul_rn((double)j, dZigW[i]);
-    if (j < dZigK[i]) {
-      g = __dmul_rn(sign, x);
+    unsigned il = i & 0x7Fu;
+    if (j < dZigK[il]) {
+      if (VALUE) g = __dmul_rn((i & 0x80u) ? 1.0 : -1.0, __dmul_rn((double)j, dZigW[il]));
       p += 2;
       return true;
     }
+    double x = __dmul_rn((double)j, dZigW[il]);
     double y;
-    if (i < 127) {
-      if (p + 3 > n) return false;
-      double u1 = __dmul_rn((double)__ldg(r + p + 2), 1.0 / 16777216.0);
-      y = __dadd_rn(dZigY[i + 1], __dmul_rn(__dsub_rn(dZigY[i], dZigY[i + 1]), u1));
+    if (il < 127) {
+      if (p + 3 > end) return false;
+      double u1 = __dmul_rn((double)rd(p + 2), 1.0 / 16777216.0);
+      y = __dadd_rn(dZigY[il + 1], __dmul_rn(__dsub_rn(dZigY[il], dZigY[il + 1]), u1));
       p += 3;
     } else {
-      if (p + 4 > n) return false;
-      uint32_t kk = __ldg(r + p + 2);
-      double u2 = __dmul_rn((double)__ldg(r + p + 3), 1.0 / 16777216.0);
+      if (p + 4 > end) return false;
+      uint32_t kk = rd(p + 2);
+      double u2 = __dmul_rn((double)rd(p + 3), 1.0 / 16777216.0);
       double lg = gic_log_k24(16777216u - kk);  // log(1 - kk/2^24), correctly rounded
       x = __dsub_rn(R, __ddiv_rn(lg, R));
       y = __dmul_rn(exp(__dmul_rn(-R, __dsub_rn(x, __dmul_rn(0.5, R)))), u2);
       p += 4;
     }
     if (y < exp(__dmul_rn(__dmul_rn(-0.5, x), x))) {
-      g = __dmul_rn(sign, x);
+      if (VALUE) g = __dmul_rn((i & 0x80u) ? 1.0 : -1.0, x);
       return true;
     }
   }
   return false;
 }
 
-// Walk one segment from `entry`; counts gaussians that start inside it.
-__device__ void walk_segment(const uint32_t *r, unsigned long long n, unsigned long long seg_start,
-                             unsigned long long seg_end, unsigned long long entry, uint32_t &count,
-                             uint32_t &exit_off, double *out, unsigned long long out_limit) {
+// Walk [seg_start, seg_end) from seg_start + entry, counting gaussians that
+// start in the segment; exit = position after the last one minus seg_end.
+template <bool VALUE>
+__device__ void walk_segment(const Reader &rd, unsigned long long stream_end, unsigned long long seg_start,
+                             unsigned long long seg_end, unsigned entry, uint32_t &count, uint32_t &exit_off,
+                             double *out, unsigned long long out_limit) {
   unsigned long long p = seg_start + entry;
   uint32_t cnt = 0;
   while (p < seg_end) {
-    double g;
-    if (!zig_gaussian(r, n, p, g)) {
+    if (VALUE && cnt >= out_limit) break;
+    double g = 0;
+    if (!zig_gaussian<VALUE>(rd, stream_end, p, g)) {
       count = cnt;
       exit_off = kUnderrun;
       return;
     }
-    if (out) {
-      if (cnt >= out_limit) break;
-      out[cnt] = g;
-    }
+    if (VALUE) out[cnt] = g;
     ++cnt;
   }
   count = cnt;
-  exit_off = (uint32_t)(p > seg_end ? p - seg_end : 0);
+  exit_off = p >= seg_end ? (uint32_t)(p - seg_end) : 0u;
 }
 
-__global__ void k_walk_speculative(const Stream *st, int nstreams, unsigned long long nseg_total,
-                                   const uint32_t *raw, uint2 *tab) {
-  unsigned long long id = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (id >= nseg_total * kSpec) return;
-  unsigned long long gseg = id / kSpec;
-  int e = (int)(id % kSpec);
+// packed (count, exit): count in the low 16 bits, exit in the high 16, 0xFFFF = underrun/overflow
+__device__ __forceinline__ uint32_t pack_ce(uint32_t cnt, uint32_t ex) {
+  return (cnt & 0xFFFFu) | ((ex == kUnderrun || ex >= 0xFFFFu ? 0xFFFFu : ex) << 16);
+}
+
+__device__ __forceinline__ void segment_bounds(const Stream &s, unsigned long long lseg, unsigned long long &a,
+                                               unsigned long long &b) {
+  a = s.raw_off + lseg * kSegLen;
+  b = a + kSegLen;
+  unsigned long long e = s.raw_off + s.raw_count;
+  if (b > e) b = e;
+}
+
+// One CTA per tile of kTileSegs consecutive segments (of any streams); the
+// tile's numbers plus an overhang are staged in shared memory, then
+// kTileSegs * kSpec threads walk every (segment, entry offset) pair.
+__global__ void __launch_bounds__(kTileSegs * kSpec) k_walk_speculative(const Stream *st, int nstreams,
+                                                                       unsigned long long nseg_total,
+                                                                       const uint32_t *raw,
+                                                                       unsigned long long raw_total,
+                                                                       uint32_t *tab) {
+  __shared__ uint32_t sm[kTileSegs * kSegLen + kOverhang];
+  unsigned long long g0 = (unsigned long long)blockIdx.x * kTileSegs;
+  if (g0 >= nseg_total) return;
+  // tile range in absolute stream positions
+  int s0 = find_stream_by_segment(st, nstreams, g0);
+  unsigned long long lo = st[s0].raw_off + (g0 - st[s0].seg_off) * kSegLen;
+  unsigned long long hi = lo + kTileSegs * kSegLen + kOverhang;
+  if (hi > raw_total) hi = raw_total;
+  for (unsigned long long q = lo + threadIdx.x; q < hi; q += blockDim.x) sm[q - lo] = __ldg(raw + q);
+  __syncthreads();
+  unsigned long long gseg = g0 + threadIdx.x / kSpec;
+  unsigned e = threadIdx.x % kSpec;
+  if (gseg >= nseg_total) return;
   int s = find_stream_by_segment(st, nstreams, gseg);
-  unsigned long long lseg = gseg - st[s].seg_off;
-  const uint32_t *r = raw + st[s].raw_off;
-  unsigned long long n = st[s].raw_count;
-  unsigned long long a = lseg * kSegLen, b = a + kSegLen;
-  if (b > n) b = n;
+  unsigned long long a, b;
+  segment_bounds(st[s], gseg - st[s].seg_off, a, b);
+  Reader rd{raw, sm, lo, hi};
   uint32_t cnt = 0, ex = 0;
-  walk_segment(r, n, a, b, (unsigned long long)e, cnt, ex, nullptr, 0);
-  tab[id] = make_uint2(cnt, ex);
+  walk_segment<false>(rd, st[s].raw_off + st[s].raw_count, a, b, e, cnt, ex, nullptr, 0);
+  tab[gseg * kSpec + e] = pack_ce(cnt, ex);
 }
 
-// One thread per stream chains the segments.  flags[0] is set on underrun.
-__global__ void k_resolve(const Stream *st, int nstreams, const uint32_t *raw, const uint2 *tab,
-                          uint32_t *seg_entry, unsigned long long *seg_base, int *flags) {
+// Follow segment g from entry e: table lookup, or a real walk when the entry
+// is beyond the speculated offsets.
+__device__ __forceinline__ void step_segment(const Stream &s, const uint32_t *raw, const uint32_t *tab,
+                                             unsigned long long gseg, unsigned e, uint32_t &cnt, uint32_t &ex) {
+  if (e < (unsigned)kSpec) {
+    uint32_t v = tab[gseg * kSpec + e];
+    cnt = v & 0xFFFFu;
+    ex = v >> 16;
+    if (ex != 0xFFFFu) return;
+  }
+  unsigned long long a, b;
+  segment_bounds(s, gseg - s.seg_off, a, b);
+  Reader rd{raw, raw, 0, 0};
+  walk_segment<false>(rd, s.raw_off + s.raw_count, a, b, e, cnt, ex, nullptr, 0);
+}
+
+// Level 1: map of each block of kBlockSegs segments for every entry offset.
+__global__ void k_block_maps(const Stream *st, int nstreams, unsigned long long nblk_total, const uint32_t *raw,
+                             const uint32_t *tab, uint2 *bmap) {
+  unsigned long long id = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= nblk_total * kSpec) return;
+  unsigned long long blk = id / kSpec;
+  unsigned e = (unsigned)(id % kSpec);
+  int s = find_stream_by_block(st, nstreams, blk);
+  const Stream &S = st[s];
+  unsigned long long lblk = blk - S.blk_off;
+  unsigned long long g = S.seg_off + lblk * kBlockSegs;
+  unsigned long long gend = min(S.seg_off + (unsigned long long)S.nseg, g + kBlockSegs);
+  uint32_t total = 0;
+  for (; g < gend; ++g) {
+    uint32_t cnt, ex;
+    step_segment(S, raw, tab, g, e, cnt, ex);
+    total += cnt;
+    if (ex == kUnderrun || ex == 0xFFFFu) { e = 0xFFFFu; break; }
+    e = ex;
+  }
+  bmap[id] = make_uint2(total, e);
+}
+
+// Level 2: one thread per stream chains its blocks.  flags[0] set on underrun.
+__global__ void k_chain_blocks(const Stream *st, int nstreams, const uint32_t *raw, const uint32_t *tab,
+                               const uint2 *bmap, uint32_t *blk_entry, unsigned long long *blk_base, int *flags) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nstreams) return;
-  const uint32_t *r = raw + st[s].raw_off;
-  unsigned long long n = st[s].raw_count;
-  unsigned long long need = st[s].gauss_count;
-  unsigned long long base = 0;
-  uint32_t e = 0;
-  for (unsigned int g = 0; g < st[s].nseg; ++g) {
-    unsigned long long gseg = st[s].seg_off + g;
-    seg_entry[gseg] = e;
-    seg_base[gseg] = base;
+  const Stream &S = st[s];
+  unsigned long long need = S.gauss_count, base = 0;
+  unsigned e = 0;
+  for (unsigned b = 0; b < S.nblk; ++b) {
+    unsigned long long blk = S.blk_off + b;
+    blk_entry[blk] = e;
+    blk_base[blk] = base;
     if (base >= need) continue;
-    uint32_t cnt, ex;
-    if (e < kSpec) {
-      uint2 v = tab[gseg * kSpec + e];
-      cnt = v.x;
+    uint32_t total, ex;
+    if (e < (unsigned)kSpec) {
+      uint2 v = bmap[blk * kSpec + e];
+      total = v.x;
       ex = v.y;
     } else {
-      unsigned long long a = (unsigned long long)g * kSegLen, b = a + kSegLen;
-      if (b > n) b = n;
-      walk_segment(r, n, a, b, e, cnt, ex, nullptr, 0);
+      // entry beyond the speculated offsets: chain the block's segments here
+      total = 0;
+      ex = e;
+      unsigned long long g = S.seg_off + (unsigned long long)b * kBlockSegs;
+      unsigned long long gend = min(S.seg_off + (unsigned long long)S.nseg, g + kBlockSegs);
+      for (; g < gend; ++g) {
+        uint32_t cnt, x2;
+        step_segment(S, raw, tab, g, ex, cnt, x2);
+        total += cnt;
+        if (x2 == kUnderrun || x2 == 0xFFFFu) { ex = 0xFFFFu; break; }
+        ex = x2;
+      }
     }
-    base += cnt;
-    if (ex == kUnderrun) {
+    base += total;
+    if (ex == 0xFFFFu) {
       if (base < need) atomicExch(flags, 1);
       e = 0;
       continue;
@@ -256,22 +359,45 @@ __global__ void k_resolve(const Stream *st, int nstreams, const uint32_t *raw, c
   if (base < need) atomicExch(flags, 1);
 }
 
+// Level 3: one thread per block writes each segment's entry and gaussian base.
+__global__ void k_chain_segments(const Stream *st, int nstreams, unsigned long long nblk_total, const uint32_t *raw,
+                                 const uint32_t *tab, const uint32_t *blk_entry, const unsigned long long *blk_base,
+                                 uint32_t *seg_entry, unsigned long long *seg_base) {
+  unsigned long long blk = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (blk >= nblk_total) return;
+  int s = find_stream_by_block(st, nstreams, blk);
+  const Stream &S = st[s];
+  unsigned long long g = S.seg_off + (blk - S.blk_off) * kBlockSegs;
+  unsigned long long gend = min(S.seg_off + (unsigned long long)S.nseg, g + kBlockSegs);
+  unsigned e = blk_entry[blk];
+  unsigned long long base = blk_base[blk];
+  for (; g < gend; ++g) {
+    seg_entry[g] = e;
+    seg_base[g] = base;
+    if (base >= S.gauss_count) { e = 0; continue; }
+    uint32_t cnt, ex;
+    step_segment(S, raw, tab, g, e, cnt, ex);
+    base += cnt;
+    e = (ex == kUnderrun || ex == 0xFFFFu) ? 0 : ex;
+  }
+}
+
 __global__ void k_walk_final(const Stream *st, int nstreams, unsigned long long nseg_total, const uint32_t *raw,
                              const uint32_t *seg_entry, const unsigned long long *seg_base, double *gauss,
                              int *flags) {
   unsigned long long gseg = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (gseg >= nseg_total) return;
   int s = find_stream_by_segment(st, nstreams, gseg);
+  const Stream &S = st[s];
   unsigned long long base = seg_base[gseg];
-  unsigned long long need = st[s].gauss_count;
+  unsigned long long need = S.gauss_count;
   if (base >= need) return;
-  unsigned long long lseg = gseg - st[s].seg_off;
-  const uint32_t *r = raw + st[s].raw_off;
-  unsigned long long n = st[s].raw_count;
-  unsigned long long a = lseg * kSegLen, b = a + kSegLen;
-  if (b > n) b = n;
+  unsigned long long a, b;
+  segment_bounds(S, gseg - S.seg_off, a, b);
+  Reader rd{raw, raw, 0, 0};
   uint32_t cnt, ex;
-  walk_segment(r, n, a, b, seg_entry[gseg], cnt, ex, gauss + st[s].gauss_off + base, need - base);
+  walk_segment<true>(rd, S.raw_off + S.raw_count, a, b, seg_entry[gseg], cnt, ex, gauss + S.gauss_off + base,
+                     need - base);
   if (ex == kUnderrun && base + cnt < need) atomicExch(flags, 1);
 }
 
@@ -376,7 +502,7 @@ static void generate_gaussians(Context &ctx, std::vector<Stream> &streams, unsig
                                double margin) {
   cudaStream_t cs = ctx.stream;
   int ns = (int)streams.size();
-  unsigned long long raw_total = 0, seg_total = 0, chunk_total = 0, max_chunks = 0;
+  unsigned long long raw_total = 0, seg_total = 0, chunk_total = 0, max_chunks = 0, blk_total = 0;
   for (auto &s : streams) {
     s.raw_off = raw_total;
     s.raw_count = (unsigned long long)(raw_needed(s.gauss_count) * margin);
@@ -385,6 +511,9 @@ static void generate_gaussians(Context &ctx, std::vector<Stream> &streams, unsig
     s.nseg = (unsigned int)((s.raw_count + kSegLen - 1) / kSegLen);
     s.seg_off = seg_total;
     seg_total += s.nseg;
+    s.nblk = (s.nseg + kBlockSegs - 1) / kBlockSegs;
+    s.blk_off = blk_total;
+    blk_total += s.nblk;
     unsigned long long blocks = s.raw_count / 24;
     s.nchunk = (unsigned int)((blocks + kChunkBlocks - 1) / kChunkBlocks);
     s.chunk_off = chunk_total;
@@ -394,9 +523,12 @@ static void generate_gaussians(Context &ctx, std::vector<Stream> &streams, unsig
   RngScratch &R = ctx.rng;
   R.raw.ensure(raw_total * sizeof(uint32_t));
   R.gauss.ensure(total_gauss * sizeof(double));
-  R.segtab.ensure(seg_total * kSpec * sizeof(uint2));
+  R.segtab.ensure(seg_total * kSpec * sizeof(uint32_t));
   R.segentry.ensure(seg_total * sizeof(uint32_t));
   R.segbase.ensure(seg_total * sizeof(unsigned long long));
+  R.blkmap.ensure(blk_total * kSpec * sizeof(uint2));
+  R.blkentry.ensure(blk_total * sizeof(uint32_t));
+  R.blkbase.ensure(blk_total * sizeof(unsigned long long));
   R.streams.ensure(streams.size() * sizeof(Stream));
   R.flags.ensure(sizeof(int) * 4);
 
@@ -430,13 +562,21 @@ static void generate_gaussians(Context &ctx, std::vector<Stream> &streams, unsig
   k_generate<<<(unsigned)((chunk_total + 127) / 128), 128, 0, cs>>>(dst, ns, chunk_total, R.chunkmul.as<U576>(),
                                                                    R.raw.as<uint32_t>());
   launched();
-  unsigned long long nspec = seg_total * kSpec;
-  k_walk_speculative<<<(unsigned)((nspec + 127) / 128), 128, 0, cs>>>(dst, ns, seg_total, R.raw.as<uint32_t>(),
-                                                                     R.segtab.as<uint2>());
+  unsigned ntiles = (unsigned)((seg_total + kTileSegs - 1) / kTileSegs);
+  k_walk_speculative<<<ntiles, kTileSegs * kSpec, 0, cs>>>(dst, ns, seg_total, R.raw.as<uint32_t>(), raw_total,
+                                                          R.segtab.as<uint32_t>());
   launched();
-  k_resolve<<<(ns + 63) / 64, 64, 0, cs>>>(dst, ns, R.raw.as<uint32_t>(), R.segtab.as<uint2>(),
-                                          R.segentry.as<uint32_t>(), R.segbase.as<unsigned long long>(),
-                                          R.flags.as<int>());
+  unsigned long long nbm = blk_total * kSpec;
+  k_block_maps<<<(unsigned)((nbm + 127) / 128), 128, 0, cs>>>(dst, ns, blk_total, R.raw.as<uint32_t>(),
+                                                             R.segtab.as<uint32_t>(), R.blkmap.as<uint2>());
+  launched();
+  k_chain_blocks<<<(ns + 63) / 64, 64, 0, cs>>>(dst, ns, R.raw.as<uint32_t>(), R.segtab.as<uint32_t>(),
+                                               R.blkmap.as<uint2>(), R.blkentry.as<uint32_t>(),
+                                               R.blkbase.as<unsigned long long>(), R.flags.as<int>());
+  launched();
+  k_chain_segments<<<(unsigned)((blk_total + 127) / 128), 128, 0, cs>>>(
+      dst, ns, blk_total, R.raw.as<uint32_t>(), R.segtab.as<uint32_t>(), R.blkentry.as<uint32_t>(),
+      R.blkbase.as<unsigned long long>(), R.segentry.as<uint32_t>(), R.segbase.as<unsigned long long>());
   launched();
   k_walk_final<<<(unsigned)((seg_total + 127) / 128), 128, 0, cs>>>(
       dst, ns, seg_total, R.raw.as<uint32_t>(), R.segentry.as<uint32_t>(), R.segbase.as<unsigned long long>(),
