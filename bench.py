@@ -26,12 +26,20 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
+    # 512^3 base grid in a 100 Mpc/h box plus a 512^3 zoom of side 25 Mpc/h (factor 4)
+    # centred at (50, 50, 50) Mpc/h: the headline two-level configuration
+    'zoom512': dict(levels=[('base', 100.0, 512), ('zoom', 192, 192, 192, 4, 512)], seed_cmd='random_seed',
+                    precision='mixed', replaced=128 ** 3),
+    'zoom512_fp64': dict(levels=[('base', 100.0, 512), ('zoom', 192, 192, 192, 4, 512)], seed_cmd='random_seed',
+                         precision='fp64', replaced=128 ** 3),
+    'zoom256': dict(levels=[('base', 100.0, 256), ('zoom', 96, 96, 96, 4, 256)], seed_cmd='random_seed',
+                    precision='mixed', replaced=64 ** 3),
     # 512^3 single level, 100 Mpc/h box (the single-level configuration at 512^3)
     'za512': dict(levels=[('base', 100.0, 512)], seed_cmd='random_seed', precision='mixed'),
     'za512_fp64': dict(levels=[('base', 100.0, 512)], seed_cmd='random_seed', precision='fp64'),
     'za256': dict(levels=[('base', 100.0, 256)], seed_cmd='random_seed', precision='mixed'),
 }
-DEFAULT_WORKLOAD = 'za512'
+DEFAULT_WORKLOAD = 'zoom512'
 COSMO = dict(omega_m=0.31, omega_lambda=0.69, omega_b=0.0, hubble=0.68, sigma8=0.81, ns=0.965, redshift=99.0)
 SEED = 8896131
 METRIC = "Mparticles/s, 512³ 2-level Zel'dovich IC: FP32+FP64 vs plain FP64 at ≤1e-5 err"
@@ -76,7 +84,9 @@ def make_gen(wl, table, device):
 
 
 def n_particles(wl):
-    return sum(lev[2] ** 3 if lev[0] == 'base' else lev[5] ** 3 for lev in wl['levels'])
+    """Particles written out: every cell of every level, less the base cells the zoom replaces
+    (genetIC's two-level particle mapper, genetIC/src/simulation/particles/mapper/twolevelmapper.hpp)."""
+    return sum(lev[2] ** 3 if lev[0] == 'base' else lev[5] ** 3 for lev in wl['levels']) - wl.get('replaced', 0)
 
 
 class Clocks:

@@ -287,10 +287,8 @@ int gic_get_normalisation(gic_ctx *ctx, double *amplitude, double *sigma8_unnorm
 int gic_draw_noise(gic_ctx *ctx, unsigned long seed, int mode) {
   API_BEGIN(ctx)
   if (C.levels.empty()) gic::fail(GIC_ERR_NOT_READY, "no grid levels");
-  for (auto &L : C.levels) {
-    gic::draw_noise_level(C, *L, seed, mode);
-    L->have_fields = false;
-  }
+  gic::draw_noise_all(C, seed, mode);
+  for (auto &L : C.levels) L->have_fields = false;
   API_END
 }
 
@@ -314,11 +312,10 @@ int gic_zeldovich(gic_ctx *ctx, int order) {
   API_BEGIN(ctx)
   if (order != 1) gic::fail(GIC_ERR_INVALID_ARG, "only order 1 (Zel'dovich) is available");
   if (C.levels.empty()) gic::fail(GIC_ERR_NOT_READY, "no grid levels");
-  if (C.levels.size() > 1) gic::fail(GIC_ERR_INVALID_ARG, "zoom levels are not supported yet");
-  for (auto &L : C.levels) {
-    gic::za_fields(C, *L);
-    gic::make_particles(C, *L);
-  }
+  int nl = (int)C.levels.size();
+  for (int l = 0; l < nl; ++l) gic::za_fields(C, l);
+  for (int l = 1; l < nl; ++l) gic::zoom_combine(C, l);
+  for (int l = 0; l < nl; ++l) gic::make_particles(C, *C.levels[l]);
   GIC_CUDA(cudaStreamSynchronize(C.stream));
   API_END
 }

@@ -61,6 +61,9 @@ struct Level {
   DevBuf noise;          // white noise (unit variance per real d.o.f.)
   DevBuf field[4];       // delta, psi_x, psi_y, psi_z
   DevBuf sqrtp;          // double sqrt(P_grid) per integer |k|^2
+  DevBuf tab_main;       // sqrt(P_grid), times the high-pass filter on zoom levels
+  DevBuf tab_lp_src;     // sqrt(P_grid) * low-pass (source side of the next zoom)
+  DevBuf tab_lp;         // low-pass filter alone
   DevBuf pos, vel;       // particles: pos double[3M], vel (precision)[3M]
   bool have_noise = false;
   bool have_fields = false;
@@ -107,6 +110,7 @@ struct Context {
   FftTables fft;
   RngScratch rng;
   DevBuf reduce;  // small scratch for reductions
+  DevBuf zoom_scratch[4];  // low-passed coarse fields during zoom combination
   bool dbl() const { return precision == GIC_FP64; }
 };
 
@@ -117,13 +121,14 @@ template <typename T>
 void fft_r2c_3d(Context &ctx, T *data, int n, double scale);
 
 // rng.cu
-void draw_noise_level(Context &ctx, Level &L, unsigned long long seed, int mode);
+void draw_noise_all(Context &ctx, unsigned long long seed, int mode);
 void gaussian_stream(Context &ctx, unsigned long long seed, size_t n, double *host);
 
 // kspace.cu
 void transfer_setup(Context &ctx, const double *table, int nrows, int ncols);
 void build_sqrtp_table(Context &ctx, Level &L);
-void za_fields(Context &ctx, Level &L);
+void za_fields(Context &ctx, int level);
+void zoom_combine(Context &ctx, int level);
 
 // particles.cu
 void make_particles(Context &ctx, Level &L);

@@ -117,7 +117,7 @@ template <> struct V2<double> { using type = double2; };
 // delta = w sqrt(P); psi_i = i k_i delta / k^2, zero at k = 0 and at the
 // positive Nyquist component (zeldovich.hpp:155-181)
 template <typename T>
-__global__ void k_za_fields(const typename V2<T>::type *noise, const double *sqrtp, int n, T kmin,
+__global__ void k_za_fields(const typename V2<T>::type *noise, const double *tab, int n, T kmin,
                             typename V2<T>::type *delta, typename V2<T>::type *px, typename V2<T>::type *py,
                             typename V2<T>::type *pz) {
   using C = typename V2<T>::type;
@@ -132,7 +132,7 @@ __global__ void k_za_fields(const typename V2<T>::type *noise, const double *sqr
   int ky = iy > H ? iy - n : iy;
   int kz = iz;
   long long q = (long long)kx * kx + (long long)ky * ky + (long long)kz * kz;
-  T s = (T)sqrtp[q];
+  T s = (T)tab[q];
   C w = noise[id];
   C d;
   d.x = w.x * s;
@@ -155,6 +155,39 @@ __global__ void k_za_fields(const typename V2<T>::type *noise, const double *sqr
   px[id] = rx;
   py[id] = ry;
   pz[id] = rz;
+}
+
+// Per-|k|^2 tables: out[q] = base[q] * f(sqrt(q) kmin), f = 1, the low-pass Fermi
+// filter 1/(1 + exp((k - kcut)/T)) with T = 0.1 kcut, or the complementary
+// high-pass sqrt(1 - LP^2) (genetIC/src/simulation/filters/filter.hpp:208-275,
+// filterfamily.hpp:106-140 with FRACTIONAL_K_SPLIT = 0.3, FRACTIONAL_FILTER_TEMPERATURE = 0.1).
+__global__ void k_filter_table(double *out, const double *base, long long nq, double kmin, double kcut, int kind) {
+  long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  double f = 1.0;
+  if (kind != 0) {
+    double k = sqrt((double)q) * kmin;
+    double temperature = kcut * 0.1;
+    double lp = 1. / (1. + exp((k - kcut) / temperature));
+    f = kind == 1 ? lp : sqrt(1. - lp * lp);
+  }
+  out[q] = (base ? base[q] : 1.0) * f;
+}
+
+// multiply a half spectrum by tab[|k|^2]
+template <typename T>
+__global__ void k_scale_table(typename V2<T>::type *c, int n, const double *tab) {
+  const int H = n / 2, S = H + 1;
+  size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t nc = (size_t)n * n * S;
+  if (id >= nc) return;
+  int iz = (int)(id % S);
+  size_t r = id / S;
+  int iy = (int)(r % n), ix = (int)(r / n);
+  long long kx = ix > H ? ix - n : ix, ky = iy > H ? iy - n : iy;
+  T s = (T)tab[kx * kx + ky * ky + (long long)iz * iz];
+  c[id].x *= s;
+  c[id].y *= s;
 }
 
 // Carroll, Press & Turner growth-factor fit, as genetIC evaluates it
@@ -251,7 +284,12 @@ void transfer_setup(Context &ctx, const double *table, int nrows, int ncols) {
   T.lnk_min = lx_all.front();
   T.lnk_max = lx_all.back();
   T.ready = true;
-  for (auto &L : ctx.levels) L->sqrtp.release();
+  for (auto &L : ctx.levels) {
+    L->sqrtp.release();
+    L->tab_main.release();
+    L->tab_lp_src.release();
+    L->tab_lp.release();
+  }
 }
 
 void build_sqrtp_table(Context &ctx, Level &L) {
@@ -268,14 +306,46 @@ void build_sqrtp_table(Context &ctx, Level &L) {
   launched();
 }
 
+// k_cut of the filter between level l-1 and l: 0.3 * N_{l-1} * kmin_{l-1}
+static double level_kcut(const Level &coarse) { return 0.3 * ((double)coarse.n * coarse.kmin()); }
+
+// tab_main = sqrt(P) (level 0) or sqrt(P) * HP(k_cut of the level above) (zoom levels)
+static void build_level_tables(Context &ctx, int li) {
+  Level &L = *ctx.levels[li];
+  build_sqrtp_table(ctx, L);
+  if (L.tab_main.ptr) return;
+  long long half = L.n / 2, nq = 3 * half * half + 1;
+  L.tab_main.ensure(nq * sizeof(double));
+  double kcut = li > 0 ? level_kcut(*ctx.levels[li - 1]) : 1.0;
+  k_filter_table<<<(unsigned)((nq + 255) / 256), 256, 0, ctx.stream>>>(L.tab_main.as<double>(), L.sqrtp.as<double>(),
+                                                                       nq, L.kmin(), kcut, li > 0 ? 2 : 0);
+  launched();
+}
+
+// on the coarse level l-1: sqrt(P) * LP and LP alone, for the copy into level l
+static void build_lowpass_tables(Context &ctx, int coarse_index) {
+  Level &C = *ctx.levels[coarse_index];
+  build_sqrtp_table(ctx, C);
+  if (C.tab_lp_src.ptr) return;
+  long long half = C.n / 2, nq = 3 * half * half + 1;
+  C.tab_lp_src.ensure(nq * sizeof(double));
+  C.tab_lp.ensure(nq * sizeof(double));
+  double kcut = level_kcut(C);
+  unsigned blocks = (unsigned)((nq + 255) / 256);
+  k_filter_table<<<blocks, 256, 0, ctx.stream>>>(C.tab_lp_src.as<double>(), C.sqrtp.as<double>(), nq, C.kmin(), kcut, 1);
+  k_filter_table<<<blocks, 256, 0, ctx.stream>>>(C.tab_lp.as<double>(), nullptr, nq, C.kmin(), kcut, 1);
+  launched(2);
+}
+
 template <typename T>
-static void za_fields_typed(Context &ctx, Level &L) {
+static void za_fields_typed(Context &ctx, int li) {
   using C = typename V2<T>::type;
+  Level &L = *ctx.levels[li];
   size_t nc = L.ncomplex();
   for (int f = 0; f < 4; ++f) L.field[f].ensure(nc * sizeof(C));
-  build_sqrtp_table(ctx, L);
+  build_level_tables(ctx, li);
   unsigned blocks = (unsigned)((nc + 255) / 256);
-  k_za_fields<T><<<blocks, 256, 0, ctx.stream>>>(L.noise.as<C>(), L.sqrtp.as<double>(), L.n, (T)L.kmin(),
+  k_za_fields<T><<<blocks, 256, 0, ctx.stream>>>(L.noise.as<C>(), L.tab_main.as<double>(), L.n, (T)L.kmin(),
                                                  L.field[0].as<C>(), L.field[1].as<C>(), L.field[2].as<C>(),
                                                  L.field[3].as<C>());
   launched();
@@ -284,12 +354,56 @@ static void za_fields_typed(Context &ctx, Level &L) {
   L.have_fields = true;
 }
 
-void za_fields(Context &ctx, Level &L) {
+template <typename T>
+void interp_add4(Context &ctx, const Level &coarse, T *const src[4], Level &fine);
+
+// low-passed level li-1 (delta, psi) in real space, interpolated into level li
+template <typename T>
+static void zoom_combine_typed(Context &ctx, int li) {
+  using C = typename V2<T>::type;
+  Level &Cl = *ctx.levels[li - 1];
+  Level &F = *ctx.levels[li];
+  size_t nc = Cl.ncomplex();
+  for (int f = 0; f < 4; ++f) ctx.zoom_scratch[f].ensure(nc * sizeof(C));
+  T *src[4];
+  for (int f = 0; f < 4; ++f) src[f] = ctx.zoom_scratch[f].as<T>();
+  build_lowpass_tables(ctx, li - 1);
+  unsigned blocks = (unsigned)((nc + 255) / 256);
+  double scale = 1.0 / std::pow((double)Cl.n, 1.5);
+  if (li - 1 == 0) {
+    // level 0 is unfiltered: its low-passed fields come straight from its noise
+    k_za_fields<T><<<blocks, 256, 0, ctx.stream>>>(Cl.noise.as<C>(), Cl.tab_lp_src.as<double>(), Cl.n, (T)Cl.kmin(),
+                                                   reinterpret_cast<C *>(src[0]), reinterpret_cast<C *>(src[1]),
+                                                   reinterpret_cast<C *>(src[2]), reinterpret_cast<C *>(src[3]));
+    launched();
+  } else {
+    // the combined real fields of level li-1, back to Fourier space, low-passed
+    for (int f = 0; f < 4; ++f) {
+      GIC_CUDA(cudaMemcpyAsync(src[f], Cl.field[f].ptr, nc * sizeof(C), cudaMemcpyDeviceToDevice, ctx.stream));
+      fft_r2c_3d<T>(ctx, src[f], Cl.n, scale);
+      k_scale_table<T><<<blocks, 256, 0, ctx.stream>>>(reinterpret_cast<C *>(src[f]), Cl.n, Cl.tab_lp.as<double>());
+      launched();
+    }
+  }
+  for (int f = 0; f < 4; ++f) fft_c2r_3d<T>(ctx, src[f], Cl.n, scale);
+  interp_add4<T>(ctx, Cl, src, F);
+}
+
+void za_fields(Context &ctx, int li) {
+  Level &L = *ctx.levels[li];
   if (!L.have_noise) fail(GIC_ERR_NOT_READY, "white noise has not been drawn");
   if (ctx.dbl())
-    za_fields_typed<double>(ctx, L);
+    za_fields_typed<double>(ctx, li);
   else
-    za_fields_typed<float>(ctx, L);
+    za_fields_typed<float>(ctx, li);
+}
+
+void zoom_combine(Context &ctx, int li) {
+  if (li < 1) return;
+  if (ctx.dbl())
+    zoom_combine_typed<double>(ctx, li);
+  else
+    zoom_combine_typed<float>(ctx, li);
 }
 
 }  // namespace gic

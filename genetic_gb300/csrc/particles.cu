@@ -13,7 +13,13 @@
 namespace gic {
 namespace {
 
+// fmod(x, period) then + period if negative, as grid.hpp:527-531; for
+// -period < x < 2 period this equals the branch below exactly (x - period is
+// exact there), which avoids a double-precision remainder per coordinate.
 __device__ __forceinline__ double wrap_coord(double x, double period) {
+  if (x >= period && x < 2 * period) return x - period;
+  if (x < 0 && x > -period) return x + period;
+  if (x >= 0 && x < period) return x;
   x = fmod(x, period);
   if (x < 0) x += period;
   return x;

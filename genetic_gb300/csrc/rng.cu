@@ -591,62 +591,75 @@ static void generate_gaussians(Context &ctx, std::vector<Stream> &streams, unsig
   }
 }
 
+// Place this level's gaussians (device pointer) on its half spectrum.
 template <typename T>
-static void draw_level_typed(Context &ctx, Level &L, unsigned long long seed, int mode) {
+static void place_level(Context &ctx, Level &L, const double *gauss, int mode) {
   cudaStream_t cs = ctx.stream;
   int n = L.n;
   size_t nc = L.ncomplex();
   L.noise.ensure(nc * 2 * sizeof(T));
   T *out = L.noise.as<T>();
-  std::vector<Stream> streams;
+  GIC_CUDA(cudaMemsetAsync(out, 0, nc * 2 * sizeof(T), cs));
   if (mode == GIC_SEED_REAL_SPACE) {
     unsigned long long m = L.ncells();
-    Stream s{};
-    s.seed = seed;
-    s.gauss_off = 0;
-    s.gauss_count = m;
-    streams.push_back(s);
-    generate_gaussians(ctx, streams, m, 1.0);
-    GIC_CUDA(cudaMemsetAsync(out, 0, nc * 2 * sizeof(T), cs));
-    k_place_real<T><<<(unsigned)((m + 255) / 256), 256, 0, cs>>>(n, ctx.rng.gauss.as<double>(), out);
+    k_place_real<T><<<(unsigned)((m + 255) / 256), 256, 0, cs>>>(n, gauss, out);
     launched();
     fft_r2c_3d<T>(ctx, out, n, 1.0 / std::pow((double)n, 1.5));
     k_zero_first<T><<<1, 1, 0, cs>>>(out);
     launched();
   } else {
-    int half = n / 2;
-    unsigned long long nmodes = shell_offset(half);
-    if (mode == GIC_SEED_FOURIER_PARALLEL) {
-      for (int ks = 1; ks < half; ++ks) {
-        Stream s{};
-        s.seed = seed + (unsigned long long)ks;
-        s.gauss_off = 2 * shell_offset(ks);
-        s.gauss_count = 2 * (shell_offset(ks + 1) - shell_offset(ks));
-        streams.push_back(s);
-      }
-    } else {
-      Stream s{};
-      s.seed = seed;
-      s.gauss_off = 0;
-      s.gauss_count = 2 * nmodes;
-      streams.push_back(s);
-    }
-    GIC_CUDA(cudaMemsetAsync(out, 0, nc * 2 * sizeof(T), cs));
+    unsigned long long nmodes = shell_offset(n / 2);
     if (nmodes > 0) {
-      generate_gaussians(ctx, streams, 2 * nmodes, 1.0);
       ctx.rng.owner.ensure(nc * sizeof(int));
       GIC_CUDA(cudaMemsetAsync(ctx.rng.owner.ptr, 0xFF, nc * sizeof(int), cs));
       unsigned blocks = (unsigned)((nmodes + 255) / 256);
       k_place_owner<<<blocks, 256, 0, cs>>>(n, nmodes, ctx.rng.owner.as<int>());
       launched();
       T norm = (T)(1.0 / std::sqrt(2.0));
-      k_place_write<T><<<blocks, 256, 0, cs>>>(n, nmodes, ctx.rng.owner.as<int>(), ctx.rng.gauss.as<double>(),
-                                               norm, mode == GIC_SEED_FOURIER_REVERSE ? 1 : 0, out);
+      k_place_write<T><<<blocks, 256, 0, cs>>>(n, nmodes, ctx.rng.owner.as<int>(), gauss, norm,
+                                               mode == GIC_SEED_FOURIER_REVERSE ? 1 : 0, out);
       launched();
     }
   }
-  GIC_CUDA(cudaStreamSynchronize(cs));
   L.have_noise = true;
+}
+
+// genetIC draws level after level (randomfieldgenerator.hpp:122-139): the
+// serial and real-space modes keep consuming one stream across levels, the
+// parallel mode reseeds every shell with seed + ks on every level, so all
+// levels share the shell streams of the largest one.
+template <typename T>
+static void draw_all_typed(Context &ctx, unsigned long long seed, int mode) {
+  std::vector<Stream> streams;
+  std::vector<unsigned long long> offset(ctx.levels.size(), 0);
+  if (mode == GIC_SEED_FOURIER_PARALLEL) {
+    int half = 0;
+    for (auto &L : ctx.levels) half = std::max(half, L->n / 2);
+    for (int ks = 1; ks < half; ++ks) {
+      Stream s{};
+      s.seed = seed + (unsigned long long)ks;
+      s.gauss_off = 2 * shell_offset(ks);
+      s.gauss_count = 2 * (shell_offset(ks + 1) - shell_offset(ks));
+      streams.push_back(s);
+    }
+    if (!streams.empty()) generate_gaussians(ctx, streams, 2 * shell_offset(half), 1.0);
+  } else {
+    unsigned long long total = 0;
+    for (size_t l = 0; l < ctx.levels.size(); ++l) {
+      offset[l] = total;
+      const Level &L = *ctx.levels[l];
+      total += mode == GIC_SEED_REAL_SPACE ? (unsigned long long)L.ncells() : 2 * shell_offset(L.n / 2);
+    }
+    Stream s{};
+    s.seed = seed;
+    s.gauss_off = 0;
+    s.gauss_count = total;
+    streams.push_back(s);
+    if (total > 0) generate_gaussians(ctx, streams, total, 1.0);
+  }
+  for (size_t l = 0; l < ctx.levels.size(); ++l)
+    place_level<T>(ctx, *ctx.levels[l], ctx.rng.gauss.as<double>() + offset[l], mode);
+  GIC_CUDA(cudaStreamSynchronize(ctx.stream));
 }
 
 void gaussian_stream(Context &ctx, unsigned long long seed, size_t n, double *host) {
@@ -659,14 +672,15 @@ void gaussian_stream(Context &ctx, unsigned long long seed, size_t n, double *ho
   GIC_CUDA(cudaStreamSynchronize(ctx.stream));
 }
 
-void draw_noise_level(Context &ctx, Level &L, unsigned long long seed, int mode) {
+void draw_noise_all(Context &ctx, unsigned long long seed, int mode) {
   if (mode < 0 || mode > 3) fail(GIC_ERR_INVALID_ARG, "unknown seeding mode");
-  if ((long long)L.n * L.n * (L.n / 2 + 1) >= (1ll << 31))
-    fail(GIC_ERR_INVALID_ARG, "grid too large for 32-bit mode indices");
+  for (auto &L : ctx.levels)
+    if ((long long)L->n * L->n * (L->n / 2 + 1) >= (1ll << 31))
+      fail(GIC_ERR_INVALID_ARG, "grid too large for 32-bit mode indices");
   if (ctx.dbl())
-    draw_level_typed<double>(ctx, L, seed, mode);
+    draw_all_typed<double>(ctx, seed, mode);
   else
-    draw_level_typed<float>(ctx, L, seed, mode);
+    draw_all_typed<float>(ctx, seed, mode);
 }
 
 }  // namespace gic

@@ -36,6 +36,8 @@ def lib():
         L.oracle_gaussian_stream.restype = ctypes.c_uint64
         L.oracle_ranlux_stream.argtypes = [ctypes.c_ulong, ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint64]
         L.oracle_rng_set_cr_log.argtypes = [ctypes.c_int]
+        L.oracle_draw_white_noise_levels.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_ulong,
+                                                     ctypes.c_int, ctypes.POINTER(ctypes.POINTER(ctypes.c_double))]
         _lib = L
     return _lib
 
@@ -84,7 +86,7 @@ def mirror(c):
 def fft_c2r(c):
     """Unitary inverse transform of a half spectrum, N^-1.5, after mirroring."""
     n = c.shape[0]
-    return np.fft.irfftn(mirror(c), s=(n, n, n)) * n ** 1.5
+    return np.fft.irfftn(mirror(c), s=(n, n, n), axes=(0, 1, 2)) * n ** 1.5
 
 
 def white_noise(n, seed, mode):
@@ -100,6 +102,27 @@ def white_noise(n, seed, mode):
     assert rc == 0
     out = out.reshape(n, n, n // 2 + 1, 2)
     return out[..., 0] + 1j * out[..., 1]
+
+
+def white_noise_levels(ns, seed, mode):
+    """Half spectra of every level, drawn in genetIC's level order."""
+    bufs = []
+    for n in ns:
+        size = n ** 3 if mode == 0 else n * n * (n // 2 + 1) * 2
+        bufs.append(np.empty(size, dtype=np.float64))
+    arr = (ctypes.POINTER(ctypes.c_double) * len(ns))(*[b.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for b in bufs])
+    nn = (ctypes.c_int * len(ns))(*ns)
+    assert lib().oracle_draw_white_noise_levels(len(ns), nn, int(seed), int(mode), arr) == 0
+    out = []
+    for n, b in zip(ns, bufs):
+        if mode == 0:
+            c = fft_r2c(b.reshape(n, n, n))
+            c[0, 0, 0] = 0.0 + 1j * c[0, 0, 0].imag
+        else:
+            b = b.reshape(n, n, n // 2 + 1, 2)
+            c = b[..., 0] + 1j * b[..., 1]
+        out.append(c)
+    return out
 
 
 def chi2(noise):
@@ -277,3 +300,93 @@ def particles(psi, box, offset, periodic, ratio):
     pos = np.where(pos < 0, pos + periodic, pos)
     vel = np.stack([p * ratio for p in psi], axis=-1).reshape(-1, 3)
     return pos, vel
+
+
+# --- zoom levels (multilevelgenerator.hpp:78-128, field.hpp:816-831, filter.hpp) ----
+
+def fermi_lowpass(k, kcut):
+    """LowPassFermiFilter (filter.hpp:208-239), temperature 0.1 k_cut."""
+    return 1. / (1. + np.exp((k - kcut) / (kcut * 0.1)))
+
+
+def kmag(n, box):
+    ki, kz, kmin = kgrid(n, box)
+    kx = (ki * kmin)[:, None, None]
+    ky = (ki * kmin)[None, :, None]
+    kzz = (kz * kmin)[None, None, :]
+    return np.sqrt(kx * kx + ky * ky + kzz * kzz)
+
+
+def displacement_spectra(delta_k, box):
+    """psi_k = i k delta_k / k^2 with the Nyquist and k = 0 zeroing (zeldovich.hpp:155-181)."""
+    n = delta_k.shape[0]
+    ki, kz, kmin = kgrid(n, box)
+    kx = (ki * kmin)[:, None, None]
+    ky = (ki * kmin)[None, :, None]
+    kzz = (kz * kmin)[None, None, :]
+    kk = kx * kx + ky * ky + kzz * kzz
+    with np.errstate(divide='ignore', invalid='ignore'):
+        base = 1j * delta_k / kk
+    base[0, 0, 0] = 0
+    out = []
+    for kc, ic in ((kx, ki[:, None, None]), (ky, ki[None, :, None]), (kzz, kz[None, None, :])):
+        p = np.where(ic == n // 2, 0.0, base * kc)
+        p[0, 0, 0] = 0
+        out.append(p)
+    return out
+
+
+def catmull_rom_weights(t):
+    t2, t3 = t * t, t * t * t
+    return np.stack([-(t - 1) ** 2 * t / 2, (2 - 5 * t2 + 3 * t3) / 2, t * (1 + 4 * t - 3 * t2) / 2,
+                     (t - 1) * t2 / 2], axis=-1)
+
+
+def interpolate_to(coarse, cbox, coffset, periodic, fbox, fn, foffset):
+    """Tricubic (Catmull-Rom tensor product) values of a coarse real field at the
+    centroids of the fine grid's cells (field.hpp:483-509, 598-617): wrap on the
+    periodic base grid, clamp on a zoom grid."""
+    nc = coarse.shape[0]
+    dxc, dxf = cbox / nc, fbox / fn
+    wrap = cbox == periodic
+    idx, wts = [], []
+    for a in range(3):
+        loc = np.arange(fn) * dxf + foffset[a] + dxf / 2 - coffset[a]
+        loc = np.fmod(loc, periodic)
+        loc = np.where(loc < 0, loc + periodic, loc)
+        u = loc / dxc - 0.5
+        i0 = np.floor(u)
+        w = catmull_rom_weights(u - i0)
+        ii = i0.astype(int)[:, None] + np.arange(-1, 3)[None, :]
+        ii = ii % nc if wrap else np.clip(ii, 0, nc - 1)
+        idx.append(ii)
+        wts.append(w)
+    g = np.einsum('xa,xayz->xyz', wts[0], coarse[idx[0]])
+    g = np.einsum('yb,xybz->xyz', wts[1], g[:, idx[1]])
+    g = np.einsum('zc,xyzc->xyz', wts[2], g[:, :, idx[2]])
+    return g
+
+
+def zoom_realisation(noises, levels, power):
+    """Real-space delta, psi_x, psi_y, psi_z of every level after combination.
+    levels: [(box, n, (x0, y0, z0))], level 0 periodic."""
+    periodic = levels[0][0]
+    raw_k = []  # per level: unfiltered delta_k
+    out = []
+    for (box, n, off), w in zip(levels, noises):
+        raw_k.append(w * sqrt_power_grid(power, n, box))
+    for li, ((box, n, off), dk) in enumerate(zip(levels, raw_k)):
+        specs = [dk] + displacement_spectra(dk, box)
+        if li > 0:
+            cbox, cn, coff = levels[li - 1]
+            kcut = 0.3 * (cn * 2. * np.pi / cbox)
+            hp = np.sqrt(1. - fermi_lowpass(kmag(n, box), kcut) ** 2)
+            specs = [s * hp for s in specs]
+        fields = [fft_c2r(s) for s in specs]
+        if li > 0:
+            lp = fermi_lowpass(kmag(cn, cbox), kcut)
+            src = [fft_r2c(f) * lp for f in out[li - 1]]
+            for f, s in zip(fields, src):
+                f += interpolate_to(fft_c2r(s), cbox, coff, periodic, box, n, off)
+        out.append(fields)
+    return out

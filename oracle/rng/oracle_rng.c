@@ -158,6 +158,33 @@ static void draw_shell(double *f, int n, int ks, double norm, oracle_ranlux *r, 
     }
 }
 
+/* Several levels, as RandomFieldGenerator::draw loops over them
+ * (randomfieldgenerator.hpp:122-139): real-space and serial Fourier modes keep
+ * drawing from one stream, the parallel mode reseeds each shell on each level. */
+int oracle_draw_white_noise_levels(int nlev, const int *ns, unsigned long seed, int mode, double **outs) {
+  oracle_ranlux r;
+  const double norm = 1.0 / sqrt(2.0);
+  if (mode == 2) {
+    for (int l = 0; l < nlev; ++l)
+      if (oracle_draw_white_noise(ns[l], seed, 2, outs[l])) return -1;
+    return 0;
+  }
+  oracle_ranlux_seed(&r, seed, 397);
+  for (int l = 0; l < nlev; ++l) {
+    int n = ns[l];
+    if (mode == 0) {
+      size_t m = (size_t)n * n * n;
+      for (size_t i = 0; i < m; ++i) outs[l][i] = oracle_gaussian_ziggurat(&r);
+    } else if (mode == 1 || mode == 3) {
+      memset(outs[l], 0, 2 * (size_t)n * n * (n / 2 + 1) * sizeof(double));
+      for (int ks = 0; ks < n / 2; ++ks) draw_shell(outs[l], n, ks, norm, &r, mode == 3);
+    } else {
+      return -1;
+    }
+  }
+  return 0;
+}
+
 int oracle_draw_white_noise(int n, unsigned long seed, int mode, double *out) {
   if (n <= 0) return -1;
   oracle_ranlux r;

@@ -54,6 +54,10 @@ uint64_t oracle_gaussian_stream(unsigned long seed, double *out, uint64_t n);
  * 3 = Fourier serial with swapped (re,im) (`seedfourier_reverse`).
  * Returns 0 on success. */
 int oracle_draw_white_noise(int n, unsigned long seed, int mode, double *out);
+/* The same for nlev levels of sizes ns[] (real-space mode: outs[l] receives
+ * ns[l]^3 gaussians; Fourier modes: half spectra), continuing one stream across
+ * levels where genetIC does. */
+int oracle_draw_white_noise_levels(int nlev, const int *ns, unsigned long seed, int mode, double **outs);
 
 #ifdef __cplusplus
 }

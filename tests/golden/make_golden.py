@@ -40,6 +40,51 @@ dump_grid 0
 """
 
 
+ZOOM_PARAMS = """Om 0.31
+Ol 0.69
+Ob 0
+hubble 0.68
+s8 0.81
+ns 0.965
+zin 99
+{seedcmd} 8896131
+camb bbks.dat
+outname out
+outdir ./
+outformat tipsy
+basegrid 50.0 32
+centre 25 25 25
+select_cube 10
+{zooms}
+done
+{dumps}
+"""
+ZOOMS = {
+    # two levels: a 25 Mpc/h zoom (factor 2) at coarse cell (8, 8, 8) around the
+    # flagged 10 Mpc/h cube at the box centre
+    'zoom2': ['zoom_grid_with_origin_at 8 8 8 2 32'],
+    # three levels: a further factor-2 zoom inside the first
+    'zoom3': ['zoom_grid_with_origin_at 8 8 8 2 32', 'zoom_grid_with_origin_at 8 8 8 2 32'],
+}
+
+
+def zoom_goldens():
+    for name, zooms in ZOOMS.items():
+        for mode, cmd in (('parallel', 'random_seed'), ('real', 'random_seed_real_space')):
+            if name == 'zoom3' and mode == 'real':
+                continue
+            with tempfile.TemporaryDirectory() as d:
+                write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+                dumps = '\n'.join('dump_grid %d' % l for l in range(len(zooms) + 1))
+                open(os.path.join(d, 'paramfile.txt'), 'w').write(
+                    ZOOM_PARAMS.format(seedcmd=cmd, zooms='\n'.join(zooms), dumps=dumps))
+                subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True)
+                grids = {'delta%d' % l: np.load(os.path.join(d, 'grid-%d.npy' % l)) for l in range(len(zooms) + 1)}
+                if name == 'zoom3':
+                    grids = {k: v.astype(np.float32) for k, v in grids.items()}
+                np.savez_compressed(os.path.join(HERE, '%s_%s.npz' % (name, mode)), **grids)
+
+
 def main():
     for mode, cmd in (('serial', 'random_seed_serial'), ('parallel', 'random_seed'), ('real', 'random_seed_real_space')):
         with tempfile.TemporaryDirectory() as d:
@@ -57,3 +102,4 @@ def main():
 
 if __name__ == '__main__':
     main()
+    zoom_goldens()

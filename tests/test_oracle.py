@@ -104,3 +104,23 @@ def test_reference_build_grid_fixture(tmp_path):
     d, _ = _run_reference(tmp_path, 'test_01c_zoom_grid')
     for g in ('grid-0.npy', 'grid-1.npy'):
         np.testing.assert_almost_equal(np.load(d / g), np.load(d / 'reference_grid' / g), decimal=4)
+
+
+ZOOM_LEVELS = {
+    'zoom2': [(50.0, 32, (0.0, 0.0, 0.0)), (25.0, 32, (12.5, 12.5, 12.5))],
+    'zoom3': [(50.0, 32, (0.0, 0.0, 0.0)), (25.0, 32, (12.5, 12.5, 12.5)), (12.5, 32, (18.75, 18.75, 18.75))],
+}
+
+
+@pytest.mark.parametrize('name,mode,tol', [('zoom2', 'parallel', 1e-12), ('zoom2', 'real', 1e-12),
+                                           ('zoom3', 'parallel', 2e-7)])
+def test_zoom_oracle_matches_reference_grids(bbks, name, mode, tol):
+    from conftest import COSMO
+    g = _load_golden('%s_%s.npz' % (name, mode))
+    levels = ZOOM_LEVELS[name]
+    fo.set_cr_log(False)
+    w = fo.white_noise_levels([l[1] for l in levels], 8896131, {'parallel': 2, 'real': 0}[mode])
+    out = fo.zoom_realisation(w, levels, fo.CambPower(bbks, COSMO))
+    for l in range(len(levels)):
+        ref = g['delta%d' % l]
+        assert np.abs(out[l][0] - ref).max() <= tol * np.abs(ref).max(), l
