@@ -111,6 +111,7 @@ struct Context {
   RngScratch rng;
   DevBuf reduce;  // small scratch for reductions
   DevBuf zoom_scratch[4];  // low-passed coarse fields during zoom combination
+  DevBuf geom;             // per-axis interpolation / centroid tables
   bool dbl() const { return precision == GIC_FP64; }
 };
 

@@ -25,9 +25,19 @@ __device__ __forceinline__ double wrap_coord(double x, double period) {
   return x;
 }
 
+// cell centroids along one axis: coord * dx + offset + dx / 2 (grid.hpp:659-669)
+__global__ void k_centroids(int n, double dx, double x0, double y0, double z0, double *c) {
+  int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= 3 * n) return;
+  int a = id / n, i = id % n;
+  double o = a == 0 ? x0 : (a == 1 ? y0 : z0);
+  c[id] = (double)i * dx + o + dx / 2;
+}
+
 template <typename T>
-__global__ void k_particles(const T *px, const T *py, const T *pz, int n, double dx, double x0, double y0,
-                            double z0, double period, T ratio, double *pos, T *vel) {
+__global__ void __launch_bounds__(256) k_particles(const T *__restrict__ px, const T *__restrict__ py,
+                                                   const T *__restrict__ pz, int n, const double *__restrict__ cen,
+                                                   double period, T ratio, double *pos, T *vel) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   size_t m = (size_t)n * n * n;
   if (i >= m) return;
@@ -40,13 +50,9 @@ __global__ void k_particles(const T *px, const T *py, const T *pz, int n, double
   vel[3 * i + 0] = sx * ratio;
   vel[3 * i + 1] = sy * ratio;
   vel[3 * i + 2] = sz * ratio;
-  // centroid = coord * dx + offset + dx/2
-  double cx = (double)x * dx + x0 + dx / 2;
-  double cy = (double)y * dx + y0 + dx / 2;
-  double cz = (double)z * dx + z0 + dx / 2;
-  pos[3 * i + 0] = wrap_coord((double)sx + cx, period);
-  pos[3 * i + 1] = wrap_coord((double)sy + cy, period);
-  pos[3 * i + 2] = wrap_coord((double)sz + cz, period);
+  pos[3 * i + 0] = wrap_coord((double)sx + __ldg(cen + x), period);
+  pos[3 * i + 1] = wrap_coord((double)sy + __ldg(cen + n + y), period);
+  pos[3 * i + 2] = wrap_coord((double)sz + __ldg(cen + 2 * n + z), period);
 }
 
 }  // namespace
@@ -62,10 +68,13 @@ static void particles_typed(Context &ctx, Level &L) {
   L.pos.ensure(3 * m * sizeof(double));
   L.vel.ensure(3 * m * sizeof(T));
   T ratio = (T)velocity_to_offset_ratio(ctx.cosmo);
+  ctx.geom.ensure(3 * (size_t)L.n * sizeof(double));
+  double *cen = ctx.geom.as<double>();
+  k_centroids<<<(3 * L.n + 127) / 128, 128, 0, ctx.stream>>>(L.n, L.dx, L.x0[0], L.x0[1], L.x0[2], cen);
   k_particles<T><<<(unsigned)((m + 255) / 256), 256, 0, ctx.stream>>>(
-      L.field[1].as<T>(), L.field[2].as<T>(), L.field[3].as<T>(), L.n, L.dx, L.x0[0], L.x0[1], L.x0[2], L.periodic,
-      ratio, L.pos.as<double>(), L.vel.as<T>());
-  launched();
+      L.field[1].as<T>(), L.field[2].as<T>(), L.field[3].as<T>(), L.n, cen, L.periodic, ratio, L.pos.as<double>(),
+      L.vel.as<T>());
+  launched(2);
 }
 
 void make_particles(Context &ctx, Level &L) {

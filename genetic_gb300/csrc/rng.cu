@@ -35,9 +35,28 @@ constexpr int kOverhang = 256;     // numbers staged past the tile end
 constexpr int kBlockSegs = 64;     // segments per block of the two-level chain
 constexpr uint32_t kUnderrun = 0xFFFFFFFFu;
 
-__constant__ double dZigY[128] = GIC_ZIG_Y_INIT;
-__constant__ double dZigW[128] = GIC_ZIG_W_INIT;
-__constant__ unsigned int dZigK[128] = GIC_ZIG_K_INIT;
+// Ziggurat tables: doubles for the values, floats for the slow-path decision,
+// copied into shared memory by the kernels that walk the stream.
+struct ZigTab {
+  unsigned int K[128];
+  float Wf[128], Yf[129];
+  double W[128], Y[129];
+};
+__device__ const ZigTab gZig = {GIC_ZIG_K_INIT, {}, {}, GIC_ZIG_W_INIT, GIC_ZIG_Y_INIT};
+
+__device__ __forceinline__ void load_zig(ZigTab &t) {
+  for (int i = threadIdx.x; i < 128; i += blockDim.x) {
+    t.K[i] = gZig.K[i];
+    t.W[i] = gZig.W[i];
+    t.Y[i] = gZig.Y[i];
+    t.Wf[i] = (float)gZig.W[i];
+    t.Yf[i] = (float)gZig.Y[i];
+  }
+  if (threadIdx.x == 0) {
+    t.Y[128] = 0.0;
+    t.Yf[128] = 0.0f;
+  }
+}
 
 struct Stream {
   unsigned long long seed;
@@ -172,40 +191,73 @@ struct Reader {
 
 // Advance p past one gaussian of the stream ending at `end`; optionally return
 // its value.  Returns false when the stream runs out.
+//
+// The accept/reject test of a slow-path attempt is first made in single
+// precision with a relative margin of 1e-4: the float evaluation of y and
+// exp(-x^2/2) is within a few 1e-6 of the double one (x <= 8.3, tables rounded
+// once), so a decision outside the margin is the double-precision decision.
+// Only attempts inside the margin are evaluated in double.  Values are always
+// computed in double.
 template <bool VALUE>
-__device__ __forceinline__ bool zig_gaussian(const Reader &rd, unsigned long long end, unsigned long long &p,
-                                             double &g) {
+__device__ __forceinline__ bool zig_gaussian(const ZigTab &T, const Reader &rd, unsigned long long end,
+                                             unsigned long long &p, double &g) {
   const double R = GIC_ZIG_PARAM_R;
+  const float Rf = (float)GIC_ZIG_PARAM_R;
   for (int guard = 0; guard < 1 << 20; ++guard) {
     if (p + 2 > end) return false;
     uint32_t k1 = rd(p), k2 = rd(p + 1);
     unsigned i = k1 & 0xFFu;
     uint32_t j = k2 & 0xFFFFFFu;
     unsigned il = i & 0x7Fu;
-    if (j < dZigK[il]) {
-      if (VALUE) g = __dmul_rn((i & 0x80u) ? 1.0 : -1.0, __dmul_rn((double)j, dZigW[il]));
+    unsigned long long neg = (i & 0x80u) ? 0ull : 0x8000000000000000ull;
+    if (j < T.K[il]) {
+      if (VALUE) g = __longlong_as_double(__double_as_longlong(__dmul_rn((double)j, T.W[il])) ^ neg);
       p += 2;
       return true;
     }
-    double x = __dmul_rn((double)j, dZigW[il]);
-    double y;
+    int accept;
+    float xf = (float)j * T.Wf[il];
     if (il < 127) {
       if (p + 3 > end) return false;
-      double u1 = __dmul_rn((double)rd(p + 2), 1.0 / 16777216.0);
-      y = __dadd_rn(dZigY[il + 1], __dmul_rn(__dsub_rn(dZigY[il], dZigY[il + 1]), u1));
+      uint32_t r2 = rd(p + 2);
+      float yf = T.Yf[il + 1] + (T.Yf[il] - T.Yf[il + 1]) * ((float)r2 * (1.0f / 16777216.0f));
+      float ef = expf(-0.5f * xf * xf);
+      accept = yf < ef * (1.0f - 1e-4f) ? 1 : (yf > ef * (1.0f + 1e-4f) ? 0 : -1);
+      if (accept < 0) {
+        double x = __dmul_rn((double)j, T.W[il]);
+        double u1 = __dmul_rn((double)r2, 1.0 / 16777216.0);
+        double y = __dadd_rn(T.Y[il + 1], __dmul_rn(__dsub_rn(T.Y[il], T.Y[il + 1]), u1));
+        accept = y < exp(__dmul_rn(__dmul_rn(-0.5, x), x)) ? 1 : 0;
+      }
       p += 3;
+      if (accept) {
+        if (VALUE) g = __longlong_as_double(__double_as_longlong(__dmul_rn((double)j, T.W[il])) ^ neg);
+        return true;
+      }
     } else {
       if (p + 4 > end) return false;
-      uint32_t kk = rd(p + 2);
-      double u2 = __dmul_rn((double)rd(p + 3), 1.0 / 16777216.0);
-      double lg = gic_log_k24(16777216u - kk);  // log(1 - kk/2^24), correctly rounded
-      x = __dsub_rn(R, __ddiv_rn(lg, R));
-      y = __dmul_rn(exp(__dmul_rn(-R, __dsub_rn(x, __dmul_rn(0.5, R)))), u2);
+      uint32_t kk = rd(p + 2), r3 = rd(p + 3);
+      float u1f = (float)(16777216u - kk) * (1.0f / 16777216.0f);
+      float u2f = (float)r3 * (1.0f / 16777216.0f);
+      float xt = Rf - logf(u1f) / Rf;
+      float yf = expf(-Rf * (xt - 0.5f * Rf)) * u2f;
+      float ef = expf(-0.5f * xt * xt);
+      accept = yf < ef * (1.0f - 1e-4f) ? 1 : (yf > ef * (1.0f + 1e-4f) ? 0 : -1);
+      double x = 0;
+      if (accept < 0 || (VALUE && accept > 0)) {
+        double lg = gic_log_k24(16777216u - kk);  // log(1 - kk/2^24), correctly rounded
+        x = __dsub_rn(R, __ddiv_rn(lg, R));
+      }
+      if (accept < 0) {
+        double u2 = __dmul_rn((double)r3, 1.0 / 16777216.0);
+        double y = __dmul_rn(exp(__dmul_rn(-R, __dsub_rn(x, __dmul_rn(0.5, R)))), u2);
+        accept = y < exp(__dmul_rn(__dmul_rn(-0.5, x), x)) ? 1 : 0;
+      }
       p += 4;
-    }
-    if (y < exp(__dmul_rn(__dmul_rn(-0.5, x), x))) {
-      if (VALUE) g = __dmul_rn((i & 0x80u) ? 1.0 : -1.0, x);
-      return true;
+      if (accept) {
+        if (VALUE) g = __longlong_as_double(__double_as_longlong(x) ^ neg);
+        return true;
+      }
     }
   }
   return false;
@@ -214,7 +266,7 @@ __device__ __forceinline__ bool zig_gaussian(const Reader &rd, unsigned long lon
 // Walk [seg_start, seg_end) from seg_start + entry, counting gaussians that
 // start in the segment; exit = position after the last one minus seg_end.
 template <bool VALUE>
-__device__ void walk_segment(const Reader &rd, unsigned long long stream_end, unsigned long long seg_start,
+__device__ void walk_segment(const ZigTab &T, const Reader &rd, unsigned long long stream_end, unsigned long long seg_start,
                              unsigned long long seg_end, unsigned entry, uint32_t &count, uint32_t &exit_off,
                              double *out, unsigned long long out_limit) {
   unsigned long long p = seg_start + entry;
@@ -222,7 +274,7 @@ __device__ void walk_segment(const Reader &rd, unsigned long long stream_end, un
   while (p < seg_end) {
     if (VALUE && cnt >= out_limit) break;
     double g = 0;
-    if (!zig_gaussian<VALUE>(rd, stream_end, p, g)) {
+    if (!zig_gaussian<VALUE>(T, rd, stream_end, p, g)) {
       count = cnt;
       exit_off = kUnderrun;
       return;
@@ -256,8 +308,10 @@ __global__ void __launch_bounds__(kTileSegs * kSpec) k_walk_speculative(const St
                                                                        unsigned long long raw_total,
                                                                        uint32_t *tab) {
   __shared__ uint32_t sm[kTileSegs * kSegLen + kOverhang];
+  __shared__ ZigTab zt;
   unsigned long long g0 = (unsigned long long)blockIdx.x * kTileSegs;
   if (g0 >= nseg_total) return;
+  load_zig(zt);
   // tile range in absolute stream positions
   int s0 = find_stream_by_segment(st, nstreams, g0);
   unsigned long long lo = st[s0].raw_off + (g0 - st[s0].seg_off) * kSegLen;
@@ -273,7 +327,7 @@ __global__ void __launch_bounds__(kTileSegs * kSpec) k_walk_speculative(const St
   segment_bounds(st[s], gseg - st[s].seg_off, a, b);
   Reader rd{raw, sm, lo, hi};
   uint32_t cnt = 0, ex = 0;
-  walk_segment<false>(rd, st[s].raw_off + st[s].raw_count, a, b, e, cnt, ex, nullptr, 0);
+  walk_segment<false>(zt, rd, st[s].raw_off + st[s].raw_count, a, b, e, cnt, ex, nullptr, 0);
   tab[gseg * kSpec + e] = pack_ce(cnt, ex);
 }
 
@@ -290,7 +344,7 @@ __device__ __forceinline__ void step_segment(const Stream &s, const uint32_t *ra
   unsigned long long a, b;
   segment_bounds(s, gseg - s.seg_off, a, b);
   Reader rd{raw, raw, 0, 0};
-  walk_segment<false>(rd, s.raw_off + s.raw_count, a, b, e, cnt, ex, nullptr, 0);
+  walk_segment<false>(gZig, rd, s.raw_off + s.raw_count, a, b, e, cnt, ex, nullptr, 0);
 }
 
 // Level 1: map of each block of kBlockSegs segments for every entry offset.
@@ -385,6 +439,9 @@ __global__ void k_chain_segments(const Stream *st, int nstreams, unsigned long l
 __global__ void k_walk_final(const Stream *st, int nstreams, unsigned long long nseg_total, const uint32_t *raw,
                              const uint32_t *seg_entry, const unsigned long long *seg_base, double *gauss,
                              int *flags) {
+  __shared__ ZigTab zt;
+  load_zig(zt);
+  __syncthreads();
   unsigned long long gseg = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (gseg >= nseg_total) return;
   int s = find_stream_by_segment(st, nstreams, gseg);
@@ -396,7 +453,7 @@ __global__ void k_walk_final(const Stream *st, int nstreams, unsigned long long 
   segment_bounds(S, gseg - S.seg_off, a, b);
   Reader rd{raw, raw, 0, 0};
   uint32_t cnt, ex;
-  walk_segment<true>(rd, S.raw_off + S.raw_count, a, b, seg_entry[gseg], cnt, ex, gauss + S.gauss_off + base,
+  walk_segment<true>(zt, rd, S.raw_off + S.raw_count, a, b, seg_entry[gseg], cnt, ex, gauss + S.gauss_off + base,
                      need - base);
   if (ex == kUnderrun && base + cnt < need) atomicExch(flags, 1);
 }

@@ -31,42 +31,53 @@ __device__ __forceinline__ double wrap_coord(double x, double period) {
   return x;
 }
 
+// Per axis and fine index: first stencil cell i0 - 1 (wrapped or clamped later)
+// and the fractional offset t of the fine centroid, evaluated in double once
+// per grid line (field.hpp:483-500): loc = centroid - coarse offset, wrapped into
+// the periodic domain; u = loc / dx_coarse - 0.5; i0 = floor(u); t = u - i0.
 template <typename T>
-__global__ void k_interp_add4(const T *__restrict__ c0, const T *__restrict__ c1, const T *__restrict__ c2,
-                              const T *__restrict__ c3, int nc, double dxc, double ox, double oy, double oz,
-                              double period, int wrap, T *f0, T *f1, T *f2, T *f3, int nf, double dxf, double fx,
-                              double fy, double fz) {
+__global__ void k_interp_axes(int nf, double dxf, double f0, double f1, double f2, double o0, double o1, double o2,
+                              double dxc, double period, int *base, T *frac) {
+  int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= 3 * nf) return;
+  int a = id / nf, x = id % nf;
+  double fo = a == 0 ? f0 : (a == 1 ? f1 : f2);
+  double co = a == 0 ? o0 : (a == 1 ? o1 : o2);
+  double l = wrap_coord((double)x * dxf + fo + dxf / 2 - co, period);
+  double u = l / dxc - 0.5;
+  double f = floor(u);
+  base[id] = (int)f;
+  frac[id] = (T)(u - f);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_interp_add4(const T *__restrict__ c0, const T *__restrict__ c1,
+                                                     const T *__restrict__ c2, const T *__restrict__ c3, int nc,
+                                                     int wrap, const int *__restrict__ base,
+                                                     const T *__restrict__ frac, T *f0, T *f1, T *f2, T *f3,
+                                                     int nf) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   size_t m = (size_t)nf * nf * nf;
   if (i >= m) return;
   size_t row = i / nf;
   int z = (int)(i % nf), y = (int)(row % nf), x = (int)(row / nf);
-  double loc[3] = {(double)x * dxf + fx + dxf / 2 - ox, (double)y * dxf + fy + dxf / 2 - oy,
-                   (double)z * dxf + fz + dxf / 2 - oz};
-  int base[3];
+  int pos[3] = {x, y, z};
   T w[3][4];
+  int idx[3][4];
+#pragma unroll
   for (int a = 0; a < 3; ++a) {
-    double l = wrap_coord(loc[a], period);
-    double u = l / dxc - 0.5;
-    double f = floor(u);
-    base[a] = (int)f;
-    catmull_rom<T>((T)(u - f), w[a]);
-  }
-  int ix[4], iy[4], iz[4];
-  for (int a = 0; a < 4; ++a) {
-    int vx = base[0] - 1 + a, vy = base[1] - 1 + a, vz = base[2] - 1 + a;
-    if (wrap) {
-      vx = (vx % nc + nc) % nc;
-      vy = (vy % nc + nc) % nc;
-      vz = (vz % nc + nc) % nc;
-    } else {
-      vx = min(max(vx, 0), nc - 1);
-      vy = min(max(vy, 0), nc - 1);
-      vz = min(max(vz, 0), nc - 1);
+    catmull_rom<T>(__ldg(frac + a * nf + pos[a]), w[a]);
+    int b0 = __ldg(base + a * nf + pos[a]);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      int v = b0 - 1 + c;
+      if (wrap) {
+        v = v < 0 ? v + nc : (v >= nc ? v - nc : v);
+      } else {
+        v = min(max(v, 0), nc - 1);
+      }
+      idx[a][c] = v;
     }
-    ix[a] = vx;
-    iy[a] = vy;
-    iz[a] = vz;
   }
   const size_t rs = (size_t)(2 * (nc / 2 + 1));
   T s0 = 0, s1 = 0, s2 = 0, s3 = 0;
@@ -75,11 +86,11 @@ __global__ void k_interp_add4(const T *__restrict__ c0, const T *__restrict__ c1
     T p0 = 0, p1 = 0, p2 = 0, p3 = 0;
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-      size_t rowi = ((size_t)ix[a] * nc + iy[b]) * rs;
+      size_t rowi = ((size_t)idx[0][a] * nc + idx[1][b]) * rs;
       T q0 = 0, q1 = 0, q2 = 0, q3 = 0;
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        size_t k = rowi + iz[c];
+        size_t k = rowi + idx[2][c];
         T wc = w[2][c];
         q0 += wc * __ldg(c0 + k);
         q1 += wc * __ldg(c1 + k);
@@ -111,11 +122,17 @@ template <typename T>
 void interp_add4(Context &ctx, const Level &coarse, T *const src[4], Level &fine) {
   size_t m = fine.ncells();
   int wrap = (coarse.box == coarse.periodic) ? 1 : 0;
+  int nf = fine.n;
+  ctx.geom.ensure(3 * (size_t)nf * (sizeof(int) + sizeof(T)));
+  int *base = ctx.geom.as<int>();
+  T *frac = reinterpret_cast<T *>(base + 3 * nf);
+  k_interp_axes<T><<<(3 * nf + 127) / 128, 128, 0, ctx.stream>>>(nf, fine.dx, fine.x0[0], fine.x0[1], fine.x0[2],
+                                                                coarse.x0[0], coarse.x0[1], coarse.x0[2], coarse.dx,
+                                                                coarse.periodic, base, frac);
   k_interp_add4<T><<<(unsigned)((m + 255) / 256), 256, 0, ctx.stream>>>(
-      src[0], src[1], src[2], src[3], coarse.n, coarse.dx, coarse.x0[0], coarse.x0[1], coarse.x0[2], coarse.periodic,
-      wrap, fine.field[0].as<T>(), fine.field[1].as<T>(), fine.field[2].as<T>(), fine.field[3].as<T>(), fine.n,
-      fine.dx, fine.x0[0], fine.x0[1], fine.x0[2]);
-  launched();
+      src[0], src[1], src[2], src[3], coarse.n, wrap, base, frac, fine.field[0].as<T>(), fine.field[1].as<T>(),
+      fine.field[2].as<T>(), fine.field[3].as<T>(), nf);
+  launched(2);
 }
 
 template void interp_add4<float>(Context &, const Level &, float *const[4], Level &);
