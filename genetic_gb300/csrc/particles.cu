@@ -34,6 +34,36 @@ __global__ void k_centroids(int n, double dx, double x0, double y0, double z0, d
   c[id] = (double)i * dx + o + dx / 2;
 }
 
+// float -> double by bit manipulation (exact; keeps the conversion off the
+// double-precision pipe).  Zero and subnormal floats map to (signed) zero
+// scaled exactly; inf/nan keep their class.
+__device__ __forceinline__ double f2d_bits(float f) {
+  unsigned u = __float_as_uint(f);
+  unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  unsigned e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+  if (e == 0) {
+    if (m == 0) return __longlong_as_double((long long)sign);
+    // subnormal float: normalise
+    int sh = __clz(m) - 8;
+    m = (m << sh) & 0x7FFFFFu;
+    unsigned long long ed = (unsigned long long)(1 - 127 - sh + 1023);
+    return __longlong_as_double((long long)(sign | (ed << 52) | ((unsigned long long)m << 29)));
+  }
+  unsigned long long ed = e == 0xFFu ? 0x7FFull : (unsigned long long)(e - 127 + 1023);
+  return __longlong_as_double((long long)(sign | (ed << 52) | ((unsigned long long)m << 29)));
+}
+
+__device__ __forceinline__ double to_double(float v) { return f2d_bits(v); }
+__device__ __forceinline__ double to_double(double v) { return v; }
+
+// wrap_coord with the common in-range case decided by integer compares on the
+// bit patterns (non-negative doubles order like their bits)
+__device__ __forceinline__ double wrap_fast(double x, double period, long long period_bits) {
+  long long b = __double_as_longlong(x);
+  if (b >= 0 && b < period_bits) return x;  // 0 <= x < period (and x != -0)
+  return wrap_coord(x, period);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_particles(const T *__restrict__ px, const T *__restrict__ py,
                                                    const T *__restrict__ pz, int n, const double *__restrict__ cen,
@@ -50,9 +80,10 @@ __global__ void __launch_bounds__(256) k_particles(const T *__restrict__ px, con
   vel[3 * i + 0] = sx * ratio;
   vel[3 * i + 1] = sy * ratio;
   vel[3 * i + 2] = sz * ratio;
-  pos[3 * i + 0] = wrap_coord((double)sx + __ldg(cen + x), period);
-  pos[3 * i + 1] = wrap_coord((double)sy + __ldg(cen + n + y), period);
-  pos[3 * i + 2] = wrap_coord((double)sz + __ldg(cen + 2 * n + z), period);
+  long long pb = __double_as_longlong(period);
+  pos[3 * i + 0] = wrap_fast(to_double(sx) + __ldg(cen + x), period, pb);
+  pos[3 * i + 1] = wrap_fast(to_double(sy) + __ldg(cen + n + y), period, pb);
+  pos[3 * i + 2] = wrap_fast(to_double(sz) + __ldg(cen + 2 * n + z), period, pb);
 }
 
 }  // namespace

@@ -714,8 +714,24 @@ static void draw_all_typed(Context &ctx, unsigned long long seed, int mode) {
     streams.push_back(s);
     if (total > 0) generate_gaussians(ctx, streams, total, 1.0);
   }
-  for (size_t l = 0; l < ctx.levels.size(); ++l)
-    place_level<T>(ctx, *ctx.levels[l], ctx.rng.gauss.as<double>() + offset[l], mode);
+  for (size_t l = 0; l < ctx.levels.size(); ++l) {
+    Level &L = *ctx.levels[l];
+    if (mode == GIC_SEED_FOURIER_PARALLEL) {
+      // same shell streams: a level of the same size as an earlier one draws the same noise
+      size_t same = l;
+      for (size_t m = 0; m < l; ++m)
+        if (ctx.levels[m]->n == L.n) { same = m; break; }
+      if (same != l) {
+        size_t bytes = L.ncomplex() * 2 * sizeof(T);
+        L.noise.ensure(bytes);
+        GIC_CUDA(cudaMemcpyAsync(L.noise.ptr, ctx.levels[same]->noise.ptr, bytes, cudaMemcpyDeviceToDevice,
+                                 ctx.stream));
+        L.have_noise = true;
+        continue;
+      }
+    }
+    place_level<T>(ctx, L, ctx.rng.gauss.as<double>() + offset[l], mode);
+  }
   GIC_CUDA(cudaStreamSynchronize(ctx.stream));
 }
 

@@ -37,17 +37,98 @@ __device__ __forceinline__ double wrap_coord(double x, double period) {
 // the periodic domain; u = loc / dx_coarse - 0.5; i0 = floor(u); t = u - i0.
 template <typename T>
 __global__ void k_interp_axes(int nf, double dxf, double f0, double f1, double f2, double o0, double o1, double o2,
-                              double dxc, double period, int *base, T *frac) {
+                              double dxc, double period, int nc, int *base, T *frac, int *ubase) {
   int id = blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= 3 * nf) return;
   int a = id / nf, x = id % nf;
   double fo = a == 0 ? f0 : (a == 1 ? f1 : f2);
   double co = a == 0 ? o0 : (a == 1 ? o1 : o2);
-  double l = wrap_coord((double)x * dxf + fo + dxf / 2 - co, period);
+  double lu = (double)x * dxf + fo + dxf / 2 - co;
+  double l = wrap_coord(lu, period);
   double u = l / dxc - 0.5;
   double f = floor(u);
   base[id] = (int)f;
   frac[id] = (T)(u - f);
+  // the same base counted from the unwrapped position: monotonic along the axis
+  ubase[id] = (int)f + (int)floor(lu / period) * nc;
+}
+
+// Separable form: a CTA owns one fine x plane and TY fine y rows.  It first
+// contracts the four coarse x planes of its stencil into a shared tile
+// P[cy][cz] (per field), then every fine (y, z) is a 4 x 4 contraction of P.
+template <typename T, int TY>
+__global__ void __launch_bounds__(256) k_interp_add4_sep(const T *__restrict__ c0, const T *__restrict__ c1,
+                                                         const T *__restrict__ c2, const T *__restrict__ c3, int nc,
+                                                         int wrap, const int *__restrict__ base,
+                                                         const T *__restrict__ frac, const int *__restrict__ ubase,
+                                                         T *f0, T *f1, T *f2, T *f3, int nf, int maxcz) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T *P = reinterpret_cast<T *>(smraw);
+  const int x = blockIdx.y;
+  const int y0 = blockIdx.x * TY;
+  const int ylast = min(y0 + TY, nf) - 1;
+  auto cw = [&](int v) { return wrap ? ((v % nc) + nc) % nc : min(max(v, 0), nc - 1); };
+  T wx[4];
+  catmull_rom<T>(__ldg(frac + x), wx);
+  int ixw[4];
+  int bx = __ldg(base + x);
+#pragma unroll
+  for (int a = 0; a < 4; ++a) ixw[a] = cw(bx - 1 + a);
+  const int cy0 = __ldg(ubase + nf + y0) - 1;
+  const int ny = __ldg(ubase + nf + ylast) + 3 - cy0;
+  const int cz0 = __ldg(ubase + 2 * nf) - 1;
+  const int nz = min(__ldg(ubase + 2 * nf + nf - 1) + 3 - cz0, maxcz);
+  const size_t rs = (size_t)(2 * (nc / 2 + 1));
+  const int tile = ny * nz;
+  for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+    int cy = cw(cy0 + e / nz), cz = cw(cz0 + e % nz);
+    T v0 = 0, v1 = 0, v2 = 0, v3 = 0;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      size_t k = ((size_t)ixw[a] * nc + cy) * rs + cz;
+      v0 += wx[a] * __ldg(c0 + k);
+      v1 += wx[a] * __ldg(c1 + k);
+      v2 += wx[a] * __ldg(c2 + k);
+      v3 += wx[a] * __ldg(c3 + k);
+    }
+    P[e] = v0;
+    P[tile + e] = v1;
+    P[2 * tile + e] = v2;
+    P[3 * tile + e] = v3;
+  }
+  __syncthreads();
+  const size_t frs = (size_t)(2 * (nf / 2 + 1));
+  const int cnt = (ylast - y0 + 1) * nf;
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    int y = y0 + e / nf, z = e % nf;
+    T wy[4], wz[4];
+    catmull_rom<T>(__ldg(frac + nf + y), wy);
+    catmull_rom<T>(__ldg(frac + 2 * nf + z), wz);
+    int py = __ldg(ubase + nf + y) - 1 - cy0;
+    int pz = __ldg(ubase + 2 * nf + z) - 1 - cz0;
+    T s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      T q0 = 0, q1 = 0, q2 = 0, q3 = 0;
+      int rowp = (py + b) * nz + pz;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        q0 += wz[c] * P[rowp + c];
+        q1 += wz[c] * P[tile + rowp + c];
+        q2 += wz[c] * P[2 * tile + rowp + c];
+        q3 += wz[c] * P[3 * tile + rowp + c];
+      }
+      s0 += wy[b] * q0;
+      s1 += wy[b] * q1;
+      s2 += wy[b] * q2;
+      s3 += wy[b] * q3;
+    }
+    size_t dst = ((size_t)x * nf + y) * frs + z;
+    f0[dst] += s0;
+    f1[dst] += s1;
+    f2[dst] += s2;
+    f3[dst] += s3;
+  }
 }
 
 template <typename T>
@@ -123,16 +204,34 @@ void interp_add4(Context &ctx, const Level &coarse, T *const src[4], Level &fine
   size_t m = fine.ncells();
   int wrap = (coarse.box == coarse.periodic) ? 1 : 0;
   int nf = fine.n;
-  ctx.geom.ensure(3 * (size_t)nf * (sizeof(int) + sizeof(T)));
+  ctx.geom.ensure(3 * (size_t)nf * (2 * sizeof(int) + sizeof(T)));
   int *base = ctx.geom.as<int>();
-  T *frac = reinterpret_cast<T *>(base + 3 * nf);
+  int *ubase = base + 3 * nf;
+  T *frac = reinterpret_cast<T *>(ubase + 3 * nf);
   k_interp_axes<T><<<(3 * nf + 127) / 128, 128, 0, ctx.stream>>>(nf, fine.dx, fine.x0[0], fine.x0[1], fine.x0[2],
                                                                 coarse.x0[0], coarse.x0[1], coarse.x0[2], coarse.dx,
-                                                                coarse.periodic, base, frac);
-  k_interp_add4<T><<<(unsigned)((m + 255) / 256), 256, 0, ctx.stream>>>(
-      src[0], src[1], src[2], src[3], coarse.n, wrap, base, frac, fine.field[0].as<T>(), fine.field[1].as<T>(),
-      fine.field[2].as<T>(), fine.field[3].as<T>(), nf);
-  launched(2);
+                                                                coarse.periodic, coarse.n, base, frac, ubase);
+  launched();
+  // coarse cells spanned by the fine grid along one axis, plus the stencil
+  double ratio = fine.dx / coarse.dx;
+  int span = (int)std::ceil(nf * ratio) + 6;
+  constexpr int TY = 8;
+  int ny = (int)std::ceil(TY * ratio) + 6;
+  size_t smem = (size_t)4 * ny * span * sizeof(T);
+  if (ratio <= 1.0 && span <= nf + 6 && smem <= 96 * 1024) {
+    GIC_CUDA(cudaFuncSetAttribute((const void *)k_interp_add4_sep<T, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+    dim3 grid((nf + TY - 1) / TY, nf);
+    k_interp_add4_sep<T, TY><<<grid, 256, smem, ctx.stream>>>(src[0], src[1], src[2], src[3], coarse.n, wrap, base,
+                                                              frac, ubase, fine.field[0].as<T>(),
+                                                              fine.field[1].as<T>(), fine.field[2].as<T>(),
+                                                              fine.field[3].as<T>(), nf, span);
+  } else {
+    k_interp_add4<T><<<(unsigned)((m + 255) / 256), 256, 0, ctx.stream>>>(
+        src[0], src[1], src[2], src[3], coarse.n, wrap, base, frac, fine.field[0].as<T>(), fine.field[1].as<T>(),
+        fine.field[2].as<T>(), fine.field[3].as<T>(), nf);
+  }
+  launched();
 }
 
 template void interp_add4<float>(Context &, const Level &, float *const[4], Level &);
