@@ -390,3 +390,249 @@ def zoom_realisation(noises, levels, power):
                 f += interpolate_to(fft_c2r(s), cbox, coff, periodic, box, n, off)
         out.append(fields)
     return out
+
+
+# --- modifications (modifications/*.hpp, multilevelfield.hpp, multilevelgrid.hpp) --------
+
+class Levels:
+    """Geometry of a multi-level context: [(box, n, (x0, y0, z0))], level 0 periodic."""
+
+    def __init__(self, levels):
+        self.levels = [(float(b), int(n), tuple(float(o) for o in off)) for b, n, off in levels]
+        self.periodic = self.levels[0][0]
+        dx0 = self.levels[0][0] / self.levels[0][1]
+        # cell-volume weights relative to level 0 (multilevelgrid.hpp:121-124)
+        self.weights = [(b / n / dx0) ** 3 for b, n, _ in self.levels]
+
+    def __len__(self):
+        return len(self.levels)
+
+    def kcut(self, l):
+        box, n, _ = self.levels[l]
+        return 0.3 * (n * (2. * np.pi / box))
+
+    def filter(self, l, k):
+        """The family filter of level l (filterfamily.hpp:106-140): LP_0 on the base, HP_0 LP_1 ... HP_{l-1} LP_l."""
+        f = np.ones_like(k)
+        for m in range(l):
+            f = f * np.sqrt(1. - fermi_lowpass(k, self.kcut(m)) ** 2)
+        if l < len(self.levels) - 1:
+            f = f * fermi_lowpass(k, self.kcut(l))
+        return f
+
+    def centroids(self, l, axis):
+        box, n, off = self.levels[l]
+        dx = box / n
+        return np.arange(n) * dx + off[axis] + dx / 2
+
+    def window_mask(self, l, window_level):
+        """Cells of level l whose centroids lie in the box of level window_level (window.hpp)."""
+        wbox, wn, woff = self.levels[window_level]
+        masks = []
+        for a in range(3):
+            c = self.centroids(l, a)
+            lo = np.fmod(woff[a], self.periodic)
+            hi = np.fmod(woff[a] + wbox, self.periodic)
+            if lo <= hi:
+                masks.append((c >= lo) & (c < hi))
+            else:
+                masks.append((c >= lo) | (c < hi))
+        return masks[0][:, None, None] & masks[1][None, :, None] & masks[2][None, None, :]
+
+
+def flag_cells(levels, l, centre, kind, size):
+    """Cells of level l selected by select_sphere / select_cube around `centre` (ic.hpp:1458-1524)."""
+    box, n, off = levels.levels[l]
+    L = levels.periodic
+    d = []
+    for a in range(3):
+        x = levels.centroids(l, a) - centre[a]
+        x = np.where(x > L / 2, x - L, np.where(x < -L / 2, x + L, x))
+        d.append(x)
+    X, Y, Z = np.meshgrid(d[0], d[1], d[2], indexing='ij')
+    if kind == 'sphere':
+        r2 = float(np.float32(size) * np.float32(size))
+        sel = X * X + Y * Y + Z * Z < r2
+    else:
+        h = float(np.float32(size) / np.float32(2))
+        sel = (np.abs(X) < h) & (np.abs(Y) < h) & (np.abs(Z) < h)
+    return np.flatnonzero(sel.ravel())
+
+
+def localisation_covector(levels, flagged, kind, direction=0):
+    """Top-hat average over the flagged cells of the finest level, or the 4th-order
+    -gradient stencil for velocity modifications (linearmodification.hpp:78-90, 202-240)."""
+    box, n, _ = levels.levels[-1]
+    out = np.zeros(n ** 3)
+    w = 1.0 / len(flagged)
+    if kind == 'overdensity':
+        np.add.at(out, flagged, w)
+        return out.reshape(n, n, n)
+    dx = box / n
+    a, b = -w / 12. / dx, w * 2. / 3. / dx
+    coords = np.array(np.unravel_index(flagged, (n, n, n)))
+    def idx(step):
+        c = coords.copy()
+        c[direction] = (c[direction] + step) % n
+        return np.ravel_multi_index(c, (n, n, n))
+    np.add.at(out, idx(-2), a)
+    np.add.at(out, idx(-1), b)
+    np.add.at(out, idx(1), -b)
+    np.add.at(out, idx(2), -a)
+    return out.reshape(n, n, n)
+
+
+def _axis_geometry(levels, fine, coarse, axis):
+    cbox, cn, coff = levels.levels[coarse]
+    dxc = cbox / cn
+    loc = levels.centroids(fine, axis) - coff[axis]
+    loc = np.fmod(loc, levels.periodic)
+    loc = np.where(loc < 0, loc + levels.periodic, loc)
+    u = loc / dxc - 0.5
+    i0 = np.floor(u)
+    return i0.astype(int), catmull_rom_weights(u - i0)
+
+
+def deinterpolate(levels, hires, fine, coarse):
+    """Transpose of the tricubic interpolation, fine real field -> coarse real field
+    (field.hpp:420-480 via multilevelgrid.hpp:245-306); stencil indices wrap."""
+    cn = levels.levels[coarse][1]
+    out = hires
+    for axis in range(3):
+        i0, w = _axis_geometry(levels, fine, coarse, axis)
+        shape = list(out.shape)
+        shape[axis] = cn
+        acc = np.zeros(shape)
+        moved = np.moveaxis(out, axis, 0)
+        accm = np.moveaxis(acc, axis, 0)
+        for a in range(4):
+            idx = (i0 + a - 1) % cn
+            np.add.at(accm, idx, w[:, a].reshape((-1,) + (1,) * (moved.ndim - 1)) * moved)
+        out = acc
+    return out
+
+
+def subsample_average(levels, fine_real, fine, coarse):
+    """Average of the fine cells inside each coarse cell covered by the fine grid, 0
+    elsewhere (SubSampleEvaluator, evaluator.hpp:180-207)."""
+    fbox, fn, foff = levels.levels[fine]
+    cbox, cn, coff = levels.levels[coarse]
+    r = int(round((cbox / cn) / (fbox / fn)))
+    m = fn // r
+    avg = fine_real.reshape(m, r, m, r, m, r).mean(axis=(1, 3, 5))
+    out = np.zeros((cn, cn, cn))
+    start = [int(round((foff[a] - coff[a]) / (cbox / cn))) for a in range(3)]
+    ix = [(start[a] + np.arange(m)) % cn for a in range(3)]
+    out[np.ix_(ix[0], ix[1], ix[2])] += avg
+    return out
+
+
+def _kmag_level(levels, l):
+    box, n, _ = levels.levels[l]
+    return kmag(n, box)
+
+
+def multilevel_covector(levels, hires_real, power_dm, velocity_scale=None):
+    """ConstraintField of a modification in Fourier space on every level
+    (multilevelgrid.hpp:245-321, linearmodification.hpp:64-75, 134-141, 242-297).
+    velocity_scale: None for an overdensity, else the velocity-to-offset ratio."""
+    nl = len(levels)
+    real = [None] * nl
+    real[-1] = fft_c2r(fft_r2c(hires_real))
+    for l in range(nl - 2, -1, -1):
+        ratio = int(round((levels.levels[l][0] / levels.levels[l][1]) /
+                          (levels.levels[l + 1][0] / levels.levels[l + 1][1])))
+        real[l] = deinterpolate(levels, real[l + 1] / ratio ** 3, l + 1, l)
+    out = []
+    for l in range(nl):
+        box, n, _ = levels.levels[l]
+        f = fft_r2c(real[l] * (levels.weights[l] / levels.weights[-1])) * levels.filter(l, _kmag_level(levels, l))
+        f = fft_r2c(fft_c2r(f))  # toReal then back to Fourier, as the reference does
+        f = f * sqrt_power_grid(power_dm, n, box)
+        if velocity_scale is not None:
+            kk = _kmag_level(levels, l) ** 2
+            with np.errstate(divide='ignore', invalid='ignore'):
+                v = -velocity_scale * f / kk
+            v[0, 0, 0] = 0
+            f = v
+        out.append(f)
+    return out
+
+
+def inner(a, b):
+    """Hermitian-weighted sum over levels of Re(conj a b) (multilevelfield.hpp:248-294)."""
+    s = 0.0
+    for x, y in zip(a, b):
+        n = x.shape[0]
+        w = np.full(x.shape[2], 2.0)
+        w[0] = 1.0
+        w[n // 2] = 1.0
+        s += float(np.sum(np.real(np.conj(x) * y) * w[None, None, :]))
+    return s
+
+
+def cross_level_term(levels, field_k, target, source):
+    """addFieldFromDifferentGridWithFilter(source, f_t f_s sqrt(w_t/w_s)) onto the
+    target's real grid (multilevelfield.hpp:362-378, field.hpp:816-831)."""
+    k = _kmag_level(levels, source)
+    filt = levels.filter(target, k) * levels.filter(source, k) * np.sqrt(levels.weights[target] / levels.weights[source])
+    src_real = fft_c2r(field_k[source] * filt)
+    if source < target:
+        tbox, tn, toff = levels.levels[target]
+        sbox, sn, soff = levels.levels[source]
+        return interpolate_to(src_real, sbox, soff, levels.periodic, tbox, tn, toff)
+    return subsample_average(levels, src_real, source, target)
+
+
+def apply_metric(levels, field_k, to_covector):
+    """MultiLevelField::applyMetric (multilevelfield.hpp:344-384); fields in Fourier space."""
+    nl = len(levels)
+    out = []
+    for l in range(nl):
+        k = _kmag_level(levels, l)
+        f = levels.filter(l, k)
+        x = field_k[l].copy()
+        if to_covector and l < nl - 1:
+            mask = levels.window_mask(l, l + 1)
+            # applyFilterInWindow(f, window, windowFirst=true) then (.., false) (field.hpp:752-775)
+            xr = fft_c2r(x)
+            inw = fft_r2c(np.where(mask, xr, 0.0)) * f
+            x = fft_r2c(np.where(mask, 0.0, xr)) + inw
+            xr = fft_c2r(x)
+            inw_r = np.where(mask, fft_c2r(x * f), 0.0)
+            x = fft_r2c(np.where(mask, 0.0, xr) + inw_r)
+        else:
+            x = x * f * f
+        xr = fft_c2r(x)
+        for s in range(nl):
+            if s != l:
+                xr = xr + cross_level_term(levels, field_k, l, s)
+        out.append(fft_r2c(xr))
+    return out
+
+
+def chi2_levels(levels, noise_k):
+    return inner(apply_metric(levels, noise_k, True), noise_k)
+
+
+def apply_linear_modifications(levels, noise_k, covectors, targets):
+    """Gram-Schmidt + correction (modificationmanager.hpp:199-217, 288-312), restated
+    with the same operation order; returns the modified noise."""
+    alphas = [[c.copy() for c in cv] for cv in covectors]
+    t = list(targets)
+    n = len(alphas)
+    for i in range(n):
+        for j in range(i):
+            r = inner(alphas[i], apply_metric(levels, alphas[j], False))
+            alphas[i] = [a - r * b for a, b in zip(alphas[i], alphas[j])]
+            t[i] -= r * t[j]
+        nrm = np.sqrt(inner(alphas[i], apply_metric(levels, alphas[i], False)))
+        alphas[i] = [a / nrm for a in alphas[i]]
+        t[i] /= nrm
+    existing = [inner(a, noise_k) for a in alphas]
+    out = [w.copy() for w in noise_k]
+    for i in range(n):
+        vec = apply_metric(levels, alphas[i], False)
+        d = t[i] - existing[i]
+        out = [o + d * v for o, v in zip(out, vec)]
+    return out
