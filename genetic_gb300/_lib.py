@@ -25,6 +25,11 @@ GIC_SEED_FOURIER_SERIAL = 1
 GIC_SEED_FOURIER_PARALLEL = 2
 GIC_SEED_FOURIER_REVERSE = 3
 
+GIC_MOD_OVERDENSITY = 0
+GIC_MOD_VX = 1
+GIC_MOD_VY = 2
+GIC_MOD_VZ = 3
+
 GIC_FIELD_NOISE = 0
 GIC_FIELD_DELTA = 1
 GIC_FIELD_PSI_X = 2
@@ -63,6 +68,10 @@ SIGNATURES = {
     'gic_fft': [_P, _I, _I, _I],
     'gic_chi2': [_P, _D],
     'gic_launch_count': [ctypes.POINTER(ctypes.c_ulonglong)],
+    'gic_calculate': [_P, _I, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_size_t, _D],
+    'gic_add_modification': [_P, _I, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_size_t, ctypes.c_double, _I],
+    'gic_clear_modifications': [_P],
+    'gic_apply_modifications': [_P, _D, _D],
     'gic_get_stream': [_P, ctypes.POINTER(_P)],
 }
 

@@ -24,8 +24,6 @@ void cuda_check(cudaError_t e, const char *what) {
   }
 }
 
-double velocity_to_offset_ratio(const Cosmo &c);
-
 static std::atomic<unsigned long long> g_launches{0};
 
 void launched(int kernels) {
@@ -372,10 +370,60 @@ int gic_fft(gic_ctx *ctx, int level, int what, int dir) {
 int gic_chi2(gic_ctx *ctx, double *chi2) {
   API_BEGIN(ctx)
   if (!chi2) gic::fail(GIC_ERR_INVALID_ARG, "null output");
-  if (C.levels.size() != 1) gic::fail(GIC_ERR_INVALID_ARG, "chi^2 over several levels is not supported yet");
-  gic::Level &L = gic::level_at(C, 0);
-  if (!L.have_noise) gic::fail(GIC_ERR_NOT_READY, "white noise has not been drawn");
-  *chi2 = C.dbl() ? gic::chi2_typed<double>(C, L) : gic::chi2_typed<float>(C, L);
+  if (C.levels.empty()) gic::fail(GIC_ERR_NOT_READY, "no grid levels");
+  for (auto &L : C.levels)
+    if (!L->have_noise) gic::fail(GIC_ERR_NOT_READY, "white noise has not been drawn");
+  if (C.levels.size() == 1)
+    *chi2 = C.dbl() ? gic::chi2_typed<double>(C, *C.levels[0]) : gic::chi2_typed<float>(C, *C.levels[0]);
+  else
+    *chi2 = gic::noise_chi2(C);
+  API_END
+}
+
+static gic::ModRequest make_request(gic::Context &C, int kind, const unsigned long long *cells, size_t n) {
+  if (kind < GIC_MOD_OVERDENSITY || kind > GIC_MOD_VZ) gic::fail(GIC_ERR_INVALID_ARG, "unknown modification");
+  if (C.levels.empty()) gic::fail(GIC_ERR_NOT_READY, "no grid levels");
+  if (!cells || n == 0)
+    gic::fail(GIC_ERR_INVALID_ARG,
+              "Linear modifications use exclusively information from the highest resolution grid but no cells have been "
+              "flagged on this grid.");
+  size_t m = C.levels.back()->ncells();
+  for (size_t i = 0; i < n; ++i)
+    if (cells[i] >= m) gic::fail(GIC_ERR_INVALID_ARG, "flagged cell outside the finest grid");
+  gic::ModRequest r;
+  r.kind = kind;
+  r.cells.assign(cells, cells + n);
+  r.target = 0;
+  return r;
+}
+
+int gic_calculate(gic_ctx *ctx, int kind, const unsigned long long *cells, size_t n, double *value) {
+  API_BEGIN(ctx)
+  if (!value) gic::fail(GIC_ERR_INVALID_ARG, "null output");
+  gic::ModRequest r = make_request(C, kind, cells, n);
+  *value = gic::modification_value(C, r);
+  API_END
+}
+
+int gic_add_modification(gic_ctx *ctx, int kind, const unsigned long long *cells, size_t n, double target,
+                         int relative) {
+  API_BEGIN(ctx)
+  gic::ModRequest r = make_request(C, kind, cells, n);
+  r.target = relative ? target * gic::modification_value(C, r) : target;
+  C.mods.push_back(std::move(r));
+  API_END
+}
+
+int gic_clear_modifications(gic_ctx *ctx) {
+  API_BEGIN(ctx)
+  C.mods.clear();
+  API_END
+}
+
+int gic_apply_modifications(gic_ctx *ctx, double *chi2_before, double *chi2_after) {
+  API_BEGIN(ctx)
+  if (C.mods.empty()) gic::fail(GIC_ERR_NOT_READY, "no modifications to apply");
+  gic::apply_modifications(C, chi2_before, chi2_after);
   API_END
 }
 

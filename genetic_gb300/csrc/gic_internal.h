@@ -61,6 +61,7 @@ struct Level {
   DevBuf noise;          // white noise (unit variance per real d.o.f.)
   DevBuf field[4];       // delta, psi_x, psi_y, psi_z
   DevBuf sqrtp;          // double sqrt(P_grid) per integer |k|^2
+  DevBuf sqrtp_dm;       // the same with the dark-matter transfer column
   DevBuf tab_main;       // sqrt(P_grid), times the high-pass filter on zoom levels
   DevBuf tab_lp_src;     // sqrt(P_grid) * low-pass (source side of the next zoom)
   DevBuf tab_lp;         // low-pass filter alone
@@ -98,6 +99,13 @@ struct RngScratch {
   int chunkmul_count = 0;
 };
 
+// a linear modification awaiting application (kind 0 overdensity, 1-3 velocity x,y,z)
+struct ModRequest {
+  int kind;
+  std::vector<unsigned long long> cells;  // flagged cells of the finest level
+  double target;
+};
+
 struct Context {
   int device = 0;
   int precision = GIC_FP64;
@@ -112,6 +120,7 @@ struct Context {
   DevBuf reduce;  // small scratch for reductions
   DevBuf zoom_scratch[4];  // low-passed coarse fields during zoom combination
   DevBuf geom;             // per-axis interpolation / centroid tables
+  std::vector<ModRequest> mods;
   bool dbl() const { return precision == GIC_FP64; }
 };
 
@@ -128,10 +137,21 @@ void gaussian_stream(Context &ctx, unsigned long long seed, size_t n, double *ho
 // kspace.cu
 void transfer_setup(Context &ctx, const double *table, int nrows, int ncols);
 void build_sqrtp_table(Context &ctx, Level &L);
+void build_sqrtp_table_species(Context &ctx, Level &L, int dm);
 void za_fields(Context &ctx, int level);
 void zoom_combine(Context &ctx, int level);
 
+// zoom.cu
+template <typename T, int NF>
+void interp_add(Context &ctx, const Level &coarse, const T *const *src, const Level &fine, T *const *dst);
+
+// modify.cu
+double modification_value(Context &ctx, const ModRequest &m);
+double noise_chi2(Context &ctx);
+void apply_modifications(Context &ctx, double *chi2_before, double *chi2_after);
+
 // particles.cu
+double velocity_to_offset_ratio(const Cosmo &c);
 void make_particles(Context &ctx, Level &L);
 
 }  // namespace gic

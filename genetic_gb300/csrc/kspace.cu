@@ -286,23 +286,29 @@ void transfer_setup(Context &ctx, const double *table, int nrows, int ncols) {
   T.ready = true;
   for (auto &L : ctx.levels) {
     L->sqrtp.release();
+    L->sqrtp_dm.release();
     L->tab_main.release();
     L->tab_lp_src.release();
     L->tab_lp.release();
   }
 }
 
-void build_sqrtp_table(Context &ctx, Level &L) {
+void build_sqrtp_table(Context &ctx, Level &L) { build_sqrtp_table_species(ctx, L, 0); }
+
+// sqrt(P_grid) by |k|^2 for the "all" transfer column (dm = 0) or the dark-matter column
+void build_sqrtp_table_species(Context &ctx, Level &L, int dm) {
   if (!ctx.transfer.ready) fail(GIC_ERR_NOT_READY, "no transfer function");
-  if (L.sqrtp.ptr) return;
+  DevBuf &tab = dm ? L.sqrtp_dm : L.sqrtp;
+  if (tab.ptr) return;
   long long half = L.n / 2;
   long long nq = 3 * half * half + 1;
-  L.sqrtp.ensure(nq * sizeof(double));
+  tab.ensure(nq * sizeof(double));
   double kw = 2. * M_PI / L.box;
   double norm = kw * kw * kw / pow(2.f * M_PI, 3.f) * (double)L.ncells();
   k_sqrtp_table<<<(unsigned)((nq + 255) / 256), 256, 0, ctx.stream>>>(
-      L.sqrtp.as<double>(), nq, L.kmin(), ctx.transfer.amplitude, ctx.cosmo.ns, norm, ctx.transfer.lnk.as<double>(),
-      ctx.transfer.lnT_all.as<double>(), ctx.transfer.c_all.as<double>(), ctx.transfer.nrows);
+      tab.as<double>(), nq, L.kmin(), ctx.transfer.amplitude, ctx.cosmo.ns, norm, ctx.transfer.lnk.as<double>(),
+      dm ? ctx.transfer.lnT_dm.as<double>() : ctx.transfer.lnT_all.as<double>(),
+      dm ? ctx.transfer.c_dm.as<double>() : ctx.transfer.c_all.as<double>(), ctx.transfer.nrows);
   launched();
 }
 

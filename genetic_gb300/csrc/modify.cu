@@ -1,0 +1,669 @@
+// Linear modifications (constraints) on the white noise, as genetIC applies them
+// (genetIC/src/simulation/modifications/modificationmanager.hpp:90-125, 199-217, 288-331,
+//  linearmodification.hpp, multilevelgrid.hpp:245-321, multilevelfield.hpp:248-384,
+//  field.hpp:752-849).
+//
+//  - covector of a modification: a top-hat (overdensity) or 4th-order gradient
+//    stencil (velocity) over the flagged cells of the finest level, transformed
+//    to Fourier space; carried to coarser levels by the transpose of the tricubic
+//    interpolation (separable: three one-axis passes), weighted by the cell-volume
+//    ratio, filtered by the level's filter of the zoom filter family, and
+//    multiplied by sqrt(P_dm) (and by -v/k^2 for velocities);
+//  - metric C (covector <-> vector): per level f_l^2 (or, towards a covector, the
+//    filter applied inside/outside the next level's window) plus cross-level terms
+//    f_t f_s sqrt(w_t/w_s) interpolated up or block-averaged down;
+//  - inner products <a|b> = sum_l sum_k Re(conj(a) b) with Hermitian weights,
+//    accumulated in double on the device;
+//  - Gram-Schmidt of the covectors: the same sequence of projections as the
+//    reference, evaluated through the Gram matrix G_ij = <a_i|C|a_j> (C is
+//    linear), which needs one metric conversion per covector instead of one per
+//    inner product; the correction sum_i d_i C a'_i is then one combination of
+//    the converted covectors.
+#include "gic_internal.h"
+#include <cmath>
+#include <algorithm>
+
+namespace gic {
+namespace {
+
+template <typename T> struct V2m;
+template <> struct V2m<float> { using type = float2; };
+template <> struct V2m<double> { using type = double2; };
+
+// --- per-|k|^2 tables ---------------------------------------------------------
+
+// table[q] = scalar * (prod_i HP(k; hp_cut_i) * prod_j LP(k; lp_cut_j))^power
+//            [* sqrtp[q]] [* -vel / k^2], k = sqrt(q) kmin
+struct TableSpec {
+  double kmin;
+  int nhp;
+  double hp_cut[8];
+  int nlp;
+  double lp_cut[4];
+  int power;
+  double scalar;
+  const double *sqrtp;
+  double vel;
+};
+
+__device__ __forceinline__ double fermi_lp(double k, double kcut) {
+  double temperature = kcut * 0.1;
+  return 1. / (1. + exp((k - kcut) / temperature));
+}
+
+__global__ void k_mod_table(double *out, long long nq, TableSpec sp) {
+  long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  double k = sqrt((double)q) * sp.kmin;
+  double f = 1.0;
+  for (int i = 0; i < sp.nhp; ++i) {
+    double lp = fermi_lp(k, sp.hp_cut[i]);
+    f *= sqrt(1. - lp * lp);
+  }
+  for (int i = 0; i < sp.nlp; ++i) f *= fermi_lp(k, sp.lp_cut[i]);
+  if (sp.power == 2) f = f * f;
+  f *= sp.scalar;
+  if (sp.sqrtp) f *= sp.sqrtp[q];
+  if (sp.vel != 0.0) f = q == 0 ? 0.0 : -sp.vel * f / (k * k);
+  out[q] = f;
+}
+
+template <typename T>
+__global__ void k_mul_table(typename V2m<T>::type *c, int n, const double *tab) {
+  const int H = n / 2, S = H + 1;
+  size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t nc = (size_t)n * n * S;
+  if (id >= nc) return;
+  int iz = (int)(id % S);
+  size_t r = id / S;
+  int iy = (int)(r % n), ix = (int)(r / n);
+  long long kx = ix > H ? ix - n : ix, ky = iy > H ? iy - n : iy;
+  T s = (T)tab[kx * kx + ky * ky + (long long)iz * iz];
+  c[id].x *= s;
+  c[id].y *= s;
+}
+
+// --- elementwise ----------------------------------------------------------------
+
+template <typename T>
+__global__ void k_axpy(T *a, const T *b, double c, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] += (T)c * b[i];
+}
+
+template <typename T>
+__global__ void k_scale(T *a, double c, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] *= (T)c;
+}
+
+// zero the cells of a padded real field inside (zero_inside = 1) or outside the window
+template <typename T>
+__global__ void k_mask(T *real, int n, const unsigned char *mx, const unsigned char *my, const unsigned char *mz,
+                       int zero_inside) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t m = (size_t)n * n * n;
+  if (i >= m) return;
+  size_t row = i / n;
+  int z = (int)(i % n), y = (int)(row % n), x = (int)(row / n);
+  int in = mx[x] && my[y] && mz[z];
+  if (in == zero_inside) real[row * (size_t)(2 * (n / 2 + 1)) + z] = 0;
+}
+
+// Hermitian-weighted Re(conj(a) b) over a half spectrum, partial sums per block
+template <typename T>
+__global__ void k_inner(const T *a, const T *b, int n, double *partial) {
+  __shared__ double red[256];
+  const int H = n / 2, S = H + 1;
+  size_t nc = (size_t)n * n * S;
+  double acc = 0;
+  for (size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x; id < nc; id += (size_t)gridDim.x * blockDim.x) {
+    int kz = (int)(id % S);
+    double w = (kz == 0 || kz == H) ? 1.0 : 2.0;
+    acc += w * ((double)a[2 * id] * (double)b[2 * id] + (double)a[2 * id + 1] * (double)b[2 * id + 1]);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+// localisation covector on the finest grid (padded real layout)
+template <typename T>
+__global__ void k_localise(T *real, int n, const unsigned long long *cells, size_t count, int kind, int dir,
+                           double w, double a, double b) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  unsigned long long c = cells[i];
+  int z = (int)(c % n);
+  unsigned long long r = c / n;
+  int y = (int)(r % n), x = (int)(r / n);
+  const size_t rs = (size_t)(2 * (n / 2 + 1));
+  auto at = [&](int dx, int dy, int dz) -> T * {
+    int xx = ((x + dx) % n + n) % n, yy = ((y + dy) % n + n) % n, zz = ((z + dz) % n + n) % n;
+    return real + ((size_t)xx * n + yy) * rs + zz;
+  };
+  if (kind == 0) {
+    atomicAdd(at(0, 0, 0), (T)w);
+    return;
+  }
+  int s[3] = {0, 0, 0};
+  s[dir] = 1;
+  atomicAdd(at(-2 * s[0], -2 * s[1], -2 * s[2]), (T)a);
+  atomicAdd(at(-s[0], -s[1], -s[2]), (T)b);
+  atomicAdd(at(s[0], s[1], s[2]), (T)(-b));
+  atomicAdd(at(2 * s[0], 2 * s[1], 2 * s[2]), (T)(-a));
+}
+
+template <typename T>
+__device__ __forceinline__ void cr_weights(T t, T (&w)[4]) {
+  T t2 = t * t, t3 = t2 * t;
+  w[0] = -(t - 1) * (t - 1) * t / 2;
+  w[1] = (2 - 5 * t2 + 3 * t3) / 2;
+  w[2] = t * (1 + 4 * t - 3 * t2) / 2;
+  w[3] = (t - 1) * t2 / 2;
+}
+
+// Transpose interpolation, one axis at a time.  `in` has dims (A0, A1, A2) with
+// strides (s0, s1, 1); the pass contracts axis `ax` of length nf into length nout
+// starting at unwrapped coarse index c0: out[..c..] += w_a(t_x) in[..x..] for
+// c = ubase[x] - 1 + a - c0.  One thread owns one line along `ax`, so no two
+// threads write the same element.
+template <typename T>
+__global__ void k_deinterp_pass(const T *in, long long in_s0, long long in_s1, T *out, long long out_s0,
+                                long long out_s1, int ax, int n0, int n1, int n2, int nf, const int *ubase,
+                                const T *frac, int c0, int nout, T scale) {
+  // the two non-contracted axes
+  int d[3] = {n0, n1, n2};
+  long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int oa = ax == 0 ? 1 : 0, ob = ax == 2 ? 1 : 2;
+  long long lines = (long long)d[oa] * d[ob];
+  if (tid >= lines) return;
+  int ib = (int)(tid % d[ob]), ia = (int)(tid / d[ob]);
+  long long is[3] = {in_s0, in_s1, 1}, os[3] = {out_s0, out_s1, 1};
+  long long ibase = (long long)ia * is[oa] + (long long)ib * is[ob];
+  long long obase = (long long)ia * os[oa] + (long long)ib * os[ob];
+  for (int x = 0; x < nf; ++x) {
+    T v = in[ibase + (long long)x * is[ax]] * scale;
+    T w[4];
+    cr_weights<T>(frac[x], w);
+    int c = ubase[x] - 1 - c0;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      int cc = c + a;
+      if (cc >= 0 && cc < nout) out[obase + (long long)cc * os[ax]] += w[a] * v;
+    }
+  }
+}
+
+// add a compact block (bx, by, bz) starting at unwrapped coarse (c0x, c0y, c0z) into a padded real coarse field
+template <typename T>
+__global__ void k_add_block(const T *blk, int bx, int by, int bz, int c0x, int c0y, int c0z, T *real, int n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t m = (size_t)bx * by * bz;
+  if (i >= m) return;
+  int z = (int)(i % bz);
+  size_t r = i / bz;
+  int y = (int)(r % by), x = (int)(r / by);
+  int X = ((c0x + x) % n + n) % n, Y = ((c0y + y) % n + n) % n, Z = ((c0z + z) % n + n) % n;
+  atomicAdd(real + ((size_t)X * n + Y) * (size_t)(2 * (n / 2 + 1)) + Z, blk[i]);
+}
+
+// coarse cells covered by the fine grid receive the mean of their r^3 fine cells
+template <typename T>
+__global__ void k_subsample_add(const T *fine, int nf, int r, int sx, int sy, int sz, T *coarse, int nc) {
+  int m = nf / r;
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)m * m * m) return;
+  int k = (int)(i % m);
+  size_t rr = i / m;
+  int j = (int)(rr % m), ii = (int)(rr / m);
+  const size_t frs = (size_t)(2 * (nf / 2 + 1));
+  T s = 0;
+  for (int a = 0; a < r; ++a)
+    for (int b = 0; b < r; ++b)
+      for (int c = 0; c < r; ++c)
+        s += fine[((size_t)(ii * r + a) * nf + (j * r + b)) * frs + (k * r + c)];
+  s /= (T)((double)r * r * r);
+  int X = ((sx + ii) % nc + nc) % nc, Y = ((sy + j) % nc + nc) % nc, Z = ((sz + k) % nc + nc) % nc;
+  coarse[((size_t)X * nc + Y) * (size_t)(2 * (nc / 2 + 1)) + Z] += s;
+}
+
+template <typename T>
+__global__ void k_axes_geom(int nf, double dxf, double f0, double f1, double f2, double o0, double o1, double o2,
+                            double dxc, double period, int nc, int *ubase, T *frac) {
+  int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= 3 * nf) return;
+  int a = id / nf, x = id % nf;
+  double fo = a == 0 ? f0 : (a == 1 ? f1 : f2);
+  double co = a == 0 ? o0 : (a == 1 ? o1 : o2);
+  double lu = (double)x * dxf + fo + dxf / 2 - co;
+  double l = fmod(lu, period);
+  if (l < 0) l += period;
+  double u = l / dxc - 0.5;
+  double f = floor(u);
+  frac[id] = (T)(u - f);
+  ubase[id] = (int)f + (int)floor(lu / period) * nc;
+}
+
+inline unsigned nblk(size_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+// --- the multi-level field algebra ------------------------------------------------
+
+template <typename T>
+struct ModEngine {
+  using C = typename V2m<T>::type;
+  Context &ctx;
+  explicit ModEngine(Context &c) : ctx(c) {}
+
+  int nl() const { return (int)ctx.levels.size(); }
+  Level &lev(int l) { return *ctx.levels[l]; }
+  size_t elems(int l) { return 2 * lev(l).ncomplex(); }
+  double scale(int l) { return 1.0 / std::pow((double)lev(l).n, 1.5); }
+
+  struct Field {
+    std::vector<std::unique_ptr<DevBuf>> b;
+    std::vector<char> fourier;
+  };
+
+  void alloc(Field &f) {
+    f.b.resize(nl());
+    f.fourier.assign(nl(), 1);
+    for (int l = 0; l < nl(); ++l) {
+      if (!f.b[l]) f.b[l] = std::make_unique<DevBuf>();
+      f.b[l]->ensure(elems(l) * sizeof(T));
+    }
+  }
+  T *ptr(Field &f, int l) { return f.b[l]->template as<T>(); }
+  void zero(Field &f, int l) { GIC_CUDA(cudaMemsetAsync(f.b[l]->ptr, 0, elems(l) * sizeof(T), ctx.stream)); }
+  void copy(Field &dst, const Field &src) {
+    alloc(dst);
+    for (int l = 0; l < nl(); ++l) {
+      GIC_CUDA(cudaMemcpyAsync(dst.b[l]->ptr, src.b[l]->ptr, elems(l) * sizeof(T), cudaMemcpyDeviceToDevice,
+                               ctx.stream));
+      dst.fourier[l] = src.fourier[l];
+    }
+  }
+  void copy_level(DevBuf &dst, const DevBuf &src, int l) {
+    dst.ensure(elems(l) * sizeof(T));
+    GIC_CUDA(cudaMemcpyAsync(dst.ptr, src.ptr, elems(l) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
+  }
+  void to_fourier(T *p, int l) { fft_r2c_3d<T>(ctx, p, lev(l).n, scale(l)); }
+  void to_real(T *p, int l) { fft_c2r_3d<T>(ctx, p, lev(l).n, scale(l)); }
+  void to_fourier(Field &f, int l) {
+    if (!f.fourier[l]) to_fourier(ptr(f, l), l);
+    f.fourier[l] = 1;
+  }
+  void to_real(Field &f, int l) {
+    if (f.fourier[l]) to_real(ptr(f, l), l);
+    f.fourier[l] = 0;
+  }
+
+  // family filter of level l (filterfamily.hpp:106-140) evaluated on grid g
+  void add_filter_factors(TableSpec &sp, int l) {
+    for (int m = 0; m < l; ++m) sp.hp_cut[sp.nhp++] = kcut(m);
+    if (l < nl() - 1) sp.lp_cut[sp.nlp++] = kcut(l);
+  }
+  double kcut(int l) { return 0.3 * ((double)lev(l).n * lev(l).kmin()); }
+
+  DevBuf tab;
+  void table(const TableSpec &sp0, int g) {
+    long long half = lev(g).n / 2, nq = 3 * half * half + 1;
+    tab.ensure(nq * sizeof(double));
+    TableSpec sp = sp0;
+    sp.kmin = lev(g).kmin();
+    k_mod_table<<<nblk(nq), 256, 0, ctx.stream>>>(tab.template as<double>(), nq, sp);
+    launched();
+  }
+
+  void mul_table(T *p, int g) {
+    k_mul_table<T><<<nblk(lev(g).ncomplex()), 256, 0, ctx.stream>>>(reinterpret_cast<C *>(p), lev(g).n,
+                                                                    tab.template as<double>());
+    launched();
+  }
+  void axpy(T *a, const T *b, double c, int l) {
+    k_axpy<T><<<nblk(elems(l)), 256, 0, ctx.stream>>>(a, b, c, elems(l));
+    launched();
+  }
+  void scale_by(T *a, double c, int l) {
+    k_scale<T><<<nblk(elems(l)), 256, 0, ctx.stream>>>(a, c, elems(l));
+    launched();
+  }
+
+  double inner(Field &a, Field &b) {
+    const int blocks = 128;
+    ctx.reduce.ensure(blocks * sizeof(double) * 8);
+    double total = 0;
+    std::vector<double> h(blocks);
+    for (int l = 0; l < nl(); ++l) {
+      to_fourier(a, l);
+      to_fourier(b, l);
+      k_inner<T><<<blocks, 256, 0, ctx.stream>>>(ptr(a, l), ptr(b, l), lev(l).n, ctx.reduce.template as<double>());
+      launched();
+      GIC_CUDA(cudaMemcpyAsync(h.data(), ctx.reduce.ptr, blocks * sizeof(double), cudaMemcpyDeviceToHost,
+                               ctx.stream));
+      GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+      for (double v : h) total += v;
+    }
+    return total;
+  }
+
+  // window of level wl on the cells of level l, per axis (window.hpp)
+  DevBuf masks;
+  void window_masks(int l, int wl) {
+    const Level &L = lev(l), &W = lev(wl);
+    double P = L.periodic;
+    std::vector<unsigned char> m(3 * (size_t)L.n);
+    for (int a = 0; a < 3; ++a) {
+      auto wrap = [P](double v) {
+        if (v < 0) v += P;
+        if (v >= P) v -= P;
+        return v;
+      };
+      double lo = wrap(W.x0[a]), hi = wrap(W.x0[a] + W.box);
+      for (int i = 0; i < L.n; ++i) {
+        double c = (double)i * L.dx + L.x0[a] + L.dx / 2;
+        bool in = lo <= hi ? (c < hi && c >= lo) : (c < hi || c >= lo);
+        m[(size_t)a * L.n + i] = in ? 1 : 0;
+      }
+    }
+    masks.ensure(m.size());
+    GIC_CUDA(cudaMemcpyAsync(masks.ptr, m.data(), m.size(), cudaMemcpyHostToDevice, ctx.stream));
+    GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+  }
+  void mask(T *real, int l, int zero_inside) {
+    int n = lev(l).n;
+    unsigned char *m = masks.template as<unsigned char>();
+    k_mask<T><<<nblk(lev(l).ncells()), 256, 0, ctx.stream>>>(real, n, m, m + n, m + 2 * n, zero_inside);
+    launched();
+  }
+
+  // f_l applied in Fourier space
+  void apply_family(T *p, int l, int power) {
+    TableSpec sp{};
+    sp.power = power;
+    sp.scalar = 1.0;
+    add_filter_factors(sp, l);
+    table(sp, l);
+    mul_table(p, l);
+  }
+
+  DevBuf tmp_src;
+  double level_weight(int l) {
+    double r = lev(l).dx / lev(0).dx;
+    return r * r * r;
+  }
+
+  void cross_term_impl(T *target_real, int t, const T *source_k, int s) {
+    TableSpec sp{};
+    sp.power = 1;
+    add_filter_factors(sp, t);
+    add_filter_factors(sp, s);
+    sp.scalar = std::sqrt(level_weight(t) / level_weight(s));
+    tmp_src.ensure(elems(s) * sizeof(T));
+    GIC_CUDA(cudaMemcpyAsync(tmp_src.ptr, source_k, elems(s) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
+    table(sp, s);
+    mul_table(tmp_src.template as<T>(), s);
+    to_real(tmp_src.template as<T>(), s);
+    if (s < t) {
+      const T *src[1] = {tmp_src.template as<T>()};
+      T *dst[1] = {target_real};
+      interp_add<T, 1>(ctx, lev(s), src, lev(t), dst);
+    } else {
+      const Level &F = lev(s), &Cl = lev(t);
+      int r = (int)std::lround(Cl.dx / F.dx);
+      int sx = (int)std::lround((F.x0[0] - Cl.x0[0]) / Cl.dx), sy = (int)std::lround((F.x0[1] - Cl.x0[1]) / Cl.dx),
+          sz = (int)std::lround((F.x0[2] - Cl.x0[2]) / Cl.dx);
+      size_t m = (size_t)(F.n / r);
+      k_subsample_add<T><<<nblk(m * m * m), 256, 0, ctx.stream>>>(tmp_src.template as<T>(), F.n, r, sx, sy, sz, target_real,
+                                                                  Cl.n);
+      launched();
+    }
+  }
+
+  // MultiLevelField::applyMetric (multilevelfield.hpp:344-384): X in Fourier space
+  void apply_metric(Field &X, Field &out, bool to_covector) {
+    for (int l = 0; l < nl(); ++l) to_fourier(X, l);
+    alloc(out);
+    DevBuf inw;
+    for (int t = 0; t < nl(); ++t) {
+      T *R = ptr(out, t);
+      GIC_CUDA(cudaMemcpyAsync(R, ptr(X, t), elems(t) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
+      if (to_covector && t < nl() - 1) {
+        window_masks(t, t + 1);
+        inw.ensure(elems(t) * sizeof(T));
+        T *I = inw.template as<T>();
+        // applyFilterInWindow(f, window, windowFirst = true)
+        GIC_CUDA(cudaMemcpyAsync(I, R, elems(t) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
+        to_real(I, t);
+        mask(I, t, 0);
+        to_fourier(I, t);
+        apply_family(I, t, 1);
+        to_real(R, t);
+        mask(R, t, 1);
+        to_fourier(R, t);
+        axpy(R, I, 1.0, t);
+        // applyFilterInWindow(f, window, windowFirst = false)
+        GIC_CUDA(cudaMemcpyAsync(I, R, elems(t) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
+        apply_family(I, t, 1);
+        to_real(I, t);
+        mask(I, t, 0);
+        to_real(R, t);
+        mask(R, t, 1);
+        axpy(R, I, 1.0, t);
+      } else {
+        apply_family(R, t, 2);
+        to_real(R, t);
+      }
+      for (int s = 0; s < nl(); ++s)
+        if (s != t) cross_term_impl(R, t, ptr(X, s), s);
+      to_fourier(R, t);
+      out.fourier[t] = 1;
+    }
+  }
+
+  // covector of one modification (kind 0 overdensity, 1..3 velocity x,y,z)
+  DevBuf cells;
+  void covector(Field &out, int kind, const unsigned long long *flagged, size_t count) {
+    int F = nl() - 1;
+    alloc(out);
+    for (int l = 0; l < nl(); ++l) zero(out, l);
+    cells.ensure(count * sizeof(unsigned long long));
+    GIC_CUDA(cudaMemcpyAsync(cells.ptr, flagged, count * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                             ctx.stream));
+    double w = 1.0 / (double)count;
+    double a = -w / 12. / lev(F).dx, b = w * 2. / 3. / lev(F).dx;
+    k_localise<T><<<nblk(count), 256, 0, ctx.stream>>>(ptr(out, F), lev(F).n, cells.template as<unsigned long long>(), count,
+                                                      kind == 0 ? 0 : 1, kind == 0 ? 0 : kind - 1, w, a, b);
+    launched();
+    out.fourier[F] = 0;
+    to_fourier(out, F);
+    if (F > 0) {
+      to_real(out, F);
+      for (int l = F - 1; l >= 0; --l) {
+        out.fourier[l] = 0;
+        deinterpolate(ptr(out, l + 1), l + 1, ptr(out, l), l);
+      }
+    }
+    for (int l = 0; l < nl(); ++l) {
+      double wr = level_weight(l) / level_weight(F);
+      if (wr != 1.0) scale_by(ptr(out, l), wr, l);
+      to_fourier(out, l);
+      apply_family(ptr(out, l), l, 1);
+      // multiply by sqrt(P_dm) (and -v/k^2 for velocities)
+      build_sqrtp_dm(l);
+      TableSpec sp{};
+      sp.power = 1;
+      sp.scalar = 1.0;
+      sp.sqrtp = lev(l).sqrtp_dm.template as<double>();
+      sp.vel = kind == 0 ? 0.0 : velocity_ratio();
+      table(sp, l);
+      mul_table(ptr(out, l), l);
+    }
+  }
+  double velocity_ratio();
+  void build_sqrtp_dm(int l);
+
+  // transpose tricubic: fine real (level f) / r^3 added into coarse real (level c)
+  DevBuf geom, t1, t2, t3;
+  void deinterpolate(const T *fine, int f, T *coarse, int c) {
+    const Level &Fl = lev(f), &Cl = lev(c);
+    int nf = Fl.n;
+    int r = (int)std::lround(Cl.dx / Fl.dx);
+    T scale = (T)(1.0 / ((double)r * r * r));
+    geom.ensure(3 * (size_t)nf * (sizeof(int) + sizeof(T)));
+    int *ub = geom.template as<int>();
+    T *fr = reinterpret_cast<T *>(ub + 3 * nf);
+    k_axes_geom<T><<<nblk(3 * nf, 128), 128, 0, ctx.stream>>>(nf, Fl.dx, Fl.x0[0], Fl.x0[1], Fl.x0[2], Cl.x0[0],
+                                                              Cl.x0[1], Cl.x0[2], Cl.dx, Cl.periodic, Cl.n, ub, fr);
+    launched();
+    std::vector<int> h(3 * nf);
+    GIC_CUDA(cudaMemcpyAsync(h.data(), ub, 3 * nf * sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
+    GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+    int c0[3], cnt[3];
+    for (int a = 0; a < 3; ++a) {
+      c0[a] = h[(size_t)a * nf] - 1;
+      cnt[a] = h[(size_t)a * nf + nf - 1] + 3 - c0[a];
+    }
+    const long long frs = 2 * (nf / 2 + 1);
+    // pass x: fine (nf, nf, nf) padded -> t1 (cnt0, nf, nf)
+    t1.ensure((size_t)cnt[0] * nf * nf * sizeof(T));
+    GIC_CUDA(cudaMemsetAsync(t1.ptr, 0, (size_t)cnt[0] * nf * nf * sizeof(T), ctx.stream));
+    k_deinterp_pass<T><<<nblk((size_t)nf * nf), 256, 0, ctx.stream>>>(
+        fine, (long long)nf * frs, frs, t1.template as<T>(), (long long)nf * nf, nf, 0, nf, nf, nf, nf, ub, fr, c0[0], cnt[0],
+        scale);
+    // pass y: t1 (cnt0, nf, nf) -> t2 (cnt0, cnt1, nf)
+    t2.ensure((size_t)cnt[0] * cnt[1] * nf * sizeof(T));
+    GIC_CUDA(cudaMemsetAsync(t2.ptr, 0, (size_t)cnt[0] * cnt[1] * nf * sizeof(T), ctx.stream));
+    k_deinterp_pass<T><<<nblk((size_t)cnt[0] * nf), 256, 0, ctx.stream>>>(
+        t1.template as<T>(), (long long)nf * nf, nf, t2.template as<T>(), (long long)cnt[1] * nf, nf, 1, cnt[0], nf, nf, nf, ub + nf,
+        fr + nf, c0[1], cnt[1], (T)1);
+    // pass z: t2 (cnt0, cnt1, nf) -> t3 (cnt0, cnt1, cnt2)
+    t3.ensure((size_t)cnt[0] * cnt[1] * cnt[2] * sizeof(T));
+    GIC_CUDA(cudaMemsetAsync(t3.ptr, 0, (size_t)cnt[0] * cnt[1] * cnt[2] * sizeof(T), ctx.stream));
+    k_deinterp_pass<T><<<nblk((size_t)cnt[0] * cnt[1]), 256, 0, ctx.stream>>>(
+        t2.template as<T>(), (long long)cnt[1] * nf, nf, t3.template as<T>(), (long long)cnt[1] * cnt[2], cnt[2], 2, cnt[0], cnt[1], nf,
+        nf, ub + 2 * nf, fr + 2 * nf, c0[2], cnt[2], (T)1);
+    size_t m = (size_t)cnt[0] * cnt[1] * cnt[2];
+    k_add_block<T><<<nblk(m), 256, 0, ctx.stream>>>(t3.template as<T>(), cnt[0], cnt[1], cnt[2], c0[0], c0[1], c0[2], coarse,
+                                                   Cl.n);
+    launched(4);
+  }
+};
+
+template <typename T>
+double ModEngine<T>::velocity_ratio() {
+  return velocity_to_offset_ratio(ctx.cosmo);
+}
+
+template <typename T>
+void ModEngine<T>::build_sqrtp_dm(int l) {
+  build_sqrtp_table_species(ctx, lev(l), 1);
+}
+
+// --- the modification manager ------------------------------------------------------
+
+template <typename T>
+static void noise_field(ModEngine<T> &E, typename ModEngine<T>::Field &W) {
+  E.alloc(W);
+  for (int l = 0; l < E.nl(); ++l) {
+    if (!E.lev(l).have_noise) fail(GIC_ERR_NOT_READY, "white noise has not been drawn");
+    E.copy_level(*W.b[l], E.lev(l).noise, l);
+    W.fourier[l] = 1;
+  }
+}
+
+template <typename T>
+static double current_value(Context &ctx, const ModRequest &m) {
+  ModEngine<T> E(ctx);
+  typename ModEngine<T>::Field W, a;
+  noise_field(E, W);
+  E.covector(a, m.kind, m.cells.data(), m.cells.size());
+  return E.inner(a, W);
+}
+
+template <typename T>
+static double chi2_of_noise(Context &ctx) {
+  ModEngine<T> E(ctx);
+  typename ModEngine<T>::Field W, cov;
+  noise_field(E, W);
+  E.apply_metric(W, cov, true);
+  return E.inner(cov, W);
+}
+
+template <typename T>
+static void apply_mods(Context &ctx, double *chi2_before, double *chi2_after) {
+  ModEngine<T> E(ctx);
+  using F = typename ModEngine<T>::Field;
+  int n = (int)ctx.mods.size();
+  if (chi2_before) *chi2_before = chi2_of_noise<T>(ctx);
+  F W;
+  noise_field(E, W);
+  std::vector<F> alpha(n), vec(n);
+  std::vector<double> b(n), t(n);
+  for (int i = 0; i < n; ++i) {
+    E.covector(alpha[i], ctx.mods[i].kind, ctx.mods[i].cells.data(), ctx.mods[i].cells.size());
+    E.apply_metric(alpha[i], vec[i], false);
+    b[i] = E.inner(alpha[i], W);
+    t[i] = ctx.mods[i].target;
+  }
+  std::vector<double> G((size_t)n * n);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) G[(size_t)i * n + j] = E.inner(alpha[i], vec[j]);
+  // Gram-Schmidt in the order of modificationmanager.hpp:288-312, on coefficient
+  // vectors: row i of L holds a'_i = sum_k L[i][k] a_k
+  std::vector<double> L((size_t)n * n, 0.0);
+  auto ip = [&](const double *x, const double *y) {
+    double s = 0;
+    for (int k = 0; k < n; ++k)
+      for (int m = 0; m < n; ++m) s += x[k] * y[m] * G[(size_t)k * n + m];
+    return s;
+  };
+  for (int i = 0; i < n; ++i) {
+    double *li = &L[(size_t)i * n];
+    li[i] = 1.0;
+    for (int j = 0; j < i; ++j) {
+      double *lj = &L[(size_t)j * n];
+      double r = ip(li, lj);
+      for (int k = 0; k < n; ++k) li[k] -= r * lj[k];
+      t[i] -= r * t[j];
+    }
+    double nrm = std::sqrt(ip(li, li));
+    for (int k = 0; k < n; ++k) li[k] /= nrm;
+    t[i] /= nrm;
+  }
+  std::vector<double> coef(n, 0.0);
+  for (int i = 0; i < n; ++i) {
+    double existing = 0;
+    for (int k = 0; k < n; ++k) existing += L[(size_t)i * n + k] * b[k];
+    double d = t[i] - existing;
+    for (int k = 0; k < n; ++k) coef[k] += d * L[(size_t)i * n + k];
+  }
+  for (int l = 0; l < E.nl(); ++l) {
+    for (int k = 0; k < n; ++k) E.axpy(E.ptr(W, l), E.ptr(vec[k], l), coef[k], l);
+    E.copy_level(E.lev(l).noise, *W.b[l], l);
+    E.lev(l).have_fields = false;
+  }
+  GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+  if (chi2_after) *chi2_after = chi2_of_noise<T>(ctx);
+}
+
+double modification_value(Context &ctx, const ModRequest &m) {
+  return ctx.dbl() ? current_value<double>(ctx, m) : current_value<float>(ctx, m);
+}
+
+double noise_chi2(Context &ctx) { return ctx.dbl() ? chi2_of_noise<double>(ctx) : chi2_of_noise<float>(ctx); }
+
+void apply_modifications(Context &ctx, double *chi2_before, double *chi2_after) {
+  if (ctx.dbl())
+    apply_mods<double>(ctx, chi2_before, chi2_after);
+  else
+    apply_mods<float>(ctx, chi2_before, chi2_after);
+}
+
+}  // namespace gic

@@ -56,12 +56,51 @@ __global__ void k_interp_axes(int nf, double dxf, double f0, double f1, double f
 // Separable form: a CTA owns one fine x plane and TY fine y rows.  It first
 // contracts the four coarse x planes of its stencil into a shared tile
 // P[cy][cz] (per field), then every fine (y, z) is a 4 x 4 contraction of P.
-template <typename T, int TY>
-__global__ void __launch_bounds__(256) k_interp_add4_sep(const T *__restrict__ c0, const T *__restrict__ c1,
-                                                         const T *__restrict__ c2, const T *__restrict__ c3, int nc,
-                                                         int wrap, const int *__restrict__ base,
-                                                         const T *__restrict__ frac, const int *__restrict__ ubase,
-                                                         T *f0, T *f1, T *f2, T *f3, int nf, int maxcz) {
+template <typename T, int NF>
+struct FieldPtrs {
+  const T *src[NF];
+  T *dst[NF];
+};
+
+// Direct form (any geometry): one thread per fine cell, 64 coarse values per field.
+template <typename T, int NF>
+__global__ void __launch_bounds__(256) k_interp_add_direct(FieldPtrs<T, NF> fp, int nc, int wrap,
+                                                           const int *__restrict__ base, const T *__restrict__ frac,
+                                                           int nf) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t m = (size_t)nf * nf * nf;
+  if (i >= m) return;
+  size_t row = i / nf;
+  int pos[3] = {(int)(row / nf), (int)(row % nf), (int)(i % nf)};
+  T w[3][4];
+  int idx[3][4];
+  for (int a = 0; a < 3; ++a) {
+    catmull_rom<T>(__ldg(frac + a * nf + pos[a]), w[a]);
+    int b0 = __ldg(base + a * nf + pos[a]);
+    for (int c = 0; c < 4; ++c) {
+      int v = b0 - 1 + c;
+      idx[a][c] = wrap ? ((v % nc) + nc) % nc : min(max(v, 0), nc - 1);
+    }
+  }
+  const size_t rs = (size_t)(2 * (nc / 2 + 1));
+  T s[NF];
+  for (int f = 0; f < NF; ++f) s[f] = 0;
+  for (int a = 0; a < 4; ++a)
+    for (int b = 0; b < 4; ++b) {
+      size_t rowi = ((size_t)idx[0][a] * nc + idx[1][b]) * rs;
+      for (int c = 0; c < 4; ++c) {
+        T wt = w[0][a] * w[1][b] * w[2][c];
+        for (int f = 0; f < NF; ++f) s[f] += wt * __ldg(fp.src[f] + rowi + idx[2][c]);
+      }
+    }
+  size_t dst = row * (size_t)(2 * (nf / 2 + 1)) + pos[2];
+  for (int f = 0; f < NF; ++f) fp.dst[f][dst] += s[f];
+}
+
+template <typename T, int NF, int TY>
+__global__ void __launch_bounds__(256) k_interp_add_sep(FieldPtrs<T, NF> fp, int nc, int wrap,
+                                                        const int *__restrict__ base, const T *__restrict__ frac,
+                                                        const int *__restrict__ ubase, int nf, int maxcz) {
   extern __shared__ __align__(16) unsigned char smraw[];
   T *P = reinterpret_cast<T *>(smraw);
   const int x = blockIdx.y;
@@ -82,19 +121,17 @@ __global__ void __launch_bounds__(256) k_interp_add4_sep(const T *__restrict__ c
   const int tile = ny * nz;
   for (int e = threadIdx.x; e < tile; e += blockDim.x) {
     int cy = cw(cy0 + e / nz), cz = cw(cz0 + e % nz);
-    T v0 = 0, v1 = 0, v2 = 0, v3 = 0;
+    T v[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) v[f] = 0;
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
       size_t k = ((size_t)ixw[a] * nc + cy) * rs + cz;
-      v0 += wx[a] * __ldg(c0 + k);
-      v1 += wx[a] * __ldg(c1 + k);
-      v2 += wx[a] * __ldg(c2 + k);
-      v3 += wx[a] * __ldg(c3 + k);
+#pragma unroll
+      for (int f = 0; f < NF; ++f) v[f] += wx[a] * __ldg(fp.src[f] + k);
     }
-    P[e] = v0;
-    P[tile + e] = v1;
-    P[2 * tile + e] = v2;
-    P[3 * tile + e] = v3;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) P[f * tile + e] = v[f];
   }
   __syncthreads();
   const size_t frs = (size_t)(2 * (nf / 2 + 1));
@@ -106,101 +143,35 @@ __global__ void __launch_bounds__(256) k_interp_add4_sep(const T *__restrict__ c
     catmull_rom<T>(__ldg(frac + 2 * nf + z), wz);
     int py = __ldg(ubase + nf + y) - 1 - cy0;
     int pz = __ldg(ubase + 2 * nf + z) - 1 - cz0;
-    T s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+    T s[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) s[f] = 0;
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-      T q0 = 0, q1 = 0, q2 = 0, q3 = 0;
       int rowp = (py + b) * nz + pz;
+      T q[NF];
+#pragma unroll
+      for (int f = 0; f < NF; ++f) q[f] = 0;
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        q0 += wz[c] * P[rowp + c];
-        q1 += wz[c] * P[tile + rowp + c];
-        q2 += wz[c] * P[2 * tile + rowp + c];
-        q3 += wz[c] * P[3 * tile + rowp + c];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) q[f] += wz[c] * P[f * tile + rowp + c];
       }
-      s0 += wy[b] * q0;
-      s1 += wy[b] * q1;
-      s2 += wy[b] * q2;
-      s3 += wy[b] * q3;
+#pragma unroll
+      for (int f = 0; f < NF; ++f) s[f] += wy[b] * q[f];
     }
     size_t dst = ((size_t)x * nf + y) * frs + z;
-    f0[dst] += s0;
-    f1[dst] += s1;
-    f2[dst] += s2;
-    f3[dst] += s3;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) fp.dst[f][dst] += s[f];
   }
-}
-
-template <typename T>
-__global__ void __launch_bounds__(256) k_interp_add4(const T *__restrict__ c0, const T *__restrict__ c1,
-                                                     const T *__restrict__ c2, const T *__restrict__ c3, int nc,
-                                                     int wrap, const int *__restrict__ base,
-                                                     const T *__restrict__ frac, T *f0, T *f1, T *f2, T *f3,
-                                                     int nf) {
-  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  size_t m = (size_t)nf * nf * nf;
-  if (i >= m) return;
-  size_t row = i / nf;
-  int z = (int)(i % nf), y = (int)(row % nf), x = (int)(row / nf);
-  int pos[3] = {x, y, z};
-  T w[3][4];
-  int idx[3][4];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    catmull_rom<T>(__ldg(frac + a * nf + pos[a]), w[a]);
-    int b0 = __ldg(base + a * nf + pos[a]);
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      int v = b0 - 1 + c;
-      if (wrap) {
-        v = v < 0 ? v + nc : (v >= nc ? v - nc : v);
-      } else {
-        v = min(max(v, 0), nc - 1);
-      }
-      idx[a][c] = v;
-    }
-  }
-  const size_t rs = (size_t)(2 * (nc / 2 + 1));
-  T s0 = 0, s1 = 0, s2 = 0, s3 = 0;
-#pragma unroll
-  for (int a = 0; a < 4; ++a) {
-    T p0 = 0, p1 = 0, p2 = 0, p3 = 0;
-#pragma unroll
-    for (int b = 0; b < 4; ++b) {
-      size_t rowi = ((size_t)idx[0][a] * nc + idx[1][b]) * rs;
-      T q0 = 0, q1 = 0, q2 = 0, q3 = 0;
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        size_t k = rowi + idx[2][c];
-        T wc = w[2][c];
-        q0 += wc * __ldg(c0 + k);
-        q1 += wc * __ldg(c1 + k);
-        q2 += wc * __ldg(c2 + k);
-        q3 += wc * __ldg(c3 + k);
-      }
-      T wb = w[1][b];
-      p0 += wb * q0;
-      p1 += wb * q1;
-      p2 += wb * q2;
-      p3 += wb * q3;
-    }
-    T wa = w[0][a];
-    s0 += wa * p0;
-    s1 += wa * p1;
-    s2 += wa * p2;
-    s3 += wa * p3;
-  }
-  size_t dst = row * (size_t)(2 * (nf / 2 + 1)) + z;
-  f0[dst] += s0;
-  f1[dst] += s1;
-  f2[dst] += s2;
-  f3[dst] += s3;
 }
 
 }  // namespace
 
-template <typename T>
-void interp_add4(Context &ctx, const Level &coarse, T *const src[4], Level &fine) {
+// Add the tricubic interpolation of NF real fields of grid `coarse` onto the
+// NF real fields of grid `fine` (any two levels, coarse cells larger).
+template <typename T, int NF>
+void interp_add(Context &ctx, const Level &coarse, const T *const *src, const Level &fine, T *const *dst) {
   size_t m = fine.ncells();
   int wrap = (coarse.box == coarse.periodic) ? 1 : 0;
   int nf = fine.n;
@@ -212,29 +183,39 @@ void interp_add4(Context &ctx, const Level &coarse, T *const src[4], Level &fine
                                                                 coarse.x0[0], coarse.x0[1], coarse.x0[2], coarse.dx,
                                                                 coarse.periodic, coarse.n, base, frac, ubase);
   launched();
-  // coarse cells spanned by the fine grid along one axis, plus the stencil
   double ratio = fine.dx / coarse.dx;
   int span = (int)std::ceil(nf * ratio) + 6;
   constexpr int TY = 8;
   int ny = (int)std::ceil(TY * ratio) + 6;
-  size_t smem = (size_t)4 * ny * span * sizeof(T);
-  if (ratio <= 1.0 && span <= nf + 6 && smem <= 96 * 1024) {
-    GIC_CUDA(cudaFuncSetAttribute((const void *)k_interp_add4_sep<T, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem));
-    dim3 grid((nf + TY - 1) / TY, nf);
-    k_interp_add4_sep<T, TY><<<grid, 256, smem, ctx.stream>>>(src[0], src[1], src[2], src[3], coarse.n, wrap, base,
-                                                              frac, ubase, fine.field[0].as<T>(),
-                                                              fine.field[1].as<T>(), fine.field[2].as<T>(),
-                                                              fine.field[3].as<T>(), nf, span);
-  } else {
-    k_interp_add4<T><<<(unsigned)((m + 255) / 256), 256, 0, ctx.stream>>>(
-        src[0], src[1], src[2], src[3], coarse.n, wrap, base, frac, fine.field[0].as<T>(), fine.field[1].as<T>(),
-        fine.field[2].as<T>(), fine.field[3].as<T>(), nf);
+  size_t smem = (size_t)NF * ny * span * sizeof(T);
+  FieldPtrs<T, NF> fp;
+  for (int f = 0; f < NF; ++f) {
+    fp.src[f] = src[f];
+    fp.dst[f] = dst[f];
   }
-  launched();
+  if (ratio <= 1.0 && smem <= 96 * 1024) {
+    GIC_CUDA(cudaFuncSetAttribute((const void *)k_interp_add_sep<T, NF, TY>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((nf + TY - 1) / TY, nf);
+    k_interp_add_sep<T, NF, TY><<<grid, 256, smem, ctx.stream>>>(fp, coarse.n, wrap, base, frac, ubase, nf, span);
+    launched();
+  } else {
+    k_interp_add_direct<T, NF><<<(unsigned)((m + 255) / 256), 256, 0, ctx.stream>>>(fp, coarse.n, wrap, base, frac,
+                                                                                   nf);
+    launched();
+  }
+}
+
+template <typename T>
+void interp_add4(Context &ctx, const Level &coarse, T *const src[4], Level &fine) {
+  T *dst[4] = {fine.field[0].as<T>(), fine.field[1].as<T>(), fine.field[2].as<T>(), fine.field[3].as<T>()};
+  const T *s[4] = {src[0], src[1], src[2], src[3]};
+  interp_add<T, 4>(ctx, coarse, s, fine, dst);
 }
 
 template void interp_add4<float>(Context &, const Level &, float *const[4], Level &);
 template void interp_add4<double>(Context &, const Level &, double *const[4], Level &);
+template void interp_add<float, 1>(Context &, const Level &, const float *const *, const Level &, float *const *);
+template void interp_add<double, 1>(Context &, const Level &, const double *const *, const Level &, double *const *);
 
 }  // namespace gic

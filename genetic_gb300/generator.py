@@ -35,7 +35,8 @@ class ICGenerator:
             raise _lib.GicError(st, lib.gic_last_error(None).decode())
         self._ctx = ctx
         self.precision = precision
-        # genetIC's defaults (genetIC/src/ic.hpp:200-210)
+        # genetIC's defaults for Om, Ob, h, ns (genetIC/src/ic.hpp:200-210); Ol, s8
+        # and zin have no default there and are always set by a paramfile
         self.cosmo = dict(omega_m=0.3, omega_lambda=0.7, omega_b=0.0, hubble=0.701, sigma8=0.8, ns=0.96,
                           redshift=0.0)
         self.levels = []  # (box, n, offset)
@@ -44,6 +45,8 @@ class ICGenerator:
         self.base_dir = '.'
         self._drawn = False
         self._done = False
+        self.centre_point = (0.0, 0.0, 0.0)
+        self.flagged = None  # flagged cells of the finest level (linear indices)
 
     # -- lifetime --------------------------------------------------------------
     def close(self):
@@ -153,6 +156,67 @@ class ICGenerator:
     def seedfourier_reverse(self, seed):
         self._seed(seed, _lib.GIC_SEED_FOURIER_REVERSE)
 
+    # -- cell selection (ic.hpp:1458-1583) ------------------------------------------
+    def centre(self, x, y, z):
+        self.centre_point = (float(x), float(y), float(z))
+
+    def _select(self, inside):
+        """Flag the cells of the finest level whose wrapped offset from the centre passes `inside`."""
+        box, n, off = self.levels[-1]
+        period = self.levels[0][0]
+        dx = box / n
+        d = []
+        for a in range(3):
+            x = np.arange(n) * dx + off[a] + dx / 2 - self.centre_point[a]
+            x = np.where(x > period / 2, x - period, x)
+            x = np.where(x < -period / 2, x + period, x)
+            d.append(x)
+        X, Y, Z = np.meshgrid(d[0], d[1], d[2], indexing='ij')
+        self.flagged = np.ascontiguousarray(np.flatnonzero(inside(X, Y, Z).ravel()), dtype=np.uint64)
+
+    def select_sphere(self, radius):
+        r2 = float(np.float32(radius) * np.float32(radius))
+        self._select(lambda X, Y, Z: X * X + Y * Y + Z * Z < r2)
+
+    def select_cube(self, side):
+        h = float(np.float32(side) / np.float32(2))
+        self._select(lambda X, Y, Z: (np.abs(X) < h) & (np.abs(Y) < h) & (np.abs(Z) < h))
+
+    # -- modifications (modificationmanager.hpp) ---------------------------------------
+    _KINDS = {'overdensity': _lib.GIC_MOD_OVERDENSITY, 'vx': _lib.GIC_MOD_VX, 'vy': _lib.GIC_MOD_VY,
+              'vz': _lib.GIC_MOD_VZ}
+
+    def _cells(self):
+        if self.flagged is None or len(self.flagged) == 0:
+            raise RuntimeError('Linear modifications use exclusively information from the highest resolution grid '
+                               'but no cells have been flagged on this grid.')
+        return self.flagged.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong)), len(self.flagged)
+
+    def calculate(self, name):
+        self.draw()
+        v = ctypes.c_double()
+        cells, n = self._cells()
+        self._call('gic_calculate', self._KINDS[name], cells, n, ctypes.byref(v))
+        return v.value
+
+    def modify(self, name, kind, target):
+        """`modify name absolute|relative target`; genetIC parses the target as a float (ic.hpp:1613)."""
+        self.draw()
+        rel = {'relative': 1, 'absolute': 0}[kind.lower()]
+        cells, n = self._cells()
+        self._call('gic_add_modification', self._KINDS[name], cells, n, float(np.float32(target)), rel)
+        self._nmods = getattr(self, '_nmods', 0) + 1
+
+    def clear_modifications(self):
+        self._call('gic_clear_modifications')
+        self._nmods = 0
+
+    def apply_modifications(self):
+        before, after = ctypes.c_double(), ctypes.c_double()
+        self._call('gic_apply_modifications', ctypes.byref(before), ctypes.byref(after))
+        self.last_chi2 = (before.value, after.value)
+        return before.value, after.value
+
     # -- realisation -------------------------------------------------------------
     def draw(self):
         if self._drawn:
@@ -162,11 +226,18 @@ class ICGenerator:
         self._call('gic_draw_noise', self.seed, self.seed_mode)
         self._drawn = True
 
-    def done(self):
-        """Draw the noise if needed, apply P(k), build the Zel'dovich fields and particles."""
+    def done(self, apply_modifications=True):
+        """Draw the noise if needed, apply the queued modifications, then P(k), the
+        Zel'dovich fields and particles (ic.hpp:1633-1648)."""
         self.draw()
+        self._modified = False
+        if apply_modifications and self._has_modifications():
+            self.apply_modifications()
         self._call('gic_zeldovich', 1)
         self._done = True
+
+    def _has_modifications(self):
+        return getattr(self, '_nmods', 0) > 0
 
     def chi2(self):
         self.draw()
@@ -210,15 +281,17 @@ _COMMANDS = {
     'random_seed_serial': 'random_seed_serial', 'seedfourier': 'random_seed_serial',
     'random_seed_real_space': 'random_seed_real_space', 'seed': 'random_seed_real_space',
     'seedfourier_reverse': 'seedfourier_reverse', 'done': 'done', 'chi2': 'chi2',
+    'centre': 'centre', 'select_sphere': 'select_sphere', 'select_cube': 'select_cube',
+    'calculate': 'calculate', 'modify': 'modify', 'clear_modifications': 'clear_modifications',
+    'apply_modifications': 'apply_modifications',
 }
 # output-side commands handled by genetIC's own writers; accepted and ignored here
 _IGNORED = {'outname', 'outdir', 'outformat', 'dump_grid', 'dump_ps', 'idfile', 'dump_idfile'}
 
 
-def run_paramfile(path, precision='fp64', device=0):
-    """Run a genetIC paramfile's realisation commands on the GPU; returns the ICGenerator."""
-    gen = ICGenerator(precision=precision, device=device)
-    gen.base_dir = os.path.dirname(os.path.abspath(path))
+def parse_paramfile(path):
+    """(line number, method, args) for each realisation command of a paramfile."""
+    out = []
     with open(path) as f:
         for lineno, line in enumerate(f, 1):
             line = line.split('#')[0].strip()
@@ -230,5 +303,15 @@ def run_paramfile(path, precision='fp64', device=0):
                 continue
             if cmd not in _COMMANDS:
                 raise ValueError('%s:%d: command %r is not on the GPU realisation path' % (path, lineno, cmd))
-            getattr(gen, _COMMANDS[cmd])(*args)
+            out.append((lineno, _COMMANDS[cmd], args))
+    return out
+
+
+def run_paramfile(path, precision='fp64', device=0):
+    """Run a genetIC paramfile's realisation commands on the GPU; returns the ICGenerator."""
+    commands = parse_paramfile(path)
+    gen = ICGenerator(precision=precision, device=device)
+    gen.base_dir = os.path.dirname(os.path.abspath(path))
+    for lineno, method, args in commands:
+        getattr(gen, method)(*args)
     return gen

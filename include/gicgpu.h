@@ -132,9 +132,34 @@ GIC_API int gic_fetch_particles(gic_ctx *ctx, int level, double *pos, double *ve
  * (fourier.hpp:479-518). */
 GIC_API int gic_fft(gic_ctx *ctx, int level, int what, int dir);
 
-/* chi^2 of the white noise: sum over modes of |w_k|^2 with Hermitian weights
- * (MultiLevelField::getChi2, multilevelfield.hpp:461-487). */
+/* chi^2 of the white noise <C^-1 w | w>: Hermitian-weighted sum of |w_k|^2 on
+ * one level; with zoom levels the covariance metric with windowed filters
+ * (MultiLevelField::getChi2, multilevelfield.hpp:461-487, 344-384). */
 GIC_API int gic_chi2(gic_ctx *ctx, double *chi2);
+
+/* modification kinds (genetIC/src/simulation/modifications/modificationmanager.hpp:160-192) */
+#define GIC_MOD_OVERDENSITY 0
+#define GIC_MOD_VX 1
+#define GIC_MOD_VY 2
+#define GIC_MOD_VZ 3
+
+/* Current value <a|w> of a modification's quantity (mean overdensity, or mean
+ * velocity component, over `cells`, the flagged cells of the finest level as
+ * linear indices) on the white noise.  Replaces
+ * ModificationManager::calculateCurrentValueByName (modificationmanager.hpp:37-45). */
+GIC_API int gic_calculate(gic_ctx *ctx, int kind, const unsigned long long *cells, size_t n, double *value);
+
+/* Queue a linear modification: absolute target, or relative (target times the
+ * current value).  Replaces ModificationManager::addModificationToList
+ * (modificationmanager.hpp:59-82). */
+GIC_API int gic_add_modification(gic_ctx *ctx, int kind, const unsigned long long *cells, size_t n, double target,
+                                 int relative);
+GIC_API int gic_clear_modifications(gic_ctx *ctx);
+
+/* Apply the queued modifications to the white noise (orthonormalised, with the
+ * covariance metric), returning chi^2 before and after.  Replaces
+ * ModificationManager::applyModifications (modificationmanager.hpp:90-125). */
+GIC_API int gic_apply_modifications(gic_ctx *ctx, double *chi2_before, double *chi2_after);
 
 /* Number of kernels this library has launched in the process so far. */
 GIC_API int gic_launch_count(unsigned long long *count);

@@ -85,6 +85,72 @@ def zoom_goldens():
                 np.savez_compressed(os.path.join(HERE, '%s_%s.npz' % (name, mode)), **grids)
 
 
+MOD_BASE = """Om 0.31
+Ol 0.69
+Ob 0
+hubble 0.68
+s8 0.81
+ns 0.965
+zin 99
+random_seed 8896131
+camb bbks.dat
+outname out
+outdir ./
+outformat tipsy
+basegrid 50.0 32
+"""
+MODS = {
+    # one level: 5 Mpc/h sphere at the centre, mean overdensity 0.05 and vx = 0
+    'mod1': """centre 25 25 25
+select_sphere 5
+calculate overdensity
+calculate vx
+modify overdensity absolute 0.05
+modify vx absolute 0
+chi2
+done
+dump_grid 0
+""",
+    # two levels: zoom factor 2 around the centre, 3 Mpc/h sphere, overdensity 0.05 and vx = vy = vz = 0
+    'mod2': """centre 25 25 25
+select_cube 10
+zoom_grid_with_origin_at 8 8 8 2 32
+centre 25 25 25
+select_sphere 3
+calculate overdensity
+calculate vx
+modify overdensity absolute 0.05
+modify vx absolute 0
+modify vy absolute 0
+modify vz absolute 0
+done
+dump_grid 0
+dump_grid 1
+""",
+}
+
+
+def mod_goldens():
+    import re
+    for name, tail in MODS.items():
+        with tempfile.TemporaryDirectory() as d:
+            write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+            open(os.path.join(d, 'paramfile.txt'), 'w').write(MOD_BASE + tail)
+            r = subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True, text=True)
+            log = r.stdout + r.stderr
+            vals = {}
+            for key, pat in (('overdensity', r'overdensity: calculated value = (\S+)'),
+                             ('vx', r'vx: calculated value = (\S+)'),
+                             ('chi2_post', r'Post-modification chi\^2 = (\S+)'),
+                             ('delta_chi2', r'Modification Delta chi\^2 = (\S+)')):
+                m = re.search(pat, log)
+                vals[key] = float(m.group(1))
+            nlev = 2 if name == 'mod2' else 1
+            grids = {'delta%d' % l: np.load(os.path.join(d, 'grid-%d.npy' % l)).astype(np.float32) for l in range(nlev)}
+            np.savez_compressed(os.path.join(HERE, '%s.npz' % name), **grids,
+                                **{k: np.array(v) for k, v in vals.items()})
+
+
 def main():
     for mode, cmd in (('serial', 'random_seed_serial'), ('parallel', 'random_seed'), ('real', 'random_seed_real_space')):
         with tempfile.TemporaryDirectory() as d:
@@ -103,3 +169,4 @@ def main():
 if __name__ == '__main__':
     main()
     zoom_goldens()
+    mod_goldens()

@@ -130,9 +130,13 @@ def test_bbks_table_format(tmp_path):
     assert np.all(np.diff(bbks(np.logspace(-3, 2, 50), 0.31, 0.049, 0.68)) < 0)
 
 
-def test_paramfile_runner_rejects_unknown_commands(tmp_path):
+def test_paramfile_parser(tmp_path):
     from genetic_gb300 import generator
     p = tmp_path / 'p.txt'
+    p.write_text('Om 0.3\n# comment\nbasegrid 50 32 # trailing\noutformat tipsy\nrandom_seed 5\ndone\n')
+    cmds = generator.parse_paramfile(str(p))
+    assert [c[1] for c in cmds] == ['Om', 'base_grid', 'random_seed', 'done']
+    assert cmds[1][2] == ['50', '32']
     p.write_text('splice 3\n')
-    with pytest.raises(Exception):
-        generator.run_paramfile(str(p))
+    with pytest.raises(ValueError, match='not on the GPU realisation path'):
+        generator.parse_paramfile(str(p))

@@ -124,3 +124,51 @@ def test_zoom_oracle_matches_reference_grids(bbks, name, mode, tol):
     for l in range(len(levels)):
         ref = g['delta%d' % l]
         assert np.abs(out[l][0] - ref).max() <= tol * np.abs(ref).max(), l
+
+
+MOD_CASES = {
+    'mod1': dict(levels=[(50.0, 32, (0.0, 0.0, 0.0))], radius=5,
+                 mods=[('overdensity', 0, 0.05), ('vx', 0, 0.0)]),
+    'mod2': dict(levels=[(50.0, 32, (0.0, 0.0, 0.0)), (25.0, 32, (12.5, 12.5, 12.5))], radius=3,
+                 mods=[('overdensity', 0, 0.05), ('vx', 0, 0.0), ('vy', 1, 0.0), ('vz', 2, 0.0)]),
+}
+
+
+def oracle_modified(bbks, case, cr_log=False):
+    """Modified noise, covector values and chi^2 of a MOD_CASES entry, from the oracle."""
+    from conftest import COSMO
+    c = MOD_CASES[case]
+    L = fo.Levels(c['levels'])
+    fo.set_cr_log(cr_log)
+    w = fo.white_noise_levels([l[1] for l in c['levels']], 8896131, 2)
+    fo.set_cr_log(False)
+    p_dm = fo.CambPower(bbks, COSMO, column=1)
+    vs = fo.velocity_to_offset_ratio(COSMO)
+    flagged = fo.flag_cells(L, len(c['levels']) - 1, (25., 25., 25.), 'sphere', c['radius'])
+    covs, targets, values = [], [], {}
+    for name, d, t in c['mods']:
+        loc = fo.localisation_covector(L, flagged, 'overdensity' if name == 'overdensity' else 'velocity', d)
+        cv = fo.multilevel_covector(L, loc, p_dm, None if name == 'overdensity' else vs)
+        values[name] = fo.inner(cv, w)
+        covs.append(cv)
+        targets.append(float(np.float32(t)))
+    before = fo.chi2_levels(L, w)
+    w2 = fo.apply_linear_modifications(L, w, covs, targets)
+    after = fo.chi2_levels(L, w2)
+    return dict(levels=L, noise=w, modified=w2, values=values, chi2=(before, after), flagged=flagged)
+
+
+@pytest.mark.parametrize('case', ['mod1', 'mod2'])
+def test_modification_oracle_matches_reference(bbks, case):
+    from conftest import COSMO
+    g = _load_golden('%s.npz' % case)
+    r = oracle_modified(bbks, case)
+    # log lines carry 6 significant digits
+    assert '%.6g' % r['values']['overdensity'] == '%.6g' % float(g['overdensity'])
+    assert '%.6g' % r['values']['vx'] == '%.6g' % float(g['vx'])
+    assert '%.6g' % (r['chi2'][1] - r['chi2'][0]) == '%.6g' % float(g['delta_chi2'])
+    levels = MOD_CASES[case]['levels']
+    out = fo.zoom_realisation(r['modified'], levels, fo.CambPower(bbks, COSMO))
+    for l in range(len(levels)):
+        ref = g['delta%d' % l].astype(np.float64)
+        assert np.abs(out[l][0] - ref).max() <= 2e-7 * np.abs(ref).max()
