@@ -25,13 +25,19 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+MODS4 = dict(centre=(50.0, 50.0, 50.0), radius=2.0,
+             list=[('overdensity', 1.5), ('vx', 0.0), ('vy', 0.0), ('vz', 0.0)])
 WORKLOADS = {
     # 512^3 base grid in a 100 Mpc/h box plus a 512^3 zoom of side 25 Mpc/h (factor 4)
     # centred at (50, 50, 50) Mpc/h: the headline two-level configuration
+    # with 4 linear modifications in a 2 Mpc/h sphere at the zoom centre: mean
+    # overdensity +1.5 and the three mean velocity components 0
     'zoom512': dict(levels=[('base', 100.0, 512), ('zoom', 192, 192, 192, 4, 512)], seed_cmd='random_seed',
-                    precision='mixed', replaced=128 ** 3),
+                    precision='mixed', replaced=128 ** 3, mods=MODS4),
     'zoom512_fp64': dict(levels=[('base', 100.0, 512), ('zoom', 192, 192, 192, 4, 512)], seed_cmd='random_seed',
-                         precision='fp64', replaced=128 ** 3),
+                         precision='fp64', replaced=128 ** 3, mods=MODS4),
+    'zoom512_nomod': dict(levels=[('base', 100.0, 512), ('zoom', 192, 192, 192, 4, 512)], seed_cmd='random_seed',
+                          precision='mixed', replaced=128 ** 3),
     'zoom256': dict(levels=[('base', 100.0, 256), ('zoom', 96, 96, 96, 4, 256)], seed_cmd='random_seed',
                     precision='mixed', replaced=64 ** 3),
     # 512^3 single level, 100 Mpc/h box (the single-level configuration at 512^3)
@@ -80,6 +86,12 @@ def make_gen(wl, table, device):
             gen.base_grid(lev[1], lev[2])
         else:
             gen.zoom_grid_with_origin_at(*lev[1:])
+    getattr(gen, wl['seed_cmd'])(SEED)
+    if wl.get('mods'):
+        gen.centre(*wl['mods']['centre'])
+        gen.select_sphere(wl['mods']['radius'])
+        for name, target in wl['mods']['list']:
+            gen.modify(name, 'absolute', target)
     return gen
 
 
@@ -248,8 +260,13 @@ def main():
             'random_seed_real_space': _lib.GIC_SEED_REAL_SPACE}[wl['seed_cmd']]
     npart = n_particles(wl)
 
+    has_mods = bool(wl.get('mods'))
+    chi2 = ctypes.c_double(), ctypes.c_double()
+
     def step(i):
         gen._call('gic_draw_noise', SEED + i, mode)
+        if has_mods:
+            gen._call('gic_apply_modifications', ctypes.byref(chi2[0]), ctypes.byref(chi2[1]))
         gen._call('gic_zeldovich', 1)
 
     for i in range(args.warmup):
@@ -305,6 +322,9 @@ def main():
         'warmup': args.warmup, 'ms_per_step': round(t * 1e3, 3), 'higher_is_better': True, 'scaling': 'weak',
         'vs_baseline': None, 'dtype': 'f32+f64' if wl['precision'] == 'mixed' else 'f64', 'data': 'synthetic',
         'config': {'workload': args.workload, 'levels': [list(l) for l in wl['levels']],
+                   'modifications': ([m[0] + '=' + str(m[1]) for m in wl['mods']['list']] +
+                                     ['sphere r=%g at %s' % (wl['mods']['radius'], wl['mods']['centre'])])
+                   if wl.get('mods') else [],
                    'precision': wl['precision'], 'seeding': wl['seed_cmd'], 'transfer': 'BBKS table, 2000 rows',
                    'particles_per_step': npart, 'l2': 'inputs larger than L2 (fields >= 0.5 GB)',
                    'parallelism': 'replicas' if world > 1 else 'single GPU'},
