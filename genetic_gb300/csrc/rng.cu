@@ -22,6 +22,7 @@
 #include "zig_tables.h"
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 namespace gic {
 namespace {
@@ -756,4 +757,173 @@ void draw_noise_all(Context &ctx, unsigned long long seed, int mode) {
     draw_all_typed<float>(ctx, seed, mode);
 }
 
+
+// ---- allocation-free gaussian stream ------------------------------------------------
+//
+// For callers that cannot allocate device memory themselves -- code running
+// inside another runtime's memory pool or budget, or under a stream capture,
+// where a cudaMalloc is not permitted -- this variant of the gaussian-stream
+// pipeline keeps all its scratch (the raw RANLUX numbers, the chunk jump
+// multipliers, the segment walk tables, the stream descriptor and the underrun
+// flag) in one file-scope device array.  The array is NoallocScratchBytes
+// bytes on every device that loads the library, for the lifetime of the
+// process, and every call shares it: calls that overlap on the GPU (different
+// streams or host threads) race on it and must be serialised by the caller.
+// Every region a call reads is written by that same call first (the flag is
+// cleared), so no state carries over from an earlier call.
+
+constexpr unsigned long long kNoallocMaxGauss = GIC_NOALLOC_MAX_GAUSSIANS;
+constexpr size_t NoallocScratchBytes = 24ull << 20;
+static __device__ __align__(256) unsigned char gNoallocScratch[NoallocScratchBytes];
+
+namespace {
+
+__global__ void k_set_stream(Stream *dst, Stream s) { *dst = s; }
+
+// pow2[i] = a^(794 kChunkBlocks 2^i) mod m, one thread
+__global__ void k_pow2_multipliers(U576 *pow2, int npow) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  U576 a;
+  u576_ranlux_multiplier(a);
+  u576_powmod(pow2[0], a, (uint64_t)kLux * kChunkBlocks);
+  for (int i = 1; i < npow; ++i) u576_mulmod(pow2[i], pow2[i - 1], pow2[i - 1]);
+}
+
+struct NoallocLayout {
+  size_t raw, pow2, chunkmul, segtab, segentry, segbase, blkmap, blkentry, blkbase, stream, flags, end;
+};
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// byte offsets of every scratch region for a stream of raw_count numbers
+NoallocLayout noalloc_layout(unsigned long long raw_count, unsigned long long nchunk, unsigned long long nseg,
+                             unsigned long long nblk, int npow) {
+  NoallocLayout L;
+  size_t o = 0;
+  L.raw = o;
+  o = align256(o + raw_count * sizeof(uint32_t));
+  L.pow2 = o;
+  o = align256(o + (size_t)npow * sizeof(U576));
+  L.chunkmul = o;
+  o = align256(o + nchunk * sizeof(U576));
+  L.segtab = o;
+  o = align256(o + nseg * kSpec * sizeof(uint32_t));
+  L.segentry = o;
+  o = align256(o + nseg * sizeof(uint32_t));
+  L.segbase = o;
+  o = align256(o + nseg * sizeof(unsigned long long));
+  L.blkmap = o;
+  o = align256(o + nblk * kSpec * sizeof(uint2));
+  L.blkentry = o;
+  o = align256(o + nblk * sizeof(uint32_t));
+  L.blkbase = o;
+  o = align256(o + nblk * sizeof(unsigned long long));
+  L.stream = o;
+  o = align256(o + sizeof(Stream));
+  L.flags = o;
+  o = align256(o + 4 * sizeof(int));
+  L.end = o;
+  return L;
+}
+
+// device address of the scratch array, looked up once per device
+std::mutex g_noalloc_mutex;
+void *g_noalloc_base[64];
+
+}  // namespace
+
+static int noalloc_scratch(void **base) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return GIC_ERR_CUDA;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_base[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, gNoallocScratch);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      return GIC_ERR_CUDA;
+    }
+    g_noalloc_base[dev] = p;
+  }
+  *base = g_noalloc_base[dev];
+  return GIC_OK;
+}
+
+static int noalloc_run(unsigned long long seed, unsigned long long n, double *out, cudaStream_t cs, double margin,
+                       bool *underrun) {
+  void *base = nullptr;
+  int st = noalloc_scratch(&base);
+  if (st != GIC_OK) return st;
+  Stream s{};
+  s.seed = seed;
+  s.raw_off = 0;
+  s.raw_count = ((unsigned long long)(raw_needed(n) * margin) + 23) / 24 * 24;
+  s.gauss_off = 0;
+  s.gauss_count = n;
+  s.nseg = (unsigned int)((s.raw_count + kSegLen - 1) / kSegLen);
+  s.seg_off = 0;
+  s.nblk = (s.nseg + kBlockSegs - 1) / kBlockSegs;
+  s.blk_off = 0;
+  s.nchunk = (unsigned int)((s.raw_count / 24 + kChunkBlocks - 1) / kChunkBlocks);
+  s.chunk_off = 0;
+  int npow = 1;
+  while ((1ull << npow) < s.nchunk) ++npow;
+  NoallocLayout L = noalloc_layout(s.raw_count, s.nchunk, s.nseg, s.nblk, npow);
+  if (L.end > NoallocScratchBytes) return GIC_ERR_INVALID_ARG;
+  unsigned char *b = static_cast<unsigned char *>(base);
+  uint32_t *raw = reinterpret_cast<uint32_t *>(b + L.raw);
+  U576 *pow2 = reinterpret_cast<U576 *>(b + L.pow2);
+  U576 *chunkmul = reinterpret_cast<U576 *>(b + L.chunkmul);
+  uint32_t *segtab = reinterpret_cast<uint32_t *>(b + L.segtab);
+  uint32_t *segentry = reinterpret_cast<uint32_t *>(b + L.segentry);
+  unsigned long long *segbase = reinterpret_cast<unsigned long long *>(b + L.segbase);
+  uint2 *blkmap = reinterpret_cast<uint2 *>(b + L.blkmap);
+  uint32_t *blkentry = reinterpret_cast<uint32_t *>(b + L.blkentry);
+  unsigned long long *blkbase = reinterpret_cast<unsigned long long *>(b + L.blkbase);
+  Stream *dst = reinterpret_cast<Stream *>(b + L.stream);
+  int *flags = reinterpret_cast<int *>(b + L.flags);
+  cudaError_t e = cudaSuccess;
+  auto ok = [&]() { e = cudaGetLastError(); return e == cudaSuccess; };
+  if (cudaMemsetAsync(flags, 0, 4 * sizeof(int), cs) != cudaSuccess) return GIC_ERR_CUDA;
+  k_set_stream<<<1, 1, 0, cs>>>(dst, s);
+  k_pow2_multipliers<<<1, 1, 0, cs>>>(pow2, npow);
+  k_chunk_multipliers<<<(s.nchunk + 127) / 128, 128, 0, cs>>>(chunkmul, (int)s.nchunk, pow2, npow);
+  k_seed<<<1, 1, 0, cs>>>(dst, 1);
+  k_generate<<<(s.nchunk + 127) / 128, 128, 0, cs>>>(dst, 1, s.nchunk, chunkmul, raw);
+  if (!ok()) return GIC_ERR_CUDA;
+  unsigned ntiles = (unsigned)((s.nseg + kTileSegs - 1) / kTileSegs);
+  k_walk_speculative<<<ntiles, kTileSegs * kSpec, 0, cs>>>(dst, 1, s.nseg, raw, s.raw_count, segtab);
+  k_block_maps<<<(s.nblk * kSpec + 127) / 128, 128, 0, cs>>>(dst, 1, s.nblk, raw, segtab, blkmap);
+  k_chain_blocks<<<1, 64, 0, cs>>>(dst, 1, raw, segtab, blkmap, blkentry, blkbase, flags);
+  k_chain_segments<<<(s.nblk + 127) / 128, 128, 0, cs>>>(dst, 1, s.nblk, raw, segtab, blkentry, blkbase, segentry,
+                                                         segbase);
+  k_walk_final<<<(s.nseg + 127) / 128, 128, 0, cs>>>(dst, 1, s.nseg, raw, segentry, segbase, out, flags);
+  if (!ok()) return GIC_ERR_CUDA;
+  int flag = 0;
+  if (cudaMemcpyAsync(&flag, flags, sizeof(int), cudaMemcpyDeviceToHost, cs) != cudaSuccess ||
+      cudaStreamSynchronize(cs) != cudaSuccess) {
+    cudaGetLastError();
+    return GIC_ERR_CUDA;
+  }
+  *underrun = flag != 0;
+  return GIC_OK;
+}
+
+}  // namespace gic
+
+extern "C" GIC_API int gic_gaussian_stream_noalloc(unsigned long seed, size_t n, double *device_out, void *stream) {
+  if (n == 0) return GIC_OK;
+  if (!device_out || n > gic::kNoallocMaxGauss) return GIC_ERR_INVALID_ARG;
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  bool underrun = false;
+  int st = gic::noalloc_run(seed, n, device_out, cs, 1.0, &underrun);
+  if (st == GIC_OK && underrun) st = gic::noalloc_run(seed, n, device_out, cs, 1.5, &underrun);
+  if (st == GIC_OK && underrun) st = GIC_ERR_INTERNAL;
+  return st;
+}
+
+namespace gic {
 }  // namespace gic

@@ -161,6 +161,22 @@ GIC_API int gic_clear_modifications(gic_ctx *ctx);
  * ModificationManager::applyModifications (modificationmanager.hpp:90-125). */
 GIC_API int gic_apply_modifications(gic_ctx *ctx, double *chi2_before, double *chi2_after);
 
+/* Allocation-free variant of gic_gaussian_stream.  No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc (for instance
+ * code that must stay inside another runtime's device-memory pool or budget).
+ * Writes the first n unit gaussians of the stream of `seed` to the caller's
+ * device buffer `device_out` (n doubles) on the caller's CUDA stream `stream`
+ * (a cudaStream_t, NULL = legacy default stream), and returns when they are
+ * there.  It allocates nothing: its scratch is one file-scope device array of
+ * 24 MiB that every device loading the library holds until the process exits.
+ * n may be at most GIC_NOALLOC_MAX_GAUSSIANS; larger n returns
+ * GIC_ERR_INVALID_ARG without touching the GPU.  The first call on each device
+ * looks up the array's device address (make it before any stream capture).
+ * All calls share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller.  Errors are status codes only (no message). */
+#define GIC_NOALLOC_MAX_GAUSSIANS (1ull << 20)
+GIC_API int gic_gaussian_stream_noalloc(unsigned long seed, size_t n, double *device_out, void *stream);
+
 /* Number of kernels this library has launched in the process so far. */
 GIC_API int gic_launch_count(unsigned long long *count);
 
