@@ -99,6 +99,19 @@ template <typename T, typename C> struct Dft<T, C, 8> {
   }
 };
 
+// Asynchronous global -> shared copies (cp.async): the whole tile is in flight
+// before the first butterfly.  8-byte copies for float complex (rows of a padded
+// half spectrum are only 8-byte aligned), 16-byte for double complex.
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  if (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 struct Radix {
   int n;
   int r[8];
@@ -163,11 +176,16 @@ __global__ void __launch_bounds__(256) k_fft_strided(typename Cx<T>::type *data,
   int tcv = (int)min((long long)TC, B - b0);
   for (int e = threadIdx.x; e < L * TC; e += blockDim.x) {
     int i = e / TC, c = e % TC;
-    C z;
-    z.x = 0;
-    z.y = 0;
-    buf0[e] = c < tcv ? base[(size_t)i * (size_t)B + c] : z;
+    if (c < tcv) {
+      cp_async<sizeof(C)>(buf0 + e, base + (size_t)i * (size_t)B + c);
+    } else {
+      C z;
+      z.x = 0;
+      z.y = 0;
+      buf0[e] = z;
+    }
   }
+  cp_async_wait_all();
   __syncthreads();
   C *src = buf0, *dst = buf1;
   int Ns = 1;
@@ -242,11 +260,16 @@ __global__ void __launch_bounds__(256) k_fft_rows_c2r(typename Cx<T>::type *data
   C *base = data + (size_t)r0 * S;
   for (int e = threadIdx.x; e < RPC * S; e += blockDim.x) {
     int row = e / S;
-    C z;
-    z.x = 0;
-    z.y = 0;
-    buf1[e] = row < rows_valid ? base[e] : z;
+    if (row < rows_valid) {
+      cp_async<sizeof(C)>(buf1 + e, base + e);
+    } else {
+      C z;
+      z.x = 0;
+      z.y = 0;
+      buf1[e] = z;
+    }
   }
+  cp_async_wait_all();
   __syncthreads();
   // Z[k] = E + i O, E = X[k] + conj(X[H-k]), O = (X[k] - conj(X[H-k])) e^{+2 pi i k/N}
   for (int e = threadIdx.x; e < RPC * H; e += blockDim.x) {
@@ -286,11 +309,16 @@ __global__ void __launch_bounds__(256) k_fft_rows_r2c(typename Cx<T>::type *data
   C *base = data + (size_t)r0 * S;
   for (int e = threadIdx.x; e < RPC * H; e += blockDim.x) {
     int row = e / H, m = e % H;
-    C z;
-    z.x = 0;
-    z.y = 0;
-    buf0[row * S + m] = row < rows_valid ? base[(size_t)row * S + m] : z;
+    if (row < rows_valid) {
+      cp_async<sizeof(C)>(buf0 + row * S + m, base + (size_t)row * S + m);
+    } else {
+      C z;
+      z.x = 0;
+      z.y = 0;
+      buf0[row * S + m] = z;
+    }
   }
+  cp_async_wait_all();
   __syncthreads();
   C *src = buf0, *dst = buf1;
   int Ns = 1;

@@ -110,18 +110,49 @@ __global__ void k_mask(T *real, int n, const unsigned char *mx, const unsigned c
   if (in == zero_inside) real[row * (size_t)(2 * (n / 2 + 1)) + z] = 0;
 }
 
-// Hermitian-weighted Re(conj(a) b) over a half spectrum, partial sums per block
+// Hermitian-weighted Re(conj(a) b) over a half spectrum, partial sums per block.
+// Float fields: every product is split exactly (fma) and accumulated in a
+// compensated float pair per thread, converted to double once -- a double-grade
+// sum without double arithmetic per element.  Double fields: plain doubles.
+__device__ __forceinline__ void acc2(float &s, float &e, float x) {
+  float t = s + x;
+  float bb = t - s;
+  e += (s - (t - bb)) + (x - bb);
+  s = t;
+}
+__device__ __forceinline__ double thread_inner(const float *a, const float *b, size_t nc, int S, int H, size_t start,
+                                               size_t step) {
+  float s = 0.f, e = 0.f;
+  for (size_t id = start; id < nc; id += step) {
+    int kz = (int)(id % S);
+    float w = (kz == 0 || kz == H) ? 1.f : 2.f;
+    float ar = a[2 * id], ai = a[2 * id + 1], br = b[2 * id], bi = b[2 * id + 1];
+    float p1 = ar * br, p2 = ai * bi;
+    float e1 = fmaf(ar, br, -p1), e2 = fmaf(ai, bi, -p2);
+    acc2(s, e, w * p1);
+    acc2(s, e, w * p2);
+    e += w * (e1 + e2);
+  }
+  return (double)s + (double)e;
+}
+__device__ __forceinline__ double thread_inner(const double *a, const double *b, size_t nc, int S, int H,
+                                               size_t start, size_t step) {
+  double acc = 0;
+  for (size_t id = start; id < nc; id += step) {
+    int kz = (int)(id % S);
+    double w = (kz == 0 || kz == H) ? 1.0 : 2.0;
+    acc += w * (a[2 * id] * b[2 * id] + a[2 * id + 1] * b[2 * id + 1]);
+  }
+  return acc;
+}
+
 template <typename T>
 __global__ void k_inner(const T *a, const T *b, int n, double *partial) {
   __shared__ double red[256];
   const int H = n / 2, S = H + 1;
   size_t nc = (size_t)n * n * S;
-  double acc = 0;
-  for (size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x; id < nc; id += (size_t)gridDim.x * blockDim.x) {
-    int kz = (int)(id % S);
-    double w = (kz == 0 || kz == H) ? 1.0 : 2.0;
-    acc += w * ((double)a[2 * id] * (double)b[2 * id] + (double)a[2 * id + 1] * (double)b[2 * id + 1]);
-  }
+  double acc = thread_inner(a, b, nc, S, H, (size_t)blockIdx.x * blockDim.x + threadIdx.x,
+                            (size_t)gridDim.x * blockDim.x);
   red[threadIdx.x] = acc;
   __syncthreads();
   for (int s = blockDim.x / 2; s > 0; s >>= 1) {
@@ -129,6 +160,20 @@ __global__ void k_inner(const T *a, const T *b, int n, double *partial) {
     __syncthreads();
   }
   if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+// sum of n doubles in a fixed order, one block
+__global__ void k_sum(const double *in, int n, double *out) {
+  __shared__ double red[256];
+  double acc = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += in[i];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
 }
 
 // localisation covector on the finest grid (padded real layout)
@@ -456,13 +501,23 @@ struct ModEngine {
         to_real(R, t);
         mask(R, t, 1);
         axpy(R, I, 1.0, t);
+        for (int s = 0; s < nl(); ++s)
+          if (s != t) cross_term_impl(R, t, ptr(X, s), s);
+        to_fourier(R, t);
       } else {
+        // f_t^2 X_t stays in Fourier space; the cross-level terms are summed in real
+        // space and transformed once: R = f_t^2 X_t + FFT(sum_s cross_s)
         apply_family(R, t, 2);
-        to_real(R, t);
+        if (nl() > 1) {
+          inw.ensure(elems(t) * sizeof(T));
+          T *Cr = inw.template as<T>();
+          GIC_CUDA(cudaMemsetAsync(Cr, 0, elems(t) * sizeof(T), ctx.stream));
+          for (int s = 0; s < nl(); ++s)
+            if (s != t) cross_term_impl(Cr, t, ptr(X, s), s);
+          to_fourier(Cr, t);
+          axpy(R, Cr, 1.0, t);
+        }
       }
-      for (int s = 0; s < nl(); ++s)
-        if (s != t) cross_term_impl(R, t, ptr(X, s), s);
-      to_fourier(R, t);
       out.fourier[t] = 1;
     }
   }
