@@ -122,12 +122,11 @@ __global__ void k_za_fields(const typename V2<T>::type *noise, const double *tab
                             typename V2<T>::type *pz) {
   using C = typename V2<T>::type;
   const int H = n / 2, S = H + 1;
-  size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  size_t nc = (size_t)n * n * S;
-  if (id >= nc) return;
-  int iz = (int)(id % S);
-  size_t r = id / S;
-  int iy = (int)(r % n), ix = (int)(r / n);
+  unsigned row = blockIdx.x * 8 + threadIdx.y;
+  int iz = blockIdx.y * 32 + threadIdx.x;
+  if (row >= (unsigned)n * (unsigned)n || iz >= S) return;
+  int ix = (int)(row / (unsigned)n), iy = (int)(row % (unsigned)n);
+  size_t id = (size_t)row * S + iz;
   int kx = ix > H ? ix - n : ix;
   int ky = iy > H ? iy - n : iy;
   int kz = iz;
@@ -175,15 +174,17 @@ __global__ void k_filter_table(double *out, const double *base, long long nq, do
 }
 
 // multiply a half spectrum by tab[|k|^2]
+inline dim3 hs_grid(int n) { return dim3((unsigned)(((size_t)n * n + 7) / 8), (unsigned)((n / 2 + 1 + 31) / 32)); }
+inline dim3 hs_block() { return dim3(32, 8); }
+
 template <typename T>
 __global__ void k_scale_table(typename V2<T>::type *c, int n, const double *tab) {
   const int H = n / 2, S = H + 1;
-  size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  size_t nc = (size_t)n * n * S;
-  if (id >= nc) return;
-  int iz = (int)(id % S);
-  size_t r = id / S;
-  int iy = (int)(r % n), ix = (int)(r / n);
+  unsigned row = blockIdx.x * 8 + threadIdx.y;
+  int iz = blockIdx.y * 32 + threadIdx.x;
+  if (row >= (unsigned)n * (unsigned)n || iz >= S) return;
+  int ix = (int)(row / (unsigned)n), iy = (int)(row % (unsigned)n);
+  size_t id = (size_t)row * S + iz;
   long long kx = ix > H ? ix - n : ix, ky = iy > H ? iy - n : iy;
   T s = (T)tab[kx * kx + ky * ky + (long long)iz * iz];
   c[id].x *= s;
@@ -350,8 +351,7 @@ static void za_fields_typed(Context &ctx, int li) {
   size_t nc = L.ncomplex();
   for (int f = 0; f < 4; ++f) L.field[f].ensure(nc * sizeof(C));
   build_level_tables(ctx, li);
-  unsigned blocks = (unsigned)((nc + 255) / 256);
-  k_za_fields<T><<<blocks, 256, 0, ctx.stream>>>(L.noise.as<C>(), L.tab_main.as<double>(), L.n, (T)L.kmin(),
+  k_za_fields<T><<<hs_grid(L.n), hs_block(), 0, ctx.stream>>>(L.noise.as<C>(), L.tab_main.as<double>(), L.n, (T)L.kmin(),
                                                  L.field[0].as<C>(), L.field[1].as<C>(), L.field[2].as<C>(),
                                                  L.field[3].as<C>());
   launched();
@@ -378,7 +378,7 @@ static void zoom_combine_typed(Context &ctx, int li) {
   double scale = 1.0 / std::pow((double)Cl.n, 1.5);
   if (li - 1 == 0) {
     // level 0 is unfiltered: its low-passed fields come straight from its noise
-    k_za_fields<T><<<blocks, 256, 0, ctx.stream>>>(Cl.noise.as<C>(), Cl.tab_lp_src.as<double>(), Cl.n, (T)Cl.kmin(),
+    k_za_fields<T><<<hs_grid(Cl.n), hs_block(), 0, ctx.stream>>>(Cl.noise.as<C>(), Cl.tab_lp_src.as<double>(), Cl.n, (T)Cl.kmin(),
                                                    reinterpret_cast<C *>(src[0]), reinterpret_cast<C *>(src[1]),
                                                    reinterpret_cast<C *>(src[2]), reinterpret_cast<C *>(src[3]));
     launched();
@@ -387,7 +387,7 @@ static void zoom_combine_typed(Context &ctx, int li) {
     for (int f = 0; f < 4; ++f) {
       GIC_CUDA(cudaMemcpyAsync(src[f], Cl.field[f].ptr, nc * sizeof(C), cudaMemcpyDeviceToDevice, ctx.stream));
       fft_r2c_3d<T>(ctx, src[f], Cl.n, scale);
-      k_scale_table<T><<<blocks, 256, 0, ctx.stream>>>(reinterpret_cast<C *>(src[f]), Cl.n, Cl.tab_lp.as<double>());
+      k_scale_table<T><<<hs_grid(Cl.n), hs_block(), 0, ctx.stream>>>(reinterpret_cast<C *>(src[f]), Cl.n, Cl.tab_lp.as<double>());
       launched();
     }
   }

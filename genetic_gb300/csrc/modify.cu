@@ -68,17 +68,24 @@ __global__ void k_mod_table(double *out, long long nq, TableSpec sp) {
   out[q] = f;
 }
 
+// Half-spectrum kernels run on a 2-D grid: x over rows (kx, ky), y over 32-wide
+// kz chunks, so no 64-bit division per element.
+constexpr int kKzChunk = 32, kRowsPerBlock = 8;
+inline dim3 hs_grid(int n) {
+  return dim3((unsigned)(((size_t)n * n + kRowsPerBlock - 1) / kRowsPerBlock), (unsigned)((n / 2 + 1 + kKzChunk - 1) / kKzChunk));
+}
+inline dim3 hs_block() { return dim3(kKzChunk, kRowsPerBlock); }
+
 template <typename T>
 __global__ void k_mul_table(typename V2m<T>::type *c, int n, const double *tab) {
   const int H = n / 2, S = H + 1;
-  size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  size_t nc = (size_t)n * n * S;
-  if (id >= nc) return;
-  int iz = (int)(id % S);
-  size_t r = id / S;
-  int iy = (int)(r % n), ix = (int)(r / n);
+  unsigned row = blockIdx.x * kRowsPerBlock + threadIdx.y;
+  int iz = blockIdx.y * kKzChunk + threadIdx.x;
+  if (row >= (unsigned)n * (unsigned)n || iz >= S) return;
+  int ix = (int)(row / (unsigned)n), iy = (int)(row % (unsigned)n);
   long long kx = ix > H ? ix - n : ix, ky = iy > H ? iy - n : iy;
   T s = (T)tab[kx * kx + ky * ky + (long long)iz * iz];
+  size_t id = (size_t)row * S + iz;
   c[id].x *= s;
   c[id].y *= s;
 }
@@ -120,12 +127,11 @@ __device__ __forceinline__ void acc2(float &s, float &e, float x) {
   e += (s - (t - bb)) + (x - bb);
   s = t;
 }
-__device__ __forceinline__ double thread_inner(const float *a, const float *b, size_t nc, int S, int H, size_t start,
-                                               size_t step) {
+__device__ __forceinline__ double thread_inner_col(const float *a, const float *b, unsigned rows, int S, int iz,
+                                                   float w, unsigned r0, unsigned rstep) {
   float s = 0.f, e = 0.f;
-  for (size_t id = start; id < nc; id += step) {
-    int kz = (int)(id % S);
-    float w = (kz == 0 || kz == H) ? 1.f : 2.f;
+  for (unsigned r = r0; r < rows; r += rstep) {
+    size_t id = (size_t)r * S + iz;
     float ar = a[2 * id], ai = a[2 * id + 1], br = b[2 * id], bi = b[2 * id + 1];
     float p1 = ar * br, p2 = ai * bi;
     float e1 = fmaf(ar, br, -p1), e2 = fmaf(ai, bi, -p2);
@@ -135,13 +141,12 @@ __device__ __forceinline__ double thread_inner(const float *a, const float *b, s
   }
   return (double)s + (double)e;
 }
-__device__ __forceinline__ double thread_inner(const double *a, const double *b, size_t nc, int S, int H,
-                                               size_t start, size_t step) {
+__device__ __forceinline__ double thread_inner_col(const double *a, const double *b, unsigned rows, int S, int iz,
+                                                   float w, unsigned r0, unsigned rstep) {
   double acc = 0;
-  for (size_t id = start; id < nc; id += step) {
-    int kz = (int)(id % S);
-    double w = (kz == 0 || kz == H) ? 1.0 : 2.0;
-    acc += w * (a[2 * id] * b[2 * id] + a[2 * id + 1] * b[2 * id + 1]);
+  for (unsigned r = r0; r < rows; r += rstep) {
+    size_t id = (size_t)r * S + iz;
+    acc += (double)w * (a[2 * id] * b[2 * id] + a[2 * id + 1] * b[2 * id + 1]);
   }
   return acc;
 }
@@ -150,16 +155,22 @@ template <typename T>
 __global__ void k_inner(const T *a, const T *b, int n, double *partial) {
   __shared__ double red[256];
   const int H = n / 2, S = H + 1;
-  size_t nc = (size_t)n * n * S;
-  double acc = thread_inner(a, b, nc, S, H, (size_t)blockIdx.x * blockDim.x + threadIdx.x,
-                            (size_t)gridDim.x * blockDim.x);
-  red[threadIdx.x] = acc;
+  const unsigned rows = (unsigned)n * (unsigned)n;
+  const int tid = threadIdx.y * kKzChunk + threadIdx.x;
+  double acc = 0;
+  // grid-stride over rows; each thread owns a kz column chunk of its rows
+  for (int iz = threadIdx.x; iz < S; iz += kKzChunk) {
+    float wf = (iz == 0 || iz == H) ? 1.f : 2.f;
+    acc += thread_inner_col(a, b, rows, S, iz, wf, blockIdx.x * kRowsPerBlock + threadIdx.y,
+                            gridDim.x * kRowsPerBlock);
+  }
+  red[tid] = acc;
   __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+  for (int s2 = 128; s2 > 0; s2 >>= 1) {
+    if (tid < s2) red[tid] += red[tid + s2];
     __syncthreads();
   }
-  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+  if (tid == 0) partial[blockIdx.x] = red[0];
 }
 
 // sum of n doubles in a fixed order, one block
@@ -367,8 +378,8 @@ struct ModEngine {
   }
 
   void mul_table(T *p, int g) {
-    k_mul_table<T><<<nblk(lev(g).ncomplex()), 256, 0, ctx.stream>>>(reinterpret_cast<C *>(p), lev(g).n,
-                                                                    tab.template as<double>());
+    k_mul_table<T><<<hs_grid(lev(g).n), hs_block(), 0, ctx.stream>>>(reinterpret_cast<C *>(p), lev(g).n,
+                                                                     tab.template as<double>());
     launched();
   }
   void axpy(T *a, const T *b, double c, int l) {
@@ -381,20 +392,21 @@ struct ModEngine {
   }
 
   double inner(Field &a, Field &b) {
-    const int blocks = 128;
-    ctx.reduce.ensure(blocks * sizeof(double) * 8);
-    double total = 0;
-    std::vector<double> h(blocks);
-    for (int l = 0; l < nl(); ++l) {
+    const int blocks = 152 * 8;
+    int L = nl();
+    ctx.reduce.ensure(((size_t)L * blocks + 1) * sizeof(double));
+    double *part = ctx.reduce.template as<double>();
+    for (int l = 0; l < L; ++l) {
       to_fourier(a, l);
       to_fourier(b, l);
-      k_inner<T><<<blocks, 256, 0, ctx.stream>>>(ptr(a, l), ptr(b, l), lev(l).n, ctx.reduce.template as<double>());
+      k_inner<T><<<blocks, hs_block(), 0, ctx.stream>>>(ptr(a, l), ptr(b, l), lev(l).n, part + (size_t)l * blocks);
       launched();
-      GIC_CUDA(cudaMemcpyAsync(h.data(), ctx.reduce.ptr, blocks * sizeof(double), cudaMemcpyDeviceToHost,
-                               ctx.stream));
-      GIC_CUDA(cudaStreamSynchronize(ctx.stream));
-      for (double v : h) total += v;
     }
+    k_sum<<<1, 256, 0, ctx.stream>>>(part, L * blocks, part + (size_t)L * blocks);
+    launched();
+    double total = 0;
+    GIC_CUDA(cudaMemcpyAsync(&total, part + (size_t)L * blocks, sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+    GIC_CUDA(cudaStreamSynchronize(ctx.stream));
     return total;
   }
 
