@@ -132,24 +132,37 @@ Radix make_plan(int L) {
 
 // ---- strided pass: complex array (A, L, B), transform along L ----------------
 
-template <typename T, int R>
+// j % Ns, j / Ns and L / (Ns R) with shifts when Ns is a power of two (ns_log >= 0)
+__device__ __forceinline__ void ns_split(int j, int Ns, int ns_log, int &jm, int &jq) {
+  if (ns_log >= 0) {
+    jm = j & (Ns - 1);
+    jq = j >> ns_log;
+  } else {
+    jm = j % Ns;
+    jq = j / Ns;
+  }
+}
+
+template <typename T, int R, int TC>
 __device__ __forceinline__ void strided_stage(const typename Cx<T>::type *src, typename Cx<T>::type *dst,
                                               typename Cx<T>::type *gout, long long B, int tcv, int L, int Ns,
-                                              int TC, int sign, const typename Cx<T>::type *tw, T scale) {
+                                              int ns_log, int sign, const typename Cx<T>::type *tw, T scale) {
   using C = typename Cx<T>::type;
   const int LR = L / R;
   const int nb = LR * TC;
+  const int span = L / (Ns * R);
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
     int c = b % TC, j = b / TC;
     C v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = src[(j + r * LR) * TC + c];
-    int jm = j % Ns;
-    int tstep = jm * (L / (Ns * R));
+    int jm, jq;
+    ns_split(j, Ns, ns_log, jm, jq);
+    int tstep = jm * span;
 #pragma unroll
     for (int r = 1; r < R; ++r) v[r] = cmul(v[r], twid(tw, r * tstep, sign));
     Dft<T, C, R>::run(v, sign);
-    int d = (j / Ns) * Ns * R + jm;
+    int d = jq * Ns * R + jm;
     if (gout) {
       if (c < tcv) {
 #pragma unroll
@@ -162,8 +175,8 @@ __device__ __forceinline__ void strided_stage(const typename Cx<T>::type *src, t
   }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) k_fft_strided(typename Cx<T>::type *data, int L, long long B, int TC,
+template <typename T, int TC>
+__global__ void __launch_bounds__(256) k_fft_strided(typename Cx<T>::type *data, int L, long long B,
                                                      Radix plan, int sign, const typename Cx<T>::type *tw,
                                                      T scale) {
   using C = typename Cx<T>::type;
@@ -188,17 +201,18 @@ __global__ void __launch_bounds__(256) k_fft_strided(typename Cx<T>::type *data,
   cp_async_wait_all();
   __syncthreads();
   C *src = buf0, *dst = buf1;
-  int Ns = 1;
+  int Ns = 1, ns_log = 0;
   for (int s = 0; s < plan.n; ++s) {
     int R = plan.r[s];
     C *g = (s == plan.n - 1) ? base : nullptr;
-    if (R == 8) strided_stage<T, 8>(src, dst, g, B, tcv, L, Ns, TC, sign, tw, scale);
-    else if (R == 4) strided_stage<T, 4>(src, dst, g, B, tcv, L, Ns, TC, sign, tw, scale);
-    else if (R == 2) strided_stage<T, 2>(src, dst, g, B, tcv, L, Ns, TC, sign, tw, scale);
-    else strided_stage<T, 3>(src, dst, g, B, tcv, L, Ns, TC, sign, tw, scale);
+    if (R == 8) strided_stage<T, 8, TC>(src, dst, g, B, tcv, L, Ns, ns_log, sign, tw, scale);
+    else if (R == 4) strided_stage<T, 4, TC>(src, dst, g, B, tcv, L, Ns, ns_log, sign, tw, scale);
+    else if (R == 2) strided_stage<T, 2, TC>(src, dst, g, B, tcv, L, Ns, ns_log, sign, tw, scale);
+    else strided_stage<T, 3, TC>(src, dst, g, B, tcv, L, Ns, ns_log, sign, tw, scale);
     __syncthreads();
     C *t = src; src = dst; dst = t;
     Ns *= R;
+    ns_log = (ns_log >= 0 && R != 3) ? ns_log + (R == 8 ? 3 : R == 4 ? 2 : 1) : -1;
   }
 }
 
@@ -207,23 +221,33 @@ __global__ void __launch_bounds__(256) k_fft_strided(typename Cx<T>::type *data,
 
 template <typename T, int R>
 __device__ __forceinline__ void row_stage(const typename Cx<T>::type *src, typename Cx<T>::type *dst,
-                                          typename Cx<T>::type *gout, int rows_valid, int H, int Ns, int RPC,
-                                          int sign, const typename Cx<T>::type *tw, T scale) {
+                                          typename Cx<T>::type *gout, int rows_valid, int H, int Ns, int ns_log,
+                                          int h_log, int RPC, int sign, const typename Cx<T>::type *tw, T scale) {
   using C = typename Cx<T>::type;
   const int HR = H / R;
   const int nb = HR * RPC;
   const int S = H + 1;
+  const int hr_log = h_log >= 0 ? h_log - (R == 8 ? 3 : R == 4 ? 2 : 1) : -1;
+  const int span = H / (Ns * R);
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-    int row = b / HR, j = b % HR;
+    int row, j;
+    if (hr_log >= 0) {
+      row = b >> hr_log;
+      j = b & (HR - 1);
+    } else {
+      row = b / HR;
+      j = b % HR;
+    }
     C v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = src[row * S + j + r * HR];
-    int jm = j % Ns;
-    int tstep = jm * (H / (Ns * R));
+    int jm, jq;
+    ns_split(j, Ns, ns_log, jm, jq);
+    int tstep = jm * span;
 #pragma unroll
     for (int r = 1; r < R; ++r) v[r] = cmul(v[r], twid(tw, 2 * r * tstep, sign));
     Dft<T, C, R>::run(v, sign);
-    int d = (j / Ns) * Ns * R + jm;
+    int d = jq * Ns * R + jm;
     if (gout) {
       if (row < rows_valid) {
 #pragma unroll
@@ -238,13 +262,15 @@ __device__ __forceinline__ void row_stage(const typename Cx<T>::type *src, typen
 
 template <typename T>
 __device__ __forceinline__ void row_stage_any(int R, const typename Cx<T>::type *src, typename Cx<T>::type *dst,
-                                              typename Cx<T>::type *gout, int rows_valid, int H, int Ns, int RPC,
-                                              int sign, const typename Cx<T>::type *tw, T scale) {
-  if (R == 8) row_stage<T, 8>(src, dst, gout, rows_valid, H, Ns, RPC, sign, tw, scale);
-  else if (R == 4) row_stage<T, 4>(src, dst, gout, rows_valid, H, Ns, RPC, sign, tw, scale);
-  else if (R == 2) row_stage<T, 2>(src, dst, gout, rows_valid, H, Ns, RPC, sign, tw, scale);
-  else row_stage<T, 3>(src, dst, gout, rows_valid, H, Ns, RPC, sign, tw, scale);
+                                              typename Cx<T>::type *gout, int rows_valid, int H, int Ns, int ns_log,
+                                              int h_log, int RPC, int sign, const typename Cx<T>::type *tw, T scale) {
+  if (R == 8) row_stage<T, 8>(src, dst, gout, rows_valid, H, Ns, ns_log, h_log, RPC, sign, tw, scale);
+  else if (R == 4) row_stage<T, 4>(src, dst, gout, rows_valid, H, Ns, ns_log, h_log, RPC, sign, tw, scale);
+  else if (R == 2) row_stage<T, 2>(src, dst, gout, rows_valid, H, Ns, ns_log, h_log, RPC, sign, tw, scale);
+  else row_stage<T, 3>(src, dst, gout, rows_valid, H, Ns, ns_log, -1, RPC, sign, tw, scale);
 }
+
+__device__ __forceinline__ int ilog2_or_neg(int v) { return (v & (v - 1)) == 0 ? 31 - __clz(v) : -1; }
 
 // c2r rows: in = N/2+1 Hermitian coefficients per row, out = N reals (in place)
 template <typename T>
@@ -284,14 +310,16 @@ __global__ void __launch_bounds__(256) k_fft_rows_c2r(typename Cx<T>::type *data
   }
   __syncthreads();
   C *src = buf0, *dst = buf1;
-  int Ns = 1;
+  int Ns = 1, ns_log = 0;
+  const int h_log = ilog2_or_neg(H);
   for (int s = 0; s < plan.n; ++s) {
     int R = plan.r[s];
     C *g = (s == plan.n - 1) ? base : nullptr;
-    row_stage_any<T>(R, src, dst, g, rows_valid, H, Ns, RPC, +1, tw, scale);
+    row_stage_any<T>(R, src, dst, g, rows_valid, H, Ns, ns_log, h_log, RPC, +1, tw, scale);
     __syncthreads();
     C *t = src; src = dst; dst = t;
     Ns *= R;
+    ns_log = (ns_log >= 0 && R != 3) ? ns_log + (R == 8 ? 3 : R == 4 ? 2 : 1) : -1;
   }
 }
 
@@ -321,13 +349,15 @@ __global__ void __launch_bounds__(256) k_fft_rows_r2c(typename Cx<T>::type *data
   cp_async_wait_all();
   __syncthreads();
   C *src = buf0, *dst = buf1;
-  int Ns = 1;
+  int Ns = 1, ns_log = 0;
+  const int h_log = ilog2_or_neg(H);
   for (int s = 0; s < plan.n; ++s) {
     int R = plan.r[s];
-    row_stage_any<T>(R, src, dst, nullptr, rows_valid, H, Ns, RPC, -1, tw, (T)1);
+    row_stage_any<T>(R, src, dst, nullptr, rows_valid, H, Ns, ns_log, h_log, RPC, -1, tw, (T)1);
     __syncthreads();
     C *t = src; src = dst; dst = t;
     Ns *= R;
+    ns_log = (ns_log >= 0 && R != 3) ? ns_log + (R == 8 ? 3 : R == 4 ? 2 : 1) : -1;
   }
   // src holds Z; X[k] = (Z[k] + conj Z[H-k])/2 - i/2 e^{-2 pi i k/N} (Z[k] - conj Z[H-k])
   for (int e = threadIdx.x; e < RPC * S; e += blockDim.x) {
@@ -379,12 +409,12 @@ void set_smem(const void *fn, size_t bytes) {
 template <typename T>
 void strided_pass(Context &ctx, typename Cx<T>::type *data, int A, int L, long long B, int sign, T scale,
                   const typename Cx<T>::type *tw) {
-  int TC = sizeof(T) == 4 ? 8 : 4;
+  constexpr int TC = sizeof(T) == 4 ? 8 : 4;
   Radix plan = make_plan(L);
   size_t smem = 2ull * L * TC * sizeof(typename Cx<T>::type);
-  set_smem<T>((const void *)k_fft_strided<T>, smem);
+  set_smem<T>((const void *)k_fft_strided<T, TC>, smem);
   dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)A);
-  k_fft_strided<T><<<grid, 256, smem, ctx.stream>>>(data, L, B, TC, plan, sign, tw, scale);
+  k_fft_strided<T, TC><<<grid, 256, smem, ctx.stream>>>(data, L, B, plan, sign, tw, scale);
   launched();
 }
 
