@@ -48,6 +48,39 @@ struct DevBuf {
   template <typename T> T *as() const { return static_cast<T *>(ptr); }
 };
 
+// Device buffers kept between calls: the fields of the modification algebra take
+// them here and give them back, so repeated applications allocate nothing.
+struct BufPool {
+  std::vector<std::unique_ptr<DevBuf>> free;
+  std::unique_ptr<DevBuf> take(size_t nbytes) {
+    int best = -1;
+    for (int i = 0; i < (int)free.size(); ++i)
+      if (free[i]->bytes >= nbytes && (best < 0 || free[i]->bytes < free[best]->bytes)) best = i;
+    if (best >= 0) {
+      std::unique_ptr<DevBuf> b = std::move(free[best]);
+      free.erase(free.begin() + best);
+      return b;
+    }
+    auto b = std::make_unique<DevBuf>();
+    try {
+      b->ensure(nbytes);
+    } catch (const Error &) {
+      free.clear();  // give idle buffers back to the device and try once more
+      b->ensure(nbytes);
+    }
+    return b;
+  }
+  void give(std::unique_ptr<DevBuf> b) {
+    if (b) free.push_back(std::move(b));
+  }
+};
+
+// scratch of the modification algebra (one user at a time; each buffer is used
+// within a single operation)
+struct ModScratch {
+  DevBuf tab, masks, tmp_src, win, cells, geom, t1, t2, t3, reduce;
+};
+
 // One grid level: N^3 cells of a cube of side `box` whose lower corner is x0.
 struct Level {
   int n = 0;
@@ -121,6 +154,8 @@ struct Context {
   DevBuf zoom_scratch[4];  // low-passed coarse fields during zoom combination
   DevBuf geom;             // per-axis interpolation / centroid tables
   std::vector<ModRequest> mods;
+  BufPool pool;
+  ModScratch modscratch;
   bool dbl() const { return precision == GIC_FP64; }
 };
 

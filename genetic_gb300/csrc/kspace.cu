@@ -374,7 +374,6 @@ static void zoom_combine_typed(Context &ctx, int li) {
   T *src[4];
   for (int f = 0; f < 4; ++f) src[f] = ctx.zoom_scratch[f].as<T>();
   build_lowpass_tables(ctx, li - 1);
-  unsigned blocks = (unsigned)((nc + 255) / 256);
   double scale = 1.0 / std::pow((double)Cl.n, 1.5);
   if (li - 1 == 0) {
     // level 0 is unfiltered: its low-passed fields come straight from its noise

@@ -104,17 +104,23 @@ __global__ void k_scale(T *a, double c, size_t n) {
   if (i < n) a[i] *= (T)c;
 }
 
-// zero the cells of a padded real field inside (zero_inside = 1) or outside the window
+// Window combinations on padded real fields (in = cell inside the window):
+//   op 0: r = (in ? 0 : r) + s      op 1: r = in ? s : r      op 2: r = in ? s : 0
 template <typename T>
-__global__ void k_mask(T *real, int n, const unsigned char *mx, const unsigned char *my, const unsigned char *mz,
-                       int zero_inside) {
-  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  size_t m = (size_t)n * n * n;
-  if (i >= m) return;
-  size_t row = i / n;
-  int z = (int)(i % n), y = (int)(row % n), x = (int)(row / n);
-  int in = mx[x] && my[y] && mz[z];
-  if (in == zero_inside) real[row * (size_t)(2 * (n / 2 + 1)) + z] = 0;
+__global__ void k_window_op(T *r, const T *s, int n, const unsigned char *mx, const unsigned char *my,
+                            const unsigned char *mz, int op) {
+  unsigned row = blockIdx.x * kRowsPerBlock + threadIdx.y;
+  int z = blockIdx.y * kKzChunk + threadIdx.x;
+  if (row >= (unsigned)n * (unsigned)n || z >= n) return;
+  int x = (int)(row / (unsigned)n), y = (int)(row % (unsigned)n);
+  bool in = mx[x] && my[y] && mz[z];
+  size_t id = (size_t)row * (size_t)(2 * (n / 2 + 1)) + z;
+  if (op == 0) r[id] = (in ? (T)0 : r[id]) + s[id];
+  else if (op == 1) { if (in) r[id] = s[id]; }
+  else r[id] = in ? s[id] : (T)0;
+}
+inline dim3 real_grid(int n) {
+  return dim3((unsigned)(((size_t)n * n + kRowsPerBlock - 1) / kRowsPerBlock), (unsigned)((n + kKzChunk - 1) / kKzChunk));
 }
 
 // Hermitian-weighted Re(conj(a) b) over a half spectrum, partial sums per block.
@@ -151,6 +157,44 @@ __device__ __forceinline__ double thread_inner_col(const double *a, const double
   return acc;
 }
 
+// sum over the n^3 cells of two padded real fields (Parseval: equals the
+// Hermitian-weighted spectral sum of their unitary transforms)
+__device__ __forceinline__ double thread_dot_col(const float *a, const float *b, unsigned rows, size_t rs, int z,
+                                                 unsigned r0, unsigned rstep) {
+  float s = 0.f, e = 0.f;
+  for (unsigned r = r0; r < rows; r += rstep) {
+    size_t id = (size_t)r * rs + z;
+    float p = a[id] * b[id];
+    e += fmaf(a[id], b[id], -p);
+    acc2(s, e, p);
+  }
+  return (double)s + (double)e;
+}
+__device__ __forceinline__ double thread_dot_col(const double *a, const double *b, unsigned rows, size_t rs, int z,
+                                                 unsigned r0, unsigned rstep) {
+  double acc = 0;
+  for (unsigned r = r0; r < rows; r += rstep) acc += a[(size_t)r * rs + z] * b[(size_t)r * rs + z];
+  return acc;
+}
+
+template <typename T>
+__global__ void k_inner_real(const T *a, const T *b, int n, double *partial) {
+  __shared__ double red[256];
+  const unsigned rows = (unsigned)n * (unsigned)n;
+  const size_t rs = (size_t)(2 * (n / 2 + 1));
+  const int tid = threadIdx.y * kKzChunk + threadIdx.x;
+  double acc = 0;
+  for (int z = threadIdx.x; z < n; z += kKzChunk)
+    acc += thread_dot_col(a, b, rows, rs, z, blockIdx.x * kRowsPerBlock + threadIdx.y, gridDim.x * kRowsPerBlock);
+  red[tid] = acc;
+  __syncthreads();
+  for (int s2 = 128; s2 > 0; s2 >>= 1) {
+    if (tid < s2) red[tid] += red[tid + s2];
+    __syncthreads();
+  }
+  if (tid == 0) partial[blockIdx.x] = red[0];
+}
+
 template <typename T>
 __global__ void k_inner(const T *a, const T *b, int n, double *partial) {
   __shared__ double red[256];
@@ -173,9 +217,11 @@ __global__ void k_inner(const T *a, const T *b, int n, double *partial) {
   if (tid == 0) partial[blockIdx.x] = red[0];
 }
 
-// sum of n doubles in a fixed order, one block
+// sums of consecutive runs of n doubles in a fixed order, one block per run
 __global__ void k_sum(const double *in, int n, double *out) {
   __shared__ double red[256];
+  in += (size_t)blockIdx.x * n;
+  out += blockIdx.x;
   double acc = 0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) acc += in[i];
   red[threadIdx.x] = acc;
@@ -315,25 +361,37 @@ template <typename T>
 struct ModEngine {
   using C = typename V2m<T>::type;
   Context &ctx;
-  explicit ModEngine(Context &c) : ctx(c) {}
+  ModScratch &S;
+  explicit ModEngine(Context &c) : ctx(c), S(c.modscratch) {}
 
   int nl() const { return (int)ctx.levels.size(); }
   Level &lev(int l) { return *ctx.levels[l]; }
   size_t elems(int l) { return 2 * lev(l).ncomplex(); }
   double scale(int l) { return 1.0 / std::pow((double)lev(l).n, 1.5); }
 
+  // one half-spectrum (or padded real) buffer per level, taken from the context's pool
   struct Field {
+    BufPool *pool = nullptr;
     std::vector<std::unique_ptr<DevBuf>> b;
     std::vector<char> fourier;
+    Field() = default;
+    Field(Field &&) = default;
+    Field &operator=(Field &&) = delete;
+    ~Field() {
+      if (pool)
+        for (auto &x : b) pool->give(std::move(x));
+    }
   };
 
   void alloc(Field &f) {
+    f.pool = &ctx.pool;
     f.b.resize(nl());
     f.fourier.assign(nl(), 1);
-    for (int l = 0; l < nl(); ++l) {
-      if (!f.b[l]) f.b[l] = std::make_unique<DevBuf>();
-      f.b[l]->ensure(elems(l) * sizeof(T));
-    }
+    for (int l = 0; l < nl(); ++l)
+      if (!f.b[l] || f.b[l]->bytes < elems(l) * sizeof(T)) {
+        ctx.pool.give(std::move(f.b[l]));
+        f.b[l] = ctx.pool.take(elems(l) * sizeof(T));
+      }
   }
   T *ptr(Field &f, int l) { return f.b[l]->template as<T>(); }
   void zero(Field &f, int l) { GIC_CUDA(cudaMemsetAsync(f.b[l]->ptr, 0, elems(l) * sizeof(T), ctx.stream)); }
@@ -367,19 +425,18 @@ struct ModEngine {
   }
   double kcut(int l) { return 0.3 * ((double)lev(l).n * lev(l).kmin()); }
 
-  DevBuf tab;
   void table(const TableSpec &sp0, int g) {
     long long half = lev(g).n / 2, nq = 3 * half * half + 1;
-    tab.ensure(nq * sizeof(double));
+    S.tab.ensure(nq * sizeof(double));
     TableSpec sp = sp0;
     sp.kmin = lev(g).kmin();
-    k_mod_table<<<nblk(nq), 256, 0, ctx.stream>>>(tab.template as<double>(), nq, sp);
+    k_mod_table<<<nblk(nq), 256, 0, ctx.stream>>>(S.tab.template as<double>(), nq, sp);
     launched();
   }
 
   void mul_table(T *p, int g) {
     k_mul_table<T><<<hs_grid(lev(g).n), hs_block(), 0, ctx.stream>>>(reinterpret_cast<C *>(p), lev(g).n,
-                                                                     tab.template as<double>());
+                                                                     S.tab.template as<double>());
     launched();
   }
   void axpy(T *a, const T *b, double c, int l) {
@@ -391,27 +448,54 @@ struct ModEngine {
     launched();
   }
 
-  double inner(Field &a, Field &b) {
+  // one term of an inner product: two half spectra, or two padded real fields, of level l
+  struct Term {
+    const T *a, *b;
+    int l;
+    bool real;
+  };
+  // sum of each group's terms; every group has the same number of terms, and all
+  // groups are read back together
+  std::vector<double> inner_groups(const std::vector<std::vector<Term>> &groups) {
     const int blocks = 152 * 8;
-    int L = nl();
-    ctx.reduce.ensure(((size_t)L * blocks + 1) * sizeof(double));
-    double *part = ctx.reduce.template as<double>();
-    for (int l = 0; l < L; ++l) {
-      to_fourier(a, l);
-      to_fourier(b, l);
-      k_inner<T><<<blocks, hs_block(), 0, ctx.stream>>>(ptr(a, l), ptr(b, l), lev(l).n, part + (size_t)l * blocks);
-      launched();
-    }
-    k_sum<<<1, 256, 0, ctx.stream>>>(part, L * blocks, part + (size_t)L * blocks);
+    const int np = (int)groups.size(), nt = np ? (int)groups[0].size() : 0;
+    const size_t per = (size_t)nt * blocks;
+    S.reduce.ensure((per * np + np) * sizeof(double));
+    double *part = S.reduce.template as<double>();
+    for (int p = 0; p < np; ++p)
+      for (int i = 0; i < nt; ++i) {
+        const Term &t = groups[p][i];
+        double *dst = part + per * p + (size_t)i * blocks;
+        if (t.real)
+          k_inner_real<T><<<blocks, hs_block(), 0, ctx.stream>>>(t.a, t.b, lev(t.l).n, dst);
+        else
+          k_inner<T><<<blocks, hs_block(), 0, ctx.stream>>>(t.a, t.b, lev(t.l).n, dst);
+        launched();
+      }
+    k_sum<<<np, 256, 0, ctx.stream>>>(part, (int)per, part + per * np);
     launched();
-    double total = 0;
-    GIC_CUDA(cudaMemcpyAsync(&total, part + (size_t)L * blocks, sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+    std::vector<double> out(np);
+    GIC_CUDA(cudaMemcpyAsync(out.data(), part + per * np, np * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
     GIC_CUDA(cudaStreamSynchronize(ctx.stream));
-    return total;
+    return out;
   }
+  // <a_i|b_i> for every pair, summed over levels, in Fourier space
+  std::vector<double> inner_many(const std::vector<std::pair<Field *, Field *>> &pairs) {
+    std::vector<std::vector<Term>> groups;
+    for (auto &pr : pairs) {
+      std::vector<Term> g;
+      for (int l = 0; l < nl(); ++l) {
+        to_fourier(*pr.first, l);
+        to_fourier(*pr.second, l);
+        g.push_back({ptr(*pr.first, l), ptr(*pr.second, l), l, false});
+      }
+      groups.push_back(std::move(g));
+    }
+    return inner_groups(groups);
+  }
+  double inner(Field &a, Field &b) { return inner_many({{&a, &b}})[0]; }
 
   // window of level wl on the cells of level l, per axis (window.hpp)
-  DevBuf masks;
   void window_masks(int l, int wl) {
     const Level &L = lev(l), &W = lev(wl);
     double P = L.periodic;
@@ -429,14 +513,14 @@ struct ModEngine {
         m[(size_t)a * L.n + i] = in ? 1 : 0;
       }
     }
-    masks.ensure(m.size());
-    GIC_CUDA(cudaMemcpyAsync(masks.ptr, m.data(), m.size(), cudaMemcpyHostToDevice, ctx.stream));
+    S.masks.ensure(m.size());
+    GIC_CUDA(cudaMemcpyAsync(S.masks.ptr, m.data(), m.size(), cudaMemcpyHostToDevice, ctx.stream));
     GIC_CUDA(cudaStreamSynchronize(ctx.stream));
   }
-  void mask(T *real, int l, int zero_inside) {
+  void window_op(T *r, const T *src, int l, int op) {
     int n = lev(l).n;
-    unsigned char *m = masks.template as<unsigned char>();
-    k_mask<T><<<nblk(lev(l).ncells()), 256, 0, ctx.stream>>>(real, n, m, m + n, m + 2 * n, zero_inside);
+    unsigned char *m = S.masks.template as<unsigned char>();
+    k_window_op<T><<<real_grid(n), hs_block(), 0, ctx.stream>>>(r, src, n, m, m + n, m + 2 * n, op);
     launched();
   }
 
@@ -450,7 +534,6 @@ struct ModEngine {
     mul_table(p, l);
   }
 
-  DevBuf tmp_src;
   double level_weight(int l) {
     double r = lev(l).dx / lev(0).dx;
     return r * r * r;
@@ -462,13 +545,13 @@ struct ModEngine {
     add_filter_factors(sp, t);
     add_filter_factors(sp, s);
     sp.scalar = std::sqrt(level_weight(t) / level_weight(s));
-    tmp_src.ensure(elems(s) * sizeof(T));
-    GIC_CUDA(cudaMemcpyAsync(tmp_src.ptr, source_k, elems(s) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
+    S.tmp_src.ensure(elems(s) * sizeof(T));
+    GIC_CUDA(cudaMemcpyAsync(S.tmp_src.ptr, source_k, elems(s) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
     table(sp, s);
-    mul_table(tmp_src.template as<T>(), s);
-    to_real(tmp_src.template as<T>(), s);
+    mul_table(S.tmp_src.template as<T>(), s);
+    to_real(S.tmp_src.template as<T>(), s);
     if (s < t) {
-      const T *src[1] = {tmp_src.template as<T>()};
+      const T *src[1] = {S.tmp_src.template as<T>()};
       T *dst[1] = {target_real};
       interp_add<T, 1>(ctx, lev(s), src, lev(t), dst);
     } else {
@@ -477,7 +560,7 @@ struct ModEngine {
       int sx = (int)std::lround((F.x0[0] - Cl.x0[0]) / Cl.dx), sy = (int)std::lround((F.x0[1] - Cl.x0[1]) / Cl.dx),
           sz = (int)std::lround((F.x0[2] - Cl.x0[2]) / Cl.dx);
       size_t m = (size_t)(F.n / r);
-      k_subsample_add<T><<<nblk(m * m * m), 256, 0, ctx.stream>>>(tmp_src.template as<T>(), F.n, r, sx, sy, sz, target_real,
+      k_subsample_add<T><<<nblk(m * m * m), 256, 0, ctx.stream>>>(S.tmp_src.template as<T>(), F.n, r, sx, sy, sz, target_real,
                                                                   Cl.n);
       launched();
     }
@@ -487,34 +570,13 @@ struct ModEngine {
   void apply_metric(Field &X, Field &out, bool to_covector) {
     for (int l = 0; l < nl(); ++l) to_fourier(X, l);
     alloc(out);
-    DevBuf inw;
+    DevBuf &inw = S.win;
     for (int t = 0; t < nl(); ++t) {
       T *R = ptr(out, t);
       GIC_CUDA(cudaMemcpyAsync(R, ptr(X, t), elems(t) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
       if (to_covector && t < nl() - 1) {
-        window_masks(t, t + 1);
-        inw.ensure(elems(t) * sizeof(T));
-        T *I = inw.template as<T>();
-        // applyFilterInWindow(f, window, windowFirst = true)
-        GIC_CUDA(cudaMemcpyAsync(I, R, elems(t) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
-        to_real(I, t);
-        mask(I, t, 0);
-        to_fourier(I, t);
-        apply_family(I, t, 1);
         to_real(R, t);
-        mask(R, t, 1);
-        to_fourier(R, t);
-        axpy(R, I, 1.0, t);
-        // applyFilterInWindow(f, window, windowFirst = false)
-        GIC_CUDA(cudaMemcpyAsync(I, R, elems(t) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
-        apply_family(I, t, 1);
-        to_real(I, t);
-        mask(I, t, 0);
-        to_real(R, t);
-        mask(R, t, 1);
-        axpy(R, I, 1.0, t);
-        for (int s = 0; s < nl(); ++s)
-          if (s != t) cross_term_impl(R, t, ptr(X, s), s);
+        windowed_covector_real(X, t, R);
         to_fourier(R, t);
       } else {
         // f_t^2 X_t stays in Fourier space; the cross-level terms are summed in real
@@ -534,24 +596,88 @@ struct ModEngine {
     }
   }
 
+  // Towards a covector on a level t with a finer level inside it: R (real, holding
+  // X_t in real space on entry) becomes, in real space,
+  //   g = f (W x) + (1 - W) x            applyFilterInWindow(f, window, true)
+  //   R = W f g + (1 - W) g              applyFilterInWindow(f, window, false)
+  // plus the cross-level terms (field.hpp:752-775, multilevelfield.hpp:344-384).
+  // The reference transforms after each masking; the sums are formed here in real
+  // space, which needs four transforms instead of six.
+  void windowed_covector_real(Field &X, int t, T *R) {
+    window_masks(t, t + 1);
+    S.win.ensure(elems(t) * sizeof(T));
+    T *I = S.win.template as<T>();
+    window_op(I, R, t, 2);  // I = W x
+    to_fourier(I, t);
+    apply_family(I, t, 1);
+    to_real(I, t);
+    window_op(R, I, t, 0);  // g = (1 - W) x + f (W x)
+    GIC_CUDA(cudaMemcpyAsync(I, R, elems(t) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
+    to_fourier(I, t);
+    apply_family(I, t, 1);
+    to_real(I, t);
+    window_op(R, I, t, 1);  // R = W (f g) + (1 - W) g
+    for (int s = 0; s < nl(); ++s)
+      if (s != t) cross_term_impl(R, t, ptr(X, s), s);
+  }
+
+  // <C_cov X | X> (OutputField::getChi2 through the covector metric), with the
+  // windowed levels' terms summed in real space
+  double chi2(Field &X) {
+    for (int l = 0; l < nl(); ++l) to_fourier(X, l);
+    std::vector<std::unique_ptr<DevBuf>> keep;
+    std::vector<Term> terms;
+    for (int t = 0; t < nl(); ++t) {
+      const size_t bytes = elems(t) * sizeof(T);
+      if (t < nl() - 1) {
+        auto R = ctx.pool.take(bytes), xr = ctx.pool.take(bytes);
+        GIC_CUDA(cudaMemcpyAsync(R->ptr, ptr(X, t), bytes, cudaMemcpyDeviceToDevice, ctx.stream));
+        to_real(R->template as<T>(), t);
+        GIC_CUDA(cudaMemcpyAsync(xr->ptr, R->ptr, bytes, cudaMemcpyDeviceToDevice, ctx.stream));
+        windowed_covector_real(X, t, R->template as<T>());
+        terms.push_back({R->template as<T>(), xr->template as<T>(), t, true});
+        keep.push_back(std::move(R));
+        keep.push_back(std::move(xr));
+      } else {
+        auto R = ctx.pool.take(bytes);
+        T *r = R->template as<T>();
+        GIC_CUDA(cudaMemcpyAsync(r, ptr(X, t), bytes, cudaMemcpyDeviceToDevice, ctx.stream));
+        apply_family(r, t, 2);
+        if (nl() > 1) {
+          S.win.ensure(bytes);
+          T *Cr = S.win.template as<T>();
+          GIC_CUDA(cudaMemsetAsync(Cr, 0, bytes, ctx.stream));
+          for (int s = 0; s < nl(); ++s)
+            if (s != t) cross_term_impl(Cr, t, ptr(X, s), s);
+          to_fourier(Cr, t);
+          axpy(r, Cr, 1.0, t);
+        }
+        terms.push_back({r, ptr(X, t), t, false});
+        keep.push_back(std::move(R));
+      }
+    }
+    double v = inner_groups({terms})[0];
+    for (auto &b : keep) ctx.pool.give(std::move(b));
+    return v;
+  }
+
   // covector of one modification (kind 0 overdensity, 1..3 velocity x,y,z)
-  DevBuf cells;
   void covector(Field &out, int kind, const unsigned long long *flagged, size_t count) {
     int F = nl() - 1;
     alloc(out);
     for (int l = 0; l < nl(); ++l) zero(out, l);
-    cells.ensure(count * sizeof(unsigned long long));
-    GIC_CUDA(cudaMemcpyAsync(cells.ptr, flagged, count * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+    S.cells.ensure(count * sizeof(unsigned long long));
+    GIC_CUDA(cudaMemcpyAsync(S.cells.ptr, flagged, count * sizeof(unsigned long long), cudaMemcpyHostToDevice,
                              ctx.stream));
     double w = 1.0 / (double)count;
     double a = -w / 12. / lev(F).dx, b = w * 2. / 3. / lev(F).dx;
-    k_localise<T><<<nblk(count), 256, 0, ctx.stream>>>(ptr(out, F), lev(F).n, cells.template as<unsigned long long>(), count,
+    k_localise<T><<<nblk(count), 256, 0, ctx.stream>>>(ptr(out, F), lev(F).n, S.cells.template as<unsigned long long>(), count,
                                                       kind == 0 ? 0 : 1, kind == 0 ? 0 : kind - 1, w, a, b);
     launched();
+    // the reference transforms the localisation covector to Fourier space and back
+    // before deinterpolating; that round trip is the identity and is skipped
     out.fourier[F] = 0;
-    to_fourier(out, F);
     if (F > 0) {
-      to_real(out, F);
       for (int l = F - 1; l >= 0; --l) {
         out.fourier[l] = 0;
         deinterpolate(ptr(out, l + 1), l + 1, ptr(out, l), l);
@@ -577,14 +703,13 @@ struct ModEngine {
   void build_sqrtp_dm(int l);
 
   // transpose tricubic: fine real (level f) / r^3 added into coarse real (level c)
-  DevBuf geom, t1, t2, t3;
   void deinterpolate(const T *fine, int f, T *coarse, int c) {
     const Level &Fl = lev(f), &Cl = lev(c);
     int nf = Fl.n;
     int r = (int)std::lround(Cl.dx / Fl.dx);
     T scale = (T)(1.0 / ((double)r * r * r));
-    geom.ensure(3 * (size_t)nf * (sizeof(int) + sizeof(T)));
-    int *ub = geom.template as<int>();
+    S.geom.ensure(3 * (size_t)nf * (sizeof(int) + sizeof(T)));
+    int *ub = S.geom.template as<int>();
     T *fr = reinterpret_cast<T *>(ub + 3 * nf);
     k_axes_geom<T><<<nblk(3 * nf, 128), 128, 0, ctx.stream>>>(nf, Fl.dx, Fl.x0[0], Fl.x0[1], Fl.x0[2], Cl.x0[0],
                                                               Cl.x0[1], Cl.x0[2], Cl.dx, Cl.periodic, Cl.n, ub, fr);
@@ -599,25 +724,25 @@ struct ModEngine {
     }
     const long long frs = 2 * (nf / 2 + 1);
     // pass x: fine (nf, nf, nf) padded -> t1 (cnt0, nf, nf)
-    t1.ensure((size_t)cnt[0] * nf * nf * sizeof(T));
-    GIC_CUDA(cudaMemsetAsync(t1.ptr, 0, (size_t)cnt[0] * nf * nf * sizeof(T), ctx.stream));
+    S.t1.ensure((size_t)cnt[0] * nf * nf * sizeof(T));
+    GIC_CUDA(cudaMemsetAsync(S.t1.ptr, 0, (size_t)cnt[0] * nf * nf * sizeof(T), ctx.stream));
     k_deinterp_pass<T><<<nblk((size_t)nf * nf), 256, 0, ctx.stream>>>(
-        fine, (long long)nf * frs, frs, t1.template as<T>(), (long long)nf * nf, nf, 0, nf, nf, nf, nf, ub, fr, c0[0], cnt[0],
+        fine, (long long)nf * frs, frs, S.t1.template as<T>(), (long long)nf * nf, nf, 0, nf, nf, nf, nf, ub, fr, c0[0], cnt[0],
         scale);
     // pass y: t1 (cnt0, nf, nf) -> t2 (cnt0, cnt1, nf)
-    t2.ensure((size_t)cnt[0] * cnt[1] * nf * sizeof(T));
-    GIC_CUDA(cudaMemsetAsync(t2.ptr, 0, (size_t)cnt[0] * cnt[1] * nf * sizeof(T), ctx.stream));
+    S.t2.ensure((size_t)cnt[0] * cnt[1] * nf * sizeof(T));
+    GIC_CUDA(cudaMemsetAsync(S.t2.ptr, 0, (size_t)cnt[0] * cnt[1] * nf * sizeof(T), ctx.stream));
     k_deinterp_pass<T><<<nblk((size_t)cnt[0] * nf), 256, 0, ctx.stream>>>(
-        t1.template as<T>(), (long long)nf * nf, nf, t2.template as<T>(), (long long)cnt[1] * nf, nf, 1, cnt[0], nf, nf, nf, ub + nf,
+        S.t1.template as<T>(), (long long)nf * nf, nf, S.t2.template as<T>(), (long long)cnt[1] * nf, nf, 1, cnt[0], nf, nf, nf, ub + nf,
         fr + nf, c0[1], cnt[1], (T)1);
     // pass z: t2 (cnt0, cnt1, nf) -> t3 (cnt0, cnt1, cnt2)
-    t3.ensure((size_t)cnt[0] * cnt[1] * cnt[2] * sizeof(T));
-    GIC_CUDA(cudaMemsetAsync(t3.ptr, 0, (size_t)cnt[0] * cnt[1] * cnt[2] * sizeof(T), ctx.stream));
+    S.t3.ensure((size_t)cnt[0] * cnt[1] * cnt[2] * sizeof(T));
+    GIC_CUDA(cudaMemsetAsync(S.t3.ptr, 0, (size_t)cnt[0] * cnt[1] * cnt[2] * sizeof(T), ctx.stream));
     k_deinterp_pass<T><<<nblk((size_t)cnt[0] * cnt[1]), 256, 0, ctx.stream>>>(
-        t2.template as<T>(), (long long)cnt[1] * nf, nf, t3.template as<T>(), (long long)cnt[1] * cnt[2], cnt[2], 2, cnt[0], cnt[1], nf,
+        S.t2.template as<T>(), (long long)cnt[1] * nf, nf, S.t3.template as<T>(), (long long)cnt[1] * cnt[2], cnt[2], 2, cnt[0], cnt[1], nf,
         nf, ub + 2 * nf, fr + 2 * nf, c0[2], cnt[2], (T)1);
     size_t m = (size_t)cnt[0] * cnt[1] * cnt[2];
-    k_add_block<T><<<nblk(m), 256, 0, ctx.stream>>>(t3.template as<T>(), cnt[0], cnt[1], cnt[2], c0[0], c0[1], c0[2], coarse,
+    k_add_block<T><<<nblk(m), 256, 0, ctx.stream>>>(S.t3.template as<T>(), cnt[0], cnt[1], cnt[2], c0[0], c0[1], c0[2], coarse,
                                                    Cl.n);
     launched(4);
   }
@@ -657,10 +782,9 @@ static double current_value(Context &ctx, const ModRequest &m) {
 template <typename T>
 static double chi2_of_noise(Context &ctx) {
   ModEngine<T> E(ctx);
-  typename ModEngine<T>::Field W, cov;
+  typename ModEngine<T>::Field W;
   noise_field(E, W);
-  E.apply_metric(W, cov, true);
-  return E.inner(cov, W);
+  return E.chi2(W);
 }
 
 template <typename T>
@@ -672,16 +796,22 @@ static void apply_mods(Context &ctx, double *chi2_before, double *chi2_after) {
   F W;
   noise_field(E, W);
   std::vector<F> alpha(n), vec(n);
-  std::vector<double> b(n), t(n);
+  std::vector<double> t(n);
   for (int i = 0; i < n; ++i) {
     E.covector(alpha[i], ctx.mods[i].kind, ctx.mods[i].cells.data(), ctx.mods[i].cells.size());
     E.apply_metric(alpha[i], vec[i], false);
-    b[i] = E.inner(alpha[i], W);
     t[i] = ctx.mods[i].target;
   }
-  std::vector<double> G((size_t)n * n);
+  // <a_i|W> and the Gram matrix G_ij = <a_i|C a_j>, read back together.  G is not
+  // assumed symmetric: the cross-level terms of C (interpolation up, block means
+  // down) are not exact transposes of each other.
+  std::vector<std::pair<F *, F *>> pairs;
+  for (int i = 0; i < n; ++i) pairs.push_back({&alpha[i], &W});
   for (int i = 0; i < n; ++i)
-    for (int j = 0; j < n; ++j) G[(size_t)i * n + j] = E.inner(alpha[i], vec[j]);
+    for (int j = 0; j < n; ++j) pairs.push_back({&alpha[i], &vec[j]});
+  std::vector<double> ip_all = E.inner_many(pairs);
+  std::vector<double> b(ip_all.begin(), ip_all.begin() + n);
+  std::vector<double> G(ip_all.begin() + n, ip_all.end());
   // Gram-Schmidt in the order of modificationmanager.hpp:288-312, on coefficient
   // vectors: row i of L holds a'_i = sum_k L[i][k] a_k
   std::vector<double> L((size_t)n * n, 0.0);
