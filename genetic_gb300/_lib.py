@@ -72,6 +72,9 @@ SIGNATURES = {
     'gic_calculate': [_P, _I, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_size_t, _D],
     'gic_add_modification': [_P, _I, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_size_t, ctypes.c_double, _I],
     'gic_clear_modifications': [_P],
+    'gic_calculate_variance': [_P, ctypes.POINTER(_P), ctypes.POINTER(ctypes.c_size_t), ctypes.c_double, _D],
+    'gic_add_variance_modification': [_P, ctypes.POINTER(_P), ctypes.POINTER(ctypes.c_size_t), ctypes.c_double,
+                                      ctypes.c_double, _I, _I, ctypes.c_double],
     'gic_apply_modifications': [_P, _D, _D],
     'gic_get_stream': [_P, ctypes.POINTER(_P)],
 }

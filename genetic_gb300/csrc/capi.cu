@@ -417,12 +417,63 @@ int gic_add_modification(gic_ctx *ctx, int kind, const unsigned long long *cells
 int gic_clear_modifications(gic_ctx *ctx) {
   API_BEGIN(ctx)
   C.mods.clear();
+  C.quads.clear();
+  API_END
+}
+
+// checkFilterScale (quadraticmodification.hpp:131-153) and the per-level cell lists
+static gic::QuadRequest make_quad_request(gic::Context &C, const unsigned long long *const *cells, const size_t *counts,
+                                          double scale) {
+  if (C.levels.empty()) gic::fail(GIC_ERR_NOT_READY, "no grid levels");
+  if (!cells || !counts) gic::fail(GIC_ERR_INVALID_ARG, "null cell lists");
+  if (scale < 0.0)
+    gic::fail(GIC_ERR_INVALID_ARG,
+              "Trying to calculate filtered variance without initialising variance filtering scale. Use "
+              "filtering_scale command to do this.");
+  if (scale < C.levels.back()->dx)
+    gic::fail(GIC_ERR_INVALID_ARG, "Variance high-pass filtering scale is smaller than the smallest pixel size.");
+  gic::QuadRequest q;
+  q.scale = scale;
+  for (size_t l = 0; l < C.levels.size(); ++l) {
+    size_t m = C.levels[l]->ncells();
+    if (counts[l] && !cells[l]) gic::fail(GIC_ERR_INVALID_ARG, "null cell list");
+    std::vector<unsigned long long> v(cells[l], cells[l] + counts[l]);
+    for (size_t i = 0; i < v.size(); ++i) {
+      if (v[i] >= m) gic::fail(GIC_ERR_INVALID_ARG, "flagged cell outside its grid");
+      if (i && v[i] <= v[i - 1]) gic::fail(GIC_ERR_INVALID_ARG, "flagged cells must be sorted and unique");
+    }
+    q.cells.push_back(std::move(v));
+  }
+  if (q.cells.back().empty())
+    gic::fail(GIC_ERR_INVALID_ARG, "no cells have been flagged on the finest grid");
+  return q;
+}
+
+int gic_calculate_variance(gic_ctx *ctx, const unsigned long long *const *cells, const size_t *counts,
+                           double filterscale, double *value) {
+  API_BEGIN(ctx)
+  if (!value) gic::fail(GIC_ERR_INVALID_ARG, "null output");
+  gic::QuadRequest q = make_quad_request(C, cells, counts, filterscale);
+  *value = gic::variance_value(C, q);
+  API_END
+}
+
+int gic_add_variance_modification(gic_ctx *ctx, const unsigned long long *const *cells, const size_t *counts,
+                                  double filterscale, double target, int relative, int init_steps, double precision) {
+  API_BEGIN(ctx)
+  if (init_steps < 2) gic::fail(GIC_ERR_INVALID_ARG, "init_steps must be at least 2");
+  if (!(precision > 0)) gic::fail(GIC_ERR_INVALID_ARG, "precision must be positive");
+  gic::QuadRequest q = make_quad_request(C, cells, counts, filterscale);
+  q.init_steps = init_steps;
+  q.precision = precision;
+  q.target = relative ? target * gic::variance_value(C, q) : target;
+  C.quads.push_back(std::move(q));
   API_END
 }
 
 int gic_apply_modifications(gic_ctx *ctx, double *chi2_before, double *chi2_after) {
   API_BEGIN(ctx)
-  if (C.mods.empty()) gic::fail(GIC_ERR_NOT_READY, "no modifications to apply");
+  if (C.mods.empty() && C.quads.empty()) gic::fail(GIC_ERR_NOT_READY, "no modifications to apply");
   gic::apply_modifications(C, chi2_before, chi2_after);
   API_END
 }

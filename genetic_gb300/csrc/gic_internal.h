@@ -78,7 +78,7 @@ struct BufPool {
 // scratch of the modification algebra (one user at a time; each buffer is used
 // within a single operation)
 struct ModScratch {
-  DevBuf tab, masks, tmp_src, win, cells, geom, t1, t2, t3, reduce;
+  DevBuf tab, masks, tmp_src, win, cells, geom, t1, t2, t3, reduce, compact, csum;
 };
 
 // One grid level: N^3 cells of a cube of side `box` whose lower corner is x0.
@@ -139,6 +139,14 @@ struct ModRequest {
   double target;
 };
 
+// variance of the high-passed dark-matter overdensity over flagged cells
+struct QuadRequest {
+  std::vector<std::vector<unsigned long long>> cells;  // flagged cells per level (sorted)
+  std::vector<std::unique_ptr<DevBuf>> dcells;         // their device copies
+  double scale = 0, target = 0, precision = 0.001;
+  int init_steps = 10;
+};
+
 struct Context {
   int device = 0;
   int precision = GIC_FP64;
@@ -154,6 +162,7 @@ struct Context {
   DevBuf zoom_scratch[4];  // low-passed coarse fields during zoom combination
   DevBuf geom;             // per-axis interpolation / centroid tables
   std::vector<ModRequest> mods;
+  std::vector<QuadRequest> quads;
   BufPool pool;
   ModScratch modscratch;
   bool dbl() const { return precision == GIC_FP64; }
@@ -183,6 +192,7 @@ void interp_add(Context &ctx, const Level &coarse, const T *const *src, const Le
 // modify.cu
 double modification_value(Context &ctx, const ModRequest &m);
 double noise_chi2(Context &ctx);
+double variance_value(Context &ctx, QuadRequest &q);
 void apply_modifications(Context &ctx, double *chi2_before, double *chi2_after);
 
 // particles.cu

@@ -44,6 +44,7 @@ struct TableSpec {
   double scalar;
   const double *sqrtp;
   double vel;
+  double var_cut;  // > 0: times 1 - LP(k; var_cut), the variance high-pass
 };
 
 __device__ __forceinline__ double fermi_lp(double k, double kcut) {
@@ -61,6 +62,7 @@ __global__ void k_mod_table(double *out, long long nq, TableSpec sp) {
     f *= sqrt(1. - lp * lp);
   }
   for (int i = 0; i < sp.nlp; ++i) f *= fermi_lp(k, sp.lp_cut[i]);
+  if (sp.var_cut > 0) f *= 1. - fermi_lp(k, sp.var_cut);
   if (sp.power == 2) f = f * f;
   f *= sp.scalar;
   if (sp.sqrtp) f *= sp.sqrtp[q];
@@ -231,6 +233,41 @@ __global__ void k_sum(const double *in, int n, double *out) {
     __syncthreads();
   }
   if (threadIdx.x == 0) *out = red[0];
+}
+
+// flagged cells (compact linear indices (x n + y) n + z) of a padded real field
+__device__ __forceinline__ size_t padded_index(unsigned long long c, int n) {
+  unsigned long long row = c / (unsigned)n;
+  return (size_t)row * (size_t)(2 * (n / 2 + 1)) + (size_t)(c - row * (unsigned)n);
+}
+template <typename T>
+__global__ void k_gather_cells(const T *real, int n, const unsigned long long *cells, size_t count, T *out) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) out[i] = real[padded_index(cells[i], n)];
+}
+template <typename T>
+__global__ void k_scatter_cells(const T *in, int n, const unsigned long long *cells, size_t count, T *real) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) real[padded_index(cells[i], n)] = in[i];
+}
+// the variance operator on the flagged values: v = (v - mean) / count, the mean
+// summed in double in one block (quadraticmodification.hpp:199-218)
+template <typename T>
+__global__ void k_center_cells(T *v, size_t count) {
+  __shared__ double red[1024];
+  __shared__ double mean;
+  double acc = 0;
+  for (size_t i = threadIdx.x; i < count; i += blockDim.x) acc += (double)v[i];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) mean = red[0] / (double)count;
+  __syncthreads();
+  const T m = (T)mean, c = (T)(double)count;
+  for (size_t i = threadIdx.x; i < count; i += blockDim.x) v[i] = (v[i] - m) / c;
 }
 
 // localisation covector on the finest grid (padded real layout)
@@ -459,6 +496,7 @@ struct ModEngine {
   std::vector<double> inner_groups(const std::vector<std::vector<Term>> &groups) {
     const int blocks = 152 * 8;
     const int np = (int)groups.size(), nt = np ? (int)groups[0].size() : 0;
+    if (np == 0) return {};
     const size_t per = (size_t)nt * blocks;
     S.reduce.ensure((per * np + np) * sizeof(double));
     double *part = S.reduce.template as<double>();
@@ -661,6 +699,92 @@ struct ModEngine {
     return v;
   }
 
+  // --- quadratic (variance) modification ---------------------------------------
+
+  void upload_cells(QuadRequest &q) {
+    if (q.dcells.size() == q.cells.size()) return;
+    q.dcells.clear();
+    for (auto &c : q.cells) {
+      auto b = std::make_unique<DevBuf>();
+      if (!c.empty()) {
+        b->ensure(c.size() * sizeof(unsigned long long));
+        GIC_CUDA(cudaMemcpyAsync(b->ptr, c.data(), c.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                                 ctx.stream));
+      }
+      q.dcells.push_back(std::move(b));
+    }
+  }
+
+  // real field of level l: keep the flagged cells, zero the rest; with `center`,
+  // also apply the variance operator to the kept values
+  void window_cells(T *real, int l, QuadRequest &q, bool center) {
+    const size_t count = q.cells[l].size();
+    const unsigned long long *cells = q.dcells[l]->template as<unsigned long long>();
+    T *v = nullptr;
+    if (count) {
+      S.compact.ensure(count * sizeof(T));
+      v = S.compact.template as<T>();
+      k_gather_cells<T><<<nblk(count), 256, 0, ctx.stream>>>(real, lev(l).n, cells, count, v);
+      launched();
+      if (center) {
+        k_center_cells<T><<<1, 1024, 0, ctx.stream>>>(v, count);
+        launched();
+      }
+    }
+    GIC_CUDA(cudaMemsetAsync(real, 0, elems(l) * sizeof(T), ctx.stream));
+    if (count) {
+      k_scatter_cells<T><<<nblk(count), 256, 0, ctx.stream>>>(v, lev(l).n, cells, count, real);
+      launched();
+    }
+  }
+
+  void mul_sqrtp_dm(T *p, int l) {
+    build_sqrtp_dm(l);
+    TableSpec sp{};
+    sp.power = 1;
+    sp.scalar = 1.0;
+    sp.sqrtp = lev(l).sqrtp_dm.template as<double>();
+    table(sp, l);
+    mul_table(p, l);
+  }
+
+  void mul_variance_highpass(T *p, int l, double scale) {
+    TableSpec sp{};
+    sp.power = 1;
+    sp.scalar = 1.0;
+    sp.var_cut = 2. * M_PI / scale;
+    table(sp, l);
+    mul_table(p, l);
+  }
+
+  // QuadraticModification::pushMultiLevelFieldThroughMatrix (quadraticmodification.hpp:59-92)
+  // with FilteredVarianceModification::pushOneLevelFieldThroughMatrix (:152-170):
+  // out = sqrt(P) C_cov [W F V F W] sqrt(P) X, a covector in Fourier space
+  void push_variance(Field &X, QuadRequest &q, Field &out) {
+    upload_cells(q);
+    Field R;
+    alloc(R);
+    for (int l = 0; l < nl(); ++l) {
+      to_fourier(X, l);
+      T *p = ptr(R, l);
+      GIC_CUDA(cudaMemcpyAsync(p, ptr(X, l), elems(l) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
+      mul_sqrtp_dm(p, l);
+      to_real(p, l);
+      window_cells(p, l, q, false);
+      to_fourier(p, l);
+      mul_variance_highpass(p, l, q.scale);
+      to_real(p, l);
+      window_cells(p, l, q, true);  // windowOperator then the variance operator
+      to_fourier(p, l);
+      mul_variance_highpass(p, l, q.scale);
+      to_real(p, l);
+      window_cells(p, l, q, false);
+      R.fourier[l] = 0;
+    }
+    apply_metric(R, out, true);
+    for (int l = 0; l < nl(); ++l) mul_sqrtp_dm(ptr(out, l), l);
+  }
+
   // covector of one modification (kind 0 overdensity, 1..3 velocity x,y,z)
   void covector(Field &out, int kind, const unsigned long long *flagged, size_t count) {
     int F = nl() - 1;
@@ -787,6 +911,91 @@ static double chi2_of_noise(Context &ctx) {
   return E.chi2(W);
 }
 
+// tools::linspace (util_functions.hpp:77-92): n + 1 points for n > 1
+static std::vector<double> linspace_targets(double start, double end, int n) {
+  std::vector<double> a;
+  if (n == 0 || n == 1 || start == end) {
+    a.push_back(end);
+  } else {
+    double step = (end - start) / n;
+    for (int c = 0; c < n + 1; ++c) a.push_back(start + c * step);
+  }
+  return a;
+}
+
+// ModificationManager::performIterations (modificationmanager.hpp:249-275) with
+// addToOrthonormalFamily (:318-333).  `lin` are the linear modifications'
+// orthonormalised vectors and D their plain products D[m][j] = <v_m|v_j>.  The
+// pushed covector of the start value is reused by the first step (the reference
+// recomputes it on the unchanged field).
+template <typename T>
+static void perform_iterations(ModEngine<T> &E, typename ModEngine<T>::Field &X,
+                               std::vector<typename ModEngine<T>::Field> &lin, const std::vector<double> &D,
+                               QuadRequest &q, int n_steps) {
+  using F = typename ModEngine<T>::Field;
+  const int n = (int)lin.size();
+  F P, CP, CP2;
+  E.push_variance(X, q, P);
+  const double start = E.inner(P, X);
+  std::vector<double> targets = linspace_targets(start, q.target, n_steps);
+  if ((int)targets.size() < n_steps + 1) fail(GIC_ERR_INVALID_ARG, "the quadratic algorithm needs at least 2 steps");
+  for (int i = 0; i < n_steps; ++i) {
+    if (i > 0) E.push_variance(X, q, P);
+    E.apply_metric(P, CP, false);
+    std::vector<std::pair<F *, F *>> pairs{{&P, &X}, {&P, &CP}};
+    for (int j = 0; j < n; ++j) pairs.push_back({&P, &lin[j]});
+    std::vector<double> ip = E.inner_many(pairs);
+    const double current = ip[0], norm = std::sqrt(ip[1]);
+    double scale_vec = 1.0;
+    F *vec = &CP;
+    if (n > 0) {
+      // p <- p - r_j v_j in order, r_j = <p|v_j> with p already reduced by v_0..v_{j-1}
+      std::vector<double> r(n);
+      for (int j = 0; j < n; ++j) {
+        r[j] = ip[2 + j];
+        for (int m = 0; m < j; ++m) r[j] -= r[m] * D[(size_t)m * n + j];
+      }
+      for (int l = 0; l < E.nl(); ++l)
+        for (int j = 0; j < n; ++j) E.axpy(E.ptr(P, l), E.ptr(lin[j], l), -r[j], l);
+      E.apply_metric(P, CP2, false);
+      scale_vec = 1.0 / std::sqrt(E.inner(P, CP2));
+      vec = &CP2;
+    } else {
+      scale_vec = 1.0 / norm;
+    }
+    const double mult = 0.5 * (targets[i + 1] - current) / norm;
+    for (int l = 0; l < E.nl(); ++l) E.axpy(E.ptr(X, l), E.ptr(*vec, l), mult * scale_vec, l);
+  }
+}
+
+// applyLinQuadModif (modificationmanager.hpp:221-246) and calculateCorrectNumberSteps (:278-285)
+template <typename T>
+static void apply_quadratic(ModEngine<T> &E, typename ModEngine<T>::Field &W,
+                            std::vector<typename ModEngine<T>::Field> &lin, QuadRequest &q) {
+  using F = typename ModEngine<T>::Field;
+  const int n = (int)lin.size();
+  std::vector<double> D;
+  if (n > 0) {
+    std::vector<std::pair<F *, F *>> pairs;
+    for (int m = 0; m < n; ++m)
+      for (int j = 0; j < n; ++j) pairs.push_back({&lin[m], &lin[j]});
+    D = E.inner_many(pairs);
+  }
+  int steps = q.init_steps;
+  {
+    F test;
+    E.copy(test, W);
+    perform_iterations<T>(E, test, lin, D, q, q.init_steps);
+    F P;
+    E.push_variance(test, q, P);
+    const double achieved = std::fabs(E.inner(P, test) - q.target);
+    const double wanted = q.target * q.precision;
+    const int n_steps = q.init_steps * (int)std::ceil(std::sqrt(achieved / wanted));
+    if (n_steps > q.init_steps) steps = n_steps;
+  }
+  perform_iterations<T>(E, W, lin, D, q, steps);
+}
+
 template <typename T>
 static void apply_mods(Context &ctx, double *chi2_before, double *chi2_after) {
   ModEngine<T> E(ctx);
@@ -841,13 +1050,42 @@ static void apply_mods(Context &ctx, double *chi2_before, double *chi2_after) {
     double d = t[i] - existing;
     for (int k = 0; k < n; ++k) coef[k] += d * L[(size_t)i * n + k];
   }
-  for (int l = 0; l < E.nl(); ++l) {
+  for (int l = 0; l < E.nl(); ++l)
     for (int k = 0; k < n; ++k) E.axpy(E.ptr(W, l), E.ptr(vec[k], l), coef[k], l);
+  if (!ctx.quads.empty()) {
+    // applyLinearModif leaves the orthonormalised covectors converted to vectors,
+    // C a'_i = sum_k L[i][k] C a_k; the quadratic steps project against those
+    std::vector<F> lin(n);
+    for (int i = 0; i < n; ++i) {
+      E.alloc(lin[i]);
+      for (int l = 0; l < E.nl(); ++l) {
+        E.zero(lin[i], l);
+        for (int k = 0; k < n; ++k) E.axpy(E.ptr(lin[i], l), E.ptr(vec[k], l), L[(size_t)i * n + k], l);
+      }
+    }
+    alpha.clear();
+    vec.clear();
+    for (auto &q : ctx.quads) apply_quadratic<T>(E, W, lin, q);
+  }
+  for (int l = 0; l < E.nl(); ++l) {
     E.copy_level(E.lev(l).noise, *W.b[l], l);
     E.lev(l).have_fields = false;
   }
   GIC_CUDA(cudaStreamSynchronize(ctx.stream));
   if (chi2_after) *chi2_after = chi2_of_noise<T>(ctx);
+}
+
+template <typename T>
+static double variance_value_t(Context &ctx, QuadRequest &q) {
+  ModEngine<T> E(ctx);
+  typename ModEngine<T>::Field W, P;
+  noise_field(E, W);
+  E.push_variance(W, q, P);
+  return E.inner(P, W);
+}
+
+double variance_value(Context &ctx, QuadRequest &q) {
+  return ctx.dbl() ? variance_value_t<double>(ctx, q) : variance_value_t<float>(ctx, q);
 }
 
 double modification_value(Context &ctx, const ModRequest &m) {

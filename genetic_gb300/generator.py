@@ -161,18 +161,21 @@ class ICGenerator:
         self.centre_point = (float(x), float(y), float(z))
 
     def _select(self, inside):
-        """Flag the cells of the finest level whose wrapped offset from the centre passes `inside`."""
-        box, n, off = self.levels[-1]
+        """Flag, on every level, the cells whose wrapped offset from the centre passes
+        `inside` (ic.hpp:1458-1485)."""
         period = self.levels[0][0]
-        dx = box / n
-        d = []
-        for a in range(3):
-            x = np.arange(n) * dx + off[a] + dx / 2 - self.centre_point[a]
-            x = np.where(x > period / 2, x - period, x)
-            x = np.where(x < -period / 2, x + period, x)
-            d.append(x)
-        X, Y, Z = np.meshgrid(d[0], d[1], d[2], indexing='ij')
-        self.flagged = np.ascontiguousarray(np.flatnonzero(inside(X, Y, Z).ravel()), dtype=np.uint64)
+        self.flagged_levels = []
+        for box, n, off in self.levels:
+            dx = box / n
+            d = []
+            for a in range(3):
+                x = np.arange(n) * dx + off[a] + dx / 2 - self.centre_point[a]
+                x = np.where(x > period / 2, x - period, x)
+                x = np.where(x < -period / 2, x + period, x)
+                d.append(x)
+            X, Y, Z = np.meshgrid(d[0], d[1], d[2], indexing='ij')
+            self.flagged_levels.append(np.ascontiguousarray(np.flatnonzero(inside(X, Y, Z).ravel()), dtype=np.uint64))
+        self.flagged = self.flagged_levels[-1]
 
     def select_sphere(self, radius):
         r2 = float(np.float32(radius) * np.float32(radius))
@@ -192,9 +195,31 @@ class ICGenerator:
                                'but no cells have been flagged on this grid.')
         return self.flagged.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong)), len(self.flagged)
 
+    # quadratic modifications: ic.hpp:150-161 (filtering scale, 10 initial steps, 0.001 precision)
+    variance_filterscale = -1.0
+    initial_number_steps = 10
+    precision_target = 0.001
+
+    def filtering_scale(self, scale):
+        """setVarianceFilteringScale (ic.hpp:355-358), parsed as a double."""
+        self.variance_filterscale = float(scale)
+
+    def _level_cells(self):
+        flagged = getattr(self, 'flagged_levels', None)
+        if flagged is None or len(flagged) != len(self.levels):
+            flagged = [np.zeros(0, dtype=np.uint64) for _ in self.levels]
+        self._keep = flagged
+        ptrs = (ctypes.c_void_p * len(flagged))(*[f.ctypes.data if len(f) else None for f in flagged])
+        counts = (ctypes.c_size_t * len(flagged))(*[len(f) for f in flagged])
+        return ptrs, counts
+
     def calculate(self, name):
         self.draw()
         v = ctypes.c_double()
+        if name.lower() == 'variance':
+            ptrs, counts = self._level_cells()
+            self._call('gic_calculate_variance', ptrs, counts, self.variance_filterscale, ctypes.byref(v))
+            return v.value
         cells, n = self._cells()
         self._call('gic_calculate', self._KINDS[name], cells, n, ctypes.byref(v))
         return v.value
@@ -203,8 +228,13 @@ class ICGenerator:
         """`modify name absolute|relative target`; genetIC parses the target as a float (ic.hpp:1613)."""
         self.draw()
         rel = {'relative': 1, 'absolute': 0}[kind.lower()]
-        cells, n = self._cells()
-        self._call('gic_add_modification', self._KINDS[name], cells, n, float(np.float32(target)), rel)
+        if name.lower() == 'variance':
+            ptrs, counts = self._level_cells()
+            self._call('gic_add_variance_modification', ptrs, counts, self.variance_filterscale,
+                       float(np.float32(target)), rel, self.initial_number_steps, self.precision_target)
+        else:
+            cells, n = self._cells()
+            self._call('gic_add_modification', self._KINDS[name], cells, n, float(np.float32(target)), rel)
         self._nmods = getattr(self, '_nmods', 0) + 1
 
     def clear_modifications(self):
@@ -283,6 +313,7 @@ _COMMANDS = {
     'seedfourier_reverse': 'seedfourier_reverse', 'done': 'done', 'chi2': 'chi2',
     'centre': 'centre', 'select_sphere': 'select_sphere', 'select_cube': 'select_cube',
     'calculate': 'calculate', 'modify': 'modify', 'clear_modifications': 'clear_modifications',
+    'filtering_scale': 'filtering_scale',
     'apply_modifications': 'apply_modifications',
 }
 # output-side commands handled by genetIC's own writers; accepted and ignored here

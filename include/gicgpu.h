@@ -156,6 +156,28 @@ GIC_API int gic_add_modification(gic_ctx *ctx, int kind, const unsigned long lon
                                  int relative);
 GIC_API int gic_clear_modifications(gic_ctx *ctx);
 
+/* Quadratic modification: the variance, over the flagged cells of each level, of
+ * the dark-matter overdensity high-passed at `filterscale` (Mpc/h; the filter is
+ * 1 - a Fermi low-pass at k = 2 pi / filterscale).  `cells[l]` / `counts[l]` hold
+ * the flagged cells of level l as sorted linear indices, one array per level.
+ * Replaces FilteredVarianceModification::calculateCurrentValue
+ * (quadraticmodification.hpp:51-57, 118-221) reached through
+ * ModificationManager::calculateCurrentValueByName (modificationmanager.hpp:37-45).
+ * Fails with GIC_ERR_INVALID_ARG when filterscale is negative (never set) or
+ * below the finest cell size, as checkFilterScale (quadraticmodification.hpp:131-153). */
+GIC_API int gic_calculate_variance(gic_ctx *ctx, const unsigned long long *const *cells, const size_t *counts,
+                                   double filterscale, double *value);
+
+/* Queue a variance modification (absolute, or relative to its current value).
+ * gic_apply_modifications applies it after the linear ones by the reference's
+ * iterative scheme: a trial of `init_steps` steps on a copy fixes the number of
+ * steps from `precision` (modificationmanager.hpp:221-285; genetIC uses 10 and
+ * 0.001, ic.hpp:160-161).  Replaces ModificationManager::addModificationToList for
+ * "variance" (modificationmanager.hpp:59-82, 188-196). */
+GIC_API int gic_add_variance_modification(gic_ctx *ctx, const unsigned long long *const *cells, const size_t *counts,
+                                          double filterscale, double target, int relative, int init_steps,
+                                          double precision);
+
 /* Apply the queued modifications to the white noise (orthonormalised, with the
  * covariance metric), returning chi^2 before and after.  Replaces
  * ModificationManager::applyModifications (modificationmanager.hpp:90-125). */

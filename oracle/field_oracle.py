@@ -615,9 +615,10 @@ def chi2_levels(levels, noise_k):
     return inner(apply_metric(levels, noise_k, True), noise_k)
 
 
-def apply_linear_modifications(levels, noise_k, covectors, targets):
+def apply_linear_modifications(levels, noise_k, covectors, targets, return_vectors=False):
     """Gram-Schmidt + correction (modificationmanager.hpp:199-217, 288-312), restated
-    with the same operation order; returns the modified noise."""
+    with the same operation order; returns the modified noise (and, with
+    return_vectors, the orthonormalised covectors converted to vectors)."""
     alphas = [[c.copy() for c in cv] for cv in covectors]
     t = list(targets)
     n = len(alphas)
@@ -631,8 +632,96 @@ def apply_linear_modifications(levels, noise_k, covectors, targets):
         t[i] /= nrm
     existing = [inner(a, noise_k) for a in alphas]
     out = [w.copy() for w in noise_k]
+    vectors = []
     for i in range(n):
         vec = apply_metric(levels, alphas[i], False)
+        vectors.append(vec)
         d = t[i] - existing[i]
         out = [o + d * v for o, v in zip(out, vec)]
+    if return_vectors:
+        return out, vectors
     return out
+
+
+# --- quadratic (variance) modification (quadraticmodification.hpp, modificationmanager.hpp) ---
+
+def variance_highpass(k, scale):
+    """1 - LP_Fermi(k; 2 pi / scale) (ComplementaryFilterAdaptor, quadraticmodification.hpp:187-195)."""
+    return 1. - fermi_lowpass(k, 2. * np.pi / scale)
+
+
+def push_variance(levels, field_k, flagged, scale, power_dm):
+    """<field| Q as a covector (QuadraticModification::pushMultiLevelFieldThroughMatrix,
+    quadraticmodification.hpp:59-92, and FilteredVarianceModification::
+    pushOneLevelFieldThroughMatrix, :152-221): per level x = sqrt(P_dm) w, then
+    window, high-pass, variance (window, minus the region mean, / n), high-pass,
+    window; the covector metric; sqrt(P_dm) again.  flagged: cells per level."""
+    pushed = []
+    sp = []
+    for l in range(len(levels)):
+        box, n, _ = levels.levels[l]
+        sp.append(sqrt_power_grid(power_dm, n, box))
+        hp = variance_highpass(kmag(n, box), scale)
+        fl = np.asarray(flagged[l], dtype=np.int64)
+
+        def window(v):
+            out = np.zeros(n ** 3)
+            out[fl] = v.ravel()[fl]
+            return out.reshape(n, n, n)
+
+        xr = window(fft_c2r(field_k[l] * sp[l]))
+        xr = window(fft_c2r(fft_r2c(xr) * hp))
+        flat = xr.ravel()
+        mean = float(np.sum(flat[fl])) / len(fl)
+        flat[fl] = (flat[fl] - mean) / len(fl)
+        xr = window(fft_c2r(fft_r2c(flat.reshape(n, n, n)) * hp))
+        pushed.append(fft_r2c(xr))
+    cov = apply_metric(levels, pushed, True)
+    return [c * s for c, s in zip(cov, sp)]
+
+
+def variance_value(levels, field_k, flagged, scale, power_dm):
+    """QuadraticModification::calculateCurrentValue (quadraticmodification.hpp:51-57)."""
+    return inner(push_variance(levels, field_k, flagged, scale, power_dm), field_k)
+
+
+def linspace_targets(start, end, n):
+    """tools::linspace (util_functions.hpp:77-92): n+1 points for n > 1."""
+    if n in (0, 1) or start == end:
+        return [end]
+    step = (end - start) / n
+    return [start + c * step for c in range(n + 1)]
+
+
+def perform_quadratic_iterations(levels, field_k, lin_vectors, flagged, scale, power_dm, target, n_steps):
+    """ModificationManager::performIterations (modificationmanager.hpp:249-275) with
+    addToOrthonormalFamily (:318-333).  lin_vectors are the orthonormalised linear
+    covectors after applyLinearModif converted them to vectors in place (:168-182),
+    so the projection uses plain products with them."""
+    field = [f.copy() for f in field_k]
+    start = variance_value(levels, field, flagged, scale, power_dm)
+    targets = linspace_targets(start, target, n_steps)
+    for i in range(n_steps):
+        p = push_variance(levels, field, flagged, scale, power_dm)
+        current = inner(p, field)
+        norm = np.sqrt(inner(p, apply_metric(levels, p, False)))
+        for v in lin_vectors:
+            r = inner(p, v)
+            p = [a - r * b for a, b in zip(p, v)]
+        n2 = np.sqrt(inner(p, apply_metric(levels, p, False)))
+        p = [a / n2 for a in p]
+        mult = 0.5 * (targets[i + 1] - current) / norm
+        vec = apply_metric(levels, p, False)
+        field = [f + mult * v for f, v in zip(field, vec)]
+    return field
+
+
+def apply_quadratic_modification(levels, field_k, lin_vectors, flagged, scale, power_dm, target,
+                                 init_steps=10, precision=0.001):
+    """applyLinQuadModif (modificationmanager.hpp:221-246) with calculateCorrectNumberSteps
+    (:278-285): a trial on a copy fixes the number of steps.  Returns (field, steps)."""
+    test = perform_quadratic_iterations(levels, field_k, lin_vectors, flagged, scale, power_dm, target, init_steps)
+    achieved = abs(variance_value(levels, test, flagged, scale, power_dm) - target)
+    n_steps = init_steps * int(np.ceil(np.sqrt(achieved / (target * precision))))
+    steps = n_steps if n_steps > init_steps else init_steps
+    return perform_quadratic_iterations(levels, field_k, lin_vectors, flagged, scale, power_dm, target, steps), steps

@@ -151,6 +151,59 @@ def mod_goldens():
                                 **{k: np.array(v) for k, v in vals.items()})
 
 
+VARS = {
+    # one level: variance of the 4 Mpc/h high-passed overdensity in an 8 Mpc/h sphere,
+    # with the mean overdensity held and the variance tripled (20 steps after the trial)
+    'var1': """centre 25 25 25
+select_sphere 8
+filtering_scale 4
+calculate variance
+calculate overdensity
+modify overdensity relative 1
+modify variance relative 3
+done
+dump_grid 0
+""",
+    # two levels: zoom factor 2 around the centre; 4 Mpc/h sphere flagged on both levels
+    'var2': """centre 25 25 25
+select_cube 10
+zoom_grid_with_origin_at 8 8 8 2 32
+centre 25 25 25
+select_sphere 4
+filtering_scale 3
+calculate variance
+calculate overdensity
+modify overdensity relative 1
+modify variance relative 1.5
+done
+dump_grid 0
+dump_grid 1
+""",
+}
+
+
+def var_goldens():
+    import re
+    for name, tail in VARS.items():
+        with tempfile.TemporaryDirectory() as d:
+            write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+            open(os.path.join(d, 'paramfile.txt'), 'w').write(MOD_BASE + tail)
+            r = subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True, text=True)
+            log = r.stdout + r.stderr
+            vals = {}
+            for key, pat in (('variance', r'variance: calculated value = (\S+)'),
+                             ('overdensity', r'overdensity: calculated value = (\S+)'),
+                             ('chi2_post', r'Post-modification chi\^2 = (\S+)'),
+                             ('delta_chi2', r'Modification Delta chi\^2 = (\S+)')):
+                vals[key] = float(re.search(pat, log).group(1))
+            m = re.search(r'(\d+) steps are required for the quadratic algorithm', log)
+            vals['steps'] = int(m.group(1)) if m else 10
+            nlev = 2 if name == 'var2' else 1
+            grids = {'delta%d' % l: np.load(os.path.join(d, 'grid-%d.npy' % l)) for l in range(nlev)}
+            np.savez_compressed(os.path.join(HERE, '%s.npz' % name), **grids,
+                                **{k: np.array(v) for k, v in vals.items()})
+
+
 def main():
     for mode, cmd in (('serial', 'random_seed_serial'), ('parallel', 'random_seed'), ('real', 'random_seed_real_space')):
         with tempfile.TemporaryDirectory() as d:
@@ -170,3 +223,4 @@ if __name__ == '__main__':
     main()
     zoom_goldens()
     mod_goldens()
+    var_goldens()

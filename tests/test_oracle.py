@@ -78,7 +78,8 @@ needs_reference = pytest.mark.skipif(not (os.path.isdir(REF_TESTS) and os.path.e
 
 @needs_reference
 @pytest.mark.parametrize('name', ['test_02k_chisquare_onelevel', 'test_02m_chisquare_twolevels',
-                                  'test_02l_chisquare_modification', 'test_02f_onelevelvariance'])
+                                  'test_02l_chisquare_modification', 'test_02f_onelevelvariance',
+                                  'test_02g_multilevelvariance'])
 def test_reference_build_log_fixtures(tmp_path, name):
     import re
     d, out = _run_reference(tmp_path, name)
@@ -172,3 +173,102 @@ def test_modification_oracle_matches_reference(bbks, case):
     for l in range(len(levels)):
         ref = g['delta%d' % l].astype(np.float64)
         assert np.abs(out[l][0] - ref).max() <= 2e-7 * np.abs(ref).max()
+
+
+# --- quadratic (variance) modification ----------------------------------------------
+
+REF_COSMO = dict(omega_m=0.279, omega_lambda=0.721, omega_b=0.0, hubble=0.701, sigma8=0.817, ns=0.96, redshift=99.0)
+needs_reference_tests = pytest.mark.skipif(not os.path.isdir(REF_TESTS), reason='reference test fixtures not present')
+
+
+def _ref_camb():
+    from genetic_gb300.transfer import read_camb
+    return read_camb(os.path.join(REF_TESTS, 'camb_transfer_kmax40_z0.dat'))
+
+
+@needs_reference_tests
+@pytest.mark.parametrize('name,levels,centre,size,want', [
+    # test_02f_onelevelvariance: select_cube 20 at (8, 8, 8), filtering_scale 10000
+    ('02f', [(64.0, 64, (0, 0, 0))], (8., 8., 8.), 20, '0.00182096'),
+    # test_02g_multilevelvariance: zoom 4x at the origin, select_cube 16 at (8, 8, 8)
+    ('02g', [(64.0, 64, (0, 0, 0)), (16.0, 64, (0., 0., 0.))], (8., 8., 8.), 16, '0.00396257'),
+])
+def test_variance_oracle_matches_reference_values(name, levels, centre, size, want):
+    np.seterr(over='ignore')
+    L = fo.Levels(levels)
+    fo.set_cr_log(False)
+    w = fo.white_noise_levels([l[1] for l in levels], 8896131, 0)
+    fl = [fo.flag_cells(L, l, centre, 'cube', size) for l in range(len(levels))]
+    p_dm = fo.CambPower(_ref_camb(), REF_COSMO, column=1)
+    assert '%.6g' % fo.variance_value(L, w, fl, 10000., p_dm) == want
+
+
+@needs_reference_tests
+def test_quadratic_oracle_matches_reference_grids():
+    """test_02i_multilevel_algorithm: overdensity held, variance doubled, two levels."""
+    np.seterr(over='ignore')
+    levels = [(64.0, 64, (0, 0, 0)), (16.0, 64, (24., 24., 24.))]
+    L = fo.Levels(levels)
+    fo.set_cr_log(False)
+    w = fo.white_noise_levels([64, 64], 8896131, 0)
+    fl = [fo.flag_cells(L, l, (32.5, 32.5, 32.5), 'cube', 6.0) for l in range(2)]
+    p_dm = fo.CambPower(_ref_camb(), REF_COSMO, column=1)
+    cv = fo.multilevel_covector(L, fo.localisation_covector(L, fl[-1], 'overdensity'), p_dm, None)
+    od, var = fo.inner(cv, w), fo.variance_value(L, w, fl, 2.0, p_dm)
+    assert ('%.6g' % od, '%.6g' % var) == ('0.00298075', '0.00232681')
+    before = fo.chi2_levels(L, w)
+    w1, vecs = fo.apply_linear_modifications(L, w, [cv], [od], return_vectors=True)
+    w2, steps = fo.apply_quadratic_modification(L, w1, vecs, fl, 2.0, p_dm, 2.0 * var)
+    assert steps == 10
+    assert '%.6g' % (fo.chi2_levels(L, w2) - before) == '3893.93'
+    out = fo.zoom_realisation(w2, levels, fo.CambPower(_ref_camb(), REF_COSMO))
+    for l in range(2):
+        ref = np.load(os.path.join(REF_TESTS, 'test_02i_multilevel_algorithm', 'reference_grid', 'grid-%d.npy' % l))
+        # the reference fixture was written with FFTW; the oracle's exact DFTs differ by ~3e-9 after the iterations
+        assert np.abs(out[l][0] - ref).max() <= 1e-8 * np.abs(ref).max()
+
+
+VAR_CASES = {
+    'var1': dict(levels=[(50.0, 32, (0.0, 0.0, 0.0))], select=('sphere', 8), scale=4.0, rel=3.0),
+    'var2': dict(levels=[(50.0, 32, (0.0, 0.0, 0.0)), (25.0, 32, (12.5, 12.5, 12.5))], select=('sphere', 4),
+                 scale=3.0, rel=1.5),
+}
+
+
+def oracle_variance(bbks, case, cr_log=False):
+    """Values, step count, chi^2 and modified noise of a VAR_CASES entry (overdensity
+    held at its value, variance scaled by `rel`), from the oracle."""
+    from conftest import COSMO
+    np.seterr(over='ignore')
+    c = VAR_CASES[case]
+    L = fo.Levels(c['levels'])
+    fo.set_cr_log(cr_log)
+    w = fo.white_noise_levels([l[1] for l in c['levels']], 8896131, 2)
+    fo.set_cr_log(False)
+    p_dm = fo.CambPower(bbks, COSMO, column=1)
+    fl = [fo.flag_cells(L, l, (25., 25., 25.), *c['select']) for l in range(len(c['levels']))]
+    cv = fo.multilevel_covector(L, fo.localisation_covector(L, fl[-1], 'overdensity'), p_dm, None)
+    od, var = fo.inner(cv, w), fo.variance_value(L, w, fl, c['scale'], p_dm)
+    before = fo.chi2_levels(L, w)
+    w1, vecs = fo.apply_linear_modifications(L, w, [cv], [od], return_vectors=True)
+    target = float(np.float32(c['rel'])) * var
+    w2, steps = fo.apply_quadratic_modification(L, w1, vecs, fl, c['scale'], p_dm, target)
+    after = fo.chi2_levels(L, w2)
+    return dict(levels=L, noise=w, modified=w2, overdensity=od, variance=var, steps=steps, chi2=(before, after),
+                flagged=fl, target=target, final=fo.variance_value(L, w2, fl, c['scale'], p_dm))
+
+
+@pytest.mark.parametrize('case', ['var1', 'var2'])
+def test_variance_oracle_matches_goldens(bbks, case):
+    from conftest import COSMO
+    g = _load_golden('%s.npz' % case)
+    r = oracle_variance(bbks, case)
+    assert '%.6g' % r['variance'] == '%.6g' % float(g['variance'])
+    assert '%.6g' % r['overdensity'] == '%.6g' % float(g['overdensity'])
+    assert r['steps'] == int(g['steps'])
+    assert '%.6g' % (r['chi2'][1] - r['chi2'][0]) == '%.6g' % float(g['delta_chi2'])
+    assert abs(r['final'] / r['target'] - 1) < 1e-3
+    out = fo.zoom_realisation(r['modified'], VAR_CASES[case]['levels'], fo.CambPower(bbks, COSMO))
+    for l in range(len(VAR_CASES[case]['levels'])):
+        ref = g['delta%d' % l]
+        assert np.abs(out[l][0] - ref).max() <= 1e-11 * np.abs(ref).max(), l
