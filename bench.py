@@ -159,6 +159,18 @@ def measured_peak_hbm():
         return 6800.0, 'fallback'
 
 
+def profiled_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summaries (profiles/*.md), or None."""
+    import glob
+    import re
+    for path in sorted(glob.glob(os.path.join(ROOT, 'profiles', '*.md'))):
+        for line in open(path):
+            m = re.match(r'traffic_bytes (.+): (\d+)\s*$', line)
+            if m and m.group(1) == kernel:
+                return int(m.group(2))
+    return None
+
+
 def fft_roofline(gen, wl, stream, reps=20):
     """Average device time of one inverse 3-D FFT of the finest level's delta field."""
     import torch
@@ -185,9 +197,10 @@ def fft_roofline(gen, wl, stream, reps=20):
     algorithmic = 6.0 * (2 * s) * nc  # 3 passes, read + write of the half spectrum
     peak, kind = measured_peak_hbm()
     achieved = algorithmic / t / 1e9
+    kernel = 'fft_c2r_3d (%d^3, %s)' % (n, 'fp32' if s == 4 else 'fp64')
     return {'bound': 'hbm', 'achieved': round(achieved, 1), 'peak': peak, 'unit': 'GB/s',
-            'frac': round(achieved / peak, 4), 'traffic': None, 'kernel': 'fft_c2r_3d (%d^3, %s)' % (
-                n, 'fp32' if s == 4 else 'fp64'), 'ms_per_launch': round(t * 1e3, 4), 'peak_source': kind}
+            'frac': round(achieved / peak, 4), 'traffic': profiled_traffic(kernel), 'kernel': kernel,
+            'ms_per_launch': round(t * 1e3, 4), 'peak_source': kind}
 
 
 def cpu_baseline_port(n=192, box=75.0, threads=None):
