@@ -3,6 +3,8 @@
 // every failure into a status code plus a message.
 #include "gic_internal.h"
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <exception>
 #include <new>
@@ -202,6 +204,17 @@ int gic_create(gic_ctx **out, const gic_device_opts *opts) {
     gic::g_create_error = cudaGetErrorString(cudaGetLastError());
     delete c;
     return GIC_ERR_CUDA;
+  }
+  // GIC_FFT_TILE selects the FFT passes by hand instead of the tuner: "generic"
+  // (runtime-length kernels) or "<cols>,<rows>" (fixed-length tile candidates)
+  if (const char *t = std::getenv("GIC_FFT_TILE")) {
+    int a = -1, b = -1;
+    if (std::strcmp(t, "generic") == 0) {
+      c->impl.fft.force_cols = -2;
+    } else if (std::sscanf(t, "%d,%d", &a, &b) == 2 && a >= 0 && b >= 0) {
+      c->impl.fft.force_cols = a;
+      c->impl.fft.force_rows = b;
+    }
   }
   *out = c;
   return GIC_OK;

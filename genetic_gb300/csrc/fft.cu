@@ -399,11 +399,336 @@ __global__ void k_mirror(typename Cx<T>::type *data, int N) {
   data[((size_t)kx * N + ky) * S + kz] = cconj(data[((size_t)sx * N + sy) * S + kz]);
 }
 
+// ---- fixed-length passes (power-of-two lengths): one padded tile, in place ----
+// A CTA owns TC transforms of compile-time length L held as a tile [L][TC + 1] in
+// shared memory (column c of the tile is one transform; the +1 pad makes row
+// strides odd in 8-byte words).  Each Stockham stage reads every butterfly's
+// inputs into registers, synchronises, and writes its outputs back in place, so
+// one buffer suffices.  Butterflies are numbered with the column fastest:
+// neighbouring threads touch neighbouring words of a tile row, free of bank
+// conflicts.  The radix schedule (8, then 4 or 2 for the remainder) and every
+// index are compile-time constants.
+
+template <typename T, int L, int TC, int TCP, int NT, int R, int NS, int SIGN, int TWM>
+__device__ __forceinline__ void tile_stage(typename Cx<T>::type *tile, const typename Cx<T>::type *tw) {
+  using C = typename Cx<T>::type;
+  constexpr int LR = L / R, NB = LR * TC, PER = (NB + NT - 1) / NT;
+  C v[PER][R];
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int b = threadIdx.x + p * NT;
+    if (NB % NT == 0 || b < NB) {
+      const int c = b % TC, j = b / TC;
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[p][r] = tile[(j + r * LR) * TCP + c];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int b = threadIdx.x + p * NT;
+    if (NB % NT == 0 || b < NB) {
+      const int c = b % TC, j = b / TC;
+      const int jm = j % NS, jq = j / NS;
+      if (NS > 1) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[p][r] = cmul(v[p][r], twid(tw, TWM * r * jm * (L / (NS * R)), SIGN));
+      }
+      Dft<T, C, R>::run(v[p], SIGN);
+      const int d = jq * NS * R + jm;
+#pragma unroll
+      for (int r = 0; r < R; ++r) tile[(d + r * NS) * TCP + c] = v[p][r];
+    }
+  }
+  __syncthreads();
+}
+
+template <typename T, int L, int TC, int TCP, int NT, int NS, int SIGN, int TWM, bool DONE = (NS >= L)>
+struct TileStages {
+  static __device__ __forceinline__ void run(typename Cx<T>::type *tile, const typename Cx<T>::type *tw) {
+    constexpr int R = (L / NS) >= 8 ? 8 : (L / NS);
+    tile_stage<T, L, TC, TCP, NT, R, NS, SIGN, TWM>(tile, tw);
+    TileStages<T, L, TC, TCP, NT, NS * R, SIGN, TWM>::run(tile, tw);
+  }
+};
+template <typename T, int L, int TC, int TCP, int NT, int NS, int SIGN, int TWM>
+struct TileStages<T, L, TC, TCP, NT, NS, SIGN, TWM, true> {
+  static __device__ __forceinline__ void run(typename Cx<T>::type *, const typename Cx<T>::type *) {}
+};
+
+// strided pass over (A, L, B) complex, transform along L; grid (ceil(B / TC), A)
+template <typename T, int L, int TC, int NT, int SIGN>
+__global__ void __launch_bounds__(NT) k_fft_cols(typename Cx<T>::type *data, long long B,
+                                                 const typename Cx<T>::type *tw, T scale) {
+  using C = typename Cx<T>::type;
+  constexpr int TCP = TC + 1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C *tile = reinterpret_cast<C *>(smraw);
+  const long long b0 = (long long)blockIdx.x * TC;
+  C *base = data + (size_t)blockIdx.y * (size_t)L * (size_t)B + b0;
+  const int tcv = (int)min((long long)TC, B - b0);
+  for (int e = threadIdx.x; e < L * TC; e += NT) {
+    const int i = e / TC, c = e % TC;
+    if (c < tcv) {
+      cp_async<sizeof(C)>(tile + i * TCP + c, base + (size_t)i * (size_t)B + c);
+    } else {
+      C z;
+      z.x = 0;
+      z.y = 0;
+      tile[i * TCP + c] = z;
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  TileStages<T, L, TC, TCP, NT, 1, SIGN, 1>::run(tile, tw);
+  for (int e = threadIdx.x; e < L * TC; e += NT) {
+    const int i = e / TC, c = e % TC;
+    if (c < tcv) base[(size_t)i * (size_t)B + c] = cscale(tile[i * TCP + c], scale);
+  }
+}
+
+// c2r rows of N = 2H reals: rows of H + 1 Hermitian coefficients are copied
+// (coalesced) into a tile [H + 1][RPC + 1] with one row per tile column, packed
+// into H complex values, transformed, and copied back as N reals per row.
+template <typename T, int H, int RPC, int NT>
+__global__ void __launch_bounds__(NT) k_fft_rows_c2r_fixed(typename Cx<T>::type *data, long long nrows,
+                                                           const typename Cx<T>::type *tw, T scale) {
+  using C = typename Cx<T>::type;
+  constexpr int S = H + 1, TCP = RPC + 1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C *tile = reinterpret_cast<C *>(smraw);
+  const long long r0 = (long long)blockIdx.x * RPC;
+  const int rows_valid = (int)min((long long)RPC, nrows - r0);
+  C *base = data + (size_t)r0 * S;
+  for (int e = threadIdx.x; e < RPC * S; e += NT) {
+    const int row = e / S, m = e % S;
+    if (row < rows_valid) {
+      cp_async<sizeof(C)>(tile + m * TCP + row, base + e);
+    } else {
+      C z;
+      z.x = 0;
+      z.y = 0;
+      tile[m * TCP + row] = z;
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  // Z[k] = E + i O, E = X[k] + conj X[H-k], O = (X[k] - conj X[H-k]) e^{+2 pi i k / N};
+  // Z[k] and Z[H-k] both come from X[k] and X[H-k], so pairs are done in place
+  for (int e = threadIdx.x; e < RPC * (H / 2 + 1); e += NT) {
+    const int row = e % RPC, k = e / RPC;
+    C a = tile[k * TCP + row], bq = tile[(H - k) * TCP + row];
+    if (k == 0) {
+      a.y = 0;
+      bq.y = 0;
+    }
+    C bc = cconj(bq);
+    C zk = cadd(cadd(a, bc), cmuli(cmul(csub(a, bc), twid(tw, k, +1)), +1));
+    if (k != 0 && 2 * k != H) {
+      C ac = cconj(a);
+      C zh = cadd(cadd(bq, ac), cmuli(cmul(csub(bq, ac), twid(tw, H - k, +1)), +1));
+      tile[(H - k) * TCP + row] = zh;
+    }
+    tile[k * TCP + row] = zk;
+  }
+  __syncthreads();
+  TileStages<T, H, RPC, TCP, NT, 1, +1, 2>::run(tile, tw);
+  for (int e = threadIdx.x; e < RPC * H; e += NT) {
+    const int row = e / H, m = e % H;
+    if (row < rows_valid) base[(size_t)row * S + m] = cscale(tile[m * TCP + row], scale);
+  }
+}
+
+// r2c rows: N reals per row (read as H complex) -> H + 1 coefficients
+template <typename T, int H, int RPC, int NT>
+__global__ void __launch_bounds__(NT) k_fft_rows_r2c_fixed(typename Cx<T>::type *data, long long nrows,
+                                                           const typename Cx<T>::type *tw, T scale) {
+  using C = typename Cx<T>::type;
+  constexpr int S = H + 1, TCP = RPC + 1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C *tile = reinterpret_cast<C *>(smraw);
+  const long long r0 = (long long)blockIdx.x * RPC;
+  const int rows_valid = (int)min((long long)RPC, nrows - r0);
+  C *base = data + (size_t)r0 * S;
+  for (int e = threadIdx.x; e < RPC * H; e += NT) {
+    const int row = e / H, m = e % H;
+    if (row < rows_valid) {
+      cp_async<sizeof(C)>(tile + m * TCP + row, base + (size_t)row * S + m);
+    } else {
+      C z;
+      z.x = 0;
+      z.y = 0;
+      tile[m * TCP + row] = z;
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  TileStages<T, H, RPC, TCP, NT, 1, -1, 2>::run(tile, tw);
+  // X[k] = (Z[k] + conj Z[H-k]) / 2 - i/2 e^{-2 pi i k / N} (Z[k] - conj Z[H-k]), k in [0, H]
+  // (Z[H] = Z[0]); X[k] and X[H-k] both come from Z[k] and Z[H-k]
+  for (int e = threadIdx.x; e < RPC * (H / 2 + 1); e += NT) {
+    const int row = e % RPC, k = e / RPC;
+    C zk = tile[(k == 0 ? 0 : k) * TCP + row];
+    C zh = tile[(k == 0 ? 0 : H - k) * TCP + row];
+    C zhc = cconj(zh), zkc = cconj(zk);
+    C xk = cadd(cscale(cadd(zk, zhc), (T)0.5), cmuli(cmul(cscale(csub(zk, zhc), (T)0.5), twid(tw, k, -1)), -1));
+    C xh = cadd(cscale(cadd(zh, zkc), (T)0.5), cmuli(cmul(cscale(csub(zh, zkc), (T)0.5), twid(tw, H - k, -1)), -1));
+    if (2 * k != H) tile[(H - k) * TCP + row] = xh;
+    tile[k * TCP + row] = xk;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < RPC * S; e += NT) {
+    const int row = e / S, m = e % S;
+    if (row < rows_valid) base[e] = cscale(tile[m * TCP + row], scale);
+  }
+}
+
 template <typename T>
 void set_smem(const void *fn, size_t bytes) {
   static size_t current = 0;
   (void)current;
   GIC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+}
+
+// launchers of the fixed-length passes; candidate tile widths per precision:
+//   strided: (TC, threads) = FP32 (8, 256) | (16, 512), FP64 (4, 256) | (8, 256)
+//   rows:    (RPC, threads) = FP32 (8, 256) | (16, 256), FP64 (4, 256) | (8, 256)
+constexpr int kFixedCandidates = 2;
+
+inline void set_smem_once(const void *fn, size_t bytes, int &done_mask) {
+  int dev = 0;
+  GIC_CUDA(cudaGetDevice(&dev));
+  if (done_mask & (1 << (dev & 31))) return;
+  GIC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  done_mask |= 1 << (dev & 31);
+}
+
+template <typename T, int N>
+struct FixedFft {
+  using C = typename Cx<T>::type;
+  static constexpr int H = N / 2, S = H + 1;
+  static constexpr bool F32 = sizeof(T) == 4;
+
+  template <int TC, int NT, int SIGN>
+  static void cols(Context &ctx, C *d, int A, long long B, const C *tw, T scale) {
+    static int mask = 0;
+    const size_t smem = (size_t)N * (TC + 1) * sizeof(C);
+    set_smem_once((const void *)k_fft_cols<T, N, TC, NT, SIGN>, smem, mask);
+    dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)A);
+    k_fft_cols<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale);
+    launched();
+  }
+  template <int RPC, int NT, bool INV>
+  static void rows(Context &ctx, C *d, const C *tw, T scale) {
+    static int mask = 0;
+    const size_t smem = (size_t)S * (RPC + 1) * sizeof(C);
+    const long long nrows = (long long)N * N;
+    const unsigned grid = (unsigned)((nrows + RPC - 1) / RPC);
+    if (INV) {
+      set_smem_once((const void *)k_fft_rows_c2r_fixed<T, H, RPC, NT>, smem, mask);
+      k_fft_rows_c2r_fixed<T, H, RPC, NT><<<grid, NT, smem, ctx.stream>>>(d, nrows, tw, scale);
+    } else {
+      set_smem_once((const void *)k_fft_rows_r2c_fixed<T, H, RPC, NT>, smem, mask);
+      k_fft_rows_r2c_fixed<T, H, RPC, NT><<<grid, NT, smem, ctx.stream>>>(d, nrows, tw, scale);
+    }
+    launched();
+  }
+  static void cols_cfg(Context &ctx, int cfg, int sign, C *d, int A, long long B, const C *tw, T scale) {
+    if (cfg == 0) {
+      if (sign > 0) cols<F32 ? 8 : 4, 256, +1>(ctx, d, A, B, tw, scale);
+      else cols<F32 ? 8 : 4, 256, -1>(ctx, d, A, B, tw, scale);
+    } else {
+      if (sign > 0) cols<F32 ? 16 : 8, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale);
+      else cols<F32 ? 16 : 8, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale);
+    }
+  }
+  static void rows_cfg(Context &ctx, int cfg, bool inv, C *d, const C *tw, T scale) {
+    if (cfg == 0) {
+      if (inv) rows<F32 ? 8 : 4, 256, true>(ctx, d, tw, scale);
+      else rows<F32 ? 8 : 4, 256, false>(ctx, d, tw, scale);
+    } else {
+      if (inv) rows<F32 ? 16 : 8, 256, true>(ctx, d, tw, scale);
+      else rows<F32 ? 16 : 8, 256, false>(ctx, d, tw, scale);
+    }
+  }
+  static void c2r(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg) {
+    cols_cfg(ctx, ccfg, +1, c, 1, (long long)N * S, tw, (T)1);
+    cols_cfg(ctx, ccfg, +1, c, N, S, tw, (T)1);
+    rows_cfg(ctx, rcfg, true, c, tw, scale);
+  }
+  static void r2c(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg) {
+    rows_cfg(ctx, rcfg, false, c, tw, (T)1);
+    cols_cfg(ctx, ccfg, -1, c, N, S, tw, (T)1);
+    cols_cfg(ctx, ccfg, -1, c, 1, (long long)N * S, tw, scale);
+  }
+  // time every candidate on a scratch array of the transform's size
+  static void tune(Context &ctx, const C *tw, int &best_cols, int &best_rows) {
+    const size_t bytes = (size_t)N * N * S * sizeof(C);
+    auto scratch = ctx.pool.take(bytes);
+    C *d = scratch->template as<C>();
+    GIC_CUDA(cudaMemsetAsync(d, 0, bytes, ctx.stream));
+    cudaEvent_t e0, e1;
+    GIC_CUDA(cudaEventCreate(&e0));
+    GIC_CUDA(cudaEventCreate(&e1));
+    auto time_it = [&](auto &&fn) {
+      fn();  // warm-up
+      GIC_CUDA(cudaEventRecord(e0, ctx.stream));
+      for (int r = 0; r < 3; ++r) fn();
+      GIC_CUDA(cudaEventRecord(e1, ctx.stream));
+      GIC_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      GIC_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      return ms;
+    };
+    float bc = 1e30f, br = 1e30f;
+    for (int c = 0; c < kFixedCandidates; ++c) {
+      float t = time_it([&] { cols_cfg(ctx, c, +1, d, 1, (long long)N * S, tw, (T)1); });
+      if (t < bc) { bc = t; best_cols = c; }
+    }
+    for (int r = 0; r < kFixedCandidates; ++r) {
+      float t = time_it([&] { rows_cfg(ctx, r, true, d, tw, (T)1); });
+      if (t < br) { br = t; best_rows = r; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx.pool.give(std::move(scratch));
+  }
+};
+
+template <typename T, int N>
+void fixed_transform(Context &ctx, typename Cx<T>::type *c, const typename Cx<T>::type *tw, double scale, bool inverse) {
+  FftTables &F = ctx.fft;
+  int cc = -1, rc = -1;
+  for (auto &t : F.tuned)
+    if (t.n == N && t.dbl == (sizeof(T) == 8)) {
+      cc = t.cols;
+      rc = t.rows;
+    }
+  if (cc < 0) {
+    cc = 0;
+    rc = 0;
+    if (N >= 128) FixedFft<T, N>::tune(ctx, tw, cc, rc);
+    F.tuned.push_back({N, sizeof(T) == 8, cc, rc});
+  }
+  if (F.force_cols >= 0) cc = F.force_cols;
+  if (F.force_rows >= 0) rc = F.force_rows;
+  if (inverse) FixedFft<T, N>::c2r(ctx, c, tw, (T)scale, cc, rc);
+  else FixedFft<T, N>::r2c(ctx, c, tw, (T)scale, cc, rc);
+}
+
+// power-of-two sizes 32..1024 use the fixed-length passes
+template <typename T>
+bool fixed_dispatch(Context &ctx, typename Cx<T>::type *c, int n, const typename Cx<T>::type *tw, double scale,
+                    bool inverse) {
+  switch (n) {
+    case 32: fixed_transform<T, 32>(ctx, c, tw, scale, inverse); return true;
+    case 64: fixed_transform<T, 64>(ctx, c, tw, scale, inverse); return true;
+    case 128: fixed_transform<T, 128>(ctx, c, tw, scale, inverse); return true;
+    case 256: fixed_transform<T, 256>(ctx, c, tw, scale, inverse); return true;
+    case 512: fixed_transform<T, 512>(ctx, c, tw, scale, inverse); return true;
+    case 1024: fixed_transform<T, 1024>(ctx, c, tw, scale, inverse); return true;
+    default: return false;
+  }
 }
 
 template <typename T>
@@ -460,6 +785,7 @@ void fft_c2r_3d(Context &ctx, T *data, int n, double scale) {
   long long mirror_threads = 2ll * n * n;
   k_mirror<T><<<(unsigned)((mirror_threads + 255) / 256), 256, 0, ctx.stream>>>(c, n);
   launched();
+  if (ctx.fft.force_cols != -2 && fixed_dispatch<T>(ctx, c, n, tw, scale, true)) return;
   strided_pass<T>(ctx, c, 1, n, (long long)n * S, +1, (T)1, tw);
   strided_pass<T>(ctx, c, n, n, S, +1, (T)1, tw);
   int rpc = rows_per_cta<T>(n);
@@ -479,6 +805,7 @@ void fft_r2c_3d(Context &ctx, T *data, int n, double scale) {
   const C *tw = (const C *)ctx.fft.get(n, sizeof(T) == 8, ctx.stream);
   C *c = reinterpret_cast<C *>(data);
   long long S = n / 2 + 1;
+  if (ctx.fft.force_cols != -2 && fixed_dispatch<T>(ctx, c, n, tw, scale, false)) return;
   int rpc = rows_per_cta<T>(n);
   Radix plan = make_plan(n / 2);
   size_t smem = 2ull * rpc * S * sizeof(C);

@@ -125,6 +125,15 @@ struct FftTables {
   };
   std::vector<std::unique_ptr<Entry>> entries;
   const void *get(int n, bool dbl, cudaStream_t s);
+  // tile widths of the fixed-length passes chosen by timing the candidates on
+  // first use, per size and precision (the choice does not change any result)
+  struct Tuned {
+    int n;
+    bool dbl;
+    int cols, rows;
+  };
+  std::vector<Tuned> tuned;
+  int force_cols = -1, force_rows = -1;  // >= 0: use this candidate (tests)
 };
 
 struct RngScratch {
