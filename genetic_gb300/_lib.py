@@ -35,6 +35,9 @@ GIC_FIELD_DELTA = 1
 GIC_FIELD_PSI_X = 2
 GIC_FIELD_PSI_Y = 3
 GIC_FIELD_PSI_Z = 4
+GIC_FIELD_PSI2_X = 5
+GIC_FIELD_PSI2_Y = 6
+GIC_FIELD_PSI2_Z = 7
 
 
 class GicDeviceOpts(ctypes.Structure):

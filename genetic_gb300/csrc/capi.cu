@@ -103,10 +103,11 @@ void fetch_typed(Context &c, Level &L, int what, double *host) {
     }
   } else {
     if (!L.have_fields) fail(GIC_ERR_NOT_READY, "fields have not been computed");
-    int f = what - GIC_FIELD_DELTA;
+    if (what >= GIC_FIELD_PSI2_X && !L.have_lpt2) fail(GIC_ERR_NOT_READY, "second-order fields have not been computed");
+    DevBuf &src = what >= GIC_FIELD_PSI2_X ? L.field2[what - GIC_FIELD_PSI2_X] : L.field[what - GIC_FIELD_DELTA];
     size_t m = L.ncells();
     c.reduce.ensure(m * sizeof(double));
-    k_unpad_real<T><<<(unsigned)((m + 255) / 256), 256, 0, s>>>(L.field[f].as<T>(), c.reduce.as<double>(), L.n);
+    k_unpad_real<T><<<(unsigned)((m + 255) / 256), 256, 0, s>>>(src.as<T>(), c.reduce.as<double>(), L.n);
     launched();
     GIC_CUDA(cudaMemcpyAsync(host, c.reduce.ptr, m * sizeof(double), cudaMemcpyDeviceToHost, s));
   }
@@ -129,6 +130,7 @@ void set_noise_typed(Context &c, Level &L, const double *host) {
   GIC_CUDA(cudaStreamSynchronize(s));
   L.have_noise = true;
   L.have_fields = false;
+  L.have_lpt2 = false;
 }
 
 template <typename T>
@@ -299,7 +301,7 @@ int gic_draw_noise(gic_ctx *ctx, unsigned long seed, int mode) {
   API_BEGIN(ctx)
   if (C.levels.empty()) gic::fail(GIC_ERR_NOT_READY, "no grid levels");
   gic::draw_noise_all(C, seed, mode);
-  for (auto &L : C.levels) L->have_fields = false;
+  for (auto &L : C.levels) L->have_fields = L->have_lpt2 = false;
   API_END
 }
 
@@ -321,12 +323,13 @@ int gic_set_noise(gic_ctx *ctx, int level, const double *host_src) {
 
 int gic_zeldovich(gic_ctx *ctx, int order) {
   API_BEGIN(ctx)
-  if (order != 1) gic::fail(GIC_ERR_INVALID_ARG, "only order 1 (Zel'dovich) is available");
+  if (order != 1 && order != 2) gic::fail(GIC_ERR_INVALID_ARG, "order must be 1 (Zel'dovich) or 2 (2LPT)");
   if (C.levels.empty()) gic::fail(GIC_ERR_NOT_READY, "no grid levels");
   int nl = (int)C.levels.size();
   for (int l = 0; l < nl; ++l) gic::za_fields(C, l);
   for (int l = 1; l < nl; ++l) gic::zoom_combine(C, l);
-  for (int l = 0; l < nl; ++l) gic::make_particles(C, *C.levels[l]);
+  if (order == 2) gic::lpt2_fields(C);
+  for (int l = 0; l < nl; ++l) gic::make_particles(C, *C.levels[l], order);
   GIC_CUDA(cudaStreamSynchronize(C.stream));
   API_END
 }
@@ -334,7 +337,7 @@ int gic_zeldovich(gic_ctx *ctx, int order) {
 int gic_fetch_level(gic_ctx *ctx, int level, int what, double *host_dst) {
   API_BEGIN(ctx)
   if (!host_dst) gic::fail(GIC_ERR_INVALID_ARG, "null buffer");
-  if (what < GIC_FIELD_NOISE || what > GIC_FIELD_PSI_Z) gic::fail(GIC_ERR_INVALID_ARG, "unknown field");
+  if (what < GIC_FIELD_NOISE || what > GIC_FIELD_PSI2_Z) gic::fail(GIC_ERR_INVALID_ARG, "unknown field");
   gic::Level &L = gic::level_at(C, level);
   if (C.dbl()) gic::fetch_typed<double>(C, L, what, host_dst);
   else gic::fetch_typed<float>(C, L, what, host_dst);

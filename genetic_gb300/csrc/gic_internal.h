@@ -98,9 +98,11 @@ struct Level {
   DevBuf tab_main;       // sqrt(P_grid), times the high-pass filter on zoom levels
   DevBuf tab_lp_src;     // sqrt(P_grid) * low-pass (source side of the next zoom)
   DevBuf tab_lp;         // low-pass filter alone
+  DevBuf field2[3];      // second-order displacements psi2_x, psi2_y, psi2_z (real)
   DevBuf pos, vel;       // particles: pos double[3M], vel (precision)[3M]
   bool have_noise = false;
   bool have_fields = false;
+  bool have_lpt2 = false;
 };
 
 struct Cosmo {
@@ -193,6 +195,7 @@ void build_sqrtp_table(Context &ctx, Level &L);
 void build_sqrtp_table_species(Context &ctx, Level &L, int dm);
 void za_fields(Context &ctx, int level);
 void zoom_combine(Context &ctx, int level);
+void lpt2_fields(Context &ctx);
 
 // zoom.cu
 template <typename T, int NF>
@@ -206,6 +209,6 @@ void apply_modifications(Context &ctx, double *chi2_before, double *chi2_after);
 
 // particles.cu
 double velocity_to_offset_ratio(const Cosmo &c);
-void make_particles(Context &ctx, Level &L);
+void make_particles(Context &ctx, Level &L, int order = 1);
 
 }  // namespace gic

@@ -156,6 +156,52 @@ __global__ void k_za_fields(const typename V2<T>::type *noise, const double *tab
   pz[id] = rz;
 }
 
+// Second derivatives of the potential (nabla^2 phi = delta): phi_ab = k_a k_b delta / k^2
+// for ab = xx, yy, zz, xy, xz, yz, delta = src * tab[q]; zero at k = 0, and the
+// mixed ones where either component is the Nyquist mode.
+template <typename T>
+__global__ void k_hessian_fields(const typename V2<T>::type *src, const double *tab, int n, T kmin,
+                                 typename V2<T>::type *const *out) {
+  using C = typename V2<T>::type;
+  const int H = n / 2, S = H + 1;
+  unsigned row = blockIdx.x * 8 + threadIdx.y;
+  int iz = blockIdx.y * 32 + threadIdx.x;
+  if (row >= (unsigned)n * (unsigned)n || iz >= S) return;
+  int ix = (int)(row / (unsigned)n), iy = (int)(row % (unsigned)n);
+  size_t id = (size_t)row * S + iz;
+  int kc[3] = {ix > H ? ix - n : ix, iy > H ? iy - n : iy, iz};
+  long long q = (long long)kc[0] * kc[0] + (long long)kc[1] * kc[1] + (long long)kc[2] * kc[2];
+  T f[3] = {(T)kc[0] * kmin, (T)kc[1] * kmin, (T)kc[2] * kmin};
+  T kk = f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
+  C w = src[id];
+  T s = q == 0 ? (T)0 : (T)tab[q] / kk;
+  const int pa[6] = {0, 1, 2, 0, 0, 1}, pb[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    int a = pa[c], b = pb[c];
+    T m = s * f[a] * f[b];
+    if (a != b && (kc[a] == H || kc[b] == H)) m = 0;
+    C o;
+    o.x = w.x * m;
+    o.y = w.y * m;
+    out[c][id] = o;
+  }
+}
+
+// S = xx yy + xx zz + yy zz - xy^2 - xz^2 - yz^2 over padded real rows, into xx
+template <typename T>
+__global__ void k_lpt2_source(T *xx, const T *yy, const T *zz, const T *xy, const T *xz, const T *yz, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T a = xx[i], b = yy[i], c = zz[i], d = xy[i], e = xz[i], f = yz[i];
+  xx[i] = a * b + a * c + b * c - d * d - e * e - f * f;
+}
+
+__global__ void k_table_scale(double *t, long long nq, double s) {
+  long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < nq) t[q] *= s;
+}
+
 // Per-|k|^2 tables: out[q] = base[q] * f(sqrt(q) kmin), f = 1, the low-pass Fermi
 // filter 1/(1 + exp((k - kcut)/T)) with T = 0.1 kcut, or the complementary
 // high-pass sqrt(1 - LP^2) (genetIC/src/simulation/filters/filter.hpp:208-275,
@@ -392,6 +438,136 @@ static void zoom_combine_typed(Context &ctx, int li) {
   }
   for (int f = 0; f < 4; ++f) fft_c2r_3d<T>(ctx, src[f], Cl.n, scale);
   interp_add4<T>(ctx, Cl, src, F);
+}
+
+// ---- second-order LPT ------------------------------------------------------------
+// No counterpart in genetIC.  psi2 = (3/7) i k S_k / k^2 with nabla^2 phi = delta and
+// S = sum_{a<b} (phi_aa phi_bb - phi_ab^2) (Scoccimarro 1998; Crocce, Pueblas &
+// Scoccimarro 2006, Einstein-de Sitter growth D2 = -3/7 D1^2).  On a zoom level both
+// the Hessian and psi2 are combined like the first-order fields: the level's own
+// part times the high-pass filter plus the coarser level's combined field
+// low-passed and interpolated in.
+
+// out[q] = scalar * (1, HP or LP filter of cut kcut)
+static void filter_table(Context &ctx, DevBuf &out, const Level &L, double kcut, int kind, double scalar) {
+  long long half = L.n / 2, nq = 3 * half * half + 1;
+  out.ensure(nq * sizeof(double));
+  unsigned blocks = (unsigned)((nq + 255) / 256);
+  k_filter_table<<<blocks, 256, 0, ctx.stream>>>(out.as<double>(), nullptr, nq, L.kmin(), kcut, kind);
+  launched();
+  if (scalar != 1.0) {
+    k_table_scale<<<blocks, 256, 0, ctx.stream>>>(out.as<double>(), nq, scalar);
+    launched();
+  }
+}
+
+// real fields of level li-1 (combined), low-passed, added into level li's real fields
+template <typename T>
+static void add_lowpassed_coarse(Context &ctx, int li, T *const *coarse, T *const *fine, int nf) {
+  using C = typename V2<T>::type;
+  Level &Cl = *ctx.levels[li - 1];
+  Level &F = *ctx.levels[li];
+  build_lowpass_tables(ctx, li - 1);
+  const size_t bytes = Cl.ncomplex() * sizeof(C);
+  const double scale = 1.0 / std::pow((double)Cl.n, 1.5);
+  auto tmp = ctx.pool.take(bytes);
+  T *t = tmp->as<T>();
+  for (int f = 0; f < nf; ++f) {
+    GIC_CUDA(cudaMemcpyAsync(t, coarse[f], bytes, cudaMemcpyDeviceToDevice, ctx.stream));
+    fft_r2c_3d<T>(ctx, t, Cl.n, scale);
+    k_scale_table<T><<<hs_grid(Cl.n), hs_block(), 0, ctx.stream>>>(reinterpret_cast<C *>(t), Cl.n,
+                                                                    Cl.tab_lp.as<double>());
+    launched();
+    fft_c2r_3d<T>(ctx, t, Cl.n, scale);
+    const T *src[1] = {t};
+    T *dst[1] = {fine[f]};
+    interp_add<T, 1>(ctx, Cl, src, F, dst);
+  }
+  ctx.pool.give(std::move(tmp));
+}
+
+template <typename T>
+static void lpt2_typed(Context &ctx) {
+  using C = typename V2<T>::type;
+  const int nl = (int)ctx.levels.size();
+  std::vector<std::vector<std::unique_ptr<DevBuf>>> hess(nl);
+  std::vector<std::unique_ptr<DevBuf>> source(nl);
+  DevBuf ptrs, tab;
+  // combined Hessian and the source S of every level
+  for (int li = 0; li < nl; ++li) {
+    Level &L = *ctx.levels[li];
+    const size_t bytes = L.ncomplex() * sizeof(C);
+    const double scale = 1.0 / std::pow((double)L.n, 1.5);
+    build_level_tables(ctx, li);
+    C *hp[6];
+    for (int c = 0; c < 6; ++c) {
+      hess[li].push_back(ctx.pool.take(bytes));
+      hp[c] = hess[li][c]->as<C>();
+    }
+    ptrs.ensure(sizeof(hp));
+    GIC_CUDA(cudaMemcpyAsync(ptrs.ptr, hp, sizeof(hp), cudaMemcpyHostToDevice, ctx.stream));
+    k_hessian_fields<T><<<hs_grid(L.n), hs_block(), 0, ctx.stream>>>(L.noise.as<C>(), L.tab_main.as<double>(), L.n,
+                                                                     (T)L.kmin(), ptrs.as<C *>());
+    launched();
+    GIC_CUDA(cudaStreamSynchronize(ctx.stream));  // ptrs is reused
+    T *real[6];
+    for (int c = 0; c < 6; ++c) {
+      real[c] = hess[li][c]->as<T>();
+      fft_c2r_3d<T>(ctx, real[c], L.n, scale);
+    }
+    if (li > 0) {
+      T *coarse[6];
+      for (int c = 0; c < 6; ++c) coarse[c] = hess[li - 1][c]->as<T>();
+      add_lowpassed_coarse<T>(ctx, li, coarse, real, 6);
+      for (auto &b : hess[li - 1]) ctx.pool.give(std::move(b));
+      hess[li - 1].clear();
+    }
+    source[li] = ctx.pool.take(bytes);
+    GIC_CUDA(cudaMemcpyAsync(source[li]->ptr, real[0], bytes, cudaMemcpyDeviceToDevice, ctx.stream));
+    const size_t nreal = 2 * L.ncomplex();
+    k_lpt2_source<T><<<(unsigned)((nreal + 255) / 256), 256, 0, ctx.stream>>>(
+        source[li]->as<T>(), real[1], real[2], real[3], real[4], real[5], nreal);
+    launched();
+  }
+  for (auto &b : hess[nl - 1]) ctx.pool.give(std::move(b));
+  // psi2 of every level from its S, combined across levels
+  for (int li = 0; li < nl; ++li) {
+    Level &L = *ctx.levels[li];
+    const size_t bytes = L.ncomplex() * sizeof(C);
+    const double scale = 1.0 / std::pow((double)L.n, 1.5);
+    for (int f = 0; f < 3; ++f) L.field2[f].ensure(bytes);
+    T *sk = source[li]->as<T>();
+    fft_r2c_3d<T>(ctx, sk, L.n, scale);
+    double kcut = li > 0 ? level_kcut(*ctx.levels[li - 1]) : 1.0;
+    filter_table(ctx, tab, L, kcut, li > 0 ? 2 : 0, 3.0 / 7.0);
+    k_za_fields<T><<<hs_grid(L.n), hs_block(), 0, ctx.stream>>>(reinterpret_cast<C *>(sk), tab.as<double>(), L.n,
+                                                                (T)L.kmin(), reinterpret_cast<C *>(sk),
+                                                                L.field2[0].as<C>(), L.field2[1].as<C>(),
+                                                                L.field2[2].as<C>());
+    launched();
+    T *real[3];
+    for (int f = 0; f < 3; ++f) {
+      real[f] = L.field2[f].as<T>();
+      fft_c2r_3d<T>(ctx, real[f], L.n, scale);
+    }
+    if (li > 0) {
+      Level &Cl = *ctx.levels[li - 1];
+      T *coarse[3] = {Cl.field2[0].as<T>(), Cl.field2[1].as<T>(), Cl.field2[2].as<T>()};
+      add_lowpassed_coarse<T>(ctx, li, coarse, real, 3);
+    }
+    L.have_lpt2 = true;
+  }
+  GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+  for (auto &b : source) ctx.pool.give(std::move(b));
+}
+
+void lpt2_fields(Context &ctx) {
+  for (auto &L : ctx.levels)
+    if (!L->have_fields) fail(GIC_ERR_NOT_READY, "first-order fields have not been computed");
+  if (ctx.dbl())
+    lpt2_typed<double>(ctx);
+  else
+    lpt2_typed<float>(ctx);
 }
 
 void za_fields(Context &ctx, int li) {

@@ -1069,7 +1069,7 @@ static void apply_mods(Context &ctx, double *chi2_before, double *chi2_after) {
   }
   for (int l = 0; l < E.nl(); ++l) {
     E.copy_level(E.lev(l).noise, *W.b[l], l);
-    E.lev(l).have_fields = false;
+    E.lev(l).have_fields = E.lev(l).have_lpt2 = false;
   }
   GIC_CUDA(cudaStreamSynchronize(ctx.stream));
   if (chi2_after) *chi2_after = chi2_of_noise<T>(ctx);

@@ -1,4 +1,4 @@
-// Zel'dovich particles of one level: position = cell centroid + psi, wrapped
+// Zel'dovich (and 2LPT) particles of one level: position = cell centroid + psi, wrapped
 // into the periodic domain, velocity = psi * 100 sqrt(Om/a^3 + OL) sqrt(a)
 // (f = 1), as ZeldovichParticleEvaluator evaluates them one index at a time
 // (genetIC/src/simulation/particles/zeldovich.hpp:87-124,
@@ -64,10 +64,14 @@ __device__ __forceinline__ double wrap_fast(double x, double period, long long p
   return wrap_coord(x, period);
 }
 
-template <typename T>
+// LPT2: second-order displacements q2 are added, pos = q + psi + psi2 and
+// vel = ratio (psi + 2 psi2) (f2 = 2 with genetIC's f = 1)
+template <typename T, bool LPT2>
 __global__ void __launch_bounds__(256) k_particles(const T *__restrict__ px, const T *__restrict__ py,
-                                                   const T *__restrict__ pz, int n, const double *__restrict__ cen,
-                                                   double period, T ratio, double *pos, T *vel) {
+                                                   const T *__restrict__ pz, const T *__restrict__ qx,
+                                                   const T *__restrict__ qy, const T *__restrict__ qz, int n,
+                                                   const double *__restrict__ cen, double period, T ratio,
+                                                   double *pos, T *vel) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   size_t m = (size_t)n * n * n;
   if (i >= m) return;
@@ -77,9 +81,19 @@ __global__ void __launch_bounds__(256) k_particles(const T *__restrict__ px, con
   int x = (int)(row / n);
   size_t src = row * (size_t)(2 * (n / 2 + 1)) + z;
   T sx = px[src], sy = py[src], sz = pz[src];
-  vel[3 * i + 0] = sx * ratio;
-  vel[3 * i + 1] = sy * ratio;
-  vel[3 * i + 2] = sz * ratio;
+  if (LPT2) {
+    T tx = qx[src], ty = qy[src], tz = qz[src];
+    vel[3 * i + 0] = (sx + 2 * tx) * ratio;
+    vel[3 * i + 1] = (sy + 2 * ty) * ratio;
+    vel[3 * i + 2] = (sz + 2 * tz) * ratio;
+    sx += tx;
+    sy += ty;
+    sz += tz;
+  } else {
+    vel[3 * i + 0] = sx * ratio;
+    vel[3 * i + 1] = sy * ratio;
+    vel[3 * i + 2] = sz * ratio;
+  }
   long long pb = __double_as_longlong(period);
   pos[3 * i + 0] = wrap_fast(to_double(sx) + __ldg(cen + x), period, pb);
   pos[3 * i + 1] = wrap_fast(to_double(sy) + __ldg(cen + n + y), period, pb);
@@ -94,7 +108,7 @@ double velocity_to_offset_ratio(const Cosmo &c) {
 }
 
 template <typename T>
-static void particles_typed(Context &ctx, Level &L) {
+static void particles_typed(Context &ctx, Level &L, int order) {
   size_t m = L.ncells();
   L.pos.ensure(3 * m * sizeof(double));
   L.vel.ensure(3 * m * sizeof(T));
@@ -102,18 +116,25 @@ static void particles_typed(Context &ctx, Level &L) {
   ctx.geom.ensure(3 * (size_t)L.n * sizeof(double));
   double *cen = ctx.geom.as<double>();
   k_centroids<<<(3 * L.n + 127) / 128, 128, 0, ctx.stream>>>(L.n, L.dx, L.x0[0], L.x0[1], L.x0[2], cen);
-  k_particles<T><<<(unsigned)((m + 255) / 256), 256, 0, ctx.stream>>>(
-      L.field[1].as<T>(), L.field[2].as<T>(), L.field[3].as<T>(), L.n, cen, L.periodic, ratio, L.pos.as<double>(),
-      L.vel.as<T>());
+  const unsigned grid = (unsigned)((m + 255) / 256);
+  if (order == 2)
+    k_particles<T, true><<<grid, 256, 0, ctx.stream>>>(L.field[1].as<T>(), L.field[2].as<T>(), L.field[3].as<T>(),
+                                                       L.field2[0].as<T>(), L.field2[1].as<T>(), L.field2[2].as<T>(),
+                                                       L.n, cen, L.periodic, ratio, L.pos.as<double>(), L.vel.as<T>());
+  else
+    k_particles<T, false><<<grid, 256, 0, ctx.stream>>>(L.field[1].as<T>(), L.field[2].as<T>(), L.field[3].as<T>(),
+                                                        nullptr, nullptr, nullptr, L.n, cen, L.periodic, ratio,
+                                                        L.pos.as<double>(), L.vel.as<T>());
   launched(2);
 }
 
-void make_particles(Context &ctx, Level &L) {
+void make_particles(Context &ctx, Level &L, int order) {
   if (!L.have_fields) fail(GIC_ERR_NOT_READY, "displacement fields not computed");
+  if (order == 2 && !L.have_lpt2) fail(GIC_ERR_NOT_READY, "second-order displacements not computed");
   if (ctx.dbl())
-    particles_typed<double>(ctx, L);
+    particles_typed<double>(ctx, L, order);
   else
-    particles_typed<float>(ctx, L);
+    particles_typed<float>(ctx, L, order);
 }
 
 }  // namespace gic

@@ -256,14 +256,15 @@ class ICGenerator:
         self._call('gic_draw_noise', self.seed, self.seed_mode)
         self._drawn = True
 
-    def done(self, apply_modifications=True):
+    def done(self, apply_modifications=True, order=1):
         """Draw the noise if needed, apply the queued modifications, then P(k), the
-        Zel'dovich fields and particles (ic.hpp:1633-1648)."""
+        Zel'dovich fields and particles (ic.hpp:1633-1648); order=2 adds the
+        second-order (2LPT) displacements, an extension genetIC does not have."""
         self.draw()
         self._modified = False
         if apply_modifications and self._has_modifications():
             self.apply_modifications()
-        self._call('gic_zeldovich', 1)
+        self._call('gic_zeldovich', int(order))
         self._done = True
 
     def _has_modifications(self):
@@ -284,7 +285,8 @@ class ICGenerator:
 
     def field(self, level=0, name='delta'):
         what = {'delta': _lib.GIC_FIELD_DELTA, 'psi_x': _lib.GIC_FIELD_PSI_X, 'psi_y': _lib.GIC_FIELD_PSI_Y,
-                'psi_z': _lib.GIC_FIELD_PSI_Z}[name]
+                'psi_z': _lib.GIC_FIELD_PSI_Z, 'psi2_x': _lib.GIC_FIELD_PSI2_X, 'psi2_y': _lib.GIC_FIELD_PSI2_Y,
+                'psi2_z': _lib.GIC_FIELD_PSI2_Z}[name]
         n = self.levels[level][1]
         out = np.empty((n, n, n), dtype=np.float64)
         self._call('gic_fetch_level', level, what, _ptr(out))

@@ -50,6 +50,10 @@ extern "C" {
 #define GIC_FIELD_PSI_X 2
 #define GIC_FIELD_PSI_Y 3
 #define GIC_FIELD_PSI_Z 4
+/* second-order (2LPT) displacements, after gic_zeldovich(ctx, 2); no genetIC counterpart */
+#define GIC_FIELD_PSI2_X 5
+#define GIC_FIELD_PSI2_Y 6
+#define GIC_FIELD_PSI2_Z 7
 
 #if defined(__GNUC__)
 #define GIC_API __attribute__((visibility("default")))
@@ -113,7 +117,10 @@ GIC_API int gic_set_noise(gic_ctx *ctx, int level, const double *host_src);
  * (genetIC/src/simulation/field/multilevelfield.hpp:410-454) +
  * ZeldovichParticleGenerator::calculateOffsetFields (genetIC/src/simulation/particles/zeldovich.hpp:152-253)
  * + initialiseParticleGeneratorBasedOnTemplate (multilevelgenerator.hpp:78-128).
- * order: 1 = Zel'dovich (the reference's only option). */
+ * order: 1 = Zel'dovich (the reference's only option); 2 = second-order LPT, an
+ * extension without a genetIC counterpart: psi2 = (3/7) i k S_k / k^2 with
+ * S = sum_{a<b} (phi_aa phi_bb - phi_ab^2), nabla^2 phi = delta, combined across
+ * levels like psi; positions q + psi + psi2, velocities ratio (psi + 2 psi2). */
 GIC_API int gic_zeldovich(gic_ctx *ctx, int order);
 
 /* Copy a level's field to the host.  Real-space fields (after gic_zeldovich)

@@ -392,6 +392,80 @@ def zoom_realisation(noises, levels, power):
     return out
 
 
+# --- second-order LPT (no counterpart in genetIC: Scoccimarro 1998, Crocce, Pueblas &
+# Scoccimarro 2006, with Einstein-de Sitter growth: D2 = -3/7 D1^2, f2 = 2) -------------
+
+LPT2_FACTOR = 3.0 / 7.0
+_PAIRS = ((0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2))
+
+
+def potential_hessian_spectra(delta_k, box):
+    """phi_ij = k_i k_j delta_k / k^2 for ij = xx, yy, zz, xy, xz, yz (nabla^2 phi = delta);
+    zero at k = 0, and the mixed ones where either component is the Nyquist mode
+    (the first-derivative rule of zeldovich.hpp:173-178 applied twice)."""
+    n = delta_k.shape[0]
+    ki, kz, kmin = kgrid(n, box)
+    comps = [((ki * kmin)[:, None, None], ki[:, None, None]), ((ki * kmin)[None, :, None], ki[None, :, None]),
+             ((kz * kmin)[None, None, :], kz[None, None, :])]
+    kk = comps[0][0] ** 2 + comps[1][0] ** 2 + comps[2][0] ** 2
+    with np.errstate(divide='ignore', invalid='ignore'):
+        base = delta_k / kk
+    base[0, 0, 0] = 0
+    out = []
+    for a, b in _PAIRS:
+        p = base * comps[a][0] * comps[b][0]
+        if a != b:
+            p = np.where((comps[a][1] == n // 2) | (comps[b][1] == n // 2), 0.0, p)
+        p[0, 0, 0] = 0
+        out.append(p)
+    return out
+
+
+def lpt2_source(phi):
+    """S = sum_{i<j} (phi_ii phi_jj - phi_ij^2), so that nabla^2 phi2 = S."""
+    xx, yy, zz, xy, xz, yz = phi
+    return xx * yy + xx * zz + yy * zz - xy * xy - xz * xz - yz * yz
+
+
+def _combine_levels(levels, own_specs, kcuts_hp):
+    """Real fields per level: own spectra (x HP on zoom levels) to real space, plus the
+    coarser level's combined fields low-passed and interpolated in (as zoom_realisation)."""
+    periodic = levels[0][0]
+    out = []
+    for li, (box, n, off) in enumerate(levels):
+        specs = own_specs[li]
+        if li > 0:
+            cbox, cn, coff = levels[li - 1]
+            kcut = 0.3 * (cn * 2. * np.pi / cbox)
+            hp = np.sqrt(1. - fermi_lowpass(kmag(n, box), kcut) ** 2)
+            specs = [s * hp for s in specs]
+        fields = [fft_c2r(s) for s in specs]
+        if li > 0:
+            lp = fermi_lowpass(kmag(cn, cbox), kcut)
+            for f, c in zip(fields, out[li - 1]):
+                f += interpolate_to(fft_c2r(fft_r2c(c) * lp), cbox, coff, periodic, box, n, off)
+        out.append(fields)
+    return out
+
+
+def lpt2_realisation(noises, levels, power):
+    """Second-order displacements (x, y, z) of every level: psi2 = (3/7) i k S_k / k^2
+    from the combined potential Hessian of each level, combined across levels like
+    the first-order fields."""
+    hess = _combine_levels(levels, [potential_hessian_spectra(w * sqrt_power_grid(power, n, box), box)
+                                    for (box, n, off), w in zip(levels, noises)], None)
+    sources = [fft_r2c(lpt2_source(h)) * LPT2_FACTOR for h in hess]
+    return _combine_levels(levels, [displacement_spectra(sk, box) for (box, n, off), sk in zip(levels, sources)],
+                           None)
+
+
+def particles_lpt2(psi1, psi2, box, offset, periodic, ratio):
+    """Positions q + psi1 + psi2 (wrapped) and velocities ratio (psi1 + 2 psi2)."""
+    pos, _ = particles([a + b for a, b in zip(psi1, psi2)], box, offset, periodic, ratio)
+    vel = np.stack([(a + 2. * b) * ratio for a, b in zip(psi1, psi2)], axis=-1).reshape(-1, 3)
+    return pos, vel
+
+
 # --- modifications (modifications/*.hpp, multilevelfield.hpp, multilevelgrid.hpp) --------
 
 class Levels:

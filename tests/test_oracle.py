@@ -272,3 +272,24 @@ def test_variance_oracle_matches_goldens(bbks, case):
     for l in range(len(VAR_CASES[case]['levels'])):
         ref = g['delta%d' % l]
         assert np.abs(out[l][0] - ref).max() <= 1e-11 * np.abs(ref).max(), l
+
+
+# --- second-order LPT (no reference counterpart: checked against the analytic solution) ---
+
+def test_lpt2_oracle_two_plane_waves():
+    """delta = A cos(k1 x) + B cos(k2 y): S = A B cos(k1 x) cos(k2 y) and
+    psi2 = (3/7) grad S / (k1^2 + k2^2); a single plane wave has psi2 = 0."""
+    n, box = 32, 50.0
+    k1, k2, A, B = 2 * np.pi * 3 / box, 2 * np.pi * 2 / box, 0.05, 0.03
+    g = np.arange(n) * box / n
+    X, Y, _ = np.meshgrid(g, g, g, indexing='ij')
+    for a, b in ((A, B), (A, 0.0)):
+        dk = fo.fft_r2c(a * np.cos(k1 * X) + b * np.cos(k2 * Y))
+        phi = [fo.fft_c2r(s) for s in fo.potential_hessian_spectra(dk, box)]
+        assert np.abs(fo.lpt2_source(phi) - a * b * np.cos(k1 * X) * np.cos(k2 * Y)).max() < 1e-15
+        psi2 = [fo.fft_c2r(s) for s in fo.displacement_spectra(fo.fft_r2c(fo.lpt2_source(phi)) * fo.LPT2_FACTOR, box)]
+        K2 = k1 * k1 + k2 * k2
+        want = [(3 / 7) * a * b * -k1 * np.sin(k1 * X) * np.cos(k2 * Y) / K2,
+                (3 / 7) * a * b * -k2 * np.cos(k1 * X) * np.sin(k2 * Y) / K2, 0 * X]
+        for p, w in zip(psi2, want):
+            assert np.abs(p - w).max() < 1e-15
