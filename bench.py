@@ -1,9 +1,10 @@
 """Throughput of the GB300 field-realisation path (Mparticles/s).
 
-One step = one complete Zel'dovich realisation of the workload: white noise
-drawn from the seed, multiplied by sqrt(P(k)), displacement spectra, inverse
-FFTs, zoom combination where the workload has zoom levels, and particle
-positions/velocities -- with the transfer table already on the device
+One step = one complete Zel'dovich (or 2LPT) realisation of the workload: white
+noise drawn from the seed, the workload's modifications applied, multiplied by
+sqrt(P(k)), displacement spectra, inverse FFTs, zoom combination where the
+workload has zoom levels, and particle positions/velocities -- with the transfer
+table already on the device
 (`value`), or end to end through the C ABI from host memory (`e2e`: the
 transfer table uploaded and the sigma8 normalisation recomputed every step,
 particles copied back to pinned host memory every step).
@@ -38,6 +39,11 @@ WORKLOADS = {
                          precision='fp64', replaced=128 ** 3, mods=MODS4),
     'zoom512_nomod': dict(levels=[('base', 100.0, 512), ('zoom', 192, 192, 192, 4, 512)], seed_cmd='random_seed',
                           precision='mixed', replaced=128 ** 3),
+    # the same with second-order (2LPT) displacements and velocities
+    'zoom512_lpt2': dict(levels=[('base', 100.0, 512), ('zoom', 192, 192, 192, 4, 512)], seed_cmd='random_seed',
+                         precision='mixed', replaced=128 ** 3, mods=MODS4, order=2),
+    'zoom512_lpt2_fp64': dict(levels=[('base', 100.0, 512), ('zoom', 192, 192, 192, 4, 512)],
+                              seed_cmd='random_seed', precision='fp64', replaced=128 ** 3, mods=MODS4, order=2),
     'zoom256': dict(levels=[('base', 100.0, 256), ('zoom', 96, 96, 96, 4, 256)], seed_cmd='random_seed',
                     precision='mixed', replaced=64 ** 3),
     # 512^3 single level, 100 Mpc/h box (the single-level configuration at 512^3)
@@ -242,6 +248,39 @@ def run_reference(args, wl, rank, world):
     print(json.dumps(line))
 
 
+def accuracy(wl_name, wl, table, device):
+    """Per-field max and RMS relative error (|a - b| / max|b|) of the workload's mixed
+    form against its plain FP64 form, both on the GPU, same seed and modifications."""
+    import genetic_gb300 as g  # noqa: F401
+    mixed = dict(wl, precision='mixed')
+    fp64 = dict(wl, precision='fp64')
+    order = wl.get('order', 1)
+    gens = []
+    for w in (mixed, fp64):
+        gen = make_gen(w, table, device)
+        gen._call('gic_draw_noise', SEED, 2)
+        if w.get('mods'):
+            c = ctypes.c_double(), ctypes.c_double()
+            gen._call('gic_apply_modifications', ctypes.byref(c[0]), ctypes.byref(c[1]))
+        gen._call('gic_zeldovich', order)
+        gens.append(gen)
+    names = ['delta', 'psi_x', 'psi_y', 'psi_z'] + (['psi2_x', 'psi2_y', 'psi2_z'] if order == 2 else [])
+    out = {}
+    for lev in range(len(wl['levels'])):
+        for name in names:
+            a = gens[0].field(lev, name)
+            b = gens[1].field(lev, name)
+            scale = float(np.abs(b).max())
+            d = np.abs(a - b)
+            out['L%d.%s' % (lev, name)] = {'max': float(d.max() / scale), 'rms': float(np.sqrt(np.mean(d * d)) / scale)}
+            del a, b, d
+    for gen in gens:
+        gen.close()
+    worst_disp = max(v['max'] for k, v in out.items() if '.psi' in k)
+    print(json.dumps({'accuracy': wl_name, 'reference': 'plain FP64 GPU path', 'fields': out,
+                      'max_rel_displacement_err': worst_disp}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -250,6 +289,8 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--workload', default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--accuracy', action='store_true',
+                    help='print the per-field error of the mixed form against FP64 instead of timing')
     args = ap.parse_args()
     rank, world, local = dist_env()
     if world > 1:
@@ -265,6 +306,9 @@ def main():
     from genetic_gb300.transfer import bbks_table
     torch.cuda.set_device(local)
     table = np.ascontiguousarray(bbks_table())
+    if args.accuracy:
+        accuracy(args.workload, wl, table, local)
+        return
     gen = make_gen(wl, table, local)
     sptr = ctypes.c_void_p()
     _lib.check(gen._ctx, gen._lib.gic_get_stream(gen._ctx, ctypes.byref(sptr)))
@@ -280,7 +324,7 @@ def main():
         gen._call('gic_draw_noise', SEED + i, mode)
         if has_mods:
             gen._call('gic_apply_modifications', ctypes.byref(chi2[0]), ctypes.byref(chi2[1]))
-        gen._call('gic_zeldovich', 1)
+        gen._call('gic_zeldovich', wl.get('order', 1))
 
     for i in range(args.warmup):
         step(i)
@@ -339,6 +383,7 @@ def main():
                                      ['sphere r=%g at %s' % (wl['mods']['radius'], wl['mods']['centre'])])
                    if wl.get('mods') else [],
                    'precision': wl['precision'], 'seeding': wl['seed_cmd'], 'transfer': 'BBKS table, 2000 rows',
+                   'lpt_order': wl.get('order', 1),
                    'particles_per_step': npart, 'l2': 'inputs larger than L2 (fields >= 0.5 GB)',
                    'parallelism': 'replicas' if world > 1 else 'single GPU'},
         'e2e': {'value': round(npart * world / t_e2e / 1e6, 3), 'unit': 'Mparticles/s',

@@ -173,8 +173,15 @@ class ICGenerator:
                 x = np.where(x > period / 2, x - period, x)
                 x = np.where(x < -period / 2, x + period, x)
                 d.append(x)
-            X, Y, Z = np.meshgrid(d[0], d[1], d[2], indexing='ij')
-            self.flagged_levels.append(np.ascontiguousarray(np.flatnonzero(inside(X, Y, Z).ravel()), dtype=np.uint64))
+            # sphere and cube tests grow with each |offset|: a slab whose x offset fails
+            # with y = z = 0 has no flagged cell
+            zero = np.zeros(1)
+            Y, Z = d[1][:, None], d[2][None, :]
+            cells = []
+            for i in np.flatnonzero(inside(d[0], zero, zero)):
+                cells.append(np.flatnonzero(inside(d[0][i], Y, Z).ravel()) + i * n * n)
+            flat = np.concatenate(cells) if cells else np.zeros(0, dtype=np.int64)
+            self.flagged_levels.append(np.ascontiguousarray(flat, dtype=np.uint64))
         self.flagged = self.flagged_levels[-1]
 
     def select_sphere(self, radius):
