@@ -75,6 +75,11 @@ SIGNATURES = {
     'gic_calculate': [_P, _I, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_size_t, _D],
     'gic_add_modification': [_P, _I, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_size_t, ctypes.c_double, _I],
     'gic_clear_modifications': [_P],
+    'gic_noise_real': [_P, _I, _P],
+    'gic_field_from_noise': [_P, _I, _I, ctypes.POINTER(_P), _P],
+    'gic_field_from_noise_adjoint': [_P, _I, _I, _P, ctypes.POINTER(_P)],
+    'gic_variance_gradient': [_P, ctypes.POINTER(_P), ctypes.POINTER(ctypes.c_size_t), ctypes.c_double,
+                              ctypes.POINTER(_P), ctypes.POINTER(_P), _I, _D],
     'gic_calculate_variance': [_P, ctypes.POINTER(_P), ctypes.POINTER(ctypes.c_size_t), ctypes.c_double, _D],
     'gic_add_variance_modification': [_P, ctypes.POINTER(_P), ctypes.POINTER(ctypes.c_size_t), ctypes.c_double,
                                       ctypes.c_double, _I, _I, ctypes.c_double],

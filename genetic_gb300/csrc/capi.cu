@@ -487,6 +487,51 @@ int gic_add_variance_modification(gic_ctx *ctx, const unsigned long long *const 
   API_END
 }
 
+int gic_noise_real(gic_ctx *ctx, int level, void *dev_out) {
+  API_BEGIN(ctx)
+  if (!dev_out) gic::fail(GIC_ERR_INVALID_ARG, "null output");
+  gic::level_at(C, level);
+  gic::noise_real(C, level, dev_out);
+  API_END
+}
+
+static void check_device_arrays(gic::Context &C, const void *const *a, const char *what) {
+  if (!a) gic::fail(GIC_ERR_INVALID_ARG, std::string("null ") + what);
+  for (size_t l = 0; l < C.levels.size(); ++l)
+    if (!a[l]) gic::fail(GIC_ERR_INVALID_ARG, std::string("null ") + what + " array of a level");
+}
+
+int gic_field_from_noise(gic_ctx *ctx, int level, int what, const void *const *dev_noise, void *dev_out) {
+  API_BEGIN(ctx)
+  if (!C.transfer.ready) gic::fail(GIC_ERR_NOT_READY, "no transfer function");
+  check_device_arrays(C, dev_noise, "noise");
+  if (!dev_out) gic::fail(GIC_ERR_INVALID_ARG, "null output");
+  gic::field_from_noise(C, level, what - GIC_FIELD_DELTA, dev_noise, dev_out);
+  API_END
+}
+
+int gic_field_from_noise_adjoint(gic_ctx *ctx, int level, int what, const void *dev_grad_out,
+                                 void *const *dev_grad_noise) {
+  API_BEGIN(ctx)
+  if (!C.transfer.ready) gic::fail(GIC_ERR_NOT_READY, "no transfer function");
+  check_device_arrays(C, dev_grad_noise, "gradient");
+  if (!dev_grad_out) gic::fail(GIC_ERR_INVALID_ARG, "null input");
+  gic::field_from_noise_adjoint(C, level, what - GIC_FIELD_DELTA, dev_grad_out, dev_grad_noise);
+  API_END
+}
+
+int gic_variance_gradient(gic_ctx *ctx, const unsigned long long *const *cells, const size_t *counts,
+                          double filterscale, const void *const *dev_noise, void *const *dev_grad, int exact,
+                          double *value) {
+  API_BEGIN(ctx)
+  if (!value) gic::fail(GIC_ERR_INVALID_ARG, "null output");
+  check_device_arrays(C, dev_noise, "noise");
+  check_device_arrays(C, dev_grad, "gradient");
+  gic::QuadRequest q = make_quad_request(C, cells, counts, filterscale);
+  *value = gic::variance_gradient(C, q, dev_noise, dev_grad, exact != 0);
+  API_END
+}
+
 int gic_apply_modifications(gic_ctx *ctx, double *chi2_before, double *chi2_after) {
   API_BEGIN(ctx)
   if (C.mods.empty() && C.quads.empty()) gic::fail(GIC_ERR_NOT_READY, "no modifications to apply");

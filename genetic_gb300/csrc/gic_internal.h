@@ -196,6 +196,9 @@ void build_sqrtp_table_species(Context &ctx, Level &L, int dm);
 void za_fields(Context &ctx, int level);
 void zoom_combine(Context &ctx, int level);
 void lpt2_fields(Context &ctx);
+// tab_main of level li (sqrt(P) times its high-pass) and the low-pass tables of a coarse level
+void level_tables(Context &ctx, int li);
+void lowpass_tables(Context &ctx, int coarse_index);
 
 // zoom.cu
 template <typename T, int NF>
@@ -206,6 +209,11 @@ double modification_value(Context &ctx, const ModRequest &m);
 double noise_chi2(Context &ctx);
 double variance_value(Context &ctx, QuadRequest &q);
 void apply_modifications(Context &ctx, double *chi2_before, double *chi2_after);
+// realisation maps on real-space white noise and their adjoints (device arrays, compact N^3)
+void field_from_noise(Context &ctx, int level, int what, const void *const *noise, void *out);
+void field_from_noise_adjoint(Context &ctx, int level, int what, const void *grad_out, void *const *grad_noise);
+double variance_gradient(Context &ctx, QuadRequest &q, const void *const *noise, void *const *grad, bool exact);
+void noise_real(Context &ctx, int level, void *out);
 
 // particles.cu
 double velocity_to_offset_ratio(const Cosmo &c);

@@ -570,6 +570,9 @@ void lpt2_fields(Context &ctx) {
     lpt2_typed<float>(ctx);
 }
 
+void level_tables(Context &ctx, int li) { build_level_tables(ctx, li); }
+void lowpass_tables(Context &ctx, int coarse_index) { build_lowpass_tables(ctx, coarse_index); }
+
 void za_fields(Context &ctx, int li) {
   Level &L = *ctx.levels[li];
   if (!L.have_noise) fail(GIC_ERR_NOT_READY, "white noise has not been drawn");

@@ -371,6 +371,19 @@ __global__ void k_subsample_add(const T *fine, int nf, int r, int sx, int sy, in
   coarse[((size_t)X * nc + Y) * (size_t)(2 * (nc / 2 + 1)) + Z] += s;
 }
 
+// transpose of k_subsample_add: every fine cell takes its coarse cell's value / r^3
+template <typename T>
+__global__ void k_subsample_transpose(const T *coarse, int nc, int r, int sx, int sy, int sz, T *fine, int nf) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)nf * nf * nf) return;
+  int z = (int)(i % nf);
+  size_t rr = i / nf;
+  int y = (int)(rr % nf), x = (int)(rr / nf);
+  int X = ((sx + x / r) % nc + nc) % nc, Y = ((sy + y / r) % nc + nc) % nc, Z = ((sz + z / r) % nc + nc) % nc;
+  fine[((size_t)x * nf + y) * (size_t)(2 * (nf / 2 + 1)) + z] =
+      coarse[((size_t)X * nc + Y) * (size_t)(2 * (nc / 2 + 1)) + Z] / (T)((double)r * r * r);
+}
+
 template <typename T>
 __global__ void k_axes_geom(int nf, double dxf, double f0, double f1, double f2, double o0, double o1, double o2,
                             double dxc, double period, int nc, int *ubase, T *frac) {
@@ -386,6 +399,57 @@ __global__ void k_axes_geom(int nf, double dxf, double f0, double f1, double f2,
   double f = floor(u);
   frac[id] = (T)(u - f);
   ubase[id] = (int)f + (int)floor(lu / period) * nc;
+}
+
+// compact N^3 real arrays <-> padded real layout (rows of 2(N/2+1))
+template <typename T>
+__global__ void k_pad(const T *compact, T *padded, int n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)n * n * n) return;
+  size_t row = i / n;
+  padded[row * (size_t)(2 * (n / 2 + 1)) + (i - row * n)] = compact[i];
+}
+template <typename T>
+__global__ void k_unpad(const T *padded, T *compact, int n, T scale) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)n * n * n) return;
+  size_t row = i / n;
+  compact[i] = padded[row * (size_t)(2 * (n / 2 + 1)) + (i - row * n)] * scale;
+}
+
+// multiply a half spectrum by the map of field `what` (0: delta = tab[q] w; 1-3:
+// psi_a = i k_a tab[q] w / k^2, zero at k = 0 and where k_a is the Nyquist mode,
+// zeldovich.hpp:155-181), or by its complex conjugate (the adjoint)
+template <typename T>
+__global__ void k_field_mult(typename V2m<T>::type *c, int n, const double *tab, T kmin, int what, int conj) {
+  const int H = n / 2, S = H + 1;
+  unsigned row = blockIdx.x * kRowsPerBlock + threadIdx.y;
+  int iz = blockIdx.y * kKzChunk + threadIdx.x;
+  if (row >= (unsigned)n * (unsigned)n || iz >= S) return;
+  int ix = (int)(row / (unsigned)n), iy = (int)(row % (unsigned)n);
+  int kc[3] = {ix > H ? ix - n : ix, iy > H ? iy - n : iy, iz};
+  long long q = (long long)kc[0] * kc[0] + (long long)kc[1] * kc[1] + (long long)kc[2] * kc[2];
+  size_t id = (size_t)row * S + iz;
+  typename V2m<T>::type v = c[id];
+  T t = (T)tab[q];
+  if (what == 0) {
+    v.x *= t;
+    v.y *= t;
+  } else {
+    int a = what - 1;
+    T f[3] = {(T)kc[0] * kmin, (T)kc[1] * kmin, (T)kc[2] * kmin};
+    T kk = f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
+    T m = (q == 0 || kc[a] == H) ? (T)0 : t * f[a] / kk;
+    T x = v.x, y = v.y;
+    if (conj) {
+      v.x = m * y;
+      v.y = -m * x;
+    } else {
+      v.x = -m * y;
+      v.y = m * x;
+    }
+  }
+  c[id] = v;
 }
 
 inline unsigned nblk(size_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
@@ -642,6 +706,12 @@ struct ModEngine {
   // The reference transforms after each masking; the sums are formed here in real
   // space, which needs four transforms instead of six.
   void windowed_covector_real(Field &X, int t, T *R) {
+    windowed_self_real(t, R);
+    for (int s = 0; s < nl(); ++s)
+      if (s != t) cross_term_impl(R, t, ptr(X, s), s);
+  }
+  // the level's own part P1^T P1 x, P1 = f W + (1 - W): symmetric
+  void windowed_self_real(int t, T *R) {
     window_masks(t, t + 1);
     S.win.ensure(elems(t) * sizeof(T));
     T *I = S.win.template as<T>();
@@ -655,8 +725,61 @@ struct ModEngine {
     apply_family(I, t, 1);
     to_real(I, t);
     window_op(R, I, t, 1);  // R = W (f g) + (1 - W) g
-    for (int s = 0; s < nl(); ++s)
-      if (s != t) cross_term_impl(R, t, ptr(X, s), s);
+  }
+
+  // Transpose of the covector metric (apply_metric(X, out, true)).  The level
+  // blocks are symmetric; the cross block (s <- t) = move_{t->s} F_t (filter
+  // f_s f_t sqrt(w_s/w_t) on grid t, then interpolation up or block means down)
+  // transposes to F_t move^T_{s->t}: the transposed interpolation (deinterpolation
+  // at unit scale) or the transposed block mean (each fine cell takes its coarse
+  // cell's value / r^3).
+  void apply_metric_cov_transpose(Field &X, Field &out) {
+    for (int l = 0; l < nl(); ++l) to_fourier(X, l);
+    alloc(out);
+    for (int t = 0; t < nl(); ++t) {
+      T *R = ptr(out, t);
+      GIC_CUDA(cudaMemcpyAsync(R, ptr(X, t), elems(t) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
+      if (t < nl() - 1) {
+        to_real(R, t);
+        windowed_self_real(t, R);
+      } else {
+        apply_family(R, t, 2);
+        to_real(R, t);
+      }
+      for (int s = 0; s < nl(); ++s)
+        if (s != t) cross_transpose_add(R, t, ptr(X, s), s);
+      to_fourier(R, t);
+      out.fourier[t] = 1;
+    }
+  }
+  void cross_transpose_add(T *target_real, int t, const T *source_k, int s) {
+    auto src = ctx.pool.take(elems(s) * sizeof(T)), buf = ctx.pool.take(elems(t) * sizeof(T));
+    T *xs = src->template as<T>(), *b = buf->template as<T>();
+    GIC_CUDA(cudaMemcpyAsync(xs, source_k, elems(s) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
+    to_real(xs, s);
+    GIC_CUDA(cudaMemsetAsync(b, 0, elems(t) * sizeof(T), ctx.stream));
+    if (s > t) {
+      deinterpolate(xs, s, b, t, true);
+    } else {
+      const Level &F = lev(t), &Cl = lev(s);
+      int r = (int)std::lround(Cl.dx / F.dx);
+      int sx = (int)std::lround((F.x0[0] - Cl.x0[0]) / Cl.dx), sy = (int)std::lround((F.x0[1] - Cl.x0[1]) / Cl.dx),
+          sz = (int)std::lround((F.x0[2] - Cl.x0[2]) / Cl.dx);
+      k_subsample_transpose<T><<<nblk(F.ncells()), 256, 0, ctx.stream>>>(xs, Cl.n, r, sx, sy, sz, b, F.n);
+      launched();
+    }
+    to_fourier(b, t);
+    TableSpec sp{};
+    sp.power = 1;
+    add_filter_factors(sp, s);
+    add_filter_factors(sp, t);
+    sp.scalar = std::sqrt(level_weight(s) / level_weight(t));
+    table(sp, t);
+    mul_table(b, t);
+    to_real(b, t);
+    axpy(target_real, b, 1.0, t);
+    ctx.pool.give(std::move(src));
+    ctx.pool.give(std::move(buf));
   }
 
   // <C_cov X | X> (OutputField::getChi2 through the covector metric), with the
@@ -761,7 +884,6 @@ struct ModEngine {
   // with FilteredVarianceModification::pushOneLevelFieldThroughMatrix (:152-170):
   // out = sqrt(P) C_cov [W F V F W] sqrt(P) X, a covector in Fourier space
   void push_variance(Field &X, QuadRequest &q, Field &out) {
-    upload_cells(q);
     Field R;
     alloc(R);
     for (int l = 0; l < nl(); ++l) {
@@ -769,7 +891,38 @@ struct ModEngine {
       T *p = ptr(R, l);
       GIC_CUDA(cudaMemcpyAsync(p, ptr(X, l), elems(l) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
       mul_sqrtp_dm(p, l);
-      to_real(p, l);
+    }
+    apply_Q(R, q);
+    apply_metric(R, out, true);
+    for (int l = 0; l < nl(); ++l) mul_sqrtp_dm(ptr(out, l), l);
+  }
+
+  // The transpose of the pushed map: sqrt(P) [W F V F W] C_cov^T sqrt(P) X.  With
+  // push_variance it gives the gradient (A + A^T) X of <A X|X>.
+  void push_variance_transpose(Field &X, QuadRequest &q, Field &out) {
+    Field R;
+    alloc(R);
+    for (int l = 0; l < nl(); ++l) {
+      to_fourier(X, l);
+      T *p = ptr(R, l);
+      GIC_CUDA(cudaMemcpyAsync(p, ptr(X, l), elems(l) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
+      mul_sqrtp_dm(p, l);
+      R.fourier[l] = 1;
+    }
+    apply_metric_cov_transpose(R, out);
+    apply_Q(out, q);
+    for (int l = 0; l < nl(); ++l) {
+      to_fourier(out, l);
+      mul_sqrtp_dm(ptr(out, l), l);
+    }
+  }
+
+  // per level W F V F W (pushOneLevelFieldThroughMatrix): Fourier in, real out
+  void apply_Q(Field &R, QuadRequest &q) {
+    upload_cells(q);
+    for (int l = 0; l < nl(); ++l) {
+      T *p = ptr(R, l);
+      to_real(R, l);
       window_cells(p, l, q, false);
       to_fourier(p, l);
       mul_variance_highpass(p, l, q.scale);
@@ -781,8 +934,136 @@ struct ModEngine {
       window_cells(p, l, q, false);
       R.fourier[l] = 0;
     }
-    apply_metric(R, out, true);
-    for (int l = 0; l < nl(); ++l) mul_sqrtp_dm(ptr(out, l), l);
+  }
+
+  // --- realisation maps on real-space white noise, and their adjoints -----------
+  // No reference counterpart: they serve gradients through the realisation.  The
+  // white noise of a level is taken as the real field w (unit gaussians); its
+  // unitary transform is the half spectrum genetIC draws.  Level L's field is
+  // C2R(m_L R2C(w_L)), plus for a zoom level L = 1 the base level's
+  // C2R(m_LP R2C(w_0)) interpolated onto the zoom cells; the adjoint applies
+  // conj(m) and, for the coarse part, the transposed interpolation.
+
+  void pad_from(const void *compact, T *padded, int l) {
+    k_pad<T><<<nblk(lev(l).ncells()), 256, 0, ctx.stream>>>(static_cast<const T *>(compact), padded, lev(l).n);
+    launched();
+  }
+  void unpad_to(const T *padded, void *compact, int l, T scale = (T)1) {
+    k_unpad<T><<<nblk(lev(l).ncells()), 256, 0, ctx.stream>>>(padded, static_cast<T *>(compact), lev(l).n, scale);
+    launched();
+  }
+  void field_mult(T *p, int l, const double *tab, int what, int conj) {
+    k_field_mult<T><<<hs_grid(lev(l).n), hs_block(), 0, ctx.stream>>>(reinterpret_cast<C *>(p), lev(l).n, tab,
+                                                                       (T)lev(l).kmin(), what, conj);
+    launched();
+  }
+  void check_map(int L, int what) {
+    if (L < 0 || L >= nl()) fail(GIC_ERR_INVALID_ARG, "level out of range");
+    if (what < 0 || what > 3) fail(GIC_ERR_INVALID_ARG, "field must be delta or a displacement component");
+    if (L > 1) fail(GIC_ERR_INVALID_ARG, "gradients through the zoom combination are available for the first zoom level");
+  }
+
+  void map_forward(int L, int what, const void *const *noise, void *out) {
+    check_map(L, what);
+    level_tables(ctx, L);
+    auto b = ctx.pool.take(elems(L) * sizeof(T));
+    T *p = b->template as<T>();
+    pad_from(noise[L], p, L);
+    to_fourier(p, L);
+    field_mult(p, L, lev(L).tab_main.template as<double>(), what, 0);
+    to_real(p, L);
+    if (L == 1) {
+      lowpass_tables(ctx, 0);
+      auto c = ctx.pool.take(elems(0) * sizeof(T));
+      T *q = c->template as<T>();
+      pad_from(noise[0], q, 0);
+      to_fourier(q, 0);
+      field_mult(q, 0, lev(0).tab_lp_src.template as<double>(), what, 0);
+      to_real(q, 0);
+      const T *src[1] = {q};
+      T *dst[1] = {p};
+      interp_add<T, 1>(ctx, lev(0), src, lev(1), dst);
+      ctx.pool.give(std::move(c));
+    }
+    unpad_to(p, out, L);
+    GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+    ctx.pool.give(std::move(b));
+  }
+
+  void map_adjoint(int L, int what, const void *g, void *const *grad) {
+    check_map(L, what);
+    level_tables(ctx, L);
+    for (int l = 0; l < nl(); ++l)
+      if (l != L && !(L == 1 && l == 0) && grad[l])
+        GIC_CUDA(cudaMemsetAsync(grad[l], 0, lev(l).ncells() * sizeof(T), ctx.stream));
+    auto b = ctx.pool.take(elems(L) * sizeof(T));
+    T *p = b->template as<T>();
+    pad_from(g, p, L);
+    std::unique_ptr<DevBuf> c;
+    if (L == 1) {
+      // transposed interpolation of the zoom-level gradient onto the base level
+      lowpass_tables(ctx, 0);
+      c = ctx.pool.take(elems(0) * sizeof(T));
+      T *q = c->template as<T>();
+      GIC_CUDA(cudaMemsetAsync(q, 0, elems(0) * sizeof(T), ctx.stream));
+      deinterpolate(p, 1, q, 0, true);
+    }
+    to_fourier(p, L);
+    field_mult(p, L, lev(L).tab_main.template as<double>(), what, 1);
+    to_real(p, L);
+    unpad_to(p, grad[L], L);
+    if (L == 1) {
+      T *q = c->template as<T>();
+      to_fourier(q, 0);
+      field_mult(q, 0, lev(0).tab_lp_src.template as<double>(), what, 1);
+      to_real(q, 0);
+      unpad_to(q, grad[0], 0);
+    }
+    GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+    ctx.pool.give(std::move(b));
+    if (c) ctx.pool.give(std::move(c));
+  }
+
+  // value <A w|w> of the variance functional (p = A w is the pushed covector,
+  // quadraticmodification.hpp:51-92) and its gradient: exact, (A + A^T) w, or the
+  // direction of the reference's quadratic solver, 2 p (equal when A is symmetric,
+  // as on one level)
+  double variance_grad(QuadRequest &q, const void *const *noise, void *const *grad, bool exact) {
+    Field W, P;
+    alloc(W);
+    for (int l = 0; l < nl(); ++l) {
+      pad_from(noise[l], ptr(W, l), l);
+      W.fourier[l] = 0;
+      to_fourier(W, l);
+    }
+    push_variance(W, q, P);
+    double v = inner(P, W);
+    if (exact) {
+      Field PT;
+      push_variance_transpose(W, q, PT);
+      for (int l = 0; l < nl(); ++l) {
+        axpy(ptr(P, l), ptr(PT, l), 1.0, l);
+        to_real(P, l);
+        unpad_to(ptr(P, l), grad[l], l, (T)1);
+      }
+    } else {
+      for (int l = 0; l < nl(); ++l) {
+        to_real(P, l);
+        unpad_to(ptr(P, l), grad[l], l, (T)2);
+      }
+    }
+    GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+    return v;
+  }
+
+  void noise_to_real(int l, void *out) {
+    if (!lev(l).have_noise) fail(GIC_ERR_NOT_READY, "white noise has not been drawn");
+    auto b = ctx.pool.take(elems(l) * sizeof(T));
+    GIC_CUDA(cudaMemcpyAsync(b->ptr, lev(l).noise.ptr, elems(l) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
+    to_real(b->template as<T>(), l);
+    unpad_to(b->template as<T>(), out, l);
+    GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+    ctx.pool.give(std::move(b));
   }
 
   // covector of one modification (kind 0 overdensity, 1..3 velocity x,y,z)
@@ -827,11 +1108,12 @@ struct ModEngine {
   void build_sqrtp_dm(int l);
 
   // transpose tricubic: fine real (level f) / r^3 added into coarse real (level c)
-  void deinterpolate(const T *fine, int f, T *coarse, int c) {
+  // unit_scale: the plain transpose of the tricubic interpolation (no 1/r^3)
+  void deinterpolate(const T *fine, int f, T *coarse, int c, bool unit_scale = false) {
     const Level &Fl = lev(f), &Cl = lev(c);
     int nf = Fl.n;
     int r = (int)std::lround(Cl.dx / Fl.dx);
-    T scale = (T)(1.0 / ((double)r * r * r));
+    T scale = unit_scale ? (T)1 : (T)(1.0 / ((double)r * r * r));
     S.geom.ensure(3 * (size_t)nf * (sizeof(int) + sizeof(T)));
     int *ub = S.geom.template as<int>();
     T *fr = reinterpret_cast<T *>(ub + 3 * nf);
@@ -1086,6 +1368,26 @@ static double variance_value_t(Context &ctx, QuadRequest &q) {
 
 double variance_value(Context &ctx, QuadRequest &q) {
   return ctx.dbl() ? variance_value_t<double>(ctx, q) : variance_value_t<float>(ctx, q);
+}
+
+void field_from_noise(Context &ctx, int level, int what, const void *const *noise, void *out) {
+  if (ctx.dbl()) ModEngine<double>(ctx).map_forward(level, what, noise, out);
+  else ModEngine<float>(ctx).map_forward(level, what, noise, out);
+}
+
+void field_from_noise_adjoint(Context &ctx, int level, int what, const void *grad_out, void *const *grad_noise) {
+  if (ctx.dbl()) ModEngine<double>(ctx).map_adjoint(level, what, grad_out, grad_noise);
+  else ModEngine<float>(ctx).map_adjoint(level, what, grad_out, grad_noise);
+}
+
+double variance_gradient(Context &ctx, QuadRequest &q, const void *const *noise, void *const *grad, bool exact) {
+  return ctx.dbl() ? ModEngine<double>(ctx).variance_grad(q, noise, grad, exact)
+                   : ModEngine<float>(ctx).variance_grad(q, noise, grad, exact);
+}
+
+void noise_real(Context &ctx, int level, void *out) {
+  if (ctx.dbl()) ModEngine<double>(ctx).noise_to_real(level, out);
+  else ModEngine<float>(ctx).noise_to_real(level, out);
 }
 
 double modification_value(Context &ctx, const ModRequest &m) {

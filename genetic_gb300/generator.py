@@ -35,6 +35,7 @@ class ICGenerator:
             raise _lib.GicError(st, lib.gic_last_error(None).decode())
         self._ctx = ctx
         self.precision = precision
+        self.device = device
         # genetIC's defaults for Om, Ob, h, ns (genetIC/src/ic.hpp:200-210); Ol, s8
         # and zin have no default there and are always set by a paramfile
         self.cosmo = dict(omega_m=0.3, omega_lambda=0.7, omega_b=0.0, hubble=0.701, sigma8=0.8, ns=0.96,

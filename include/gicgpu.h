@@ -185,6 +185,35 @@ GIC_API int gic_add_variance_modification(gic_ctx *ctx, const unsigned long long
                                           double filterscale, double target, int relative, int init_steps,
                                           double precision);
 
+/* ---- Gradients through the realisation (no genetIC counterpart) -------------
+ * For the Python autograd binding.  Arrays are DEVICE pointers in the context's
+ * precision (float for GIC_MIXED, double for GIC_FP64), compact n^3 per level in
+ * genetIC's (x n + y) n + z order.  A level's white noise is taken as its real
+ * field w (unit gaussians), the inverse unitary transform of the half spectrum
+ * the reference draws.  Calls run on the context's stream and return when done.
+ * Gradients through the zoom combination are available for levels 0 and 1. */
+
+/* The drawn white noise of a level as a real field. */
+GIC_API int gic_noise_real(gic_ctx *ctx, int level, void *dev_out);
+
+/* `what` (GIC_FIELD_DELTA or GIC_FIELD_PSI_X..Z) of `level` from the real white
+ * noise of every level (dev_noise[l]), as gic_zeldovich forms it (own level times
+ * sqrt(P) and its high-pass; on level 1 plus the base level's low-passed field
+ * interpolated in), and its adjoint: dev_grad_noise[l] = (d field / d w_l)^T g. */
+GIC_API int gic_field_from_noise(gic_ctx *ctx, int level, int what, const void *const *dev_noise, void *dev_out);
+GIC_API int gic_field_from_noise_adjoint(gic_ctx *ctx, int level, int what, const void *dev_grad_out,
+                                         void *const *dev_grad_noise);
+
+/* The variance functional <A w|w> of gic_calculate_variance at the real white
+ * noise dev_noise[l] (A w = the pushed covector, quadraticmodification.hpp:59-92),
+ * and its gradient in dev_grad[l]: with `exact`, (A + A^T) w through the
+ * transposed kernels; otherwise 2 A w, the direction of the reference's quadratic
+ * solver (modificationmanager.hpp:249-275).  The two agree on one level; across
+ * levels the covector metric's cross terms make A unsymmetric. */
+GIC_API int gic_variance_gradient(gic_ctx *ctx, const unsigned long long *const *cells, const size_t *counts,
+                                  double filterscale, const void *const *dev_noise, void *const *dev_grad,
+                                  int exact, double *value);
+
 /* Apply the queued modifications to the white noise (orthonormalised, with the
  * covariance metric), returning chi^2 before and after.  Replaces
  * ModificationManager::applyModifications (modificationmanager.hpp:90-125). */
