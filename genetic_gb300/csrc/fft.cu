@@ -28,8 +28,19 @@ template <> struct Cx<double> { using type = double2; };
 
 template <typename C> __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
 template <typename C> __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
-template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
-  C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+// complex product with its fused multiply-adds spelled out, so that every pass
+// (fixed-length or runtime-length, any tile width) rounds it the same way
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  float2 r;
+  r.x = fmaf(a.x, b.x, -(a.y * b.y));
+  r.y = fmaf(a.x, b.y, a.y * b.x);
+  return r;
+}
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  double2 r;
+  r.x = fma(a.x, b.x, -(a.y * b.y));
+  r.y = fma(a.x, b.y, a.y * b.x);
+  return r;
 }
 // multiply by s*i (s = +-1)
 template <typename C> __device__ __forceinline__ C cmuli(C a, int s) {
@@ -487,6 +498,207 @@ __global__ void __launch_bounds__(NT) k_fft_cols(typename Cx<T>::type *data, lon
   }
 }
 
+// ---- fused passes: the first stage reads HBM into registers, the last writes HBM ----
+// Shared memory then carries only the exchanges between stages (4 accesses per
+// element at L = 512 instead of 8).  The tile is unpadded: every access is
+// column-fastest.  Inputs and outputs are described by small functors.
+
+__host__ __device__ constexpr int next_radix(int L, int NS) { return (L / NS) >= 8 ? 8 : L / NS; }
+__host__ __device__ constexpr int last_stage_ns(int L) {
+  int ns = 1;
+  while (ns * next_radix(L, ns) < L) ns *= next_radix(L, ns);
+  return ns;
+}
+
+// stages with NS in [NS, STOP), shared memory to shared memory
+template <typename T, int L, int TC, int TCP, int NT, int NS, int STOP, int SIGN, int TWM, bool DONE = (NS >= STOP)>
+struct TileStagesUntil {
+  static __device__ __forceinline__ void run(typename Cx<T>::type *tile, const typename Cx<T>::type *tw) {
+    constexpr int R = next_radix(L, NS);
+    tile_stage<T, L, TC, TCP, NT, R, NS, SIGN, TWM>(tile, tw);
+    TileStagesUntil<T, L, TC, TCP, NT, NS * R, STOP, SIGN, TWM>::run(tile, tw);
+  }
+};
+template <typename T, int L, int TC, int TCP, int NT, int NS, int STOP, int SIGN, int TWM>
+struct TileStagesUntil<T, L, TC, TCP, NT, NS, STOP, SIGN, TWM, true> {
+  static __device__ __forceinline__ void run(typename Cx<T>::type *, const typename Cx<T>::type *) {}
+};
+
+// first stage (NS = 1, no twiddles): inputs from `in(c, position)`, outputs to the tile
+template <typename T, int L, int TC, int NT, int SIGN, class In>
+__device__ __forceinline__ void first_stage_from(typename Cx<T>::type *tile, const In &in) {
+  using C = typename Cx<T>::type;
+  constexpr int R = next_radix(L, 1), LR = L / R, NB = LR * TC, PER = (NB + NT - 1) / NT;
+  C v[PER][R];
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int b = threadIdx.x + p * NT;
+    if (NB % NT == 0 || b < NB) {
+      const int c = b % TC, j = b / TC;
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[p][r] = in(c, j + r * LR);
+    }
+  }
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int b = threadIdx.x + p * NT;
+    if (NB % NT == 0 || b < NB) {
+      const int c = b % TC, j = b / TC;
+      Dft<T, C, R>::run(v[p], SIGN);
+#pragma unroll
+      for (int r = 0; r < R; ++r) tile[(j * R + r) * TC + c] = v[p][r];
+    }
+  }
+  __syncthreads();
+}
+
+// last stage: inputs from the tile, outputs to `out(c, position, value)`
+template <typename T, int L, int TC, int NT, int SIGN, int TWM, class Out>
+__device__ __forceinline__ void last_stage_to(const typename Cx<T>::type *tile, const typename Cx<T>::type *tw,
+                                              const Out &out) {
+  using C = typename Cx<T>::type;
+  constexpr int NS = last_stage_ns(L), R = L / NS, LR = L / R, NB = LR * TC, PER = (NB + NT - 1) / NT;
+  C v[PER][R];
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int b = threadIdx.x + p * NT;
+    if (NB % NT == 0 || b < NB) {
+      const int c = b % TC, j = b / TC;
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[p][r] = tile[(j + r * LR) * TC + c];
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[p][r] = cmul(v[p][r], twid(tw, TWM * r * j * (L / (NS * R)), SIGN));
+      Dft<T, C, R>::run(v[p], SIGN);
+#pragma unroll
+      for (int r = 0; r < R; ++r) out(c, j + r * NS, v[p][r]);
+    }
+  }
+}
+
+template <typename C>
+__device__ __forceinline__ C czero() {
+  C z;
+  z.x = 0;
+  z.y = 0;
+  return z;
+}
+
+template <typename C>
+struct ColsIn {
+  const C *base;
+  long long B;
+  int tcv;
+  __device__ __forceinline__ C operator()(int c, int m) const {
+    return c < tcv ? base[(size_t)m * (size_t)B + c] : czero<C>();
+  }
+};
+template <typename C, typename T>
+struct ColsOut {
+  C *base;
+  long long B;
+  int tcv;
+  T scale;
+  __device__ __forceinline__ void operator()(int c, int m, C v) const {
+    if (c < tcv) base[(size_t)m * (size_t)B + c] = cscale(v, scale);
+  }
+};
+// c2r packing on the fly: Z[m] = (X[m] + conj X[H-m]) + i (X[m] - conj X[H-m]) e^{+2 pi i m / N}
+template <typename C>
+struct RowsC2RIn {
+  const C *base;
+  const C *tw;
+  int S, H, rows_valid;
+  __device__ __forceinline__ C operator()(int c, int m) const {
+    if (c >= rows_valid) return czero<C>();
+    C a = base[(size_t)c * S + m], bq = base[(size_t)c * S + (H - m)];
+    if (m == 0) {
+      a.y = 0;
+      bq.y = 0;
+    }
+    C bc = cconj(bq);
+    return cadd(cadd(a, bc), cmuli(cmul(csub(a, bc), twid(tw, m, +1)), +1));
+  }
+};
+template <typename C, typename T>
+struct RowsOut {
+  C *base;
+  int S, rows_valid;
+  T scale;
+  __device__ __forceinline__ void operator()(int c, int m, C v) const {
+    if (c < rows_valid) base[(size_t)c * S + m] = cscale(v, scale);
+  }
+};
+template <typename C>
+struct RowsIn {
+  const C *base;
+  int S, rows_valid;
+  __device__ __forceinline__ C operator()(int c, int m) const {
+    return c < rows_valid ? base[(size_t)c * S + m] : czero<C>();
+  }
+};
+
+template <typename T, int L, int TC, int NT, int SIGN>
+__global__ void __launch_bounds__(NT, 1024 / NT) k_fft_cols_fused(typename Cx<T>::type *data, long long B,
+                                                       const typename Cx<T>::type *tw, T scale) {
+  using C = typename Cx<T>::type;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C *tile = reinterpret_cast<C *>(smraw);
+  const long long b0 = (long long)blockIdx.x * TC;
+  C *base = data + (size_t)blockIdx.y * (size_t)L * (size_t)B + b0;
+  const int tcv = (int)min((long long)TC, B - b0);
+  first_stage_from<T, L, TC, NT, SIGN>(tile, ColsIn<C>{base, B, tcv});
+  constexpr int R0 = next_radix(L, 1), NSL = last_stage_ns(L);
+  TileStagesUntil<T, L, TC, TC, NT, R0, NSL, SIGN, 1>::run(tile, tw);
+  last_stage_to<T, L, TC, NT, SIGN, 1>(tile, tw, ColsOut<C, T>{base, B, tcv, scale});
+}
+
+template <typename T, int H, int RPC, int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) k_fft_rows_c2r_fused(typename Cx<T>::type *data, long long nrows,
+                                                           const typename Cx<T>::type *tw, T scale) {
+  using C = typename Cx<T>::type;
+  constexpr int S = H + 1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C *tile = reinterpret_cast<C *>(smraw);
+  const long long r0 = (long long)blockIdx.x * RPC;
+  const int rows_valid = (int)min((long long)RPC, nrows - r0);
+  C *base = data + (size_t)r0 * S;
+  first_stage_from<T, H, RPC, NT, +1>(tile, RowsC2RIn<C>{base, tw, S, H, rows_valid});
+  constexpr int R0 = next_radix(H, 1), NSL = last_stage_ns(H);
+  TileStagesUntil<T, H, RPC, RPC, NT, R0, NSL, +1, 2>::run(tile, tw);
+  last_stage_to<T, H, RPC, NT, +1, 2>(tile, tw, RowsOut<C, T>{base, S, rows_valid, scale});
+}
+
+template <typename T, int H, int RPC, int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) k_fft_rows_r2c_fused(typename Cx<T>::type *data, long long nrows,
+                                                           const typename Cx<T>::type *tw, T scale) {
+  using C = typename Cx<T>::type;
+  constexpr int S = H + 1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C *tile = reinterpret_cast<C *>(smraw);  // [H + 1][RPC]
+  const long long r0 = (long long)blockIdx.x * RPC;
+  const int rows_valid = (int)min((long long)RPC, nrows - r0);
+  C *base = data + (size_t)r0 * S;
+  first_stage_from<T, H, RPC, NT, -1>(tile, RowsIn<C>{base, S, rows_valid});
+  constexpr int R0 = next_radix(H, 1);
+  TileStagesUntil<T, H, RPC, RPC, NT, R0, H, -1, 2>::run(tile, tw);
+  // X[k] and X[H-k] from Z[k] and Z[H-k] (Z[H] = Z[0]), in place
+  for (int e = threadIdx.x; e < RPC * (H / 2 + 1); e += NT) {
+    const int row = e % RPC, k = e / RPC;
+    C zk = tile[k * RPC + row];
+    C zh = tile[(k == 0 ? 0 : H - k) * RPC + row];
+    C zhc = cconj(zh), zkc = cconj(zk);
+    C xk = cadd(cscale(cadd(zk, zhc), (T)0.5), cmuli(cmul(cscale(csub(zk, zhc), (T)0.5), twid(tw, k, -1)), -1));
+    C xh = cadd(cscale(cadd(zh, zkc), (T)0.5), cmuli(cmul(cscale(csub(zh, zkc), (T)0.5), twid(tw, H - k, -1)), -1));
+    if (2 * k != H) tile[(H - k) * RPC + row] = xh;
+    tile[k * RPC + row] = xk;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < RPC * S; e += NT) {
+    const int row = e % RPC, m = e / RPC;
+    if (row < rows_valid) base[(size_t)row * S + m] = cscale(tile[m * RPC + row], scale);
+  }
+}
+
 // c2r rows of N = 2H reals: rows of H + 1 Hermitian coefficients are copied
 // (coalesced) into a tile [H + 1][RPC + 1] with one row per tile column, packed
 // into H complex values, transformed, and copied back as N reals per row.
@@ -591,9 +803,11 @@ void set_smem(const void *fn, size_t bytes) {
 }
 
 // launchers of the fixed-length passes; candidate tile widths per precision:
-//   strided: (TC, threads) = FP32 (8, 256) | (16, 512), FP64 (4, 256) | (8, 256)
-//   rows:    (RPC, threads) = FP32 (8, 256) | (16, 256), FP64 (4, 256) | (8, 256)
-constexpr int kFixedCandidates = 2;
+//   strided: (TC, threads) = FP32 (8, 256) | (16, 512) | fused (8, 512) | fused (16, 512),
+//            FP64 (4, 256) | (8, 256) | fused (4, 256) | fused (8, 128)
+//   rows:    (RPC, threads) = FP32 (8, 256) | (16, 256) | fused (16, 256) | (32, 512),
+//            FP64 (4, 256) | (8, 256) | fused (8, 256) | (16, 512)
+constexpr int kFixedCandidates = 4;
 
 inline void set_smem_once(const void *fn, size_t bytes, int &done_mask) {
   int dev = 0;
@@ -618,6 +832,30 @@ struct FixedFft {
     k_fft_cols<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale);
     launched();
   }
+  template <int TC, int NT, int SIGN>
+  static void cols_fused(Context &ctx, C *d, int A, long long B, const C *tw, T scale) {
+    static int mask = 0;
+    const size_t smem = (size_t)N * TC * sizeof(C);
+    set_smem_once((const void *)k_fft_cols_fused<T, N, TC, NT, SIGN>, smem, mask);
+    dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)A);
+    k_fft_cols_fused<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale);
+    launched();
+  }
+  template <int RPC, int NT, bool INV>
+  static void rows_fused(Context &ctx, C *d, const C *tw, T scale) {
+    static int mask = 0;
+    const size_t smem = (size_t)(INV ? H : S) * RPC * sizeof(C);
+    const long long nrows = (long long)N * N;
+    const unsigned grid = (unsigned)((nrows + RPC - 1) / RPC);
+    if (INV) {
+      set_smem_once((const void *)k_fft_rows_c2r_fused<T, H, RPC, NT>, smem, mask);
+      k_fft_rows_c2r_fused<T, H, RPC, NT><<<grid, NT, smem, ctx.stream>>>(d, nrows, tw, scale);
+    } else {
+      set_smem_once((const void *)k_fft_rows_r2c_fused<T, H, RPC, NT>, smem, mask);
+      k_fft_rows_r2c_fused<T, H, RPC, NT><<<grid, NT, smem, ctx.stream>>>(d, nrows, tw, scale);
+    }
+    launched();
+  }
   template <int RPC, int NT, bool INV>
   static void rows(Context &ctx, C *d, const C *tw, T scale) {
     static int mask = 0;
@@ -634,7 +872,13 @@ struct FixedFft {
     launched();
   }
   static void cols_cfg(Context &ctx, int cfg, int sign, C *d, int A, long long B, const C *tw, T scale) {
-    if (cfg == 0) {
+    if (cfg == 2) {
+      if (sign > 0) cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale);
+      else cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale);
+    } else if (cfg == 3) {
+      if (sign > 0) cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, +1>(ctx, d, A, B, tw, scale);
+      else cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, -1>(ctx, d, A, B, tw, scale);
+    } else if (cfg == 0) {
       if (sign > 0) cols<F32 ? 8 : 4, 256, +1>(ctx, d, A, B, tw, scale);
       else cols<F32 ? 8 : 4, 256, -1>(ctx, d, A, B, tw, scale);
     } else {
@@ -643,7 +887,13 @@ struct FixedFft {
     }
   }
   static void rows_cfg(Context &ctx, int cfg, bool inv, C *d, const C *tw, T scale) {
-    if (cfg == 0) {
+    if (cfg == 2) {
+      if (inv) rows_fused<F32 ? 16 : 8, 256, true>(ctx, d, tw, scale);
+      else rows_fused<F32 ? 16 : 8, 256, false>(ctx, d, tw, scale);
+    } else if (cfg == 3) {
+      if (inv) rows<F32 ? 32 : 16, 512, true>(ctx, d, tw, scale);
+      else rows<F32 ? 32 : 16, 512, false>(ctx, d, tw, scale);
+    } else if (cfg == 0) {
       if (inv) rows<F32 ? 8 : 4, 256, true>(ctx, d, tw, scale);
       else rows<F32 ? 8 : 4, 256, false>(ctx, d, tw, scale);
     } else {
