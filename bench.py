@@ -51,6 +51,16 @@ WORKLOADS = {
     'za512_fp64': dict(levels=[('base', 100.0, 512)], seed_cmd='random_seed', precision='fp64'),
     'za256': dict(levels=[('base', 100.0, 256)], seed_cmd='random_seed', precision='mixed'),
 }
+# 64 independent realisations in one batch (mixed precision, seeds 1..64): 32 single-level
+# 128^3 boxes (50 Mpc/h), 24 single-level 192^3 boxes (75 Mpc/h) and 8 two-level zooms of a
+# 256^3 base (100 Mpc/h) plus a 128^3 zoom of side 25 Mpc/h centred at (50, 50, 50), each zoom
+# with 2 modifications: overdensity +1.0 in a 1.5 Mpc/h sphere at the centre and -0.5 in a
+# 3 Mpc/h sphere 5 Mpc/h along x
+BATCH64 = ([dict(levels=[('base', 50.0, 128)], mods=[])] * 32 +
+           [dict(levels=[('base', 75.0, 192)], mods=[])] * 24 +
+           [dict(levels=[('base', 100.0, 256), ('zoom', 96, 96, 96, 2, 128)], replaced=64 ** 3,
+                 mods=[((50.0, 50.0, 50.0), 1.5, 1.0), ((55.0, 50.0, 50.0), 3.0, -0.5)])] * 8)
+WORKLOADS['batch64'] = dict(batch=BATCH64, precision='mixed', seed_cmd='random_seed', levels=[])
 DEFAULT_WORKLOAD = 'zoom512'
 COSMO = dict(omega_m=0.31, omega_lambda=0.69, omega_b=0.0, hubble=0.68, sigma8=0.81, ns=0.965, redshift=99.0)
 SEED = 8896131
@@ -248,6 +258,93 @@ def run_reference(args, wl, rank, world):
     print(json.dumps(line))
 
 
+def run_batch(args, wl, table, local, rank, world):
+    """The batch workload through gic_batch_realise: one step = one realisation of
+    every member.  Also times the same realisations one after another through the
+    plain entry points, for comparison."""
+    import torch
+    from genetic_gb300.batch import Batch
+    from genetic_gb300.generator import _ptr
+    gens = []
+    for m in wl['batch']:
+        w = dict(levels=m['levels'], precision=wl['precision'], seed_cmd=wl['seed_cmd'])
+        gen = make_gen(w, table, local)
+        for centre, radius, target in m['mods']:
+            gen.centre(*centre)
+            gen.select_sphere(radius)
+            gen.modify('overdensity', 'absolute', target)
+        gens.append(gen)
+    npart = sum(n_particles(dict(levels=m['levels'], replaced=m.get('replaced', 0))) for m in wl['batch'])
+    batch = Batch(gens)
+    stream = torch.cuda.ExternalStream(batch.stream(), device=torch.device('cuda', local))
+    nthreads = min(16, os.cpu_count() or 1)
+
+    def step(i):
+        batch.realise([1 + k + 64 * i for k in range(len(gens))], threads=nthreads)
+
+    for i in range(args.warmup):
+        step(i)
+    launches0 = ctypes.c_ulonglong()
+    gens[0]._lib.gic_launch_count(ctypes.byref(launches0))
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        start.record(stream)
+        for i in range(args.steps):
+            step(args.warmup + i)
+        end.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    launches1 = ctypes.c_ulonglong()
+    gens[0]._lib.gic_launch_count(ctypes.byref(launches1))
+    t = max_over_ranks(start.elapsed_time(end) * 1e-3 / args.steps, world)
+    # the same realisations one at a time through the plain entry points
+    t0 = time.perf_counter()
+    for k, gen in enumerate(gens):
+        gen._call('gic_draw_noise', 1 + k, 2)
+        if wl['batch'][k]['mods']:
+            gen._call('gic_apply_modifications', None, None)
+        gen._call('gic_zeldovich', 1)
+    torch.cuda.synchronize()
+    t_seq = time.perf_counter() - t0
+    # end to end: every member's particles copied back to pinned host memory each step
+    pinned = []
+    for gen in gens:
+        for lev in range(len(gen.levels)):
+            n = gen.levels[lev][1]
+            pinned.append((gen, lev, torch.empty((n ** 3, 3), dtype=torch.float64, pin_memory=True).numpy(),
+                           torch.empty((n ** 3, 3), dtype=torch.float64, pin_memory=True).numpy()))
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        step(i)
+        for gen, lev, pos, vel in pinned:
+            gen._call('gic_fetch_particles', lev, _ptr(pos), _ptr(vel))
+    t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
+    d2h = sum(p.nbytes + v.nbytes for _, _, p, v in pinned)
+    batch.close()
+    for gen in gens:
+        gen.close()
+    if rank != 0:
+        return
+    line = {
+        'metric': METRIC, 'value': round(npart * world / t / 1e6, 3), 'unit': 'Mparticles/s', 'n_gpus': world,
+        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(t * 1e3, 3), 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32+f64', 'data': 'synthetic',
+        'config': {'workload': args.workload, 'members': '32 x 128^3 (50 Mpc/h), 24 x 192^3 (75 Mpc/h), '
+                   '8 x (256^3 base 100 Mpc/h + 128^3 zoom of 25 Mpc/h, 2 overdensity modifications)',
+                   'realisations_per_step': len(gens), 'particles_per_step': npart, 'host_threads': nthreads,
+                   'sequential_ms_per_step': round(t_seq * 1e3, 3), 'precision': wl['precision'],
+                   'parallelism': 'replicas' if world > 1 else 'single GPU',
+                   'l2': 'inputs larger than L2 (the batch holds tens of GB)'},
+        'e2e': {'value': round(npart * world / t_e2e / 1e6, 3), 'unit': 'Mparticles/s', 'h2d_bytes_per_step': 0,
+                'd2h_bytes_per_step': int(d2h)},
+        'gpu_launches': int(launches1.value - launches0.value),
+        'clocks': clk.summary(),
+    }
+    print(json.dumps(line))
+
+
 def accuracy(wl_name, wl, table, device):
     """Per-field max and RMS relative error (|a - b| / max|b|) of the workload's mixed
     form against its plain FP64 form, both on the GPU, same seed and modifications."""
@@ -308,6 +405,9 @@ def main():
     table = np.ascontiguousarray(bbks_table())
     if args.accuracy:
         accuracy(args.workload, wl, table, local)
+        return
+    if wl.get('batch'):
+        run_batch(args, wl, table, local, rank, world)
         return
     gen = make_gen(wl, table, local)
     sptr = ctypes.c_void_p()

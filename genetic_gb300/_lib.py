@@ -75,6 +75,11 @@ SIGNATURES = {
     'gic_calculate': [_P, _I, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_size_t, _D],
     'gic_add_modification': [_P, _I, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_size_t, ctypes.c_double, _I],
     'gic_clear_modifications': [_P],
+    'gic_batch_create': [ctypes.POINTER(_P), ctypes.POINTER(_P), _I],
+    'gic_batch_destroy': [_P],
+    'gic_batch_realise': [_P, ctypes.POINTER(ctypes.c_ulong), ctypes.POINTER(_I), _I, _I],
+    'gic_batch_last_error': [_P],
+    'gic_batch_get_stream': [_P, ctypes.POINTER(_P)],
     'gic_noise_real': [_P, _I, _P],
     'gic_field_from_noise': [_P, _I, _I, ctypes.POINTER(_P), _P],
     'gic_field_from_noise_adjoint': [_P, _I, _I, _P, ctypes.POINTER(_P)],
@@ -101,7 +106,7 @@ def load():
     for name, args in SIGNATURES.items():
         fn = getattr(lib, name)
         fn.argtypes = args
-        fn.restype = ctypes.c_char_p if name == 'gic_last_error' else ctypes.c_int
+        fn.restype = ctypes.c_char_p if name in ('gic_last_error', 'gic_batch_last_error') else ctypes.c_int
     _lib = lib
     return lib
 

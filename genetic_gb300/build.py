@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, 'csrc')
 BUILD = os.path.join(HERE, '_build')
 LIB = os.path.join(HERE, 'libgicgpu.so')
-SOURCES = ['capi.cu', 'rng.cu', 'fft.cu', 'kspace.cu', 'particles.cu', 'zoom.cu', 'modify.cu']
+SOURCES = ['capi.cu', 'rng.cu', 'fft.cu', 'kspace.cu', 'particles.cu', 'zoom.cu', 'modify.cu', 'batch.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-Xcompiler', '-fvisibility=hidden',
          '--expt-relaxed-constexpr']

@@ -10,9 +10,6 @@
 #include <new>
 #include <atomic>
 
-struct gic_ctx {
-  gic::Context impl;
-};
 
 namespace gic {
 
@@ -32,6 +29,9 @@ void launched(int kernels) {
   cuda_check(cudaGetLastError(), "kernel launch");
   g_launches.fetch_add((unsigned long long)kernels, std::memory_order_relaxed);
 }
+
+unsigned long long launch_count() { return g_launches.load(); }
+void count_launches(unsigned long long kernels) { g_launches.fetch_add(kernels, std::memory_order_relaxed); }
 
 namespace {
 

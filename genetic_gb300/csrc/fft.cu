@@ -18,6 +18,8 @@
 #include "gic_internal.h"
 #include <cmath>
 #include <algorithm>
+#include <atomic>
+#include <mutex>
 
 namespace gic {
 namespace {
@@ -797,8 +799,6 @@ __global__ void __launch_bounds__(NT) k_fft_rows_r2c_fixed(typename Cx<T>::type 
 
 template <typename T>
 void set_smem(const void *fn, size_t bytes) {
-  static size_t current = 0;
-  (void)current;
   GIC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
 }
 
@@ -809,12 +809,13 @@ void set_smem(const void *fn, size_t bytes) {
 //            FP64 (4, 256) | (8, 256) | fused (8, 256) | (16, 512)
 constexpr int kFixedCandidates = 4;
 
-inline void set_smem_once(const void *fn, size_t bytes, int &done_mask) {
+// the dynamic shared-memory limit of a kernel, set once per device (any host thread)
+inline void set_smem_once(const void *fn, size_t bytes, std::atomic<int> &done_mask) {
   int dev = 0;
   GIC_CUDA(cudaGetDevice(&dev));
-  if (done_mask & (1 << (dev & 31))) return;
+  if (done_mask.load() & (1 << (dev & 31))) return;
   GIC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-  done_mask |= 1 << (dev & 31);
+  done_mask.fetch_or(1 << (dev & 31));
 }
 
 template <typename T, int N>
@@ -825,7 +826,7 @@ struct FixedFft {
 
   template <int TC, int NT, int SIGN>
   static void cols(Context &ctx, C *d, int A, long long B, const C *tw, T scale) {
-    static int mask = 0;
+    static std::atomic<int> mask{0};
     const size_t smem = (size_t)N * (TC + 1) * sizeof(C);
     set_smem_once((const void *)k_fft_cols<T, N, TC, NT, SIGN>, smem, mask);
     dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)A);
@@ -834,7 +835,7 @@ struct FixedFft {
   }
   template <int TC, int NT, int SIGN>
   static void cols_fused(Context &ctx, C *d, int A, long long B, const C *tw, T scale) {
-    static int mask = 0;
+    static std::atomic<int> mask{0};
     const size_t smem = (size_t)N * TC * sizeof(C);
     set_smem_once((const void *)k_fft_cols_fused<T, N, TC, NT, SIGN>, smem, mask);
     dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)A);
@@ -843,7 +844,7 @@ struct FixedFft {
   }
   template <int RPC, int NT, bool INV>
   static void rows_fused(Context &ctx, C *d, const C *tw, T scale) {
-    static int mask = 0;
+    static std::atomic<int> mask{0};
     const size_t smem = (size_t)(INV ? H : S) * RPC * sizeof(C);
     const long long nrows = (long long)N * N;
     const unsigned grid = (unsigned)((nrows + RPC - 1) / RPC);
@@ -858,7 +859,7 @@ struct FixedFft {
   }
   template <int RPC, int NT, bool INV>
   static void rows(Context &ctx, C *d, const C *tw, T scale) {
-    static int mask = 0;
+    static std::atomic<int> mask{0};
     const size_t smem = (size_t)S * (RPC + 1) * sizeof(C);
     const long long nrows = (long long)N * N;
     const unsigned grid = (unsigned)((nrows + RPC - 1) / RPC);
@@ -945,20 +946,39 @@ struct FixedFft {
   }
 };
 
+// tuning results shared by every context of the process, per device, size and precision
+struct SharedTune {
+  int device, n;
+  bool dbl;
+  int cols, rows;
+};
+std::mutex g_tune_mutex;
+std::vector<SharedTune> g_tuned;
+
 template <typename T, int N>
 void fixed_transform(Context &ctx, typename Cx<T>::type *c, const typename Cx<T>::type *tw, double scale, bool inverse) {
   FftTables &F = ctx.fft;
+  const bool dbl = sizeof(T) == 8;
   int cc = -1, rc = -1;
   for (auto &t : F.tuned)
-    if (t.n == N && t.dbl == (sizeof(T) == 8)) {
+    if (t.n == N && t.dbl == dbl) {
       cc = t.cols;
       rc = t.rows;
     }
   if (cc < 0) {
-    cc = 0;
-    rc = 0;
-    if (N >= 128) FixedFft<T, N>::tune(ctx, tw, cc, rc);
-    F.tuned.push_back({N, sizeof(T) == 8, cc, rc});
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    for (auto &t : g_tuned)
+      if (t.device == ctx.device && t.n == N && t.dbl == dbl) {
+        cc = t.cols;
+        rc = t.rows;
+      }
+    if (cc < 0) {
+      cc = 0;
+      rc = 0;
+      if (N >= 128) FixedFft<T, N>::tune(ctx, tw, cc, rc);
+      g_tuned.push_back({ctx.device, N, dbl, cc, rc});
+    }
+    F.tuned.push_back({N, dbl, cc, rc});
   }
   if (F.force_cols >= 0) cc = F.force_cols;
   if (F.force_rows >= 0) rc = F.force_rows;

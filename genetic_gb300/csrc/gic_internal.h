@@ -17,6 +17,8 @@ struct Error {
 [[noreturn]] void fail(int code, const std::string &msg);
 // check the last launch and count it (gic_launch_count)
 void launched(int kernels = 1);
+unsigned long long launch_count();
+void count_launches(unsigned long long kernels);  // kernels run by a graph launch
 void cuda_check(cudaError_t e, const char *what);
 #define GIC_CUDA(call) ::gic::cuda_check((call), #call)
 
@@ -220,3 +222,8 @@ double velocity_to_offset_ratio(const Cosmo &c);
 void make_particles(Context &ctx, Level &L, int order = 1);
 
 }  // namespace gic
+
+// the opaque handle of the C ABI
+struct gic_ctx {
+  gic::Context impl;
+};

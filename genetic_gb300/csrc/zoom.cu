@@ -11,6 +11,7 @@
 // wrap when the coarse grid is the periodic base grid and clamp otherwise.
 // One thread per fine cell does all four fields (delta, psi_x, psi_y, psi_z).
 #include "gic_internal.h"
+#include <atomic>
 #include <cmath>
 
 namespace gic {
@@ -194,8 +195,15 @@ void interp_add(Context &ctx, const Level &coarse, const T *const *src, const Le
     fp.dst[f] = dst[f];
   }
   if (ratio <= 1.0 && smem <= 96 * 1024) {
-    GIC_CUDA(cudaFuncSetAttribute((const void *)k_interp_add_sep<T, NF, TY>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // raise the kernel's shared-memory limit to the 96 KB ceiling once per device
+    static std::atomic<int> mask{0};
+    int dev = 0;
+    GIC_CUDA(cudaGetDevice(&dev));
+    if (!(mask.load() & (1 << (dev & 31)))) {
+      GIC_CUDA(cudaFuncSetAttribute((const void *)k_interp_add_sep<T, NF, TY>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+      mask.fetch_or(1 << (dev & 31));
+    }
     dim3 grid((nf + TY - 1) / TY, nf);
     k_interp_add_sep<T, NF, TY><<<grid, 256, smem, ctx.stream>>>(fp, coarse.n, wrap, base, frac, ubase, nf, span);
     launched();

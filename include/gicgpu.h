@@ -235,6 +235,24 @@ GIC_API int gic_apply_modifications(gic_ctx *ctx, double *chi2_before, double *c
 #define GIC_NOALLOC_MAX_GAUSSIANS (1ull << 20)
 GIC_API int gic_gaussian_stream_noalloc(unsigned long seed, size_t n, double *device_out, void *stream);
 
+/* ---- Batches of independent realisations on one GPU (no genetIC counterpart) ----
+ * A batch groups contexts of one device (any sizes, levels and modifications).
+ * gic_batch_realise draws every context's white noise (seeds[i], seeding mode
+ * modes[i], or the parallel Fourier mode when modes is NULL) and applies its
+ * queued modifications from `threads` host threads, each context on its own
+ * stream; then it runs every context's field maps and particles (order 1 or 2).
+ * For order 1 those maps run as one CUDA graph over all contexts, captured on the
+ * first call and replayed while the contexts' buffers stay the same.  Returns
+ * when all realisations are complete; results are then read per context. */
+typedef struct gic_batch gic_batch;
+GIC_API int gic_batch_create(gic_batch **out, gic_ctx *const *ctxs, int n);
+GIC_API int gic_batch_destroy(gic_batch *batch);
+GIC_API int gic_batch_realise(gic_batch *batch, const unsigned long *seeds, const int *modes, int order, int threads);
+GIC_API const char *gic_batch_last_error(const gic_batch *batch);
+/* The stream a batch's graph runs on; every realisation of gic_batch_realise is
+ * ordered between work queued on it before the call and work queued after. */
+GIC_API int gic_batch_get_stream(gic_batch *batch, void **stream);
+
 /* Number of kernels this library has launched in the process so far. */
 GIC_API int gic_launch_count(unsigned long long *count);
 
