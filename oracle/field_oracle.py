@@ -61,9 +61,21 @@ def ranlux_stream(seed, n):
 
 # --- white noise (randomfieldgenerator.hpp:122-260) ---------------------------
 
+_FFT_WORKERS = None
+
+
+def set_fft_workers(workers):
+    """Host threads for the transforms (scipy.fft's pocketfft); None: numpy, one thread."""
+    global _FFT_WORKERS
+    _FFT_WORKERS = workers
+
+
 def fft_r2c(real):
     """Unitary forward transform, N^-1.5 (fourier.hpp:479-518)."""
     n = real.shape[0]
+    if _FFT_WORKERS:
+        import scipy.fft
+        return scipy.fft.rfftn(real, workers=_FFT_WORKERS) / n ** 1.5
     return np.fft.rfftn(real) / n ** 1.5
 
 
@@ -86,6 +98,9 @@ def mirror(c):
 def fft_c2r(c):
     """Unitary inverse transform of a half spectrum, N^-1.5, after mirroring."""
     n = c.shape[0]
+    if _FFT_WORKERS:
+        import scipy.fft
+        return scipy.fft.irfftn(mirror(c), s=(n, n, n), axes=(0, 1, 2), workers=_FFT_WORKERS) * n ** 1.5
     return np.fft.irfftn(mirror(c), s=(n, n, n), axes=(0, 1, 2)) * n ** 1.5
 
 
