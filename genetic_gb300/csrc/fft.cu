@@ -58,6 +58,15 @@ template <typename C> __device__ __forceinline__ C twid(const C *tw, int m, int 
   return w;
 }
 
+// per-|k|^2 table value at half-spectrum cell (kx, col), col = ky (N/2 + 1) + kz, of
+// an N^3 grid: the multiplier fused into the x pass (first of c2r, last of r2c)
+__device__ __forceinline__ double qtab(const double *tab, int N, int kx, long long col) {
+  const int S = N / 2 + 1, H = N / 2;
+  const int ky = (int)(col / S), kz = (int)(col - (long long)ky * S);
+  const long long a = kx > H ? kx - N : kx, b = ky > H ? ky - N : ky;
+  return tab[a * a + b * b + (long long)kz * kz];
+}
+
 template <typename T, typename C, int R> struct Dft;
 template <typename T, typename C> struct Dft<T, C, 2> {
   static __device__ __forceinline__ void run(C (&v)[2], int) {
@@ -159,7 +168,8 @@ __device__ __forceinline__ void ns_split(int j, int Ns, int ns_log, int &jm, int
 template <typename T, int R, int TC>
 __device__ __forceinline__ void strided_stage(const typename Cx<T>::type *src, typename Cx<T>::type *dst,
                                               typename Cx<T>::type *gout, long long B, int tcv, int L, int Ns,
-                                              int ns_log, int sign, const typename Cx<T>::type *tw, T scale) {
+                                              int ns_log, int sign, const typename Cx<T>::type *tw, T scale,
+                                              const double *tab, long long b0) {
   using C = typename Cx<T>::type;
   const int LR = L / R;
   const int nb = LR * TC;
@@ -179,7 +189,11 @@ __device__ __forceinline__ void strided_stage(const typename Cx<T>::type *src, t
     if (gout) {
       if (c < tcv) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) gout[(size_t)(d + r * Ns) * (size_t)B + c] = cscale(v[r], scale);
+        for (int r = 0; r < R; ++r) {
+          C o = cscale(v[r], scale);
+          if (tab) o = cscale(o, (T)qtab(tab, L, d + r * Ns, b0 + c));
+          gout[(size_t)(d + r * Ns) * (size_t)B + c] = o;
+        }
       }
     } else {
 #pragma unroll
@@ -188,10 +202,12 @@ __device__ __forceinline__ void strided_stage(const typename Cx<T>::type *src, t
   }
 }
 
+// tab: optional per-|k|^2 multiplier of the x pass, on the inputs (sign > 0) or the
+// scaled outputs (sign < 0)
 template <typename T, int TC>
 __global__ void __launch_bounds__(256) k_fft_strided(typename Cx<T>::type *data, int L, long long B,
                                                      Radix plan, int sign, const typename Cx<T>::type *tw,
-                                                     T scale) {
+                                                     T scale, const double *tab) {
   using C = typename Cx<T>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
   C *buf0 = reinterpret_cast<C *>(smraw);
@@ -213,15 +229,23 @@ __global__ void __launch_bounds__(256) k_fft_strided(typename Cx<T>::type *data,
   }
   cp_async_wait_all();
   __syncthreads();
+  if (sign > 0 && tab) {
+    for (int e = threadIdx.x; e < L * TC; e += blockDim.x) {
+      int i = e / TC, c = e % TC;
+      if (c < tcv) buf0[e] = cscale(buf0[e], (T)qtab(tab, L, i, b0 + c));
+    }
+    __syncthreads();
+  }
+  const double *otab = sign < 0 ? tab : nullptr;
   C *src = buf0, *dst = buf1;
   int Ns = 1, ns_log = 0;
   for (int s = 0; s < plan.n; ++s) {
     int R = plan.r[s];
     C *g = (s == plan.n - 1) ? base : nullptr;
-    if (R == 8) strided_stage<T, 8, TC>(src, dst, g, B, tcv, L, Ns, ns_log, sign, tw, scale);
-    else if (R == 4) strided_stage<T, 4, TC>(src, dst, g, B, tcv, L, Ns, ns_log, sign, tw, scale);
-    else if (R == 2) strided_stage<T, 2, TC>(src, dst, g, B, tcv, L, Ns, ns_log, sign, tw, scale);
-    else strided_stage<T, 3, TC>(src, dst, g, B, tcv, L, Ns, ns_log, sign, tw, scale);
+    if (R == 8) strided_stage<T, 8, TC>(src, dst, g, B, tcv, L, Ns, ns_log, sign, tw, scale, otab, b0);
+    else if (R == 4) strided_stage<T, 4, TC>(src, dst, g, B, tcv, L, Ns, ns_log, sign, tw, scale, otab, b0);
+    else if (R == 2) strided_stage<T, 2, TC>(src, dst, g, B, tcv, L, Ns, ns_log, sign, tw, scale, otab, b0);
+    else strided_stage<T, 3, TC>(src, dst, g, B, tcv, L, Ns, ns_log, sign, tw, scale, otab, b0);
     __syncthreads();
     C *t = src; src = dst; dst = t;
     Ns *= R;
@@ -470,9 +494,11 @@ struct TileStages<T, L, TC, TCP, NT, NS, SIGN, TWM, true> {
 };
 
 // strided pass over (A, L, B) complex, transform along L; grid (ceil(B / TC), A)
+// tab: optional per-|k|^2 multiplier (x pass only, B = L (L/2 + 1)): applied to
+// the inputs when SIGN > 0 (c2r) and to the scaled outputs when SIGN < 0 (r2c)
 template <typename T, int L, int TC, int NT, int SIGN>
 __global__ void __launch_bounds__(NT) k_fft_cols(typename Cx<T>::type *data, long long B,
-                                                 const typename Cx<T>::type *tw, T scale) {
+                                                 const typename Cx<T>::type *tw, T scale, const double *tab) {
   using C = typename Cx<T>::type;
   constexpr int TCP = TC + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -493,10 +519,21 @@ __global__ void __launch_bounds__(NT) k_fft_cols(typename Cx<T>::type *data, lon
   }
   cp_async_wait_all();
   __syncthreads();
+  if (SIGN > 0 && tab) {
+    for (int e = threadIdx.x; e < L * tcv; e += NT) {
+      const int i = e / tcv, c = e % tcv;
+      tile[i * TCP + c] = cscale(tile[i * TCP + c], (T)qtab(tab, L, i, b0 + c));
+    }
+    __syncthreads();
+  }
   TileStages<T, L, TC, TCP, NT, 1, SIGN, 1>::run(tile, tw);
   for (int e = threadIdx.x; e < L * TC; e += NT) {
     const int i = e / TC, c = e % TC;
-    if (c < tcv) base[(size_t)i * (size_t)B + c] = cscale(tile[i * TCP + c], scale);
+    if (c < tcv) {
+      C v = cscale(tile[i * TCP + c], scale);
+      if (SIGN < 0 && tab) v = cscale(v, (T)qtab(tab, L, i, b0 + c));
+      base[(size_t)i * (size_t)B + c] = v;
+    }
   }
 }
 
@@ -590,8 +627,13 @@ struct ColsIn {
   const C *base;
   long long B;
   int tcv;
+  const double *tab;  // optional multiplier (x pass of an L^3 grid)
+  int L;
+  long long b0;
   __device__ __forceinline__ C operator()(int c, int m) const {
-    return c < tcv ? base[(size_t)m * (size_t)B + c] : czero<C>();
+    if (c >= tcv) return czero<C>();
+    C v = base[(size_t)m * (size_t)B + c];
+    return tab ? cscale(v, (decltype(v.x))qtab(tab, L, m, b0 + c)) : v;
   }
 };
 template <typename C, typename T>
@@ -600,8 +642,14 @@ struct ColsOut {
   long long B;
   int tcv;
   T scale;
+  const double *tab;
+  int L;
+  long long b0;
   __device__ __forceinline__ void operator()(int c, int m, C v) const {
-    if (c < tcv) base[(size_t)m * (size_t)B + c] = cscale(v, scale);
+    if (c >= tcv) return;
+    v = cscale(v, scale);
+    if (tab) v = cscale(v, (T)qtab(tab, L, m, b0 + c));
+    base[(size_t)m * (size_t)B + c] = v;
   }
 };
 // c2r packing on the fly: Z[m] = (X[m] + conj X[H-m]) + i (X[m] - conj X[H-m]) e^{+2 pi i m / N}
@@ -641,17 +689,17 @@ struct RowsIn {
 
 template <typename T, int L, int TC, int NT, int SIGN>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_fft_cols_fused(typename Cx<T>::type *data, long long B,
-                                                       const typename Cx<T>::type *tw, T scale) {
+                                                       const typename Cx<T>::type *tw, T scale, const double *tab) {
   using C = typename Cx<T>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
   C *tile = reinterpret_cast<C *>(smraw);
   const long long b0 = (long long)blockIdx.x * TC;
   C *base = data + (size_t)blockIdx.y * (size_t)L * (size_t)B + b0;
   const int tcv = (int)min((long long)TC, B - b0);
-  first_stage_from<T, L, TC, NT, SIGN>(tile, ColsIn<C>{base, B, tcv});
+  first_stage_from<T, L, TC, NT, SIGN>(tile, ColsIn<C>{base, B, tcv, SIGN > 0 ? tab : nullptr, L, b0});
   constexpr int R0 = next_radix(L, 1), NSL = last_stage_ns(L);
   TileStagesUntil<T, L, TC, TC, NT, R0, NSL, SIGN, 1>::run(tile, tw);
-  last_stage_to<T, L, TC, NT, SIGN, 1>(tile, tw, ColsOut<C, T>{base, B, tcv, scale});
+  last_stage_to<T, L, TC, NT, SIGN, 1>(tile, tw, ColsOut<C, T>{base, B, tcv, scale, SIGN < 0 ? tab : nullptr, L, b0});
 }
 
 template <typename T, int H, int RPC, int NT>
@@ -825,21 +873,21 @@ struct FixedFft {
   static constexpr bool F32 = sizeof(T) == 4;
 
   template <int TC, int NT, int SIGN>
-  static void cols(Context &ctx, C *d, int A, long long B, const C *tw, T scale) {
+  static void cols(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const double *tab) {
     static std::atomic<int> mask{0};
     const size_t smem = (size_t)N * (TC + 1) * sizeof(C);
     set_smem_once((const void *)k_fft_cols<T, N, TC, NT, SIGN>, smem, mask);
     dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)A);
-    k_fft_cols<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale);
+    k_fft_cols<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab);
     launched();
   }
   template <int TC, int NT, int SIGN>
-  static void cols_fused(Context &ctx, C *d, int A, long long B, const C *tw, T scale) {
+  static void cols_fused(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const double *tab) {
     static std::atomic<int> mask{0};
     const size_t smem = (size_t)N * TC * sizeof(C);
     set_smem_once((const void *)k_fft_cols_fused<T, N, TC, NT, SIGN>, smem, mask);
     dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)A);
-    k_fft_cols_fused<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale);
+    k_fft_cols_fused<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab);
     launched();
   }
   template <int RPC, int NT, bool INV>
@@ -872,19 +920,20 @@ struct FixedFft {
     }
     launched();
   }
-  static void cols_cfg(Context &ctx, int cfg, int sign, C *d, int A, long long B, const C *tw, T scale) {
+  static void cols_cfg(Context &ctx, int cfg, int sign, C *d, int A, long long B, const C *tw, T scale,
+                       const double *tab = nullptr) {
     if (cfg == 2) {
-      if (sign > 0) cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale);
-      else cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale);
+      if (sign > 0) cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab);
+      else cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale, tab);
     } else if (cfg == 3) {
-      if (sign > 0) cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, +1>(ctx, d, A, B, tw, scale);
-      else cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, -1>(ctx, d, A, B, tw, scale);
+      if (sign > 0) cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, +1>(ctx, d, A, B, tw, scale, tab);
+      else cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, -1>(ctx, d, A, B, tw, scale, tab);
     } else if (cfg == 0) {
-      if (sign > 0) cols<F32 ? 8 : 4, 256, +1>(ctx, d, A, B, tw, scale);
-      else cols<F32 ? 8 : 4, 256, -1>(ctx, d, A, B, tw, scale);
+      if (sign > 0) cols<F32 ? 8 : 4, 256, +1>(ctx, d, A, B, tw, scale, tab);
+      else cols<F32 ? 8 : 4, 256, -1>(ctx, d, A, B, tw, scale, tab);
     } else {
-      if (sign > 0) cols<F32 ? 16 : 8, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale);
-      else cols<F32 ? 16 : 8, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale);
+      if (sign > 0) cols<F32 ? 16 : 8, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab);
+      else cols<F32 ? 16 : 8, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale, tab);
     }
   }
   static void rows_cfg(Context &ctx, int cfg, bool inv, C *d, const C *tw, T scale) {
@@ -902,15 +951,15 @@ struct FixedFft {
       else rows<F32 ? 16 : 8, 256, false>(ctx, d, tw, scale);
     }
   }
-  static void c2r(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg) {
-    cols_cfg(ctx, ccfg, +1, c, 1, (long long)N * S, tw, (T)1);
+  static void c2r(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, const double *tab) {
+    cols_cfg(ctx, ccfg, +1, c, 1, (long long)N * S, tw, (T)1, tab);
     cols_cfg(ctx, ccfg, +1, c, N, S, tw, (T)1);
     rows_cfg(ctx, rcfg, true, c, tw, scale);
   }
-  static void r2c(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg) {
+  static void r2c(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, const double *tab) {
     rows_cfg(ctx, rcfg, false, c, tw, (T)1);
     cols_cfg(ctx, ccfg, -1, c, N, S, tw, (T)1);
-    cols_cfg(ctx, ccfg, -1, c, 1, (long long)N * S, tw, scale);
+    cols_cfg(ctx, ccfg, -1, c, 1, (long long)N * S, tw, scale, tab);
   }
   // time every candidate on a scratch array of the transform's size
   static void tune(Context &ctx, const C *tw, int &best_cols, int &best_rows) {
@@ -956,7 +1005,8 @@ std::mutex g_tune_mutex;
 std::vector<SharedTune> g_tuned;
 
 template <typename T, int N>
-void fixed_transform(Context &ctx, typename Cx<T>::type *c, const typename Cx<T>::type *tw, double scale, bool inverse) {
+void fixed_transform(Context &ctx, typename Cx<T>::type *c, const typename Cx<T>::type *tw, double scale, bool inverse,
+                     const double *tab) {
   FftTables &F = ctx.fft;
   const bool dbl = sizeof(T) == 8;
   int cc = -1, rc = -1;
@@ -982,34 +1032,34 @@ void fixed_transform(Context &ctx, typename Cx<T>::type *c, const typename Cx<T>
   }
   if (F.force_cols >= 0) cc = F.force_cols;
   if (F.force_rows >= 0) rc = F.force_rows;
-  if (inverse) FixedFft<T, N>::c2r(ctx, c, tw, (T)scale, cc, rc);
-  else FixedFft<T, N>::r2c(ctx, c, tw, (T)scale, cc, rc);
+  if (inverse) FixedFft<T, N>::c2r(ctx, c, tw, (T)scale, cc, rc, tab);
+  else FixedFft<T, N>::r2c(ctx, c, tw, (T)scale, cc, rc, tab);
 }
 
 // power-of-two sizes 32..1024 use the fixed-length passes
 template <typename T>
 bool fixed_dispatch(Context &ctx, typename Cx<T>::type *c, int n, const typename Cx<T>::type *tw, double scale,
-                    bool inverse) {
+                    bool inverse, const double *tab) {
   switch (n) {
-    case 32: fixed_transform<T, 32>(ctx, c, tw, scale, inverse); return true;
-    case 64: fixed_transform<T, 64>(ctx, c, tw, scale, inverse); return true;
-    case 128: fixed_transform<T, 128>(ctx, c, tw, scale, inverse); return true;
-    case 256: fixed_transform<T, 256>(ctx, c, tw, scale, inverse); return true;
-    case 512: fixed_transform<T, 512>(ctx, c, tw, scale, inverse); return true;
-    case 1024: fixed_transform<T, 1024>(ctx, c, tw, scale, inverse); return true;
+    case 32: fixed_transform<T, 32>(ctx, c, tw, scale, inverse, tab); return true;
+    case 64: fixed_transform<T, 64>(ctx, c, tw, scale, inverse, tab); return true;
+    case 128: fixed_transform<T, 128>(ctx, c, tw, scale, inverse, tab); return true;
+    case 256: fixed_transform<T, 256>(ctx, c, tw, scale, inverse, tab); return true;
+    case 512: fixed_transform<T, 512>(ctx, c, tw, scale, inverse, tab); return true;
+    case 1024: fixed_transform<T, 1024>(ctx, c, tw, scale, inverse, tab); return true;
     default: return false;
   }
 }
 
 template <typename T>
 void strided_pass(Context &ctx, typename Cx<T>::type *data, int A, int L, long long B, int sign, T scale,
-                  const typename Cx<T>::type *tw) {
+                  const typename Cx<T>::type *tw, const double *tab = nullptr) {
   constexpr int TC = sizeof(T) == 4 ? 8 : 4;
   Radix plan = make_plan(L);
   size_t smem = 2ull * L * TC * sizeof(typename Cx<T>::type);
   set_smem<T>((const void *)k_fft_strided<T, TC>, smem);
   dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)A);
-  k_fft_strided<T, TC><<<grid, 256, smem, ctx.stream>>>(data, L, B, plan, sign, tw, scale);
+  k_fft_strided<T, TC><<<grid, 256, smem, ctx.stream>>>(data, L, B, plan, sign, tw, scale, tab);
   launched();
 }
 
@@ -1046,7 +1096,7 @@ const void *FftTables::get(int n, bool dbl, cudaStream_t s) {
 }
 
 template <typename T>
-void fft_c2r_3d(Context &ctx, T *data, int n, double scale) {
+void fft_c2r_3d(Context &ctx, T *data, int n, double scale, const double *pre_tab) {
   using C = typename Cx<T>::type;
   if (n < 2 || n % 2) fail(GIC_ERR_INVALID_ARG, "FFT size must be even");
   const C *tw = (const C *)ctx.fft.get(n, sizeof(T) == 8, ctx.stream);
@@ -1055,8 +1105,8 @@ void fft_c2r_3d(Context &ctx, T *data, int n, double scale) {
   long long mirror_threads = 2ll * n * n;
   k_mirror<T><<<(unsigned)((mirror_threads + 255) / 256), 256, 0, ctx.stream>>>(c, n);
   launched();
-  if (ctx.fft.force_cols != -2 && fixed_dispatch<T>(ctx, c, n, tw, scale, true)) return;
-  strided_pass<T>(ctx, c, 1, n, (long long)n * S, +1, (T)1, tw);
+  if (ctx.fft.force_cols != -2 && fixed_dispatch<T>(ctx, c, n, tw, scale, true, pre_tab)) return;
+  strided_pass<T>(ctx, c, 1, n, (long long)n * S, +1, (T)1, tw, pre_tab);
   strided_pass<T>(ctx, c, n, n, S, +1, (T)1, tw);
   int rpc = rows_per_cta<T>(n);
   Radix plan = make_plan(n / 2);
@@ -1069,13 +1119,13 @@ void fft_c2r_3d(Context &ctx, T *data, int n, double scale) {
 }
 
 template <typename T>
-void fft_r2c_3d(Context &ctx, T *data, int n, double scale) {
+void fft_r2c_3d(Context &ctx, T *data, int n, double scale, const double *post_tab) {
   using C = typename Cx<T>::type;
   if (n < 2 || n % 2) fail(GIC_ERR_INVALID_ARG, "FFT size must be even");
   const C *tw = (const C *)ctx.fft.get(n, sizeof(T) == 8, ctx.stream);
   C *c = reinterpret_cast<C *>(data);
   long long S = n / 2 + 1;
-  if (ctx.fft.force_cols != -2 && fixed_dispatch<T>(ctx, c, n, tw, scale, false)) return;
+  if (ctx.fft.force_cols != -2 && fixed_dispatch<T>(ctx, c, n, tw, scale, false, post_tab)) return;
   int rpc = rows_per_cta<T>(n);
   Radix plan = make_plan(n / 2);
   size_t smem = 2ull * rpc * S * sizeof(C);
@@ -1085,12 +1135,12 @@ void fft_r2c_3d(Context &ctx, T *data, int n, double scale) {
                                                                                    (T)1);
   launched();
   strided_pass<T>(ctx, c, n, n, S, -1, (T)1, tw);
-  strided_pass<T>(ctx, c, 1, n, (long long)n * S, -1, (T)scale, tw);
+  strided_pass<T>(ctx, c, 1, n, (long long)n * S, -1, (T)scale, tw, post_tab);
 }
 
-template void fft_c2r_3d<float>(Context &, float *, int, double);
-template void fft_c2r_3d<double>(Context &, double *, int, double);
-template void fft_r2c_3d<float>(Context &, float *, int, double);
-template void fft_r2c_3d<double>(Context &, double *, int, double);
+template void fft_c2r_3d<float>(Context &, float *, int, double, const double *);
+template void fft_c2r_3d<double>(Context &, double *, int, double, const double *);
+template void fft_r2c_3d<float>(Context &, float *, int, double, const double *);
+template void fft_r2c_3d<double>(Context &, double *, int, double, const double *);
 
 }  // namespace gic

@@ -182,10 +182,12 @@ struct Context {
 };
 
 // fft.cu
+// pre_tab / post_tab: optional per-|k|^2 multiplier applied to the half spectrum
+// before the inverse / after the forward transform, fused into the x pass
 template <typename T>
-void fft_c2r_3d(Context &ctx, T *data, int n, double scale);
+void fft_c2r_3d(Context &ctx, T *data, int n, double scale, const double *pre_tab = nullptr);
 template <typename T>
-void fft_r2c_3d(Context &ctx, T *data, int n, double scale);
+void fft_r2c_3d(Context &ctx, T *data, int n, double scale, const double *post_tab = nullptr);
 
 // rng.cu
 void draw_noise_all(Context &ctx, unsigned long long seed, int mode);

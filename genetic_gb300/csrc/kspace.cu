@@ -431,9 +431,7 @@ static void zoom_combine_typed(Context &ctx, int li) {
     // the combined real fields of level li-1, back to Fourier space, low-passed
     for (int f = 0; f < 4; ++f) {
       GIC_CUDA(cudaMemcpyAsync(src[f], Cl.field[f].ptr, nc * sizeof(C), cudaMemcpyDeviceToDevice, ctx.stream));
-      fft_r2c_3d<T>(ctx, src[f], Cl.n, scale);
-      k_scale_table<T><<<hs_grid(Cl.n), hs_block(), 0, ctx.stream>>>(reinterpret_cast<C *>(src[f]), Cl.n, Cl.tab_lp.as<double>());
-      launched();
+      fft_r2c_3d<T>(ctx, src[f], Cl.n, scale, Cl.tab_lp.as<double>());  // low-passed on the way out
     }
   }
   for (int f = 0; f < 4; ++f) fft_c2r_3d<T>(ctx, src[f], Cl.n, scale);
@@ -475,10 +473,7 @@ static void add_lowpassed_coarse(Context &ctx, int li, T *const *coarse, T *cons
   for (int f = 0; f < nf; ++f) {
     GIC_CUDA(cudaMemcpyAsync(t, coarse[f], bytes, cudaMemcpyDeviceToDevice, ctx.stream));
     fft_r2c_3d<T>(ctx, t, Cl.n, scale);
-    k_scale_table<T><<<hs_grid(Cl.n), hs_block(), 0, ctx.stream>>>(reinterpret_cast<C *>(t), Cl.n,
-                                                                    Cl.tab_lp.as<double>());
-    launched();
-    fft_c2r_3d<T>(ctx, t, Cl.n, scale);
+    fft_c2r_3d<T>(ctx, t, Cl.n, scale, Cl.tab_lp.as<double>());  // low-passed on the way back
     const T *src[1] = {t};
     T *dst[1] = {fine[f]};
     interp_add<T, 1>(ctx, Cl, src, F, dst);

@@ -510,6 +510,9 @@ struct ModEngine {
   }
   void to_fourier(T *p, int l) { fft_r2c_3d<T>(ctx, p, lev(l).n, scale(l)); }
   void to_real(T *p, int l) { fft_c2r_3d<T>(ctx, p, lev(l).n, scale(l)); }
+  // times the current table (S.tab), then to real space: the multiply rides on the
+  // transform's first pass (bit-identical to mul_table followed by to_real)
+  void to_real_times_table(T *p, int l) { fft_c2r_3d<T>(ctx, p, lev(l).n, scale(l), S.tab.template as<double>()); }
   void to_fourier(Field &f, int l) {
     if (!f.fourier[l]) to_fourier(ptr(f, l), l);
     f.fourier[l] = 1;
@@ -628,12 +631,15 @@ struct ModEngine {
 
   // f_l applied in Fourier space
   void apply_family(T *p, int l, int power) {
+    family_table(l, power);
+    mul_table(p, l);
+  }
+  void family_table(int l, int power) {
     TableSpec sp{};
     sp.power = power;
     sp.scalar = 1.0;
     add_filter_factors(sp, l);
     table(sp, l);
-    mul_table(p, l);
   }
 
   double level_weight(int l) {
@@ -650,8 +656,7 @@ struct ModEngine {
     S.tmp_src.ensure(elems(s) * sizeof(T));
     GIC_CUDA(cudaMemcpyAsync(S.tmp_src.ptr, source_k, elems(s) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
     table(sp, s);
-    mul_table(S.tmp_src.template as<T>(), s);
-    to_real(S.tmp_src.template as<T>(), s);
+    to_real_times_table(S.tmp_src.template as<T>(), s);
     if (s < t) {
       const T *src[1] = {S.tmp_src.template as<T>()};
       T *dst[1] = {target_real};
@@ -717,13 +722,13 @@ struct ModEngine {
     T *I = S.win.template as<T>();
     window_op(I, R, t, 2);  // I = W x
     to_fourier(I, t);
-    apply_family(I, t, 1);
-    to_real(I, t);
+    family_table(t, 1);
+    to_real_times_table(I, t);
     window_op(R, I, t, 0);  // g = (1 - W) x + f (W x)
     GIC_CUDA(cudaMemcpyAsync(I, R, elems(t) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
     to_fourier(I, t);
-    apply_family(I, t, 1);
-    to_real(I, t);
+    family_table(t, 1);
+    to_real_times_table(I, t);
     window_op(R, I, t, 1);  // R = W (f g) + (1 - W) g
   }
 
@@ -775,8 +780,7 @@ struct ModEngine {
     add_filter_factors(sp, t);
     sp.scalar = std::sqrt(level_weight(s) / level_weight(t));
     table(sp, t);
-    mul_table(b, t);
-    to_real(b, t);
+    to_real_times_table(b, t);
     axpy(target_real, b, 1.0, t);
     ctx.pool.give(std::move(src));
     ctx.pool.give(std::move(buf));
@@ -871,13 +875,12 @@ struct ModEngine {
     mul_table(p, l);
   }
 
-  void mul_variance_highpass(T *p, int l, double scale) {
+  void variance_highpass_table(int l, double scale) {
     TableSpec sp{};
     sp.power = 1;
     sp.scalar = 1.0;
     sp.var_cut = 2. * M_PI / scale;
     table(sp, l);
-    mul_table(p, l);
   }
 
   // QuadraticModification::pushMultiLevelFieldThroughMatrix (quadraticmodification.hpp:59-92)
@@ -924,13 +927,12 @@ struct ModEngine {
       T *p = ptr(R, l);
       to_real(R, l);
       window_cells(p, l, q, false);
+      variance_highpass_table(l, q.scale);
       to_fourier(p, l);
-      mul_variance_highpass(p, l, q.scale);
-      to_real(p, l);
+      to_real_times_table(p, l);
       window_cells(p, l, q, true);  // windowOperator then the variance operator
       to_fourier(p, l);
-      mul_variance_highpass(p, l, q.scale);
-      to_real(p, l);
+      to_real_times_table(p, l);
       window_cells(p, l, q, false);
       R.fourier[l] = 0;
     }
