@@ -35,6 +35,9 @@ GIC_FIELD_DELTA = 1
 GIC_FIELD_PSI_X = 2
 GIC_FIELD_PSI_Y = 3
 GIC_FIELD_PSI_Z = 4
+GIC_NOISE_REVERSE = 0
+GIC_NOISE_REVERSE_SMALL_K = 1
+GIC_NOISE_UNIT_MODULUS = 2
 GIC_FIELD_PSI2_X = 5
 GIC_FIELD_PSI2_Y = 6
 GIC_FIELD_PSI2_Z = 7
@@ -75,6 +78,7 @@ SIGNATURES = {
     'gic_calculate': [_P, _I, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_size_t, _D],
     'gic_add_modification': [_P, _I, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_size_t, ctypes.c_double, _I],
     'gic_clear_modifications': [_P],
+    'gic_noise_op': [_P, _I, ctypes.c_double],
     'gic_batch_create': [ctypes.POINTER(_P), ctypes.POINTER(_P), _I],
     'gic_batch_destroy': [_P],
     'gic_batch_realise': [_P, ctypes.POINTER(ctypes.c_ulong), ctypes.POINTER(_I), _I, _I],

@@ -305,6 +305,14 @@ int gic_draw_noise(gic_ctx *ctx, unsigned long seed, int mode) {
   API_END
 }
 
+int gic_noise_op(gic_ctx *ctx, int op, double param) {
+  API_BEGIN(ctx)
+  if (op < GIC_NOISE_REVERSE || op > GIC_NOISE_UNIT_MODULUS) gic::fail(GIC_ERR_INVALID_ARG, "unknown noise operation");
+  if (C.levels.empty()) gic::fail(GIC_ERR_NOT_READY, "no grid levels");
+  gic::noise_op(C, op, param);
+  API_END
+}
+
 int gic_gaussian_stream(gic_ctx *ctx, unsigned long seed, size_t n, double *host_dst) {
   API_BEGIN(ctx)
   if (!host_dst && n) gic::fail(GIC_ERR_INVALID_ARG, "null buffer");

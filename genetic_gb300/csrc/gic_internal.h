@@ -202,6 +202,7 @@ void zoom_combine(Context &ctx, int level);
 void lpt2_fields(Context &ctx);
 // tab_main of level li (sqrt(P) times its high-pass) and the low-pass tables of a coarse level
 void level_tables(Context &ctx, int li);
+void noise_op(Context &ctx, int op, double param);
 void lowpass_tables(Context &ctx, int coarse_index);
 
 // zoom.cu

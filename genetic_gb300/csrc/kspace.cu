@@ -565,6 +565,59 @@ void lpt2_fields(Context &ctx) {
     lpt2_typed<float>(ctx);
 }
 
+// ---- operations on the drawn white noise (ic.hpp:1342-1344, 1652-1705) ----------
+// op 0: w -> -w (reverse, multilevelfield.hpp:182-191); op 1: -w where 0 < k^2 < kmax^2,
+// k^2 in the grid's physical units as the reference forms it (reverseSmallK);
+// op 2: w -> w / |w| (enforcePowerSpectrumOneGrid, multilevelfield.hpp:498-510)
+template <typename T>
+__global__ void k_noise_op(typename V2<T>::type *w, int n, double kmin, int op, double k2max) {
+  const int H = n / 2, S = H + 1;
+  unsigned row = blockIdx.x * 8 + threadIdx.y;
+  int iz = blockIdx.y * 32 + threadIdx.x;
+  if (row >= (unsigned)n * (unsigned)n || iz >= S) return;
+  int ix = (int)(row / (unsigned)n), iy = (int)(row % (unsigned)n);
+  size_t id = (size_t)row * S + iz;
+  typename V2<T>::type v = w[id];
+  if (op == 0) {
+    v.x = -v.x;
+    v.y = -v.y;
+  } else if (op == 1) {
+    double kx = (double)(ix > H ? ix - n : ix) * kmin, ky = (double)(iy > H ? iy - n : iy) * kmin,
+           kz = (double)iz * kmin;
+    double k2 = kx * kx + ky * ky + kz * kz;
+    if (k2 < k2max && k2 != 0) {
+      v.x = -v.x;
+      v.y = -v.y;
+    }
+  } else {
+    T a = hypot(v.x, v.y);
+    if (a != 0) {
+      v.x /= a;
+      v.y /= a;
+    }
+  }
+  w[id] = v;
+}
+
+template <typename T>
+static void noise_op_typed(Context &ctx, int op, double param) {
+  using C = typename V2<T>::type;
+  for (auto &Lp : ctx.levels) {
+    Level &L = *Lp;
+    k_noise_op<T><<<hs_grid(L.n), hs_block(), 0, ctx.stream>>>(L.noise.as<C>(), L.n, L.kmin(), op, param * param);
+    launched();
+    L.have_fields = L.have_lpt2 = false;
+  }
+  GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+}
+
+void noise_op(Context &ctx, int op, double param) {
+  for (auto &L : ctx.levels)
+    if (!L->have_noise) fail(GIC_ERR_NOT_READY, "white noise has not been drawn");
+  if (ctx.dbl()) noise_op_typed<double>(ctx, op, param);
+  else noise_op_typed<float>(ctx, op, param);
+}
+
 void level_tables(Context &ctx, int li) { build_level_tables(ctx, li); }
 void lowpass_tables(Context &ctx, int coarse_index) { build_lowpass_tables(ctx, coarse_index); }
 

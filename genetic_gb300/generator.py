@@ -257,12 +257,32 @@ class ICGenerator:
 
     # -- realisation -------------------------------------------------------------
     def draw(self):
+        """initialiseAllRandomComponents (ic.hpp:1334-1352): draw, then the exact power
+        spectrum if `fix_power` was given."""
         if self._drawn:
             return
         if self.seed is None:
             raise RuntimeError('The random number generator has not been seeded')
         self._call('gic_draw_noise', self.seed, self.seed_mode)
+        if getattr(self, '_fix_power', False):
+            self._call('gic_noise_op', _lib.GIC_NOISE_UNIT_MODULUS, 0.0)
         self._drawn = True
+
+    def fix_power(self):
+        """setExactPowerSpectrumEnforcement (ic.hpp:669-671)."""
+        self._fix_power = True
+
+    exact_power_spectrum_enforcement = fix_power
+
+    def reverse(self):
+        """ICGenerator::reverse (ic.hpp:1652-1655): the white noise changes sign."""
+        self.draw()
+        self._call('gic_noise_op', _lib.GIC_NOISE_REVERSE, 0.0)
+
+    def reverse_small_k(self, kmax):
+        """ICGenerator::reverseSmallK (ic.hpp:1690-1705), kmax in h/Mpc."""
+        self.draw()
+        self._call('gic_noise_op', _lib.GIC_NOISE_REVERSE_SMALL_K, float(kmax))
 
     def done(self, apply_modifications=True, order=1):
         """Draw the noise if needed, apply the queued modifications, then P(k), the
@@ -323,7 +343,8 @@ _COMMANDS = {
     'seedfourier_reverse': 'seedfourier_reverse', 'done': 'done', 'chi2': 'chi2',
     'centre': 'centre', 'select_sphere': 'select_sphere', 'select_cube': 'select_cube',
     'calculate': 'calculate', 'modify': 'modify', 'clear_modifications': 'clear_modifications',
-    'filtering_scale': 'filtering_scale',
+    'filtering_scale': 'filtering_scale', 'fix_power': 'fix_power',
+    'exact_power_spectrum_enforcement': 'fix_power', 'reverse': 'reverse', 'reverse_small_k': 'reverse_small_k',
     'apply_modifications': 'apply_modifications',
 }
 # output-side commands handled by genetIC's own writers; accepted and ignored here

@@ -106,6 +106,17 @@ GIC_API int gic_draw_noise(gic_ctx *ctx, unsigned long seed, int mode);
  * diagnostics. */
 GIC_API int gic_gaussian_stream(gic_ctx *ctx, unsigned long seed, size_t n, double *host_dst);
 
+/* Operations on the drawn white noise of every level:
+ *   GIC_NOISE_REVERSE           w -> -w; ICGenerator::reverse (ic.hpp:1652-1655, multilevelfield.hpp:182-191)
+ *   GIC_NOISE_REVERSE_SMALL_K   w -> -w where 0 < k^2 < param^2 (k in h/Mpc on each level's grid);
+ *                               ICGenerator::reverseSmallK (ic.hpp:1690-1705)
+ *   GIC_NOISE_UNIT_MODULUS      w -> w / |w|, the exact power spectrum of `fix_power`, applied by
+ *                               genetIC right after drawing (ic.hpp:1342-1344, multilevelfield.hpp:395-407, 498-510) */
+#define GIC_NOISE_REVERSE 0
+#define GIC_NOISE_REVERSE_SMALL_K 1
+#define GIC_NOISE_UNIT_MODULUS 2
+GIC_API int gic_noise_op(gic_ctx *ctx, int op, double param);
+
 /* Upload / download a level's white noise as a half spectrum of interleaved
  * (re,im) doubles.  Replaces Field data access for import_level / dump_grid_fourier. */
 GIC_API int gic_set_noise(gic_ctx *ctx, int level, const double *host_src);

@@ -407,6 +407,26 @@ def zoom_realisation(noises, levels, power):
     return out
 
 
+# --- operations on the white noise (ic.hpp:1342-1344, 1652-1705) ---------------------------
+
+def noise_reverse_small_k(noise, box, kmax):
+    """-w where 0 < k^2 < kmax^2, k = integer * 2 pi / box per component (reverseSmallK)."""
+    n = noise.shape[0]
+    ki, kz, kmin = kgrid(n, box)
+    kx = (ki * kmin)[:, None, None]
+    ky = (ki * kmin)[None, :, None]
+    kzz = (kz * kmin)[None, None, :]
+    k2 = kx * kx + ky * ky + kzz * kzz
+    return np.where((k2 < kmax * kmax) & (k2 != 0), -noise, noise)
+
+
+def noise_unit_modulus(noise):
+    """w / |w| where w != 0 (enforcePowerSpectrumOneGrid, multilevelfield.hpp:498-510)."""
+    a = np.abs(noise)
+    with np.errstate(invalid='ignore', divide='ignore'):
+        return np.where(a == 0, 0, noise / np.where(a == 0, 1, a))
+
+
 # --- second-order LPT (no counterpart in genetIC: Scoccimarro 1998, Crocce, Pueblas &
 # Scoccimarro 2006, with Einstein-de Sitter growth: D2 = -3/7 D1^2, f2 = 2) -------------
 

@@ -204,6 +204,30 @@ def var_goldens():
                                 **{k: np.array(v) for k, v in vals.items()})
 
 
+OPS = {
+    # noise operations on one level and on two (the zoom2 geometry)
+    'ops_reverse': (['reverse'], 1),
+    'ops_reverse_small_k': (['reverse_small_k 0.5'], 1),
+    'ops_fix_power': (['fix_power'], 1),
+    'ops_reverse_small_k_zoom': (['reverse_small_k 0.7'], 2),
+    'ops_fix_power_zoom': (['fix_power'], 2),
+}
+
+
+def ops_goldens():
+    for name, (cmds, nlev) in OPS.items():
+        with tempfile.TemporaryDirectory() as d:
+            write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+            zoom = 'centre 25 25 25\nselect_cube 10\nzoom_grid_with_origin_at 8 8 8 2 32\n' if nlev == 2 else ''
+            body = (MOD_BASE + zoom + '\n'.join(cmds) + '\ndone\n' +
+                    ''.join('dump_grid %d\n' % l for l in range(nlev)))
+            # fix_power must precede the first draw: put it before the grid commands' draw
+            open(os.path.join(d, 'paramfile.txt'), 'w').write(body)
+            subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True)
+            grids = {'delta%d' % l: np.load(os.path.join(d, 'grid-%d.npy' % l)) for l in range(nlev)}
+            np.savez_compressed(os.path.join(HERE, '%s.npz' % name), **grids)
+
+
 def main():
     for mode, cmd in (('serial', 'random_seed_serial'), ('parallel', 'random_seed'), ('real', 'random_seed_real_space')):
         with tempfile.TemporaryDirectory() as d:
@@ -224,3 +248,4 @@ if __name__ == '__main__':
     zoom_goldens()
     mod_goldens()
     var_goldens()
+    ops_goldens()

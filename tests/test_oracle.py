@@ -293,3 +293,39 @@ def test_lpt2_oracle_two_plane_waves():
                 (3 / 7) * a * b * -k2 * np.cos(k1 * X) * np.sin(k2 * Y) / K2, 0 * X]
         for p, w in zip(psi2, want):
             assert np.abs(p - w).max() < 1e-15
+
+
+# --- operations on the white noise ----------------------------------------------------
+
+OPS_CASES = {
+    'ops_reverse': ('reverse', None, 1), 'ops_reverse_small_k': ('reverse_small_k', 0.5, 1),
+    'ops_fix_power': ('fix_power', None, 1), 'ops_reverse_small_k_zoom': ('reverse_small_k', 0.7, 2),
+    'ops_fix_power_zoom': ('fix_power', None, 2),
+}
+OPS_LEVELS = {1: [(50.0, 32, (0.0, 0.0, 0.0))], 2: [(50.0, 32, (0.0, 0.0, 0.0)), (25.0, 32, (12.5, 12.5, 12.5))]}
+
+
+def oracle_noise_op(case, cr_log=False):
+    op, param, nlev = OPS_CASES[case]
+    levels = OPS_LEVELS[nlev]
+    fo.set_cr_log(cr_log)
+    w = fo.white_noise_levels([l[1] for l in levels], 8896131, 2)
+    fo.set_cr_log(False)
+    if op == 'reverse':
+        w = [-x for x in w]
+    elif op == 'reverse_small_k':
+        w = [fo.noise_reverse_small_k(x, l[0], param) for x, l in zip(w, levels)]
+    else:
+        w = [fo.noise_unit_modulus(x) for x in w]
+    return levels, w
+
+
+@pytest.mark.parametrize('case', sorted(OPS_CASES))
+def test_noise_op_oracle_matches_reference(bbks, case):
+    from conftest import COSMO
+    g = _load_golden('%s.npz' % case)
+    levels, w = oracle_noise_op(case)
+    out = fo.zoom_realisation(w, levels, fo.CambPower(bbks, COSMO))
+    for l in range(len(levels)):
+        ref = g['delta%d' % l]
+        assert np.abs(out[l][0] - ref).max() <= 1e-12 * np.abs(ref).max(), l
