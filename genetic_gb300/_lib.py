@@ -29,6 +29,10 @@ GIC_MOD_OVERDENSITY = 0
 GIC_MOD_VX = 1
 GIC_MOD_VY = 2
 GIC_MOD_VZ = 3
+GIC_MOD_POTENTIAL = 4
+GIC_MOD_LX = 5
+GIC_MOD_LY = 6
+GIC_MOD_LZ = 7
 
 GIC_FIELD_NOISE = 0
 GIC_FIELD_DELTA = 1

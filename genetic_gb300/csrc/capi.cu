@@ -405,7 +405,7 @@ int gic_chi2(gic_ctx *ctx, double *chi2) {
 }
 
 static gic::ModRequest make_request(gic::Context &C, int kind, const unsigned long long *cells, size_t n) {
-  if (kind < GIC_MOD_OVERDENSITY || kind > GIC_MOD_VZ) gic::fail(GIC_ERR_INVALID_ARG, "unknown modification");
+  if (kind < GIC_MOD_OVERDENSITY || kind > GIC_MOD_LZ) gic::fail(GIC_ERR_INVALID_ARG, "unknown modification");
   if (C.levels.empty()) gic::fail(GIC_ERR_NOT_READY, "no grid levels");
   if (!cells || n == 0)
     gic::fail(GIC_ERR_INVALID_ARG,

@@ -297,6 +297,71 @@ __global__ void k_localise(T *real, int n, const unsigned long long *cells, size
   atomicAdd(at(2 * s[0], 2 * s[1], 2 * s[2]), (T)(-a));
 }
 
+// angular-momentum localisation covector (AngMomentumModification::calculateLocalisationCovector,
+// linearmodification.hpp:333-383): per flagged cell at centroid q, with dq = centre - q
+// (wrapped), coefficients c[dir+2] = dq[dir+1], c[dir+1] = -dq[dir+2], and along each
+// other axis the 4th-order gradient stencil a, b scaled by that coefficient
+template <typename T>
+__global__ void k_localise_am(T *real, int n, const unsigned long long *cells, size_t count, int dir, double dx,
+                              double x0, double y0, double z0, double cx, double cy, double cz, double period,
+                              double a, double b) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  unsigned long long c = cells[i];
+  int pz = (int)(c % n);
+  unsigned long long r = c / n;
+  int py = (int)(r % n), px = (int)(r / n);
+  const int p[3] = {px, py, pz};
+  const double q[3] = {px * dx + x0 + dx / 2, py * dx + y0 + dx / 2, pz * dx + z0 + dx / 2};
+  const double cen[3] = {cx, cy, cz};
+  double dq[3];
+  for (int k = 0; k < 3; ++k) {
+    double v = cen[k] - q[k];
+    if (v > period / 2) v -= period;
+    if (v < -period / 2) v += period;
+    dq[k] = v;
+  }
+  const int d1 = (dir + 1) % 3, d2 = (dir + 2) % 3;
+  double coeff[3];
+  coeff[dir] = 0;
+  coeff[d2] = dq[d1];
+  coeff[d1] = -dq[d2];
+  const size_t rs = (size_t)(2 * (n / 2 + 1));
+  for (int ax = 0; ax < 3; ++ax) {
+    if (ax == dir) continue;
+    auto at = [&](int step) -> T * {
+      int s[3] = {p[0], p[1], p[2]};
+      s[ax] = ((s[ax] + step) % n + n) % n;
+      return real + ((size_t)s[0] * n + s[1]) * rs + s[2];
+    };
+    atomicAdd(at(-2), (T)(coeff[ax] * a));
+    atomicAdd(at(-1), (T)(coeff[ax] * b));
+    atomicAdd(at(1), (T)(-(coeff[ax] * b)));
+    atomicAdd(at(2), (T)(-(coeff[ax] * a)));
+  }
+}
+
+// cosmology::densityToPotential (cosmology/parameters.hpp:209-225): times -prefac / k^2.
+// The reference's guard against k = 0 tests the y component of k, so every mode with
+// ky = 0 is set to zero; that behaviour is kept.
+template <typename T>
+__global__ void k_density_to_potential(typename V2m<T>::type *c, int n, double kmin, double prefac) {
+  const int H = n / 2, S = H + 1;
+  unsigned row = blockIdx.x * kRowsPerBlock + threadIdx.y;
+  int iz = blockIdx.y * kKzChunk + threadIdx.x;
+  if (row >= (unsigned)n * (unsigned)n || iz >= S) return;
+  int ix = (int)(row / (unsigned)n), iy = (int)(row % (unsigned)n);
+  double kx = (double)(ix > H ? ix - n : ix) * kmin, ky = (double)(iy > H ? iy - n : iy) * kmin,
+         kz = (double)iz * kmin;
+  double ksq = kx * kx + ky * ky + kz * kz;
+  double inv = ky == 0.0 ? 0.0 : 1.0 / ksq;
+  size_t id = (size_t)row * S + iz;
+  typename V2m<T>::type v = c[id];
+  v.x = (T)(-prefac * (double)v.x * inv);
+  v.y = (T)(-prefac * (double)v.y * inv);
+  c[id] = v;
+}
+
 template <typename T>
 __device__ __forceinline__ void cr_weights(T t, T (&w)[4]) {
   T t2 = t * t, t3 = t2 * t;
@@ -1077,9 +1142,40 @@ struct ModEngine {
     GIC_CUDA(cudaMemcpyAsync(S.cells.ptr, flagged, count * sizeof(unsigned long long), cudaMemcpyHostToDevice,
                              ctx.stream));
     double w = 1.0 / (double)count;
-    double a = -w / 12. / lev(F).dx, b = w * 2. / 3. / lev(F).dx;
-    k_localise<T><<<nblk(count), 256, 0, ctx.stream>>>(ptr(out, F), lev(F).n, S.cells.template as<unsigned long long>(), count,
-                                                      kind == 0 ? 0 : 1, kind == 0 ? 0 : kind - 1, w, a, b);
+    if (kind >= GIC_MOD_LX) {
+      // centre of the flagged cells, wrapped (Grid::getCentreWrapped, grid.hpp:466-494)
+      const Level &Lf = lev(F);
+      const double P = Lf.periodic;
+      auto wrapped = [P](double v) {
+        if (v > P / 2) v -= P;
+        if (v < -P / 2) v += P;
+        return v;
+      };
+      auto centroid = [&](unsigned long long id, int axis) {
+        unsigned long long zz = id % Lf.n, rr = id / Lf.n, yy = rr % Lf.n, xx = rr / Lf.n;
+        unsigned long long ii = axis == 0 ? xx : (axis == 1 ? yy : zz);
+        return (double)ii * Lf.dx + Lf.x0[axis] + Lf.dx / 2;
+      };
+      double cen[3];
+      for (int ax = 0; ax < 3; ++ax) {
+        double p0 = centroid(flagged[0], ax), run = 0.0;
+        for (size_t i = 1; i < count; ++i) run += wrapped(centroid(flagged[i], ax) - p0);
+        run /= (double)count;
+        double v = run + p0;
+        v = std::fmod(v, P);
+        if (v < 0) v += P;
+        cen[ax] = v;
+      }
+      const double norm = (double)count * Lf.dx;
+      k_localise_am<T><<<nblk(count), 256, 0, ctx.stream>>>(ptr(out, F), Lf.n, S.cells.template as<unsigned long long>(),
+                                                           count, kind - GIC_MOD_LX, Lf.dx, Lf.x0[0], Lf.x0[1], Lf.x0[2],
+                                                           cen[0], cen[1], cen[2], P, 1. / 12. / norm, -2. / 3. / norm);
+    } else {
+      const bool vel = kind >= GIC_MOD_VX && kind <= GIC_MOD_VZ;
+      double a = -w / 12. / lev(F).dx, b = w * 2. / 3. / lev(F).dx;
+      k_localise<T><<<nblk(count), 256, 0, ctx.stream>>>(ptr(out, F), lev(F).n, S.cells.template as<unsigned long long>(),
+                                                        count, vel ? 1 : 0, vel ? kind - GIC_MOD_VX : 0, w, a, b);
+    }
     launched();
     // the reference transforms the localisation covector to Fourier space and back
     // before deinterpolating; that round trip is the identity and is skipped
@@ -1101,9 +1197,17 @@ struct ModEngine {
       sp.power = 1;
       sp.scalar = 1.0;
       sp.sqrtp = lev(l).sqrtp_dm.template as<double>();
-      sp.vel = kind == 0 ? 0.0 : velocity_ratio();
+      const bool velocity_like = (kind >= GIC_MOD_VX && kind <= GIC_MOD_VZ) || kind >= GIC_MOD_LX;
+      sp.vel = velocity_like ? velocity_ratio() : 0.0;
       table(sp, l);
       mul_table(ptr(out, l), l);
+      if (kind == GIC_MOD_POTENTIAL) {
+        // 3/2 Om0 / a (H0/h)^2 / c^2 in (h/Mpc)^2 (cosmology/parameters.hpp:213-216)
+        const double prefac = 3. / 2. * ctx.cosmo.om / ctx.cosmo.a * 100. * 100. / (299792.) / (299792.);
+        k_density_to_potential<T><<<hs_grid(lev(l).n), hs_block(), 0, ctx.stream>>>(reinterpret_cast<C *>(ptr(out, l)),
+                                                                                     lev(l).n, lev(l).kmin(), prefac);
+        launched();
+      }
     }
   }
   double velocity_ratio();

@@ -189,13 +189,26 @@ class ICGenerator:
         r2 = float(np.float32(radius) * np.float32(radius))
         self._select(lambda X, Y, Z: X * X + Y * Y + Z * Z < r2)
 
+    def select_ellipse(self, a, b, c):
+        """ICGenerator::selectEllipse (ic.hpp:1503-1513): semi-axes parsed as floats."""
+        a2, b2, c2 = (float(np.float32(v) * np.float32(v)) for v in (a, b, c))
+        self._select(lambda X, Y, Z: X * X / a2 + Y * Y / b2 + Z * Z / c2 < 1.)
+
     def select_cube(self, side):
         h = float(np.float32(side) / np.float32(2))
         self._select(lambda X, Y, Z: (np.abs(X) < h) & (np.abs(Y) < h) & (np.abs(Z) < h))
 
     # -- modifications (modificationmanager.hpp) ---------------------------------------
+    # names as ModificationManager matches them, case-insensitively (modificationmanager.hpp:160-192)
     _KINDS = {'overdensity': _lib.GIC_MOD_OVERDENSITY, 'vx': _lib.GIC_MOD_VX, 'vy': _lib.GIC_MOD_VY,
-              'vz': _lib.GIC_MOD_VZ}
+              'vz': _lib.GIC_MOD_VZ, 'potential': _lib.GIC_MOD_POTENTIAL, 'lx': _lib.GIC_MOD_LX, 'ly': _lib.GIC_MOD_LY,
+              'lz': _lib.GIC_MOD_LZ}
+
+    def _kind(self, name):
+        try:
+            return self._KINDS[name.lower()]
+        except KeyError:
+            raise ValueError('%s is an unknown modification name' % name) from None
 
     def _cells(self):
         if self.flagged is None or len(self.flagged) == 0:
@@ -229,7 +242,7 @@ class ICGenerator:
             self._call('gic_calculate_variance', ptrs, counts, self.variance_filterscale, ctypes.byref(v))
             return v.value
         cells, n = self._cells()
-        self._call('gic_calculate', self._KINDS[name], cells, n, ctypes.byref(v))
+        self._call('gic_calculate', self._kind(name), cells, n, ctypes.byref(v))
         return v.value
 
     def modify(self, name, kind, target):
@@ -242,7 +255,7 @@ class ICGenerator:
                        float(np.float32(target)), rel, self.initial_number_steps, self.precision_target)
         else:
             cells, n = self._cells()
-            self._call('gic_add_modification', self._KINDS[name], cells, n, float(np.float32(target)), rel)
+            self._call('gic_add_modification', self._kind(name), cells, n, float(np.float32(target)), rel)
         self._nmods = getattr(self, '_nmods', 0) + 1
 
     def clear_modifications(self):
@@ -341,7 +354,8 @@ _COMMANDS = {
     'random_seed_serial': 'random_seed_serial', 'seedfourier': 'random_seed_serial',
     'random_seed_real_space': 'random_seed_real_space', 'seed': 'random_seed_real_space',
     'seedfourier_reverse': 'seedfourier_reverse', 'done': 'done', 'chi2': 'chi2',
-    'centre': 'centre', 'select_sphere': 'select_sphere', 'select_cube': 'select_cube',
+    'centre': 'centre', 'center': 'centre', 'select_sphere': 'select_sphere', 'select_cube': 'select_cube',
+    'select_ellipse': 'select_ellipse',
     'calculate': 'calculate', 'modify': 'modify', 'clear_modifications': 'clear_modifications',
     'filtering_scale': 'filtering_scale', 'fix_power': 'fix_power',
     'exact_power_spectrum_enforcement': 'fix_power', 'reverse': 'reverse', 'reverse_small_k': 'reverse_small_k',

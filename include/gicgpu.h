@@ -160,6 +160,10 @@ GIC_API int gic_chi2(gic_ctx *ctx, double *chi2);
 #define GIC_MOD_VX 1
 #define GIC_MOD_VY 2
 #define GIC_MOD_VZ 3
+#define GIC_MOD_POTENTIAL 4 /* PotentialModification (linearmodification.hpp:146-169) */
+#define GIC_MOD_LX 5        /* AngMomentumModification (linearmodification.hpp:300-412), x, y, z */
+#define GIC_MOD_LY 6
+#define GIC_MOD_LZ 7
 
 /* Current value <a|w> of a modification's quantity (mean overdensity, or mean
  * velocity component, over `cells`, the flagged cells of the finest level as

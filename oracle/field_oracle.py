@@ -562,6 +562,9 @@ def flag_cells(levels, l, centre, kind, size):
     if kind == 'sphere':
         r2 = float(np.float32(size) * np.float32(size))
         sel = X * X + Y * Y + Z * Z < r2
+    elif kind == 'ellipse':
+        a2, b2, c2 = (float(np.float32(v) * np.float32(v)) for v in size)
+        sel = X * X / a2 + Y * Y / b2 + Z * Z / c2 < 1.
     else:
         h = float(np.float32(size) / np.float32(2))
         sel = (np.abs(X) < h) & (np.abs(Y) < h) & (np.abs(Z) < h)
@@ -589,6 +592,73 @@ def localisation_covector(levels, flagged, kind, direction=0):
     np.add.at(out, idx(1), -b)
     np.add.at(out, idx(2), -a)
     return out.reshape(n, n, n)
+
+
+def flagged_centre(levels, flagged):
+    """Grid::getCentreWrapped (grid.hpp:466-494) on the finest level: the mean of the
+    wrapped offsets from the first cell, added back and wrapped."""
+    box, n, off = levels.levels[-1]
+    L = levels.periodic
+    dx = box / n
+    coords = np.array(np.unravel_index(np.asarray(flagged, dtype=np.int64), (n, n, n)), dtype=np.float64)
+    cen = []
+    for a in range(3):
+        c = coords[a] * dx + off[a] + dx / 2
+        d = c[1:] - c[0]
+        d = np.where(d > L / 2, d - L, np.where(d < -L / 2, d + L, d))
+        run = 0.0
+        for v in d:  # the reference's running sum, in order
+            run += v
+        v = run / len(c) + c[0]
+        cen.append(np.fmod(v, L) + (L if np.fmod(v, L) < 0 else 0))
+    return np.array(cen)
+
+
+def localisation_covector_am(levels, flagged, direction):
+    """AngMomentumModification::calculateLocalisationCovector (linearmodification.hpp:333-383)."""
+    box, n, off = levels.levels[-1]
+    L = levels.periodic
+    dx = box / n
+    cen = flagged_centre(levels, flagged)
+    norm = len(flagged) * dx
+    a, b = 1. / 12. / norm, -2. / 3. / norm
+    out = np.zeros(n ** 3)
+    coords = np.array(np.unravel_index(np.asarray(flagged, dtype=np.int64), (n, n, n)))
+    q = coords * dx + np.array(off)[:, None] + dx / 2
+    dq = cen[:, None] - q
+    dq = np.where(dq > L / 2, dq - L, np.where(dq < -L / 2, dq + L, dq))
+    d1, d2 = (direction + 1) % 3, (direction + 2) % 3
+    coeff = np.zeros_like(dq)
+    coeff[d2] = dq[d1]
+    coeff[d1] = -dq[d2]
+    for ax in range(3):
+        if ax == direction:
+            continue
+        def idx(step):
+            c = coords.copy()
+            c[ax] = (c[ax] + step) % n
+            return np.ravel_multi_index(c, (n, n, n))
+        np.add.at(out, idx(-2), coeff[ax] * a)
+        np.add.at(out, idx(-1), coeff[ax] * b)
+        np.add.at(out, idx(1), -coeff[ax] * b)
+        np.add.at(out, idx(2), -coeff[ax] * a)
+    return out.reshape(n, n, n)
+
+
+def density_to_potential(field_k, box, cosmo):
+    """cosmology::densityToPotential (cosmology/parameters.hpp:209-225), including its
+    k = 0 guard that tests the y component, so modes with ky = 0 become zero."""
+    n = field_k.shape[0]
+    ki, kz, kmin = kgrid(n, box)
+    kx = (ki * kmin)[:, None, None]
+    ky = (ki * kmin)[None, :, None]
+    kzz = (kz * kmin)[None, None, :]
+    ksq = kx * kx + ky * ky + kzz * kzz
+    a = 1.0 / (cosmo['redshift'] + 1.0)
+    prefac = 3. / 2. * cosmo['omega_m'] / a * 100. * 100. / (299792.) / (299792.)
+    with np.errstate(divide='ignore'):
+        inv = np.where(ky == 0.0, 0.0, 1.0 / ksq)
+    return -prefac * field_k * inv
 
 
 def _axis_geometry(levels, fine, coarse, axis):
@@ -641,10 +711,12 @@ def _kmag_level(levels, l):
     return kmag(n, box)
 
 
-def multilevel_covector(levels, hires_real, power_dm, velocity_scale=None):
+def multilevel_covector(levels, hires_real, power_dm, velocity_scale=None, potential_cosmo=None):
     """ConstraintField of a modification in Fourier space on every level
     (multilevelgrid.hpp:245-321, linearmodification.hpp:64-75, 134-141, 242-297).
-    velocity_scale: None for an overdensity, else the velocity-to-offset ratio."""
+    velocity_scale: None for an overdensity, else the velocity-to-offset ratio
+    (velocity and angular-momentum modifications); potential_cosmo: the cosmology of
+    a potential modification (linearmodification.hpp:160-167)."""
     nl = len(levels)
     real = [None] * nl
     real[-1] = fft_c2r(fft_r2c(hires_real))
@@ -664,6 +736,8 @@ def multilevel_covector(levels, hires_real, power_dm, velocity_scale=None):
                 v = -velocity_scale * f / kk
             v[0, 0, 0] = 0
             f = v
+        if potential_cosmo is not None:
+            f = density_to_potential(f, box, potential_cosmo)
         out.append(f)
     return out
 

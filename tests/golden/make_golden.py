@@ -228,6 +228,58 @@ def ops_goldens():
             np.savez_compressed(os.path.join(HERE, '%s.npz' % name), **grids)
 
 
+MODS_MORE = {
+    # potential and angular momentum, one level and a factor-2 zoom
+    'mod_pot1': ("""centre 25 25 25
+select_sphere 5
+calculate potential
+modify potential relative 2
+done
+dump_grid 0
+""", 1),
+    'mod_am1': ("""centre 25 25 25
+select_ellipse 10 7.5 5
+calculate Ly
+calculate Lz
+modify Ly absolute 100
+modify Lz relative 0.5
+done
+dump_grid 0
+""", 1),
+    'mod_am2': ("""centre 25 25 25
+select_cube 10
+zoom_grid_with_origin_at 8 8 8 2 32
+center 25.3 24.8 25
+select_sphere 4
+calculate Lx
+calculate potential
+modify Lx absolute 50
+modify potential absolute 0
+done
+dump_grid 0
+dump_grid 1
+""", 2),
+}
+
+
+def mod_more_goldens():
+    import re
+    for name, (tail, nlev) in MODS_MORE.items():
+        with tempfile.TemporaryDirectory() as d:
+            write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+            open(os.path.join(d, 'paramfile.txt'), 'w').write(MOD_BASE + tail)
+            r = subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True, text=True)
+            log = r.stdout + r.stderr
+            vals = {}
+            for key in ('potential', 'Lx', 'Ly', 'Lz'):
+                m = re.search(r'%s: calculated value = (\S+)' % key, log)
+                if m:
+                    vals[key] = float(m.group(1))
+            vals['delta_chi2'] = float(re.search(r'Modification Delta chi\^2 = (\S+)', log).group(1))
+            grids = {'delta%d' % l: np.load(os.path.join(d, 'grid-%d.npy' % l)) for l in range(nlev)}
+            np.savez_compressed(os.path.join(HERE, '%s.npz' % name), **grids, **{k: np.array(v) for k, v in vals.items()})
+
+
 def main():
     for mode, cmd in (('serial', 'random_seed_serial'), ('parallel', 'random_seed'), ('real', 'random_seed_real_space')):
         with tempfile.TemporaryDirectory() as d:
@@ -249,3 +301,4 @@ if __name__ == '__main__':
     mod_goldens()
     var_goldens()
     ops_goldens()
+    mod_more_goldens()

@@ -329,3 +329,62 @@ def test_noise_op_oracle_matches_reference(bbks, case):
     for l in range(len(levels)):
         ref = g['delta%d' % l]
         assert np.abs(out[l][0] - ref).max() <= 1e-12 * np.abs(ref).max(), l
+
+
+# --- potential and angular-momentum modifications ----------------------------------------
+
+MOD_MORE_CASES = {
+    'mod_pot1': dict(levels=[(50.0, 32, (0.0, 0.0, 0.0))], centre=(25., 25., 25.), select=('sphere', 5),
+                     calc=['potential'], mods=[('potential', 'relative', 2.0)]),
+    'mod_am1': dict(levels=[(50.0, 32, (0.0, 0.0, 0.0))], centre=(25., 25., 25.), select=('ellipse', (10, 7.5, 5)),
+                    calc=['Ly', 'Lz'], mods=[('Ly', 'absolute', 100.0), ('Lz', 'relative', 0.5)]),
+    'mod_am2': dict(levels=[(50.0, 32, (0.0, 0.0, 0.0)), (25.0, 32, (12.5, 12.5, 12.5))], centre=(25.3, 24.8, 25.),
+                    select=('sphere', 4), calc=['Lx', 'potential'],
+                    mods=[('Lx', 'absolute', 50.0), ('potential', 'absolute', 0.0)]),
+}
+
+
+def oracle_mod_more(bbks, case, cr_log=False):
+    from conftest import COSMO
+    c = MOD_MORE_CASES[case]
+    L = fo.Levels(c['levels'])
+    fo.set_cr_log(cr_log)
+    w = fo.white_noise_levels([l[1] for l in c['levels']], 8896131, 2)
+    fo.set_cr_log(False)
+    p_dm = fo.CambPower(bbks, COSMO, column=1)
+    vs = fo.velocity_to_offset_ratio(COSMO)
+    flagged = fo.flag_cells(L, len(c['levels']) - 1, c['centre'], *c['select'])
+
+    def covector(name):
+        if name == 'potential':
+            loc = fo.localisation_covector(L, flagged, 'overdensity')
+            return fo.multilevel_covector(L, loc, p_dm, None, potential_cosmo=COSMO)
+        d = {'Lx': 0, 'Ly': 1, 'Lz': 2}[name]
+        return fo.multilevel_covector(L, fo.localisation_covector_am(L, flagged, d), p_dm, vs)
+
+    values = {name: fo.inner(covector(name), w) for name in c['calc']}
+    covs, targets = [], []
+    for name, kind, t in c['mods']:
+        cv = covector(name)
+        t32 = float(np.float32(t))
+        targets.append(t32 * fo.inner(cv, w) if kind == 'relative' else t32)
+        covs.append(cv)
+    before = fo.chi2_levels(L, w)
+    w2 = fo.apply_linear_modifications(L, w, covs, targets)
+    after = fo.chi2_levels(L, w2)
+    return dict(levels=L, noise=w, modified=w2, values=values, chi2=(before, after), flagged=flagged)
+
+
+@pytest.mark.parametrize('case', sorted(MOD_MORE_CASES))
+def test_potential_and_angular_momentum_oracle(bbks, case):
+    from conftest import COSMO
+    g = _load_golden('%s.npz' % case)
+    r = oracle_mod_more(bbks, case)
+    for name, v in r['values'].items():
+        assert '%.6g' % v == '%.6g' % float(g[name]), name
+    assert '%.6g' % (r['chi2'][1] - r['chi2'][0]) == '%.6g' % float(g['delta_chi2'])
+    levels = MOD_MORE_CASES[case]['levels']
+    out = fo.zoom_realisation(r['modified'], levels, fo.CambPower(bbks, COSMO))
+    for l in range(len(levels)):
+        ref = g['delta%d' % l]
+        assert np.abs(out[l][0] - ref).max() <= 1e-11 * np.abs(ref).max(), l
