@@ -473,6 +473,28 @@ static gic::QuadRequest make_quad_request(gic::Context &C, const unsigned long l
   return q;
 }
 
+int gic_splice(gic_ctx *ctx, unsigned long new_seed, const unsigned long long *const *cells, const size_t *counts,
+               int *iterations) {
+  API_BEGIN(ctx)
+  if (C.levels.empty()) gic::fail(GIC_ERR_NOT_READY, "no grid levels");
+  for (auto &L : C.levels)
+    if (!L->have_noise) gic::fail(GIC_ERR_NOT_READY, "white noise has not been drawn");
+  if (!C.transfer.ready) gic::fail(GIC_ERR_NOT_READY, "no transfer function");
+  if (!cells || !counts) gic::fail(GIC_ERR_INVALID_ARG, "null cell lists");
+  std::vector<std::vector<unsigned long long>> lists;
+  for (size_t l = 0; l < C.levels.size(); ++l) {
+    if (counts[l] && !cells[l]) gic::fail(GIC_ERR_INVALID_ARG, "null cell list");
+    std::vector<unsigned long long> v(cells[l], cells[l] + counts[l]);
+    for (auto c : v)
+      if (c >= C.levels[l]->ncells()) gic::fail(GIC_ERR_INVALID_ARG, "flagged cell outside its grid");
+    lists.push_back(std::move(v));
+  }
+  std::vector<int> its = gic::splice(C, new_seed, lists);
+  if (iterations)
+    for (size_t l = 0; l < its.size(); ++l) iterations[l] = its[l];
+  API_END
+}
+
 int gic_calculate_variance(gic_ctx *ctx, const unsigned long long *const *cells, const size_t *counts,
                            double filterscale, double *value) {
   API_BEGIN(ctx)

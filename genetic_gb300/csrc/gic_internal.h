@@ -203,6 +203,10 @@ void lpt2_fields(Context &ctx);
 // tab_main of level li (sqrt(P) times its high-pass) and the low-pass tables of a coarse level
 void level_tables(Context &ctx, int li);
 void noise_op(Context &ctx, int op, double param);
+void preconditioner_table(Context &ctx, const Level &L, double power, DevBuf &out);
+// splice every level's noise with a new real-space draw of new_seed (flagged cells
+// per level keep the new field); returns the CG iterations per level
+std::vector<int> splice(Context &ctx, unsigned long long new_seed, const std::vector<std::vector<unsigned long long>> &cells);
 void lowpass_tables(Context &ctx, int coarse_index);
 
 // zoom.cu

@@ -95,8 +95,11 @@ __global__ void k_sigma8_terms(const double *ks, const int *count, double ns, do
   if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
 }
 
+// P_grid^power by q (applyTransferFunction, field.hpp:394-412: cov^power where cov != 0);
+// fundamental_one: the k = 0 value set to 1 first, as spliceOneLevel's preconditioner
 __global__ void k_sqrtp_table(double *tab, long long nq, double kmin, double amplitude, double ns, double norm,
-                              const double *lx, const double *ly, const double *c, int n) {
+                              const double *lx, const double *ly, const double *c, int n, double power = 0.5,
+                              int fundamental_one = 0) {
   long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nq) return;
   double k = sqrt((double)q) * kmin;
@@ -106,7 +109,8 @@ __global__ void k_sqrtp_table(double *tab, long long nq, double kmin, double amp
     p = amplitude * pow(k, ns) * t * t;
   }
   double spec = p * norm;
-  if (spec != 0.0) spec = pow(spec, 0.5);
+  if (q == 0 && fundamental_one) spec = 1.0;
+  if (spec != 0.0 && power != 1.0) spec = pow(spec, power);
   tab[q] = spec;
 }
 
@@ -619,6 +623,19 @@ void noise_op(Context &ctx, int op, double param) {
 }
 
 void level_tables(Context &ctx, int li) { build_level_tables(ctx, li); }
+
+// P_grid^power of a level ("all" transfer column), k = 0 set to 1 first (splicing)
+void preconditioner_table(Context &ctx, const Level &L, double power, DevBuf &out) {
+  if (!ctx.transfer.ready) fail(GIC_ERR_NOT_READY, "no transfer function");
+  long long half = L.n / 2, nq = 3 * half * half + 1;
+  out.ensure(nq * sizeof(double));
+  double kw = 2. * M_PI / L.box;
+  double norm = kw * kw * kw / pow(2.f * M_PI, 3.f) * (double)L.ncells();
+  k_sqrtp_table<<<(unsigned)((nq + 255) / 256), 256, 0, ctx.stream>>>(
+      out.as<double>(), nq, L.kmin(), ctx.transfer.amplitude, ctx.cosmo.ns, norm, ctx.transfer.lnk.as<double>(),
+      ctx.transfer.lnT_all.as<double>(), ctx.transfer.c_all.as<double>(), ctx.transfer.nrows, power, 1);
+  launched();
+}
 void lowpass_tables(Context &ctx, int coarse_index) { build_lowpass_tables(ctx, coarse_index); }
 
 void za_fields(Context &ctx, int li) {

@@ -219,6 +219,37 @@ __global__ void k_inner(const T *a, const T *b, int n, double *partial) {
   if (tid == 0) partial[blockIdx.x] = red[0];
 }
 
+// partial dot products of two flat arrays (grid-stride, one value per block)
+template <typename T>
+__global__ void k_dot_flat(const T *a, const T *b, size_t n, double *partial) {
+  __shared__ double red[256];
+  double acc = 0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    acc += (double)a[i] * (double)b[i];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+// the tail of genetIC's real-space buffer after an inverse transform: padded positions
+// [n^3, n^2 (n + 2)) of the c2r output -- the last rows' values, and their padding
+// slots (the kz = n/2 coefficient after the x and y passes, which this library's c2r
+// leaves unscaled) -- divided by n^1.5 (fourier.hpp:388-404, 479-518)
+template <typename T>
+__global__ void k_extract_tail(const T *padded, T *tail, int n, T scale) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t n3 = (size_t)n * n * n, len = (size_t)n * n * (n + 2) - n3;
+  if (t >= len) return;
+  size_t p = n3 + t;
+  T v = padded[p];
+  if ((int)(p % (size_t)(n + 2)) >= n) v *= scale;
+  tail[t] = v;
+}
+
 // sums of consecutive runs of n doubles in a fixed order, one block per run
 __global__ void k_sum(const double *in, int n, double *out) {
   __shared__ double red[256];
@@ -250,6 +281,13 @@ __global__ void k_scatter_cells(const T *in, int n, const unsigned long long *ce
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < count) real[padded_index(cells[i], n)] = in[i];
 }
+// zero the flagged cells of a padded real field
+template <typename T>
+__global__ void k_zero_cells(T *real, int n, const unsigned long long *cells, size_t count) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) real[padded_index(cells[i], n)] = (T)0;
+}
+
 // the variance operator on the flagged values: v = (v - mean) / count, the mean
 // summed in double in one block (quadraticmodification.hpp:199-218)
 template <typename T>
@@ -617,11 +655,14 @@ struct ModEngine {
     launched();
   }
 
-  // one term of an inner product: two half spectra, or two padded real fields, of level l
+  // one term of an inner product: two half spectra or two padded real fields of level
+  // l, or two flat arrays of `count` values
+  enum TermKind { kFourier = 0, kReal = 1, kFlat = 2 };
   struct Term {
     const T *a, *b;
     int l;
-    bool real;
+    int kind;
+    size_t count = 0;
   };
   // sum of each group's terms; every group has the same number of terms, and all
   // groups are read back together
@@ -636,8 +677,10 @@ struct ModEngine {
       for (int i = 0; i < nt; ++i) {
         const Term &t = groups[p][i];
         double *dst = part + per * p + (size_t)i * blocks;
-        if (t.real)
+        if (t.kind == kReal)
           k_inner_real<T><<<blocks, hs_block(), 0, ctx.stream>>>(t.a, t.b, lev(t.l).n, dst);
+        else if (t.kind == kFlat)
+          k_dot_flat<T><<<blocks, 256, 0, ctx.stream>>>(t.a, t.b, t.count, dst);
         else
           k_inner<T><<<blocks, hs_block(), 0, ctx.stream>>>(t.a, t.b, lev(t.l).n, dst);
         launched();
@@ -657,7 +700,7 @@ struct ModEngine {
       for (int l = 0; l < nl(); ++l) {
         to_fourier(*pr.first, l);
         to_fourier(*pr.second, l);
-        g.push_back({ptr(*pr.first, l), ptr(*pr.second, l), l, false});
+        g.push_back({ptr(*pr.first, l), ptr(*pr.second, l), l, kFourier});
       }
       groups.push_back(std::move(g));
     }
@@ -865,7 +908,7 @@ struct ModEngine {
         to_real(R->template as<T>(), t);
         GIC_CUDA(cudaMemcpyAsync(xr->ptr, R->ptr, bytes, cudaMemcpyDeviceToDevice, ctx.stream));
         windowed_covector_real(X, t, R->template as<T>());
-        terms.push_back({R->template as<T>(), xr->template as<T>(), t, true});
+        terms.push_back({R->template as<T>(), xr->template as<T>(), t, kReal});
         keep.push_back(std::move(R));
         keep.push_back(std::move(xr));
       } else {
@@ -882,7 +925,7 @@ struct ModEngine {
           to_fourier(Cr, t);
           axpy(r, Cr, 1.0, t);
         }
-        terms.push_back({r, ptr(X, t), t, false});
+        terms.push_back({r, ptr(X, t), t, kFourier});
         keep.push_back(std::move(R));
       }
     }
@@ -1131,6 +1174,162 @@ struct ModEngine {
     unpad_to(b->template as<T>(), out, l);
     GIC_CUDA(cudaStreamSynchronize(ctx.stream));
     ctx.pool.give(std::move(b));
+  }
+
+  // --- splicing (splice.hpp:37-118, tools/numerics/cg.hpp:13-59) -------------------
+  // genetIC holds a real field compact at the front of the padded transform buffer; its
+  // +=, -=, addScaled, negation and innerProduct run over the whole buffer, the mask
+  // multiply over the n^3 values only.  The CG's scalars therefore include the
+  // buffer's tail, the part of the last inverse transform's padded output that the
+  // compaction did not overwrite.  A Stored field carries that tail (2 n^2 values)
+  // beside the padded field, so the iterations follow the reference's.
+  struct Stored {
+    std::unique_ptr<DevBuf> buf, tail;
+  };
+  size_t tail_len(int l) {
+    const size_t n = lev(l).n;
+    return n * n * (n + 2) - n * n * n;
+  }
+  void take(Stored &s, int l) {
+    s.buf = ctx.pool.take(elems(l) * sizeof(T));
+    s.tail = ctx.pool.take(tail_len(l) * sizeof(T));
+  }
+  void give(Stored &s) {
+    ctx.pool.give(std::move(s.buf));
+    ctx.pool.give(std::move(s.tail));
+  }
+  T *sb(Stored &s) { return s.buf->template as<T>(); }
+  T *st(Stored &s) { return s.tail->template as<T>(); }
+  void copy_stored(Stored &dst, Stored &src, int l) {
+    GIC_CUDA(cudaMemcpyAsync(dst.buf->ptr, src.buf->ptr, elems(l) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
+    GIC_CUDA(cudaMemcpyAsync(dst.tail->ptr, src.tail->ptr, tail_len(l) * sizeof(T), cudaMemcpyDeviceToDevice,
+                             ctx.stream));
+  }
+  void extract_tail(Stored &s, int l) {
+    k_extract_tail<T><<<nblk(tail_len(l)), 256, 0, ctx.stream>>>(sb(s), st(s), lev(l).n, (T)scale(l));
+    launched();
+  }
+  void axpy_stored(Stored &a, Stored &b, double c, int l) {
+    axpy(sb(a), sb(b), c, l);
+    k_axpy<T><<<nblk(tail_len(l)), 256, 0, ctx.stream>>>(st(a), st(b), c, tail_len(l));
+    launched();
+  }
+  void scale_stored(Stored &a, double c, int l) {
+    scale_by(sb(a), c, l);
+    k_scale<T><<<nblk(tail_len(l)), 256, 0, ctx.stream>>>(st(a), c, tail_len(l));
+    launched();
+  }
+  // <a|b> and <c|d> over the whole buffers, read back together
+  std::vector<double> dots(Stored &a, Stored &b, Stored &c, Stored &d, int l) {
+    return inner_groups({{{sb(a), sb(b), l, kReal}, {st(a), st(b), l, kFlat, tail_len(l)}},
+                         {{sb(c), sb(d), l, kReal}, {st(c), st(d), l, kFlat, tail_len(l)}}});
+  }
+  // real field -> R2C -> times tab -> C2R (Field::applyTransferFunction between transforms)
+  void apply_precond(T *buf, int l, const double *tab) {
+    to_fourier(buf, l);
+    fft_c2r_3d<T>(ctx, buf, lev(l).n, scale(l), tab);
+  }
+  void zero_cells(T *buf, int l, const unsigned long long *cells, size_t count) {
+    if (!count) return;
+    k_zero_cells<T><<<nblk(count), 256, 0, ctx.stream>>>(buf, lev(l).n, cells, count);
+    launched();
+  }
+  void keep_cells(T *buf, int l, const unsigned long long *cells, size_t count) {
+    T *v = nullptr;
+    if (count) {
+      S.compact.ensure(count * sizeof(T));
+      v = S.compact.template as<T>();
+      k_gather_cells<T><<<nblk(count), 256, 0, ctx.stream>>>(buf, lev(l).n, cells, count, v);
+      launched();
+    }
+    GIC_CUDA(cudaMemsetAsync(buf, 0, elems(l) * sizeof(T), ctx.stream));
+    if (count) {
+      k_scatter_cells<T><<<nblk(count), 256, 0, ctx.stream>>>(v, lev(l).n, cells, count, buf);
+      launched();
+    }
+  }
+
+  // spliceOneLevel(a = new, b = original): Fourier in (a_k, b_k), Fourier out (into out_k)
+  int splice_level(int l, const T *a_k, const T *b_k, T *out_k, const unsigned long long *cells, size_t count) {
+    const size_t bytes = elems(l) * sizeof(T);
+    DevBuf half, minus1, mhalf;
+    preconditioner_table(ctx, lev(l), 0.5, half);
+    preconditioner_table(ctx, lev(l), -1.0, minus1);
+    preconditioner_table(ctx, lev(l), -0.5, mhalf);
+    const double *h = half.template as<double>(), *m1 = minus1.template as<double>();
+    Stored dd, z, r, d, x, qd;
+    for (Stored *s : {&dd, &z, &r, &d, &x, &qd}) take(*s, l);
+    // delta_diff = C^1/2 (b - a), real
+    GIC_CUDA(cudaMemcpyAsync(sb(dd), b_k, bytes, cudaMemcpyDeviceToDevice, ctx.stream));
+    axpy(sb(dd), a_k, -1.0, l);
+    fft_c2r_3d<T>(ctx, sb(dd), lev(l).n, scale(l), h);
+    extract_tail(dd, l);
+    // z = C^1/2 Mc C^-1 M delta_diff
+    GIC_CUDA(cudaMemcpyAsync(sb(z), sb(dd), bytes, cudaMemcpyDeviceToDevice, ctx.stream));
+    keep_cells(sb(z), l, cells, count);
+    apply_precond(sb(z), l, m1);
+    zero_cells(sb(z), l, cells, count);
+    apply_precond(sb(z), l, h);
+    extract_tail(z, l);
+    // X v = C^1/2 Mc C^-1 Mc C^1/2 v
+    auto X = [&](Stored &v, Stored &o) {
+      GIC_CUDA(cudaMemcpyAsync(sb(o), sb(v), bytes, cudaMemcpyDeviceToDevice, ctx.stream));
+      apply_precond(sb(o), l, h);
+      zero_cells(sb(o), l, cells, count);
+      apply_precond(sb(o), l, m1);
+      zero_cells(sb(o), l, cells, count);
+      apply_precond(sb(o), l, h);
+      extract_tail(o, l);
+    };
+    // conjugateGradient(X, z), rtol 1e-6, atol 1e-12
+    copy_stored(r, z, l);
+    copy_stored(d, r, l);
+    scale_stored(d, -1.0, l);
+    GIC_CUDA(cudaMemsetAsync(sb(x), 0, bytes, ctx.stream));
+    GIC_CUDA(cudaMemsetAsync(st(x), 0, tail_len(l) * sizeof(T), ctx.stream));
+    const double scale_b = std::sqrt(dots(z, z, z, z, l)[0]);
+    int it = 0;
+    if (scale_b != 0.0) {
+      const long long n3 = (long long)lev(l).ncells();
+      // the reference stops at n^3 + 1 iterations; a mixed-precision solve that stops
+      // improving (no new smallest residual in 100 iterations) ends early
+      const long long cap = std::min<long long>(n3 + 1, 100000);
+      double best = INFINITY;
+      int since_best = 0;
+      for (it = 0; it < cap; ++it) {
+        X(d, qd);
+        std::vector<double> a = dots(r, d, d, qd, l);
+        const double dqd = a[1], alpha = -a[0] / dqd;
+        axpy_stored(x, d, alpha, l);
+        X(x, r);
+        axpy_stored(r, z, -1.0, l);
+        std::vector<double> b = dots(r, r, r, qd, l);
+        const double norm = std::sqrt(b[0]);
+        if (norm < 1e-6 * scale_b || norm < 1e-12) break;
+        if (norm < best) {
+          best = norm;
+          since_best = 0;
+        } else if (!ctx.dbl() && ++since_best >= 100) {
+          break;
+        }
+        const double beta = b[1] / dqd;
+        scale_stored(d, beta, l);
+        axpy_stored(d, r, -1.0, l);
+      }
+    }
+    // alpha = C^1/2 x; result = Mc alpha + C^1/2 b - M delta_diff, then C^-1/2
+    apply_precond(sb(x), l, h);
+    zero_cells(sb(x), l, cells, count);
+    GIC_CUDA(cudaMemcpyAsync(sb(qd), b_k, bytes, cudaMemcpyDeviceToDevice, ctx.stream));
+    fft_c2r_3d<T>(ctx, sb(qd), lev(l).n, scale(l), h);
+    axpy(sb(x), sb(qd), 1.0, l);
+    keep_cells(sb(dd), l, cells, count);
+    axpy(sb(x), sb(dd), -1.0, l);
+    fft_r2c_3d<T>(ctx, sb(x), lev(l).n, scale(l), mhalf.template as<double>());
+    GIC_CUDA(cudaMemcpyAsync(out_k, sb(x), bytes, cudaMemcpyDeviceToDevice, ctx.stream));
+    GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+    for (Stored *s : {&dd, &z, &r, &d, &x, &qd}) give(*s);
+    return it;
   }
 
   // covector of one modification (kind 0 overdensity, 1..3 velocity x,y,z)
@@ -1489,6 +1688,43 @@ void field_from_noise_adjoint(Context &ctx, int level, int what, const void *gra
 double variance_gradient(Context &ctx, QuadRequest &q, const void *const *noise, void *const *grad, bool exact) {
   return ctx.dbl() ? ModEngine<double>(ctx).variance_grad(q, noise, grad, exact)
                    : ModEngine<float>(ctx).variance_grad(q, noise, grad, exact);
+}
+
+template <typename T>
+static std::vector<int> splice_t(Context &ctx, unsigned long long new_seed,
+                                 const std::vector<std::vector<unsigned long long>> &cells) {
+  ModEngine<T> E(ctx);
+  const int nl = E.nl();
+  // the original noise, then a new real-space draw into the levels (ic.hpp:1658-1688)
+  std::vector<std::unique_ptr<DevBuf>> original(nl);
+  for (int l = 0; l < nl; ++l) {
+    original[l] = ctx.pool.take(E.elems(l) * sizeof(T));
+    GIC_CUDA(cudaMemcpyAsync(original[l]->ptr, E.lev(l).noise.ptr, E.elems(l) * sizeof(T), cudaMemcpyDeviceToDevice,
+                             ctx.stream));
+  }
+  draw_noise_all(ctx, new_seed, GIC_SEED_REAL_SPACE);
+  std::vector<int> its(nl);
+  std::vector<std::unique_ptr<DevBuf>> dcells(nl);
+  for (int l = 0; l < nl; ++l) {
+    const size_t count = cells[l].size();
+    dcells[l] = std::make_unique<DevBuf>();
+    if (count) {
+      dcells[l]->ensure(count * sizeof(unsigned long long));
+      GIC_CUDA(cudaMemcpyAsync(dcells[l]->ptr, cells[l].data(), count * sizeof(unsigned long long),
+                               cudaMemcpyHostToDevice, ctx.stream));
+    }
+    T *noise = E.lev(l).noise.template as<T>();
+    its[l] = E.splice_level(l, noise, original[l]->template as<T>(), noise,
+                            dcells[l]->template as<unsigned long long>(), count);
+    E.lev(l).have_fields = E.lev(l).have_lpt2 = false;
+  }
+  for (auto &b : original) ctx.pool.give(std::move(b));
+  return its;
+}
+
+std::vector<int> splice(Context &ctx, unsigned long long new_seed,
+                        const std::vector<std::vector<unsigned long long>> &cells) {
+  return ctx.dbl() ? splice_t<double>(ctx, new_seed, cells) : splice_t<float>(ctx, new_seed, cells);
 }
 
 void noise_real(Context &ctx, int level, void *out) {

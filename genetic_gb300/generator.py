@@ -287,6 +287,15 @@ class ICGenerator:
 
     exact_power_spectrum_enforcement = fix_power
 
+    def splice(self, new_seed):
+        """ICGenerator::splice (ic.hpp:1658-1688): the flagged cells of every level take a
+        new real-space white-noise draw; returns the CG iterations per level."""
+        self.draw()
+        ptrs, counts = self._level_cells()
+        its = (ctypes.c_int * len(self.levels))()
+        self._call('gic_splice', int(new_seed), ptrs, counts, its)
+        return list(its)
+
     def reverse(self):
         """ICGenerator::reverse (ic.hpp:1652-1655): the white noise changes sign."""
         self.draw()
@@ -359,6 +368,7 @@ _COMMANDS = {
     'calculate': 'calculate', 'modify': 'modify', 'clear_modifications': 'clear_modifications',
     'filtering_scale': 'filtering_scale', 'fix_power': 'fix_power',
     'exact_power_spectrum_enforcement': 'fix_power', 'reverse': 'reverse', 'reverse_small_k': 'reverse_small_k',
+    'splice': 'splice',
     'apply_modifications': 'apply_modifications',
 }
 # output-side commands handled by genetIC's own writers; accepted and ignored here

@@ -178,6 +178,16 @@ GIC_API int gic_add_modification(gic_ctx *ctx, int kind, const unsigned long lon
                                  int relative);
 GIC_API int gic_clear_modifications(gic_ctx *ctx);
 
+/* Splicing: replace the white noise on each level's flagged cells (cells[l], as
+ * for the variance) by a new real-space draw of `new_seed`, keeping the rest as
+ * close to the original as the covariance allows: spliceOneLevel's preconditioned
+ * conjugate-gradient solve per level (modifications/splice.hpp:37-118,
+ * tools/numerics/cg.hpp:13-59, ICGenerator::splice ic.hpp:1658-1688), including the
+ * reference's inner products over its whole transform buffers.  iterations[l]
+ * (optional) receives each level's CG iterations. */
+GIC_API int gic_splice(gic_ctx *ctx, unsigned long new_seed, const unsigned long long *const *cells,
+                       const size_t *counts, int *iterations);
+
 /* Quadratic modification: the variance, over the flagged cells of each level, of
  * the dark-matter overdensity high-passed at `filterscale` (Mpc/h; the filter is
  * 1 - a Fermi low-pass at k = 2 pi / filterscale).  `cells[l]` / `counts[l]` hold

@@ -908,3 +908,122 @@ def apply_quadratic_modification(levels, field_k, lin_vectors, flagged, scale, p
     n_steps = init_steps * int(np.ceil(np.sqrt(achieved / (target * precision))))
     steps = n_steps if n_steps > init_steps else init_steps
     return perform_quadratic_iterations(levels, field_k, lin_vectors, flagged, scale, power_dm, target, steps), steps
+
+
+# --- splicing (modifications/splice.hpp:37-118, tools/numerics/cg.hpp:13-59) -----------------
+
+def power_grid(power, n, box):
+    """P_grid on every stored mode (the covariance genetIC keeps per level, camb.hpp:101-139)."""
+    return sqrt_power_grid(power, n, box) ** 2
+
+
+def apply_transfer(field_k, cov, p):
+    """Field::applyTransferFunction (field.hpp:394-412): times cov^p, cov^p = cov where p = 1,
+    and 0 where cov = 0."""
+    with np.errstate(divide='ignore', invalid='ignore'):
+        t = np.where(cov != 0.0, np.power(cov, p), 0.0) if p != 1.0 else cov
+    return field_k * t
+
+
+def c2r_with_tail(c):
+    """Field::toReal as genetIC stores the result: the n^3 values compact at the front of
+    the padded buffer (fourier.hpp:388-404, 479-518), and behind them the padded c2r
+    output that the compaction did not overwrite -- the last rows' values and their
+    padding slots, which hold the kz = n/2 coefficient after the x and y passes -- all
+    divided by n^1.5.  Returns (real field, tail of 2 n^2 values)."""
+    n = c.shape[0]
+    m = mirror(c)
+    xy = np.fft.ifft(np.fft.ifft(m, axis=0), axis=1) * n * n
+    real = np.fft.irfftn(m, s=(n, n, n), axes=(0, 1, 2)) * n ** 3
+    padded = np.zeros((n, n, n + 2))
+    padded[:, :, :n] = real
+    padded[:, :, n] = xy[:, :, n // 2].real
+    padded[:, :, n + 1] = xy[:, :, n // 2].imag
+    flat = padded.ravel() / n ** 1.5
+    return real / n ** 1.5, flat[n ** 3:].copy()
+
+
+class StoredReal:
+    """A real field as genetIC holds it: values plus the buffer's tail.  Field's +=, -=,
+    addScaled, negation and innerProduct run over the whole buffer (field.hpp:331-383);
+    the mask multiply over the n^3 values only (field.hpp:306-318)."""
+
+    def __init__(self, r, t):
+        self.r, self.t = r, t
+
+    def __add__(self, o):
+        return StoredReal(self.r + o.r, self.t + o.t)
+
+    def __sub__(self, o):
+        return StoredReal(self.r - o.r, self.t - o.t)
+
+    def __neg__(self):
+        return StoredReal(-self.r, -self.t)
+
+    def scaled(self, a):
+        return StoredReal(self.r * a, self.t * a)
+
+    def masked(self, m):
+        return StoredReal(self.r * m, self.t.copy())
+
+    def dot(self, o):
+        return float(np.sum(self.r * o.r) + np.sum(self.t * o.t))
+
+
+def conjugate_gradient(Q, b, rtol=1e-6, atol=1e-12):
+    """tools::numerics::conjugateGradient on StoredReal fields; returns (x, iterations)."""
+    residual = StoredReal(b.r.copy(), b.t.copy())
+    direction = -residual
+    x = StoredReal(np.zeros_like(b.r), np.zeros_like(b.t))
+    scale = np.sqrt(b.dot(b))
+    if scale == 0.0:
+        return x, 0
+    for i in range(b.r.size + 1):
+        q_dir = Q(direction)
+        alpha = -residual.dot(direction) / direction.dot(q_dir)
+        x = x + direction.scaled(alpha)
+        residual = Q(x) - b
+        norm = np.sqrt(residual.dot(residual))
+        if norm < rtol * scale or norm < atol:
+            break
+        beta = residual.dot(q_dir) / direction.dot(q_dir)
+        direction = direction.scaled(beta) - residual
+    return x, i
+
+
+def splice_one_level(a_k, b_k, cov, flagged):
+    """spliceOneLevel(a, b, cov): the field equal to a on the flagged cells and closest
+    to b elsewhere in the C^-1 norm (splice.hpp:37-118); Fourier in, Fourier out; also
+    the CG iterations.  The CG's scalars include the buffers' tails, as in the reference."""
+    n = a_k.shape[0]
+    mask = np.zeros(n ** 3)
+    mask[np.asarray(flagged, dtype=np.int64)] = 1.0
+    mask = mask.reshape(n, n, n)
+    compl = 1.0 - mask
+    pre = cov.copy()
+    pre[0, 0, 0] = 1.0
+
+    def P(f, p):
+        return StoredReal(*c2r_with_tail(apply_transfer(fft_r2c(f.r), pre, p)))
+
+    delta_diff = StoredReal(*c2r_with_tail(apply_transfer(b_k - a_k, pre, 0.5)))
+    z = P(P(delta_diff.masked(mask), -1.0).masked(compl), 0.5)
+
+    def X(v):
+        return P(P(P(v, 0.5).masked(compl), -1.0).masked(compl), 0.5)
+
+    alpha, its = conjugate_gradient(X, z)
+    alpha = P(alpha, 0.5)
+    b_delta = StoredReal(*c2r_with_tail(apply_transfer(b_k, pre, 0.5)))
+    result = alpha.masked(compl) + b_delta - delta_diff.masked(mask)
+    return apply_transfer(fft_r2c(result.r), pre, -0.5), its
+
+
+def splice_levels(levels, original, new, power, flagged):
+    """ICGenerator::splice (ic.hpp:1658-1688) per level: the new field on the flagged cells."""
+    out, its = [], []
+    for (box, n, off), w_old, w_new, fl in zip(levels, original, new, flagged):
+        s, i = splice_one_level(w_new, w_old, power_grid(power, n, box), fl)
+        out.append(s)
+        its.append(i)
+    return out, its

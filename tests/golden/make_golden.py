@@ -280,6 +280,38 @@ def mod_more_goldens():
             np.savez_compressed(os.path.join(HERE, '%s.npz' % name), **grids, **{k: np.array(v) for k, v in vals.items()})
 
 
+SPLICES = {
+    'splice1': ("""centre 25 25 25
+select_sphere 8
+splice 8896132
+done
+dump_grid 0
+""", 1),
+    'splice2': ("""centre 25 25 25
+select_cube 10
+zoom_grid_with_origin_at 8 8 8 2 32
+centre 25 25 25
+select_sphere 5
+splice 8896132
+done
+dump_grid 0
+dump_grid 1
+""", 2),
+}
+
+
+def splice_goldens():
+    import re
+    for name, (tail, nlev) in SPLICES.items():
+        with tempfile.TemporaryDirectory() as d:
+            write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+            open(os.path.join(d, 'paramfile.txt'), 'w').write(MOD_BASE + tail)
+            r = subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True, text=True)
+            its = [int(v) for v in re.findall(r'Conjugate gradient ended after (\d+) iterations', r.stdout + r.stderr)]
+            grids = {'delta%d' % l: np.load(os.path.join(d, 'grid-%d.npy' % l)) for l in range(nlev)}
+            np.savez_compressed(os.path.join(HERE, '%s.npz' % name), **grids, iterations=np.array(its))
+
+
 def main():
     for mode, cmd in (('serial', 'random_seed_serial'), ('parallel', 'random_seed'), ('real', 'random_seed_real_space')):
         with tempfile.TemporaryDirectory() as d:
@@ -302,3 +334,4 @@ if __name__ == '__main__':
     var_goldens()
     ops_goldens()
     mod_more_goldens()
+    splice_goldens()

@@ -137,6 +137,6 @@ def test_paramfile_parser(tmp_path):
     cmds = generator.parse_paramfile(str(p))
     assert [c[1] for c in cmds] == ['Om', 'base_grid', 'random_seed', 'done']
     assert cmds[1][2] == ['50', '32']
-    p.write_text('splice 3\n')
+    p.write_text('supersample 2\n')
     with pytest.raises(ValueError, match='not on the GPU realisation path'):
         generator.parse_paramfile(str(p))

@@ -388,3 +388,53 @@ def test_potential_and_angular_momentum_oracle(bbks, case):
     for l in range(len(levels)):
         ref = g['delta%d' % l]
         assert np.abs(out[l][0] - ref).max() <= 1e-11 * np.abs(ref).max(), l
+
+
+# --- splicing -----------------------------------------------------------------------------
+
+SPLICE_CASES = {
+    'splice1': dict(levels=[(50.0, 32, (0.0, 0.0, 0.0))], select=('sphere', 8)),
+    'splice2': dict(levels=[(50.0, 32, (0.0, 0.0, 0.0)), (25.0, 32, (12.5, 12.5, 12.5))], select=('sphere', 5)),
+}
+
+
+def oracle_splice(bbks, case, cr_log=False):
+    from conftest import COSMO
+    c = SPLICE_CASES[case]
+    L = fo.Levels(c['levels'])
+    fo.set_cr_log(cr_log)
+    w = fo.white_noise_levels([l[1] for l in c['levels']], 8896131, 2)
+    wn = fo.white_noise_levels([l[1] for l in c['levels']], 8896132, 0)
+    fo.set_cr_log(False)
+    fl = [fo.flag_cells(L, l, (25., 25., 25.), *c['select']) for l in range(len(c['levels']))]
+    out, its = fo.splice_levels(L.levels, w, wn, fo.CambPower(bbks, COSMO), fl)
+    return out, its
+
+
+@needs_reference_tests
+def test_splice_oracle_matches_reference_fixture():
+    """test_24_splicing: real-space seed, 16^3, select_sphere 10, splice 8896132."""
+    power = fo.CambPower(_ref_camb(), REF_COSMO)
+    L = fo.Levels([(50.0, 16, (0, 0, 0))])
+    fo.set_cr_log(False)
+    w = fo.white_noise_levels([16], 8896131, 0)
+    wn = fo.white_noise_levels([16], 8896132, 0)
+    fl = [fo.flag_cells(L, 0, (25., 25., 25.), 'sphere', 10)]
+    s, its = fo.splice_levels(L.levels, w, wn, power, fl)
+    assert its == [16]
+    out = fo.zoom_realisation(s, L.levels, power)
+    ref = np.load(os.path.join(REF_TESTS, 'test_24_splicing', 'reference_grid', 'grid-0.npy'))
+    assert np.abs(out[0][0] - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize('case', sorted(SPLICE_CASES))
+def test_splice_oracle_matches_goldens(bbks, case):
+    from conftest import COSMO
+    g = _load_golden('%s.npz' % case)
+    out, its = oracle_splice(bbks, case)
+    assert its == list(g['iterations'])
+    levels = SPLICE_CASES[case]['levels']
+    fields = fo.zoom_realisation(out, levels, fo.CambPower(bbks, COSMO))
+    for l in range(len(levels)):
+        ref = g['delta%d' % l]
+        assert np.abs(fields[l][0] - ref).max() <= 1e-12 * np.abs(ref).max(), l
