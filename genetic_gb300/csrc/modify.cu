@@ -92,6 +92,132 @@ __global__ void k_mul_table(typename V2m<T>::type *c, int n, const double *tab) 
   c[id].y *= s;
 }
 
+// out = tab[q] x (+ add): the metric's level term f^2 X plus its transformed cross terms
+template <typename T>
+__global__ void k_mul_table_add(typename V2m<T>::type *out, const typename V2m<T>::type *x, int n, const double *tab,
+                                const typename V2m<T>::type *add) {
+  const int H = n / 2, S = H + 1;
+  unsigned row = blockIdx.x * kRowsPerBlock + threadIdx.y;
+  int iz = blockIdx.y * kKzChunk + threadIdx.x;
+  if (row >= (unsigned)n * (unsigned)n || iz >= S) return;
+  int ix = (int)(row / (unsigned)n), iy = (int)(row % (unsigned)n);
+  long long kx = ix > H ? ix - n : ix, ky = iy > H ? iy - n : iy;
+  T s = (T)tab[kx * kx + ky * ky + (long long)iz * iz];
+  size_t id = (size_t)row * S + iz;
+  typename V2m<T>::type v = x[id];
+  v.x *= s;
+  v.y *= s;
+  if (add) {
+    v.x += add[id].x;
+    v.y += add[id].y;
+  }
+  out[id] = v;
+}
+
+// a += sum_k c[k] b[k] over n values (up to 8 sources in one pass)
+constexpr int kMaxAxpy = 8;
+template <typename T>
+struct AxpySources {
+  const T *b[kMaxAxpy];
+  double c[kMaxAxpy];
+  int nb;
+};
+template <typename T>
+__global__ void k_axpy_multi(T *a, AxpySources<T> src, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T v = a[i];
+  for (int k = 0; k < src.nb; ++k) v += (T)src.c[k] * src.b[k][i];
+  a[i] = v;
+}
+
+// all products <a_i|b_j> (i < na <= 4, j < nb <= 5) of half spectra in one pass over the
+// fields, Hermitian-weighted; the partial sum of each block for product
+// g = (ia0 + i) nb_total + jb0 + j goes to partial[g * pstride + block]
+constexpr int kBlockA = 4, kBlockB = 5;
+template <typename T>
+struct BlockFields {
+  const T *a[kBlockA];
+  const T *b[kBlockB];
+  int na, nb;
+};
+// per-thread accumulator of Hermitian-weighted products: a compensated float pair for
+// float fields (every product split exactly with fma, as k_inner), a double for double
+template <typename T>
+struct ProdAcc;
+template <>
+struct ProdAcc<float> {
+  float s = 0.f, e = 0.f;
+  __device__ __forceinline__ void add(float ar, float ai, float br, float bi, float w) {
+    float p1 = ar * br, p2 = ai * bi;
+    float e1 = fmaf(ar, br, -p1), e2 = fmaf(ai, bi, -p2);
+    float t = s + w * p1, bb = t - s;
+    e += (s - (t - bb)) + (w * p1 - bb);
+    s = t;
+    t = s + w * p2;
+    bb = t - s;
+    e += (s - (t - bb)) + (w * p2 - bb);
+    s = t;
+    e += w * (e1 + e2);
+  }
+  __device__ __forceinline__ double get() const { return (double)s + (double)e; }
+};
+template <>
+struct ProdAcc<double> {
+  double s = 0;
+  __device__ __forceinline__ void add(double ar, double ai, double br, double bi, double w) {
+    s += w * (ar * br + ai * bi);
+  }
+  __device__ __forceinline__ double get() const { return s; }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_inner_block(BlockFields<T> f, int n, double *partial, int ia0, int jb0,
+                                                     int nb_total, size_t pstride) {
+  __shared__ double red[256];
+  const int H = n / 2, S = H + 1;
+  const unsigned rows = (unsigned)n * (unsigned)n;
+  const int tid = threadIdx.y * kKzChunk + threadIdx.x;
+  double total[kBlockA * kBlockB];
+#pragma unroll
+  for (int p = 0; p < kBlockA * kBlockB; ++p) total[p] = 0;
+  for (int iz = threadIdx.x; iz < S; iz += kKzChunk) {
+    const T w = (iz == 0 || iz == H) ? (T)1 : (T)2;
+    ProdAcc<T> acc[kBlockA * kBlockB];
+    for (unsigned r = blockIdx.x * kRowsPerBlock + threadIdx.y; r < rows; r += gridDim.x * kRowsPerBlock) {
+      const size_t id = 2 * ((size_t)r * S + iz);
+      T br[kBlockB], bi[kBlockB];
+#pragma unroll
+      for (int j = 0; j < kBlockB; ++j)
+        if (j < f.nb) {
+          br[j] = f.b[j][id];
+          bi[j] = f.b[j][id + 1];
+        }
+#pragma unroll
+      for (int i = 0; i < kBlockA; ++i)
+        if (i < f.na) {
+          const T ar = f.a[i][id], ai = f.a[i][id + 1];
+#pragma unroll
+          for (int j = 0; j < kBlockB; ++j)
+            if (j < f.nb) acc[i * kBlockB + j].add(ar, ai, br[j], bi[j], w);
+        }
+    }
+#pragma unroll
+    for (int p = 0; p < kBlockA * kBlockB; ++p) total[p] += acc[p].get();
+  }
+  for (int i = 0; i < f.na; ++i)
+    for (int j = 0; j < f.nb; ++j) {
+      red[tid] = total[i * kBlockB + j];
+      __syncthreads();
+      for (int s2 = 128; s2 > 0; s2 >>= 1) {
+        if (tid < s2) red[tid] += red[tid + s2];
+        __syncthreads();
+      }
+      if (tid == 0) partial[(size_t)((ia0 + i) * nb_total + jb0 + j) * pstride + blockIdx.x] = red[0];
+      __syncthreads();
+    }
+}
+
 // --- elementwise ----------------------------------------------------------------
 
 template <typename T>
@@ -708,6 +834,53 @@ struct ModEngine {
   }
   double inner(Field &a, Field &b) { return inner_many({{&a, &b}})[0]; }
 
+  // M[i][j] = <A_i|B_j> summed over levels (Fourier), each field read once per level
+  // for every 4 x 5 block of products; one read-back for the whole matrix
+  std::vector<double> inner_block(const std::vector<Field *> &A, const std::vector<Field *> &B) {
+    const int blocks = 152 * 4;
+    const int L = nl(), na = (int)A.size(), nbt = (int)B.size(), np = na * nbt;
+    if (np == 0) return {};
+    const size_t pstride = (size_t)L * blocks;
+    S.reduce.ensure((pstride * np + np) * sizeof(double));
+    double *part = S.reduce.template as<double>();
+    for (Field *f : A)
+      for (int l = 0; l < L; ++l) to_fourier(*f, l);
+    for (Field *f : B)
+      for (int l = 0; l < L; ++l) to_fourier(*f, l);
+    for (int ia = 0; ia < na; ia += kBlockA)
+      for (int jb = 0; jb < nbt; jb += kBlockB)
+        for (int l = 0; l < L; ++l) {
+          BlockFields<T> bf{};
+          bf.na = std::min(kBlockA, na - ia);
+          bf.nb = std::min(kBlockB, nbt - jb);
+          for (int i = 0; i < bf.na; ++i) bf.a[i] = ptr(*A[ia + i], l);
+          for (int j = 0; j < bf.nb; ++j) bf.b[j] = ptr(*B[jb + j], l);
+          k_inner_block<T><<<blocks, hs_block(), 0, ctx.stream>>>(bf, lev(l).n, part + (size_t)l * blocks, ia, jb,
+                                                                   nbt, pstride);
+          launched();
+        }
+    k_sum<<<np, 256, 0, ctx.stream>>>(part, (int)pstride, part + pstride * np);
+    launched();
+    std::vector<double> out(np);
+    GIC_CUDA(cudaMemcpyAsync(out.data(), part + pstride * np, np * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+    GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+    return out;
+  }
+
+  // a += sum_k c[k] b[k] over a level's half spectrum, up to kMaxAxpy sources per pass
+  void axpy_many(T *a, const std::vector<const T *> &b, const std::vector<double> &c, int l) {
+    for (size_t k0 = 0; k0 < b.size(); k0 += kMaxAxpy) {
+      AxpySources<T> src{};
+      src.nb = (int)std::min<size_t>(kMaxAxpy, b.size() - k0);
+      for (int k = 0; k < src.nb; ++k) {
+        src.b[k] = b[k0 + k];
+        src.c[k] = c[k0 + k];
+      }
+      k_axpy_multi<T><<<nblk(elems(l)), 256, 0, ctx.stream>>>(a, src, elems(l));
+      launched();
+    }
+  }
+
   // window of level wl on the cells of level l, per axis (window.hpp)
   void window_masks(int l, int wl) {
     const Level &L = lev(l), &W = lev(wl);
@@ -788,15 +961,15 @@ struct ModEngine {
     DevBuf &inw = S.win;
     for (int t = 0; t < nl(); ++t) {
       T *R = ptr(out, t);
-      GIC_CUDA(cudaMemcpyAsync(R, ptr(X, t), elems(t) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
       if (to_covector && t < nl() - 1) {
+        GIC_CUDA(cudaMemcpyAsync(R, ptr(X, t), elems(t) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
         to_real(R, t);
         windowed_covector_real(X, t, R);
         to_fourier(R, t);
       } else {
         // f_t^2 X_t stays in Fourier space; the cross-level terms are summed in real
-        // space and transformed once: R = f_t^2 X_t + FFT(sum_s cross_s)
-        apply_family(R, t, 2);
+        // space and transformed once: R = f_t^2 X_t + FFT(sum_s cross_s), in one pass
+        const C *add = nullptr;
         if (nl() > 1) {
           inw.ensure(elems(t) * sizeof(T));
           T *Cr = inw.template as<T>();
@@ -804,8 +977,12 @@ struct ModEngine {
           for (int s = 0; s < nl(); ++s)
             if (s != t) cross_term_impl(Cr, t, ptr(X, s), s);
           to_fourier(Cr, t);
-          axpy(R, Cr, 1.0, t);
+          add = reinterpret_cast<const C *>(Cr);
         }
+        family_table(t, 2);
+        k_mul_table_add<T><<<hs_grid(lev(t).n), hs_block(), 0, ctx.stream>>>(
+            reinterpret_cast<C *>(R), reinterpret_cast<const C *>(ptr(X, t)), lev(t).n, S.tab.template as<double>(), add);
+        launched();
       }
       out.fourier[t] = 1;
     }
@@ -1386,20 +1563,20 @@ struct ModEngine {
       }
     }
     for (int l = 0; l < nl(); ++l) {
-      double wr = level_weight(l) / level_weight(F);
-      if (wr != 1.0) scale_by(ptr(out, l), wr, l);
-      to_fourier(out, l);
-      apply_family(ptr(out, l), l, 1);
-      // multiply by sqrt(P_dm) (and -v/k^2 for velocities)
+      // weight ratio (dx_l/dx_F)^3, the level's family filter, sqrt(P_dm) and, for
+      // velocities and angular momenta, -v/k^2: one table, applied as the forward
+      // transform stores its last pass
       build_sqrtp_dm(l);
       TableSpec sp{};
       sp.power = 1;
-      sp.scalar = 1.0;
+      sp.scalar = level_weight(l) / level_weight(F);
+      add_filter_factors(sp, l);
       sp.sqrtp = lev(l).sqrtp_dm.template as<double>();
       const bool velocity_like = (kind >= GIC_MOD_VX && kind <= GIC_MOD_VZ) || kind >= GIC_MOD_LX;
       sp.vel = velocity_like ? velocity_ratio() : 0.0;
       table(sp, l);
-      mul_table(ptr(out, l), l);
+      fft_r2c_3d<T>(ctx, ptr(out, l), lev(l).n, scale(l), S.tab.template as<double>());
+      out.fourier[l] = 1;
       if (kind == GIC_MOD_POTENTIAL) {
         // 3/2 Om0 / a (H0/h)^2 / c^2 in (h/Mpc)^2 (cosmology/parameters.hpp:213-216)
         const double prefac = 3. / 2. * ctx.cosmo.om / ctx.cosmo.a * 100. * 100. / (299792.) / (299792.);
@@ -1529,9 +1706,9 @@ static void perform_iterations(ModEngine<T> &E, typename ModEngine<T>::Field &X,
   for (int i = 0; i < n_steps; ++i) {
     if (i > 0) E.push_variance(X, q, P);
     E.apply_metric(P, CP, false);
-    std::vector<std::pair<F *, F *>> pairs{{&P, &X}, {&P, &CP}};
-    for (int j = 0; j < n; ++j) pairs.push_back({&P, &lin[j]});
-    std::vector<double> ip = E.inner_many(pairs);
+    std::vector<F *> Bs{&X, &CP};
+    for (int j = 0; j < n; ++j) Bs.push_back(&lin[j]);
+    std::vector<double> ip = E.inner_block({&P}, Bs);
     const double current = ip[0], norm = std::sqrt(ip[1]);
     double scale_vec = 1.0;
     F *vec = &CP;
@@ -1542,8 +1719,13 @@ static void perform_iterations(ModEngine<T> &E, typename ModEngine<T>::Field &X,
         r[j] = ip[2 + j];
         for (int m = 0; m < j; ++m) r[j] -= r[m] * D[(size_t)m * n + j];
       }
-      for (int l = 0; l < E.nl(); ++l)
-        for (int j = 0; j < n; ++j) E.axpy(E.ptr(P, l), E.ptr(lin[j], l), -r[j], l);
+      std::vector<double> mr(n);
+      for (int j = 0; j < n; ++j) mr[j] = -r[j];
+      for (int l = 0; l < E.nl(); ++l) {
+        std::vector<const T *> srcs;
+        for (int j = 0; j < n; ++j) srcs.push_back(E.ptr(lin[j], l));
+        E.axpy_many(E.ptr(P, l), srcs, mr, l);
+      }
       E.apply_metric(P, CP2, false);
       scale_vec = 1.0 / std::sqrt(E.inner(P, CP2));
       vec = &CP2;
@@ -1601,13 +1783,15 @@ static void apply_mods(Context &ctx, double *chi2_before, double *chi2_after) {
   // <a_i|W> and the Gram matrix G_ij = <a_i|C a_j>, read back together.  G is not
   // assumed symmetric: the cross-level terms of C (interpolation up, block means
   // down) are not exact transposes of each other.
-  std::vector<std::pair<F *, F *>> pairs;
-  for (int i = 0; i < n; ++i) pairs.push_back({&alpha[i], &W});
-  for (int i = 0; i < n; ++i)
-    for (int j = 0; j < n; ++j) pairs.push_back({&alpha[i], &vec[j]});
-  std::vector<double> ip_all = E.inner_many(pairs);
-  std::vector<double> b(ip_all.begin(), ip_all.begin() + n);
-  std::vector<double> G(ip_all.begin() + n, ip_all.end());
+  std::vector<F *> As, Bs{&W};
+  for (int i = 0; i < n; ++i) As.push_back(&alpha[i]);
+  for (int j = 0; j < n; ++j) Bs.push_back(&vec[j]);
+  std::vector<double> M = E.inner_block(As, Bs);  // M[i][0] = <a_i|W>, M[i][1 + j] = G_ij
+  std::vector<double> b(n), G((size_t)n * n);
+  for (int i = 0; i < n; ++i) {
+    b[i] = M[(size_t)i * (n + 1)];
+    for (int j = 0; j < n; ++j) G[(size_t)i * n + j] = M[(size_t)i * (n + 1) + 1 + j];
+  }
   // Gram-Schmidt in the order of modificationmanager.hpp:288-312, on coefficient
   // vectors: row i of L holds a'_i = sum_k L[i][k] a_k
   std::vector<double> L((size_t)n * n, 0.0);
@@ -1637,8 +1821,11 @@ static void apply_mods(Context &ctx, double *chi2_before, double *chi2_after) {
     double d = t[i] - existing;
     for (int k = 0; k < n; ++k) coef[k] += d * L[(size_t)i * n + k];
   }
-  for (int l = 0; l < E.nl(); ++l)
-    for (int k = 0; k < n; ++k) E.axpy(E.ptr(W, l), E.ptr(vec[k], l), coef[k], l);
+  for (int l = 0; l < E.nl() && n > 0; ++l) {
+    std::vector<const T *> srcs;
+    for (int k = 0; k < n; ++k) srcs.push_back(E.ptr(vec[k], l));
+    E.axpy_many(E.ptr(W, l), srcs, coef, l);
+  }
   if (!ctx.quads.empty()) {
     // applyLinearModif leaves the orthonormalised covectors converted to vectors,
     // C a'_i = sum_k L[i][k] C a_k; the quadratic steps project against those
