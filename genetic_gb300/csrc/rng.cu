@@ -31,8 +31,7 @@ constexpr int kLux = 794;          // 24-bit steps per delivered block
 constexpr int kChunkBlocks = 16;   // blocks per generator thread
 constexpr int kSegLen = 1024;      // stream numbers per ziggurat segment
 constexpr int kSpec = 8;           // speculative entry offsets per segment
-constexpr int kTileSegs = 8;       // segments staged together in shared memory
-constexpr int kOverhang = 256;     // numbers staged past the tile end
+constexpr int kSpecThreads = 128;  // segments per CTA of the speculative walk
 constexpr int kBlockSegs = 64;     // segments per block of the two-level chain
 constexpr uint32_t kUnderrun = 0xFFFFFFFFu;
 
@@ -179,15 +178,42 @@ __global__ void __launch_bounds__(128) k_generate(const Stream *st, int nstreams
 // further attempts.  Consumption is found with integer work alone on the fast
 // path; doubles are only used on the slow path and for the final values.
 
-// Stream numbers come from a shared-memory copy of the tile when the index is
-// inside it, else from global memory.
-struct Reader {
-  const uint32_t *g;       // raw buffer (absolute indices)
-  const uint32_t *sm;      // shared copy of [lo, hi)
-  unsigned long long lo, hi;
-  __device__ __forceinline__ uint32_t operator()(unsigned long long p) const {
-    return (p >= lo && p < hi) ? sm[p - lo] : __ldg(g + p);
+// j * w rounded to the nearest double (ties to even), for 0 < j < 2^24 and w a positive
+// normal double whose product stays normal: the ziggurat's x = j W[i].  Exactly the
+// value of __dmul_rn((double)j, w), formed on the integer pipe: the 77-bit product of
+// j and w's 53-bit significand, rounded to 53 bits, with the exponent adjusted.
+__device__ __forceinline__ double mul_u24_rn(uint32_t j, double w) {
+  const unsigned long long wb = (unsigned long long)__double_as_longlong(w);
+  const int ew = (int)((wb >> 52) & 0x7FF);
+  const unsigned long long mw = (wb & ((1ull << 52) - 1)) | (1ull << 52);
+  const unsigned long long lo = (unsigned long long)j * mw, hi = __umul64hi((unsigned long long)j, mw);
+  const int nbits = hi ? 128 - __clzll((long long)hi) : 64 - __clzll((long long)lo);
+  const int sh = nbits - 53;  // 0..24
+  unsigned long long m, rem = 0, half = 0;
+  if (sh == 0) {
+    m = lo;
+  } else {
+    m = (lo >> sh) | (hi << (64 - sh));
+    rem = lo & ((1ull << sh) - 1);
+    half = 1ull << (sh - 1);
   }
+  int e = sh + ew;
+  if (rem > half || (rem == half && half && (m & 1))) {
+    ++m;
+    if (m == (1ull << 53)) {
+      m >>= 1;
+      ++e;
+    }
+  }
+  return __longlong_as_double((long long)(((unsigned long long)e << 52) | (m & ((1ull << 52) - 1))));
+}
+
+// Stream numbers by absolute position: the walks of neighbouring threads read
+// disjoint segments, and the eight entry walks of one segment read the same lines
+// again, so they come through L1.
+struct Reader {
+  const uint32_t *g;
+  __device__ __forceinline__ uint32_t operator()(unsigned long long p) const { return __ldg(g + p); }
 };
 
 // Advance p past one gaussian of the stream ending at `end`; optionally return
@@ -212,7 +238,8 @@ __device__ __forceinline__ bool zig_gaussian(const ZigTab &T, const Reader &rd, 
     unsigned il = i & 0x7Fu;
     unsigned long long neg = (i & 0x80u) ? 0ull : 0x8000000000000000ull;
     if (j < T.K[il]) {
-      if (VALUE) g = __longlong_as_double(__double_as_longlong(__dmul_rn((double)j, T.W[il])) ^ neg);
+      if (VALUE) g = j ? __longlong_as_double(__double_as_longlong(mul_u24_rn(j, T.W[il])) ^ neg)
+                       : __longlong_as_double((long long)neg);
       p += 2;
       return true;
     }
@@ -232,7 +259,8 @@ __device__ __forceinline__ bool zig_gaussian(const ZigTab &T, const Reader &rd, 
       }
       p += 3;
       if (accept) {
-        if (VALUE) g = __longlong_as_double(__double_as_longlong(__dmul_rn((double)j, T.W[il])) ^ neg);
+        if (VALUE) g = j ? __longlong_as_double(__double_as_longlong(mul_u24_rn(j, T.W[il])) ^ neg)
+                         : __longlong_as_double((long long)neg);
         return true;
       }
     } else {
@@ -300,36 +328,73 @@ __device__ __forceinline__ void segment_bounds(const Stream &s, unsigned long lo
   if (b > e) b = e;
 }
 
-// One CTA per tile of kTileSegs consecutive segments (of any streams); the
-// tile's numbers plus an overhang are staged in shared memory, then
-// kTileSegs * kSpec threads walk every (segment, entry offset) pair.
-__global__ void __launch_bounds__(kTileSegs * kSpec) k_walk_speculative(const Stream *st, int nstreams,
-                                                                       unsigned long long nseg_total,
-                                                                       const uint32_t *raw,
-                                                                       unsigned long long raw_total,
-                                                                       uint32_t *tab) {
-  __shared__ uint32_t sm[kTileSegs * kSegLen + kOverhang];
+// One thread per segment tabulates (count, exit) for the entry offsets 0..kSpec-1.
+// The walk from entry 0 marks the start of each of its gaussians in a bitmap of
+// the segment (a column of shared memory per thread, conflict-free).  The walk
+// from entry e > 0 then runs only until it stands on a marked position: from
+// there on both are the same walk, so its count is the gaussians it found before
+// plus entry 0's from that position on, and its exit (or underrun) is entry 0's.
+// Fast-path gaussians take 2 numbers, so even entries meet entry 0 at once and odd
+// ones after the first 3-number attempt of either walk: the kSpec tables cost
+// about 1.3 walks of the segment instead of kSpec.
+__global__ void __launch_bounds__(kSpecThreads) k_walk_speculative(const Stream *st, int nstreams,
+                                                                    unsigned long long nseg_total,
+                                                                    const uint32_t *raw, uint32_t *tab) {
   __shared__ ZigTab zt;
-  unsigned long long g0 = (unsigned long long)blockIdx.x * kTileSegs;
-  if (g0 >= nseg_total) return;
+  __shared__ uint32_t marks[kSegLen / 32][kSpecThreads];
   load_zig(zt);
-  // tile range in absolute stream positions
-  int s0 = find_stream_by_segment(st, nstreams, g0);
-  unsigned long long lo = st[s0].raw_off + (g0 - st[s0].seg_off) * kSegLen;
-  unsigned long long hi = lo + kTileSegs * kSegLen + kOverhang;
-  if (hi > raw_total) hi = raw_total;
-  for (unsigned long long q = lo + threadIdx.x; q < hi; q += blockDim.x) sm[q - lo] = __ldg(raw + q);
+  const int t = threadIdx.x;
+  for (int w = 0; w < kSegLen / 32; ++w) marks[w][t] = 0u;
   __syncthreads();
-  unsigned long long gseg = g0 + threadIdx.x / kSpec;
-  unsigned e = threadIdx.x % kSpec;
+  unsigned long long gseg = (unsigned long long)blockIdx.x * kSpecThreads + t;
   if (gseg >= nseg_total) return;
   int s = find_stream_by_segment(st, nstreams, gseg);
+  const Stream &S = st[s];
   unsigned long long a, b;
-  segment_bounds(st[s], gseg - st[s].seg_off, a, b);
-  Reader rd{raw, sm, lo, hi};
-  uint32_t cnt = 0, ex = 0;
-  walk_segment<false>(zt, rd, st[s].raw_off + st[s].raw_count, a, b, e, cnt, ex, nullptr, 0);
-  tab[gseg * kSpec + e] = pack_ce(cnt, ex);
+  segment_bounds(S, gseg - S.seg_off, a, b);
+  const unsigned long long end = S.raw_off + S.raw_count;
+  const Reader rd{raw};
+  double g;
+  unsigned long long p = a;
+  uint32_t total0 = 0, ex0;
+  bool under = false;
+  while (p < b) {
+    uint32_t r = (uint32_t)(p - a);
+    marks[r >> 5][t] |= 1u << (r & 31);
+    if (!zig_gaussian<false>(zt, rd, end, p, g)) {
+      under = true;
+      break;
+    }
+    ++total0;
+  }
+  ex0 = under ? kUnderrun : (uint32_t)(p - b);
+  uint32_t *out = tab + gseg * kSpec;
+  out[0] = pack_ce(total0, ex0);
+  for (unsigned e = 1; e < (unsigned)kSpec; ++e) {
+    unsigned long long q = a + e;
+    uint32_t cnt = 0, ex = 0;
+    bool met = false;
+    while (q < b) {
+      uint32_t r = (uint32_t)(q - a);
+      uint32_t word = marks[r >> 5][t];
+      if ((word >> (r & 31)) & 1u) {
+        uint32_t before = __popc(word & ((1u << (r & 31)) - 1u));  // entry 0's gaussians before r
+        for (uint32_t w = 0; w < (r >> 5); ++w) before += __popc(marks[w][t]);
+        cnt += total0 - before;
+        ex = ex0;
+        met = true;
+        break;
+      }
+      if (!zig_gaussian<false>(zt, rd, end, q, g)) {
+        ex = kUnderrun;
+        met = true;
+        break;
+      }
+      ++cnt;
+    }
+    if (!met) ex = (uint32_t)(q - b);
+    out[e] = pack_ce(cnt, ex);
+  }
 }
 
 // Follow segment g from entry e: table lookup, or a real walk when the entry
@@ -344,7 +409,7 @@ __device__ __forceinline__ void step_segment(const Stream &s, const uint32_t *ra
   }
   unsigned long long a, b;
   segment_bounds(s, gseg - s.seg_off, a, b);
-  Reader rd{raw, raw, 0, 0};
+  const Reader rd{raw};
   walk_segment<false>(gZig, rd, s.raw_off + s.raw_count, a, b, e, cnt, ex, nullptr, 0);
 }
 
@@ -452,7 +517,7 @@ __global__ void k_walk_final(const Stream *st, int nstreams, unsigned long long 
   if (base >= need) return;
   unsigned long long a, b;
   segment_bounds(S, gseg - S.seg_off, a, b);
-  Reader rd{raw, raw, 0, 0};
+  const Reader rd{raw};
   uint32_t cnt, ex;
   walk_segment<true>(zt, rd, S.raw_off + S.raw_count, a, b, seg_entry[gseg], cnt, ex, gauss + S.gauss_off + base,
                      need - base);
@@ -620,9 +685,8 @@ static void generate_gaussians(Context &ctx, std::vector<Stream> &streams, unsig
   k_generate<<<(unsigned)((chunk_total + 127) / 128), 128, 0, cs>>>(dst, ns, chunk_total, R.chunkmul.as<U576>(),
                                                                    R.raw.as<uint32_t>());
   launched();
-  unsigned ntiles = (unsigned)((seg_total + kTileSegs - 1) / kTileSegs);
-  k_walk_speculative<<<ntiles, kTileSegs * kSpec, 0, cs>>>(dst, ns, seg_total, R.raw.as<uint32_t>(), raw_total,
-                                                          R.segtab.as<uint32_t>());
+  k_walk_speculative<<<(unsigned)((seg_total + kSpecThreads - 1) / kSpecThreads), kSpecThreads, 0, cs>>>(
+      dst, ns, seg_total, R.raw.as<uint32_t>(), R.segtab.as<uint32_t>());
   launched();
   unsigned long long nbm = blk_total * kSpec;
   k_block_maps<<<(unsigned)((nbm + 127) / 128), 128, 0, cs>>>(dst, ns, blk_total, R.raw.as<uint32_t>(),
@@ -894,8 +958,7 @@ static int noalloc_run(unsigned long long seed, unsigned long long n, double *ou
   k_seed<<<1, 1, 0, cs>>>(dst, 1);
   k_generate<<<(s.nchunk + 127) / 128, 128, 0, cs>>>(dst, 1, s.nchunk, chunkmul, raw);
   if (!ok()) return GIC_ERR_CUDA;
-  unsigned ntiles = (unsigned)((s.nseg + kTileSegs - 1) / kTileSegs);
-  k_walk_speculative<<<ntiles, kTileSegs * kSpec, 0, cs>>>(dst, 1, s.nseg, raw, s.raw_count, segtab);
+  k_walk_speculative<<<(s.nseg + kSpecThreads - 1) / kSpecThreads, kSpecThreads, 0, cs>>>(dst, 1, s.nseg, raw, segtab);
   k_block_maps<<<(s.nblk * kSpec + 127) / 128, 128, 0, cs>>>(dst, 1, s.nblk, raw, segtab, blkmap);
   k_chain_blocks<<<1, 64, 0, cs>>>(dst, 1, raw, segtab, blkmap, blkentry, blkbase, flags);
   k_chain_segments<<<(s.nblk + 127) / 128, 128, 0, cs>>>(dst, 1, s.nblk, raw, segtab, blkentry, blkbase, segentry,
