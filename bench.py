@@ -328,12 +328,16 @@ def run_batch(args, wl, table, local, rank, world):
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier(world)
     torch.cuda.synchronize()
+    if args.profile_range:
+        torch.cuda.profiler.start()
     with Clocks(local) as clk:
         start.record(stream)
         for i in range(args.steps):
             step(args.warmup + i)
         end.record(stream)
         torch.cuda.synchronize()
+    if args.profile_range:
+        torch.cuda.profiler.stop()
     barrier(world)
     launches1 = ctypes.c_ulonglong()
     gens[0]._lib.gic_launch_count(ctypes.byref(launches1))
@@ -425,6 +429,8 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--workload', default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--profile-range', action='store_true',
+                    help='bracket the timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off)')
     ap.add_argument('--accuracy', action='store_true',
                     help='print the per-field error of the mixed form against FP64 instead of timing')
     args = ap.parse_args()
@@ -472,12 +478,16 @@ def main():
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier(world)
     torch.cuda.synchronize()
+    if args.profile_range:
+        torch.cuda.profiler.start()
     with Clocks(local) as clk:
         start.record(stream)
         for i in range(args.steps):
             step(args.warmup + i)
         end.record(stream)
         torch.cuda.synchronize()
+    if args.profile_range:
+        torch.cuda.profiler.stop()
     barrier(world)
     launches1 = ctypes.c_ulonglong()
     gen._lib.gic_launch_count(ctypes.byref(launches1))

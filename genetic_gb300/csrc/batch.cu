@@ -55,7 +55,9 @@ void append_signature(const Context &C, std::vector<uintptr_t> &sig) {
     sig.push_back((uintptr_t)e->f32.ptr);
     sig.push_back((uintptr_t)e->f64.ptr);
   }
-  for (auto &t : C.fft.tuned) sig.push_back((uintptr_t)(t.n * 64 + t.cols * 8 + t.rows));
+  for (auto &t : C.fft.tuned) sig.push_back((uintptr_t)(t.n * 64 + t.cols * 8 + t.rows) * 16 + (uintptr_t)(t.planes + 1));
+  sig.push_back((uintptr_t)C.fft.plane_sync.ptr);
+  sig.push_back((uintptr_t)C.fft.wait_flag_dev);
 }
 
 void field_maps(Context &C, int order) {
@@ -243,6 +245,8 @@ GIC_API int gic_batch_realise(gic_batch *b, const unsigned long *seeds, const in
       }
     }
     gic::cuda_check(cudaStreamSynchronize(b->origin), "cudaStreamSynchronize");
+    for (auto *c : b->ctxs)
+      if (gic::take_fft_wait_error(c->impl)) gic::fail(GIC_ERR_CUDA, c->impl.last_error);
     for (auto *c : b->ctxs)
       for (auto &L : c->impl.levels) {
         L->have_fields = true;

@@ -174,6 +174,7 @@ using gic::Error;
     C.last_error = e.what();                               \
     return GIC_ERR_INTERNAL;                               \
   }                                                        \
+  if (gic::take_fft_wait_error(C)) return GIC_ERR_CUDA;   \
   C.last_error.clear();                                    \
   return GIC_OK;
 
@@ -208,14 +209,17 @@ int gic_create(gic_ctx **out, const gic_device_opts *opts) {
     return GIC_ERR_CUDA;
   }
   // GIC_FFT_TILE selects the FFT passes by hand instead of the tuner: "generic"
-  // (runtime-length kernels) or "<cols>,<rows>" (fixed-length tile candidates)
+  // (runtime-length kernels), "<cols>,<rows>" (fixed-length tile candidates, separate
+  // y and z passes) or "<cols>,<rows>,<plane variant>" (x pass, then the plane pass)
   if (const char *t = std::getenv("GIC_FFT_TILE")) {
-    int a = -1, b = -1;
+    int a = -1, b = -1, p = -1;
+    const int got = std::sscanf(t, "%d,%d,%d", &a, &b, &p);
     if (std::strcmp(t, "generic") == 0) {
       c->impl.fft.force_cols = -2;
-    } else if (std::sscanf(t, "%d,%d", &a, &b) == 2 && a >= 0 && b >= 0) {
+    } else if (got >= 2 && a >= 0 && b >= 0) {
       c->impl.fft.force_cols = a;
       c->impl.fft.force_rows = b;
+      c->impl.fft.force_planes = got == 3 && p >= 0 ? p : -1;
     }
   }
   *out = c;

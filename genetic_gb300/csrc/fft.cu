@@ -622,7 +622,9 @@ __device__ __forceinline__ C czero() {
   return z;
 }
 
-template <typename C>
+// CG: load through L2 only (ld.global.cg), for data that other CTAs of the same
+// launch wrote
+template <typename C, bool CG = false>
 struct ColsIn {
   const C *base;
   long long B;
@@ -632,7 +634,8 @@ struct ColsIn {
   long long b0;
   __device__ __forceinline__ C operator()(int c, int m) const {
     if (c >= tcv) return czero<C>();
-    C v = base[(size_t)m * (size_t)B + c];
+    const C *p = base + (size_t)m * (size_t)B + c;
+    C v = CG ? __ldcg(p) : *p;
     return tab ? cscale(v, (decltype(v.x))qtab(tab, L, m, b0 + c)) : v;
   }
 };
@@ -749,31 +752,23 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_fft_rows_r2c_fused(typename C
   }
 }
 
-// c2r rows of N = 2H reals: rows of H + 1 Hermitian coefficients are copied
-// (coalesced) into a tile [H + 1][RPC + 1] with one row per tile column, packed
-// into H complex values, transformed, and copied back as N reals per row.
-template <typename T, int H, int RPC, int NT>
-__global__ void __launch_bounds__(NT) k_fft_rows_c2r_fixed(typename Cx<T>::type *data, long long nrows,
-                                                           const typename Cx<T>::type *tw, T scale) {
+// CG: the rows are loaded through L2 only (data other CTAs of the same launch
+// wrote), else with asynchronous copies
+template <typename T, int H, int RPC, int NT, bool CG>
+__device__ __forceinline__ void rows_c2r_tile(typename Cx<T>::type *tile, typename Cx<T>::type *base, int rows_valid,
+                                              const typename Cx<T>::type *tw, T scale) {
   using C = typename Cx<T>::type;
   constexpr int S = H + 1, TCP = RPC + 1;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  C *tile = reinterpret_cast<C *>(smraw);
-  const long long r0 = (long long)blockIdx.x * RPC;
-  const int rows_valid = (int)min((long long)RPC, nrows - r0);
-  C *base = data + (size_t)r0 * S;
   for (int e = threadIdx.x; e < RPC * S; e += NT) {
     const int row = e / S, m = e % S;
     if (row < rows_valid) {
-      cp_async<sizeof(C)>(tile + m * TCP + row, base + e);
+      if (CG) tile[m * TCP + row] = __ldcg(base + e);
+      else cp_async<sizeof(C)>(tile + m * TCP + row, base + e);
     } else {
-      C z;
-      z.x = 0;
-      z.y = 0;
-      tile[m * TCP + row] = z;
+      tile[m * TCP + row] = czero<C>();
     }
   }
-  cp_async_wait_all();
+  if (!CG) cp_async_wait_all();
   __syncthreads();
   // Z[k] = E + i O, E = X[k] + conj X[H-k], O = (X[k] - conj X[H-k]) e^{+2 pi i k / N};
   // Z[k] and Z[H-k] both come from X[k] and X[H-k], so pairs are done in place
@@ -801,29 +796,37 @@ __global__ void __launch_bounds__(NT) k_fft_rows_c2r_fixed(typename Cx<T>::type 
   }
 }
 
-// r2c rows: N reals per row (read as H complex) -> H + 1 coefficients
+// c2r rows of N = 2H reals: rows of H + 1 Hermitian coefficients are copied
+// (coalesced) into a tile [H + 1][RPC + 1] with one row per tile column, packed
+// into H complex values, transformed, and copied back as N reals per row.
 template <typename T, int H, int RPC, int NT>
-__global__ void __launch_bounds__(NT) k_fft_rows_r2c_fixed(typename Cx<T>::type *data, long long nrows,
+__global__ void __launch_bounds__(NT) k_fft_rows_c2r_fixed(typename Cx<T>::type *data, long long nrows,
                                                            const typename Cx<T>::type *tw, T scale) {
   using C = typename Cx<T>::type;
-  constexpr int S = H + 1, TCP = RPC + 1;
+  constexpr int S = H + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
   C *tile = reinterpret_cast<C *>(smraw);
   const long long r0 = (long long)blockIdx.x * RPC;
   const int rows_valid = (int)min((long long)RPC, nrows - r0);
-  C *base = data + (size_t)r0 * S;
+  rows_c2r_tile<T, H, RPC, NT, false>(tile, data + (size_t)r0 * S, rows_valid, tw, scale);
+}
+
+// r2c rows: N reals per row (read as H complex) -> H + 1 coefficients
+template <typename T, int H, int RPC, int NT, bool CG>
+__device__ __forceinline__ void rows_r2c_tile(typename Cx<T>::type *tile, typename Cx<T>::type *base, int rows_valid,
+                                              const typename Cx<T>::type *tw, T scale) {
+  using C = typename Cx<T>::type;
+  constexpr int S = H + 1, TCP = RPC + 1;
   for (int e = threadIdx.x; e < RPC * H; e += NT) {
     const int row = e / H, m = e % H;
     if (row < rows_valid) {
-      cp_async<sizeof(C)>(tile + m * TCP + row, base + (size_t)row * S + m);
+      if (CG) tile[m * TCP + row] = __ldcg(base + (size_t)row * S + m);
+      else cp_async<sizeof(C)>(tile + m * TCP + row, base + (size_t)row * S + m);
     } else {
-      C z;
-      z.x = 0;
-      z.y = 0;
-      tile[m * TCP + row] = z;
+      tile[m * TCP + row] = czero<C>();
     }
   }
-  cp_async_wait_all();
+  if (!CG) cp_async_wait_all();
   __syncthreads();
   TileStages<T, H, RPC, TCP, NT, 1, -1, 2>::run(tile, tw);
   // X[k] = (Z[k] + conj Z[H-k]) / 2 - i/2 e^{-2 pi i k / N} (Z[k] - conj Z[H-k]), k in [0, H]
@@ -842,6 +845,122 @@ __global__ void __launch_bounds__(NT) k_fft_rows_r2c_fixed(typename Cx<T>::type 
   for (int e = threadIdx.x; e < RPC * S; e += NT) {
     const int row = e / S, m = e % S;
     if (row < rows_valid) base[e] = cscale(tile[m * TCP + row], scale);
+  }
+}
+
+template <typename T, int H, int RPC, int NT>
+__global__ void __launch_bounds__(NT) k_fft_rows_r2c_fixed(typename Cx<T>::type *data, long long nrows,
+                                                           const typename Cx<T>::type *tw, T scale) {
+  using C = typename Cx<T>::type;
+  constexpr int S = H + 1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C *tile = reinterpret_cast<C *>(smraw);
+  const long long r0 = (long long)blockIdx.x * RPC;
+  const int rows_valid = (int)min((long long)RPC, nrows - r0);
+  rows_r2c_tile<T, H, RPC, NT, false>(tile, data + (size_t)r0 * S, rows_valid, tw, scale);
+}
+
+// ---- plane pass: y transforms and z rows of every x plane in one persistent kernel ----
+// After the x pass (before it, for r2c) each x plane of N (N/2 + 1) coefficients is
+// finished by the y transforms of its column tiles and the real transforms of its
+// rows.  As two passes they send the whole array through HBM twice.  Here resident
+// CTAs take tasks from a ticket counter in an order that runs the second kind of
+// task of a group of planes `lag` groups after the first kind, so a plane is still
+// in L2 when it is read again and HBM carries one read and one write of the array for
+// both transforms.  A second-kind task waits (one thread, bounded) for its plane's
+// count of finished first-kind tasks; those hold smaller tickets, so they were taken
+// by CTAs that are running, and the wait ends.  Tiles written by other CTAs of the
+// launch are read through L2 only (ld.global.cg), never from a stale L1 line.
+//   c2r (INV): first kind = y transform of TC columns (sign +1), second = RPC rows c2r
+//   r2c:       first kind = RPC rows r2c, second = y transform of TC columns (sign -1)
+// sync: N plane counters and the ticket, zeroed before the launch; wait_flag is set
+// when a wait gives up (the host reports it).
+constexpr unsigned kPlaneSpinLimit = 1u << 22;
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void red_release_gpu(unsigned *p, unsigned v) {
+  asm volatile("fence.acq_rel.gpu;\n\tred.relaxed.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+template <int N, int TC, int RPC>
+struct PlaneTasks {
+  static constexpr int S = N / 2 + 1, NY = (S + TC - 1) / TC, NZ = N / RPC;
+};
+
+template <typename T, int N, int TC, int RPC, int NT, bool INV>
+__global__ void __launch_bounds__(NT, 1024 / NT) k_fft_planes(typename Cx<T>::type *data,
+                                                               const typename Cx<T>::type *tw, T scale, int group,
+                                                               int lag, unsigned *sync, int *wait_flag) {
+  using C = typename Cx<T>::type;
+  using PT = PlaneTasks<N, TC, RPC>;
+  constexpr int H = N / 2, S = PT::S;
+  constexpr int P1 = INV ? PT::NY : PT::NZ, P2 = INV ? PT::NZ : PT::NY;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C *tile = reinterpret_cast<C *>(smraw);
+  __shared__ int s_ticket;
+  unsigned *plane_done = sync, *ticket = sync + N;
+  const int ngroups = N / group;
+  const int A = P1 * group, B = P2 * group;
+  const int total = (A + B) * ngroups;
+  for (;;) {
+    if (threadIdx.x == 0) s_ticket = (int)atomicAdd(ticket, 1u);
+    __syncthreads();
+    const int t = s_ticket;
+    if (t >= total) return;
+    // ticket -> (kind, group, index): lag steps of first kinds, then first and second
+    // kinds alternating by group, then the last lag groups' second kinds
+    bool first;
+    int g, idx;
+    if (t < lag * A) {
+      first = true;
+      g = t / A;
+      idx = t % A;
+    } else if (t - lag * A < (ngroups - lag) * (A + B)) {
+      const int u = t - lag * A, step = lag + u / (A + B), r = u % (A + B);
+      first = r < A;
+      g = first ? step : step - lag;
+      idx = first ? r : r - A;
+    } else {
+      const int u = t - lag * A - (ngroups - lag) * (A + B);
+      first = false;
+      g = ngroups + u / B - lag;
+      idx = u % B;
+    }
+    const int plane = g * group + idx % group, sub = idx / group;
+    if (!first) {
+      if (threadIdx.x == 0) {
+        unsigned spins = 0;
+        while (ld_acquire_gpu(plane_done + plane) < (unsigned)P1) {
+          if (++spins > kPlaneSpinLimit) {
+            atomicExch(wait_flag, 1);
+            break;
+          }
+          __nanosleep(100);
+        }
+      }
+      __syncthreads();
+    }
+    const bool rows_task = first != INV;
+    C *pbase = data + (size_t)plane * (size_t)N * S;
+    if (rows_task) {
+      if (INV) rows_c2r_tile<T, H, RPC, NT, true>(tile, pbase + (size_t)sub * RPC * S, RPC, tw, scale);
+      else rows_r2c_tile<T, H, RPC, NT, true>(tile, pbase + (size_t)sub * RPC * S, RPC, tw, (T)1);
+    } else {
+      constexpr int SIGN = INV ? +1 : -1;
+      const long long b0 = (long long)sub * TC;
+      const int tcv = (int)min((long long)TC, (long long)S - b0);
+      C *base = pbase + b0;
+      first_stage_from<T, N, TC, NT, SIGN>(tile, ColsIn<C, true>{base, S, tcv, nullptr, N, b0});
+      constexpr int R0 = next_radix(N, 1), NSL = last_stage_ns(N);
+      TileStagesUntil<T, N, TC, TC, NT, R0, NSL, SIGN, 1>::run(tile, tw);
+      last_stage_to<T, N, TC, NT, SIGN, 1>(tile, tw, ColsOut<C, T>{base, S, tcv, (T)1, nullptr, N, b0});
+    }
+    __syncthreads();
+    if (first && threadIdx.x == 0) red_release_gpu(plane_done + plane, 1u);
   }
 }
 
@@ -951,18 +1070,63 @@ struct FixedFft {
       else rows<F32 ? 16 : 8, 256, false>(ctx, d, tw, scale);
     }
   }
-  static void c2r(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, const double *tab) {
+  // plane pass (N >= 256 in FP32, N >= 512 in FP64): column tiles and row tiles sized for 512 threads and about
+  // 64 KB of shared memory, two CTAs per SM; `group` planes per step of the ticket order
+  static constexpr bool kPlanes = F32 ? N >= 256 : N >= 512;
+  static constexpr int kPlaneVariants = 3;
+  template <bool INV>
+  static void planes(Context &ctx, C *d, const C *tw, T scale, int variant) {
+    if constexpr (kPlanes) {
+      constexpr int PTC = F32 ? (N >= 1024 ? 8 : 16) : (N >= 1024 ? 4 : 8);
+      constexpr int PRPC = F32 ? (N >= 1024 ? 16 : 32) : (N >= 1024 ? 8 : 16);
+      constexpr int PNT = 512;
+      static std::atomic<int> mask{0};
+      static std::atomic<int> resident{0};
+      const void *fn = (const void *)k_fft_planes<T, N, PTC, PRPC, PNT, INV>;
+      const size_t smem = std::max((size_t)N * PTC, (size_t)S * (PRPC + 1)) * sizeof(C);
+      set_smem_once(fn, smem, mask);
+      int dev = 0, nsm = 0;
+      GIC_CUDA(cudaGetDevice(&dev));
+      GIC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+      if (resident.load() == 0) {
+        int nb = 0;
+        GIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, PNT, smem));
+        resident.store(std::max(nb, 1));
+      }
+      using PT = PlaneTasks<N, PTC, PRPC>;
+      const int ctas = resident.load() * nsm;
+      const int group = std::max(1, 2048 / N), ngroups = N / group;
+      const int per_step = (PT::NY + PT::NZ) * group;
+      // lag: 1, 2 or 4 times the resident CTAs, in ticket steps
+      const int lag = std::max(1, std::min(ngroups, ((1 << variant) * ctas + per_step - 1) / per_step));
+      const int total = per_step * ngroups;
+      ctx.fft.plane_sync.ensure((size_t)(N + 1) * sizeof(unsigned));
+      GIC_CUDA(cudaMemsetAsync(ctx.fft.plane_sync.ptr, 0, (size_t)(N + 1) * sizeof(unsigned), ctx.stream));
+      k_fft_planes<T, N, PTC, PRPC, PNT, INV><<<std::min(ctas, total), PNT, smem, ctx.stream>>>(
+          d, tw, scale, group, lag, ctx.fft.plane_sync.template as<unsigned>(), ctx.fft.wait_flag());
+      launched();
+    }
+  }
+  static void c2r(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, int pv, const double *tab) {
     cols_cfg(ctx, ccfg, +1, c, 1, (long long)N * S, tw, (T)1, tab);
+    if (kPlanes && pv >= 0) {
+      planes<true>(ctx, c, tw, scale, pv);
+      return;
+    }
     cols_cfg(ctx, ccfg, +1, c, N, S, tw, (T)1);
     rows_cfg(ctx, rcfg, true, c, tw, scale);
   }
-  static void r2c(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, const double *tab) {
-    rows_cfg(ctx, rcfg, false, c, tw, (T)1);
-    cols_cfg(ctx, ccfg, -1, c, N, S, tw, (T)1);
+  static void r2c(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, int pv, const double *tab) {
+    if (kPlanes && pv >= 0) {
+      planes<false>(ctx, c, tw, (T)1, pv);
+    } else {
+      rows_cfg(ctx, rcfg, false, c, tw, (T)1);
+      cols_cfg(ctx, ccfg, -1, c, N, S, tw, (T)1);
+    }
     cols_cfg(ctx, ccfg, -1, c, 1, (long long)N * S, tw, scale, tab);
   }
   // time every candidate on a scratch array of the transform's size
-  static void tune(Context &ctx, const C *tw, int &best_cols, int &best_rows) {
+  static void tune(Context &ctx, const C *tw, int &best_cols, int &best_rows, int &best_planes) {
     const size_t bytes = (size_t)N * N * S * sizeof(C);
     auto scratch = ctx.pool.take(bytes);
     C *d = scratch->template as<C>();
@@ -989,6 +1153,18 @@ struct FixedFft {
       float t = time_it([&] { rows_cfg(ctx, r, true, d, tw, (T)1); });
       if (t < br) { br = t; best_rows = r; }
     }
+    // the plane pass against the best separate y and z passes
+    best_planes = -1;
+    if (kPlanes) {
+      float bp = time_it([&] {
+        cols_cfg(ctx, best_cols, +1, d, N, S, tw, (T)1);
+        rows_cfg(ctx, best_rows, true, d, tw, (T)1);
+      });
+      for (int v = 0; v < kPlaneVariants; ++v) {
+        float t = time_it([&] { planes<true>(ctx, d, tw, (T)1, v); });
+        if (t < bp) { bp = t; best_planes = v; }
+      }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     ctx.pool.give(std::move(scratch));
@@ -999,7 +1175,7 @@ struct FixedFft {
 struct SharedTune {
   int device, n;
   bool dbl;
-  int cols, rows;
+  int cols, rows, planes;
 };
 std::mutex g_tune_mutex;
 std::vector<SharedTune> g_tuned;
@@ -1009,11 +1185,12 @@ void fixed_transform(Context &ctx, typename Cx<T>::type *c, const typename Cx<T>
                      const double *tab) {
   FftTables &F = ctx.fft;
   const bool dbl = sizeof(T) == 8;
-  int cc = -1, rc = -1;
+  int cc = -1, rc = -1, pv = -1;
   for (auto &t : F.tuned)
     if (t.n == N && t.dbl == dbl) {
       cc = t.cols;
       rc = t.rows;
+      pv = t.planes;
     }
   if (cc < 0) {
     std::lock_guard<std::mutex> lock(g_tune_mutex);
@@ -1021,19 +1198,22 @@ void fixed_transform(Context &ctx, typename Cx<T>::type *c, const typename Cx<T>
       if (t.device == ctx.device && t.n == N && t.dbl == dbl) {
         cc = t.cols;
         rc = t.rows;
+        pv = t.planes;
       }
     if (cc < 0) {
       cc = 0;
       rc = 0;
-      if (N >= 128) FixedFft<T, N>::tune(ctx, tw, cc, rc);
-      g_tuned.push_back({ctx.device, N, dbl, cc, rc});
+      pv = -1;
+      if (N >= 128) FixedFft<T, N>::tune(ctx, tw, cc, rc, pv);
+      g_tuned.push_back({ctx.device, N, dbl, cc, rc, pv});
     }
-    F.tuned.push_back({N, dbl, cc, rc});
+    F.tuned.push_back({N, dbl, cc, rc, pv});
   }
   if (F.force_cols >= 0) cc = F.force_cols;
   if (F.force_rows >= 0) rc = F.force_rows;
-  if (inverse) FixedFft<T, N>::c2r(ctx, c, tw, (T)scale, cc, rc, tab);
-  else FixedFft<T, N>::r2c(ctx, c, tw, (T)scale, cc, rc, tab);
+  if (F.force_planes >= -1) pv = std::min(F.force_planes, FixedFft<T, N>::kPlaneVariants - 1);
+  if (inverse) FixedFft<T, N>::c2r(ctx, c, tw, (T)scale, cc, rc, pv, tab);
+  else FixedFft<T, N>::r2c(ctx, c, tw, (T)scale, cc, rc, pv, tab);
 }
 
 // power-of-two sizes 32..1024 use the fixed-length passes
@@ -1071,6 +1251,22 @@ int rows_per_cta(int N) {
 }
 
 }  // namespace
+
+int *FftTables::wait_flag() {
+  if (!wait_flag_host) {
+    void *h = nullptr, *d = nullptr;
+    GIC_CUDA(cudaHostAlloc(&h, sizeof(int), cudaHostAllocMapped));
+    *static_cast<int *>(h) = 0;
+    if (cudaHostGetDevicePointer(&d, h, 0) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFreeHost(h);
+      fail(GIC_ERR_CUDA, "cudaHostGetDevicePointer failed");
+    }
+    wait_flag_host = static_cast<int *>(h);
+    wait_flag_dev = static_cast<int *>(d);
+  }
+  return wait_flag_dev;
+}
 
 const void *FftTables::get(int n, bool dbl, cudaStream_t s) {
   for (auto &e : entries)
@@ -1136,6 +1332,14 @@ void fft_r2c_3d(Context &ctx, T *data, int n, double scale, const double *post_t
   launched();
   strided_pass<T>(ctx, c, n, n, S, -1, (T)1, tw);
   strided_pass<T>(ctx, c, 1, n, (long long)n * S, -1, (T)scale, tw, post_tab);
+}
+
+bool take_fft_wait_error(Context &ctx) {
+  volatile int *f = ctx.fft.wait_flag_host;
+  if (!f || *f == 0) return false;
+  *f = 0;
+  ctx.last_error = "FFT plane pass: a wait for another CTA's tiles gave up; results of the transform are invalid";
+  return true;
 }
 
 template void fft_c2r_3d<float>(Context &, float *, int, double, const double *);

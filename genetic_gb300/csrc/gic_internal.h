@@ -131,13 +131,26 @@ struct FftTables {
   const void *get(int n, bool dbl, cudaStream_t s);
   // tile widths of the fixed-length passes chosen by timing the candidates on
   // first use, per size and precision (the choice does not change any result)
+  // planes: variant of the plane pass that replaces the y and z passes, or -1 (none)
   struct Tuned {
     int n;
     bool dbl;
-    int cols, rows;
+    int cols, rows, planes;
   };
   std::vector<Tuned> tuned;
   int force_cols = -1, force_rows = -1;  // >= 0: use this candidate (tests)
+  int force_planes = -2;                 // -2: tuned, -1: separate y and z passes, >= 0: this variant
+  // plane pass: N plane counters and a ticket, zeroed before each launch; a word of
+  // mapped host memory the kernel sets when one of its waits gives up
+  DevBuf plane_sync;
+  int *wait_flag_host = nullptr, *wait_flag_dev = nullptr;
+  int *wait_flag();
+  FftTables() = default;
+  FftTables(const FftTables &) = delete;
+  FftTables &operator=(const FftTables &) = delete;
+  ~FftTables() {
+    if (wait_flag_host) cudaFreeHost(wait_flag_host);
+  }
 };
 
 struct RngScratch {
@@ -188,6 +201,9 @@ template <typename T>
 void fft_c2r_3d(Context &ctx, T *data, int n, double scale, const double *pre_tab = nullptr);
 template <typename T>
 void fft_r2c_3d(Context &ctx, T *data, int n, double scale, const double *post_tab = nullptr);
+// after the stream has synchronised: true (with ctx.last_error set) when a wait of the
+// plane pass gave up since the last check; clears the flag
+bool take_fft_wait_error(Context &ctx);
 
 // rng.cu
 void draw_noise_all(Context &ctx, unsigned long long seed, int mode);
