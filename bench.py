@@ -46,6 +46,10 @@ WORKLOADS = {
                               seed_cmd='random_seed', precision='fp64', replaced=128 ** 3, mods=MODS4, order=2),
     'zoom256': dict(levels=[('base', 100.0, 256), ('zoom', 96, 96, 96, 4, 256)], seed_cmd='random_seed',
                     precision='mixed', replaced=64 ** 3),
+    # the headline layout at 384^3 (fields of 0.23 GB, above L2; a few GB on the device):
+    # the case kernel profiles of the modification algebra are captured on
+    'zoom384': dict(levels=[('base', 100.0, 384), ('zoom', 144, 144, 144, 4, 384)], seed_cmd='random_seed',
+                    precision='mixed', replaced=96 ** 3, mods=MODS4),
     # 512^3 single level, 100 Mpc/h box (the single-level configuration at 512^3)
     'za512': dict(levels=[('base', 100.0, 512)], seed_cmd='random_seed', precision='mixed'),
     'za512_fp64': dict(levels=[('base', 100.0, 512)], seed_cmd='random_seed', precision='fp64'),
@@ -188,7 +192,7 @@ def profiled_traffic(kernel):
 
 
 def fft_roofline(gen, wl, stream, reps=20):
-    """Average device time of one inverse 3-D FFT of the finest level's delta field."""
+    """Average device time of one inverse 3-D FFT of the finest level's x displacement field."""
     import torch
     from genetic_gb300 import _lib
     level = len(wl['levels']) - 1
@@ -197,14 +201,14 @@ def fft_roofline(gen, wl, stream, reps=20):
     nc = n * n * (n // 2 + 1)
     # the field is in real space after a realisation: forward then inverse keeps it meaningful
     for _ in range(3):
-        gen._call('gic_fft', level, _lib.GIC_FIELD_DELTA, -1)
-        gen._call('gic_fft', level, _lib.GIC_FIELD_DELTA, +1)
+        gen._call('gic_fft', level, _lib.GIC_FIELD_PSI_X, -1)
+        gen._call('gic_fft', level, _lib.GIC_FIELD_PSI_X, +1)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * reps + 1)]
     times = []
     for r in range(reps):
-        gen._call('gic_fft', level, _lib.GIC_FIELD_DELTA, -1)
+        gen._call('gic_fft', level, _lib.GIC_FIELD_PSI_X, -1)
         ev[2 * r].record(stream)
-        gen._call('gic_fft', level, _lib.GIC_FIELD_DELTA, +1)
+        gen._call('gic_fft', level, _lib.GIC_FIELD_PSI_X, +1)
         ev[2 * r + 1].record(stream)
     torch.cuda.synchronize()
     for r in range(reps):

@@ -77,6 +77,7 @@ SIGNATURES = {
     'gic_fetch_level': [_P, _I, _I, _D],
     'gic_fetch_particles': [_P, _I, _D, _D],
     'gic_fft': [_P, _I, _I, _I],
+    'gic_fft_box': [_P, _I, _I, _I, _P, _P],
     'gic_chi2': [_P, _D],
     'gic_launch_count': [ctypes.POINTER(ctypes.c_ulonglong)],
     'gic_calculate': [_P, _I, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_size_t, _D],

@@ -250,6 +250,7 @@ GIC_API int gic_batch_realise(gic_batch *b, const unsigned long *seeds, const in
     for (auto *c : b->ctxs)
       for (auto &L : c->impl.levels) {
         L->have_fields = true;
+        L->have_delta = false;  // delta is made on demand from the new fields
         if (order == 2) L->have_lpt2 = true;
       }
   } catch (const gic::Error &e) {

@@ -104,6 +104,7 @@ void fetch_typed(Context &c, Level &L, int what, double *host) {
   } else {
     if (!L.have_fields) fail(GIC_ERR_NOT_READY, "fields have not been computed");
     if (what >= GIC_FIELD_PSI2_X && !L.have_lpt2) fail(GIC_ERR_NOT_READY, "second-order fields have not been computed");
+    if (what == GIC_FIELD_DELTA) ensure_delta(c);
     DevBuf &src = what >= GIC_FIELD_PSI2_X ? L.field2[what - GIC_FIELD_PSI2_X] : L.field[what - GIC_FIELD_DELTA];
     size_t m = L.ncells();
     c.reduce.ensure(m * sizeof(double));
@@ -383,6 +384,10 @@ int gic_fft(gic_ctx *ctx, int level, int what, int dir) {
   if (dir != -1 && dir != 1) gic::fail(GIC_ERR_INVALID_ARG, "dir must be -1 (forward) or +1 (inverse)");
   gic::DevBuf *buf = what == GIC_FIELD_NOISE ? &L.noise : (what >= GIC_FIELD_DELTA && what <= GIC_FIELD_PSI_Z ? &L.field[what - 1] : nullptr);
   if (!buf || !buf->ptr) gic::fail(GIC_ERR_NOT_READY, "field not allocated");
+  if (what == GIC_FIELD_DELTA) {
+    gic::ensure_delta(C);
+    L.have_delta = false;  // transformed in place
+  }
   double scale = 1.0 / std::pow((double)L.n, 1.5);
   if (C.dbl()) {
     if (dir < 0) gic::fft_r2c_3d<double>(C, buf->as<double>(), L.n, scale);
@@ -390,6 +395,34 @@ int gic_fft(gic_ctx *ctx, int level, int what, int dir) {
   } else {
     if (dir < 0) gic::fft_r2c_3d<float>(C, buf->as<float>(), L.n, scale);
     else gic::fft_c2r_3d<float>(C, buf->as<float>(), L.n, scale);
+  }
+  GIC_CUDA(cudaStreamSynchronize(C.stream));
+  API_END
+}
+
+int gic_fft_box(gic_ctx *ctx, int level, int what, int dir, const int *start, const int *len) {
+  API_BEGIN(ctx)
+  gic::Level &L = gic::level_at(C, level);
+  if (dir != -1 && dir != 1) gic::fail(GIC_ERR_INVALID_ARG, "dir must be -1 (forward) or +1 (inverse)");
+  if (!start || !len) gic::fail(GIC_ERR_INVALID_ARG, "null box");
+  gic::DevBuf *buf = what == GIC_FIELD_NOISE ? &L.noise : (what >= GIC_FIELD_DELTA && what <= GIC_FIELD_PSI_Z ? &L.field[what - 1] : nullptr);
+  if (!buf || !buf->ptr) gic::fail(GIC_ERR_NOT_READY, "field not allocated");
+  if (what == GIC_FIELD_DELTA) {
+    gic::ensure_delta(C);
+    L.have_delta = false;  // transformed in place
+  }
+  gic::CellBox box;
+  for (int a = 0; a < 3; ++a) {
+    if (len[a] < 1 || len[a] > L.n) gic::fail(GIC_ERR_INVALID_ARG, "box lengths must be in [1, n]");
+    box.set_axis(a, start[a], (long long)start[a] + len[a], 0, L.n);
+  }
+  double scale = 1.0 / std::pow((double)L.n, 1.5);
+  if (C.dbl()) {
+    if (dir < 0) gic::fft_r2c_3d<double>(C, buf->as<double>(), L.n, scale, nullptr, &box);
+    else gic::fft_c2r_3d<double>(C, buf->as<double>(), L.n, scale, nullptr, &box);
+  } else {
+    if (dir < 0) gic::fft_r2c_3d<float>(C, buf->as<float>(), L.n, scale, nullptr, &box);
+    else gic::fft_c2r_3d<float>(C, buf->as<float>(), L.n, scale, nullptr, &box);
   }
   GIC_CUDA(cudaStreamSynchronize(C.stream));
   API_END

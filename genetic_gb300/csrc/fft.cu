@@ -493,18 +493,20 @@ struct TileStages<T, L, TC, TCP, NT, NS, SIGN, TWM, true> {
   static __device__ __forceinline__ void run(typename Cx<T>::type *, const typename Cx<T>::type *) {}
 };
 
-// strided pass over (A, L, B) complex, transform along L; grid (ceil(B / TC), A)
+// strided pass over (A, L, B) complex, transform along L; grid (ceil(B / TC), na):
+// planes (a0 + blockIdx.y) mod A, na <= A of them
 // tab: optional per-|k|^2 multiplier (x pass only, B = L (L/2 + 1)): applied to
 // the inputs when SIGN > 0 (c2r) and to the scaled outputs when SIGN < 0 (r2c)
 template <typename T, int L, int TC, int NT, int SIGN>
 __global__ void __launch_bounds__(NT) k_fft_cols(typename Cx<T>::type *data, long long B,
-                                                 const typename Cx<T>::type *tw, T scale, const double *tab) {
+                                                 const typename Cx<T>::type *tw, T scale, const double *tab, int a0,
+                                                 int A) {
   using C = typename Cx<T>::type;
   constexpr int TCP = TC + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
   C *tile = reinterpret_cast<C *>(smraw);
   const long long b0 = (long long)blockIdx.x * TC;
-  C *base = data + (size_t)blockIdx.y * (size_t)L * (size_t)B + b0;
+  C *base = data + (size_t)((a0 + (int)blockIdx.y) % A) * (size_t)L * (size_t)B + b0;
   const int tcv = (int)min((long long)TC, B - b0);
   for (int e = threadIdx.x; e < L * TC; e += NT) {
     const int i = e / TC, c = e % TC;
@@ -534,6 +536,34 @@ __global__ void __launch_bounds__(NT) k_fft_cols(typename Cx<T>::type *data, lon
       if (SIGN < 0 && tab) v = cscale(v, (T)qtab(tab, L, i, b0 + c));
       base[(size_t)i * (size_t)B + c] = v;
     }
+  }
+}
+
+// First row of the row tile a CTA of a fixed-length row pass owns: grid (tiles, planes),
+// plane (x0 + blockIdx.y) mod N, tile (ty0 + blockIdx.x) mod (N / RPC) of RPC rows.
+// The whole transform is x0 = ty0 = 0 on an (N / RPC, N) grid; a box of rows is a
+// cyclic range of planes times a cyclic range of tiles.
+template <int N, int RPC>
+__device__ __forceinline__ long long row_tile_start(int x0, int ty0) {
+  const int plane = (x0 + (int)blockIdx.y) % N, tile = (ty0 + (int)blockIdx.x) % (N / RPC);
+  return (long long)plane * N + (long long)tile * RPC;
+}
+
+// the padding word (coefficient N/2) of every row outside the box's row tiles, zeroed:
+// a forward transform whose input is zero outside the box skips those rows, and their
+// spectra are then zero only if this word, not read as input, is zero too
+template <typename C>
+__global__ void k_zero_row_tails(C *data, int N, int x0, int nx, int ty0, int nty, int rpc) {
+  const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= (long long)N * N) return;
+  const int x = (int)(row / N), y = (int)(row % N);
+  const int ntile = N / rpc;
+  const bool in = (x - x0 + N) % N < nx && (y / rpc - ty0 + ntile) % ntile < nty;
+  if (!in) {
+    C z;
+    z.x = 0;
+    z.y = 0;
+    data[row * (N / 2 + 1) + N / 2] = z;
   }
 }
 
@@ -692,12 +722,13 @@ struct RowsIn {
 
 template <typename T, int L, int TC, int NT, int SIGN>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_fft_cols_fused(typename Cx<T>::type *data, long long B,
-                                                       const typename Cx<T>::type *tw, T scale, const double *tab) {
+                                                       const typename Cx<T>::type *tw, T scale, const double *tab,
+                                                       int a0, int A) {
   using C = typename Cx<T>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
   C *tile = reinterpret_cast<C *>(smraw);
   const long long b0 = (long long)blockIdx.x * TC;
-  C *base = data + (size_t)blockIdx.y * (size_t)L * (size_t)B + b0;
+  C *base = data + (size_t)((a0 + (int)blockIdx.y) % A) * (size_t)L * (size_t)B + b0;
   const int tcv = (int)min((long long)TC, B - b0);
   first_stage_from<T, L, TC, NT, SIGN>(tile, ColsIn<C>{base, B, tcv, SIGN > 0 ? tab : nullptr, L, b0});
   constexpr int R0 = next_radix(L, 1), NSL = last_stage_ns(L);
@@ -706,14 +737,14 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_fft_cols_fused(typename Cx<T>
 }
 
 template <typename T, int H, int RPC, int NT>
-__global__ void __launch_bounds__(NT, 1024 / NT) k_fft_rows_c2r_fused(typename Cx<T>::type *data, long long nrows,
+__global__ void __launch_bounds__(NT, 1024 / NT) k_fft_rows_c2r_fused(typename Cx<T>::type *data, int x0, int ty0,
                                                            const typename Cx<T>::type *tw, T scale) {
   using C = typename Cx<T>::type;
   constexpr int S = H + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
   C *tile = reinterpret_cast<C *>(smraw);
-  const long long r0 = (long long)blockIdx.x * RPC;
-  const int rows_valid = (int)min((long long)RPC, nrows - r0);
+  const long long r0 = row_tile_start<2 * H, RPC>(x0, ty0);
+  const int rows_valid = RPC;
   C *base = data + (size_t)r0 * S;
   first_stage_from<T, H, RPC, NT, +1>(tile, RowsC2RIn<C>{base, tw, S, H, rows_valid});
   constexpr int R0 = next_radix(H, 1), NSL = last_stage_ns(H);
@@ -722,14 +753,14 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_fft_rows_c2r_fused(typename C
 }
 
 template <typename T, int H, int RPC, int NT>
-__global__ void __launch_bounds__(NT, 1024 / NT) k_fft_rows_r2c_fused(typename Cx<T>::type *data, long long nrows,
+__global__ void __launch_bounds__(NT, 1024 / NT) k_fft_rows_r2c_fused(typename Cx<T>::type *data, int x0, int ty0,
                                                            const typename Cx<T>::type *tw, T scale) {
   using C = typename Cx<T>::type;
   constexpr int S = H + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
   C *tile = reinterpret_cast<C *>(smraw);  // [H + 1][RPC]
-  const long long r0 = (long long)blockIdx.x * RPC;
-  const int rows_valid = (int)min((long long)RPC, nrows - r0);
+  const long long r0 = row_tile_start<2 * H, RPC>(x0, ty0);
+  const int rows_valid = RPC;
   C *base = data + (size_t)r0 * S;
   first_stage_from<T, H, RPC, NT, -1>(tile, RowsIn<C>{base, S, rows_valid});
   constexpr int R0 = next_radix(H, 1);
@@ -800,14 +831,14 @@ __device__ __forceinline__ void rows_c2r_tile(typename Cx<T>::type *tile, typena
 // (coalesced) into a tile [H + 1][RPC + 1] with one row per tile column, packed
 // into H complex values, transformed, and copied back as N reals per row.
 template <typename T, int H, int RPC, int NT>
-__global__ void __launch_bounds__(NT) k_fft_rows_c2r_fixed(typename Cx<T>::type *data, long long nrows,
+__global__ void __launch_bounds__(NT) k_fft_rows_c2r_fixed(typename Cx<T>::type *data, int x0, int ty0,
                                                            const typename Cx<T>::type *tw, T scale) {
   using C = typename Cx<T>::type;
   constexpr int S = H + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
   C *tile = reinterpret_cast<C *>(smraw);
-  const long long r0 = (long long)blockIdx.x * RPC;
-  const int rows_valid = (int)min((long long)RPC, nrows - r0);
+  const long long r0 = row_tile_start<2 * H, RPC>(x0, ty0);
+  const int rows_valid = RPC;
   rows_c2r_tile<T, H, RPC, NT, false>(tile, data + (size_t)r0 * S, rows_valid, tw, scale);
 }
 
@@ -849,14 +880,14 @@ __device__ __forceinline__ void rows_r2c_tile(typename Cx<T>::type *tile, typena
 }
 
 template <typename T, int H, int RPC, int NT>
-__global__ void __launch_bounds__(NT) k_fft_rows_r2c_fixed(typename Cx<T>::type *data, long long nrows,
+__global__ void __launch_bounds__(NT) k_fft_rows_r2c_fixed(typename Cx<T>::type *data, int x0, int ty0,
                                                            const typename Cx<T>::type *tw, T scale) {
   using C = typename Cx<T>::type;
   constexpr int S = H + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
   C *tile = reinterpret_cast<C *>(smraw);
-  const long long r0 = (long long)blockIdx.x * RPC;
-  const int rows_valid = (int)min((long long)RPC, nrows - r0);
+  const long long r0 = row_tile_start<2 * H, RPC>(x0, ty0);
+  const int rows_valid = RPC;
   rows_r2c_tile<T, H, RPC, NT, false>(tile, data + (size_t)r0 * S, rows_valid, tw, scale);
 }
 
@@ -991,83 +1022,107 @@ struct FixedFft {
   static constexpr int H = N / 2, S = H + 1;
   static constexpr bool F32 = sizeof(T) == 4;
 
+  // planes and rows of a box (the whole transform: x0 = y0 = 0, nx = ny = N)
+  struct Sel {
+    int x0, nx, y0, ny;
+    bool whole() const { return nx >= N && ny >= N; }
+  };
+  static Sel whole_sel() { return Sel{0, N, 0, N}; }
+
   template <int TC, int NT, int SIGN>
-  static void cols(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const double *tab) {
+  static void cols(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const double *tab, int a0, int na) {
     static std::atomic<int> mask{0};
     const size_t smem = (size_t)N * (TC + 1) * sizeof(C);
     set_smem_once((const void *)k_fft_cols<T, N, TC, NT, SIGN>, smem, mask);
-    dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)A);
-    k_fft_cols<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab);
+    dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)na);
+    k_fft_cols<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A);
     launched();
   }
   template <int TC, int NT, int SIGN>
-  static void cols_fused(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const double *tab) {
+  static void cols_fused(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const double *tab, int a0,
+                         int na) {
     static std::atomic<int> mask{0};
     const size_t smem = (size_t)N * TC * sizeof(C);
     set_smem_once((const void *)k_fft_cols_fused<T, N, TC, NT, SIGN>, smem, mask);
-    dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)A);
-    k_fft_cols_fused<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab);
+    dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)na);
+    k_fft_cols_fused<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A);
     launched();
   }
+  // row tiles of RPC rows covering the selection: grid (tiles, planes); for a
+  // forward transform of a partial selection, the other rows' padding words zeroed
+  template <int RPC>
+  static dim3 row_grid(Context &ctx, C *d, const Sel &sel, bool inverse, int &ty0) {
+    constexpr int NTILE = N / RPC;
+    ty0 = sel.y0 / RPC;
+    const int nty = std::min(NTILE, (sel.y0 + sel.ny - 1) / RPC - ty0 + 1);
+    if (!inverse && !sel.whole()) {
+      const long long nrows = (long long)N * N;
+      k_zero_row_tails<C><<<(unsigned)((nrows + 255) / 256), 256, 0, ctx.stream>>>(d, N, sel.x0, sel.nx, ty0, nty, RPC);
+      launched();
+    }
+    return dim3((unsigned)nty, (unsigned)sel.nx);
+  }
   template <int RPC, int NT, bool INV>
-  static void rows_fused(Context &ctx, C *d, const C *tw, T scale) {
+  static void rows_fused(Context &ctx, C *d, const C *tw, T scale, const Sel &sel) {
     static std::atomic<int> mask{0};
     const size_t smem = (size_t)(INV ? H : S) * RPC * sizeof(C);
-    const long long nrows = (long long)N * N;
-    const unsigned grid = (unsigned)((nrows + RPC - 1) / RPC);
+    int ty0 = 0;
+    const dim3 grid = row_grid<RPC>(ctx, d, sel, INV, ty0);
     if (INV) {
       set_smem_once((const void *)k_fft_rows_c2r_fused<T, H, RPC, NT>, smem, mask);
-      k_fft_rows_c2r_fused<T, H, RPC, NT><<<grid, NT, smem, ctx.stream>>>(d, nrows, tw, scale);
+      k_fft_rows_c2r_fused<T, H, RPC, NT><<<grid, NT, smem, ctx.stream>>>(d, sel.x0, ty0, tw, scale);
     } else {
       set_smem_once((const void *)k_fft_rows_r2c_fused<T, H, RPC, NT>, smem, mask);
-      k_fft_rows_r2c_fused<T, H, RPC, NT><<<grid, NT, smem, ctx.stream>>>(d, nrows, tw, scale);
+      k_fft_rows_r2c_fused<T, H, RPC, NT><<<grid, NT, smem, ctx.stream>>>(d, sel.x0, ty0, tw, scale);
     }
     launched();
   }
   template <int RPC, int NT, bool INV>
-  static void rows(Context &ctx, C *d, const C *tw, T scale) {
+  static void rows(Context &ctx, C *d, const C *tw, T scale, const Sel &sel) {
     static std::atomic<int> mask{0};
     const size_t smem = (size_t)S * (RPC + 1) * sizeof(C);
-    const long long nrows = (long long)N * N;
-    const unsigned grid = (unsigned)((nrows + RPC - 1) / RPC);
+    int ty0 = 0;
+    const dim3 grid = row_grid<RPC>(ctx, d, sel, INV, ty0);
     if (INV) {
       set_smem_once((const void *)k_fft_rows_c2r_fixed<T, H, RPC, NT>, smem, mask);
-      k_fft_rows_c2r_fixed<T, H, RPC, NT><<<grid, NT, smem, ctx.stream>>>(d, nrows, tw, scale);
+      k_fft_rows_c2r_fixed<T, H, RPC, NT><<<grid, NT, smem, ctx.stream>>>(d, sel.x0, ty0, tw, scale);
     } else {
       set_smem_once((const void *)k_fft_rows_r2c_fixed<T, H, RPC, NT>, smem, mask);
-      k_fft_rows_r2c_fixed<T, H, RPC, NT><<<grid, NT, smem, ctx.stream>>>(d, nrows, tw, scale);
+      k_fft_rows_r2c_fixed<T, H, RPC, NT><<<grid, NT, smem, ctx.stream>>>(d, sel.x0, ty0, tw, scale);
     }
     launched();
   }
+  // a0, na: the planes (a0 + i) mod A, i < na, of the strided pass (na < 0: all A)
   static void cols_cfg(Context &ctx, int cfg, int sign, C *d, int A, long long B, const C *tw, T scale,
-                       const double *tab = nullptr) {
+                       const double *tab = nullptr, int a0 = 0, int na = -1) {
+    if (na < 0) na = A;
     if (cfg == 2) {
-      if (sign > 0) cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab);
-      else cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale, tab);
+      if (sign > 0) cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na);
+      else cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na);
     } else if (cfg == 3) {
-      if (sign > 0) cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, +1>(ctx, d, A, B, tw, scale, tab);
-      else cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, -1>(ctx, d, A, B, tw, scale, tab);
+      if (sign > 0) cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, +1>(ctx, d, A, B, tw, scale, tab, a0, na);
+      else cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, -1>(ctx, d, A, B, tw, scale, tab, a0, na);
     } else if (cfg == 0) {
-      if (sign > 0) cols<F32 ? 8 : 4, 256, +1>(ctx, d, A, B, tw, scale, tab);
-      else cols<F32 ? 8 : 4, 256, -1>(ctx, d, A, B, tw, scale, tab);
+      if (sign > 0) cols<F32 ? 8 : 4, 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na);
+      else cols<F32 ? 8 : 4, 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na);
     } else {
-      if (sign > 0) cols<F32 ? 16 : 8, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab);
-      else cols<F32 ? 16 : 8, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale, tab);
+      if (sign > 0) cols<F32 ? 16 : 8, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na);
+      else cols<F32 ? 16 : 8, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na);
     }
   }
-  static void rows_cfg(Context &ctx, int cfg, bool inv, C *d, const C *tw, T scale) {
+  static void rows_cfg(Context &ctx, int cfg, bool inv, C *d, const C *tw, T scale, const Sel &sel = whole_sel()) {
     if (cfg == 2) {
-      if (inv) rows_fused<F32 ? 16 : 8, 256, true>(ctx, d, tw, scale);
-      else rows_fused<F32 ? 16 : 8, 256, false>(ctx, d, tw, scale);
+      if (inv) rows_fused<F32 ? 16 : 8, 256, true>(ctx, d, tw, scale, sel);
+      else rows_fused<F32 ? 16 : 8, 256, false>(ctx, d, tw, scale, sel);
     } else if (cfg == 3) {
-      if (inv) rows<F32 ? 32 : 16, 512, true>(ctx, d, tw, scale);
-      else rows<F32 ? 32 : 16, 512, false>(ctx, d, tw, scale);
+      if (inv) rows<F32 ? 32 : 16, 512, true>(ctx, d, tw, scale, sel);
+      else rows<F32 ? 32 : 16, 512, false>(ctx, d, tw, scale, sel);
     } else if (cfg == 0) {
-      if (inv) rows<F32 ? 8 : 4, 256, true>(ctx, d, tw, scale);
-      else rows<F32 ? 8 : 4, 256, false>(ctx, d, tw, scale);
+      if (inv) rows<F32 ? 8 : 4, 256, true>(ctx, d, tw, scale, sel);
+      else rows<F32 ? 8 : 4, 256, false>(ctx, d, tw, scale, sel);
     } else {
-      if (inv) rows<F32 ? 16 : 8, 256, true>(ctx, d, tw, scale);
-      else rows<F32 ? 16 : 8, 256, false>(ctx, d, tw, scale);
+      if (inv) rows<F32 ? 16 : 8, 256, true>(ctx, d, tw, scale, sel);
+      else rows<F32 ? 16 : 8, 256, false>(ctx, d, tw, scale, sel);
     }
   }
   // plane pass (N >= 256 in FP32, N >= 512 in FP64): column tiles and row tiles sized for 512 threads and about
@@ -1107,21 +1162,27 @@ struct FixedFft {
       launched();
     }
   }
-  static void c2r(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, int pv, const double *tab) {
+  // inverse: the x pass over every column, then the y transforms of the selected
+  // planes and the real transforms of the selected rows (output valid there)
+  static void c2r(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, int pv, const double *tab,
+                  const Sel &sel) {
     cols_cfg(ctx, ccfg, +1, c, 1, (long long)N * S, tw, (T)1, tab);
-    if (kPlanes && pv >= 0) {
+    if (kPlanes && pv >= 0 && sel.whole()) {
       planes<true>(ctx, c, tw, scale, pv);
       return;
     }
-    cols_cfg(ctx, ccfg, +1, c, N, S, tw, (T)1);
-    rows_cfg(ctx, rcfg, true, c, tw, scale);
+    cols_cfg(ctx, ccfg, +1, c, N, S, tw, (T)1, nullptr, sel.x0, sel.nx);
+    rows_cfg(ctx, rcfg, true, c, tw, scale, sel);
   }
-  static void r2c(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, int pv, const double *tab) {
-    if (kPlanes && pv >= 0) {
+  // forward, input zero outside the selection: the selected rows, the selected
+  // planes' y transforms, then the x pass over every column
+  static void r2c(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, int pv, const double *tab,
+                  const Sel &sel) {
+    if (kPlanes && pv >= 0 && sel.whole()) {
       planes<false>(ctx, c, tw, (T)1, pv);
     } else {
-      rows_cfg(ctx, rcfg, false, c, tw, (T)1);
-      cols_cfg(ctx, ccfg, -1, c, N, S, tw, (T)1);
+      rows_cfg(ctx, rcfg, false, c, tw, (T)1, sel);
+      cols_cfg(ctx, ccfg, -1, c, N, S, tw, (T)1, nullptr, sel.x0, sel.nx);
     }
     cols_cfg(ctx, ccfg, -1, c, 1, (long long)N * S, tw, scale, tab);
   }
@@ -1182,7 +1243,7 @@ std::vector<SharedTune> g_tuned;
 
 template <typename T, int N>
 void fixed_transform(Context &ctx, typename Cx<T>::type *c, const typename Cx<T>::type *tw, double scale, bool inverse,
-                     const double *tab) {
+                     const double *tab, const CellBox *box) {
   FftTables &F = ctx.fft;
   const bool dbl = sizeof(T) == 8;
   int cc = -1, rc = -1, pv = -1;
@@ -1212,21 +1273,30 @@ void fixed_transform(Context &ctx, typename Cx<T>::type *c, const typename Cx<T>
   if (F.force_cols >= 0) cc = F.force_cols;
   if (F.force_rows >= 0) rc = F.force_rows;
   if (F.force_planes >= -1) pv = std::min(F.force_planes, FixedFft<T, N>::kPlaneVariants - 1);
-  if (inverse) FixedFft<T, N>::c2r(ctx, c, tw, (T)scale, cc, rc, pv, tab);
-  else FixedFft<T, N>::r2c(ctx, c, tw, (T)scale, cc, rc, pv, tab);
+  typename FixedFft<T, N>::Sel sel = FixedFft<T, N>::whole_sel();
+  if (box && box->len[0] < N) {
+    sel.x0 = ((box->start[0] % N) + N) % N;
+    sel.nx = box->len[0];
+  }
+  if (box && box->len[1] < N) {
+    sel.y0 = ((box->start[1] % N) + N) % N;
+    sel.ny = box->len[1];
+  }
+  if (inverse) FixedFft<T, N>::c2r(ctx, c, tw, (T)scale, cc, rc, pv, tab, sel);
+  else FixedFft<T, N>::r2c(ctx, c, tw, (T)scale, cc, rc, pv, tab, sel);
 }
 
 // power-of-two sizes 32..1024 use the fixed-length passes
 template <typename T>
 bool fixed_dispatch(Context &ctx, typename Cx<T>::type *c, int n, const typename Cx<T>::type *tw, double scale,
-                    bool inverse, const double *tab) {
+                    bool inverse, const double *tab, const CellBox *box) {
   switch (n) {
-    case 32: fixed_transform<T, 32>(ctx, c, tw, scale, inverse, tab); return true;
-    case 64: fixed_transform<T, 64>(ctx, c, tw, scale, inverse, tab); return true;
-    case 128: fixed_transform<T, 128>(ctx, c, tw, scale, inverse, tab); return true;
-    case 256: fixed_transform<T, 256>(ctx, c, tw, scale, inverse, tab); return true;
-    case 512: fixed_transform<T, 512>(ctx, c, tw, scale, inverse, tab); return true;
-    case 1024: fixed_transform<T, 1024>(ctx, c, tw, scale, inverse, tab); return true;
+    case 32: fixed_transform<T, 32>(ctx, c, tw, scale, inverse, tab, box); return true;
+    case 64: fixed_transform<T, 64>(ctx, c, tw, scale, inverse, tab, box); return true;
+    case 128: fixed_transform<T, 128>(ctx, c, tw, scale, inverse, tab, box); return true;
+    case 256: fixed_transform<T, 256>(ctx, c, tw, scale, inverse, tab, box); return true;
+    case 512: fixed_transform<T, 512>(ctx, c, tw, scale, inverse, tab, box); return true;
+    case 1024: fixed_transform<T, 1024>(ctx, c, tw, scale, inverse, tab, box); return true;
     default: return false;
   }
 }
@@ -1292,7 +1362,7 @@ const void *FftTables::get(int n, bool dbl, cudaStream_t s) {
 }
 
 template <typename T>
-void fft_c2r_3d(Context &ctx, T *data, int n, double scale, const double *pre_tab) {
+void fft_c2r_3d(Context &ctx, T *data, int n, double scale, const double *pre_tab, const CellBox *box) {
   using C = typename Cx<T>::type;
   if (n < 2 || n % 2) fail(GIC_ERR_INVALID_ARG, "FFT size must be even");
   const C *tw = (const C *)ctx.fft.get(n, sizeof(T) == 8, ctx.stream);
@@ -1301,7 +1371,7 @@ void fft_c2r_3d(Context &ctx, T *data, int n, double scale, const double *pre_ta
   long long mirror_threads = 2ll * n * n;
   k_mirror<T><<<(unsigned)((mirror_threads + 255) / 256), 256, 0, ctx.stream>>>(c, n);
   launched();
-  if (ctx.fft.force_cols != -2 && fixed_dispatch<T>(ctx, c, n, tw, scale, true, pre_tab)) return;
+  if (ctx.fft.force_cols != -2 && fixed_dispatch<T>(ctx, c, n, tw, scale, true, pre_tab, box)) return;
   strided_pass<T>(ctx, c, 1, n, (long long)n * S, +1, (T)1, tw, pre_tab);
   strided_pass<T>(ctx, c, n, n, S, +1, (T)1, tw);
   int rpc = rows_per_cta<T>(n);
@@ -1315,13 +1385,13 @@ void fft_c2r_3d(Context &ctx, T *data, int n, double scale, const double *pre_ta
 }
 
 template <typename T>
-void fft_r2c_3d(Context &ctx, T *data, int n, double scale, const double *post_tab) {
+void fft_r2c_3d(Context &ctx, T *data, int n, double scale, const double *post_tab, const CellBox *box) {
   using C = typename Cx<T>::type;
   if (n < 2 || n % 2) fail(GIC_ERR_INVALID_ARG, "FFT size must be even");
   const C *tw = (const C *)ctx.fft.get(n, sizeof(T) == 8, ctx.stream);
   C *c = reinterpret_cast<C *>(data);
   long long S = n / 2 + 1;
-  if (ctx.fft.force_cols != -2 && fixed_dispatch<T>(ctx, c, n, tw, scale, false, post_tab)) return;
+  if (ctx.fft.force_cols != -2 && fixed_dispatch<T>(ctx, c, n, tw, scale, false, post_tab, box)) return;
   int rpc = rows_per_cta<T>(n);
   Radix plan = make_plan(n / 2);
   size_t smem = 2ull * rpc * S * sizeof(C);
@@ -1342,9 +1412,9 @@ bool take_fft_wait_error(Context &ctx) {
   return true;
 }
 
-template void fft_c2r_3d<float>(Context &, float *, int, double, const double *);
-template void fft_c2r_3d<double>(Context &, double *, int, double, const double *);
-template void fft_r2c_3d<float>(Context &, float *, int, double, const double *);
-template void fft_r2c_3d<double>(Context &, double *, int, double, const double *);
+template void fft_c2r_3d<float>(Context &, float *, int, double, const double *, const CellBox *);
+template void fft_c2r_3d<double>(Context &, double *, int, double, const double *, const CellBox *);
+template void fft_r2c_3d<float>(Context &, float *, int, double, const double *, const CellBox *);
+template void fft_r2c_3d<double>(Context &, double *, int, double, const double *, const CellBox *);
 
 }  // namespace gic

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
+#include <cmath>
 #include <vector>
 #include <memory>
 #include "../../include/gicgpu.h"
@@ -103,7 +104,8 @@ struct Level {
   DevBuf field2[3];      // second-order displacements psi2_x, psi2_y, psi2_z (real)
   DevBuf pos, vel;       // particles: pos double[3M], vel (precision)[3M]
   bool have_noise = false;
-  bool have_fields = false;
+  bool have_fields = false;  // displacements in real space
+  bool have_delta = false;   // delta in real space (made on demand)
   bool have_lpt2 = false;
 };
 
@@ -195,12 +197,50 @@ struct Context {
 };
 
 // fft.cu
+// A box of an n^3 grid's cells: per axis the cyclic range [start, start + len) mod n.
+// Given to a forward transform, its input is zero outside the box; given to an
+// inverse transform, only its output inside the box is wanted.  The fixed-length
+// transforms then skip the x planes and y rows outside it (the z range is not used);
+// the values they produce for the box are the same bits as the whole transform's.
+struct CellBox {
+  int start[3] = {0, 0, 0}, len[3] = {0, 0, 0};
+  static CellBox whole(int n) {
+    CellBox b;
+    for (int a = 0; a < 3; ++a) b.len[a] = n;
+    return b;
+  }
+  // per axis [lo - margin, hi + margin) of a cyclic axis of n cells (any lo, hi)
+  void set_axis(int a, long long lo, long long hi, int margin, int n) {
+    long long len_ = hi - lo + 2ll * margin;
+    if (len_ >= n || len_ <= 0) {
+      start[a] = 0;
+      len[a] = n;
+      return;
+    }
+    start[a] = (int)((((lo - margin) % n) + n) % n);
+    len[a] = (int)len_;
+  }
+};
+// cells of the coarse level that the fine level covers, `margin` extra cells each side
+inline CellBox footprint_box(const Level &fine, const Level &coarse, int margin) {
+  CellBox b = CellBox::whole(coarse.n);
+  for (int a = 0; a < 3; ++a) {
+    double rel = std::fmod(fine.x0[a] - coarse.x0[a], coarse.periodic);
+    if (rel < 0) rel += coarse.periodic;
+    const long long lo = (long long)std::floor(rel / coarse.dx);
+    const long long hi = (long long)std::ceil((rel + (double)fine.n * fine.dx) / coarse.dx);
+    b.set_axis(a, lo, hi, margin, coarse.n);
+  }
+  return b;
+}
 // pre_tab / post_tab: optional per-|k|^2 multiplier applied to the half spectrum
 // before the inverse / after the forward transform, fused into the x pass
 template <typename T>
-void fft_c2r_3d(Context &ctx, T *data, int n, double scale, const double *pre_tab = nullptr);
+void fft_c2r_3d(Context &ctx, T *data, int n, double scale, const double *pre_tab = nullptr,
+                const CellBox *box = nullptr);
 template <typename T>
-void fft_r2c_3d(Context &ctx, T *data, int n, double scale, const double *post_tab = nullptr);
+void fft_r2c_3d(Context &ctx, T *data, int n, double scale, const double *post_tab = nullptr,
+                const CellBox *box = nullptr);
 // after the stream has synchronised: true (with ctx.last_error set) when a wait of the
 // plane pass gave up since the last check; clears the flag
 bool take_fft_wait_error(Context &ctx);
@@ -213,8 +253,15 @@ void gaussian_stream(Context &ctx, unsigned long long seed, size_t n, double *ho
 void transfer_setup(Context &ctx, const double *table, int nrows, int ncols);
 void build_sqrtp_table(Context &ctx, Level &L);
 void build_sqrtp_table_species(Context &ctx, Level &L, int dm);
-void za_fields(Context &ctx, int level);
-void zoom_combine(Context &ctx, int level);
+// field masks of the real-space field maps (bit f: Level::field[f])
+constexpr unsigned kFieldDelta = 1u, kFieldsPsi = 14u;
+// Zel'dovich fields of a level in real space (the particles need the displacements
+// only; delta is made on demand by ensure_delta), and the low-passed coarser level
+// interpolated in (zoom levels)
+void za_fields(Context &ctx, int level, unsigned mask = kFieldsPsi);
+void zoom_combine(Context &ctx, int level, unsigned mask = kFieldsPsi);
+// delta of every level in real space, if the displacements were computed since it last was
+void ensure_delta(Context &ctx);
 void lpt2_fields(Context &ctx);
 // tab_main of level li (sqrt(P) times its high-pass) and the low-pass tables of a coarse level
 void level_tables(Context &ctx, int li);

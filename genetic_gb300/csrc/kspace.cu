@@ -120,6 +120,7 @@ template <> struct V2<double> { using type = double2; };
 
 // delta = w sqrt(P); psi_i = i k_i delta / k^2, zero at k = 0 and at the
 // positive Nyquist component (zeldovich.hpp:155-181)
+// (outputs: delta may be null; px, py, pz are all null or all set)
 template <typename T>
 __global__ void k_za_fields(const typename V2<T>::type *noise, const double *tab, int n, T kmin,
                             typename V2<T>::type *delta, typename V2<T>::type *px, typename V2<T>::type *py,
@@ -140,7 +141,8 @@ __global__ void k_za_fields(const typename V2<T>::type *noise, const double *tab
   C d;
   d.x = w.x * s;
   d.y = w.y * s;
-  delta[id] = d;
+  if (delta) delta[id] = d;
+  if (!px) return;
   T fx = (T)kx * kmin, fy = (T)ky * kmin, fz = (T)kz * kmin;
   T kk = fx * fx + fy * fy + fz * fz;
   C base;
@@ -394,28 +396,34 @@ static void build_lowpass_tables(Context &ctx, int coarse_index) {
   launched(2);
 }
 
+// the fields of `mask` (bit f: field f; kFieldDelta, kFieldsPsi) of level li in real space
 template <typename T>
-static void za_fields_typed(Context &ctx, int li) {
+static void za_fields_typed(Context &ctx, int li, unsigned mask) {
   using C = typename V2<T>::type;
   Level &L = *ctx.levels[li];
   size_t nc = L.ncomplex();
   for (int f = 0; f < 4; ++f) L.field[f].ensure(nc * sizeof(C));
   build_level_tables(ctx, li);
+  auto out = [&](int f) { return (mask >> f) & 1u ? L.field[f].as<C>() : nullptr; };
   k_za_fields<T><<<hs_grid(L.n), hs_block(), 0, ctx.stream>>>(L.noise.as<C>(), L.tab_main.as<double>(), L.n, (T)L.kmin(),
-                                                 L.field[0].as<C>(), L.field[1].as<C>(), L.field[2].as<C>(),
-                                                 L.field[3].as<C>());
+                                                 out(0), out(1), out(2), out(3));
   launched();
   double scale = 1.0 / std::pow((double)L.n, 1.5);
-  for (int f = 0; f < 4; ++f) fft_c2r_3d<T>(ctx, L.field[f].as<T>(), L.n, scale);
-  L.have_fields = true;
+  for (int f = 0; f < 4; ++f)
+    if ((mask >> f) & 1u) fft_c2r_3d<T>(ctx, L.field[f].as<T>(), L.n, scale);
+  if (mask & kFieldsPsi) {
+    L.have_fields = true;
+    L.have_delta = false;
+  }
+  if (mask & kFieldDelta) L.have_delta = true;
 }
 
 template <typename T>
-void interp_add4(Context &ctx, const Level &coarse, T *const src[4], Level &fine);
+void interp_add_fields(Context &ctx, const Level &coarse, T *const src[4], Level &fine, unsigned mask);
 
-// low-passed level li-1 (delta, psi) in real space, interpolated into level li
+// low-passed level li-1 (the fields of `mask`) in real space, interpolated into level li
 template <typename T>
-static void zoom_combine_typed(Context &ctx, int li) {
+static void zoom_combine_typed(Context &ctx, int li, unsigned mask) {
   using C = typename V2<T>::type;
   Level &Cl = *ctx.levels[li - 1];
   Level &F = *ctx.levels[li];
@@ -427,19 +435,23 @@ static void zoom_combine_typed(Context &ctx, int li) {
   double scale = 1.0 / std::pow((double)Cl.n, 1.5);
   if (li - 1 == 0) {
     // level 0 is unfiltered: its low-passed fields come straight from its noise
+    auto out = [&](int f) { return (mask >> f) & 1u ? reinterpret_cast<C *>(src[f]) : nullptr; };
     k_za_fields<T><<<hs_grid(Cl.n), hs_block(), 0, ctx.stream>>>(Cl.noise.as<C>(), Cl.tab_lp_src.as<double>(), Cl.n, (T)Cl.kmin(),
-                                                   reinterpret_cast<C *>(src[0]), reinterpret_cast<C *>(src[1]),
-                                                   reinterpret_cast<C *>(src[2]), reinterpret_cast<C *>(src[3]));
+                                                   out(0), out(1), out(2), out(3));
     launched();
   } else {
     // the combined real fields of level li-1, back to Fourier space, low-passed
     for (int f = 0; f < 4; ++f) {
+      if (!((mask >> f) & 1u)) continue;
       GIC_CUDA(cudaMemcpyAsync(src[f], Cl.field[f].ptr, nc * sizeof(C), cudaMemcpyDeviceToDevice, ctx.stream));
       fft_r2c_3d<T>(ctx, src[f], Cl.n, scale, Cl.tab_lp.as<double>());  // low-passed on the way out
     }
   }
-  for (int f = 0; f < 4; ++f) fft_c2r_3d<T>(ctx, src[f], Cl.n, scale);
-  interp_add4<T>(ctx, Cl, src, F);
+  // the interpolation reads the coarse cells around the fine level only
+  const CellBox fp = footprint_box(F, Cl, 3);
+  for (int f = 0; f < 4; ++f)
+    if ((mask >> f) & 1u) fft_c2r_3d<T>(ctx, src[f], Cl.n, scale, nullptr, &fp);
+  interp_add_fields<T>(ctx, Cl, src, F, mask);
 }
 
 // ---- second-order LPT ------------------------------------------------------------
@@ -638,21 +650,33 @@ void preconditioner_table(Context &ctx, const Level &L, double power, DevBuf &ou
 }
 void lowpass_tables(Context &ctx, int coarse_index) { build_lowpass_tables(ctx, coarse_index); }
 
-void za_fields(Context &ctx, int li) {
+void za_fields(Context &ctx, int li, unsigned mask) {
   Level &L = *ctx.levels[li];
   if (!L.have_noise) fail(GIC_ERR_NOT_READY, "white noise has not been drawn");
   if (ctx.dbl())
-    za_fields_typed<double>(ctx, li);
+    za_fields_typed<double>(ctx, li, mask);
   else
-    za_fields_typed<float>(ctx, li);
+    za_fields_typed<float>(ctx, li, mask);
 }
 
-void zoom_combine(Context &ctx, int li) {
+void zoom_combine(Context &ctx, int li, unsigned mask) {
   if (li < 1) return;
   if (ctx.dbl())
-    zoom_combine_typed<double>(ctx, li);
+    zoom_combine_typed<double>(ctx, li, mask);
   else
-    zoom_combine_typed<float>(ctx, li);
+    zoom_combine_typed<float>(ctx, li, mask);
+}
+
+void ensure_delta(Context &ctx) {
+  bool all = true;
+  for (auto &L : ctx.levels) {
+    if (!L->have_fields) fail(GIC_ERR_NOT_READY, "fields have not been computed");
+    all = all && L->have_delta;
+  }
+  if (all) return;
+  const int nl = (int)ctx.levels.size();
+  for (int l = 0; l < nl; ++l) za_fields(ctx, l, kFieldDelta);
+  for (int l = 1; l < nl; ++l) zoom_combine(ctx, l, kFieldDelta);
 }
 
 }  // namespace gic

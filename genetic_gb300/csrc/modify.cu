@@ -683,6 +683,45 @@ __global__ void k_field_mult(typename V2m<T>::type *c, int n, const double *tab,
 
 inline unsigned nblk(size_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
 
+// axis a of `box`: the shortest cyclic range of n coordinates holding every occupied
+// one (the complement of the longest run of empty ones), widened by `margin`
+void cyclic_cover(CellBox &box, int a, const unsigned char *occupied, int n, int margin) {
+  int best = 0, best_start = 0, run = 0;
+  for (int k = 0; k < 2 * n; ++k) {
+    if (occupied[k % n]) {
+      run = 0;
+      continue;
+    }
+    ++run;
+    if (run > best && run <= n) {
+      best = run;
+      best_start = k - run + 1;
+    }
+  }
+  if (best == n) {  // nothing occupied: an empty range stands for "no cells"; keep the whole axis
+    box.start[a] = 0;
+    box.len[a] = n;
+    return;
+  }
+  box.set_axis(a, (long long)best_start + best, (long long)best_start + n, margin, n);
+}
+
+// box of a list of cells (x n + y) n + z of an n^3 grid, widened by `margin` cells
+CellBox cells_box(const unsigned long long *cells, size_t count, int n, int margin) {
+  CellBox b = CellBox::whole(n);
+  if (count == 0) return b;
+  std::vector<unsigned char> occ(3 * (size_t)n, 0);
+  for (size_t i = 0; i < count; ++i) {
+    unsigned long long c = cells[i];
+    occ[2 * (size_t)n + c % n] = 1;
+    c /= n;
+    occ[(size_t)n + c % n] = 1;
+    occ[c / n] = 1;
+  }
+  for (int a = 0; a < 3; ++a) cyclic_cover(b, a, &occ[(size_t)a * n], n, margin);
+  return b;
+}
+
 }  // namespace
 
 // --- the multi-level field algebra ------------------------------------------------
@@ -737,11 +776,17 @@ struct ModEngine {
     dst.ensure(elems(l) * sizeof(T));
     GIC_CUDA(cudaMemcpyAsync(dst.ptr, src.ptr, elems(l) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
   }
-  void to_fourier(T *p, int l) { fft_r2c_3d<T>(ctx, p, lev(l).n, scale(l)); }
+  // box: the forward transform's input is zero outside it / only the inverse
+  // transform's output inside it is used (the transforms skip the rest)
+  void to_fourier(T *p, int l, const CellBox *box = nullptr) { fft_r2c_3d<T>(ctx, p, lev(l).n, scale(l), nullptr, box); }
   void to_real(T *p, int l) { fft_c2r_3d<T>(ctx, p, lev(l).n, scale(l)); }
   // times the current table (S.tab), then to real space: the multiply rides on the
   // transform's first pass (bit-identical to mul_table followed by to_real)
-  void to_real_times_table(T *p, int l) { fft_c2r_3d<T>(ctx, p, lev(l).n, scale(l), S.tab.template as<double>()); }
+  void to_real_times_table(T *p, int l, const CellBox *box = nullptr) {
+    fft_c2r_3d<T>(ctx, p, lev(l).n, scale(l), S.tab.template as<double>(), box);
+  }
+  // cells of level c that the fine level f covers (margin: extra cells each side), cyclic
+  CellBox footprint(int f, int c, int margin) { return footprint_box(lev(f), lev(c), margin); }
   void to_fourier(Field &f, int l) {
     if (!f.fourier[l]) to_fourier(ptr(f, l), l);
     f.fourier[l] = 1;
@@ -902,7 +947,10 @@ struct ModEngine {
     S.masks.ensure(m.size());
     GIC_CUDA(cudaMemcpyAsync(S.masks.ptr, m.data(), m.size(), cudaMemcpyHostToDevice, ctx.stream));
     GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+    win_box = CellBox::whole(L.n);
+    for (int a = 0; a < 3; ++a) cyclic_cover(win_box, a, &m[(size_t)a * L.n], L.n, 0);
   }
+  CellBox win_box;  // cells inside the last window_masks' window
   void window_op(T *r, const T *src, int l, int op) {
     int n = lev(l).n;
     unsigned char *m = S.masks.template as<unsigned char>();
@@ -937,7 +985,13 @@ struct ModEngine {
     S.tmp_src.ensure(elems(s) * sizeof(T));
     GIC_CUDA(cudaMemcpyAsync(S.tmp_src.ptr, source_k, elems(s) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
     table(sp, s);
-    to_real_times_table(S.tmp_src.template as<T>(), s);
+    if (s < t) {
+      // the interpolation reads the coarse cells around the fine level only
+      const CellBox fp = footprint(t, s, 3);
+      to_real_times_table(S.tmp_src.template as<T>(), s, &fp);
+    } else {
+      to_real_times_table(S.tmp_src.template as<T>(), s);
+    }
     if (s < t) {
       const T *src[1] = {S.tmp_src.template as<T>()};
       T *dst[1] = {target_real};
@@ -976,7 +1030,14 @@ struct ModEngine {
           GIC_CUDA(cudaMemsetAsync(Cr, 0, elems(t) * sizeof(T), ctx.stream));
           for (int s = 0; s < nl(); ++s)
             if (s != t) cross_term_impl(Cr, t, ptr(X, s), s);
-          to_fourier(Cr, t);
+          // with no coarser source, the block means of the finer levels fill only
+          // the next level's footprint
+          if (t == 0) {
+            const CellBox fp = footprint(1, 0, 1);
+            to_fourier(Cr, t, &fp);
+          } else {
+            to_fourier(Cr, t);
+          }
           add = reinterpret_cast<const C *>(Cr);
         }
         family_table(t, 2);
@@ -1005,15 +1066,16 @@ struct ModEngine {
     window_masks(t, t + 1);
     S.win.ensure(elems(t) * sizeof(T));
     T *I = S.win.template as<T>();
-    window_op(I, R, t, 2);  // I = W x
-    to_fourier(I, t);
+    window_op(I, R, t, 2);  // I = W x: zero outside the window
+    const CellBox wb = win_box;
+    to_fourier(I, t, &wb);
     family_table(t, 1);
     to_real_times_table(I, t);
     window_op(R, I, t, 0);  // g = (1 - W) x + f (W x)
     GIC_CUDA(cudaMemcpyAsync(I, R, elems(t) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
     to_fourier(I, t);
     family_table(t, 1);
-    to_real_times_table(I, t);
+    to_real_times_table(I, t, &wb);  // f g is read inside the window only
     window_op(R, I, t, 1);  // R = W (f g) + (1 - W) g
   }
 
@@ -1556,10 +1618,14 @@ struct ModEngine {
     // the reference transforms the localisation covector to Fourier space and back
     // before deinterpolating; that round trip is the identity and is skipped
     out.fourier[F] = 0;
+    // support of each level's real covector: the flagged cells and the stencils' reach
+    // (2 cells) on the finest level, the deinterpolation block on coarser ones
+    std::vector<CellBox> support(nl());
+    support[F] = cells_box(flagged, count, lev(F).n, 2);
     if (F > 0) {
       for (int l = F - 1; l >= 0; --l) {
         out.fourier[l] = 0;
-        deinterpolate(ptr(out, l + 1), l + 1, ptr(out, l), l);
+        support[l] = deinterpolate(ptr(out, l + 1), l + 1, ptr(out, l), l, false, &support[l + 1]);
       }
     }
     for (int l = 0; l < nl(); ++l) {
@@ -1575,7 +1641,7 @@ struct ModEngine {
       const bool velocity_like = (kind >= GIC_MOD_VX && kind <= GIC_MOD_VZ) || kind >= GIC_MOD_LX;
       sp.vel = velocity_like ? velocity_ratio() : 0.0;
       table(sp, l);
-      fft_r2c_3d<T>(ctx, ptr(out, l), lev(l).n, scale(l), S.tab.template as<double>());
+      fft_r2c_3d<T>(ctx, ptr(out, l), lev(l).n, scale(l), S.tab.template as<double>(), &support[l]);
       out.fourier[l] = 1;
       if (kind == GIC_MOD_POTENTIAL) {
         // 3/2 Om0 / a (H0/h)^2 / c^2 in (h/Mpc)^2 (cosmology/parameters.hpp:213-216)
@@ -1591,7 +1657,12 @@ struct ModEngine {
 
   // transpose tricubic: fine real (level f) / r^3 added into coarse real (level c)
   // unit_scale: the plain transpose of the tricubic interpolation (no 1/r^3)
-  void deinterpolate(const T *fine, int f, T *coarse, int c, bool unit_scale = false) {
+  // returns the block of coarse cells it adds into
+  // fine_box: the fine field is zero outside it; the passes then run over its cells
+  // only (an axis whose range wraps around the fine grid is taken whole).  Skipped
+  // cells would only add zeros, so the sums are the same.
+  CellBox deinterpolate(const T *fine, int f, T *coarse, int c, bool unit_scale = false,
+                        const CellBox *fine_box = nullptr) {
     const Level &Fl = lev(f), &Cl = lev(c);
     int nf = Fl.n;
     int r = (int)std::lround(Cl.dx / Fl.dx);
@@ -1605,34 +1676,44 @@ struct ModEngine {
     std::vector<int> h(3 * nf);
     GIC_CUDA(cudaMemcpyAsync(h.data(), ub, 3 * nf * sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
     GIC_CUDA(cudaStreamSynchronize(ctx.stream));
-    int c0[3], cnt[3];
+    // fine ranges [f0, f0 + fn) per axis, and the coarse block they reach
+    int f0[3], fn[3], c0[3], cnt[3];
     for (int a = 0; a < 3; ++a) {
-      c0[a] = h[(size_t)a * nf] - 1;
-      cnt[a] = h[(size_t)a * nf + nf - 1] + 3 - c0[a];
+      const bool cut = fine_box && fine_box->len[a] < nf && fine_box->start[a] + fine_box->len[a] <= nf;
+      f0[a] = cut ? fine_box->start[a] : 0;
+      fn[a] = cut ? fine_box->len[a] : nf;
+      c0[a] = h[(size_t)a * nf + f0[a]] - 1;
+      cnt[a] = h[(size_t)a * nf + f0[a] + fn[a] - 1] + 3 - c0[a];
     }
     const long long frs = 2 * (nf / 2 + 1);
-    // pass x: fine (nf, nf, nf) padded -> t1 (cnt0, nf, nf)
-    S.t1.ensure((size_t)cnt[0] * nf * nf * sizeof(T));
-    GIC_CUDA(cudaMemsetAsync(S.t1.ptr, 0, (size_t)cnt[0] * nf * nf * sizeof(T), ctx.stream));
-    k_deinterp_pass<T><<<nblk((size_t)nf * nf), 256, 0, ctx.stream>>>(
-        fine, (long long)nf * frs, frs, S.t1.template as<T>(), (long long)nf * nf, nf, 0, nf, nf, nf, nf, ub, fr, c0[0], cnt[0],
-        scale);
-    // pass y: t1 (cnt0, nf, nf) -> t2 (cnt0, cnt1, nf)
-    S.t2.ensure((size_t)cnt[0] * cnt[1] * nf * sizeof(T));
-    GIC_CUDA(cudaMemsetAsync(S.t2.ptr, 0, (size_t)cnt[0] * cnt[1] * nf * sizeof(T), ctx.stream));
-    k_deinterp_pass<T><<<nblk((size_t)cnt[0] * nf), 256, 0, ctx.stream>>>(
-        S.t1.template as<T>(), (long long)nf * nf, nf, S.t2.template as<T>(), (long long)cnt[1] * nf, nf, 1, cnt[0], nf, nf, nf, ub + nf,
-        fr + nf, c0[1], cnt[1], (T)1);
-    // pass z: t2 (cnt0, cnt1, nf) -> t3 (cnt0, cnt1, cnt2)
-    S.t3.ensure((size_t)cnt[0] * cnt[1] * cnt[2] * sizeof(T));
-    GIC_CUDA(cudaMemsetAsync(S.t3.ptr, 0, (size_t)cnt[0] * cnt[1] * cnt[2] * sizeof(T), ctx.stream));
+    const T *in = fine + (long long)f0[0] * nf * frs + (long long)f0[1] * frs + f0[2];
+    // pass x: fine box (fn0, fn1, fn2) -> t1 (cnt0, fn1, fn2)
+    const size_t b1 = (size_t)cnt[0] * fn[1] * fn[2];
+    S.t1.ensure(b1 * sizeof(T));
+    GIC_CUDA(cudaMemsetAsync(S.t1.ptr, 0, b1 * sizeof(T), ctx.stream));
+    k_deinterp_pass<T><<<nblk((size_t)fn[1] * fn[2]), 256, 0, ctx.stream>>>(
+        in, (long long)nf * frs, frs, S.t1.template as<T>(), (long long)fn[1] * fn[2], fn[2], 0, fn[0], fn[1], fn[2], fn[0],
+        ub + f0[0], fr + f0[0], c0[0], cnt[0], scale);
+    // pass y: t1 (cnt0, fn1, fn2) -> t2 (cnt0, cnt1, fn2)
+    const size_t b2 = (size_t)cnt[0] * cnt[1] * fn[2];
+    S.t2.ensure(b2 * sizeof(T));
+    GIC_CUDA(cudaMemsetAsync(S.t2.ptr, 0, b2 * sizeof(T), ctx.stream));
+    k_deinterp_pass<T><<<nblk((size_t)cnt[0] * fn[2]), 256, 0, ctx.stream>>>(
+        S.t1.template as<T>(), (long long)fn[1] * fn[2], fn[2], S.t2.template as<T>(), (long long)cnt[1] * fn[2], fn[2], 1,
+        cnt[0], fn[1], fn[2], fn[1], ub + nf + f0[1], fr + nf + f0[1], c0[1], cnt[1], (T)1);
+    // pass z: t2 (cnt0, cnt1, fn2) -> t3 (cnt0, cnt1, cnt2)
+    const size_t b3 = (size_t)cnt[0] * cnt[1] * cnt[2];
+    S.t3.ensure(b3 * sizeof(T));
+    GIC_CUDA(cudaMemsetAsync(S.t3.ptr, 0, b3 * sizeof(T), ctx.stream));
     k_deinterp_pass<T><<<nblk((size_t)cnt[0] * cnt[1]), 256, 0, ctx.stream>>>(
-        S.t2.template as<T>(), (long long)cnt[1] * nf, nf, S.t3.template as<T>(), (long long)cnt[1] * cnt[2], cnt[2], 2, cnt[0], cnt[1], nf,
-        nf, ub + 2 * nf, fr + 2 * nf, c0[2], cnt[2], (T)1);
-    size_t m = (size_t)cnt[0] * cnt[1] * cnt[2];
-    k_add_block<T><<<nblk(m), 256, 0, ctx.stream>>>(S.t3.template as<T>(), cnt[0], cnt[1], cnt[2], c0[0], c0[1], c0[2], coarse,
-                                                   Cl.n);
+        S.t2.template as<T>(), (long long)cnt[1] * fn[2], fn[2], S.t3.template as<T>(), (long long)cnt[1] * cnt[2], cnt[2], 2,
+        cnt[0], cnt[1], fn[2], fn[2], ub + 2 * nf + f0[2], fr + 2 * nf + f0[2], c0[2], cnt[2], (T)1);
+    k_add_block<T><<<nblk(b3), 256, 0, ctx.stream>>>(S.t3.template as<T>(), cnt[0], cnt[1], cnt[2], c0[0], c0[1], c0[2],
+                                                    coarse, Cl.n);
     launched(4);
+    CellBox b = CellBox::whole(Cl.n);
+    for (int a = 0; a < 3; ++a) b.set_axis(a, c0[a], (long long)c0[a] + cnt[a], 0, Cl.n);
+    return b;
   }
 };
 

@@ -214,15 +214,20 @@ void interp_add(Context &ctx, const Level &coarse, const T *const *src, const Le
   }
 }
 
+// the fields of `mask` (bit f: delta, psi_x, psi_y, psi_z): all four, the three
+// displacements, or delta alone
 template <typename T>
-void interp_add4(Context &ctx, const Level &coarse, T *const src[4], Level &fine) {
+void interp_add_fields(Context &ctx, const Level &coarse, T *const src[4], Level &fine, unsigned mask) {
   T *dst[4] = {fine.field[0].as<T>(), fine.field[1].as<T>(), fine.field[2].as<T>(), fine.field[3].as<T>()};
   const T *s[4] = {src[0], src[1], src[2], src[3]};
-  interp_add<T, 4>(ctx, coarse, s, fine, dst);
+  if (mask == 15u) interp_add<T, 4>(ctx, coarse, s, fine, dst);
+  else if (mask == 14u) interp_add<T, 3>(ctx, coarse, s + 1, fine, dst + 1);
+  else if (mask == 1u) interp_add<T, 1>(ctx, coarse, s, fine, dst);
+  else fail(GIC_ERR_INTERNAL, "unsupported field mask for the zoom interpolation");
 }
 
-template void interp_add4<float>(Context &, const Level &, float *const[4], Level &);
-template void interp_add4<double>(Context &, const Level &, double *const[4], Level &);
+template void interp_add_fields<float>(Context &, const Level &, float *const[4], Level &, unsigned);
+template void interp_add_fields<double>(Context &, const Level &, double *const[4], Level &, unsigned);
 template void interp_add<float, 1>(Context &, const Level &, const float *const *, const Level &, float *const *);
 template void interp_add<double, 1>(Context &, const Level &, const double *const *, const Level &, double *const *);
 

@@ -150,6 +150,14 @@ GIC_API int gic_fetch_particles(gic_ctx *ctx, int level, double *pos, double *ve
  * (fourier.hpp:479-518). */
 GIC_API int gic_fft(gic_ctx *ctx, int level, int what, int dir);
 
+/* gic_fft restricted to a box of the level's cells: per axis a the cyclic range
+ * start[a] .. start[a] + len[a] - 1 (mod n).  dir = -1: the real field must be zero
+ * outside the box (the padding words of the rows need not be); dir = +1: only the
+ * real values inside the box are defined afterwards.  Inside the box the values are
+ * the bits gic_fft gives; the transforms skip the x planes and y rows outside it.
+ * No genetIC counterpart: FFTW plans always transform the whole grid. */
+GIC_API int gic_fft_box(gic_ctx *ctx, int level, int what, int dir, const int *start, const int *len);
+
 /* chi^2 of the white noise <C^-1 w | w>: Hermitian-weighted sum of |w_k|^2 on
  * one level; with zoom levels the covariance metric with windowed filters
  * (MultiLevelField::getChi2, multilevelfield.hpp:461-487, 344-384). */

@@ -96,3 +96,50 @@ def test_plane_pass_bit_identical_512(built, bbks, precision, monkeypatch):
         raw, back = _roundtrip_raw(precision, 512, bbks, 11)
         assert np.array_equal(raw, ref[0]), tile
         assert np.array_equal(back, ref[1]), tile
+
+
+BOXES = [((3, 5, 0), (9, 17, 1)), ((60, 50, 7), (10, 20, 3)), ((0, 0, 0), (64, 12, 5)), ((17, 0, 2), (5, 64, 64)),
+         ((1, 2, 3), (64, 64, 64))]
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'mixed'])
+@pytest.mark.parametrize('n', [64, 256])
+def test_box_transforms_match_whole(built, bbks, precision, n):
+    """Transforms restricted to a box of cells (the rows and planes outside skipped)
+    give the whole transform's bits: forward transforms of fields zero outside the
+    box (padding words of every row left non-zero, which the transform must not
+    read), inverse transforms inside the box; boxes wrap around the grid."""
+    from genetic_gb300.generator import _ptr
+    gen = make_generator(precision, bbks, [('base', 50.0, n)], 7, 'random_seed')
+    rng = np.random.default_rng(5)
+    sx = n // 64
+    for start, length in BOXES:
+        start = np.array([s * sx for s in start], dtype=np.int32)
+        length = np.array([min(n, l * sx) for l in length], dtype=np.int32)
+        inside = [((np.arange(n) - start[a]) % n) < length[a] for a in range(3)]
+        mask = inside[0][:, None, None] & inside[1][None, :, None] & inside[2][None, None, :]
+        # forward: padded real layout, zero outside the box, padding words non-zero
+        real = np.zeros((n, n, 2 * (n // 2 + 1)))
+        real[:, :, :n] = np.where(mask, rng.standard_normal((n, n, n)), 0.0)
+        real[:, :, n:] = 7.0
+        out = {}
+        for kind in ('whole', 'box'):
+            gen._call('gic_set_noise', 0, _ptr(np.ascontiguousarray(real)))
+            if kind == 'whole':
+                gen._call('gic_fft', 0, 0, -1)
+            else:
+                gen._call('gic_fft_box', 0, 0, -1, _ptr(start), _ptr(length))
+            out[kind] = gen.noise(0)
+        assert np.array_equal(out['whole'], out['box']), (start, length)
+        # inverse: the reals inside the box
+        spec = np.ascontiguousarray(rng.standard_normal((n, n, n // 2 + 1, 2)))
+        for kind in ('whole', 'box'):
+            gen._call('gic_set_noise', 0, _ptr(spec))
+            if kind == 'whole':
+                gen._call('gic_fft', 0, 0, +1)
+            else:
+                gen._call('gic_fft_box', 0, 0, +1, _ptr(start), _ptr(length))
+            raw = gen.noise(0)
+            out[kind] = np.stack([raw.real, raw.imag], -1).reshape(n, n, -1)[:, :, :n]
+        assert np.array_equal(out['whole'][mask], out['box'][mask]), (start, length)
+    gen.close()
