@@ -196,6 +196,29 @@ struct Context {
   bool dbl() const { return precision == GIC_FP64; }
 };
 
+// (row, kz) of this thread's element of an n x n x (n/2 + 1) half spectrum, for a 1-D
+// launch of hs_elements(n) threads: flat indexing gives every warp one contiguous
+// span, so each sector is written whole by one warp (rows of n/2 + 1 coefficients
+// are not sector-aligned, and a (row, kz-chunk) grid splits sectors between CTAs)
+#ifdef __CUDACC__
+__device__ __forceinline__ bool hs_cell(int n, unsigned &row, int &iz) {
+  const unsigned S = (unsigned)(n / 2 + 1);
+  const unsigned long long e = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned long long total = (unsigned long long)n * (unsigned long long)n * S;
+  if (e >= total) return false;
+  if (total <= 0xFFFFFFFFull) {
+    const unsigned e32 = (unsigned)e;
+    row = e32 / S;
+    iz = (int)(e32 - row * S);
+  } else {
+    row = (unsigned)(e / S);
+    iz = (int)(e - (unsigned long long)row * S);
+  }
+  return true;
+}
+#endif
+inline unsigned long long hs_elements(int n) { return (unsigned long long)n * n * (n / 2 + 1); }
+
 // fft.cu
 // A box of an n^3 grid's cells: per axis the cyclic range [start, start + len) mod n.
 // Given to a forward transform, its input is zero outside the box; given to an

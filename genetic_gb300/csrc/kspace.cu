@@ -127,9 +127,9 @@ __global__ void k_za_fields(const typename V2<T>::type *noise, const double *tab
                             typename V2<T>::type *pz) {
   using C = typename V2<T>::type;
   const int H = n / 2, S = H + 1;
-  unsigned row = blockIdx.x * 8 + threadIdx.y;
-  int iz = blockIdx.y * 32 + threadIdx.x;
-  if (row >= (unsigned)n * (unsigned)n || iz >= S) return;
+  unsigned row;
+  int iz;
+  if (!hs_cell(n, row, iz)) return;
   int ix = (int)(row / (unsigned)n), iy = (int)(row % (unsigned)n);
   size_t id = (size_t)row * S + iz;
   int kx = ix > H ? ix - n : ix;
@@ -170,9 +170,9 @@ __global__ void k_hessian_fields(const typename V2<T>::type *src, const double *
                                  typename V2<T>::type *const *out) {
   using C = typename V2<T>::type;
   const int H = n / 2, S = H + 1;
-  unsigned row = blockIdx.x * 8 + threadIdx.y;
-  int iz = blockIdx.y * 32 + threadIdx.x;
-  if (row >= (unsigned)n * (unsigned)n || iz >= S) return;
+  unsigned row;
+  int iz;
+  if (!hs_cell(n, row, iz)) return;
   int ix = (int)(row / (unsigned)n), iy = (int)(row % (unsigned)n);
   size_t id = (size_t)row * S + iz;
   int kc[3] = {ix > H ? ix - n : ix, iy > H ? iy - n : iy, iz};
@@ -226,15 +226,15 @@ __global__ void k_filter_table(double *out, const double *base, long long nq, do
 }
 
 // multiply a half spectrum by tab[|k|^2]
-inline dim3 hs_grid(int n) { return dim3((unsigned)(((size_t)n * n + 7) / 8), (unsigned)((n / 2 + 1 + 31) / 32)); }
-inline dim3 hs_block() { return dim3(32, 8); }
+inline dim3 hs_grid(int n) { return dim3((unsigned)((hs_elements(n) + 255) / 256)); }
+inline dim3 hs_block() { return dim3(256); }
 
 template <typename T>
 __global__ void k_scale_table(typename V2<T>::type *c, int n, const double *tab) {
   const int H = n / 2, S = H + 1;
-  unsigned row = blockIdx.x * 8 + threadIdx.y;
-  int iz = blockIdx.y * 32 + threadIdx.x;
-  if (row >= (unsigned)n * (unsigned)n || iz >= S) return;
+  unsigned row;
+  int iz;
+  if (!hs_cell(n, row, iz)) return;
   int ix = (int)(row / (unsigned)n), iy = (int)(row % (unsigned)n);
   size_t id = (size_t)row * S + iz;
   long long kx = ix > H ? ix - n : ix, ky = iy > H ? iy - n : iy;
@@ -588,9 +588,9 @@ void lpt2_fields(Context &ctx) {
 template <typename T>
 __global__ void k_noise_op(typename V2<T>::type *w, int n, double kmin, int op, double k2max) {
   const int H = n / 2, S = H + 1;
-  unsigned row = blockIdx.x * 8 + threadIdx.y;
-  int iz = blockIdx.y * 32 + threadIdx.x;
-  if (row >= (unsigned)n * (unsigned)n || iz >= S) return;
+  unsigned row;
+  int iz;
+  if (!hs_cell(n, row, iz)) return;
   int ix = (int)(row / (unsigned)n), iy = (int)(row % (unsigned)n);
   size_t id = (size_t)row * S + iz;
   typename V2<T>::type v = w[id];

@@ -20,6 +20,7 @@
 //    inner product; the correction sum_i d_i C a'_i is then one combination of
 //    the converted covectors.
 #include "gic_internal.h"
+#include <atomic>
 #include <cmath>
 #include <algorithm>
 
@@ -73,17 +74,18 @@ __global__ void k_mod_table(double *out, long long nq, TableSpec sp) {
 // Half-spectrum kernels run on a 2-D grid: x over rows (kx, ky), y over 32-wide
 // kz chunks, so no 64-bit division per element.
 constexpr int kKzChunk = 32, kRowsPerBlock = 8;
-inline dim3 hs_grid(int n) {
-  return dim3((unsigned)(((size_t)n * n + kRowsPerBlock - 1) / kRowsPerBlock), (unsigned)((n / 2 + 1 + kKzChunk - 1) / kKzChunk));
-}
-inline dim3 hs_block() { return dim3(kKzChunk, kRowsPerBlock); }
+// elementwise half-spectrum kernels: one thread per coefficient, flat (hs_cell)
+inline dim3 hs_grid(int n) { return dim3((unsigned)((hs_elements(n) + 255) / 256)); }
+inline dim3 hs_block() { return dim3(256); }
+// reductions: warps of kKzChunk lanes walking rows, kRowsPerBlock warps per CTA
+inline dim3 red_block() { return dim3(kKzChunk, kRowsPerBlock); }
 
 template <typename T>
 __global__ void k_mul_table(typename V2m<T>::type *c, int n, const double *tab) {
   const int H = n / 2, S = H + 1;
-  unsigned row = blockIdx.x * kRowsPerBlock + threadIdx.y;
-  int iz = blockIdx.y * kKzChunk + threadIdx.x;
-  if (row >= (unsigned)n * (unsigned)n || iz >= S) return;
+  unsigned row;
+  int iz;
+  if (!hs_cell(n, row, iz)) return;
   int ix = (int)(row / (unsigned)n), iy = (int)(row % (unsigned)n);
   long long kx = ix > H ? ix - n : ix, ky = iy > H ? iy - n : iy;
   T s = (T)tab[kx * kx + ky * ky + (long long)iz * iz];
@@ -97,9 +99,9 @@ template <typename T>
 __global__ void k_mul_table_add(typename V2m<T>::type *out, const typename V2m<T>::type *x, int n, const double *tab,
                                 const typename V2m<T>::type *add) {
   const int H = n / 2, S = H + 1;
-  unsigned row = blockIdx.x * kRowsPerBlock + threadIdx.y;
-  int iz = blockIdx.y * kKzChunk + threadIdx.x;
-  if (row >= (unsigned)n * (unsigned)n || iz >= S) return;
+  unsigned row;
+  int iz;
+  if (!hs_cell(n, row, iz)) return;
   int ix = (int)(row / (unsigned)n), iy = (int)(row % (unsigned)n);
   long long kx = ix > H ? ix - n : ix, ky = iy > H ? iy - n : iy;
   T s = (T)tab[kx * kx + ky * ky + (long long)iz * iz];
@@ -178,13 +180,12 @@ __global__ void __launch_bounds__(256) k_inner_block(BlockFields<T> f, int n, do
   const int H = n / 2, S = H + 1;
   const unsigned rows = (unsigned)n * (unsigned)n;
   const int tid = threadIdx.y * kKzChunk + threadIdx.x;
-  double total[kBlockA * kBlockB];
-#pragma unroll
-  for (int p = 0; p < kBlockA * kBlockB; ++p) total[p] = 0;
-  for (int iz = threadIdx.x; iz < S; iz += kKzChunk) {
-    const T w = (iz == 0 || iz == H) ? (T)1 : (T)2;
-    ProdAcc<T> acc[kBlockA * kBlockB];
-    for (unsigned r = blockIdx.x * kRowsPerBlock + threadIdx.y; r < rows; r += gridDim.x * kRowsPerBlock) {
+  ProdAcc<T> acc[kBlockA * kBlockB];
+  // a warp walks whole rows (one contiguous span of S coefficients per field), rows
+  // strided over the grid
+  for (unsigned r = blockIdx.x * kRowsPerBlock + threadIdx.y; r < rows; r += gridDim.x * kRowsPerBlock) {
+    for (int iz = threadIdx.x; iz < S; iz += kKzChunk) {
+      const T w = (iz == 0 || iz == H) ? (T)1 : (T)2;
       const size_t id = 2 * ((size_t)r * S + iz);
       T br[kBlockB], bi[kBlockB];
 #pragma unroll
@@ -202,12 +203,14 @@ __global__ void __launch_bounds__(256) k_inner_block(BlockFields<T> f, int n, do
             if (j < f.nb) acc[i * kBlockB + j].add(ar, ai, br[j], bi[j], w);
         }
     }
-#pragma unroll
-    for (int p = 0; p < kBlockA * kBlockB; ++p) total[p] += acc[p].get();
   }
   for (int i = 0; i < f.na; ++i)
     for (int j = 0; j < f.nb; ++j) {
-      red[tid] = total[i * kBlockB + j];
+      double v = 0;
+#pragma unroll
+      for (int p = 0; p < kBlockA * kBlockB; ++p)
+        if (p == i * kBlockB + j) v = acc[p].get();
+      red[tid] = v;
       __syncthreads();
       for (int s2 = 128; s2 > 0; s2 >>= 1) {
         if (tid < s2) red[tid] += red[tid + s2];
@@ -237,9 +240,11 @@ __global__ void k_scale(T *a, double c, size_t n) {
 template <typename T>
 __global__ void k_window_op(T *r, const T *s, int n, const unsigned char *mx, const unsigned char *my,
                             const unsigned char *mz, int op) {
-  unsigned row = blockIdx.x * kRowsPerBlock + threadIdx.y;
-  int z = blockIdx.y * kKzChunk + threadIdx.x;
-  if (row >= (unsigned)n * (unsigned)n || z >= n) return;
+  // one thread per cell, flat over the n^3 cells (rows of n, padded in memory)
+  const unsigned long long e = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (unsigned long long)n * n * n) return;
+  const unsigned row = (unsigned)(e / (unsigned)n);
+  const int z = (int)(e - (unsigned long long)row * (unsigned)n);
   int x = (int)(row / (unsigned)n), y = (int)(row % (unsigned)n);
   bool in = mx[x] && my[y] && mz[z];
   size_t id = (size_t)row * (size_t)(2 * (n / 2 + 1)) + z;
@@ -247,9 +252,7 @@ __global__ void k_window_op(T *r, const T *s, int n, const unsigned char *mx, co
   else if (op == 1) { if (in) r[id] = s[id]; }
   else r[id] = in ? s[id] : (T)0;
 }
-inline dim3 real_grid(int n) {
-  return dim3((unsigned)(((size_t)n * n + kRowsPerBlock - 1) / kRowsPerBlock), (unsigned)((n + kKzChunk - 1) / kKzChunk));
-}
+inline dim3 real_grid(int n) { return dim3((unsigned)(((unsigned long long)n * n * n + 255) / 256)); }
 
 // Hermitian-weighted Re(conj(a) b) over a half spectrum, partial sums per block.
 // Float fields: every product is split exactly (fma) and accumulated in a
@@ -511,9 +514,9 @@ __global__ void k_localise_am(T *real, int n, const unsigned long long *cells, s
 template <typename T>
 __global__ void k_density_to_potential(typename V2m<T>::type *c, int n, double kmin, double prefac) {
   const int H = n / 2, S = H + 1;
-  unsigned row = blockIdx.x * kRowsPerBlock + threadIdx.y;
-  int iz = blockIdx.y * kKzChunk + threadIdx.x;
-  if (row >= (unsigned)n * (unsigned)n || iz >= S) return;
+  unsigned row;
+  int iz;
+  if (!hs_cell(n, row, iz)) return;
   int ix = (int)(row / (unsigned)n), iy = (int)(row % (unsigned)n);
   double kx = (double)(ix > H ? ix - n : ix) * kmin, ky = (double)(iy > H ? iy - n : iy) * kmin,
          kz = (double)iz * kmin;
@@ -652,9 +655,9 @@ __global__ void k_unpad(const T *padded, T *compact, int n, T scale) {
 template <typename T>
 __global__ void k_field_mult(typename V2m<T>::type *c, int n, const double *tab, T kmin, int what, int conj) {
   const int H = n / 2, S = H + 1;
-  unsigned row = blockIdx.x * kRowsPerBlock + threadIdx.y;
-  int iz = blockIdx.y * kKzChunk + threadIdx.x;
-  if (row >= (unsigned)n * (unsigned)n || iz >= S) return;
+  unsigned row;
+  int iz;
+  if (!hs_cell(n, row, iz)) return;
   int ix = (int)(row / (unsigned)n), iy = (int)(row % (unsigned)n);
   int kc[3] = {ix > H ? ix - n : ix, iy > H ? iy - n : iy, iz};
   long long q = (long long)kc[0] * kc[0] + (long long)kc[1] * kc[1] + (long long)kc[2] * kc[2];
@@ -849,11 +852,11 @@ struct ModEngine {
         const Term &t = groups[p][i];
         double *dst = part + per * p + (size_t)i * blocks;
         if (t.kind == kReal)
-          k_inner_real<T><<<blocks, hs_block(), 0, ctx.stream>>>(t.a, t.b, lev(t.l).n, dst);
+          k_inner_real<T><<<blocks, red_block(), 0, ctx.stream>>>(t.a, t.b, lev(t.l).n, dst);
         else if (t.kind == kFlat)
           k_dot_flat<T><<<blocks, 256, 0, ctx.stream>>>(t.a, t.b, t.count, dst);
         else
-          k_inner<T><<<blocks, hs_block(), 0, ctx.stream>>>(t.a, t.b, lev(t.l).n, dst);
+          k_inner<T><<<blocks, red_block(), 0, ctx.stream>>>(t.a, t.b, lev(t.l).n, dst);
         launched();
       }
     k_sum<<<np, 256, 0, ctx.stream>>>(part, (int)per, part + per * np);
@@ -882,7 +885,16 @@ struct ModEngine {
   // M[i][j] = <A_i|B_j> summed over levels (Fourier), each field read once per level
   // for every 4 x 5 block of products; one read-back for the whole matrix
   std::vector<double> inner_block(const std::vector<Field *> &A, const std::vector<Field *> &B) {
-    const int blocks = 152 * 4;
+    // one wave of resident CTAs
+    static std::atomic<int> per_sm{0};
+    if (per_sm.load() == 0) {
+      int nb = 0;
+      GIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_inner_block<T>, kKzChunk * kRowsPerBlock, 0));
+      per_sm.store(std::max(nb, 1));
+    }
+    int nsm = 0;
+    GIC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx.device));
+    const int blocks = per_sm.load() * nsm;
     const int L = nl(), na = (int)A.size(), nbt = (int)B.size(), np = na * nbt;
     if (np == 0) return {};
     const size_t pstride = (size_t)L * blocks;
@@ -900,7 +912,7 @@ struct ModEngine {
           bf.nb = std::min(kBlockB, nbt - jb);
           for (int i = 0; i < bf.na; ++i) bf.a[i] = ptr(*A[ia + i], l);
           for (int j = 0; j < bf.nb; ++j) bf.b[j] = ptr(*B[jb + j], l);
-          k_inner_block<T><<<blocks, hs_block(), 0, ctx.stream>>>(bf, lev(l).n, part + (size_t)l * blocks, ia, jb,
+          k_inner_block<T><<<blocks, red_block(), 0, ctx.stream>>>(bf, lev(l).n, part + (size_t)l * blocks, ia, jb,
                                                                    nbt, pstride);
           launched();
         }

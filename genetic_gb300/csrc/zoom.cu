@@ -54,9 +54,6 @@ __global__ void k_interp_axes(int nf, double dxf, double f0, double f1, double f
   ubase[id] = (int)f + (int)floor(lu / period) * nc;
 }
 
-// Separable form: a CTA owns one fine x plane and TY fine y rows.  It first
-// contracts the four coarse x planes of its stencil into a shared tile
-// P[cy][cz] (per field), then every fine (y, z) is a 4 x 4 contraction of P.
 template <typename T, int NF>
 struct FieldPtrs {
   const T *src[NF];
@@ -98,8 +95,90 @@ __global__ void __launch_bounds__(256) k_interp_add_direct(FieldPtrs<T, NF> fp, 
   for (int f = 0; f < NF; ++f) fp.dst[f][dst] += s[f];
 }
 
+// Separable form: a CTA owns one fine x plane and TY fine y rows.  Three contractions,
+// each done once: the four coarse x planes of the stencil into P[cy][cz], then z into
+// Q[cy][z] = sum_c wz_c(z) P[cy][pz(z) + c] for every coarse row cy of the block and
+// fine z, then every fine (y, z) is sum_b wy_b(y) Q[py(y) + b][z].  The sums run in the
+// order of the direct 4 x 4 contraction of P, so the values are the same.
 template <typename T, int NF, int TY>
 __global__ void __launch_bounds__(256) k_interp_add_sep(FieldPtrs<T, NF> fp, int nc, int wrap,
+                                                        const int *__restrict__ base, const T *__restrict__ frac,
+                                                        const int *__restrict__ ubase, int nf, int maxcz, int maxcy) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T *P = reinterpret_cast<T *>(smraw);
+  const int x = blockIdx.y;
+  const int y0 = blockIdx.x * TY;
+  const int ylast = min(y0 + TY, nf) - 1;
+  auto cw = [&](int v) { return wrap ? ((v % nc) + nc) % nc : min(max(v, 0), nc - 1); };
+  T wx[4];
+  catmull_rom<T>(__ldg(frac + x), wx);
+  int ixw[4];
+  int bx = __ldg(base + x);
+#pragma unroll
+  for (int a = 0; a < 4; ++a) ixw[a] = cw(bx - 1 + a);
+  const int cy0 = __ldg(ubase + nf + y0) - 1;
+  const int ny = min(__ldg(ubase + nf + ylast) + 3 - cy0, maxcy);
+  const int cz0 = __ldg(ubase + 2 * nf) - 1;
+  const int nz = min(__ldg(ubase + 2 * nf + nf - 1) + 3 - cz0, maxcz);
+  T *Q = P + (size_t)NF * maxcy * maxcz;  // [NF][maxcy][nf]
+  const size_t rs = (size_t)(2 * (nc / 2 + 1));
+  const int tile = ny * nz;
+  for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+    int cy = cw(cy0 + e / nz), cz = cw(cz0 + e % nz);
+    T v[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) v[f] = 0;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      size_t k = ((size_t)ixw[a] * nc + cy) * rs + cz;
+#pragma unroll
+      for (int f = 0; f < NF; ++f) v[f] += wx[a] * __ldg(fp.src[f] + k);
+    }
+#pragma unroll
+    for (int f = 0; f < NF; ++f) P[f * tile + e] = v[f];
+  }
+  __syncthreads();
+  for (int z = threadIdx.x; z < nf; z += blockDim.x) {
+    T wz[4];
+    catmull_rom<T>(__ldg(frac + 2 * nf + z), wz);
+    const int pz = __ldg(ubase + 2 * nf + z) - 1 - cz0;
+    for (int cy = 0; cy < ny; ++cy) {
+      const int rowp = cy * nz + pz;
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        T q = 0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) q += wz[c] * P[f * tile + rowp + c];
+        Q[((size_t)f * maxcy + cy) * nf + z] = q;
+      }
+    }
+  }
+  __syncthreads();
+  const size_t frs = (size_t)(2 * (nf / 2 + 1));
+  for (int y = y0; y <= ylast; ++y) {
+    T wy[4];
+    catmull_rom<T>(__ldg(frac + nf + y), wy);
+    const int py = __ldg(ubase + nf + y) - 1 - cy0;
+    for (int z = threadIdx.x; z < nf; z += blockDim.x) {
+      T s[NF];
+#pragma unroll
+      for (int f = 0; f < NF; ++f) s[f] = 0;
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) s[f] += wy[b] * Q[((size_t)f * maxcy + py + b) * nf + z];
+      }
+      size_t dst = ((size_t)x * nf + y) * frs + z;
+#pragma unroll
+      for (int f = 0; f < NF; ++f) fp.dst[f][dst] += s[f];
+    }
+  }
+}
+
+// The same with the direct 4 x 4 contraction of P per fine cell (smaller shared memory:
+// P only), for geometries whose Q does not fit.
+template <typename T, int NF, int TY>
+__global__ void __launch_bounds__(256) k_interp_add_tile(FieldPtrs<T, NF> fp, int nc, int wrap,
                                                         const int *__restrict__ base, const T *__restrict__ frac,
                                                         const int *__restrict__ ubase, int nf, int maxcz) {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -186,9 +265,10 @@ void interp_add(Context &ctx, const Level &coarse, const T *const *src, const Le
   launched();
   double ratio = fine.dx / coarse.dx;
   int span = (int)std::ceil(nf * ratio) + 6;
-  constexpr int TY = 8;
+  // fine rows per CTA: more rows amortise the coarse contractions, within 96 KB of P and Q
+  constexpr int TY = NF == 1 ? 32 : 16;
   int ny = (int)std::ceil(TY * ratio) + 6;
-  size_t smem = (size_t)NF * ny * span * sizeof(T);
+  size_t smem = (size_t)NF * ny * ((size_t)span + nf) * sizeof(T);
   FieldPtrs<T, NF> fp;
   for (int f = 0; f < NF; ++f) {
     fp.src[f] = src[f];
@@ -205,7 +285,22 @@ void interp_add(Context &ctx, const Level &coarse, const T *const *src, const Le
       mask.fetch_or(1 << (dev & 31));
     }
     dim3 grid((nf + TY - 1) / TY, nf);
-    k_interp_add_sep<T, NF, TY><<<grid, 256, smem, ctx.stream>>>(fp, coarse.n, wrap, base, frac, ubase, nf, span);
+    k_interp_add_sep<T, NF, TY><<<grid, 256, smem, ctx.stream>>>(fp, coarse.n, wrap, base, frac, ubase, nf, span, ny);
+    launched();
+  } else if (ratio <= 1.0 && (size_t)NF * ((size_t)std::ceil(8 * ratio) + 6) * span * sizeof(T) <= 96 * 1024) {
+    constexpr int TY8 = 8;
+    const int ny8 = (int)std::ceil(TY8 * ratio) + 6;
+    const size_t smem8 = (size_t)NF * ny8 * span * sizeof(T);
+    static std::atomic<int> mask{0};
+    int dev = 0;
+    GIC_CUDA(cudaGetDevice(&dev));
+    if (!(mask.load() & (1 << (dev & 31)))) {
+      GIC_CUDA(cudaFuncSetAttribute((const void *)k_interp_add_tile<T, NF, TY8>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+      mask.fetch_or(1 << (dev & 31));
+    }
+    dim3 grid((nf + TY8 - 1) / TY8, nf);
+    k_interp_add_tile<T, NF, TY8><<<grid, 256, smem8, ctx.stream>>>(fp, coarse.n, wrap, base, frac, ubase, nf, span);
     launched();
   } else {
     k_interp_add_direct<T, NF><<<(unsigned)((m + 255) / 256), 256, 0, ctx.stream>>>(fp, coarse.n, wrap, base, frac,
