@@ -500,7 +500,7 @@ struct TileStages<T, L, TC, TCP, NT, NS, SIGN, TWM, true> {
 template <typename T, int L, int TC, int NT, int SIGN>
 __global__ void __launch_bounds__(NT) k_fft_cols(typename Cx<T>::type *data, long long B,
                                                  const typename Cx<T>::type *tw, T scale, const double *tab, int a0,
-                                                 int A) {
+                                                 int A, int m0, int mn) {
   using C = typename Cx<T>::type;
   constexpr int TCP = TC + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -508,9 +508,11 @@ __global__ void __launch_bounds__(NT) k_fft_cols(typename Cx<T>::type *data, lon
   const long long b0 = (long long)blockIdx.x * TC;
   C *base = data + (size_t)((a0 + (int)blockIdx.y) % A) * (size_t)L * (size_t)B + b0;
   const int tcv = (int)min((long long)TC, B - b0);
+  // the window limits the loads of a forward pass and the stores of an inverse one
+  const int lm0 = SIGN < 0 ? m0 : 0, lmn = SIGN < 0 ? mn : L, sm0 = SIGN > 0 ? m0 : 0, smn = SIGN > 0 ? mn : L;
   for (int e = threadIdx.x; e < L * TC; e += NT) {
     const int i = e / TC, c = e % TC;
-    if (c < tcv) {
+    if (c < tcv && (i - lm0 + L) % L < lmn) {
       cp_async<sizeof(C)>(tile + i * TCP + c, base + (size_t)i * (size_t)B + c);
     } else {
       C z;
@@ -531,7 +533,7 @@ __global__ void __launch_bounds__(NT) k_fft_cols(typename Cx<T>::type *data, lon
   TileStages<T, L, TC, TCP, NT, 1, SIGN, 1>::run(tile, tw);
   for (int e = threadIdx.x; e < L * TC; e += NT) {
     const int i = e / TC, c = e % TC;
-    if (c < tcv) {
+    if (c < tcv && (i - sm0 + L) % L < smn) {
       C v = cscale(tile[i * TCP + c], scale);
       if (SIGN < 0 && tab) v = cscale(v, (T)qtab(tab, L, i, b0 + c));
       base[(size_t)i * (size_t)B + c] = v;
@@ -654,6 +656,9 @@ __device__ __forceinline__ C czero() {
 
 // CG: load through L2 only (ld.global.cg), for data that other CTAs of the same
 // launch wrote
+// m0, mn: the positions (m0 + i) mod L, i < mn, along the transform that are read
+// (others are zero: forward passes) or written (others are not wanted: inverse
+// passes); mn = L for all
 template <typename C, bool CG = false>
 struct ColsIn {
   const C *base;
@@ -662,8 +667,9 @@ struct ColsIn {
   const double *tab;  // optional multiplier (x pass of an L^3 grid)
   int L;
   long long b0;
+  int m0 = 0, mn = 1 << 30;
   __device__ __forceinline__ C operator()(int c, int m) const {
-    if (c >= tcv) return czero<C>();
+    if (c >= tcv || (m - m0 + L) % L >= mn) return czero<C>();
     const C *p = base + (size_t)m * (size_t)B + c;
     C v = CG ? __ldcg(p) : *p;
     return tab ? cscale(v, (decltype(v.x))qtab(tab, L, m, b0 + c)) : v;
@@ -678,8 +684,9 @@ struct ColsOut {
   const double *tab;
   int L;
   long long b0;
+  int m0 = 0, mn = 1 << 30;
   __device__ __forceinline__ void operator()(int c, int m, C v) const {
-    if (c >= tcv) return;
+    if (c >= tcv || (m - m0 + L) % L >= mn) return;
     v = cscale(v, scale);
     if (tab) v = cscale(v, (T)qtab(tab, L, m, b0 + c));
     base[(size_t)m * (size_t)B + c] = v;
@@ -723,17 +730,20 @@ struct RowsIn {
 template <typename T, int L, int TC, int NT, int SIGN>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_fft_cols_fused(typename Cx<T>::type *data, long long B,
                                                        const typename Cx<T>::type *tw, T scale, const double *tab,
-                                                       int a0, int A) {
+                                                       int a0, int A, int m0, int mn) {
   using C = typename Cx<T>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
   C *tile = reinterpret_cast<C *>(smraw);
   const long long b0 = (long long)blockIdx.x * TC;
   C *base = data + (size_t)((a0 + (int)blockIdx.y) % A) * (size_t)L * (size_t)B + b0;
   const int tcv = (int)min((long long)TC, B - b0);
-  first_stage_from<T, L, TC, NT, SIGN>(tile, ColsIn<C>{base, B, tcv, SIGN > 0 ? tab : nullptr, L, b0});
+  // the window limits the loads of a forward pass and the stores of an inverse one
+  const int lm0 = SIGN < 0 ? m0 : 0, lmn = SIGN < 0 ? mn : L, sm0 = SIGN > 0 ? m0 : 0, smn = SIGN > 0 ? mn : L;
+  first_stage_from<T, L, TC, NT, SIGN>(tile, ColsIn<C>{base, B, tcv, SIGN > 0 ? tab : nullptr, L, b0, lm0, lmn});
   constexpr int R0 = next_radix(L, 1), NSL = last_stage_ns(L);
   TileStagesUntil<T, L, TC, TC, NT, R0, NSL, SIGN, 1>::run(tile, tw);
-  last_stage_to<T, L, TC, NT, SIGN, 1>(tile, tw, ColsOut<C, T>{base, B, tcv, scale, SIGN < 0 ? tab : nullptr, L, b0});
+  last_stage_to<T, L, TC, NT, SIGN, 1>(tile, tw,
+                                       ColsOut<C, T>{base, B, tcv, scale, SIGN < 0 ? tab : nullptr, L, b0, sm0, smn});
 }
 
 template <typename T, int H, int RPC, int NT>
@@ -1030,22 +1040,23 @@ struct FixedFft {
   static Sel whole_sel() { return Sel{0, N, 0, N}; }
 
   template <int TC, int NT, int SIGN>
-  static void cols(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const double *tab, int a0, int na) {
+  static void cols(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const double *tab, int a0, int na,
+                   int m0, int mn) {
     static std::atomic<int> mask{0};
     const size_t smem = (size_t)N * (TC + 1) * sizeof(C);
     set_smem_once((const void *)k_fft_cols<T, N, TC, NT, SIGN>, smem, mask);
     dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)na);
-    k_fft_cols<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A);
+    k_fft_cols<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A, m0, mn);
     launched();
   }
   template <int TC, int NT, int SIGN>
   static void cols_fused(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const double *tab, int a0,
-                         int na) {
+                         int na, int m0, int mn) {
     static std::atomic<int> mask{0};
     const size_t smem = (size_t)N * TC * sizeof(C);
     set_smem_once((const void *)k_fft_cols_fused<T, N, TC, NT, SIGN>, smem, mask);
     dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)na);
-    k_fft_cols_fused<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A);
+    k_fft_cols_fused<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A, m0, mn);
     launched();
   }
   // row tiles of RPC rows covering the selection: grid (tiles, planes); for a
@@ -1092,22 +1103,23 @@ struct FixedFft {
     }
     launched();
   }
-  // a0, na: the planes (a0 + i) mod A, i < na, of the strided pass (na < 0: all A)
+  // a0, na: the planes (a0 + i) mod A, i < na, of the strided pass (na < 0: all A);
+  // m0, mn: the positions along the transform read (forward) or written (inverse)
   static void cols_cfg(Context &ctx, int cfg, int sign, C *d, int A, long long B, const C *tw, T scale,
-                       const double *tab = nullptr, int a0 = 0, int na = -1) {
+                       const double *tab = nullptr, int a0 = 0, int na = -1, int m0 = 0, int mn = N) {
     if (na < 0) na = A;
     if (cfg == 2) {
-      if (sign > 0) cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na);
-      else cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na);
+      if (sign > 0) cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn);
+      else cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn);
     } else if (cfg == 3) {
-      if (sign > 0) cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, +1>(ctx, d, A, B, tw, scale, tab, a0, na);
-      else cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, -1>(ctx, d, A, B, tw, scale, tab, a0, na);
+      if (sign > 0) cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn);
+      else cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn);
     } else if (cfg == 0) {
-      if (sign > 0) cols<F32 ? 8 : 4, 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na);
-      else cols<F32 ? 8 : 4, 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na);
+      if (sign > 0) cols<F32 ? 8 : 4, 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn);
+      else cols<F32 ? 8 : 4, 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn);
     } else {
-      if (sign > 0) cols<F32 ? 16 : 8, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na);
-      else cols<F32 ? 16 : 8, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na);
+      if (sign > 0) cols<F32 ? 16 : 8, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn);
+      else cols<F32 ? 16 : 8, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn);
     }
   }
   static void rows_cfg(Context &ctx, int cfg, bool inv, C *d, const C *tw, T scale, const Sel &sel = whole_sel()) {
@@ -1166,12 +1178,13 @@ struct FixedFft {
   // planes and the real transforms of the selected rows (output valid there)
   static void c2r(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, int pv, const double *tab,
                   const Sel &sel) {
-    cols_cfg(ctx, ccfg, +1, c, 1, (long long)N * S, tw, (T)1, tab);
+    // the x pass stores the selected planes only, the y pass the selected rows only
+    cols_cfg(ctx, ccfg, +1, c, 1, (long long)N * S, tw, (T)1, tab, 0, -1, sel.x0, sel.nx);
     if (kPlanes && pv >= 0 && sel.whole()) {
       planes<true>(ctx, c, tw, scale, pv);
       return;
     }
-    cols_cfg(ctx, ccfg, +1, c, N, S, tw, (T)1, nullptr, sel.x0, sel.nx);
+    cols_cfg(ctx, ccfg, +1, c, N, S, tw, (T)1, nullptr, sel.x0, sel.nx, sel.y0, sel.ny);
     rows_cfg(ctx, rcfg, true, c, tw, scale, sel);
   }
   // forward, input zero outside the selection: the selected rows, the selected
@@ -1182,9 +1195,11 @@ struct FixedFft {
       planes<false>(ctx, c, tw, (T)1, pv);
     } else {
       rows_cfg(ctx, rcfg, false, c, tw, (T)1, sel);
-      cols_cfg(ctx, ccfg, -1, c, N, S, tw, (T)1, nullptr, sel.x0, sel.nx);
+      // rows outside the selection are zero: the y pass does not read them
+      cols_cfg(ctx, ccfg, -1, c, N, S, tw, (T)1, nullptr, sel.x0, sel.nx, sel.y0, sel.ny);
     }
-    cols_cfg(ctx, ccfg, -1, c, 1, (long long)N * S, tw, scale, tab);
+    // planes outside the selection are zero: the x pass does not read them
+    cols_cfg(ctx, ccfg, -1, c, 1, (long long)N * S, tw, scale, tab, 0, -1, sel.x0, sel.nx);
   }
   // time every candidate on a scratch array of the transform's size
   static void tune(Context &ctx, const C *tw, int &best_cols, int &best_rows, int &best_planes) {

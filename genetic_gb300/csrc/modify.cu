@@ -143,47 +143,48 @@ struct BlockFields {
   const T *b[kBlockB];
   int na, nb;
 };
-// per-thread accumulator of Hermitian-weighted products: a compensated float pair for
-// float fields (every product split exactly with fma, as k_inner), a double for double
+// Sums of one row's products in the field's precision, then rows accumulated in a
+// compensated float pair (float fields) or a double: float fields carry 6e-8
+// relative rounding already, and a row holds at most N/2 + 1 products.
 template <typename T>
-struct ProdAcc;
+struct RowAcc;
 template <>
-struct ProdAcc<float> {
-  float s = 0.f, e = 0.f;
-  __device__ __forceinline__ void add(float ar, float ai, float br, float bi, float w) {
-    float p1 = ar * br, p2 = ai * bi;
-    float e1 = fmaf(ar, br, -p1), e2 = fmaf(ai, bi, -p2);
-    float t = s + w * p1, bb = t - s;
-    e += (s - (t - bb)) + (w * p1 - bb);
+struct RowAcc<float> {
+  float s, e;
+  __device__ __forceinline__ void zero() { s = e = 0.f; }
+  __device__ __forceinline__ void add(float x) {
+    const float t = s + x, bb = t - s;
+    e += (s - (t - bb)) + (x - bb);
     s = t;
-    t = s + w * p2;
-    bb = t - s;
-    e += (s - (t - bb)) + (w * p2 - bb);
-    s = t;
-    e += w * (e1 + e2);
   }
   __device__ __forceinline__ double get() const { return (double)s + (double)e; }
 };
 template <>
-struct ProdAcc<double> {
-  double s = 0;
-  __device__ __forceinline__ void add(double ar, double ai, double br, double bi, double w) {
-    s += w * (ar * br + ai * bi);
-  }
+struct RowAcc<double> {
+  double s;
+  __device__ __forceinline__ void zero() { s = 0; }
+  __device__ __forceinline__ void add(double x) { s += x; }
   __device__ __forceinline__ double get() const { return s; }
 };
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_inner_block(BlockFields<T> f, int n, double *partial, int ia0, int jb0,
+__global__ void __launch_bounds__(256, 3) k_inner_block(BlockFields<T> f, int n, double *partial, int ia0, int jb0,
                                                      int nb_total, size_t pstride) {
   __shared__ double red[256];
+  // the row accumulators live in shared memory (one column per thread, touched once
+  // per row), which keeps the registers for the loads in flight
+  __shared__ RowAcc<T> acc[kBlockA * kBlockB][kKzChunk * kRowsPerBlock];
   const int H = n / 2, S = H + 1;
   const unsigned rows = (unsigned)n * (unsigned)n;
   const int tid = threadIdx.y * kKzChunk + threadIdx.x;
-  ProdAcc<T> acc[kBlockA * kBlockB];
+#pragma unroll
+  for (int p = 0; p < kBlockA * kBlockB; ++p) acc[p][tid].zero();
   // a warp walks whole rows (one contiguous span of S coefficients per field), rows
   // strided over the grid
   for (unsigned r = blockIdx.x * kRowsPerBlock + threadIdx.y; r < rows; r += gridDim.x * kRowsPerBlock) {
+    T row[kBlockA * kBlockB];
+#pragma unroll
+    for (int p = 0; p < kBlockA * kBlockB; ++p) row[p] = 0;
     for (int iz = threadIdx.x; iz < S; iz += kKzChunk) {
       const T w = (iz == 0 || iz == H) ? (T)1 : (T)2;
       const size_t id = 2 * ((size_t)r * S + iz);
@@ -200,17 +201,15 @@ __global__ void __launch_bounds__(256) k_inner_block(BlockFields<T> f, int n, do
           const T ar = f.a[i][id], ai = f.a[i][id + 1];
 #pragma unroll
           for (int j = 0; j < kBlockB; ++j)
-            if (j < f.nb) acc[i * kBlockB + j].add(ar, ai, br[j], bi[j], w);
+            if (j < f.nb) row[i * kBlockB + j] += w * (ar * br[j] + ai * bi[j]);
         }
     }
+#pragma unroll
+    for (int p = 0; p < kBlockA * kBlockB; ++p) acc[p][tid].add(row[p]);
   }
   for (int i = 0; i < f.na; ++i)
     for (int j = 0; j < f.nb; ++j) {
-      double v = 0;
-#pragma unroll
-      for (int p = 0; p < kBlockA * kBlockB; ++p)
-        if (p == i * kBlockB + j) v = acc[p].get();
-      red[tid] = v;
+      red[tid] = acc[i * kBlockB + j][tid].get();
       __syncthreads();
       for (int s2 = 128; s2 > 0; s2 >>= 1) {
         if (tid < s2) red[tid] += red[tid + s2];
@@ -240,19 +239,21 @@ __global__ void k_scale(T *a, double c, size_t n) {
 template <typename T>
 __global__ void k_window_op(T *r, const T *s, int n, const unsigned char *mx, const unsigned char *my,
                             const unsigned char *mz, int op) {
-  // one thread per cell, flat over the n^3 cells (rows of n, padded in memory)
-  const unsigned long long e = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= (unsigned long long)n * n * n) return;
-  const unsigned row = (unsigned)(e / (unsigned)n);
-  const int z = (int)(e - (unsigned long long)row * (unsigned)n);
-  int x = (int)(row / (unsigned)n), y = (int)(row % (unsigned)n);
-  bool in = mx[x] && my[y] && mz[z];
-  size_t id = (size_t)row * (size_t)(2 * (n / 2 + 1)) + z;
-  if (op == 0) r[id] = (in ? (T)0 : r[id]) + s[id];
-  else if (op == 1) { if (in) r[id] = s[id]; }
-  else r[id] = in ? s[id] : (T)0;
+  // a CTA per row of n cells: the row's x and y window tests once, then its cells
+  const unsigned row = blockIdx.x;
+  const int x = (int)(row / (unsigned)n), y = (int)(row - (unsigned)x * (unsigned)n);
+  const bool row_in = mx[x] && my[y];
+  const size_t base = (size_t)row * (size_t)(2 * (n / 2 + 1));
+  for (int z = threadIdx.x; z < n; z += blockDim.x) {
+    const bool in = row_in && mz[z];
+    const size_t id = base + z;
+    if (op == 0) r[id] = (in ? (T)0 : r[id]) + s[id];
+    else if (op == 1) { if (in) r[id] = s[id]; }
+    else r[id] = in ? s[id] : (T)0;
+  }
 }
-inline dim3 real_grid(int n) { return dim3((unsigned)(((unsigned long long)n * n * n + 255) / 256)); }
+inline dim3 real_grid(int n) { return dim3((unsigned)((unsigned long long)n * n)); }
+inline dim3 real_block(int n) { return dim3((unsigned)std::min(256, (n + 31) / 32 * 32)); }
 
 // Hermitian-weighted Re(conj(a) b) over a half spectrum, partial sums per block.
 // Float fields: every product is split exactly (fma) and accumulated in a
@@ -966,7 +967,7 @@ struct ModEngine {
   void window_op(T *r, const T *src, int l, int op) {
     int n = lev(l).n;
     unsigned char *m = S.masks.template as<unsigned char>();
-    k_window_op<T><<<real_grid(n), hs_block(), 0, ctx.stream>>>(r, src, n, m, m + n, m + 2 * n, op);
+    k_window_op<T><<<real_grid(n), real_block(n), 0, ctx.stream>>>(r, src, n, m, m + n, m + 2 * n, op);
     launched();
   }
 
