@@ -59,8 +59,11 @@ template <typename C> __device__ __forceinline__ C twid(const C *tw, int m, int 
 }
 
 // per-|k|^2 table value at half-spectrum cell (kx, col), col = ky (N/2 + 1) + kz, of
-// an N^3 grid: the multiplier fused into the x pass (first of c2r, last of r2c)
-__device__ __forceinline__ double qtab(const double *tab, int N, int kx, long long col) {
+// an N^3 grid: the multiplier fused into the x pass (first of c2r, last of r2c).
+// Tables are in the transform's precision: a float FFT reads float values, as a
+// double-to-float conversion per element would occupy the FP64 pipe.
+template <typename TT>
+__device__ __forceinline__ TT qtab(const TT *tab, int N, int kx, long long col) {
   const int S = N / 2 + 1, H = N / 2;
   const int ky = (int)(col / S), kz = (int)(col - (long long)ky * S);
   const long long a = kx > H ? kx - N : kx, b = ky > H ? ky - N : ky;
@@ -169,7 +172,7 @@ template <typename T, int R, int TC>
 __device__ __forceinline__ void strided_stage(const typename Cx<T>::type *src, typename Cx<T>::type *dst,
                                               typename Cx<T>::type *gout, long long B, int tcv, int L, int Ns,
                                               int ns_log, int sign, const typename Cx<T>::type *tw, T scale,
-                                              const double *tab, long long b0) {
+                                              const T *tab, long long b0) {
   using C = typename Cx<T>::type;
   const int LR = L / R;
   const int nb = LR * TC;
@@ -191,7 +194,7 @@ __device__ __forceinline__ void strided_stage(const typename Cx<T>::type *src, t
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           C o = cscale(v[r], scale);
-          if (tab) o = cscale(o, (T)qtab(tab, L, d + r * Ns, b0 + c));
+          if (tab) o = cscale(o, qtab(tab, L, d + r * Ns, b0 + c));
           gout[(size_t)(d + r * Ns) * (size_t)B + c] = o;
         }
       }
@@ -207,7 +210,7 @@ __device__ __forceinline__ void strided_stage(const typename Cx<T>::type *src, t
 template <typename T, int TC>
 __global__ void __launch_bounds__(256) k_fft_strided(typename Cx<T>::type *data, int L, long long B,
                                                      Radix plan, int sign, const typename Cx<T>::type *tw,
-                                                     T scale, const double *tab) {
+                                                     T scale, const T *tab) {
   using C = typename Cx<T>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
   C *buf0 = reinterpret_cast<C *>(smraw);
@@ -232,11 +235,11 @@ __global__ void __launch_bounds__(256) k_fft_strided(typename Cx<T>::type *data,
   if (sign > 0 && tab) {
     for (int e = threadIdx.x; e < L * TC; e += blockDim.x) {
       int i = e / TC, c = e % TC;
-      if (c < tcv) buf0[e] = cscale(buf0[e], (T)qtab(tab, L, i, b0 + c));
+      if (c < tcv) buf0[e] = cscale(buf0[e], qtab(tab, L, i, b0 + c));
     }
     __syncthreads();
   }
-  const double *otab = sign < 0 ? tab : nullptr;
+  const T *otab = sign < 0 ? tab : nullptr;
   C *src = buf0, *dst = buf1;
   int Ns = 1, ns_log = 0;
   for (int s = 0; s < plan.n; ++s) {
@@ -499,7 +502,7 @@ struct TileStages<T, L, TC, TCP, NT, NS, SIGN, TWM, true> {
 // the inputs when SIGN > 0 (c2r) and to the scaled outputs when SIGN < 0 (r2c)
 template <typename T, int L, int TC, int NT, int SIGN>
 __global__ void __launch_bounds__(NT) k_fft_cols(typename Cx<T>::type *data, long long B,
-                                                 const typename Cx<T>::type *tw, T scale, const double *tab, int a0,
+                                                 const typename Cx<T>::type *tw, T scale, const T *tab, int a0,
                                                  int A, int m0, int mn) {
   using C = typename Cx<T>::type;
   constexpr int TCP = TC + 1;
@@ -526,7 +529,7 @@ __global__ void __launch_bounds__(NT) k_fft_cols(typename Cx<T>::type *data, lon
   if (SIGN > 0 && tab) {
     for (int e = threadIdx.x; e < L * tcv; e += NT) {
       const int i = e / tcv, c = e % tcv;
-      tile[i * TCP + c] = cscale(tile[i * TCP + c], (T)qtab(tab, L, i, b0 + c));
+      tile[i * TCP + c] = cscale(tile[i * TCP + c], qtab(tab, L, i, b0 + c));
     }
     __syncthreads();
   }
@@ -535,7 +538,7 @@ __global__ void __launch_bounds__(NT) k_fft_cols(typename Cx<T>::type *data, lon
     const int i = e / TC, c = e % TC;
     if (c < tcv && (i - sm0 + L) % L < smn) {
       C v = cscale(tile[i * TCP + c], scale);
-      if (SIGN < 0 && tab) v = cscale(v, (T)qtab(tab, L, i, b0 + c));
+      if (SIGN < 0 && tab) v = cscale(v, qtab(tab, L, i, b0 + c));
       base[(size_t)i * (size_t)B + c] = v;
     }
   }
@@ -664,7 +667,7 @@ struct ColsIn {
   const C *base;
   long long B;
   int tcv;
-  const double *tab;  // optional multiplier (x pass of an L^3 grid)
+  const decltype(C::x) *tab;  // optional multiplier (x pass of an L^3 grid), field precision
   int L;
   long long b0;
   int m0 = 0, mn = 1 << 30;
@@ -672,7 +675,7 @@ struct ColsIn {
     if (c >= tcv || (m - m0 + L) % L >= mn) return czero<C>();
     const C *p = base + (size_t)m * (size_t)B + c;
     C v = CG ? __ldcg(p) : *p;
-    return tab ? cscale(v, (decltype(v.x))qtab(tab, L, m, b0 + c)) : v;
+    return tab ? cscale(v, qtab(tab, L, m, b0 + c)) : v;
   }
 };
 template <typename C, typename T>
@@ -681,14 +684,14 @@ struct ColsOut {
   long long B;
   int tcv;
   T scale;
-  const double *tab;
+  const T *tab;
   int L;
   long long b0;
   int m0 = 0, mn = 1 << 30;
   __device__ __forceinline__ void operator()(int c, int m, C v) const {
     if (c >= tcv || (m - m0 + L) % L >= mn) return;
     v = cscale(v, scale);
-    if (tab) v = cscale(v, (T)qtab(tab, L, m, b0 + c));
+    if (tab) v = cscale(v, qtab(tab, L, m, b0 + c));
     base[(size_t)m * (size_t)B + c] = v;
   }
 };
@@ -729,7 +732,7 @@ struct RowsIn {
 
 template <typename T, int L, int TC, int NT, int SIGN>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_fft_cols_fused(typename Cx<T>::type *data, long long B,
-                                                       const typename Cx<T>::type *tw, T scale, const double *tab,
+                                                       const typename Cx<T>::type *tw, T scale, const T *tab,
                                                        int a0, int A, int m0, int mn) {
   using C = typename Cx<T>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -1040,7 +1043,7 @@ struct FixedFft {
   static Sel whole_sel() { return Sel{0, N, 0, N}; }
 
   template <int TC, int NT, int SIGN>
-  static void cols(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const double *tab, int a0, int na,
+  static void cols(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const T *tab, int a0, int na,
                    int m0, int mn) {
     static std::atomic<int> mask{0};
     const size_t smem = (size_t)N * (TC + 1) * sizeof(C);
@@ -1050,7 +1053,7 @@ struct FixedFft {
     launched();
   }
   template <int TC, int NT, int SIGN>
-  static void cols_fused(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const double *tab, int a0,
+  static void cols_fused(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const T *tab, int a0,
                          int na, int m0, int mn) {
     static std::atomic<int> mask{0};
     const size_t smem = (size_t)N * TC * sizeof(C);
@@ -1106,7 +1109,7 @@ struct FixedFft {
   // a0, na: the planes (a0 + i) mod A, i < na, of the strided pass (na < 0: all A);
   // m0, mn: the positions along the transform read (forward) or written (inverse)
   static void cols_cfg(Context &ctx, int cfg, int sign, C *d, int A, long long B, const C *tw, T scale,
-                       const double *tab = nullptr, int a0 = 0, int na = -1, int m0 = 0, int mn = N) {
+                       const T *tab = nullptr, int a0 = 0, int na = -1, int m0 = 0, int mn = N) {
     if (na < 0) na = A;
     if (cfg == 2) {
       if (sign > 0) cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn);
@@ -1176,7 +1179,7 @@ struct FixedFft {
   }
   // inverse: the x pass over every column, then the y transforms of the selected
   // planes and the real transforms of the selected rows (output valid there)
-  static void c2r(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, int pv, const double *tab,
+  static void c2r(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, int pv, const T *tab,
                   const Sel &sel) {
     // the x pass stores the selected planes only, the y pass the selected rows only
     cols_cfg(ctx, ccfg, +1, c, 1, (long long)N * S, tw, (T)1, tab, 0, -1, sel.x0, sel.nx);
@@ -1189,7 +1192,7 @@ struct FixedFft {
   }
   // forward, input zero outside the selection: the selected rows, the selected
   // planes' y transforms, then the x pass over every column
-  static void r2c(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, int pv, const double *tab,
+  static void r2c(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, int pv, const T *tab,
                   const Sel &sel) {
     if (kPlanes && pv >= 0 && sel.whole()) {
       planes<false>(ctx, c, tw, (T)1, pv);
@@ -1258,7 +1261,7 @@ std::vector<SharedTune> g_tuned;
 
 template <typename T, int N>
 void fixed_transform(Context &ctx, typename Cx<T>::type *c, const typename Cx<T>::type *tw, double scale, bool inverse,
-                     const double *tab, const CellBox *box) {
+                     const T *tab, const CellBox *box) {
   FftTables &F = ctx.fft;
   const bool dbl = sizeof(T) == 8;
   int cc = -1, rc = -1, pv = -1;
@@ -1304,7 +1307,7 @@ void fixed_transform(Context &ctx, typename Cx<T>::type *c, const typename Cx<T>
 // power-of-two sizes 32..1024 use the fixed-length passes
 template <typename T>
 bool fixed_dispatch(Context &ctx, typename Cx<T>::type *c, int n, const typename Cx<T>::type *tw, double scale,
-                    bool inverse, const double *tab, const CellBox *box) {
+                    bool inverse, const T *tab, const CellBox *box) {
   switch (n) {
     case 32: fixed_transform<T, 32>(ctx, c, tw, scale, inverse, tab, box); return true;
     case 64: fixed_transform<T, 64>(ctx, c, tw, scale, inverse, tab, box); return true;
@@ -1318,7 +1321,7 @@ bool fixed_dispatch(Context &ctx, typename Cx<T>::type *c, int n, const typename
 
 template <typename T>
 void strided_pass(Context &ctx, typename Cx<T>::type *data, int A, int L, long long B, int sign, T scale,
-                  const typename Cx<T>::type *tw, const double *tab = nullptr) {
+                  const typename Cx<T>::type *tw, const T *tab = nullptr) {
   constexpr int TC = sizeof(T) == 4 ? 8 : 4;
   Radix plan = make_plan(L);
   size_t smem = 2ull * L * TC * sizeof(typename Cx<T>::type);
@@ -1377,7 +1380,7 @@ const void *FftTables::get(int n, bool dbl, cudaStream_t s) {
 }
 
 template <typename T>
-void fft_c2r_3d(Context &ctx, T *data, int n, double scale, const double *pre_tab, const CellBox *box) {
+void fft_c2r_3d(Context &ctx, T *data, int n, double scale, const T *pre_tab, const CellBox *box) {
   using C = typename Cx<T>::type;
   if (n < 2 || n % 2) fail(GIC_ERR_INVALID_ARG, "FFT size must be even");
   const C *tw = (const C *)ctx.fft.get(n, sizeof(T) == 8, ctx.stream);
@@ -1400,7 +1403,7 @@ void fft_c2r_3d(Context &ctx, T *data, int n, double scale, const double *pre_ta
 }
 
 template <typename T>
-void fft_r2c_3d(Context &ctx, T *data, int n, double scale, const double *post_tab, const CellBox *box) {
+void fft_r2c_3d(Context &ctx, T *data, int n, double scale, const T *post_tab, const CellBox *box) {
   using C = typename Cx<T>::type;
   if (n < 2 || n % 2) fail(GIC_ERR_INVALID_ARG, "FFT size must be even");
   const C *tw = (const C *)ctx.fft.get(n, sizeof(T) == 8, ctx.stream);
@@ -1427,9 +1430,9 @@ bool take_fft_wait_error(Context &ctx) {
   return true;
 }
 
-template void fft_c2r_3d<float>(Context &, float *, int, double, const double *, const CellBox *);
+template void fft_c2r_3d<float>(Context &, float *, int, double, const float *, const CellBox *);
 template void fft_c2r_3d<double>(Context &, double *, int, double, const double *, const CellBox *);
-template void fft_r2c_3d<float>(Context &, float *, int, double, const double *, const CellBox *);
+template void fft_r2c_3d<float>(Context &, float *, int, double, const float *, const CellBox *);
 template void fft_r2c_3d<double>(Context &, double *, int, double, const double *, const CellBox *);
 
 }  // namespace gic

@@ -81,7 +81,7 @@ struct BufPool {
 // scratch of the modification algebra (one user at a time; each buffer is used
 // within a single operation)
 struct ModScratch {
-  DevBuf tab, masks, tmp_src, win, cells, geom, t1, t2, t3, reduce, compact, csum;
+  DevBuf tab, tabf, conv, masks, tmp_src, win, cells, geom, t1, t2, t3, reduce, compact, csum;
 };
 
 // One grid level: N^3 cells of a cube of side `box` whose lower corner is x0.
@@ -101,6 +101,7 @@ struct Level {
   DevBuf tab_main;       // sqrt(P_grid), times the high-pass filter on zoom levels
   DevBuf tab_lp_src;     // sqrt(P_grid) * low-pass (source side of the next zoom)
   DevBuf tab_lp;         // low-pass filter alone
+  DevBuf tab_main_f, tab_lp_src_f, tab_lp_f;  // float copies of the three (float fields)
   DevBuf field2[3];      // second-order displacements psi2_x, psi2_y, psi2_z (real)
   DevBuf pos, vel;       // particles: pos double[3M], vel (precision)[3M]
   bool have_noise = false;
@@ -219,6 +220,19 @@ __device__ __forceinline__ bool hs_cell(int n, unsigned &row, int &iz) {
 #endif
 inline unsigned long long hs_elements(int n) { return (unsigned long long)n * n * (n / 2 + 1); }
 
+// A table of nq doubles in the fields' precision: the table itself (T = double) or a
+// float copy made in `shadow` (T = float).  Float kernels read float tables: converting
+// a double per element would occupy the FP64 pipe, a few percent of the FP32 rate.
+template <typename T>
+const T *typed_table(Context &ctx, DevBuf &shadow, const double *tab, size_t nq);
+// the level tables in the fields' precision (their float copies are made with them)
+template <typename T>
+const T *tab_main(const Level &L);
+template <typename T>
+const T *tab_lp_src(const Level &L);
+template <typename T>
+const T *tab_lp(const Level &L);
+
 // fft.cu
 // A box of an n^3 grid's cells: per axis the cyclic range [start, start + len) mod n.
 // Given to a forward transform, its input is zero outside the box; given to an
@@ -257,12 +271,13 @@ inline CellBox footprint_box(const Level &fine, const Level &coarse, int margin)
   return b;
 }
 // pre_tab / post_tab: optional per-|k|^2 multiplier applied to the half spectrum
-// before the inverse / after the forward transform, fused into the x pass
+// before the inverse / after the forward transform, fused into the x pass; in the
+// transform's precision (typed_table gives a float copy of a double table)
 template <typename T>
-void fft_c2r_3d(Context &ctx, T *data, int n, double scale, const double *pre_tab = nullptr,
+void fft_c2r_3d(Context &ctx, T *data, int n, double scale, const T *pre_tab = nullptr,
                 const CellBox *box = nullptr);
 template <typename T>
-void fft_r2c_3d(Context &ctx, T *data, int n, double scale, const double *post_tab = nullptr,
+void fft_r2c_3d(Context &ctx, T *data, int n, double scale, const T *post_tab = nullptr,
                 const CellBox *box = nullptr);
 // after the stream has synchronised: true (with ctx.last_error set) when a wait of the
 // plane pass gave up since the last check; clears the flag

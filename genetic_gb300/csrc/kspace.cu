@@ -122,7 +122,7 @@ template <> struct V2<double> { using type = double2; };
 // positive Nyquist component (zeldovich.hpp:155-181)
 // (outputs: delta may be null; px, py, pz are all null or all set)
 template <typename T>
-__global__ void k_za_fields(const typename V2<T>::type *noise, const double *tab, int n, T kmin,
+__global__ void k_za_fields(const typename V2<T>::type *noise, const T *tab, int n, T kmin,
                             typename V2<T>::type *delta, typename V2<T>::type *px, typename V2<T>::type *py,
                             typename V2<T>::type *pz) {
   using C = typename V2<T>::type;
@@ -166,7 +166,7 @@ __global__ void k_za_fields(const typename V2<T>::type *noise, const double *tab
 // for ab = xx, yy, zz, xy, xz, yz, delta = src * tab[q]; zero at k = 0, and the
 // mixed ones where either component is the Nyquist mode.
 template <typename T>
-__global__ void k_hessian_fields(const typename V2<T>::type *src, const double *tab, int n, T kmin,
+__global__ void k_hessian_fields(const typename V2<T>::type *src, const T *tab, int n, T kmin,
                                  typename V2<T>::type *const *out) {
   using C = typename V2<T>::type;
   const int H = n / 2, S = H + 1;
@@ -201,6 +201,11 @@ __global__ void k_lpt2_source(T *xx, const T *yy, const T *zz, const T *xy, cons
   if (i >= n) return;
   T a = xx[i], b = yy[i], c = zz[i], d = xy[i], e = xz[i], f = yz[i];
   xx[i] = a * b + a * c + b * c - d * d - e * e - f * f;
+}
+
+__global__ void k_table_to_float(float *out, const double *in, long long nq) {
+  long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < nq) out[q] = (float)in[q];
 }
 
 __global__ void k_table_scale(double *t, long long nq, double s) {
@@ -343,6 +348,9 @@ void transfer_setup(Context &ctx, const double *table, int nrows, int ncols) {
     L->tab_main.release();
     L->tab_lp_src.release();
     L->tab_lp.release();
+    L->tab_main_f.release();
+    L->tab_lp_src_f.release();
+    L->tab_lp_f.release();
   }
 }
 
@@ -378,7 +386,10 @@ static void build_level_tables(Context &ctx, int li) {
   double kcut = li > 0 ? level_kcut(*ctx.levels[li - 1]) : 1.0;
   k_filter_table<<<(unsigned)((nq + 255) / 256), 256, 0, ctx.stream>>>(L.tab_main.as<double>(), L.sqrtp.as<double>(),
                                                                        nq, L.kmin(), kcut, li > 0 ? 2 : 0);
-  launched();
+  L.tab_main_f.ensure(nq * sizeof(float));
+  k_table_to_float<<<(unsigned)((nq + 255) / 256), 256, 0, ctx.stream>>>(L.tab_main_f.as<float>(), L.tab_main.as<double>(),
+                                                                         nq);
+  launched(2);
 }
 
 // on the coarse level l-1: sqrt(P) * LP and LP alone, for the copy into level l
@@ -393,7 +404,34 @@ static void build_lowpass_tables(Context &ctx, int coarse_index) {
   unsigned blocks = (unsigned)((nq + 255) / 256);
   k_filter_table<<<blocks, 256, 0, ctx.stream>>>(C.tab_lp_src.as<double>(), C.sqrtp.as<double>(), nq, C.kmin(), kcut, 1);
   k_filter_table<<<blocks, 256, 0, ctx.stream>>>(C.tab_lp.as<double>(), nullptr, nq, C.kmin(), kcut, 1);
-  launched(2);
+  C.tab_lp_src_f.ensure(nq * sizeof(float));
+  C.tab_lp_f.ensure(nq * sizeof(float));
+  k_table_to_float<<<blocks, 256, 0, ctx.stream>>>(C.tab_lp_src_f.as<float>(), C.tab_lp_src.as<double>(), nq);
+  k_table_to_float<<<blocks, 256, 0, ctx.stream>>>(C.tab_lp_f.as<float>(), C.tab_lp.as<double>(), nq);
+  launched(4);
+}
+
+template <>
+const double *tab_main<double>(const Level &L) { return L.tab_main.as<double>(); }
+template <>
+const float *tab_main<float>(const Level &L) { return L.tab_main_f.as<float>(); }
+template <>
+const double *tab_lp_src<double>(const Level &L) { return L.tab_lp_src.as<double>(); }
+template <>
+const float *tab_lp_src<float>(const Level &L) { return L.tab_lp_src_f.as<float>(); }
+template <>
+const double *tab_lp<double>(const Level &L) { return L.tab_lp.as<double>(); }
+template <>
+const float *tab_lp<float>(const Level &L) { return L.tab_lp_f.as<float>(); }
+
+template <>
+const double *typed_table<double>(Context &, DevBuf &, const double *tab, size_t) { return tab; }
+template <>
+const float *typed_table<float>(Context &ctx, DevBuf &shadow, const double *tab, size_t nq) {
+  shadow.ensure(nq * sizeof(float));
+  k_table_to_float<<<(unsigned)((nq + 255) / 256), 256, 0, ctx.stream>>>(shadow.as<float>(), tab, (long long)nq);
+  launched();
+  return shadow.as<float>();
 }
 
 // the fields of `mask` (bit f: field f; kFieldDelta, kFieldsPsi) of level li in real space
@@ -405,7 +443,7 @@ static void za_fields_typed(Context &ctx, int li, unsigned mask) {
   for (int f = 0; f < 4; ++f) L.field[f].ensure(nc * sizeof(C));
   build_level_tables(ctx, li);
   auto out = [&](int f) { return (mask >> f) & 1u ? L.field[f].as<C>() : nullptr; };
-  k_za_fields<T><<<hs_grid(L.n), hs_block(), 0, ctx.stream>>>(L.noise.as<C>(), L.tab_main.as<double>(), L.n, (T)L.kmin(),
+  k_za_fields<T><<<hs_grid(L.n), hs_block(), 0, ctx.stream>>>(L.noise.as<C>(), tab_main<T>(L), L.n, (T)L.kmin(),
                                                  out(0), out(1), out(2), out(3));
   launched();
   double scale = 1.0 / std::pow((double)L.n, 1.5);
@@ -436,7 +474,7 @@ static void zoom_combine_typed(Context &ctx, int li, unsigned mask) {
   if (li - 1 == 0) {
     // level 0 is unfiltered: its low-passed fields come straight from its noise
     auto out = [&](int f) { return (mask >> f) & 1u ? reinterpret_cast<C *>(src[f]) : nullptr; };
-    k_za_fields<T><<<hs_grid(Cl.n), hs_block(), 0, ctx.stream>>>(Cl.noise.as<C>(), Cl.tab_lp_src.as<double>(), Cl.n, (T)Cl.kmin(),
+    k_za_fields<T><<<hs_grid(Cl.n), hs_block(), 0, ctx.stream>>>(Cl.noise.as<C>(), tab_lp_src<T>(Cl), Cl.n, (T)Cl.kmin(),
                                                    out(0), out(1), out(2), out(3));
     launched();
   } else {
@@ -444,7 +482,7 @@ static void zoom_combine_typed(Context &ctx, int li, unsigned mask) {
     for (int f = 0; f < 4; ++f) {
       if (!((mask >> f) & 1u)) continue;
       GIC_CUDA(cudaMemcpyAsync(src[f], Cl.field[f].ptr, nc * sizeof(C), cudaMemcpyDeviceToDevice, ctx.stream));
-      fft_r2c_3d<T>(ctx, src[f], Cl.n, scale, Cl.tab_lp.as<double>());  // low-passed on the way out
+      fft_r2c_3d<T>(ctx, src[f], Cl.n, scale, tab_lp<T>(Cl));  // low-passed on the way out
     }
   }
   // the interpolation reads the coarse cells around the fine level only
@@ -489,7 +527,7 @@ static void add_lowpassed_coarse(Context &ctx, int li, T *const *coarse, T *cons
   for (int f = 0; f < nf; ++f) {
     GIC_CUDA(cudaMemcpyAsync(t, coarse[f], bytes, cudaMemcpyDeviceToDevice, ctx.stream));
     fft_r2c_3d<T>(ctx, t, Cl.n, scale);
-    fft_c2r_3d<T>(ctx, t, Cl.n, scale, Cl.tab_lp.as<double>());  // low-passed on the way back
+    fft_c2r_3d<T>(ctx, t, Cl.n, scale, tab_lp<T>(Cl));  // low-passed on the way back
     const T *src[1] = {t};
     T *dst[1] = {fine[f]};
     interp_add<T, 1>(ctx, Cl, src, F, dst);
@@ -503,7 +541,7 @@ static void lpt2_typed(Context &ctx) {
   const int nl = (int)ctx.levels.size();
   std::vector<std::vector<std::unique_ptr<DevBuf>>> hess(nl);
   std::vector<std::unique_ptr<DevBuf>> source(nl);
-  DevBuf ptrs, tab;
+  DevBuf ptrs, tab, tabt;
   // combined Hessian and the source S of every level
   for (int li = 0; li < nl; ++li) {
     Level &L = *ctx.levels[li];
@@ -517,7 +555,7 @@ static void lpt2_typed(Context &ctx) {
     }
     ptrs.ensure(sizeof(hp));
     GIC_CUDA(cudaMemcpyAsync(ptrs.ptr, hp, sizeof(hp), cudaMemcpyHostToDevice, ctx.stream));
-    k_hessian_fields<T><<<hs_grid(L.n), hs_block(), 0, ctx.stream>>>(L.noise.as<C>(), L.tab_main.as<double>(), L.n,
+    k_hessian_fields<T><<<hs_grid(L.n), hs_block(), 0, ctx.stream>>>(L.noise.as<C>(), tab_main<T>(L), L.n,
                                                                      (T)L.kmin(), ptrs.as<C *>());
     launched();
     GIC_CUDA(cudaStreamSynchronize(ctx.stream));  // ptrs is reused
@@ -551,7 +589,9 @@ static void lpt2_typed(Context &ctx) {
     fft_r2c_3d<T>(ctx, sk, L.n, scale);
     double kcut = li > 0 ? level_kcut(*ctx.levels[li - 1]) : 1.0;
     filter_table(ctx, tab, L, kcut, li > 0 ? 2 : 0, 3.0 / 7.0);
-    k_za_fields<T><<<hs_grid(L.n), hs_block(), 0, ctx.stream>>>(reinterpret_cast<C *>(sk), tab.as<double>(), L.n,
+    const long long nq_l = 3ll * (L.n / 2) * (L.n / 2) + 1;
+    k_za_fields<T><<<hs_grid(L.n), hs_block(), 0, ctx.stream>>>(reinterpret_cast<C *>(sk),
+                                                                typed_table<T>(ctx, tabt, tab.as<double>(), nq_l), L.n,
                                                                 (T)L.kmin(), reinterpret_cast<C *>(sk),
                                                                 L.field2[0].as<C>(), L.field2[1].as<C>(),
                                                                 L.field2[2].as<C>());

@@ -53,7 +53,8 @@ __device__ __forceinline__ double fermi_lp(double k, double kcut) {
   return 1. / (1. + exp((k - kcut) / temperature));
 }
 
-__global__ void k_mod_table(double *out, long long nq, TableSpec sp) {
+// out: the table; outf (optional): its float copy, for float fields
+__global__ void k_mod_table(double *out, float *outf, long long nq, TableSpec sp) {
   long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nq) return;
   double k = sqrt((double)q) * sp.kmin;
@@ -69,6 +70,7 @@ __global__ void k_mod_table(double *out, long long nq, TableSpec sp) {
   if (sp.sqrtp) f *= sp.sqrtp[q];
   if (sp.vel != 0.0) f = q == 0 ? 0.0 : -sp.vel * f / (k * k);
   out[q] = f;
+  if (outf) outf[q] = (float)f;
 }
 
 // Half-spectrum kernels run on a 2-D grid: x over rows (kx, ky), y over 32-wide
@@ -81,7 +83,7 @@ inline dim3 hs_block() { return dim3(256); }
 inline dim3 red_block() { return dim3(kKzChunk, kRowsPerBlock); }
 
 template <typename T>
-__global__ void k_mul_table(typename V2m<T>::type *c, int n, const double *tab) {
+__global__ void k_mul_table(typename V2m<T>::type *c, int n, const T *tab) {
   const int H = n / 2, S = H + 1;
   unsigned row;
   int iz;
@@ -96,7 +98,7 @@ __global__ void k_mul_table(typename V2m<T>::type *c, int n, const double *tab) 
 
 // out = tab[q] x (+ add): the metric's level term f^2 X plus its transformed cross terms
 template <typename T>
-__global__ void k_mul_table_add(typename V2m<T>::type *out, const typename V2m<T>::type *x, int n, const double *tab,
+__global__ void k_mul_table_add(typename V2m<T>::type *out, const typename V2m<T>::type *x, int n, const T *tab,
                                 const typename V2m<T>::type *add) {
   const int H = n / 2, S = H + 1;
   unsigned row;
@@ -121,7 +123,8 @@ constexpr int kMaxAxpy = 8;
 template <typename T>
 struct AxpySources {
   const T *b[kMaxAxpy];
-  double c[kMaxAxpy];
+  T c[kMaxAxpy];  // rounded to the field precision on the host (a per-element double->float
+                  // conversion would occupy the FP64 pipe)
   int nb;
 };
 template <typename T>
@@ -129,8 +132,33 @@ __global__ void k_axpy_multi(T *a, AxpySources<T> src, size_t n) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   T v = a[i];
-  for (int k = 0; k < src.nb; ++k) v += (T)src.c[k] * src.b[k][i];
+  for (int k = 0; k < src.nb; ++k) v += src.c[k] * src.b[k][i];
   a[i] = v;
+}
+// the same with NB sources known at compile time and 16-byte vectors (4 floats or 2
+// doubles per thread): every source's load is in flight before the sums, which run in
+// the order above
+template <typename T> struct Vec16;
+template <> struct Vec16<float> { using type = float4; static constexpr int W = 4; };
+template <> struct Vec16<double> { using type = double2; static constexpr int W = 2; };
+template <typename T, int NB>
+__global__ void k_axpy_multi_vec(T *a, AxpySources<T> src, size_t nvec) {
+  using V = typename Vec16<T>::type;
+  constexpr int W = Vec16<T>::W;
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nvec) return;
+  V v = reinterpret_cast<V *>(a)[i];
+  V b[NB];
+#pragma unroll
+  for (int k = 0; k < NB; ++k) b[k] = reinterpret_cast<const V *>(src.b[k])[i];
+  T *pv = reinterpret_cast<T *>(&v);
+#pragma unroll
+  for (int k = 0; k < NB; ++k) {
+    const T *pb = reinterpret_cast<const T *>(&b[k]);
+#pragma unroll
+    for (int w = 0; w < W; ++w) pv[w] += src.c[k] * pb[w];
+  }
+  reinterpret_cast<V *>(a)[i] = v;
 }
 
 // all products <a_i|b_j> (i < na <= 4, j < nb <= 5) of half spectra in one pass over the
@@ -223,15 +251,15 @@ __global__ void __launch_bounds__(256, 3) k_inner_block(BlockFields<T> f, int n,
 // --- elementwise ----------------------------------------------------------------
 
 template <typename T>
-__global__ void k_axpy(T *a, const T *b, double c, size_t n) {
+__global__ void k_axpy(T *a, const T *b, T c, size_t n) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) a[i] += (T)c * b[i];
+  if (i < n) a[i] += c * b[i];
 }
 
 template <typename T>
-__global__ void k_scale(T *a, double c, size_t n) {
+__global__ void k_scale(T *a, T c, size_t n) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) a[i] *= (T)c;
+  if (i < n) a[i] *= c;
 }
 
 // Window combinations on padded real fields (in = cell inside the window):
@@ -654,7 +682,7 @@ __global__ void k_unpad(const T *padded, T *compact, int n, T scale) {
 // psi_a = i k_a tab[q] w / k^2, zero at k = 0 and where k_a is the Nyquist mode,
 // zeldovich.hpp:155-181), or by its complex conjugate (the adjoint)
 template <typename T>
-__global__ void k_field_mult(typename V2m<T>::type *c, int n, const double *tab, T kmin, int what, int conj) {
+__global__ void k_field_mult(typename V2m<T>::type *c, int n, const T *tab, T kmin, int what, int conj) {
   const int H = n / 2, S = H + 1;
   unsigned row;
   int iz;
@@ -787,7 +815,7 @@ struct ModEngine {
   // times the current table (S.tab), then to real space: the multiply rides on the
   // transform's first pass (bit-identical to mul_table followed by to_real)
   void to_real_times_table(T *p, int l, const CellBox *box = nullptr) {
-    fft_c2r_3d<T>(ctx, p, lev(l).n, scale(l), S.tab.template as<double>(), box);
+    fft_c2r_3d<T>(ctx, p, lev(l).n, scale(l), tabT(), box);
   }
   // cells of level c that the fine level f covers (margin: extra cells each side), cyclic
   CellBox footprint(int f, int c, int margin) { return footprint_box(lev(f), lev(c), margin); }
@@ -810,19 +838,25 @@ struct ModEngine {
   void table(const TableSpec &sp0, int g) {
     long long half = lev(g).n / 2, nq = 3 * half * half + 1;
     S.tab.ensure(nq * sizeof(double));
+    if (sizeof(T) == 4) S.tabf.ensure(nq * sizeof(float));
     TableSpec sp = sp0;
     sp.kmin = lev(g).kmin();
-    k_mod_table<<<nblk(nq), 256, 0, ctx.stream>>>(S.tab.template as<double>(), nq, sp);
+    k_mod_table<<<nblk(nq), 256, 0, ctx.stream>>>(S.tab.template as<double>(),
+                                                 sizeof(T) == 4 ? S.tabf.template as<float>() : nullptr, nq, sp);
     launched();
+  }
+  // the current table in the fields' precision
+  const T *tabT() const {
+    if constexpr (sizeof(T) == 4) return S.tabf.template as<float>();
+    else return S.tab.template as<double>();
   }
 
   void mul_table(T *p, int g) {
-    k_mul_table<T><<<hs_grid(lev(g).n), hs_block(), 0, ctx.stream>>>(reinterpret_cast<C *>(p), lev(g).n,
-                                                                     S.tab.template as<double>());
+    k_mul_table<T><<<hs_grid(lev(g).n), hs_block(), 0, ctx.stream>>>(reinterpret_cast<C *>(p), lev(g).n, tabT());
     launched();
   }
   void axpy(T *a, const T *b, double c, int l) {
-    k_axpy<T><<<nblk(elems(l)), 256, 0, ctx.stream>>>(a, b, c, elems(l));
+    k_axpy<T><<<nblk(elems(l)), 256, 0, ctx.stream>>>(a, b, (T)c, elems(l));
     launched();
   }
   void scale_by(T *a, double c, int l) {
@@ -932,9 +966,27 @@ struct ModEngine {
       src.nb = (int)std::min<size_t>(kMaxAxpy, b.size() - k0);
       for (int k = 0; k < src.nb; ++k) {
         src.b[k] = b[k0 + k];
-        src.c[k] = c[k0 + k];
+        src.c[k] = (T)c[k0 + k];
       }
-      k_axpy_multi<T><<<nblk(elems(l)), 256, 0, ctx.stream>>>(a, src, elems(l));
+      constexpr int W = Vec16<T>::W;
+      const size_t n = elems(l);
+      bool aligned = n % W == 0 && (uintptr_t)a % 16 == 0;
+      for (int k = 0; k < src.nb; ++k) aligned = aligned && (uintptr_t)src.b[k] % 16 == 0;
+      if (aligned) {
+        const size_t nv = n / W;
+        switch (src.nb) {
+          case 1: k_axpy_multi_vec<T, 1><<<nblk(nv), 256, 0, ctx.stream>>>(a, src, nv); break;
+          case 2: k_axpy_multi_vec<T, 2><<<nblk(nv), 256, 0, ctx.stream>>>(a, src, nv); break;
+          case 3: k_axpy_multi_vec<T, 3><<<nblk(nv), 256, 0, ctx.stream>>>(a, src, nv); break;
+          case 4: k_axpy_multi_vec<T, 4><<<nblk(nv), 256, 0, ctx.stream>>>(a, src, nv); break;
+          case 5: k_axpy_multi_vec<T, 5><<<nblk(nv), 256, 0, ctx.stream>>>(a, src, nv); break;
+          case 6: k_axpy_multi_vec<T, 6><<<nblk(nv), 256, 0, ctx.stream>>>(a, src, nv); break;
+          case 7: k_axpy_multi_vec<T, 7><<<nblk(nv), 256, 0, ctx.stream>>>(a, src, nv); break;
+          default: k_axpy_multi_vec<T, 8><<<nblk(nv), 256, 0, ctx.stream>>>(a, src, nv); break;
+        }
+      } else {
+        k_axpy_multi<T><<<nblk(n), 256, 0, ctx.stream>>>(a, src, n);
+      }
       launched();
     }
   }
@@ -1055,7 +1107,7 @@ struct ModEngine {
         }
         family_table(t, 2);
         k_mul_table_add<T><<<hs_grid(lev(t).n), hs_block(), 0, ctx.stream>>>(
-            reinterpret_cast<C *>(R), reinterpret_cast<const C *>(ptr(X, t)), lev(t).n, S.tab.template as<double>(), add);
+            reinterpret_cast<C *>(R), reinterpret_cast<const C *>(ptr(X, t)), lev(t).n, tabT(), add);
         launched();
       }
       out.fourier[t] = 1;
@@ -1314,7 +1366,7 @@ struct ModEngine {
     k_unpad<T><<<nblk(lev(l).ncells()), 256, 0, ctx.stream>>>(padded, static_cast<T *>(compact), lev(l).n, scale);
     launched();
   }
-  void field_mult(T *p, int l, const double *tab, int what, int conj) {
+  void field_mult(T *p, int l, const T *tab, int what, int conj) {
     k_field_mult<T><<<hs_grid(lev(l).n), hs_block(), 0, ctx.stream>>>(reinterpret_cast<C *>(p), lev(l).n, tab,
                                                                        (T)lev(l).kmin(), what, conj);
     launched();
@@ -1332,7 +1384,7 @@ struct ModEngine {
     T *p = b->template as<T>();
     pad_from(noise[L], p, L);
     to_fourier(p, L);
-    field_mult(p, L, lev(L).tab_main.template as<double>(), what, 0);
+    field_mult(p, L, tab_main<T>(lev(L)), what, 0);
     to_real(p, L);
     if (L == 1) {
       lowpass_tables(ctx, 0);
@@ -1340,7 +1392,7 @@ struct ModEngine {
       T *q = c->template as<T>();
       pad_from(noise[0], q, 0);
       to_fourier(q, 0);
-      field_mult(q, 0, lev(0).tab_lp_src.template as<double>(), what, 0);
+      field_mult(q, 0, tab_lp_src<T>(lev(0)), what, 0);
       to_real(q, 0);
       const T *src[1] = {q};
       T *dst[1] = {p};
@@ -1371,13 +1423,13 @@ struct ModEngine {
       deinterpolate(p, 1, q, 0, true);
     }
     to_fourier(p, L);
-    field_mult(p, L, lev(L).tab_main.template as<double>(), what, 1);
+    field_mult(p, L, tab_main<T>(lev(L)), what, 1);
     to_real(p, L);
     unpad_to(p, grad[L], L);
     if (L == 1) {
       T *q = c->template as<T>();
       to_fourier(q, 0);
-      field_mult(q, 0, lev(0).tab_lp_src.template as<double>(), what, 1);
+      field_mult(q, 0, tab_lp_src<T>(lev(0)), what, 1);
       to_real(q, 0);
       unpad_to(q, grad[0], 0);
     }
@@ -1463,7 +1515,7 @@ struct ModEngine {
   }
   void axpy_stored(Stored &a, Stored &b, double c, int l) {
     axpy(sb(a), sb(b), c, l);
-    k_axpy<T><<<nblk(tail_len(l)), 256, 0, ctx.stream>>>(st(a), st(b), c, tail_len(l));
+    k_axpy<T><<<nblk(tail_len(l)), 256, 0, ctx.stream>>>(st(a), st(b), (T)c, tail_len(l));
     launched();
   }
   void scale_stored(Stored &a, double c, int l) {
@@ -1477,7 +1529,7 @@ struct ModEngine {
                          {{sb(c), sb(d), l, kReal}, {st(c), st(d), l, kFlat, tail_len(l)}}});
   }
   // real field -> R2C -> times tab -> C2R (Field::applyTransferFunction between transforms)
-  void apply_precond(T *buf, int l, const double *tab) {
+  void apply_precond(T *buf, int l, const T *tab) {
     to_fourier(buf, l);
     fft_c2r_3d<T>(ctx, buf, lev(l).n, scale(l), tab);
   }
@@ -1508,7 +1560,12 @@ struct ModEngine {
     preconditioner_table(ctx, lev(l), 0.5, half);
     preconditioner_table(ctx, lev(l), -1.0, minus1);
     preconditioner_table(ctx, lev(l), -0.5, mhalf);
-    const double *h = half.template as<double>(), *m1 = minus1.template as<double>();
+    // in the fields' precision
+    DevBuf half_t, minus1_t, mhalf_t;
+    const size_t nq = 3 * (size_t)(lev(l).n / 2) * (lev(l).n / 2) + 1;
+    const T *h = typed_table<T>(ctx, half_t, half.template as<double>(), nq);
+    const T *m1 = typed_table<T>(ctx, minus1_t, minus1.template as<double>(), nq);
+    const T *mh = typed_table<T>(ctx, mhalf_t, mhalf.template as<double>(), nq);
     Stored dd, z, r, d, x, qd;
     for (Stored *s : {&dd, &z, &r, &d, &x, &qd}) take(*s, l);
     // delta_diff = C^1/2 (b - a), real
@@ -1577,7 +1634,7 @@ struct ModEngine {
     axpy(sb(x), sb(qd), 1.0, l);
     keep_cells(sb(dd), l, cells, count);
     axpy(sb(x), sb(dd), -1.0, l);
-    fft_r2c_3d<T>(ctx, sb(x), lev(l).n, scale(l), mhalf.template as<double>());
+    fft_r2c_3d<T>(ctx, sb(x), lev(l).n, scale(l), mh);
     GIC_CUDA(cudaMemcpyAsync(out_k, sb(x), bytes, cudaMemcpyDeviceToDevice, ctx.stream));
     GIC_CUDA(cudaStreamSynchronize(ctx.stream));
     for (Stored *s : {&dd, &z, &r, &d, &x, &qd}) give(*s);
@@ -1654,7 +1711,7 @@ struct ModEngine {
       const bool velocity_like = (kind >= GIC_MOD_VX && kind <= GIC_MOD_VZ) || kind >= GIC_MOD_LX;
       sp.vel = velocity_like ? velocity_ratio() : 0.0;
       table(sp, l);
-      fft_r2c_3d<T>(ctx, ptr(out, l), lev(l).n, scale(l), S.tab.template as<double>(), &support[l]);
+      fft_r2c_3d<T>(ctx, ptr(out, l), lev(l).n, scale(l), tabT(), &support[l]);
       out.fourier[l] = 1;
       if (kind == GIC_MOD_POTENTIAL) {
         // 3/2 Om0 / a (H0/h)^2 / c^2 in (h/Mpc)^2 (cosmology/parameters.hpp:213-216)
