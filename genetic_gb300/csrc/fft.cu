@@ -554,24 +554,6 @@ __device__ __forceinline__ long long row_tile_start(int x0, int ty0) {
   return (long long)plane * N + (long long)tile * RPC;
 }
 
-// the padding word (coefficient N/2) of every row outside the box's row tiles, zeroed:
-// a forward transform whose input is zero outside the box skips those rows, and their
-// spectra are then zero only if this word, not read as input, is zero too
-template <typename C>
-__global__ void k_zero_row_tails(C *data, int N, int x0, int nx, int ty0, int nty, int rpc) {
-  const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= (long long)N * N) return;
-  const int x = (int)(row / N), y = (int)(row % N);
-  const int ntile = N / rpc;
-  const bool in = (x - x0 + N) % N < nx && (y / rpc - ty0 + ntile) % ntile < nty;
-  if (!in) {
-    C z;
-    z.x = 0;
-    z.y = 0;
-    data[row * (N / 2 + 1) + N / 2] = z;
-  }
-}
-
 // ---- fused passes: the first stage reads HBM into registers, the last writes HBM ----
 // Shared memory then carries only the exchanges between stages (4 accesses per
 // element at L = 512 instead of 8).  The tile is unpadded: every access is
@@ -1062,18 +1044,12 @@ struct FixedFft {
     k_fft_cols_fused<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A, m0, mn);
     launched();
   }
-  // row tiles of RPC rows covering the selection: grid (tiles, planes); for a
-  // forward transform of a partial selection, the other rows' padding words zeroed
+  // row tiles of RPC rows covering the selection: grid (tiles, planes)
   template <int RPC>
-  static dim3 row_grid(Context &ctx, C *d, const Sel &sel, bool inverse, int &ty0) {
+  static dim3 row_grid(const Sel &sel, int &ty0) {
     constexpr int NTILE = N / RPC;
     ty0 = sel.y0 / RPC;
     const int nty = std::min(NTILE, (sel.y0 + sel.ny - 1) / RPC - ty0 + 1);
-    if (!inverse && !sel.whole()) {
-      const long long nrows = (long long)N * N;
-      k_zero_row_tails<C><<<(unsigned)((nrows + 255) / 256), 256, 0, ctx.stream>>>(d, N, sel.x0, sel.nx, ty0, nty, RPC);
-      launched();
-    }
     return dim3((unsigned)nty, (unsigned)sel.nx);
   }
   template <int RPC, int NT, bool INV>
@@ -1081,7 +1057,7 @@ struct FixedFft {
     static std::atomic<int> mask{0};
     const size_t smem = (size_t)(INV ? H : S) * RPC * sizeof(C);
     int ty0 = 0;
-    const dim3 grid = row_grid<RPC>(ctx, d, sel, INV, ty0);
+    const dim3 grid = row_grid<RPC>(sel, ty0);
     if (INV) {
       set_smem_once((const void *)k_fft_rows_c2r_fused<T, H, RPC, NT>, smem, mask);
       k_fft_rows_c2r_fused<T, H, RPC, NT><<<grid, NT, smem, ctx.stream>>>(d, sel.x0, ty0, tw, scale);
@@ -1096,7 +1072,7 @@ struct FixedFft {
     static std::atomic<int> mask{0};
     const size_t smem = (size_t)S * (RPC + 1) * sizeof(C);
     int ty0 = 0;
-    const dim3 grid = row_grid<RPC>(ctx, d, sel, INV, ty0);
+    const dim3 grid = row_grid<RPC>(sel, ty0);
     if (INV) {
       set_smem_once((const void *)k_fft_rows_c2r_fixed<T, H, RPC, NT>, smem, mask);
       k_fft_rows_c2r_fixed<T, H, RPC, NT><<<grid, NT, smem, ctx.stream>>>(d, sel.x0, ty0, tw, scale);
@@ -1420,6 +1396,10 @@ void fft_r2c_3d(Context &ctx, T *data, int n, double scale, const T *post_tab, c
   launched();
   strided_pass<T>(ctx, c, n, n, S, -1, (T)1, tw);
   strided_pass<T>(ctx, c, 1, n, (long long)n * S, -1, (T)scale, tw, post_tab);
+}
+
+bool fft_prunes(const Context &ctx, int n) {
+  return ctx.fft.force_cols != -2 && n >= 32 && n <= 1024 && (n & (n - 1)) == 0;
 }
 
 bool take_fft_wait_error(Context &ctx) {

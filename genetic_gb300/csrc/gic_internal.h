@@ -161,11 +161,42 @@ struct RngScratch {
   int chunkmul_count = 0;
 };
 
+// A box of an n^3 grid's cells: per axis the cyclic range [start, start + len) mod n.
+// Given to a forward transform, its input is zero outside the box; given to an
+// inverse transform, only its output inside the box is wanted.  The fixed-length
+// transforms then skip the x planes and y rows outside it (the z range is not used);
+// the values they produce for the box are the same bits as the whole transform's.
+struct CellBox {
+  int start[3] = {0, 0, 0}, len[3] = {0, 0, 0};
+  static CellBox whole(int n) {
+    CellBox b;
+    for (int a = 0; a < 3; ++a) b.len[a] = n;
+    return b;
+  }
+  // per axis [lo - margin, hi + margin) of a cyclic axis of n cells (any lo, hi)
+  void set_axis(int a, long long lo, long long hi, int margin, int n) {
+    long long len_ = hi - lo + 2ll * margin;
+    if (len_ >= n || len_ <= 0) {
+      start[a] = 0;
+      len[a] = n;
+      return;
+    }
+    start[a] = (int)((((lo - margin) % n) + n) % n);
+    len[a] = (int)len_;
+  }
+};
 // a linear modification awaiting application (kind 0 overdensity, 1-3 velocity x,y,z)
 struct ModRequest {
   int kind;
   std::vector<unsigned long long> cells;  // flagged cells of the finest level
   double target;
+  // made at first use and kept: the cells on the device, their box on the finest level
+  // (with the stencils' reach) and, for angular momenta, their wrapped centre
+  std::shared_ptr<DevBuf> dcells;
+  CellBox box;
+  bool have_box = false;
+  double centre[3] = {0, 0, 0};
+  bool have_centre = false;
 };
 
 // variance of the high-passed dark-matter overdensity over flagged cells
@@ -234,30 +265,6 @@ template <typename T>
 const T *tab_lp(const Level &L);
 
 // fft.cu
-// A box of an n^3 grid's cells: per axis the cyclic range [start, start + len) mod n.
-// Given to a forward transform, its input is zero outside the box; given to an
-// inverse transform, only its output inside the box is wanted.  The fixed-length
-// transforms then skip the x planes and y rows outside it (the z range is not used);
-// the values they produce for the box are the same bits as the whole transform's.
-struct CellBox {
-  int start[3] = {0, 0, 0}, len[3] = {0, 0, 0};
-  static CellBox whole(int n) {
-    CellBox b;
-    for (int a = 0; a < 3; ++a) b.len[a] = n;
-    return b;
-  }
-  // per axis [lo - margin, hi + margin) of a cyclic axis of n cells (any lo, hi)
-  void set_axis(int a, long long lo, long long hi, int margin, int n) {
-    long long len_ = hi - lo + 2ll * margin;
-    if (len_ >= n || len_ <= 0) {
-      start[a] = 0;
-      len[a] = n;
-      return;
-    }
-    start[a] = (int)((((lo - margin) % n) + n) % n);
-    len[a] = (int)len_;
-  }
-};
 // cells of the coarse level that the fine level covers, `margin` extra cells each side
 inline CellBox footprint_box(const Level &fine, const Level &coarse, int margin) {
   CellBox b = CellBox::whole(coarse.n);
@@ -279,6 +286,9 @@ void fft_c2r_3d(Context &ctx, T *data, int n, double scale, const T *pre_tab = n
 template <typename T>
 void fft_r2c_3d(Context &ctx, T *data, int n, double scale, const T *post_tab = nullptr,
                 const CellBox *box = nullptr);
+// whether transforms of size n honour a box (the fixed-length passes), so that a forward
+// transform reads only the box's x planes and its input need be valid there only
+bool fft_prunes(const Context &ctx, int n);
 // after the stream has synchronised: true (with ctx.last_error set) when a wait of the
 // plane pass gave up since the last check; clears the flag
 bool take_fft_wait_error(Context &ctx);
@@ -315,7 +325,7 @@ template <typename T, int NF>
 void interp_add(Context &ctx, const Level &coarse, const T *const *src, const Level &fine, T *const *dst);
 
 // modify.cu
-double modification_value(Context &ctx, const ModRequest &m);
+double modification_value(Context &ctx, ModRequest &m);
 double noise_chi2(Context &ctx);
 double variance_value(Context &ctx, QuadRequest &q);
 void apply_modifications(Context &ctx, double *chi2_before, double *chi2_after);

@@ -1642,13 +1642,40 @@ struct ModEngine {
   }
 
   // covector of one modification (kind 0 overdensity, 1..3 velocity x,y,z)
-  void covector(Field &out, int kind, const unsigned long long *flagged, size_t count) {
+  // the x planes of `box` of a level's real field set to zero (one or two ranges)
+  void zero_planes(T *p, int l, const CellBox &box) {
+    const int n = lev(l).n;
+    const size_t plane = (size_t)n * 2 * (n / 2 + 1) * sizeof(T);
+    const int x0 = box.start[0], nx = std::min(box.len[0], n);
+    const int first = std::min(nx, n - x0);
+    GIC_CUDA(cudaMemsetAsync(reinterpret_cast<char *>(p) + (size_t)x0 * plane, 0, (size_t)first * plane, ctx.stream));
+    if (nx > first) GIC_CUDA(cudaMemsetAsync(p, 0, (size_t)(nx - first) * plane, ctx.stream));
+  }
+
+  // covector of one modification (kind 0 overdensity, 1..3 velocity x,y,z, 4 potential,
+  // 5..7 angular momentum); the request keeps its device cells, box and centre
+  void covector(Field &out, ModRequest &m) {
+    const int kind = m.kind;
+    const unsigned long long *flagged = m.cells.data();
+    const size_t count = m.cells.size();
     int F = nl() - 1;
     alloc(out);
-    for (int l = 0; l < nl(); ++l) zero(out, l);
-    S.cells.ensure(count * sizeof(unsigned long long));
-    GIC_CUDA(cudaMemcpyAsync(S.cells.ptr, flagged, count * sizeof(unsigned long long), cudaMemcpyHostToDevice,
-                             ctx.stream));
+    if (!m.dcells) {
+      m.dcells = std::make_shared<DevBuf>();
+      m.dcells->ensure(count * sizeof(unsigned long long));
+      GIC_CUDA(cudaMemcpyAsync(m.dcells->ptr, flagged, count * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                               ctx.stream));
+    }
+    if (!m.have_box) {
+      // the flagged cells and the stencils' reach (2 cells)
+      m.box = cells_box(flagged, count, lev(F).n, 2);
+      m.have_box = true;
+    }
+    // a level's real covector is read inside its support only when its transform is
+    // box-restricted: then only the support's x planes are zeroed
+    if (fft_prunes(ctx, lev(F).n)) zero_planes(ptr(out, F), F, m.box);
+    else zero(out, F);
+    const unsigned long long *dcells = m.dcells->template as<unsigned long long>();
     double w = 1.0 / (double)count;
     if (kind >= GIC_MOD_LX) {
       // centre of the flagged cells, wrapped (Grid::getCentreWrapped, grid.hpp:466-494)
@@ -1664,24 +1691,27 @@ struct ModEngine {
         unsigned long long ii = axis == 0 ? xx : (axis == 1 ? yy : zz);
         return (double)ii * Lf.dx + Lf.x0[axis] + Lf.dx / 2;
       };
-      double cen[3];
-      for (int ax = 0; ax < 3; ++ax) {
-        double p0 = centroid(flagged[0], ax), run = 0.0;
-        for (size_t i = 1; i < count; ++i) run += wrapped(centroid(flagged[i], ax) - p0);
-        run /= (double)count;
-        double v = run + p0;
-        v = std::fmod(v, P);
-        if (v < 0) v += P;
-        cen[ax] = v;
+      if (!m.have_centre) {
+        for (int ax = 0; ax < 3; ++ax) {
+          double p0 = centroid(flagged[0], ax), run = 0.0;
+          for (size_t i = 1; i < count; ++i) run += wrapped(centroid(flagged[i], ax) - p0);
+          run /= (double)count;
+          double v = run + p0;
+          v = std::fmod(v, P);
+          if (v < 0) v += P;
+          m.centre[ax] = v;
+        }
+        m.have_centre = true;
       }
+      const double *cen = m.centre;
       const double norm = (double)count * Lf.dx;
-      k_localise_am<T><<<nblk(count), 256, 0, ctx.stream>>>(ptr(out, F), Lf.n, S.cells.template as<unsigned long long>(),
+      k_localise_am<T><<<nblk(count), 256, 0, ctx.stream>>>(ptr(out, F), Lf.n, dcells,
                                                            count, kind - GIC_MOD_LX, Lf.dx, Lf.x0[0], Lf.x0[1], Lf.x0[2],
                                                            cen[0], cen[1], cen[2], P, 1. / 12. / norm, -2. / 3. / norm);
     } else {
       const bool vel = kind >= GIC_MOD_VX && kind <= GIC_MOD_VZ;
       double a = -w / 12. / lev(F).dx, b = w * 2. / 3. / lev(F).dx;
-      k_localise<T><<<nblk(count), 256, 0, ctx.stream>>>(ptr(out, F), lev(F).n, S.cells.template as<unsigned long long>(),
+      k_localise<T><<<nblk(count), 256, 0, ctx.stream>>>(ptr(out, F), lev(F).n, dcells,
                                                         count, vel ? 1 : 0, vel ? kind - GIC_MOD_VX : 0, w, a, b);
     }
     launched();
@@ -1691,11 +1721,13 @@ struct ModEngine {
     // support of each level's real covector: the flagged cells and the stencils' reach
     // (2 cells) on the finest level, the deinterpolation block on coarser ones
     std::vector<CellBox> support(nl());
-    support[F] = cells_box(flagged, count, lev(F).n, 2);
+    support[F] = m.box;
     if (F > 0) {
       for (int l = F - 1; l >= 0; --l) {
         out.fourier[l] = 0;
-        support[l] = deinterpolate(ptr(out, l + 1), l + 1, ptr(out, l), l, false, &support[l + 1]);
+        const bool prune = fft_prunes(ctx, lev(l).n);
+        if (!prune) zero(out, l);
+        support[l] = deinterpolate(ptr(out, l + 1), l + 1, ptr(out, l), l, false, &support[l + 1], prune);
       }
     }
     for (int l = 0; l < nl(); ++l) {
@@ -1731,8 +1763,10 @@ struct ModEngine {
   // fine_box: the fine field is zero outside it; the passes then run over its cells
   // only (an axis whose range wraps around the fine grid is taken whole).  Skipped
   // cells would only add zeros, so the sums are the same.
+  // zero_block: first set to zero the coarse x planes the block covers (a caller that
+  // reads the coarse field in the block's planes only need not zero the rest)
   CellBox deinterpolate(const T *fine, int f, T *coarse, int c, bool unit_scale = false,
-                        const CellBox *fine_box = nullptr) {
+                        const CellBox *fine_box = nullptr, bool zero_block = false) {
     const Level &Fl = lev(f), &Cl = lev(c);
     int nf = Fl.n;
     int r = (int)std::lround(Cl.dx / Fl.dx);
@@ -1778,11 +1812,12 @@ struct ModEngine {
     k_deinterp_pass<T><<<nblk((size_t)cnt[0] * cnt[1]), 256, 0, ctx.stream>>>(
         S.t2.template as<T>(), (long long)cnt[1] * fn[2], fn[2], S.t3.template as<T>(), (long long)cnt[1] * cnt[2], cnt[2], 2,
         cnt[0], cnt[1], fn[2], fn[2], ub + 2 * nf + f0[2], fr + 2 * nf + f0[2], c0[2], cnt[2], (T)1);
+    CellBox b = CellBox::whole(Cl.n);
+    for (int a = 0; a < 3; ++a) b.set_axis(a, c0[a], (long long)c0[a] + cnt[a], 0, Cl.n);
+    if (zero_block) zero_planes(coarse, c, b);
     k_add_block<T><<<nblk(b3), 256, 0, ctx.stream>>>(S.t3.template as<T>(), cnt[0], cnt[1], cnt[2], c0[0], c0[1], c0[2],
                                                     coarse, Cl.n);
     launched(4);
-    CellBox b = CellBox::whole(Cl.n);
-    for (int a = 0; a < 3; ++a) b.set_axis(a, c0[a], (long long)c0[a] + cnt[a], 0, Cl.n);
     return b;
   }
 };
@@ -1799,6 +1834,35 @@ void ModEngine<T>::build_sqrtp_dm(int l) {
 
 // --- the modification manager ------------------------------------------------------
 
+// W borrows the levels' noise buffers (no copy) for the lifetime of the loan; the
+// buffers return to the levels when it ends, also on an error
+template <typename T>
+struct NoiseLoan {
+  ModEngine<T> &E;
+  typename ModEngine<T>::Field &W;
+  NoiseLoan(ModEngine<T> &e, typename ModEngine<T>::Field &w) : E(e), W(w) {
+    W.pool = nullptr;
+    W.b.resize(E.nl());
+    W.fourier.assign(E.nl(), 1);
+    for (int l = 0; l < E.nl(); ++l) {
+      Level &L = E.lev(l);
+      if (!L.have_noise || !L.noise.ptr) fail(GIC_ERR_NOT_READY, "white noise has not been drawn");
+      W.b[l] = std::make_unique<DevBuf>();
+      std::swap(W.b[l]->ptr, L.noise.ptr);
+      std::swap(W.b[l]->bytes, L.noise.bytes);
+    }
+  }
+  ~NoiseLoan() {
+    for (int l = 0; l < (int)W.b.size(); ++l) {
+      if (!W.b[l]) continue;
+      Level &L = E.lev(l);
+      std::swap(W.b[l]->ptr, L.noise.ptr);
+      std::swap(W.b[l]->bytes, L.noise.bytes);
+    }
+    W.b.clear();
+  }
+};
+
 template <typename T>
 static void noise_field(ModEngine<T> &E, typename ModEngine<T>::Field &W) {
   E.alloc(W);
@@ -1810,11 +1874,11 @@ static void noise_field(ModEngine<T> &E, typename ModEngine<T>::Field &W) {
 }
 
 template <typename T>
-static double current_value(Context &ctx, const ModRequest &m) {
+static double current_value(Context &ctx, ModRequest &m) {
   ModEngine<T> E(ctx);
   typename ModEngine<T>::Field W, a;
-  noise_field(E, W);
-  E.covector(a, m.kind, m.cells.data(), m.cells.size());
+  NoiseLoan<T> loan(E, W);
+  E.covector(a, m);
   return E.inner(a, W);
 }
 
@@ -1822,7 +1886,7 @@ template <typename T>
 static double chi2_of_noise(Context &ctx) {
   ModEngine<T> E(ctx);
   typename ModEngine<T>::Field W;
-  noise_field(E, W);
+  NoiseLoan<T> loan(E, W);
   return E.chi2(W);
 }
 
@@ -1922,12 +1986,14 @@ static void apply_mods(Context &ctx, double *chi2_before, double *chi2_after) {
   using F = typename ModEngine<T>::Field;
   int n = (int)ctx.mods.size();
   if (chi2_before) *chi2_before = chi2_of_noise<T>(ctx);
+  {
+  // the modifications work on the noise buffers themselves
   F W;
-  noise_field(E, W);
+  NoiseLoan<T> loan(E, W);
   std::vector<F> alpha(n), vec(n);
   std::vector<double> t(n);
   for (int i = 0; i < n; ++i) {
-    E.covector(alpha[i], ctx.mods[i].kind, ctx.mods[i].cells.data(), ctx.mods[i].cells.size());
+    E.covector(alpha[i], ctx.mods[i]);
     E.apply_metric(alpha[i], vec[i], false);
     t[i] = ctx.mods[i].target;
   }
@@ -1992,10 +2058,8 @@ static void apply_mods(Context &ctx, double *chi2_before, double *chi2_after) {
     vec.clear();
     for (auto &q : ctx.quads) apply_quadratic<T>(E, W, lin, q);
   }
-  for (int l = 0; l < E.nl(); ++l) {
-    E.copy_level(E.lev(l).noise, *W.b[l], l);
-    E.lev(l).have_fields = E.lev(l).have_lpt2 = false;
   }
+  for (int l = 0; l < E.nl(); ++l) E.lev(l).have_fields = E.lev(l).have_lpt2 = false;
   GIC_CUDA(cudaStreamSynchronize(ctx.stream));
   if (chi2_after) *chi2_after = chi2_of_noise<T>(ctx);
 }
@@ -2070,7 +2134,7 @@ void noise_real(Context &ctx, int level, void *out) {
   else ModEngine<float>(ctx).noise_to_real(level, out);
 }
 
-double modification_value(Context &ctx, const ModRequest &m) {
+double modification_value(Context &ctx, ModRequest &m) {
   return ctx.dbl() ? current_value<double>(ctx, m) : current_value<float>(ctx, m);
 }
 
