@@ -439,6 +439,25 @@ __global__ void k_mirror(typename Cx<T>::type *data, int N) {
   data[((size_t)kx * N + ky) * S + kz] = cconj(data[((size_t)sx * N + sy) * S + kz]);
 }
 
+// The same mirroring out of place: the kz = 0 and kz = N/2 planes of src, mirrored,
+// into dst (the first pass of an out-of-place inverse reads those two planes from dst
+// and every other column from src)
+template <typename T>
+__global__ void k_mirror_from(typename Cx<T>::type *dst, const typename Cx<T>::type *src, int N) {
+  const int H = N / 2, S = H + 1;
+  long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long per_plane = (long long)N * N;
+  if (id >= 2 * per_plane) return;
+  int plane = (int)(id / per_plane);
+  int kz = plane ? H : 0;
+  long long rem = id % per_plane;
+  int kx = (int)(rem / N), ky = (int)(rem % N);
+  const size_t at = ((size_t)kx * N + ky) * S + kz;
+  if (kx > H) dst[at] = cconj(src[((size_t)(N - kx) * N + (N - ky) % N) * S + kz]);
+  else if ((kx == 0 || kx == H) && ky > H) dst[at] = cconj(src[((size_t)kx * N + (N - ky)) * S + kz]);
+  else dst[at] = src[at];
+}
+
 // ---- fixed-length passes (power-of-two lengths): one padded tile, in place ----
 // A CTA owns TC transforms of compile-time length L held as a tile [L][TC + 1] in
 // shared memory (column c of the tile is one transform; the +1 pad makes row
@@ -503,7 +522,7 @@ struct TileStages<T, L, TC, TCP, NT, NS, SIGN, TWM, true> {
 template <typename T, int L, int TC, int NT, int SIGN>
 __global__ void __launch_bounds__(NT) k_fft_cols(typename Cx<T>::type *data, long long B,
                                                  const typename Cx<T>::type *tw, T scale, const T *tab, int a0,
-                                                 int A, int m0, int mn) {
+                                                 int A, int m0, int mn, const typename Cx<T>::type *src) {
   using C = typename Cx<T>::type;
   constexpr int TCP = TC + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -516,7 +535,10 @@ __global__ void __launch_bounds__(NT) k_fft_cols(typename Cx<T>::type *data, lon
   for (int e = threadIdx.x; e < L * TC; e += NT) {
     const int i = e / TC, c = e % TC;
     if (c < tcv && (i - lm0 + L) % L < lmn) {
-      cp_async<sizeof(C)>(tile + i * TCP + c, base + (size_t)i * (size_t)B + c);
+      // out-of-place x pass: columns other than kz = 0 and kz = L/2 come from src
+      const int kz = (int)((b0 + c) % (L / 2 + 1));
+      const C *from = (src && kz != 0 && kz != L / 2) ? src + (base - data) : base;
+      cp_async<sizeof(C)>(tile + i * TCP + c, from + (size_t)i * (size_t)B + c);
     } else {
       C z;
       z.x = 0;
@@ -653,9 +675,16 @@ struct ColsIn {
   int L;
   long long b0;
   int m0 = 0, mn = 1 << 30;
+  // out-of-place x pass: columns other than kz = 0 and kz = L/2 come from alt (same layout)
+  const C *alt = nullptr;
   __device__ __forceinline__ C operator()(int c, int m) const {
     if (c >= tcv || (m - m0 + L) % L >= mn) return czero<C>();
-    const C *p = base + (size_t)m * (size_t)B + c;
+    const C *from = base;
+    if (alt) {
+      const int kz = (int)((b0 + c) % (L / 2 + 1));
+      if (kz != 0 && kz != L / 2) from = alt;
+    }
+    const C *p = from + (size_t)m * (size_t)B + c;
     C v = CG ? __ldcg(p) : *p;
     return tab ? cscale(v, qtab(tab, L, m, b0 + c)) : v;
   }
@@ -715,7 +744,8 @@ struct RowsIn {
 template <typename T, int L, int TC, int NT, int SIGN>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_fft_cols_fused(typename Cx<T>::type *data, long long B,
                                                        const typename Cx<T>::type *tw, T scale, const T *tab,
-                                                       int a0, int A, int m0, int mn) {
+                                                       int a0, int A, int m0, int mn,
+                                                       const typename Cx<T>::type *src) {
   using C = typename Cx<T>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
   C *tile = reinterpret_cast<C *>(smraw);
@@ -724,7 +754,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_fft_cols_fused(typename Cx<T>
   const int tcv = (int)min((long long)TC, B - b0);
   // the window limits the loads of a forward pass and the stores of an inverse one
   const int lm0 = SIGN < 0 ? m0 : 0, lmn = SIGN < 0 ? mn : L, sm0 = SIGN > 0 ? m0 : 0, smn = SIGN > 0 ? mn : L;
-  first_stage_from<T, L, TC, NT, SIGN>(tile, ColsIn<C>{base, B, tcv, SIGN > 0 ? tab : nullptr, L, b0, lm0, lmn});
+  const C *alt = src ? src + (base - data) : nullptr;
+  first_stage_from<T, L, TC, NT, SIGN>(tile, ColsIn<C>{base, B, tcv, SIGN > 0 ? tab : nullptr, L, b0, lm0, lmn, alt});
   constexpr int R0 = next_radix(L, 1), NSL = last_stage_ns(L);
   TileStagesUntil<T, L, TC, TC, NT, R0, NSL, SIGN, 1>::run(tile, tw);
   last_stage_to<T, L, TC, NT, SIGN, 1>(tile, tw,
@@ -1026,22 +1057,22 @@ struct FixedFft {
 
   template <int TC, int NT, int SIGN>
   static void cols(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const T *tab, int a0, int na,
-                   int m0, int mn) {
+                   int m0, int mn, const C *src) {
     static std::atomic<int> mask{0};
     const size_t smem = (size_t)N * (TC + 1) * sizeof(C);
     set_smem_once((const void *)k_fft_cols<T, N, TC, NT, SIGN>, smem, mask);
     dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)na);
-    k_fft_cols<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A, m0, mn);
+    k_fft_cols<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A, m0, mn, src);
     launched();
   }
   template <int TC, int NT, int SIGN>
   static void cols_fused(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const T *tab, int a0,
-                         int na, int m0, int mn) {
+                         int na, int m0, int mn, const C *src) {
     static std::atomic<int> mask{0};
     const size_t smem = (size_t)N * TC * sizeof(C);
     set_smem_once((const void *)k_fft_cols_fused<T, N, TC, NT, SIGN>, smem, mask);
     dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)na);
-    k_fft_cols_fused<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A, m0, mn);
+    k_fft_cols_fused<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A, m0, mn, src);
     launched();
   }
   // row tiles of RPC rows covering the selection: grid (tiles, planes)
@@ -1084,21 +1115,23 @@ struct FixedFft {
   }
   // a0, na: the planes (a0 + i) mod A, i < na, of the strided pass (na < 0: all A);
   // m0, mn: the positions along the transform read (forward) or written (inverse)
+  // src: an out-of-place inverse x pass reads the columns other than kz = 0, N/2 from src
   static void cols_cfg(Context &ctx, int cfg, int sign, C *d, int A, long long B, const C *tw, T scale,
-                       const T *tab = nullptr, int a0 = 0, int na = -1, int m0 = 0, int mn = N) {
+                       const T *tab = nullptr, int a0 = 0, int na = -1, int m0 = 0, int mn = N,
+                       const C *src = nullptr) {
     if (na < 0) na = A;
     if (cfg == 2) {
-      if (sign > 0) cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn);
-      else cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn);
+      if (sign > 0) cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src);
+      else cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src);
     } else if (cfg == 3) {
-      if (sign > 0) cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn);
-      else cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn);
+      if (sign > 0) cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src);
+      else cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src);
     } else if (cfg == 0) {
-      if (sign > 0) cols<F32 ? 8 : 4, 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn);
-      else cols<F32 ? 8 : 4, 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn);
+      if (sign > 0) cols<F32 ? 8 : 4, 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src);
+      else cols<F32 ? 8 : 4, 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src);
     } else {
-      if (sign > 0) cols<F32 ? 16 : 8, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn);
-      else cols<F32 ? 16 : 8, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn);
+      if (sign > 0) cols<F32 ? 16 : 8, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src);
+      else cols<F32 ? 16 : 8, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src);
     }
   }
   static void rows_cfg(Context &ctx, int cfg, bool inv, C *d, const C *tw, T scale, const Sel &sel = whole_sel()) {
@@ -1156,9 +1189,9 @@ struct FixedFft {
   // inverse: the x pass over every column, then the y transforms of the selected
   // planes and the real transforms of the selected rows (output valid there)
   static void c2r(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, int pv, const T *tab,
-                  const Sel &sel) {
+                  const Sel &sel, const C *src = nullptr) {
     // the x pass stores the selected planes only, the y pass the selected rows only
-    cols_cfg(ctx, ccfg, +1, c, 1, (long long)N * S, tw, (T)1, tab, 0, -1, sel.x0, sel.nx);
+    cols_cfg(ctx, ccfg, +1, c, 1, (long long)N * S, tw, (T)1, tab, 0, -1, sel.x0, sel.nx, src);
     if (kPlanes && pv >= 0 && sel.whole()) {
       planes<true>(ctx, c, tw, scale, pv);
       return;
@@ -1237,7 +1270,7 @@ std::vector<SharedTune> g_tuned;
 
 template <typename T, int N>
 void fixed_transform(Context &ctx, typename Cx<T>::type *c, const typename Cx<T>::type *tw, double scale, bool inverse,
-                     const T *tab, const CellBox *box) {
+                     const T *tab, const CellBox *box, const typename Cx<T>::type *src) {
   FftTables &F = ctx.fft;
   const bool dbl = sizeof(T) == 8;
   int cc = -1, rc = -1, pv = -1;
@@ -1276,21 +1309,21 @@ void fixed_transform(Context &ctx, typename Cx<T>::type *c, const typename Cx<T>
     sel.y0 = ((box->start[1] % N) + N) % N;
     sel.ny = box->len[1];
   }
-  if (inverse) FixedFft<T, N>::c2r(ctx, c, tw, (T)scale, cc, rc, pv, tab, sel);
+  if (inverse) FixedFft<T, N>::c2r(ctx, c, tw, (T)scale, cc, rc, pv, tab, sel, src);
   else FixedFft<T, N>::r2c(ctx, c, tw, (T)scale, cc, rc, pv, tab, sel);
 }
 
 // power-of-two sizes 32..1024 use the fixed-length passes
 template <typename T>
 bool fixed_dispatch(Context &ctx, typename Cx<T>::type *c, int n, const typename Cx<T>::type *tw, double scale,
-                    bool inverse, const T *tab, const CellBox *box) {
+                    bool inverse, const T *tab, const CellBox *box, const typename Cx<T>::type *src = nullptr) {
   switch (n) {
-    case 32: fixed_transform<T, 32>(ctx, c, tw, scale, inverse, tab, box); return true;
-    case 64: fixed_transform<T, 64>(ctx, c, tw, scale, inverse, tab, box); return true;
-    case 128: fixed_transform<T, 128>(ctx, c, tw, scale, inverse, tab, box); return true;
-    case 256: fixed_transform<T, 256>(ctx, c, tw, scale, inverse, tab, box); return true;
-    case 512: fixed_transform<T, 512>(ctx, c, tw, scale, inverse, tab, box); return true;
-    case 1024: fixed_transform<T, 1024>(ctx, c, tw, scale, inverse, tab, box); return true;
+    case 32: fixed_transform<T, 32>(ctx, c, tw, scale, inverse, tab, box, src); return true;
+    case 64: fixed_transform<T, 64>(ctx, c, tw, scale, inverse, tab, box, src); return true;
+    case 128: fixed_transform<T, 128>(ctx, c, tw, scale, inverse, tab, box, src); return true;
+    case 256: fixed_transform<T, 256>(ctx, c, tw, scale, inverse, tab, box, src); return true;
+    case 512: fixed_transform<T, 512>(ctx, c, tw, scale, inverse, tab, box, src); return true;
+    case 1024: fixed_transform<T, 1024>(ctx, c, tw, scale, inverse, tab, box, src); return true;
     default: return false;
   }
 }
@@ -1410,6 +1443,28 @@ bool take_fft_wait_error(Context &ctx) {
   return true;
 }
 
+template <typename T>
+void fft_c2r_3d_from(Context &ctx, T *dst, const T *src, int n, double scale, const T *pre_tab, const CellBox *box) {
+  using C = typename Cx<T>::type;
+  if (n < 2 || n % 2) fail(GIC_ERR_INVALID_ARG, "FFT size must be even");
+  if (!fft_prunes(ctx, n)) {
+    // runtime-length passes: copy, then transform in place
+    GIC_CUDA(cudaMemcpyAsync(dst, src, (size_t)n * n * (n / 2 + 1) * sizeof(C), cudaMemcpyDeviceToDevice, ctx.stream));
+    fft_c2r_3d<T>(ctx, dst, n, scale, pre_tab, box);
+    return;
+  }
+  const C *tw = (const C *)ctx.fft.get(n, sizeof(T) == 8, ctx.stream);
+  C *d = reinterpret_cast<C *>(dst);
+  const C *s = reinterpret_cast<const C *>(src);
+  long long mirror_threads = 2ll * n * n;
+  k_mirror_from<T><<<(unsigned)((mirror_threads + 255) / 256), 256, 0, ctx.stream>>>(d, s, n);
+  launched();
+  fixed_dispatch<T>(ctx, d, n, tw, scale, true, pre_tab, box, s);
+}
+
+template void fft_c2r_3d_from<float>(Context &, float *, const float *, int, double, const float *, const CellBox *);
+template void fft_c2r_3d_from<double>(Context &, double *, const double *, int, double, const double *,
+                                      const CellBox *);
 template void fft_c2r_3d<float>(Context &, float *, int, double, const float *, const CellBox *);
 template void fft_c2r_3d<double>(Context &, double *, int, double, const double *, const CellBox *);
 template void fft_r2c_3d<float>(Context &, float *, int, double, const float *, const CellBox *);

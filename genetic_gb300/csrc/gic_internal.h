@@ -286,6 +286,11 @@ void fft_c2r_3d(Context &ctx, T *data, int n, double scale, const T *pre_tab = n
 template <typename T>
 void fft_r2c_3d(Context &ctx, T *data, int n, double scale, const T *post_tab = nullptr,
                 const CellBox *box = nullptr);
+// the inverse transform of src (unchanged) into dst: the first pass reads src, so no
+// copy of the spectrum is made (the runtime-length passes copy, then transform)
+template <typename T>
+void fft_c2r_3d_from(Context &ctx, T *dst, const T *src, int n, double scale, const T *pre_tab = nullptr,
+                     const CellBox *box = nullptr);
 // whether transforms of size n honour a box (the fixed-length passes), so that a forward
 // transform reads only the box's x planes and its input need be valid there only
 bool fft_prunes(const Context &ctx, int n);
@@ -322,7 +327,8 @@ void lowpass_tables(Context &ctx, int coarse_index);
 
 // zoom.cu
 template <typename T, int NF>
-void interp_add(Context &ctx, const Level &coarse, const T *const *src, const Level &fine, T *const *dst);
+void interp_add(Context &ctx, const Level &coarse, const T *const *src, const Level &fine, T *const *dst,
+                bool assign = false);
 
 // modify.cu
 double modification_value(Context &ctx, ModRequest &m);

@@ -1041,26 +1041,24 @@ struct ModEngine {
     return r * r * r;
   }
 
-  void cross_term_impl(T *target_real, int t, const T *source_k, int s) {
+  // assign: a coarser source's interpolation replaces target_real (every cell of the
+  // finer level is written) instead of adding to it
+  void cross_term_impl(T *target_real, int t, const T *source_k, int s, bool assign = false) {
     TableSpec sp{};
     sp.power = 1;
     add_filter_factors(sp, t);
     add_filter_factors(sp, s);
     sp.scalar = std::sqrt(level_weight(t) / level_weight(s));
     S.tmp_src.ensure(elems(s) * sizeof(T));
-    GIC_CUDA(cudaMemcpyAsync(S.tmp_src.ptr, source_k, elems(s) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
     table(sp, s);
-    if (s < t) {
-      // the interpolation reads the coarse cells around the fine level only
-      const CellBox fp = footprint(t, s, 3);
-      to_real_times_table(S.tmp_src.template as<T>(), s, &fp);
-    } else {
-      to_real_times_table(S.tmp_src.template as<T>(), s);
-    }
+    // source (Fourier, unchanged) times the table, to real space in tmp_src; the
+    // interpolation up reads the coarse cells around the fine level only
+    const CellBox fp = footprint(t, s, 3);
+    fft_c2r_3d_from<T>(ctx, S.tmp_src.template as<T>(), source_k, lev(s).n, scale(s), tabT(), s < t ? &fp : nullptr);
     if (s < t) {
       const T *src[1] = {S.tmp_src.template as<T>()};
       T *dst[1] = {target_real};
-      interp_add<T, 1>(ctx, lev(s), src, lev(t), dst);
+      interp_add<T, 1>(ctx, lev(s), src, lev(t), dst, assign);
     } else {
       const Level &F = lev(s), &Cl = lev(t);
       int r = (int)std::lround(Cl.dx / F.dx);
@@ -1081,8 +1079,7 @@ struct ModEngine {
     for (int t = 0; t < nl(); ++t) {
       T *R = ptr(out, t);
       if (to_covector && t < nl() - 1) {
-        GIC_CUDA(cudaMemcpyAsync(R, ptr(X, t), elems(t) * sizeof(T), cudaMemcpyDeviceToDevice, ctx.stream));
-        to_real(R, t);
+        fft_c2r_3d_from<T>(ctx, R, ptr(X, t), lev(t).n, scale(t));
         windowed_covector_real(X, t, R);
         to_fourier(R, t);
       } else {
@@ -1092,17 +1089,23 @@ struct ModEngine {
         if (nl() > 1) {
           inw.ensure(elems(t) * sizeof(T));
           T *Cr = inw.template as<T>();
-          GIC_CUDA(cudaMemsetAsync(Cr, 0, elems(t) * sizeof(T), ctx.stream));
-          for (int s = 0; s < nl(); ++s)
-            if (s != t) cross_term_impl(Cr, t, ptr(X, s), s);
-          // with no coarser source, the block means of the finer levels fill only
-          // the next level's footprint
+          // with no coarser source (t = 0) the block means of the finer levels fill only
+          // the next level's footprint: only its planes are zeroed (the transform reads
+          // those only); otherwise the coarser source's interpolation assigns every cell
+          const CellBox fp = footprint(std::min(t + 1, nl() - 1), t, 1);
+          bool first = true;
           if (t == 0) {
-            const CellBox fp = footprint(1, 0, 1);
-            to_fourier(Cr, t, &fp);
-          } else {
-            to_fourier(Cr, t);
+            if (fft_prunes(ctx, lev(0).n)) zero_planes(Cr, 0, fp);
+            else GIC_CUDA(cudaMemsetAsync(Cr, 0, elems(t) * sizeof(T), ctx.stream));
+            first = false;
           }
+          for (int s = 0; s < nl(); ++s)
+            if (s != t) {
+              cross_term_impl(Cr, t, ptr(X, s), s, first && s < t);
+              first = false;
+            }
+          if (t == 0) to_fourier(Cr, t, &fp);
+          else to_fourier(Cr, t);
           add = reinterpret_cast<const C *>(Cr);
         }
         family_table(t, 2);
@@ -1208,8 +1211,7 @@ struct ModEngine {
       const size_t bytes = elems(t) * sizeof(T);
       if (t < nl() - 1) {
         auto R = ctx.pool.take(bytes), xr = ctx.pool.take(bytes);
-        GIC_CUDA(cudaMemcpyAsync(R->ptr, ptr(X, t), bytes, cudaMemcpyDeviceToDevice, ctx.stream));
-        to_real(R->template as<T>(), t);
+        fft_c2r_3d_from<T>(ctx, R->template as<T>(), ptr(X, t), lev(t).n, scale(t));
         GIC_CUDA(cudaMemcpyAsync(xr->ptr, R->ptr, bytes, cudaMemcpyDeviceToDevice, ctx.stream));
         windowed_covector_real(X, t, R->template as<T>());
         terms.push_back({R->template as<T>(), xr->template as<T>(), t, kReal});
@@ -1223,9 +1225,9 @@ struct ModEngine {
         if (nl() > 1) {
           S.win.ensure(bytes);
           T *Cr = S.win.template as<T>();
-          GIC_CUDA(cudaMemsetAsync(Cr, 0, bytes, ctx.stream));
+          // t is the finest level: the first (coarser) source's interpolation assigns
           for (int s = 0; s < nl(); ++s)
-            if (s != t) cross_term_impl(Cr, t, ptr(X, s), s);
+            if (s != t) cross_term_impl(Cr, t, ptr(X, s), s, s == 0);
           to_fourier(Cr, t);
           axpy(r, Cr, 1.0, t);
         }

@@ -58,6 +58,7 @@ template <typename T, int NF>
 struct FieldPtrs {
   const T *src[NF];
   T *dst[NF];
+  int assign;  // 1: dst = interpolation (dst need not be initialised), 0: dst += it
 };
 
 // Direct form (any geometry): one thread per fine cell, 64 coarse values per field.
@@ -92,7 +93,7 @@ __global__ void __launch_bounds__(256) k_interp_add_direct(FieldPtrs<T, NF> fp, 
       }
     }
   size_t dst = row * (size_t)(2 * (nf / 2 + 1)) + pos[2];
-  for (int f = 0; f < NF; ++f) fp.dst[f][dst] += s[f];
+  for (int f = 0; f < NF; ++f) fp.dst[f][dst] = fp.assign ? s[f] : fp.dst[f][dst] + s[f];
 }
 
 // Separable form: a CTA owns one fine x plane and TY fine y rows.  Three contractions,
@@ -170,7 +171,7 @@ __global__ void __launch_bounds__(256) k_interp_add_sep(FieldPtrs<T, NF> fp, int
       }
       size_t dst = ((size_t)x * nf + y) * frs + z;
 #pragma unroll
-      for (int f = 0; f < NF; ++f) fp.dst[f][dst] += s[f];
+      for (int f = 0; f < NF; ++f) fp.dst[f][dst] = fp.assign ? s[f] : fp.dst[f][dst] + s[f];
     }
   }
 }
@@ -242,7 +243,7 @@ __global__ void __launch_bounds__(256) k_interp_add_tile(FieldPtrs<T, NF> fp, in
     }
     size_t dst = ((size_t)x * nf + y) * frs + z;
 #pragma unroll
-    for (int f = 0; f < NF; ++f) fp.dst[f][dst] += s[f];
+    for (int f = 0; f < NF; ++f) fp.dst[f][dst] = fp.assign ? s[f] : fp.dst[f][dst] + s[f];
   }
 }
 
@@ -251,7 +252,7 @@ __global__ void __launch_bounds__(256) k_interp_add_tile(FieldPtrs<T, NF> fp, in
 // Add the tricubic interpolation of NF real fields of grid `coarse` onto the
 // NF real fields of grid `fine` (any two levels, coarse cells larger).
 template <typename T, int NF>
-void interp_add(Context &ctx, const Level &coarse, const T *const *src, const Level &fine, T *const *dst) {
+void interp_add(Context &ctx, const Level &coarse, const T *const *src, const Level &fine, T *const *dst, bool assign) {
   size_t m = fine.ncells();
   int wrap = (coarse.box == coarse.periodic) ? 1 : 0;
   int nf = fine.n;
@@ -270,6 +271,7 @@ void interp_add(Context &ctx, const Level &coarse, const T *const *src, const Le
   int ny = (int)std::ceil(TY * ratio) + 6;
   size_t smem = (size_t)NF * ny * ((size_t)span + nf) * sizeof(T);
   FieldPtrs<T, NF> fp;
+  fp.assign = assign ? 1 : 0;
   for (int f = 0; f < NF; ++f) {
     fp.src[f] = src[f];
     fp.dst[f] = dst[f];
@@ -323,7 +325,7 @@ void interp_add_fields(Context &ctx, const Level &coarse, T *const src[4], Level
 
 template void interp_add_fields<float>(Context &, const Level &, float *const[4], Level &, unsigned);
 template void interp_add_fields<double>(Context &, const Level &, double *const[4], Level &, unsigned);
-template void interp_add<float, 1>(Context &, const Level &, const float *const *, const Level &, float *const *);
-template void interp_add<double, 1>(Context &, const Level &, const double *const *, const Level &, double *const *);
+template void interp_add<float, 1>(Context &, const Level &, const float *const *, const Level &, float *const *, bool);
+template void interp_add<double, 1>(Context &, const Level &, const double *const *, const Level &, double *const *, bool);
 
 }  // namespace gic
