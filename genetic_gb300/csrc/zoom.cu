@@ -156,11 +156,29 @@ __global__ void __launch_bounds__(256) k_interp_add_sep(FieldPtrs<T, NF> fp, int
   }
   __syncthreads();
   const size_t frs = (size_t)(2 * (nf / 2 + 1));
-  for (int y = y0; y <= ylast; ++y) {
-    T wy[4];
-    catmull_rom<T>(__ldg(frac + nf + y), wy);
-    const int py = __ldg(ubase + nf + y) - 1 - cy0;
-    for (int z = threadIdx.x; z < nf; z += blockDim.x) {
+  // fine cells (y, z) of the block, U per thread at a time: their destination loads are
+  // all issued before the sums (the read-modify-write is otherwise latency-bound)
+  constexpr int U = 4;
+  const int cnt = (ylast - y0 + 1) * nf;
+  for (int e0 = threadIdx.x; e0 < cnt; e0 += U * blockDim.x) {
+    T cur[U][NF];
+    size_t dsts[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int e = e0 + u * blockDim.x;
+      const int y = y0 + e / nf, z = e % nf;
+      dsts[u] = ((size_t)x * nf + y) * frs + z;
+#pragma unroll
+      for (int f = 0; f < NF; ++f) cur[u][f] = (e < cnt && !fp.assign) ? fp.dst[f][dsts[u]] : (T)0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int e = e0 + u * blockDim.x;
+      if (e >= cnt) break;
+      const int y = y0 + e / nf, z = e % nf;
+      T wy[4];
+      catmull_rom<T>(__ldg(frac + nf + y), wy);
+      const int py = __ldg(ubase + nf + y) - 1 - cy0;
       T s[NF];
 #pragma unroll
       for (int f = 0; f < NF; ++f) s[f] = 0;
@@ -169,9 +187,8 @@ __global__ void __launch_bounds__(256) k_interp_add_sep(FieldPtrs<T, NF> fp, int
 #pragma unroll
         for (int f = 0; f < NF; ++f) s[f] += wy[b] * Q[((size_t)f * maxcy + py + b) * nf + z];
       }
-      size_t dst = ((size_t)x * nf + y) * frs + z;
 #pragma unroll
-      for (int f = 0; f < NF; ++f) fp.dst[f][dst] = fp.assign ? s[f] : fp.dst[f][dst] + s[f];
+      for (int f = 0; f < NF; ++f) fp.dst[f][dsts[u]] = fp.assign ? s[f] : cur[u][f] + s[f];
     }
   }
 }
