@@ -268,6 +268,7 @@ int gic_level_add(gic_ctx *ctx, double box, int n, double x0, double y0, double 
   L->dx = box / n;
   L->periodic = C.levels.empty() ? box : C.levels[0]->periodic;
   C.levels.push_back(std::move(L));
+  C.table_cache.clear();
   if (level_id) *level_id = (int)C.levels.size() - 1;
   API_END
 }
@@ -284,6 +285,7 @@ int gic_set_cosmology(gic_ctx *ctx, const gic_cosmo *cosmo) {
   C.cosmo.z = cosmo->redshift;
   C.cosmo.a = 1. / (cosmo->redshift + 1.);
   C.have_cosmo = true;
+  C.table_cache.clear();
   API_END
 }
 

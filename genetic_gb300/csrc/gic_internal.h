@@ -207,6 +207,14 @@ struct QuadRequest {
   int init_steps = 10;
 };
 
+// A per-|k|^2 table of the modification algebra, kept across calls: it depends on its
+// specification (filters, scalars, level), on the transfer function and on the
+// cosmology, so the cache is emptied when those or the levels change.
+struct CachedTable {
+  std::vector<unsigned char> key;
+  DevBuf d, f;  // the table and its float copy
+};
+
 struct Context {
   int device = 0;
   int precision = GIC_FP64;
@@ -225,6 +233,7 @@ struct Context {
   std::vector<QuadRequest> quads;
   BufPool pool;
   ModScratch modscratch;
+  std::vector<std::unique_ptr<CachedTable>> table_cache;
   bool dbl() const { return precision == GIC_FP64; }
 };
 

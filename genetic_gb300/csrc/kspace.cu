@@ -342,6 +342,7 @@ void transfer_setup(Context &ctx, const double *table, int nrows, int ncols) {
   T.lnk_min = lx_all.front();
   T.lnk_max = lx_all.back();
   T.ready = true;
+  ctx.table_cache.clear();
   for (auto &L : ctx.levels) {
     L->sqrtp.release();
     L->sqrtp_dm.release();

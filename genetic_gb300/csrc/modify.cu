@@ -812,7 +812,7 @@ struct ModEngine {
   // transform's output inside it is used (the transforms skip the rest)
   void to_fourier(T *p, int l, const CellBox *box = nullptr) { fft_r2c_3d<T>(ctx, p, lev(l).n, scale(l), nullptr, box); }
   void to_real(T *p, int l) { fft_c2r_3d<T>(ctx, p, lev(l).n, scale(l)); }
-  // times the current table (S.tab), then to real space: the multiply rides on the
+  // times the current table, then to real space: the multiply rides on the
   // transform's first pass (bit-identical to mul_table followed by to_real)
   void to_real_times_table(T *p, int l, const CellBox *box = nullptr) {
     fft_c2r_3d<T>(ctx, p, lev(l).n, scale(l), tabT(), box);
@@ -835,20 +835,47 @@ struct ModEngine {
   }
   double kcut(int l) { return 0.3 * ((double)lev(l).n * lev(l).kmin()); }
 
+  // the table of `sp0` on grid g becomes the current one: from the context's cache, or
+  // built (k_mod_table, double with a float copy) and cached
   void table(const TableSpec &sp0, int g) {
     long long half = lev(g).n / 2, nq = 3 * half * half + 1;
-    S.tab.ensure(nq * sizeof(double));
-    if (sizeof(T) == 4) S.tabf.ensure(nq * sizeof(float));
     TableSpec sp = sp0;
     sp.kmin = lev(g).kmin();
-    k_mod_table<<<nblk(nq), 256, 0, ctx.stream>>>(S.tab.template as<double>(),
-                                                 sizeof(T) == 4 ? S.tabf.template as<float>() : nullptr, nq, sp);
+    std::vector<unsigned char> key;
+    auto put = [&key](const void *p, size_t n) {
+      const unsigned char *b = static_cast<const unsigned char *>(p);
+      key.insert(key.end(), b, b + n);
+    };
+    const int dims[6] = {g, lev(g).n, sp.nhp, sp.nlp, sp.power, (int)sizeof(T)};
+    put(dims, sizeof(dims));
+    put(&sp.kmin, sizeof(double));
+    put(sp.hp_cut, sp.nhp * sizeof(double));
+    put(sp.lp_cut, sp.nlp * sizeof(double));
+    put(&sp.scalar, sizeof(double));
+    put(&sp.sqrtp, sizeof(sp.sqrtp));
+    put(&sp.vel, sizeof(double));
+    put(&sp.var_cut, sizeof(double));
+    for (auto &e : ctx.table_cache)
+      if (e->key == key) {
+        cur_tab = e.get();
+        return;
+      }
+    if (ctx.table_cache.size() >= 128) ctx.table_cache.clear();
+    auto e = std::make_unique<CachedTable>();
+    e->key = std::move(key);
+    e->d.ensure(nq * sizeof(double));
+    if (sizeof(T) == 4) e->f.ensure(nq * sizeof(float));
+    k_mod_table<<<nblk(nq), 256, 0, ctx.stream>>>(e->d.template as<double>(),
+                                                 sizeof(T) == 4 ? e->f.template as<float>() : nullptr, nq, sp);
     launched();
+    cur_tab = e.get();
+    ctx.table_cache.push_back(std::move(e));
   }
+  CachedTable *cur_tab = nullptr;
   // the current table in the fields' precision
   const T *tabT() const {
-    if constexpr (sizeof(T) == 4) return S.tabf.template as<float>();
-    else return S.tab.template as<double>();
+    if constexpr (sizeof(T) == 4) return cur_tab->f.template as<float>();
+    else return cur_tab->d.template as<double>();
   }
 
   void mul_table(T *p, int g) {
