@@ -157,7 +157,7 @@ struct FftTables {
 };
 
 struct RngScratch {
-  DevBuf raw, gauss, owner, segtab, segentry, segbase, blkmap, blkentry, blkbase, streams, chunkmul, flags;
+  DevBuf raw, gauss, owner, segtab, segentry, segbase, blkmap, blkentry, blkbase, streams, chunkmul, flags, tailq;
   int chunkmul_count = 0;
 };
 

@@ -225,9 +225,16 @@ struct Reader {
 // once), so a decision outside the margin is the double-precision decision.
 // Only attempts inside the margin are evaluated in double.  Values are always
 // computed in double.
+// Accepted base-strip tail samples need x = R - log(1 - kk/2^24) / R in double, a
+// correctly rounded double-double log and a division: about a thousand FP64
+// instructions, run by one lane of a warp at a time, and on GB300 each of them holds the
+// narrow FP64 pipe for the whole warp.  With `defer` set the value is left to
+// k_tail_values (a dense pass over the queued samples): the sample's kk and sign go to
+// tail_kk / tail_neg (tail_kk > 0) and g is not set.
 template <bool VALUE>
 __device__ __forceinline__ bool zig_gaussian(const ZigTab &T, const Reader &rd, unsigned long long end,
-                                             unsigned long long &p, double &g) {
+                                             unsigned long long &p, double &g, bool defer = false,
+                                             uint32_t *tail_kk = nullptr, unsigned long long *tail_neg = nullptr) {
   const double R = GIC_ZIG_PARAM_R;
   const float Rf = (float)GIC_ZIG_PARAM_R;
   for (int guard = 0; guard < 1 << 20; ++guard) {
@@ -273,6 +280,12 @@ __device__ __forceinline__ bool zig_gaussian(const ZigTab &T, const Reader &rd, 
       float ef = expf(-0.5f * xt * xt);
       accept = yf < ef * (1.0f - 1e-4f) ? 1 : (yf > ef * (1.0f + 1e-4f) ? 0 : -1);
       double x = 0;
+      if (VALUE && accept > 0 && defer) {
+        p += 4;
+        *tail_kk = 16777216u - kk;
+        *tail_neg = neg;
+        return true;
+      }
       if (accept < 0 || (VALUE && accept > 0)) {
         double lg = gic_log_k24(16777216u - kk);  // log(1 - kk/2^24), correctly rounded
         x = __dsub_rn(R, __ddiv_rn(lg, R));
@@ -294,21 +307,51 @@ __device__ __forceinline__ bool zig_gaussian(const ZigTab &T, const Reader &rd, 
 
 // Walk [seg_start, seg_end) from seg_start + entry, counting gaussians that
 // start in the segment; exit = position after the last one minus seg_end.
+// tail samples whose values k_tail_values computes: where the value goes, its argument
+// 2^24 - kk and its sign bit
+struct TailSample {
+  double *at;
+  uint32_t arg;
+  uint32_t neg;  // 1: negative
+};
+struct TailQueue {
+  TailSample *items = nullptr;  // null: values computed in place
+  unsigned *count = nullptr;
+  unsigned cap = 0;
+};
+
 template <bool VALUE>
 __device__ void walk_segment(const ZigTab &T, const Reader &rd, unsigned long long stream_end, unsigned long long seg_start,
                              unsigned long long seg_end, unsigned entry, uint32_t &count, uint32_t &exit_off,
-                             double *out, unsigned long long out_limit) {
+                             double *out, unsigned long long out_limit, TailQueue q = TailQueue{}) {
   unsigned long long p = seg_start + entry;
   uint32_t cnt = 0;
   while (p < seg_end) {
     if (VALUE && cnt >= out_limit) break;
     double g = 0;
-    if (!zig_gaussian<VALUE>(T, rd, stream_end, p, g)) {
+    uint32_t tail_kk = 0;
+    unsigned long long tail_neg = 0;
+    const unsigned long long p_before = p;
+    if (!zig_gaussian<VALUE>(T, rd, stream_end, p, g, VALUE && q.items != nullptr, &tail_kk, &tail_neg)) {
       count = cnt;
       exit_off = kUnderrun;
       return;
     }
-    if (VALUE) out[cnt] = g;
+    if (VALUE) {
+      if (tail_kk) {
+        const unsigned slot = atomicAdd(q.count, 1u);
+        if (slot < q.cap) {
+          q.items[slot] = TailSample{out + cnt, tail_kk, tail_neg ? 1u : 0u};
+        } else {
+          // queue full: this sample's value in place
+          unsigned long long p2 = p_before;
+          zig_gaussian<VALUE>(T, rd, stream_end, p2, g);
+          out[cnt] = g;
+        }
+      } else {
+        out[cnt] = g;
+      }
+    }
     ++cnt;
   }
   count = cnt;
@@ -504,7 +547,7 @@ __global__ void k_chain_segments(const Stream *st, int nstreams, unsigned long l
 
 __global__ void k_walk_final(const Stream *st, int nstreams, unsigned long long nseg_total, const uint32_t *raw,
                              const uint32_t *seg_entry, const unsigned long long *seg_base, double *gauss,
-                             int *flags) {
+                             int *flags, TailQueue q) {
   __shared__ ZigTab zt;
   load_zig(zt);
   __syncthreads();
@@ -520,8 +563,21 @@ __global__ void k_walk_final(const Stream *st, int nstreams, unsigned long long 
   const Reader rd{raw};
   uint32_t cnt, ex;
   walk_segment<true>(zt, rd, S.raw_off + S.raw_count, a, b, seg_entry[gseg], cnt, ex, gauss + S.gauss_off + base,
-                     need - base);
+                     need - base, q);
   if (ex == kUnderrun && base + cnt < need) atomicExch(flags, 1);
+}
+
+// The deferred tail values: x = R - log(1 - kk/2^24) / R, correctly rounded log, one
+// sample per thread
+__global__ void k_tail_values(TailQueue q) {
+  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned n = min(*q.count, q.cap);
+  if (i >= n) return;
+  const TailSample t = q.items[i];
+  const double R = GIC_ZIG_PARAM_R;
+  const double lg = gic_log_k24(t.arg);
+  const double x = __dsub_rn(R, __ddiv_rn(lg, R));
+  *t.at = __longlong_as_double(__double_as_longlong(x) ^ (t.neg ? 0x8000000000000000ull : 0ull));
 }
 
 // ---- placement ----------------------------------------------------------------
@@ -700,10 +756,16 @@ static void generate_gaussians(Context &ctx, std::vector<Stream> &streams, unsig
       dst, ns, blk_total, R.raw.as<uint32_t>(), R.segtab.as<uint32_t>(), R.blkentry.as<uint32_t>(),
       R.blkbase.as<unsigned long long>(), R.segentry.as<uint32_t>(), R.segbase.as<unsigned long long>());
   launched();
+  // tail samples, about 6e-4 of the gaussians: a queue of 1/512 of them (overflow is
+  // computed in place), its count in the flags word 3
+  const unsigned tail_cap = (unsigned)std::min<unsigned long long>(total_gauss / 512 + 4096, 1ull << 30);
+  R.tailq.ensure((size_t)tail_cap * sizeof(TailSample));
+  TailQueue q{R.tailq.as<TailSample>(), reinterpret_cast<unsigned *>(R.flags.as<int>() + 3), tail_cap};
   k_walk_final<<<(unsigned)((seg_total + 127) / 128), 128, 0, cs>>>(
       dst, ns, seg_total, R.raw.as<uint32_t>(), R.segentry.as<uint32_t>(), R.segbase.as<unsigned long long>(),
-      R.gauss.as<double>(), R.flags.as<int>());
-  launched();
+      R.gauss.as<double>(), R.flags.as<int>(), q);
+  k_tail_values<<<(tail_cap + 255) / 256, 256, 0, cs>>>(q);
+  launched(2);
   int flag = 0;
   GIC_CUDA(cudaMemcpyAsync(&flag, R.flags.ptr, sizeof(int), cudaMemcpyDeviceToHost, cs));
   GIC_CUDA(cudaStreamSynchronize(cs));
@@ -963,7 +1025,7 @@ static int noalloc_run(unsigned long long seed, unsigned long long n, double *ou
   k_chain_blocks<<<1, 64, 0, cs>>>(dst, 1, raw, segtab, blkmap, blkentry, blkbase, flags);
   k_chain_segments<<<(s.nblk + 127) / 128, 128, 0, cs>>>(dst, 1, s.nblk, raw, segtab, blkentry, blkbase, segentry,
                                                          segbase);
-  k_walk_final<<<(s.nseg + 127) / 128, 128, 0, cs>>>(dst, 1, s.nseg, raw, segentry, segbase, out, flags);
+  k_walk_final<<<(s.nseg + 127) / 128, 128, 0, cs>>>(dst, 1, s.nseg, raw, segentry, segbase, out, flags, TailQueue{});
   if (!ok()) return GIC_ERR_CUDA;
   int flag = 0;
   if (cudaMemcpyAsync(&flag, flags, sizeof(int), cudaMemcpyDeviceToHost, cs) != cudaSuccess ||
