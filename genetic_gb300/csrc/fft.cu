@@ -522,7 +522,9 @@ struct TileStages<T, L, TC, TCP, NT, NS, SIGN, TWM, true> {
 template <typename T, int L, int TC, int NT, int SIGN>
 __global__ void __launch_bounds__(NT) k_fft_cols(typename Cx<T>::type *data, long long B,
                                                  const typename Cx<T>::type *tw, T scale, const T *tab, int a0,
-                                                 int A, int m0, int mn, const typename Cx<T>::type *src) {
+                                                 int A, int m0, int mn, const typename Cx<T>::type *src,
+                                                 typename Cx<T>::type *dst, const typename Cx<T>::type *xsrc,
+                                                 const T *xtab) {
   using C = typename Cx<T>::type;
   constexpr int TCP = TC + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -561,7 +563,13 @@ __global__ void __launch_bounds__(NT) k_fft_cols(typename Cx<T>::type *data, lon
     if (c < tcv && (i - sm0 + L) % L < smn) {
       C v = cscale(tile[i * TCP + c], scale);
       if (SIGN < 0 && tab) v = cscale(v, qtab(tab, L, i, b0 + c));
-      base[(size_t)i * (size_t)B + c] = v;
+      const size_t at = (size_t)i * (size_t)B + c;
+      if (dst) {
+        const size_t off = (size_t)(base - data);
+        dst[off + at] = cadd(cscale(xsrc[off + at], qtab(xtab, L, i, b0 + c)), v);
+      } else {
+        base[at] = v;
+      }
     }
   }
 }
@@ -699,11 +707,21 @@ struct ColsOut {
   int L;
   long long b0;
   int m0 = 0, mn = 1 << 30;
+  // forward x pass with an epilogue: the output goes to obase (same layout) as
+  // xtab[q] * xsrc + result
+  C *obase = nullptr;
+  const C *xsrc = nullptr;
+  const T *xtab = nullptr;
   __device__ __forceinline__ void operator()(int c, int m, C v) const {
     if (c >= tcv || (m - m0 + L) % L >= mn) return;
     v = cscale(v, scale);
     if (tab) v = cscale(v, qtab(tab, L, m, b0 + c));
-    base[(size_t)m * (size_t)B + c] = v;
+    const size_t at = (size_t)m * (size_t)B + c;
+    if (obase) {
+      obase[at] = cadd(cscale(xsrc[at], qtab(xtab, L, m, b0 + c)), v);
+      return;
+    }
+    base[at] = v;
   }
 };
 // c2r packing on the fly: Z[m] = (X[m] + conj X[H-m]) + i (X[m] - conj X[H-m]) e^{+2 pi i m / N}
@@ -745,7 +763,8 @@ template <typename T, int L, int TC, int NT, int SIGN>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_fft_cols_fused(typename Cx<T>::type *data, long long B,
                                                        const typename Cx<T>::type *tw, T scale, const T *tab,
                                                        int a0, int A, int m0, int mn,
-                                                       const typename Cx<T>::type *src) {
+                                                       const typename Cx<T>::type *src, typename Cx<T>::type *dst,
+                                                       const typename Cx<T>::type *xsrc, const T *xtab) {
   using C = typename Cx<T>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
   C *tile = reinterpret_cast<C *>(smraw);
@@ -758,8 +777,10 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_fft_cols_fused(typename Cx<T>
   first_stage_from<T, L, TC, NT, SIGN>(tile, ColsIn<C>{base, B, tcv, SIGN > 0 ? tab : nullptr, L, b0, lm0, lmn, alt});
   constexpr int R0 = next_radix(L, 1), NSL = last_stage_ns(L);
   TileStagesUntil<T, L, TC, TC, NT, R0, NSL, SIGN, 1>::run(tile, tw);
+  const size_t off = (size_t)(base - data);
   last_stage_to<T, L, TC, NT, SIGN, 1>(tile, tw,
-                                       ColsOut<C, T>{base, B, tcv, scale, SIGN < 0 ? tab : nullptr, L, b0, sm0, smn});
+                                       ColsOut<C, T>{base, B, tcv, scale, SIGN < 0 ? tab : nullptr, L, b0, sm0, smn,
+                                                     dst ? dst + off : nullptr, xsrc ? xsrc + off : nullptr, xtab});
 }
 
 template <typename T, int H, int RPC, int NT>
@@ -1057,22 +1078,24 @@ struct FixedFft {
 
   template <int TC, int NT, int SIGN>
   static void cols(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const T *tab, int a0, int na,
-                   int m0, int mn, const C *src) {
+                   int m0, int mn, const C *src, C *dst, const C *xsrc, const T *xtab) {
     static std::atomic<int> mask{0};
     const size_t smem = (size_t)N * (TC + 1) * sizeof(C);
     set_smem_once((const void *)k_fft_cols<T, N, TC, NT, SIGN>, smem, mask);
     dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)na);
-    k_fft_cols<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A, m0, mn, src);
+    k_fft_cols<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A, m0, mn, src, dst, xsrc,
+                                                                   xtab);
     launched();
   }
   template <int TC, int NT, int SIGN>
   static void cols_fused(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const T *tab, int a0,
-                         int na, int m0, int mn, const C *src) {
+                         int na, int m0, int mn, const C *src, C *dst, const C *xsrc, const T *xtab) {
     static std::atomic<int> mask{0};
     const size_t smem = (size_t)N * TC * sizeof(C);
     set_smem_once((const void *)k_fft_cols_fused<T, N, TC, NT, SIGN>, smem, mask);
     dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)na);
-    k_fft_cols_fused<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A, m0, mn, src);
+    k_fft_cols_fused<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A, m0, mn, src, dst,
+                                                                         xsrc, xtab);
     launched();
   }
   // row tiles of RPC rows covering the selection: grid (tiles, planes)
@@ -1116,22 +1139,23 @@ struct FixedFft {
   // a0, na: the planes (a0 + i) mod A, i < na, of the strided pass (na < 0: all A);
   // m0, mn: the positions along the transform read (forward) or written (inverse)
   // src: an out-of-place inverse x pass reads the columns other than kz = 0, N/2 from src
+  // dst, xsrc, xtab: a forward x pass writes xtab[q] xsrc + result to dst instead of in place
   static void cols_cfg(Context &ctx, int cfg, int sign, C *d, int A, long long B, const C *tw, T scale,
                        const T *tab = nullptr, int a0 = 0, int na = -1, int m0 = 0, int mn = N,
-                       const C *src = nullptr) {
+                       const C *src = nullptr, C *dst = nullptr, const C *xsrc = nullptr, const T *xtab = nullptr) {
     if (na < 0) na = A;
     if (cfg == 2) {
-      if (sign > 0) cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src);
-      else cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src);
+      if (sign > 0) cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src, dst, xsrc, xtab);
+      else cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src, dst, xsrc, xtab);
     } else if (cfg == 3) {
-      if (sign > 0) cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src);
-      else cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src);
+      if (sign > 0) cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src, dst, xsrc, xtab);
+      else cols_fused<F32 ? 16 : 8, F32 ? 512 : 128, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src, dst, xsrc, xtab);
     } else if (cfg == 0) {
-      if (sign > 0) cols<F32 ? 8 : 4, 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src);
-      else cols<F32 ? 8 : 4, 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src);
+      if (sign > 0) cols<F32 ? 8 : 4, 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src, dst, xsrc, xtab);
+      else cols<F32 ? 8 : 4, 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src, dst, xsrc, xtab);
     } else {
-      if (sign > 0) cols<F32 ? 16 : 8, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src);
-      else cols<F32 ? 16 : 8, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src);
+      if (sign > 0) cols<F32 ? 16 : 8, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src, dst, xsrc, xtab);
+      else cols<F32 ? 16 : 8, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src, dst, xsrc, xtab);
     }
   }
   static void rows_cfg(Context &ctx, int cfg, bool inv, C *d, const C *tw, T scale, const Sel &sel = whole_sel()) {
@@ -1202,7 +1226,7 @@ struct FixedFft {
   // forward, input zero outside the selection: the selected rows, the selected
   // planes' y transforms, then the x pass over every column
   static void r2c(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, int pv, const T *tab,
-                  const Sel &sel) {
+                  const Sel &sel, C *dst = nullptr, const C *xsrc = nullptr, const T *xtab = nullptr) {
     if (kPlanes && pv >= 0 && sel.whole()) {
       planes<false>(ctx, c, tw, (T)1, pv);
     } else {
@@ -1211,7 +1235,7 @@ struct FixedFft {
       cols_cfg(ctx, ccfg, -1, c, N, S, tw, (T)1, nullptr, sel.x0, sel.nx, sel.y0, sel.ny);
     }
     // planes outside the selection are zero: the x pass does not read them
-    cols_cfg(ctx, ccfg, -1, c, 1, (long long)N * S, tw, scale, tab, 0, -1, sel.x0, sel.nx);
+    cols_cfg(ctx, ccfg, -1, c, 1, (long long)N * S, tw, scale, tab, 0, -1, sel.x0, sel.nx, nullptr, dst, xsrc, xtab);
   }
   // time every candidate on a scratch array of the transform's size
   static void tune(Context &ctx, const C *tw, int &best_cols, int &best_rows, int &best_planes) {
@@ -1270,7 +1294,8 @@ std::vector<SharedTune> g_tuned;
 
 template <typename T, int N>
 void fixed_transform(Context &ctx, typename Cx<T>::type *c, const typename Cx<T>::type *tw, double scale, bool inverse,
-                     const T *tab, const CellBox *box, const typename Cx<T>::type *src) {
+                     const T *tab, const CellBox *box, const typename Cx<T>::type *src, typename Cx<T>::type *dst,
+                     const typename Cx<T>::type *xsrc, const T *xtab) {
   FftTables &F = ctx.fft;
   const bool dbl = sizeof(T) == 8;
   int cc = -1, rc = -1, pv = -1;
@@ -1310,20 +1335,22 @@ void fixed_transform(Context &ctx, typename Cx<T>::type *c, const typename Cx<T>
     sel.ny = box->len[1];
   }
   if (inverse) FixedFft<T, N>::c2r(ctx, c, tw, (T)scale, cc, rc, pv, tab, sel, src);
-  else FixedFft<T, N>::r2c(ctx, c, tw, (T)scale, cc, rc, pv, tab, sel);
+  else FixedFft<T, N>::r2c(ctx, c, tw, (T)scale, cc, rc, pv, tab, sel, dst, xsrc, xtab);
 }
 
 // power-of-two sizes 32..1024 use the fixed-length passes
 template <typename T>
 bool fixed_dispatch(Context &ctx, typename Cx<T>::type *c, int n, const typename Cx<T>::type *tw, double scale,
-                    bool inverse, const T *tab, const CellBox *box, const typename Cx<T>::type *src = nullptr) {
+                    bool inverse, const T *tab, const CellBox *box, const typename Cx<T>::type *src = nullptr,
+                    typename Cx<T>::type *dst = nullptr, const typename Cx<T>::type *xsrc = nullptr,
+                    const T *xtab = nullptr) {
   switch (n) {
-    case 32: fixed_transform<T, 32>(ctx, c, tw, scale, inverse, tab, box, src); return true;
-    case 64: fixed_transform<T, 64>(ctx, c, tw, scale, inverse, tab, box, src); return true;
-    case 128: fixed_transform<T, 128>(ctx, c, tw, scale, inverse, tab, box, src); return true;
-    case 256: fixed_transform<T, 256>(ctx, c, tw, scale, inverse, tab, box, src); return true;
-    case 512: fixed_transform<T, 512>(ctx, c, tw, scale, inverse, tab, box, src); return true;
-    case 1024: fixed_transform<T, 1024>(ctx, c, tw, scale, inverse, tab, box, src); return true;
+    case 32: fixed_transform<T, 32>(ctx, c, tw, scale, inverse, tab, box, src, dst, xsrc, xtab); return true;
+    case 64: fixed_transform<T, 64>(ctx, c, tw, scale, inverse, tab, box, src, dst, xsrc, xtab); return true;
+    case 128: fixed_transform<T, 128>(ctx, c, tw, scale, inverse, tab, box, src, dst, xsrc, xtab); return true;
+    case 256: fixed_transform<T, 256>(ctx, c, tw, scale, inverse, tab, box, src, dst, xsrc, xtab); return true;
+    case 512: fixed_transform<T, 512>(ctx, c, tw, scale, inverse, tab, box, src, dst, xsrc, xtab); return true;
+    case 1024: fixed_transform<T, 1024>(ctx, c, tw, scale, inverse, tab, box, src, dst, xsrc, xtab); return true;
     default: return false;
   }
 }
@@ -1442,6 +1469,41 @@ bool take_fft_wait_error(Context &ctx) {
   ctx.last_error = "FFT plane pass: a wait for another CTA's tiles gave up; results of the transform are invalid";
   return true;
 }
+
+// dst = xtab[q] x + (the forward transform of data, times post_tab): the x pass writes the sum
+template <typename T>
+__global__ void k_fft_add_epilogue(typename Cx<T>::type *dst, const typename Cx<T>::type *data,
+                                   const typename Cx<T>::type *x, const T *xtab, int n) {
+  const size_t S = (size_t)(n / 2 + 1);
+  const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= (size_t)n * n * S) return;
+  const int kx = (int)(id / ((size_t)n * S));
+  dst[id] = cadd(cscale(x[id], qtab(xtab, n, kx, (long long)(id - (size_t)kx * n * S))), data[id]);
+}
+
+template <typename T>
+void fft_r2c_3d_add(Context &ctx, T *data, int n, double scale, const T *post_tab, const CellBox *box, T *dst,
+                    const T *x, const T *xtab) {
+  using C = typename Cx<T>::type;
+  if (n < 2 || n % 2) fail(GIC_ERR_INVALID_ARG, "FFT size must be even");
+  C *c = reinterpret_cast<C *>(data);
+  if (fft_prunes(ctx, n)) {
+    const C *tw = (const C *)ctx.fft.get(n, sizeof(T) == 8, ctx.stream);
+    fixed_dispatch<T>(ctx, c, n, tw, scale, false, post_tab, box, nullptr, reinterpret_cast<C *>(dst),
+                      reinterpret_cast<const C *>(x), xtab);
+    return;
+  }
+  fft_r2c_3d<T>(ctx, data, n, scale, post_tab, box);
+  const size_t m = (size_t)n * n * (n / 2 + 1);
+  k_fft_add_epilogue<T><<<(unsigned)((m + 255) / 256), 256, 0, ctx.stream>>>(
+      reinterpret_cast<C *>(dst), c, reinterpret_cast<const C *>(x), xtab, n);
+  launched();
+}
+
+template void fft_r2c_3d_add<float>(Context &, float *, int, double, const float *, const CellBox *, float *,
+                                    const float *, const float *);
+template void fft_r2c_3d_add<double>(Context &, double *, int, double, const double *, const CellBox *, double *,
+                                     const double *, const double *);
 
 template <typename T>
 void fft_c2r_3d_from(Context &ctx, T *dst, const T *src, int n, double scale, const T *pre_tab, const CellBox *box) {

@@ -300,6 +300,12 @@ void fft_r2c_3d(Context &ctx, T *data, int n, double scale, const T *post_tab = 
 template <typename T>
 void fft_c2r_3d_from(Context &ctx, T *dst, const T *src, int n, double scale, const T *pre_tab = nullptr,
                      const CellBox *box = nullptr);
+// dst = xtab[q] x + the forward transform of data (times post_tab); data is overwritten
+// (the sum is formed by the x pass as it stores, one read and write of a field less than
+// a separate multiply-add)
+template <typename T>
+void fft_r2c_3d_add(Context &ctx, T *data, int n, double scale, const T *post_tab, const CellBox *box, T *dst,
+                    const T *x, const T *xtab);
 // whether transforms of size n honour a box (the fixed-length passes), so that a forward
 // transform reads only the box's x planes and its input need be valid there only
 bool fft_prunes(const Context &ctx, int n);

@@ -1131,14 +1131,15 @@ struct ModEngine {
               cross_term_impl(Cr, t, ptr(X, s), s, first && s < t);
               first = false;
             }
-          if (t == 0) to_fourier(Cr, t, &fp);
-          else to_fourier(Cr, t);
-          add = reinterpret_cast<const C *>(Cr);
+          // R = f_t^2 X_t + FFT(Cr), the sum formed by the transform's last pass
+          family_table(t, 2);
+          fft_r2c_3d_add<T>(ctx, Cr, lev(t).n, scale(t), nullptr, t == 0 ? &fp : nullptr, R, ptr(X, t), tabT());
+        } else {
+          family_table(t, 2);
+          k_mul_table_add<T><<<hs_grid(lev(t).n), hs_block(), 0, ctx.stream>>>(
+              reinterpret_cast<C *>(R), reinterpret_cast<const C *>(ptr(X, t)), lev(t).n, tabT(), add);
+          launched();
         }
-        family_table(t, 2);
-        k_mul_table_add<T><<<hs_grid(lev(t).n), hs_block(), 0, ctx.stream>>>(
-            reinterpret_cast<C *>(R), reinterpret_cast<const C *>(ptr(X, t)), lev(t).n, tabT(), add);
-        launched();
       }
       out.fourier[t] = 1;
     }
@@ -1247,16 +1248,18 @@ struct ModEngine {
       } else {
         auto R = ctx.pool.take(bytes);
         T *r = R->template as<T>();
-        GIC_CUDA(cudaMemcpyAsync(r, ptr(X, t), bytes, cudaMemcpyDeviceToDevice, ctx.stream));
-        apply_family(r, t, 2);
         if (nl() > 1) {
           S.win.ensure(bytes);
           T *Cr = S.win.template as<T>();
           // t is the finest level: the first (coarser) source's interpolation assigns
           for (int s = 0; s < nl(); ++s)
             if (s != t) cross_term_impl(Cr, t, ptr(X, s), s, s == 0);
-          to_fourier(Cr, t);
-          axpy(r, Cr, 1.0, t);
+          // r = f_t^2 X_t + FFT(Cr), formed by the transform's last pass
+          family_table(t, 2);
+          fft_r2c_3d_add<T>(ctx, Cr, lev(t).n, scale(t), nullptr, nullptr, r, ptr(X, t), tabT());
+        } else {
+          GIC_CUDA(cudaMemcpyAsync(r, ptr(X, t), bytes, cudaMemcpyDeviceToDevice, ctx.stream));
+          apply_family(r, t, 2);
         }
         terms.push_back({r, ptr(X, t), t, kFourier});
         keep.push_back(std::move(R));
