@@ -266,10 +266,11 @@ __global__ void k_scale(T *a, T c, size_t n) {
 //   op 0: r = (in ? 0 : r) + s      op 1: r = in ? s : r      op 2: r = in ? s : 0
 template <typename T>
 __global__ void k_window_op(T *r, const T *s, int n, const unsigned char *mx, const unsigned char *my,
-                            const unsigned char *mz, int op) {
-  // a CTA per row of n cells: the row's x and y window tests once, then its cells
-  const unsigned row = blockIdx.x;
-  const int x = (int)(row / (unsigned)n), y = (int)(row - (unsigned)x * (unsigned)n);
+                            const unsigned char *mz, int op, int x0, int y0, int ny) {
+  // a CTA per row of n cells of the rows x0 + i, y0 + j (cyclic; blockIdx.x = i ny + j):
+  // the row's x and y window tests once, then its cells
+  const int x = (x0 + (int)(blockIdx.x / (unsigned)ny)) % n, y = (y0 + (int)(blockIdx.x % (unsigned)ny)) % n;
+  const unsigned row = (unsigned)x * (unsigned)n + (unsigned)y;
   const bool row_in = mx[x] && my[y];
   const size_t base = (size_t)row * (size_t)(2 * (n / 2 + 1));
   for (int z = threadIdx.x; z < n; z += blockDim.x) {
@@ -280,7 +281,6 @@ __global__ void k_window_op(T *r, const T *s, int n, const unsigned char *mx, co
     else r[id] = in ? s[id] : (T)0;
   }
 }
-inline dim3 real_grid(int n) { return dim3((unsigned)((unsigned long long)n * n)); }
 inline dim3 real_block(int n) { return dim3((unsigned)std::min(256, (n + 31) / 32 * 32)); }
 
 // Hermitian-weighted Re(conj(a) b) over a half spectrum, partial sums per block.
@@ -1043,10 +1043,14 @@ struct ModEngine {
     for (int a = 0; a < 3; ++a) cyclic_cover(win_box, a, &m[(size_t)a * L.n], L.n, 0);
   }
   CellBox win_box;  // cells inside the last window_masks' window
-  void window_op(T *r, const T *src, int l, int op) {
+  // rows: only these rows (x and y ranges of the box) are combined; null: all
+  void window_op(T *r, const T *src, int l, int op, const CellBox *rows = nullptr) {
     int n = lev(l).n;
     unsigned char *m = S.masks.template as<unsigned char>();
-    k_window_op<T><<<real_grid(n), real_block(n), 0, ctx.stream>>>(r, src, n, m, m + n, m + 2 * n, op);
+    const int x0 = rows ? rows->start[0] : 0, nx = rows ? rows->len[0] : n;
+    const int y0 = rows ? rows->start[1] : 0, ny = rows ? rows->len[1] : n;
+    k_window_op<T><<<(unsigned)((size_t)nx * ny), real_block(n), 0, ctx.stream>>>(r, src, n, m, m + n, m + 2 * n, op,
+                                                                                   x0, ny > 0 ? y0 : 0, ny);
     launched();
   }
 
@@ -1162,8 +1166,13 @@ struct ModEngine {
     window_masks(t, t + 1);
     S.win.ensure(elems(t) * sizeof(T));
     T *I = S.win.template as<T>();
-    window_op(I, R, t, 2);  // I = W x: zero outside the window
     const CellBox wb = win_box;
+    // I = W x, zero outside the window.  The box-restricted transform reads the window's
+    // x planes and the row tiles (at most 32 rows) around its y range only, so only those
+    // rows are written (the whole field when the transform is not box-restricted)
+    CellBox rows_wide = wb;
+    rows_wide.set_axis(1, wb.start[1], (long long)wb.start[1] + wb.len[1], 32, lev(t).n);
+    window_op(I, R, t, 2, fft_prunes(ctx, lev(t).n) ? &rows_wide : nullptr);
     to_fourier(I, t, &wb);
     family_table(t, 1);
     to_real_times_table(I, t);
@@ -1172,7 +1181,7 @@ struct ModEngine {
     to_fourier(I, t);
     family_table(t, 1);
     to_real_times_table(I, t, &wb);  // f g is read inside the window only
-    window_op(R, I, t, 1);  // R = W (f g) + (1 - W) g
+    window_op(R, I, t, 1, &wb);  // R = W (f g) + (1 - W) g: the window's rows only
   }
 
   // Transpose of the covector metric (apply_metric(X, out, true)).  The level

@@ -138,6 +138,12 @@ __global__ void __launch_bounds__(256) k_interp_add_sep(FieldPtrs<T, NF> fp, int
 #pragma unroll
     for (int f = 0; f < NF; ++f) P[f * tile + e] = v[f];
   }
+  __shared__ T wys[TY][4];
+  __shared__ int pys[TY];
+  for (int r = threadIdx.x; r <= ylast - y0; r += blockDim.x) {
+    catmull_rom<T>(__ldg(frac + nf + y0 + r), wys[r]);
+    pys[r] = __ldg(ubase + nf + y0 + r) - 1 - cy0;
+  }
   __syncthreads();
   for (int z = threadIdx.x; z < nf; z += blockDim.x) {
     T wz[4];
@@ -156,39 +162,37 @@ __global__ void __launch_bounds__(256) k_interp_add_sep(FieldPtrs<T, NF> fp, int
   }
   __syncthreads();
   const size_t frs = (size_t)(2 * (nf / 2 + 1));
-  // fine cells (y, z) of the block, U per thread at a time: their destination loads are
-  // all issued before the sums (the read-modify-write is otherwise latency-bound)
+  // fine cells: a thread owns z columns and walks the block's rows U at a time, their
+  // destination loads issued before the sums (the read-modify-write is otherwise
+  // latency-bound); the rows' y weights come from shared memory
   constexpr int U = 4;
-  const int cnt = (ylast - y0 + 1) * nf;
-  for (int e0 = threadIdx.x; e0 < cnt; e0 += U * blockDim.x) {
-    T cur[U][NF];
-    size_t dsts[U];
+  const int nrows = ylast - y0 + 1;
+  for (int z = threadIdx.x; z < nf; z += blockDim.x) {
+    for (int r0 = 0; r0 < nrows; r0 += U) {
+      T cur[U][NF];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int e = e0 + u * blockDim.x;
-      const int y = y0 + e / nf, z = e % nf;
-      dsts[u] = ((size_t)x * nf + y) * frs + z;
+      for (int u = 0; u < U; ++u) {
+        const size_t at = ((size_t)x * nf + (y0 + r0 + u)) * frs + z;
 #pragma unroll
-      for (int f = 0; f < NF; ++f) cur[u][f] = (e < cnt && !fp.assign) ? fp.dst[f][dsts[u]] : (T)0;
-    }
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int e = e0 + u * blockDim.x;
-      if (e >= cnt) break;
-      const int y = y0 + e / nf, z = e % nf;
-      T wy[4];
-      catmull_rom<T>(__ldg(frac + nf + y), wy);
-      const int py = __ldg(ubase + nf + y) - 1 - cy0;
-      T s[NF];
-#pragma unroll
-      for (int f = 0; f < NF; ++f) s[f] = 0;
-#pragma unroll
-      for (int b = 0; b < 4; ++b) {
-#pragma unroll
-        for (int f = 0; f < NF; ++f) s[f] += wy[b] * Q[((size_t)f * maxcy + py + b) * nf + z];
+        for (int f = 0; f < NF; ++f) cur[u][f] = (r0 + u < nrows && !fp.assign) ? fp.dst[f][at] : (T)0;
       }
 #pragma unroll
-      for (int f = 0; f < NF; ++f) fp.dst[f][dsts[u]] = fp.assign ? s[f] : cur[u][f] + s[f];
+      for (int u = 0; u < U; ++u) {
+        const int r = r0 + u;
+        if (r >= nrows) break;
+        const int py = pys[r];
+        T s[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) s[f] = 0;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+#pragma unroll
+          for (int f = 0; f < NF; ++f) s[f] += wys[r][b] * Q[((size_t)f * maxcy + py + b) * nf + z];
+        }
+        const size_t at = ((size_t)x * nf + (y0 + r)) * frs + z;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) fp.dst[f][at] = fp.assign ? s[f] : cur[u][f] + s[f];
+      }
     }
   }
 }
