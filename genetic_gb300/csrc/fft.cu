@@ -759,8 +759,9 @@ struct RowsIn {
   }
 };
 
-template <typename T, int L, int TC, int NT, int SIGN>
-__global__ void __launch_bounds__(NT, 1024 / NT) k_fft_cols_fused(typename Cx<T>::type *data, long long B,
+// MINB: CTAs per SM the registers are capped for (1024 / NT: 64 registers)
+template <typename T, int L, int TC, int NT, int SIGN, int MINB = 1024 / NT>
+__global__ void __launch_bounds__(NT, MINB) k_fft_cols_fused(typename Cx<T>::type *data, long long B,
                                                        const typename Cx<T>::type *tw, T scale, const T *tab,
                                                        int a0, int A, int m0, int mn,
                                                        const typename Cx<T>::type *src, typename Cx<T>::type *dst,
@@ -1052,7 +1053,8 @@ void set_smem(const void *fn, size_t bytes) {
 //            FP64 (4, 256) | (8, 256) | fused (4, 256) | fused (8, 128)
 //   rows:    (RPC, threads) = FP32 (8, 256) | (16, 256) | fused (16, 256) | (32, 512),
 //            FP64 (4, 256) | (8, 256) | fused (8, 256) | (16, 512)
-constexpr int kFixedCandidates = 4;
+constexpr int kFixedCandidates = 4;  // row-pass candidates
+constexpr int kColsCandidates = 6;   // strided-pass candidates (the last two: fused, 8 columns, 3 or 4 CTAs per SM)
 
 // the dynamic shared-memory limit of a kernel, set once per device (any host thread)
 inline void set_smem_once(const void *fn, size_t bytes, std::atomic<int> &done_mask) {
@@ -1087,15 +1089,15 @@ struct FixedFft {
                                                                    xtab);
     launched();
   }
-  template <int TC, int NT, int SIGN>
+  template <int TC, int NT, int SIGN, int MINB = 1024 / NT>
   static void cols_fused(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const T *tab, int a0,
                          int na, int m0, int mn, const C *src, C *dst, const C *xsrc, const T *xtab) {
     static std::atomic<int> mask{0};
     const size_t smem = (size_t)N * TC * sizeof(C);
-    set_smem_once((const void *)k_fft_cols_fused<T, N, TC, NT, SIGN>, smem, mask);
+    set_smem_once((const void *)k_fft_cols_fused<T, N, TC, NT, SIGN, MINB>, smem, mask);
     dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)na);
-    k_fft_cols_fused<T, N, TC, NT, SIGN><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A, m0, mn, src, dst,
-                                                                         xsrc, xtab);
+    k_fft_cols_fused<T, N, TC, NT, SIGN, MINB><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A, m0, mn, src,
+                                                                               dst, xsrc, xtab);
     launched();
   }
   // row tiles of RPC rows covering the selection: grid (tiles, planes)
@@ -1144,6 +1146,18 @@ struct FixedFft {
                        const T *tab = nullptr, int a0 = 0, int na = -1, int m0 = 0, int mn = N,
                        const C *src = nullptr, C *dst = nullptr, const C *xsrc = nullptr, const T *xtab = nullptr) {
     if (na < 0) na = A;
+    if (cfg == 4) {
+      // fused, 8 columns, registers capped for 3 CTAs of 512 threads per SM (48 warps)
+      if (sign > 0) cols_fused<F32 ? 8 : 4, 512, +1, 3>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src, dst, xsrc, xtab);
+      else cols_fused<F32 ? 8 : 4, 512, -1, 3>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src, dst, xsrc, xtab);
+      return;
+    }
+    if (cfg == 5) {
+      // fused, 8 columns, registers capped for 4 CTAs of 512 threads per SM (64 warps)
+      if (sign > 0) cols_fused<F32 ? 8 : 4, 512, +1, 4>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src, dst, xsrc, xtab);
+      else cols_fused<F32 ? 8 : 4, 512, -1, 4>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src, dst, xsrc, xtab);
+      return;
+    }
     if (cfg == 2) {
       if (sign > 0) cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, +1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src, dst, xsrc, xtab);
       else cols_fused<F32 ? 8 : 4, F32 ? 512 : 256, -1>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src, dst, xsrc, xtab);
@@ -1257,7 +1271,7 @@ struct FixedFft {
       return ms;
     };
     float bc = 1e30f, br = 1e30f;
-    for (int c = 0; c < kFixedCandidates; ++c) {
+    for (int c = 0; c < kColsCandidates; ++c) {
       float t = time_it([&] { cols_cfg(ctx, c, +1, d, 1, (long long)N * S, tw, (T)1); });
       if (t < bc) { bc = t; best_cols = c; }
     }

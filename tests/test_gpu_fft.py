@@ -51,7 +51,7 @@ def test_fft_passes_bit_identical_across_tiles(built, bbks, precision, n, monkey
     schedule, the twiddles and the rounding of every operation (complex products
     are explicit fused multiply-adds)."""
     out = {}
-    for tile in ('generic', '0,0', '1,1', '2,2', '3,3', '0,2', '2,0', '1,3', '3,3,0', '1,2,1', '0,1,2'):
+    for tile in ('generic', '0,0', '1,1', '2,2', '3,3', '0,2', '2,0', '1,3', '3,3,0', '1,2,1', '0,1,2', '4,1', '5,3'):
         monkeypatch.setenv('GIC_FFT_TILE', tile)
         _, reals, back = _noise_roundtrip(precision, n, bbks)
         out[tile] = (reals, back)
@@ -91,7 +91,7 @@ def test_plane_pass_bit_identical_512(built, bbks, precision, monkeypatch):
     in every lag variant, for 512^3 in both precisions."""
     monkeypatch.setenv('GIC_FFT_TILE', '3,3')
     ref = _roundtrip_raw(precision, 512, bbks, 11)
-    for tile in ('1,0', '3,3,0', '3,3,1', '3,3,2'):
+    for tile in ('1,0', '3,3,0', '3,3,1', '3,3,2', '4,1', '5,1'):
         monkeypatch.setenv('GIC_FFT_TILE', tile)
         raw, back = _roundtrip_raw(precision, 512, bbks, 11)
         assert np.array_equal(raw, ref[0]), tile
