@@ -81,7 +81,8 @@ struct BufPool {
 // scratch of the modification algebra (one user at a time; each buffer is used
 // within a single operation)
 struct ModScratch {
-  DevBuf tab, tabf, conv, masks, tmp_src, win, cells, geom, t1, t2, t3, reduce, compact, csum;
+  DevBuf tab, tabf, conv, masks, tmp_src, win, cells, geom, t1, t2, t3, reduce, compact, csum, fold, btab;
+  int btab_n = 0, btab_r = 0;  // the (N, r) btab holds the block filter of
 };
 
 // One grid level: N^3 cells of a cube of side `box` whose lower corner is x0.

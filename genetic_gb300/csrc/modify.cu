@@ -632,6 +632,76 @@ __global__ void k_subsample_add(const T *fine, int nf, int r, int sx, int sy, in
   coarse[((size_t)X * nc + Y) * (size_t)(2 * (nc / 2 + 1)) + Z] += s;
 }
 
+// Block means of an inverse transform, formed in Fourier space.  With unitary transforms,
+// the mean over the r^3 fine cells of block X of f = IFFT_N(F) is IFFT_{N/r}(G)(X) with
+//   G(K) = r^-1.5 sum_{m in [0,r)^3} F(K + m N/r) b(K_x + m_x N/r) b(..y) b(..z),
+//   b(k) = (1/r) sum_{j<r} exp(+2 pi i k j / N)
+// (a box filter, then decimation: the r^3 aliases of K fold onto it).  F = in * tab[q] on
+// the fine half spectrum, completed by Hermitian symmetry; on the kz = 0 and N/2 planes
+// the conjugate halves are taken from their partners, as the inverse transform's mirror
+// does.  out: the (N/r)^3 half spectrum G.  btab: b(k), k < N.
+template <typename T>
+__global__ void k_fold_block_means(typename V2m<T>::type *out, const typename V2m<T>::type *in, int N, int r,
+                                   const T *tab, const typename V2m<T>::type *btab, T fac) {
+  using C = typename V2m<T>::type;
+  const int nc = N / r, Sc = nc / 2 + 1, H = N / 2, S = H + 1;
+  const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= (size_t)nc * nc * Sc) return;
+  const int KZ = (int)(id % Sc);
+  const size_t rr = id / Sc;
+  const int KY = (int)(rr % nc), KX = (int)(rr / nc);
+  T ar = 0, ai = 0;
+  for (int mx = 0; mx < r; ++mx) {
+    const int kx = KX + mx * nc;
+    const C bx = btab[kx];
+    for (int my = 0; my < r; ++my) {
+      const int ky = KY + my * nc;
+      const C by = btab[ky];
+      // bxy = bx by
+      const T bxy_r = bx.x * by.x - bx.y * by.y, bxy_i = bx.x * by.y + bx.y * by.x;
+      for (int mz = 0; mz < r; ++mz) {
+        const int kz = KZ + mz * nc;
+        C f;
+        if (kz > H) {
+          const C g = in[((size_t)((N - kx) % N) * N + (N - ky) % N) * S + (N - kz)];
+          f.x = g.x;
+          f.y = -g.y;
+        } else if ((kz == 0 || kz == H) && (kx > H || ((kx == 0 || kx == H) && ky > H))) {
+          const C g = in[((size_t)((N - kx) % N) * N + (N - ky) % N) * S + kz];
+          f.x = g.x;
+          f.y = -g.y;
+        } else {
+          f = in[((size_t)kx * N + ky) * S + kz];
+        }
+        const long long sxk = kx > H ? kx - N : kx, syk = ky > H ? ky - N : ky, szk = kz > H ? N - kz : kz;
+        const T t = tab[sxk * sxk + syk * syk + szk * szk];
+        const C bz = btab[kz];
+        const T b_r = bxy_r * bz.x - bxy_i * bz.y, b_i = bxy_r * bz.y + bxy_i * bz.x;
+        const T fr = f.x * t, fi = f.y * t;
+        ar += fr * b_r - fi * b_i;
+        ai += fr * b_i + fi * b_r;
+      }
+    }
+  }
+  C o;
+  o.x = ar * fac;
+  o.y = ai * fac;
+  out[id] = o;
+}
+
+// coarse[(s + X) mod nc] += means[X] for X in [0, m)^3 (means: padded real layout of m^3)
+template <typename T>
+__global__ void k_block_add(const T *means, int m, int sx, int sy, int sz, T *coarse, int nc) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)m * m * m) return;
+  const int k = (int)(i % m);
+  const size_t rr = i / m;
+  const int j = (int)(rr % m), ii = (int)(rr / m);
+  const T v = means[((size_t)ii * m + j) * (size_t)(2 * (m / 2 + 1)) + k];
+  int X = ((sx + ii) % nc + nc) % nc, Y = ((sy + j) % nc + nc) % nc, Z = ((sz + k) % nc + nc) % nc;
+  coarse[((size_t)X * nc + Y) * (size_t)(2 * (nc / 2 + 1)) + Z] += v;
+}
+
 // transpose of k_subsample_add: every fine cell takes its coarse cell's value / r^3
 template <typename T>
 __global__ void k_subsample_transpose(const T *coarse, int nc, int r, int sx, int sy, int sz, T *fine, int nf) {
@@ -1072,6 +1142,50 @@ struct ModEngine {
     return r * r * r;
   }
 
+  // The block means of the finer level s (spectrum source_k times the current table), added
+  // into the coarse real field of level t, formed in Fourier space (k_fold_block_means)
+  // and inverse-transformed on the (n_s/r)^3 grid: one pass over the fine spectrum
+  // instead of its n_s^3 inverse transform.  False when the geometry does not allow it.
+  bool fold_block_means(T *target_real, int t, const T *source_k, int s) {
+    const Level &F = lev(s), &Cl = lev(t);
+    const int r = (int)std::lround(Cl.dx / F.dx);
+    if (r < 2 || F.n % r || (F.n / r) % 2 || F.n / r < 8) return false;
+    const int nc = F.n / r;
+    // b(k) = (1/r) sum_j exp(+2 pi i k j / N), cached per (N, r)
+    if (S.btab_n != F.n || S.btab_r != r) {
+      std::vector<C> hb(F.n);
+      for (int k = 0; k < F.n; ++k) {
+        long double sr = 0, si = 0;
+        for (int j = 0; j < r; ++j) {
+          const long double a = 2.0L * 3.141592653589793238462643383279502884L * (long double)k * j / (long double)F.n;
+          sr += cosl(a);
+          si += sinl(a);
+        }
+        hb[k].x = (T)(sr / r);
+        hb[k].y = (T)(si / r);
+      }
+      S.btab.ensure(F.n * sizeof(C));
+      GIC_CUDA(cudaMemcpyAsync(S.btab.ptr, hb.data(), F.n * sizeof(C), cudaMemcpyHostToDevice, ctx.stream));
+      GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+      S.btab_n = F.n;
+      S.btab_r = r;
+    }
+    const size_t ncomplex = (size_t)nc * nc * (nc / 2 + 1);
+    S.fold.ensure(ncomplex * sizeof(C));
+    C *g = S.fold.template as<C>();
+    k_fold_block_means<T><<<nblk(ncomplex), 256, 0, ctx.stream>>>(g, reinterpret_cast<const C *>(source_k), F.n, r,
+                                                                  tabT(), S.btab.template as<C>(),
+                                                                  (T)std::pow((double)r, -1.5));
+    launched();
+    fft_c2r_3d<T>(ctx, reinterpret_cast<T *>(g), nc, std::pow((double)nc, -1.5));
+    const int sx = (int)std::lround((F.x0[0] - Cl.x0[0]) / Cl.dx), sy = (int)std::lround((F.x0[1] - Cl.x0[1]) / Cl.dx),
+              sz = (int)std::lround((F.x0[2] - Cl.x0[2]) / Cl.dx);
+    const size_t m3 = (size_t)nc * nc * nc;
+    k_block_add<T><<<nblk(m3), 256, 0, ctx.stream>>>(reinterpret_cast<const T *>(g), nc, sx, sy, sz, target_real, Cl.n);
+    launched();
+    return true;
+  }
+
   // assign: a coarser source's interpolation replaces target_real (every cell of the
   // finer level is written) instead of adding to it
   void cross_term_impl(T *target_real, int t, const T *source_k, int s, bool assign = false) {
@@ -1080,8 +1194,9 @@ struct ModEngine {
     add_filter_factors(sp, t);
     add_filter_factors(sp, s);
     sp.scalar = std::sqrt(level_weight(t) / level_weight(s));
-    S.tmp_src.ensure(elems(s) * sizeof(T));
     table(sp, s);
+    if (s > t && fold_block_means(target_real, t, source_k, s)) return;
+    S.tmp_src.ensure(elems(s) * sizeof(T));
     // source (Fourier, unchanged) times the table, to real space in tmp_src; the
     // interpolation up reads the coarse cells around the fine level only
     const CellBox fp = footprint(t, s, 3);
