@@ -65,39 +65,55 @@ __device__ __forceinline__ double wrap_fast(double x, double period, long long p
 }
 
 // LPT2: second-order displacements q2 are added, pos = q + psi + psi2 and
-// vel = ratio (psi + 2 psi2) (f2 = 2 with genetIC's f = 1)
+// vel = ratio (psi + 2 psi2) (f2 = 2 with genetIC's f = 1).
+// A CTA per row (x, y) of n cells, 256 of them at a time: each thread evaluates one
+// particle into shared memory, then the CTA writes the 256 particles' positions and
+// velocities as contiguous runs (3 components per particle, interleaved).
 template <typename T, bool LPT2>
 __global__ void __launch_bounds__(256) k_particles(const T *__restrict__ px, const T *__restrict__ py,
                                                    const T *__restrict__ pz, const T *__restrict__ qx,
                                                    const T *__restrict__ qy, const T *__restrict__ qz, int n,
                                                    const double *__restrict__ cen, double period, T ratio,
                                                    double *pos, T *vel) {
-  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  size_t m = (size_t)n * n * n;
-  if (i >= m) return;
-  size_t row = i / n;
-  int z = (int)(i % n);
-  int y = (int)(row % n);
-  int x = (int)(row / n);
-  size_t src = row * (size_t)(2 * (n / 2 + 1)) + z;
-  T sx = px[src], sy = py[src], sz = pz[src];
-  if (LPT2) {
-    T tx = qx[src], ty = qy[src], tz = qz[src];
-    vel[3 * i + 0] = (sx + 2 * tx) * ratio;
-    vel[3 * i + 1] = (sy + 2 * ty) * ratio;
-    vel[3 * i + 2] = (sz + 2 * tz) * ratio;
-    sx += tx;
-    sy += ty;
-    sz += tz;
-  } else {
-    vel[3 * i + 0] = sx * ratio;
-    vel[3 * i + 1] = sy * ratio;
-    vel[3 * i + 2] = sz * ratio;
+  __shared__ double sp[3 * 256];
+  __shared__ T sv[3 * 256];
+  const unsigned row = blockIdx.x;
+  const int x = (int)(row / (unsigned)n), y = (int)(row - (unsigned)x * (unsigned)n);
+  const size_t src_row = (size_t)row * (size_t)(2 * (n / 2 + 1));
+  const double cx = __ldg(cen + x), cy = __ldg(cen + n + y);
+  const long long pb = __double_as_longlong(period);
+  const int t = threadIdx.x;
+  for (int z0 = 0; z0 < n; z0 += 256) {
+    const int z = z0 + t;
+    if (z < n) {
+      const size_t src = src_row + z;
+      T sx = px[src], sy = py[src], sz = pz[src];
+      if (LPT2) {
+        T tx = qx[src], ty = qy[src], tz = qz[src];
+        sv[3 * t + 0] = (sx + 2 * tx) * ratio;
+        sv[3 * t + 1] = (sy + 2 * ty) * ratio;
+        sv[3 * t + 2] = (sz + 2 * tz) * ratio;
+        sx += tx;
+        sy += ty;
+        sz += tz;
+      } else {
+        sv[3 * t + 0] = sx * ratio;
+        sv[3 * t + 1] = sy * ratio;
+        sv[3 * t + 2] = sz * ratio;
+      }
+      sp[3 * t + 0] = wrap_fast(to_double(sx) + cx, period, pb);
+      sp[3 * t + 1] = wrap_fast(to_double(sy) + cy, period, pb);
+      sp[3 * t + 2] = wrap_fast(to_double(sz) + __ldg(cen + 2 * n + z), period, pb);
+    }
+    __syncthreads();
+    const size_t o = 3 * ((size_t)row * n + z0);
+    const int cnt = 3 * min(256, n - z0);
+    for (int e = t; e < cnt; e += 256) {
+      pos[o + e] = sp[e];
+      vel[o + e] = sv[e];
+    }
+    __syncthreads();
   }
-  long long pb = __double_as_longlong(period);
-  pos[3 * i + 0] = wrap_fast(to_double(sx) + __ldg(cen + x), period, pb);
-  pos[3 * i + 1] = wrap_fast(to_double(sy) + __ldg(cen + n + y), period, pb);
-  pos[3 * i + 2] = wrap_fast(to_double(sz) + __ldg(cen + 2 * n + z), period, pb);
 }
 
 }  // namespace
@@ -116,7 +132,7 @@ static void particles_typed(Context &ctx, Level &L, int order) {
   ctx.geom.ensure(3 * (size_t)L.n * sizeof(double));
   double *cen = ctx.geom.as<double>();
   k_centroids<<<(3 * L.n + 127) / 128, 128, 0, ctx.stream>>>(L.n, L.dx, L.x0[0], L.x0[1], L.x0[2], cen);
-  const unsigned grid = (unsigned)((m + 255) / 256);
+  const unsigned grid = (unsigned)((size_t)L.n * L.n);  // a CTA per row of cells
   if (order == 2)
     k_particles<T, true><<<grid, 256, 0, ctx.stream>>>(L.field[1].as<T>(), L.field[2].as<T>(), L.field[3].as<T>(),
                                                        L.field2[0].as<T>(), L.field2[1].as<T>(), L.field2[2].as<T>(),
