@@ -759,8 +759,10 @@ struct RowsIn {
   }
 };
 
-// MINB: CTAs per SM the registers are capped for (1024 / NT: 64 registers)
-template <typename T, int L, int TC, int NT, int SIGN, int MINB = 1024 / NT>
+// MINB: CTAs per SM the registers are capped for (1024 / NT: 64 registers).  EXT: the
+// out-of-place source, position windows and epilogue are compiled in (a plain pass
+// without them keeps fewer registers)
+template <typename T, int L, int TC, int NT, int SIGN, int MINB = 1024 / NT, bool EXT = true>
 __global__ void __launch_bounds__(NT, MINB) k_fft_cols_fused(typename Cx<T>::type *data, long long B,
                                                        const typename Cx<T>::type *tw, T scale, const T *tab,
                                                        int a0, int A, int m0, int mn,
@@ -773,15 +775,17 @@ __global__ void __launch_bounds__(NT, MINB) k_fft_cols_fused(typename Cx<T>::typ
   C *base = data + (size_t)((a0 + (int)blockIdx.y) % A) * (size_t)L * (size_t)B + b0;
   const int tcv = (int)min((long long)TC, B - b0);
   // the window limits the loads of a forward pass and the stores of an inverse one
-  const int lm0 = SIGN < 0 ? m0 : 0, lmn = SIGN < 0 ? mn : L, sm0 = SIGN > 0 ? m0 : 0, smn = SIGN > 0 ? mn : L;
-  const C *alt = src ? src + (base - data) : nullptr;
+  const int lm0 = EXT && SIGN < 0 ? m0 : 0, lmn = EXT && SIGN < 0 ? mn : (1 << 30);
+  const int sm0 = EXT && SIGN > 0 ? m0 : 0, smn = EXT && SIGN > 0 ? mn : (1 << 30);
+  const C *alt = EXT && src ? src + (base - data) : nullptr;
   first_stage_from<T, L, TC, NT, SIGN>(tile, ColsIn<C>{base, B, tcv, SIGN > 0 ? tab : nullptr, L, b0, lm0, lmn, alt});
   constexpr int R0 = next_radix(L, 1), NSL = last_stage_ns(L);
   TileStagesUntil<T, L, TC, TC, NT, R0, NSL, SIGN, 1>::run(tile, tw);
   const size_t off = (size_t)(base - data);
   last_stage_to<T, L, TC, NT, SIGN, 1>(tile, tw,
                                        ColsOut<C, T>{base, B, tcv, scale, SIGN < 0 ? tab : nullptr, L, b0, sm0, smn,
-                                                     dst ? dst + off : nullptr, xsrc ? xsrc + off : nullptr, xtab});
+                                                     EXT && dst ? dst + off : nullptr, EXT && xsrc ? xsrc + off : nullptr,
+                                                     xtab});
 }
 
 template <typename T, int H, int RPC, int NT>
@@ -1092,12 +1096,18 @@ struct FixedFft {
   template <int TC, int NT, int SIGN, int MINB = 1024 / NT>
   static void cols_fused(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const T *tab, int a0,
                          int na, int m0, int mn, const C *src, C *dst, const C *xsrc, const T *xtab) {
-    static std::atomic<int> mask{0};
+    static std::atomic<int> mask{0}, mask_plain{0};
     const size_t smem = (size_t)N * TC * sizeof(C);
-    set_smem_once((const void *)k_fft_cols_fused<T, N, TC, NT, SIGN, MINB>, smem, mask);
     dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)na);
-    k_fft_cols_fused<T, N, TC, NT, SIGN, MINB><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A, m0, mn, src,
-                                                                               dst, xsrc, xtab);
+    if (src || dst || m0 != 0 || mn < N) {
+      set_smem_once((const void *)k_fft_cols_fused<T, N, TC, NT, SIGN, MINB, true>, smem, mask);
+      k_fft_cols_fused<T, N, TC, NT, SIGN, MINB, true><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A, m0, mn,
+                                                                                       src, dst, xsrc, xtab);
+    } else {
+      set_smem_once((const void *)k_fft_cols_fused<T, N, TC, NT, SIGN, MINB, false>, smem, mask_plain);
+      k_fft_cols_fused<T, N, TC, NT, SIGN, MINB, false><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A, m0,
+                                                                                        mn, src, dst, xsrc, xtab);
+    }
     launched();
   }
   // row tiles of RPC rows covering the selection: grid (tiles, planes)
