@@ -80,9 +80,12 @@ struct BufPool {
 
 // scratch of the modification algebra (one user at a time; each buffer is used
 // within a single operation)
+struct GeomEntry;
 struct ModScratch {
   DevBuf tab, tabf, conv, masks, tmp_src, win, cells, geom, t1, t2, t3, reduce, compact, csum, fold, btab;
   int btab_n = 0, btab_r = 0;  // the (N, r) btab holds the block filter of
+  std::vector<std::unique_ptr<GeomEntry>> geom_cache;
+  const unsigned char *cur_masks = nullptr;  // the masks of the last window setup (in geom_cache)
 };
 
 // One grid level: N^3 cells of a cube of side `box` whose lower corner is x0.
@@ -187,6 +190,13 @@ struct CellBox {
   }
 };
 // a linear modification awaiting application (kind 0 overdensity, 1-3 velocity x,y,z)
+// geometry derived from the levels alone (window masks, deinterpolation axes), kept per key
+struct GeomEntry {
+  std::vector<double> key;
+  DevBuf dev;
+  std::vector<int> host;
+  CellBox box;
+};
 struct ModRequest {
   int kind;
   std::vector<unsigned long long> cells;  // flagged cells of the finest level

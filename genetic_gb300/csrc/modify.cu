@@ -1089,8 +1089,33 @@ struct ModEngine {
   }
 
   // window of level wl on the cells of level l, per axis (window.hpp)
+  // the cached geometry entry of `key` (created empty when new)
+  GeomEntry &geom_entry(const std::vector<double> &key, bool &fresh) {
+    for (auto &e : S.geom_cache)
+      if (e->key == key) {
+        fresh = false;
+        return *e;
+      }
+    if (S.geom_cache.size() >= 64)  // keep the masks in use; cudaFree orders after pending work
+      for (size_t i = S.geom_cache.size(); i-- > 0;)
+        if (S.geom_cache[i]->dev.ptr != (const void *)S.cur_masks) S.geom_cache.erase(S.geom_cache.begin() + i);
+    S.geom_cache.push_back(std::make_unique<GeomEntry>());
+    S.geom_cache.back()->key = key;
+    fresh = true;
+    return *S.geom_cache.back();
+  }
+
   void window_masks(int l, int wl) {
     const Level &L = lev(l), &W = lev(wl);
+    bool fresh = false;
+    GeomEntry &g = geom_entry({1.0, (double)l, (double)wl, (double)L.n, L.dx, L.x0[0], L.x0[1], L.x0[2], L.periodic,
+                               W.box, W.x0[0], W.x0[1], W.x0[2]},
+                              fresh);
+    if (!fresh) {
+      S.cur_masks = g.dev.template as<unsigned char>();
+      win_box = g.box;
+      return;
+    }
     double P = L.periodic;
     std::vector<unsigned char> m(3 * (size_t)L.n);
     for (int a = 0; a < 3; ++a) {
@@ -1106,17 +1131,19 @@ struct ModEngine {
         m[(size_t)a * L.n + i] = in ? 1 : 0;
       }
     }
-    S.masks.ensure(m.size());
-    GIC_CUDA(cudaMemcpyAsync(S.masks.ptr, m.data(), m.size(), cudaMemcpyHostToDevice, ctx.stream));
+    g.dev.ensure(m.size());
+    GIC_CUDA(cudaMemcpyAsync(g.dev.ptr, m.data(), m.size(), cudaMemcpyHostToDevice, ctx.stream));
     GIC_CUDA(cudaStreamSynchronize(ctx.stream));
-    win_box = CellBox::whole(L.n);
-    for (int a = 0; a < 3; ++a) cyclic_cover(win_box, a, &m[(size_t)a * L.n], L.n, 0);
+    g.box = CellBox::whole(L.n);
+    for (int a = 0; a < 3; ++a) cyclic_cover(g.box, a, &m[(size_t)a * L.n], L.n, 0);
+    S.cur_masks = g.dev.template as<unsigned char>();
+    win_box = g.box;
   }
   CellBox win_box;  // cells inside the last window_masks' window
   // rows: only these rows (x and y ranges of the box) are combined; null: all
   void window_op(T *r, const T *src, int l, int op, const CellBox *rows = nullptr) {
     int n = lev(l).n;
-    unsigned char *m = S.masks.template as<unsigned char>();
+    const unsigned char *m = S.cur_masks;
     const int x0 = rows ? rows->start[0] : 0, nx = rows ? rows->len[0] : n;
     const int y0 = rows ? rows->start[1] : 0, ny = rows ? rows->len[1] : n;
     k_window_op<T><<<(unsigned)((size_t)nx * ny), real_block(n), 0, ctx.stream>>>(r, src, n, m, m + n, m + 2 * n, op,
@@ -1927,15 +1954,25 @@ struct ModEngine {
     int nf = Fl.n;
     int r = (int)std::lround(Cl.dx / Fl.dx);
     T scale = unit_scale ? (T)1 : (T)(1.0 / ((double)r * r * r));
-    S.geom.ensure(3 * (size_t)nf * (sizeof(int) + sizeof(T)));
-    int *ub = S.geom.template as<int>();
+    // the per-axis stencil geometry of this pair of levels, computed once
+    bool fresh = false;
+    GeomEntry &ge = geom_entry({2.0, (double)f, (double)c, (double)nf, Fl.dx, Fl.x0[0], Fl.x0[1], Fl.x0[2], Cl.x0[0],
+                                Cl.x0[1], Cl.x0[2], Cl.dx, Cl.periodic, (double)Cl.n, (double)sizeof(T)},
+                               fresh);
+    if (fresh) {
+      ge.dev.ensure(3 * (size_t)nf * (sizeof(int) + sizeof(T)));
+      int *ub0 = ge.dev.template as<int>();
+      k_axes_geom<T><<<nblk(3 * nf, 128), 128, 0, ctx.stream>>>(nf, Fl.dx, Fl.x0[0], Fl.x0[1], Fl.x0[2], Cl.x0[0], Cl.x0[1],
+                                                                Cl.x0[2], Cl.dx, Cl.periodic, Cl.n, ub0,
+                                                                reinterpret_cast<T *>(ub0 + 3 * nf));
+      launched();
+      ge.host.resize(3 * nf);
+      GIC_CUDA(cudaMemcpyAsync(ge.host.data(), ub0, 3 * nf * sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
+      GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+    }
+    int *ub = ge.dev.template as<int>();
     T *fr = reinterpret_cast<T *>(ub + 3 * nf);
-    k_axes_geom<T><<<nblk(3 * nf, 128), 128, 0, ctx.stream>>>(nf, Fl.dx, Fl.x0[0], Fl.x0[1], Fl.x0[2], Cl.x0[0],
-                                                              Cl.x0[1], Cl.x0[2], Cl.dx, Cl.periodic, Cl.n, ub, fr);
-    launched();
-    std::vector<int> h(3 * nf);
-    GIC_CUDA(cudaMemcpyAsync(h.data(), ub, 3 * nf * sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
-    GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+    const std::vector<int> &h = ge.host;
     // fine ranges [f0, f0 + fn) per axis, and the coarse block they reach
     int f0[3], fn[3], c0[3], cnt[3];
     for (int a = 0; a < 3; ++a) {
