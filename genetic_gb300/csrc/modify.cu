@@ -46,6 +46,7 @@ struct TableSpec {
   const double *sqrtp;
   double vel;
   double var_cut;  // > 0: times 1 - LP(k; var_cut), the variance high-pass
+  double offset;   // added last
 };
 
 __device__ __forceinline__ double fermi_lp(double k, double kcut) {
@@ -69,6 +70,7 @@ __global__ void k_mod_table(double *out, float *outf, long long nq, TableSpec sp
   f *= sp.scalar;
   if (sp.sqrtp) f *= sp.sqrtp[q];
   if (sp.vel != 0.0) f = q == 0 ? 0.0 : -sp.vel * f / (k * k);
+  f += sp.offset;
   out[q] = f;
   if (outf) outf[q] = (float)f;
 }
@@ -346,6 +348,31 @@ __global__ void k_inner_real(const T *a, const T *b, int n, double *partial) {
   double acc = 0;
   for (int z = threadIdx.x; z < n; z += kKzChunk)
     acc += thread_dot_col(a, b, rows, rs, z, blockIdx.x * kRowsPerBlock + threadIdx.y, gridDim.x * kRowsPerBlock);
+  red[tid] = acc;
+  __syncthreads();
+  for (int s2 = 128; s2 > 0; s2 >>= 1) {
+    if (tid < s2) red[tid] += red[tid + s2];
+    __syncthreads();
+  }
+  if (tid == 0) partial[blockIdx.x] = red[0];
+}
+
+// sum over the cells of a box (cyclic ranges per axis) of two padded real fields
+template <typename T>
+__global__ void k_inner_real_box(const T *a, const T *b, int n, CellBox box, double *partial) {
+  __shared__ double red[256];
+  const size_t rs = (size_t)(2 * (n / 2 + 1));
+  const int tid = threadIdx.y * kKzChunk + threadIdx.x;
+  const unsigned ny = (unsigned)box.len[1], rows = (unsigned)box.len[0] * ny;
+  double acc = 0;
+  for (unsigned r = blockIdx.x * kRowsPerBlock + threadIdx.y; r < rows; r += gridDim.x * kRowsPerBlock) {
+    const int x = (box.start[0] + (int)(r / ny)) % n, y = (box.start[1] + (int)(r % ny)) % n;
+    const size_t base = ((size_t)x * (size_t)n + (size_t)y) * rs;
+    for (int j = threadIdx.x; j < box.len[2]; j += kKzChunk) {
+      const size_t id = base + (size_t)((box.start[2] + j) % n);
+      acc += (double)a[id] * (double)b[id];
+    }
+  }
   red[tid] = acc;
   __syncthreads();
   for (int s2 = 128; s2 > 0; s2 >>= 1) {
@@ -925,6 +952,7 @@ struct ModEngine {
     put(&sp.sqrtp, sizeof(sp.sqrtp));
     put(&sp.vel, sizeof(double));
     put(&sp.var_cut, sizeof(double));
+    put(&sp.offset, sizeof(double));
     for (auto &e : ctx.table_cache)
       if (e->key == key) {
         cur_tab = e.get();
@@ -963,12 +991,14 @@ struct ModEngine {
 
   // one term of an inner product: two half spectra or two padded real fields of level
   // l, or two flat arrays of `count` values
-  enum TermKind { kFourier = 0, kReal = 1, kFlat = 2 };
+  // kRealBox: two padded real fields of level l over the cells of `box` only
+  enum TermKind { kFourier = 0, kReal = 1, kFlat = 2, kRealBox = 3 };
   struct Term {
     const T *a, *b;
     int l;
     int kind;
     size_t count = 0;
+    CellBox box{};
   };
   // sum of each group's terms; every group has the same number of terms, and all
   // groups are read back together
@@ -987,6 +1017,8 @@ struct ModEngine {
           k_inner_real<T><<<blocks, red_block(), 0, ctx.stream>>>(t.a, t.b, lev(t.l).n, dst);
         else if (t.kind == kFlat)
           k_dot_flat<T><<<blocks, 256, 0, ctx.stream>>>(t.a, t.b, t.count, dst);
+        else if (t.kind == kRealBox)
+          k_inner_real_box<T><<<blocks, red_block(), 0, ctx.stream>>>(t.a, t.b, lev(t.l).n, t.box, dst);
         else
           k_inner<T><<<blocks, red_block(), 0, ctx.stream>>>(t.a, t.b, lev(t.l).n, dst);
         launched();
@@ -1389,13 +1421,48 @@ struct ModEngine {
     for (int t = 0; t < nl(); ++t) {
       const size_t bytes = elems(t) * sizeof(T);
       if (t < nl() - 1) {
-        auto R = ctx.pool.take(bytes), xr = ctx.pool.take(bytes);
-        fft_c2r_3d_from<T>(ctx, R->template as<T>(), ptr(X, t), lev(t).n, scale(t));
-        GIC_CUDA(cudaMemcpyAsync(xr->ptr, R->ptr, bytes, cudaMemcpyDeviceToDevice, ctx.stream));
-        windowed_covector_real(X, t, R->template as<T>());
-        terms.push_back({R->template as<T>(), xr->template as<T>(), t, kReal});
-        keep.push_back(std::move(R));
+        // The level's own covector part is P1^T P1 x with P1 = f W + (1 - W)
+        // (windowed_self_real), so its term <P1^T P1 x|x> is |P1 x|^2, and
+        // P1 x = x + (f - 1) W x is X + (f - 1) FFT(W x) in Fourier space: formed by
+        // the forward transform's last pass.  The cross terms add <cross|x> in real
+        // space.  x is then needed inside the window and where the cross terms land
+        // only: on the coarsest level (no coarser source) that is the next level's
+        // footprint, and the transforms are box-restricted to it.
+        const int n = lev(t).n;
+        const bool prune = fft_prunes(ctx, n);
+        const bool in_box = prune && t == 0;
+        const CellBox B = in_box ? footprint(t + 1, t, 1) : CellBox::whole(n);
+        auto xr = ctx.pool.take(bytes), G = ctx.pool.take(bytes), Cr = ctx.pool.take(bytes);
+        T *x = xr->template as<T>(), *g = G->template as<T>(), *cr = Cr->template as<T>();
+        fft_c2r_3d_from<T>(ctx, x, ptr(X, t), n, scale(t), nullptr, in_box ? &B : nullptr);
+        window_masks(t, t + 1);
+        const CellBox wb = win_box;
+        CellBox rows_wide = wb;
+        rows_wide.set_axis(1, wb.start[1], (long long)wb.start[1] + wb.len[1], 32, n);
+        S.win.ensure(bytes);
+        T *I = S.win.template as<T>();
+        window_op(I, x, t, 2, prune ? &rows_wide : nullptr);  // I = W x
+        TableSpec one{}, fm{};
+        one.power = fm.power = 1;
+        one.scalar = fm.scalar = 1.0;
+        add_filter_factors(fm, t);
+        fm.offset = -1.0;
+        // a lookup that finds its table builds nothing and evicts nothing: both stay valid
+        table(one, t);
+        table(fm, t);
+        const T *tab_fm = tabT();
+        table(one, t);
+        const T *tab_one = tabT();
+        fft_r2c_3d_add<T>(ctx, I, n, scale(t), tab_fm, &wb, g, ptr(X, t), tab_one);
+        terms.push_back({g, g, t, kFourier});
+        if (in_box) zero_planes(cr, t, B);
+        else GIC_CUDA(cudaMemsetAsync(cr, 0, bytes, ctx.stream));
+        for (int s = 0; s < nl(); ++s)
+          if (s != t) cross_term_impl(cr, t, ptr(X, s), s);
+        terms.push_back({cr, x, t, in_box ? kRealBox : kReal, 0, B});
         keep.push_back(std::move(xr));
+        keep.push_back(std::move(G));
+        keep.push_back(std::move(Cr));
       } else {
         auto R = ctx.pool.take(bytes);
         T *r = R->template as<T>();
