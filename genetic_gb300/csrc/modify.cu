@@ -250,6 +250,90 @@ __global__ void __launch_bounds__(256, 3) k_inner_block(BlockFields<T> f, int n,
     }
 }
 
+// The same products for a full NA x NB block, walking the half spectra as one flat
+// array of 16-byte vectors (two float or one double coefficient): every coefficient
+// summed with weight 1, and the kz = 0 and kz = N/2 planes (weight 1 in the Hermitian
+// sum, 2 elsewhere) counted again with weight -1/2, so twice the sum is the weighted one.
+// Each thread sums four vectors in the field's precision, then into its compensated
+// shared-memory accumulators.
+__device__ __forceinline__ float vdot(const float4 &a, const float4 &b) {
+  return fmaf(a.x, b.x, fmaf(a.y, b.y, fmaf(a.z, b.z, a.w * b.w)));
+}
+__device__ __forceinline__ double vdot(const double2 &a, const double2 &b) { return a.x * b.x + a.y * b.y; }
+
+template <typename T, int NA, int NB>
+__global__ void __launch_bounds__(256, 2) k_inner_block_flat(BlockFields<T> f, int n, double *partial, int ia0,
+                                                          int jb0, int nb_total, size_t pstride) {
+  using V = typename Vec16<T>::type;
+  __shared__ double red[256];
+  __shared__ RowAcc<T> acc[NA * NB][256];
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int p = 0; p < NA * NB; ++p) acc[p][tid].zero();
+  const int H = n / 2, S = H + 1;
+  // n is even, so n^2 (n/2 + 1) coefficients fill whole vectors
+  const size_t nv = (size_t)n * n * S * 2 / Vec16<T>::W;
+  const size_t step = (size_t)gridDim.x * blockDim.x;
+  size_t q = (size_t)blockIdx.x * blockDim.x + tid;
+  while (q < nv) {
+    T part[NA * NB];
+#pragma unroll
+    for (int p = 0; p < NA * NB; ++p) part[p] = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (q < nv) {
+        V b[NB];
+#pragma unroll
+        for (int j = 0; j < NB; ++j) b[j] = __ldg(reinterpret_cast<const V *>(f.b[j]) + q);
+#pragma unroll
+        for (int i = 0; i < NA; ++i) {
+          const V a = __ldg(reinterpret_cast<const V *>(f.a[i]) + q);
+#pragma unroll
+          for (int j = 0; j < NB; ++j) part[i * NB + j] += vdot(a, b[j]);
+        }
+      }
+      q += step;
+    }
+#pragma unroll
+    for (int p = 0; p < NA * NB; ++p) acc[p][tid].add(part[p]);
+  }
+  // the kz = 0 and kz = N/2 planes once more, weight -1/2
+  const unsigned rows = (unsigned)n * (unsigned)n;
+  for (unsigned r = blockIdx.x * blockDim.x + tid; r < rows; r += (unsigned)step) {
+    T part[NA * NB];
+#pragma unroll
+    for (int p = 0; p < NA * NB; ++p) part[p] = 0;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const size_t id = 2 * ((size_t)r * S + (h ? H : 0));
+      T br[NB], bi[NB];
+#pragma unroll
+      for (int j = 0; j < NB; ++j) {
+        br[j] = f.b[j][id];
+        bi[j] = f.b[j][id + 1];
+      }
+#pragma unroll
+      for (int i = 0; i < NA; ++i) {
+        const T ar = f.a[i][id], ai = f.a[i][id + 1];
+#pragma unroll
+        for (int j = 0; j < NB; ++j) part[i * NB + j] += ar * br[j] + ai * bi[j];
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < NA * NB; ++p) acc[p][tid].add((T)-0.5 * part[p]);
+  }
+  for (int p = 0; p < NA * NB; ++p) {
+    red[tid] = 2.0 * acc[p][tid].get();
+    __syncthreads();
+    for (int s2 = 128; s2 > 0; s2 >>= 1) {
+      if (tid < s2) red[tid] += red[tid + s2];
+      __syncthreads();
+    }
+    if (tid == 0) partial[(size_t)((ia0 + p / NB) * nb_total + jb0 + p % NB) * pstride + blockIdx.x] = red[0];
+    __syncthreads();
+  }
+}
+
 // --- elementwise ----------------------------------------------------------------
 
 template <typename T>
@@ -1056,14 +1140,23 @@ struct ModEngine {
       GIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_inner_block<T>, kKzChunk * kRowsPerBlock, 0));
       per_sm.store(std::max(nb, 1));
     }
+    static std::atomic<int> per_sm_flat{0};
+    if (per_sm_flat.load() == 0) {
+      int nb = 0;
+      GIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_inner_block_flat<T, kBlockA, kBlockB>, 256, 0));
+      per_sm_flat.store(std::max(nb, 1));
+    }
     int nsm = 0;
     GIC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx.device));
-    const int blocks = per_sm.load() * nsm;
+    const int nb_row = per_sm.load() * nsm, blocks_flat = per_sm_flat.load() * nsm;
+    const int blocks = std::max(nb_row, blocks_flat);
     const int L = nl(), na = (int)A.size(), nbt = (int)B.size(), np = na * nbt;
     if (np == 0) return {};
     const size_t pstride = (size_t)L * blocks;
     S.reduce.ensure((pstride * np + np) * sizeof(double));
     double *part = S.reduce.template as<double>();
+    // each product has `blocks` slots per level; a kernel with fewer CTAs leaves zeros
+    if (nb_row != blocks_flat) GIC_CUDA(cudaMemsetAsync(part, 0, pstride * np * sizeof(double), ctx.stream));
     for (Field *f : A)
       for (int l = 0; l < L; ++l) to_fourier(*f, l);
     for (Field *f : B)
@@ -1074,10 +1167,23 @@ struct ModEngine {
           BlockFields<T> bf{};
           bf.na = std::min(kBlockA, na - ia);
           bf.nb = std::min(kBlockB, nbt - jb);
-          for (int i = 0; i < bf.na; ++i) bf.a[i] = ptr(*A[ia + i], l);
-          for (int j = 0; j < bf.nb; ++j) bf.b[j] = ptr(*B[jb + j], l);
-          k_inner_block<T><<<blocks, red_block(), 0, ctx.stream>>>(bf, lev(l).n, part + (size_t)l * blocks, ia, jb,
-                                                                   nbt, pstride);
+          bool aligned = true;
+          for (int i = 0; i < bf.na; ++i) {
+            bf.a[i] = ptr(*A[ia + i], l);
+            aligned = aligned && (reinterpret_cast<uintptr_t>(bf.a[i]) % 16 == 0);
+          }
+          for (int j = 0; j < bf.nb; ++j) {
+            bf.b[j] = ptr(*B[jb + j], l);
+            aligned = aligned && (reinterpret_cast<uintptr_t>(bf.b[j]) % 16 == 0);
+          }
+          // slots [l blocks, (l + 1) blocks) of each product; unused ones are zeroed
+          double *slot = part + (size_t)l * blocks;
+          if (aligned && bf.na == kBlockA && bf.nb == kBlockB) {
+            k_inner_block_flat<T, kBlockA, kBlockB><<<blocks_flat, 256, 0, ctx.stream>>>(bf, lev(l).n, slot, ia, jb, nbt,
+                                                                                        pstride);
+          } else {
+            k_inner_block<T><<<nb_row, red_block(), 0, ctx.stream>>>(bf, lev(l).n, slot, ia, jb, nbt, pstride);
+          }
           launched();
         }
     k_sum<<<np, 256, 0, ctx.stream>>>(part, (int)pstride, part + pstride * np);
