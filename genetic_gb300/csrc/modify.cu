@@ -751,10 +751,13 @@ __global__ void k_subsample_add(const T *fine, int nf, int r, int sx, int sy, in
 // the fine half spectrum, completed by Hermitian symmetry; on the kz = 0 and N/2 planes
 // the conjugate halves are taken from their partners, as the inverse transform's mirror
 // does.  out: the (N/r)^3 half spectrum G.  btab: b(k), k < N.
-template <typename T>
-__global__ void k_fold_block_means(typename V2m<T>::type *out, const typename V2m<T>::type *in, int N, int r,
+// R > 0: the ratio r known at compile time; each (kx, ky) column's R coefficients are
+// loaded together before their sums (which run in the same order)
+template <typename T, int R>
+__global__ void k_fold_block_means(typename V2m<T>::type *out, const typename V2m<T>::type *in, int N, int r_rt,
                                    const T *tab, const typename V2m<T>::type *btab, T fac) {
   using C = typename V2m<T>::type;
+  const int r = R > 0 ? R : r_rt;
   const int nc = N / r, Sc = nc / 2 + 1, H = N / 2, S = H + 1;
   const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= (size_t)nc * nc * Sc) return;
@@ -770,6 +773,30 @@ __global__ void k_fold_block_means(typename V2m<T>::type *out, const typename V2
       const C by = btab[ky];
       // bxy = bx by
       const T bxy_r = bx.x * by.x - bx.y * by.y, bxy_i = bx.x * by.y + bx.y * by.x;
+      if constexpr (R > 0) {
+        C f[R];
+        T t[R];
+#pragma unroll
+        for (int mz = 0; mz < R; ++mz) {
+          const int kz = KZ + mz * nc;
+          // the stored coefficient, or the conjugate of its Hermitian partner
+          const bool mir = kz > H || ((kz == 0 || kz == H) && (kx > H || ((kx == 0 || kx == H) && ky > H)));
+          const int qx = mir ? (N - kx) % N : kx, qy = mir ? (N - ky) % N : ky, qz = kz > H ? N - kz : kz;
+          f[mz] = in[((size_t)qx * N + qy) * S + qz];
+          if (mir) f[mz].y = -f[mz].y;
+          const long long sxk = kx > H ? kx - N : kx, syk = ky > H ? ky - N : ky;
+          t[mz] = tab[sxk * sxk + syk * syk + (long long)qz * qz];
+        }
+#pragma unroll
+        for (int mz = 0; mz < R; ++mz) {
+          const C bz = btab[KZ + mz * nc];
+          const T b_r = bxy_r * bz.x - bxy_i * bz.y, b_i = bxy_r * bz.y + bxy_i * bz.x;
+          const T fr = f[mz].x * t[mz], fi = f[mz].y * t[mz];
+          ar += fr * b_r - fi * b_i;
+          ai += fr * b_i + fi * b_r;
+        }
+        continue;
+      }
       for (int mz = 0; mz < r; ++mz) {
         const int kz = KZ + mz * nc;
         C f;
@@ -1103,7 +1130,13 @@ struct ModEngine {
           k_dot_flat<T><<<blocks, 256, 0, ctx.stream>>>(t.a, t.b, t.count, dst);
         else if (t.kind == kRealBox)
           k_inner_real_box<T><<<blocks, red_block(), 0, ctx.stream>>>(t.a, t.b, lev(t.l).n, t.box, dst);
-        else
+        else if (reinterpret_cast<uintptr_t>(t.a) % 16 == 0 && reinterpret_cast<uintptr_t>(t.b) % 16 == 0) {
+          BlockFields<T> bf{};
+          bf.a[0] = t.a;
+          bf.b[0] = t.b;
+          bf.na = bf.nb = 1;
+          k_inner_block_flat<T, 1, 1><<<blocks, 256, 0, ctx.stream>>>(bf, lev(t.l).n, dst, 0, 0, 1, 0);
+        } else
           k_inner<T><<<blocks, red_block(), 0, ctx.stream>>>(t.a, t.b, lev(t.l).n, dst);
         launched();
       }
@@ -1338,9 +1371,13 @@ struct ModEngine {
     const size_t ncomplex = (size_t)nc * nc * (nc / 2 + 1);
     S.fold.ensure(ncomplex * sizeof(C));
     C *g = S.fold.template as<C>();
-    k_fold_block_means<T><<<nblk(ncomplex), 256, 0, ctx.stream>>>(g, reinterpret_cast<const C *>(source_k), F.n, r,
-                                                                  tabT(), S.btab.template as<C>(),
-                                                                  (T)std::pow((double)r, -1.5));
+    const T fac = (T)std::pow((double)r, -1.5);
+    const C *src = reinterpret_cast<const C *>(source_k);
+    const C *bt = S.btab.template as<C>();
+    if (r == 2) k_fold_block_means<T, 2><<<nblk(ncomplex), 256, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac);
+    else if (r == 4) k_fold_block_means<T, 4><<<nblk(ncomplex), 256, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac);
+    else if (r == 8) k_fold_block_means<T, 8><<<nblk(ncomplex), 256, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac);
+    else k_fold_block_means<T, 0><<<nblk(ncomplex), 256, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac);
     launched();
     fft_c2r_3d<T>(ctx, reinterpret_cast<T *>(g), nc, std::pow((double)nc, -1.5));
     const int sx = (int)std::lround((F.x0[0] - Cl.x0[0]) / Cl.dx), sy = (int)std::lround((F.x0[1] - Cl.x0[1]) / Cl.dx),

@@ -124,19 +124,34 @@ __global__ void __launch_bounds__(256) k_interp_add_sep(FieldPtrs<T, NF> fp, int
   T *Q = P + (size_t)NF * maxcy * maxcz;  // [NF][maxcy][nf]
   const size_t rs = (size_t)(2 * (nc / 2 + 1));
   const int tile = ny * nz;
-  for (int e = threadIdx.x; e < tile; e += blockDim.x) {
-    int cy = cw(cy0 + e / nz), cz = cw(cz0 + e % nz);
-    T v[NF];
+  // cw without a division for the indices within one period of the grid
+  auto cwf = [&](int v) {
+    if (!wrap) return min(max(v, 0), nc - 1);
+    if (v >= 0 && v < nc) return v;
+    if (v < 0 && v >= -nc) return v + nc;
+    if (v >= nc && v < 2 * nc) return v - nc;
+    return ((v % nc) + nc) % nc;
+  };
+  // a warp per coarse row of the tile, its lanes along z
+  const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31), nwarps = (int)(blockDim.x >> 5);
+  for (int cyi = warp; cyi < ny; cyi += nwarps) {
+    const int cy = cwf(cy0 + cyi);
+    size_t k0[4];
 #pragma unroll
-    for (int f = 0; f < NF; ++f) v[f] = 0;
+    for (int a = 0; a < 4; ++a) k0[a] = ((size_t)ixw[a] * nc + cy) * rs;
+    for (int czi = lane; czi < nz; czi += 32) {
+      const int cz = cwf(cz0 + czi);
+      T v[NF];
 #pragma unroll
-    for (int a = 0; a < 4; ++a) {
-      size_t k = ((size_t)ixw[a] * nc + cy) * rs + cz;
+      for (int f = 0; f < NF; ++f) v[f] = 0;
 #pragma unroll
-      for (int f = 0; f < NF; ++f) v[f] += wx[a] * __ldg(fp.src[f] + k);
+      for (int a = 0; a < 4; ++a) {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) v[f] += wx[a] * __ldg(fp.src[f] + k0[a] + cz);
+      }
+#pragma unroll
+      for (int f = 0; f < NF; ++f) P[f * tile + cyi * nz + czi] = v[f];
     }
-#pragma unroll
-    for (int f = 0; f < NF; ++f) P[f * tile + e] = v[f];
   }
   __shared__ T wys[TY][4];
   __shared__ int pys[TY];
