@@ -193,9 +193,10 @@ struct CellBox {
 // geometry derived from the levels alone (window masks, deinterpolation axes), kept per key
 struct GeomEntry {
   std::vector<double> key;
-  DevBuf dev;
+  DevBuf dev, aux;
   std::vector<int> host;
   CellBox box;
+  int umin[3] = {0, 0, 0}, ncu[3] = {0, 0, 0}, roff[3] = {0, 0, 0};  // per-axis tables in aux
 };
 struct ModRequest {
   int kind;

@@ -679,35 +679,43 @@ __device__ __forceinline__ void cr_weights(T t, T (&w)[4]) {
 }
 
 // Transpose interpolation, one axis at a time.  `in` has dims (A0, A1, A2) with
-// strides (s0, s1, 1); the pass contracts axis `ax` of length nf into length nout
-// starting at unwrapped coarse index c0: out[..c..] += w_a(t_x) in[..x..] for
-// c = ubase[x] - 1 + a - c0.  One thread owns one line along `ax`, so no two
-// threads write the same element.
+// strides (s0, s1, 1); the pass contracts axis `ax` of nf fine cells into nout coarse
+// cells starting at unwrapped coarse index c0: out[..c..] = sum over x of
+// w_a(t_x) in[..x..] for c = ubase[x] - 1 + a, taken in increasing x, a thread per
+// output element.  range[u - umin] = the first and last fine cell (whole
+// axis) reaching unwrapped coarse index u; ubase and frac start at the line's first
+// fine cell x0 (whole-axis index), nf cells.  Every output element is written.
 template <typename T>
-__global__ void k_deinterp_pass(const T *in, long long in_s0, long long in_s1, T *out, long long out_s0,
-                                long long out_s1, int ax, int n0, int n1, int n2, int nf, const int *ubase,
-                                const T *frac, int c0, int nout, T scale) {
-  // the two non-contracted axes
+__global__ void k_deinterp_gather(const T *in, long long in_s0, long long in_s1, T *out, long long out_s0,
+                                  long long out_s1, int ax, int n0, int n1, int n2, int nf, const int *ubase,
+                                  const T *frac, const int2 *range, int umin, int ncu, int x0, int c0, int nout,
+                                  T scale) {
   int d[3] = {n0, n1, n2};
-  long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  int oa = ax == 0 ? 1 : 0, ob = ax == 2 ? 1 : 2;
-  long long lines = (long long)d[oa] * d[ob];
-  if (tid >= lines) return;
-  int ib = (int)(tid % d[ob]), ia = (int)(tid / d[ob]);
+  const int oa = ax == 0 ? 1 : 0, ob = ax == 2 ? 1 : 2;
+  const long long lines = (long long)d[oa] * d[ob];
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= lines * nout) return;
+  const long long line = tid % lines;
+  const int cc = (int)(tid / lines);
+  const int ib = (int)(line % d[ob]), ia = (int)(line / d[ob]);
   long long is[3] = {in_s0, in_s1, 1}, os[3] = {out_s0, out_s1, 1};
-  long long ibase = (long long)ia * is[oa] + (long long)ib * is[ob];
-  long long obase = (long long)ia * os[oa] + (long long)ib * os[ob];
-  for (int x = 0; x < nf; ++x) {
-    T v = in[ibase + (long long)x * is[ax]] * scale;
-    T w[4];
-    cr_weights<T>(frac[x], w);
-    int c = ubase[x] - 1 - c0;
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-      int cc = c + a;
-      if (cc >= 0 && cc < nout) out[obase + (long long)cc * os[ax]] += w[a] * v;
+  const long long ibase = (long long)ia * is[oa] + (long long)ib * is[ob];
+  const long long obase = (long long)ia * os[oa] + (long long)ib * os[ob];
+  const int u = c0 + cc, ui = u - umin;
+  T acc = 0;
+  if (ui >= 0 && ui < ncu) {
+    const int2 rg = range[ui];
+    const int lo = max(rg.x - x0, 0), hi = min(rg.y - x0, nf - 1);
+    for (int x = lo; x <= hi; ++x) {
+      const int a = u - (ubase[x] - 1);
+      if (a < 0 || a > 3) continue;
+      const T v = in[ibase + (long long)x * is[ax]] * scale;
+      T w[4];
+      cr_weights<T>(frac[x], w);
+      acc += w[a] * v;
     }
   }
+  out[obase + (long long)cc * os[ax]] = acc;
 }
 
 // add a compact block (bx, by, bz) starting at unwrapped coarse (c0x, c0y, c0z) into a padded real coarse field
@@ -795,8 +803,7 @@ __global__ void k_fold_block_means(typename V2m<T>::type *out, const typename V2
           ar += fr * b_r - fi * b_i;
           ai += fr * b_i + fi * b_r;
         }
-        continue;
-      }
+      } else {
       for (int mz = 0; mz < r; ++mz) {
         const int kz = KZ + mz * nc;
         C f;
@@ -818,6 +825,7 @@ __global__ void k_fold_block_means(typename V2m<T>::type *out, const typename V2
         const T fr = f.x * t, fi = f.y * t;
         ar += fr * b_r - fi * b_i;
         ai += fr * b_i + fi * b_r;
+      }
       }
     }
   }
@@ -2179,7 +2187,36 @@ struct ModEngine {
       ge.host.resize(3 * nf);
       GIC_CUDA(cudaMemcpyAsync(ge.host.data(), ub0, 3 * nf * sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
       GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+      // per axis, the fine cells reaching each coarse index: [first, last]
+      std::vector<int> rg;
+      for (int a = 0; a < 3; ++a) {
+        const int *ua = &ge.host[(size_t)a * nf];
+        int lo = ua[0], hi = ua[0];
+        for (int x = 1; x < nf; ++x) {
+          lo = std::min(lo, ua[x]);
+          hi = std::max(hi, ua[x]);
+        }
+        ge.umin[a] = lo - 1;
+        ge.ncu[a] = hi + 3 - ge.umin[a];
+        ge.roff[a] = (int)(rg.size() / 2);
+        rg.resize(rg.size() + 2 * (size_t)ge.ncu[a]);
+        int *t = &rg[2 * (size_t)ge.roff[a]];
+        for (int i = 0; i < ge.ncu[a]; ++i) {
+          t[2 * i] = nf;
+          t[2 * i + 1] = -1;
+        }
+        for (int x = 0; x < nf; ++x)
+          for (int k = 0; k < 4; ++k) {
+            const int i = ua[x] - 1 + k - ge.umin[a];
+            t[2 * i] = std::min(t[2 * i], x);
+            t[2 * i + 1] = std::max(t[2 * i + 1], x);
+          }
+      }
+      ge.aux.ensure(rg.size() * sizeof(int));
+      GIC_CUDA(cudaMemcpyAsync(ge.aux.ptr, rg.data(), rg.size() * sizeof(int), cudaMemcpyHostToDevice, ctx.stream));
+      GIC_CUDA(cudaStreamSynchronize(ctx.stream));
     }
+    const int2 *ranges = ge.aux.template as<int2>();
     int *ub = ge.dev.template as<int>();
     T *fr = reinterpret_cast<T *>(ub + 3 * nf);
     const std::vector<int> &h = ge.host;
@@ -2197,24 +2234,23 @@ struct ModEngine {
     // pass x: fine box (fn0, fn1, fn2) -> t1 (cnt0, fn1, fn2)
     const size_t b1 = (size_t)cnt[0] * fn[1] * fn[2];
     S.t1.ensure(b1 * sizeof(T));
-    GIC_CUDA(cudaMemsetAsync(S.t1.ptr, 0, b1 * sizeof(T), ctx.stream));
-    k_deinterp_pass<T><<<nblk((size_t)fn[1] * fn[2]), 256, 0, ctx.stream>>>(
+    k_deinterp_gather<T><<<nblk(b1), 256, 0, ctx.stream>>>(
         in, (long long)nf * frs, frs, S.t1.template as<T>(), (long long)fn[1] * fn[2], fn[2], 0, fn[0], fn[1], fn[2], fn[0],
-        ub + f0[0], fr + f0[0], c0[0], cnt[0], scale);
+        ub + f0[0], fr + f0[0], ranges + ge.roff[0], ge.umin[0], ge.ncu[0], f0[0], c0[0], cnt[0], scale);
     // pass y: t1 (cnt0, fn1, fn2) -> t2 (cnt0, cnt1, fn2)
     const size_t b2 = (size_t)cnt[0] * cnt[1] * fn[2];
     S.t2.ensure(b2 * sizeof(T));
-    GIC_CUDA(cudaMemsetAsync(S.t2.ptr, 0, b2 * sizeof(T), ctx.stream));
-    k_deinterp_pass<T><<<nblk((size_t)cnt[0] * fn[2]), 256, 0, ctx.stream>>>(
+    k_deinterp_gather<T><<<nblk(b2), 256, 0, ctx.stream>>>(
         S.t1.template as<T>(), (long long)fn[1] * fn[2], fn[2], S.t2.template as<T>(), (long long)cnt[1] * fn[2], fn[2], 1,
-        cnt[0], fn[1], fn[2], fn[1], ub + nf + f0[1], fr + nf + f0[1], c0[1], cnt[1], (T)1);
+        cnt[0], fn[1], fn[2], fn[1], ub + nf + f0[1], fr + nf + f0[1], ranges + ge.roff[1], ge.umin[1], ge.ncu[1], f0[1],
+        c0[1], cnt[1], (T)1);
     // pass z: t2 (cnt0, cnt1, fn2) -> t3 (cnt0, cnt1, cnt2)
     const size_t b3 = (size_t)cnt[0] * cnt[1] * cnt[2];
     S.t3.ensure(b3 * sizeof(T));
-    GIC_CUDA(cudaMemsetAsync(S.t3.ptr, 0, b3 * sizeof(T), ctx.stream));
-    k_deinterp_pass<T><<<nblk((size_t)cnt[0] * cnt[1]), 256, 0, ctx.stream>>>(
+    k_deinterp_gather<T><<<nblk(b3), 256, 0, ctx.stream>>>(
         S.t2.template as<T>(), (long long)cnt[1] * fn[2], fn[2], S.t3.template as<T>(), (long long)cnt[1] * cnt[2], cnt[2], 2,
-        cnt[0], cnt[1], fn[2], fn[2], ub + 2 * nf + f0[2], fr + 2 * nf + f0[2], c0[2], cnt[2], (T)1);
+        cnt[0], cnt[1], fn[2], fn[2], ub + 2 * nf + f0[2], fr + 2 * nf + f0[2], ranges + ge.roff[2], ge.umin[2],
+        ge.ncu[2], f0[2], c0[2], cnt[2], (T)1);
     CellBox b = CellBox::whole(Cl.n);
     for (int a = 0; a < 3; ++a) b.set_axis(a, c0[a], (long long)c0[a] + cnt[a], 0, Cl.n);
     if (zero_block) zero_planes(coarse, c, b);
