@@ -1329,6 +1329,12 @@ void fixed_transform(Context &ctx, typename Cx<T>::type *c, const typename Cx<T>
       rc = t.rows;
       pv = t.planes;
     }
+  // a choice pinned by hand (GIC_FFT_TILE) replaces the tuner
+  if (cc < 0 && F.force_cols >= 0 && F.force_rows >= 0) {
+    cc = F.force_cols;
+    rc = F.force_rows;
+    pv = -1;
+  }
   if (cc < 0) {
     std::lock_guard<std::mutex> lock(g_tune_mutex);
     for (auto &t : g_tuned)
