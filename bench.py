@@ -121,6 +121,51 @@ def n_particles(wl):
     return sum(lev[2] ** 3 if lev[0] == 'base' else lev[5] ** 3 for lev in wl['levels']) - wl.get('replaced', 0)
 
 
+def tipsy_map(wl):
+    """The gic_tipsy_map of a one- or two-level workload: the zoom replaces the base cells it
+    covers; particle masses, softenings and TipsyOutput's factors as genetIC forms them
+    (genetIC/src/io/tipsy.hpp:200-239, simulation/particles/zeldovich.hpp:55-62, 112-121),
+    the masses summed as a product per level.  None for other workloads."""
+    from genetic_gb300._lib import GicTipsyMap
+    levels = wl['levels']
+    _, L, n0 = levels[0]
+    if len(levels) > 2 or n0 > 1024:
+        return None, None
+    m = GicTipsyMap()
+    m.nlevels = len(levels)
+    m.n[0] = n0
+    dx = [L / n0]
+    counts = [n0 ** 3]
+    m.ratio = 1
+    rep = np.zeros(0, dtype=np.uint64)
+    if len(levels) == 2:
+        _, ox, oy, oz, factor, n1 = levels[1]
+        span = n0 // factor
+        m.n[1] = n1
+        m.ratio = factor * n1 // n0
+        m.origin[0], m.origin[1], m.origin[2] = ox, oy, oz
+        ax = [(o + np.arange(span)) % n0 for o in (ox, oy, oz)]
+        rep = np.sort(((ax[0][:, None, None] * n0 + ax[1][None, :, None]) * n0 + ax[2][None, None, :]).ravel())
+        rep = rep.astype(np.uint64)
+        dx.append(L / factor / n1)
+        counts = [n0 ** 3 - len(rep), len(rep) * m.ratio ** 3]
+    om, h = COSMO['omega_m'], COSMO['hubble']
+    a = 1.0 / (1.0 + COSMO['redshift'])
+    mass = [27.744948 * om * L ** 3 * (d / L) ** 3 for d in dx]
+    tot = sum(c * ms for c, ms in zip(counts, mass))
+    m.mass_factor = om / tot
+    m.pos_factor = 1.0 / L
+    kms = np.sqrt(4.3022682e-6 * (1e10 / h / m.mass_factor) / (L * 1000 / h))
+    m.vel_factor = a ** -0.5 / kms
+    for l, d in enumerate(dx):
+        m.mass[l] = mass[l]
+        m.eps[l] = d * 0.01075
+    m._rep = rep  # keep alive
+    m.replaced = rep.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong))
+    m.n_replaced = len(rep)
+    return m, sum(counts)
+
+
 class Clocks:
     """nvidia-smi samples while the timed region runs."""
 
@@ -522,6 +567,33 @@ def main():
         e2e_step(i)
     t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
     d2h = sum(p.nbytes + v.nbytes for p, v in pinned)
+    del pinned
+
+    # end to end to genetIC's tipsy records: the step, then the records of every particle
+    # in mapper order packed on the device (gic_tipsy_pack) into pinned host memory
+    e2e_tipsy = None
+    try:
+        tmap, ntot = tipsy_map(wl)
+        if tmap is not None:
+            recs = torch.empty((ntot * 9,), dtype=torch.float32, pin_memory=True).numpy()
+
+            def tipsy_step(i):
+                step(i)
+                gen._call('gic_tipsy_pack', ctypes.byref(tmap), 0, ntot, recs.ctypes.data_as(ctypes.c_void_p))
+
+            tipsy_step(0)
+            barrier(world)
+            t0 = time.perf_counter()
+            for i in range(args.steps):
+                tipsy_step(i)
+            t_tipsy = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
+            n0 = wl['levels'][0][2]
+            e2e_tipsy = {'value': round(ntot * world / t_tipsy / 1e6, 3), 'unit': 'Mparticles/s',
+                         'h2d_bytes_per_step': int(8 * tmap.n_replaced + 16 * n0 * n0 + 8),
+                         'd2h_bytes_per_step': int(recs.nbytes)}
+            del recs
+    except Exception as e:  # reported, never fatal to the benchmark line
+        e2e_tipsy = {'error': str(e)[:200]}
     roof = fft_roofline(gen, wl, stream)
     gen.close()
 
@@ -541,6 +613,7 @@ def main():
                    'parallelism': 'replicas' if world > 1 else 'single GPU'},
         'e2e': {'value': round(npart * world / t_e2e / 1e6, 3), 'unit': 'Mparticles/s',
                 'h2d_bytes_per_step': int(table.nbytes), 'd2h_bytes_per_step': int(d2h)},
+        'e2e_tipsy': e2e_tipsy,
         'gpu_launches': int(launches1.value - launches0.value),
         'roofline': roof,
         'clocks': clk.summary(),

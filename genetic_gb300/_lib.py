@@ -59,6 +59,14 @@ class GicCosmo(ctypes.Structure):
 _P = ctypes.c_void_p
 _D = ctypes.POINTER(ctypes.c_double)
 _I = ctypes.c_int
+
+
+class GicTipsyMap(ctypes.Structure):
+    """gic_tipsy_map: the particles of one level or a two-level zoom in genetIC's mapper order."""
+    _fields_ = [('nlevels', ctypes.c_int), ('n', ctypes.c_int * 2), ('ratio', ctypes.c_int),
+                ('origin', ctypes.c_int * 3), ('replaced', ctypes.POINTER(ctypes.c_ulonglong)),
+                ('n_replaced', ctypes.c_ulonglong), ('mass', ctypes.c_double * 2), ('eps', ctypes.c_double * 2),
+                ('pos_factor', ctypes.c_double), ('vel_factor', ctypes.c_double), ('mass_factor', ctypes.c_double)]
 # symbol -> argument types (all return int unless noted)
 SIGNATURES = {
     'gic_create': [ctypes.POINTER(_P), ctypes.POINTER(GicDeviceOpts)],
@@ -100,6 +108,9 @@ SIGNATURES = {
                                       ctypes.c_double, _I, _I, ctypes.c_double],
     'gic_apply_modifications': [_P, _D, _D],
     'gic_get_stream': [_P, ctypes.POINTER(_P)],
+    'gic_tipsy_count': [_P, ctypes.POINTER(ctypes.c_ulonglong)],
+    'gic_tipsy_pack_host': [_P, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.c_ulonglong, ctypes.c_ulonglong, _P, _I],
+    'gic_tipsy_pack': [_P, _P, ctypes.c_ulonglong, ctypes.c_ulonglong, _P],
 }
 
 _lib = None

@@ -12,7 +12,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, 'csrc')
 BUILD = os.path.join(HERE, '_build')
 LIB = os.path.join(HERE, 'libgicgpu.so')
-SOURCES = ['capi.cu', 'rng.cu', 'fft.cu', 'kspace.cu', 'particles.cu', 'zoom.cu', 'modify.cu', 'batch.cu']
+SOURCES = ['capi.cu', 'rng.cu', 'fft.cu', 'kspace.cu', 'particles.cu', 'zoom.cu', 'modify.cu', 'batch.cu', 'writers.cu']
+# the host packer rounds every product and difference separately, as genetIC's host build does
+SOURCE_FLAGS = {'writers.cu': ['-Xcompiler', '-ffp-contract=off']}
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-Xcompiler', '-fvisibility=hidden',
          '--expt-relaxed-constexpr']
@@ -27,7 +29,7 @@ def nvcc():
 
 def _compile(src, extra):
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + '.o')
-    cmd = [nvcc(), *ARCH, *FLAGS, *extra, '-I', os.path.join(HERE, '..', 'include'), '-c',
+    cmd = [nvcc(), *ARCH, *FLAGS, *SOURCE_FLAGS.get(src, []), *extra, '-I', os.path.join(HERE, '..', 'include'), '-c',
            os.path.join(CSRC, src), '-o', obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -152,6 +152,8 @@ double chi2_typed(Context &c, Level &L) {
 thread_local std::string g_create_error;
 
 }  // namespace
+
+std::string &host_error() { return g_create_error; }
 }  // namespace gic
 
 using gic::Error;
@@ -356,6 +358,46 @@ int gic_fetch_level(gic_ctx *ctx, int level, int what, double *host_dst) {
   gic::Level &L = gic::level_at(C, level);
   if (C.dbl()) gic::fetch_typed<double>(C, L, what, host_dst);
   else gic::fetch_typed<float>(C, L, what, host_dst);
+  API_END
+}
+
+// calls without a context: failures reported through gic_last_error(NULL)
+#define HOST_BEGIN try {
+#define HOST_END                                           \
+  }                                                        \
+  catch (const Error &e) {                                 \
+    gic::host_error() = e.msg;                             \
+    return e.code;                                         \
+  }                                                        \
+  catch (const std::bad_alloc &) {                         \
+    gic::host_error() = "host allocation failed";          \
+    return GIC_ERR_OOM;                                    \
+  }                                                        \
+  catch (const std::exception &e) {                        \
+    gic::host_error() = e.what();                          \
+    return GIC_ERR_INTERNAL;                               \
+  }                                                        \
+  gic::host_error().clear();                               \
+  return GIC_OK;
+
+int gic_tipsy_count(const gic_tipsy_map *map, unsigned long long *count) {
+  HOST_BEGIN
+  if (!count) gic::fail(GIC_ERR_INVALID_ARG, "null count");
+  *count = gic::tipsy_count(map);
+  HOST_END
+}
+
+int gic_tipsy_pack_host(const gic_tipsy_map *map, const double *const *pos, const double *const *vel,
+                        unsigned long long first, unsigned long long count, gic_tipsy_dark *out, int threads) {
+  HOST_BEGIN
+  gic::tipsy_pack_host(map, pos, vel, first, count, out, threads);
+  HOST_END
+}
+
+int gic_tipsy_pack(gic_ctx *ctx, const gic_tipsy_map *map, unsigned long long first, unsigned long long count,
+                   gic_tipsy_dark *host_out) {
+  API_BEGIN(ctx)
+  gic::tipsy_pack_device(C, map, first, count, host_out);
   API_END
 }
 

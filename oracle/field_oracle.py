@@ -1027,3 +1027,67 @@ def splice_levels(levels, original, new, power, flagged):
         out.append(s)
         its.append(i)
     return out, its
+
+
+# --- tipsy output (genetIC/src/io/tipsy.hpp:109-145, 200-262) ---------------------------
+
+def mapper_order(n0, replaced=(), n1=0, ratio=1, origin=(0, 0, 0)):
+    """(level, cell) of every particle in genetIC's mapper order: the level-0 cells
+    not replaced, in cell order, then for every replaced level-0 cell (ascending) the
+    ratio^3 level-1 cells under it, x, y, z ascending (OneLevelParticleMapper;
+    TwoLevelParticleMapper, particles/mapper/twolevelmapper.hpp:262-320, 869-893;
+    Grid::insertCubeIdsIntoVector, grid.hpp:704-729; iterateOverCube, coordinate.hpp:197-208)."""
+    replaced = np.sort(np.asarray(replaced, dtype=np.int64))
+    keep = np.ones(n0 ** 3, dtype=bool)
+    keep[replaced] = False
+    lev = [np.zeros(int(keep.sum()), dtype=np.int64)]
+    cells = [np.flatnonzero(keep)]
+    if len(replaced):
+        px, py, pz = replaced // (n0 * n0), (replaced // n0) % n0, replaced % n0
+        px, py, pz = ((px - origin[0]) % n0, (py - origin[1]) % n0, (pz - origin[2]) % n0)
+        s = np.arange(ratio ** 3)
+        sx, sy, sz = s // (ratio * ratio), (s // ratio) % ratio, s % ratio
+        fx = px[:, None] * ratio + sx[None, :]
+        fy = py[:, None] * ratio + sy[None, :]
+        fz = pz[:, None] * ratio + sz[None, :]
+        fine = ((fx * n1 + fy) * n1 + fz).ravel()
+        lev.append(np.ones(len(fine), dtype=np.int64))
+        cells.append(fine)
+    return np.concatenate(lev), np.concatenate(cells)
+
+
+def tipsy_factors(levels, cosmo, order_levels):
+    """Per-level particle mass and softening (zeldovich.hpp:55-62, 112-121, grid.hpp:112)
+    and TipsyOutput's factors (tipsy.hpp:200-239): mass_factor = Om / (masses summed in
+    mapper order), pos_factor = 1 / box, vel_factor = a^-1/2 / dKmsUnit."""
+    L = levels[0][0]
+    om, h = cosmo['omega_m'], cosmo['hubble']
+    a = 1.0 / (1.0 + cosmo['redshift'])
+    box_mass = 27.744948 * om * pow(L, 3.0)
+    mass = [box_mass * pow((b / n) / L, 3.0) for b, n, _ in levels]
+    eps = [(b / n) * 1.0 * 0.01075 for b, n, _ in levels]
+    tot = 0.0
+    for lv in order_levels:  # the reference's running double sum
+        tot += mass[lv]
+    mass_factor = om / tot
+    pos_factor = 1. / L
+    kpc = L * 1000 / h
+    msol = 1e10 / h / mass_factor
+    kms = np.sqrt(4.3022682e-6 * msol / kpc)
+    vel_factor = pow(a, -0.5) / kms
+    return mass, eps, pos_factor, vel_factor, mass_factor
+
+
+def tipsy_records(order, pos, vel, mass, eps, pos_factor, vel_factor, mass_factor):
+    """Dark records (mass, x, y, z, vx, vy, vz, eps, phi) as float32 (tipsy.hpp:61-63,
+    123-131): products and differences in double, then rounded to float."""
+    lev, cells = order
+    out = np.zeros((len(cells), 9), dtype=np.float32)
+    for l in range(len(pos)):
+        sel = lev == l
+        c = cells[sel]
+        out[sel, 0] = np.float32(mass[l] * mass_factor)
+        out[sel, 1:4] = (pos[l][c] * pos_factor - 0.5).astype(np.float32)
+        out[sel, 4:7] = (vel[l][c] * vel_factor).astype(np.float32)
+        out[sel, 7] = np.float32(eps[l] * pos_factor)
+    return out

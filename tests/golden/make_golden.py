@@ -312,6 +312,19 @@ def splice_goldens():
             np.savez_compressed(os.path.join(HERE, '%s.npz' % name), **grids, iterations=np.array(its))
 
 
+def tipsy_goldens():
+    """The reference's tipsy file of the two-level zoom2 case (random_seed): header and dark records."""
+    with tempfile.TemporaryDirectory() as d:
+        write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+        open(os.path.join(d, 'paramfile.txt'), 'w').write(
+            ZOOM_PARAMS.format(seedcmd='random_seed', zooms='\n'.join(ZOOMS['zoom2']), dumps=''))
+        subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True)
+        raw = open(os.path.join(d, 'out.tipsy'), 'rb').read()
+        header = np.frombuffer(raw[8:28], '<i4').copy()
+        t, _, dark = read_tipsy(os.path.join(d, 'out.tipsy'))
+        np.savez_compressed(os.path.join(HERE, 'tipsy_zoom2.npz'), scalefactor=np.float64(t), header=header, dark=dark)
+
+
 def main():
     for mode, cmd in (('serial', 'random_seed_serial'), ('parallel', 'random_seed'), ('real', 'random_seed_real_space')):
         with tempfile.TemporaryDirectory() as d:
@@ -335,3 +348,4 @@ if __name__ == '__main__':
     ops_goldens()
     mod_more_goldens()
     splice_goldens()
+    tipsy_goldens()

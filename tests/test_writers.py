@@ -1,0 +1,138 @@
+"""Tipsy records in genetIC's particle-mapper order (CPU): the oracle against the
+reference's own tipsy file, and the C ABI's host packer against the oracle."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+import field_oracle as fo
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, 'tests', 'golden')
+
+# the reference run of tests/golden/make_golden.py:tipsy_goldens (the zoom2 case)
+ZOOM2 = [(50.0, 32, (0.0, 0.0, 0.0)), (25.0, 32, (12.5, 12.5, 12.5))]
+ORIGIN = (8, 8, 8)
+
+
+def make_map(levels, replaced, factors, ratio=2, origin=ORIGIN):
+    from genetic_gb300._lib import GicTipsyMap
+    mass, eps, pf, vf, mf = factors
+    m = GicTipsyMap()
+    m.nlevels = len(levels)
+    for l, (_, n, _) in enumerate(levels):
+        m.n[l] = n
+        m.mass[l] = mass[l]
+        m.eps[l] = eps[l]
+    m.ratio = ratio
+    for a in range(3):
+        m.origin[a] = origin[a]
+    rep = np.ascontiguousarray(replaced, dtype=np.uint64)
+    m._rep = rep  # keep alive
+    m.replaced = rep.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong))
+    m.n_replaced = len(rep)
+    m.pos_factor, m.vel_factor, m.mass_factor = pf, vf, mf
+    return m
+
+
+def pack_host(lib, m, pos, vel, first=0, count=None, threads=4):
+    total = ctypes.c_ulonglong()
+    assert lib.gic_tipsy_count(ctypes.byref(m), ctypes.byref(total)) == 0
+    if count is None:
+        count = total.value - first
+    out = np.zeros((count, 9), dtype=np.float32)
+    P = ctypes.POINTER(ctypes.c_double)
+    pp = (P * 2)(*[np.ascontiguousarray(p).ctypes.data_as(P) for p in pos] + [None] * (2 - len(pos)))
+    vv = (P * 2)(*[np.ascontiguousarray(v).ctypes.data_as(P) for v in vel] + [None] * (2 - len(vel)))
+    rc = lib.gic_tipsy_pack_host(ctypes.byref(m), pp, vv, first, count, out.ctypes.data_as(ctypes.c_void_p), threads)
+    return rc, out
+
+
+@pytest.fixture(scope='module')
+def zoom2_particles(bbks):
+    from conftest import COSMO
+    w = fo.white_noise_levels([l[1] for l in ZOOM2], 8896131, 2)
+    out = fo.zoom_realisation(w, ZOOM2, fo.CambPower(bbks, COSMO))
+    ratio = fo.velocity_to_offset_ratio(COSMO)
+    pv = [fo.particles(out[l][1:4], b, off, ZOOM2[0][0], ratio) for l, (b, n, off) in enumerate(ZOOM2)]
+    replaced = fo.flag_cells(fo.Levels(ZOOM2), 0, (25., 25., 25.), 'cube', 10)
+    order = fo.mapper_order(32, replaced, 32, 2, ORIGIN)
+    factors = fo.tipsy_factors(ZOOM2, COSMO, order[0])
+    return dict(pos=[p for p, _ in pv], vel=[v for _, v in pv], replaced=replaced, order=order, factors=factors)
+
+
+def test_oracle_tipsy_matches_reference_file(zoom2_particles):
+    g = np.load(os.path.join(GOLDEN, 'tipsy_zoom2.npz'))
+    z = zoom2_particles
+    ref = g['dark']
+    assert int(g['header'][0]) == len(z['order'][1]) == len(ref)
+    got = fo.tipsy_records(z['order'], z['pos'], z['vel'], *z['factors'])
+    # mass and softening follow from the geometry and the summed masses: exact
+    assert np.array_equal(got[:, 0], ref[:, 0]) and np.array_equal(got[:, 7:], ref[:, 7:])
+    # positions (box units, |x| <= 0.5) and velocities: the oracle's doubles agree with the
+    # reference build's to ~1e-12, so the floats agree to one rounding step
+    assert np.abs(got[:, 1:4] - ref[:, 1:4]).max() <= 6e-8
+    assert np.abs(got[:, 4:7] - ref[:, 4:7]).max() <= 2e-7 * np.abs(ref[:, 4:7]).max()
+
+
+def test_host_packer_matches_oracle_bit_for_bit(built, zoom2_particles):
+    from genetic_gb300 import _lib
+    lib = _lib.load()
+    z = zoom2_particles
+    m = make_map(ZOOM2, z['replaced'], z['factors'])
+    want = fo.tipsy_records(z['order'], z['pos'], z['vel'], *z['factors'])
+    rc, got = pack_host(lib, m, z['pos'], z['vel'])
+    assert rc == 0
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    # a window straddling the two levels, and a single thread
+    n_kept = 32 ** 3 - len(z['replaced'])
+    rc, part = pack_host(lib, m, z['pos'], z['vel'], first=n_kept - 100, count=900, threads=1)
+    assert rc == 0 and np.array_equal(part.view(np.uint32), want[n_kept - 100:n_kept + 800].view(np.uint32))
+
+
+def test_mapper_order_one_level_and_wrapped_origin(built):
+    """Cell ids carried through the positions: the packer's order is the oracle's."""
+    from genetic_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(5)
+    # one level: every cell in order
+    n = 8
+    pos = [np.repeat(np.arange(n ** 3, dtype=np.float64)[:, None], 3, 1)]
+    vel = [np.zeros((n ** 3, 3))]
+    m = make_map([(1.0, n, (0, 0, 0))], [], ([1.0], [0.0], 1.0, 1.0, 1.0))
+    rc, got = pack_host(lib, m, pos, vel)
+    assert rc == 0 and np.array_equal(got[:, 1], np.arange(n ** 3, dtype=np.float32) - 0.5)
+    # two levels, ratio 4, zoom origin near the top corner so blocks wrap around the box
+    n0, r, n1, org = 8, 4, 16, (6, 6, 7)
+    coords = [(x, y, z) for x in (6, 7, 0, 1) for y in (6, 7, 0, 1) for z in (7, 0, 1, 2)]
+    cells = np.array(sorted(rng.choice([(x * n0 + y) * n0 + z for x, y, z in coords], 20, replace=False)))
+    pos = [np.repeat(np.arange(n0 ** 3, dtype=np.float64)[:, None], 3, 1),
+           np.repeat(1000. + np.arange(n1 ** 3, dtype=np.float64)[:, None], 3, 1)]
+    vel = [np.zeros((n0 ** 3, 3)), np.zeros((n1 ** 3, 3))]
+    m = make_map([(1.0, n0, (0, 0, 0)), (1.0, n1, (0, 0, 0))], cells, ([1.0, 1.0], [0.0, 0.0], 1.0, 1.0, 1.0),
+                 ratio=r, origin=org)
+    rc, got = pack_host(lib, m, pos, vel)
+    lev, want = fo.mapper_order(n0, cells, n1, r, org)
+    assert rc == 0
+    assert np.array_equal(got[:, 1].astype(np.float64) + 0.5, want + 1000. * lev)
+
+
+def test_tipsy_map_errors(built):
+    from genetic_gb300 import _lib
+    lib = _lib.load()
+    f = ([1.0, 1.0], [0.0, 0.0], 1.0, 1.0, 1.0)
+    cnt = ctypes.c_ulonglong()
+    # a replaced cell outside the level-1 grid (the reference throws out_of_range)
+    m = make_map([(1.0, 8, (0, 0, 0)), (1.0, 8, (0, 0, 0))], [0, 4 * 8 * 8], f, ratio=2, origin=(0, 0, 0))
+    assert lib.gic_tipsy_count(ctypes.byref(m), ctypes.byref(cnt)) == _lib.GIC_ERR_INVALID_ARG
+    assert b'outside high resolution grid' in lib.gic_last_error(None)
+    # not ascending
+    m = make_map([(1.0, 8, (0, 0, 0)), (1.0, 8, (0, 0, 0))], [5, 3], f, ratio=2, origin=(0, 0, 0))
+    assert lib.gic_tipsy_count(ctypes.byref(m), ctypes.byref(cnt)) == _lib.GIC_ERR_INVALID_ARG
+    # a window past the end
+    m = make_map([(1.0, 4, (0, 0, 0))], [], f)
+    pos = [np.zeros((64, 3))]
+    rc, _ = pack_host(lib, m, pos, pos, first=60, count=5)
+    assert rc == _lib.GIC_ERR_INVALID_ARG
+    assert lib.gic_tipsy_count(ctypes.byref(m), ctypes.byref(cnt)) == 0 and cnt.value == 64
