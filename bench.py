@@ -122,16 +122,16 @@ def n_particles(wl):
 
 
 def tipsy_map(wl):
-    """The gic_tipsy_map of a one- or two-level workload: the zoom replaces the base cells it
+    """The gic_particle_map of a one- or two-level workload: the zoom replaces the base cells it
     covers; particle masses, softenings and TipsyOutput's factors as genetIC forms them
     (genetIC/src/io/tipsy.hpp:200-239, simulation/particles/zeldovich.hpp:55-62, 112-121),
     the masses summed as a product per level.  None for other workloads."""
-    from genetic_gb300._lib import GicTipsyMap
+    from genetic_gb300._lib import GicParticleMap
     levels = wl['levels']
     _, L, n0 = levels[0]
     if len(levels) > 2 or n0 > 1024:
         return None, None
-    m = GicTipsyMap()
+    m = GicParticleMap()
     m.nlevels = len(levels)
     m.n[0] = n0
     dx = [L / n0]

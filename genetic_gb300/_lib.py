@@ -61,8 +61,8 @@ _D = ctypes.POINTER(ctypes.c_double)
 _I = ctypes.c_int
 
 
-class GicTipsyMap(ctypes.Structure):
-    """gic_tipsy_map: the particles of one level or a two-level zoom in genetIC's mapper order."""
+class GicParticleMap(ctypes.Structure):
+    """gic_particle_map: the particles of one level or a two-level zoom in genetIC's mapper order."""
     _fields_ = [('nlevels', ctypes.c_int), ('n', ctypes.c_int * 2), ('ratio', ctypes.c_int),
                 ('origin', ctypes.c_int * 3), ('replaced', ctypes.POINTER(ctypes.c_ulonglong)),
                 ('n_replaced', ctypes.c_ulonglong), ('mass', ctypes.c_double * 2), ('eps', ctypes.c_double * 2),
@@ -111,6 +111,8 @@ SIGNATURES = {
     'gic_tipsy_count': [_P, ctypes.POINTER(ctypes.c_ulonglong)],
     'gic_tipsy_pack_host': [_P, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.c_ulonglong, ctypes.c_ulonglong, _P, _I],
     'gic_tipsy_pack': [_P, _P, ctypes.c_ulonglong, ctypes.c_ulonglong, _P],
+    'gic_gadget_pack_host': [_P, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.c_ulonglong, ctypes.c_ulonglong, _P, _P,
+                             _P, _P, _I],
 }
 
 _lib = None

@@ -380,21 +380,29 @@ int gic_fetch_level(gic_ctx *ctx, int level, int what, double *host_dst) {
   gic::host_error().clear();                               \
   return GIC_OK;
 
-int gic_tipsy_count(const gic_tipsy_map *map, unsigned long long *count) {
+int gic_tipsy_count(const gic_particle_map *map, unsigned long long *count) {
   HOST_BEGIN
   if (!count) gic::fail(GIC_ERR_INVALID_ARG, "null count");
   *count = gic::tipsy_count(map);
   HOST_END
 }
 
-int gic_tipsy_pack_host(const gic_tipsy_map *map, const double *const *pos, const double *const *vel,
+int gic_tipsy_pack_host(const gic_particle_map *map, const double *const *pos, const double *const *vel,
                         unsigned long long first, unsigned long long count, gic_tipsy_dark *out, int threads) {
   HOST_BEGIN
   gic::tipsy_pack_host(map, pos, vel, first, count, out, threads);
   HOST_END
 }
 
-int gic_tipsy_pack(gic_ctx *ctx, const gic_tipsy_map *map, unsigned long long first, unsigned long long count,
+int gic_gadget_pack_host(const gic_particle_map *map, const double *const *pos, const double *const *vel,
+                         unsigned long long first, unsigned long long count, float *pos_out, float *vel_out,
+                         unsigned long long *ids, float *mass_out, int threads) {
+  HOST_BEGIN
+  gic::gadget_pack_host(map, pos, vel, first, count, pos_out, vel_out, ids, mass_out, threads);
+  HOST_END
+}
+
+int gic_tipsy_pack(gic_ctx *ctx, const gic_particle_map *map, unsigned long long first, unsigned long long count,
                    gic_tipsy_dark *host_out) {
   API_BEGIN(ctx)
   gic::tipsy_pack_device(C, map, first, count, host_out);

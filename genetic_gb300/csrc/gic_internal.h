@@ -377,10 +377,13 @@ void make_particles(Context &ctx, Level &L, int order = 1);
 // the opaque handle of the C ABI
 namespace gic {
 // tipsy records (writers.cu)
-unsigned long long tipsy_count(const gic_tipsy_map *m);
-void tipsy_pack_host(const gic_tipsy_map *m, const double *const *pos, const double *const *vel, unsigned long long first,
+unsigned long long tipsy_count(const gic_particle_map *m);
+void tipsy_pack_host(const gic_particle_map *m, const double *const *pos, const double *const *vel, unsigned long long first,
                      unsigned long long count, gic_tipsy_dark *out, int threads);
-void tipsy_pack_device(Context &C, const gic_tipsy_map *m, unsigned long long first, unsigned long long count,
+void gadget_pack_host(const gic_particle_map *m, const double *const *pos, const double *const *vel,
+                      unsigned long long first, unsigned long long count, float *pos_out, float *vel_out,
+                      unsigned long long *ids, float *mass_out, int threads);
+void tipsy_pack_device(Context &C, const gic_particle_map *m, unsigned long long first, unsigned long long count,
                        gic_tipsy_dark *host_out);
 // the message of the last failure of a call without a context (this thread)
 std::string &host_error();

@@ -101,7 +101,7 @@ __host__ __device__ inline void tipsy_record(gic_tipsy_dark &o, const double *po
 
 // the map's view, checked; replaced cells must lie under the level-1 grid, as
 // TwoLevelParticleMapper requires (calculateHiresParticleList throws otherwise)
-MapView check_map(const gic_tipsy_map *m) {
+MapView check_map(const gic_particle_map *m) {
   if (!m) fail(GIC_ERR_INVALID_ARG, "null map");
   MapView v{};
   v.nlevels = m->nlevels;
@@ -145,7 +145,7 @@ MapView check_map(const gic_tipsy_map *m) {
 
 unsigned long long map_size(const MapView &v) { return v.n_kept + v.n_replaced * v.per_block; }
 
-TipsyConst tipsy_const(const gic_tipsy_map *m) {
+TipsyConst tipsy_const(const gic_particle_map *m) {
   TipsyConst c{};
   for (int l = 0; l < 2; ++l) {
     c.mass[l] = m->mass[l];
@@ -187,9 +187,10 @@ inline void row_mask(const MapView &v, unsigned long long row, unsigned long lon
   }
 }
 
-template <typename V>
-void pack_host_t(const MapView &v, const double *const *pos, const V *const *vel, const TipsyConst &c,
-                 unsigned long long first, unsigned long long count, gic_tipsy_dark *out, int threads) {
+// every particle of [first, first + count) in mapper order, on `threads` host threads
+// (0: all cores): f(o, level, cell) with o the particle's index in the map
+template <typename F>
+void for_each_particle(const MapView &v, unsigned long long first, unsigned long long count, int threads, const F &f) {
   std::vector<unsigned long long> rep_begin, kept_before;
   row_tables(v, rep_begin, kept_before);
   const unsigned long long rows = (unsigned long long)v.n0 * v.n0, end = first + count;
@@ -204,14 +205,13 @@ void pack_host_t(const MapView &v, const double *const *pos, const V *const *vel
         const int rk = row_rank(w, pre, z);
         if (rk < 0) continue;
         const unsigned long long o = kb + (unsigned long long)rk;
-        if (o >= first && o < end) tipsy_record(out[o - first], pos[0], vel[0], row * v.n0 + z, 0, c);
+        if (o >= first && o < end) f(o, 0, row * v.n0 + z);
       }
     }
   };
   const unsigned long long f0 = std::max(first, v.n_kept), f1 = std::max(end, v.n_kept);
   auto fine = [&](unsigned long long o0, unsigned long long o1) {
-    for (unsigned long long o = o0; o < o1; ++o)
-      tipsy_record(out[o - first], pos[1], vel[1], fine_cell(v, o - v.n_kept), 1, c);
+    for (unsigned long long o = o0; o < o1; ++o) f(o, 1, fine_cell(v, o - v.n_kept));
   };
   int nt = threads > 0 ? threads : (int)std::max(1u, std::thread::hardware_concurrency());
   std::vector<std::thread> pool;
@@ -267,7 +267,7 @@ __global__ void k_tipsy_fine(gic_tipsy_dark *out, unsigned long long first, unsi
 
 }  // namespace
 
-unsigned long long tipsy_count(const gic_tipsy_map *m) { return map_size(check_map(m)); }
+unsigned long long tipsy_count(const gic_particle_map *m) { return map_size(check_map(m)); }
 
 static void check_window(const MapView &v, unsigned long long first, unsigned long long count, const void *out) {
   const unsigned long long total = map_size(v);
@@ -275,13 +275,39 @@ static void check_window(const MapView &v, unsigned long long first, unsigned lo
   if (count && !out) fail(GIC_ERR_INVALID_ARG, "null output");
 }
 
-void tipsy_pack_host(const gic_tipsy_map *m, const double *const *pos, const double *const *vel, unsigned long long first,
+void tipsy_pack_host(const gic_particle_map *m, const double *const *pos, const double *const *vel, unsigned long long first,
                      unsigned long long count, gic_tipsy_dark *out, int threads) {
   const MapView v = check_map(m);
   check_window(v, first, count, out);
   if (!pos || !vel || !pos[0] || !vel[0] || (v.nlevels == 2 && (!pos[1] || !vel[1])))
     fail(GIC_ERR_INVALID_ARG, "null particle arrays");
-  if (count) pack_host_t<double>(v, pos, vel, tipsy_const(m), first, count, out, threads);
+  if (!count) return;
+  const TipsyConst c = tipsy_const(m);
+  for_each_particle(v, first, count, threads, [&](unsigned long long o, int l, unsigned long long cell) {
+    tipsy_record(out[o - first], pos[l], vel[l], cell, l, c);
+  });
+}
+
+void gadget_pack_host(const gic_particle_map *m, const double *const *pos, const double *const *vel,
+                      unsigned long long first, unsigned long long count, float *pos_out, float *vel_out,
+                      unsigned long long *ids, float *mass_out, int threads) {
+  const MapView v = check_map(m);
+  const void *any = pos_out ? (const void *)pos_out : vel_out ? (const void *)vel_out : ids ? (const void *)ids
+                                                                                         : (const void *)mass_out;
+  check_window(v, first, count, any);
+  auto arrays_ok = [&](const double *const *a) { return a && a[0] && (v.nlevels == 1 || a[1]); };
+  if ((pos_out && !arrays_ok(pos)) || (vel_out && !arrays_ok(vel))) fail(GIC_ERR_INVALID_ARG, "null particle arrays");
+  if (!count) return;
+  const float mass[2] = {(float)m->mass[0], (float)m->mass[1]};
+  for_each_particle(v, first, count, threads, [&](unsigned long long o, int l, unsigned long long cell) {
+    const unsigned long long k = o - first;
+    for (int a = 0; a < 3; ++a) {
+      if (pos_out) pos_out[3 * k + a] = (float)pos[l][3 * cell + a];
+      if (vel_out) vel_out[3 * k + a] = (float)vel[l][3 * cell + a];
+    }
+    if (ids) ids[k] = o;
+    if (mass_out) mass_out[k] = mass[l];
+  });
 }
 
 template <typename V>
@@ -302,7 +328,7 @@ static void launch_tipsy(Context &C, const MapView &dv, const TipsyConst &c, uns
   }
 }
 
-void tipsy_pack_device(Context &C, const gic_tipsy_map *m, unsigned long long first, unsigned long long count,
+void tipsy_pack_device(Context &C, const gic_particle_map *m, unsigned long long first, unsigned long long count,
                        gic_tipsy_dark *host_out) {
   const MapView v = check_map(m);
   check_window(v, first, count, host_out);

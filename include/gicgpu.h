@@ -170,24 +170,35 @@ typedef struct {
   unsigned long long n_replaced;
   double mass[2], eps[2];
   double pos_factor, vel_factor, mass_factor;
-} gic_tipsy_map;
+} gic_particle_map;
 
 /* Number of particles of the map (TwoLevelParticleMapper::size).  Without a
  * context: a failure's message is gic_last_error(NULL). */
-GIC_API int gic_tipsy_count(const gic_tipsy_map *map, unsigned long long *count);
+GIC_API int gic_tipsy_count(const gic_particle_map *map, unsigned long long *count);
 
 /* Records [first, first + count) of the map from host particles (pos[l], vel[l]:
  * 3 doubles per cell of level l in cell order, as gic_fetch_particles writes them),
  * packed by `threads` host threads (0: all cores).  Replaces the packing loop of
  * TipsyOutput::saveNextBlockOfTipsyParticles (tipsy.hpp:109-145). */
-GIC_API int gic_tipsy_pack_host(const gic_tipsy_map *map, const double *const *pos, const double *const *vel,
+GIC_API int gic_tipsy_pack_host(const gic_particle_map *map, const double *const *pos, const double *const *vel,
                                 unsigned long long first, unsigned long long count, gic_tipsy_dark *out, int threads);
 
 /* The same records packed on the device from the context's particles (after
  * gic_zeldovich; levels 0 and 1 of the context) and copied to host_out: 36 bytes
  * per particle cross to the host instead of the 48 of gic_fetch_particles. */
-GIC_API int gic_tipsy_pack(gic_ctx *ctx, const gic_tipsy_map *map, unsigned long long first, unsigned long long count,
+GIC_API int gic_tipsy_pack(gic_ctx *ctx, const gic_particle_map *map, unsigned long long first, unsigned long long count,
                            gic_tipsy_dark *host_out);
+
+/* Gadget blocks (io::gadget::GadgetOutput, genetIC/src/io/gadget.hpp:481-520) of the map's
+ * particles [first, first + count) from host particles, every level of gadget particle
+ * type 1 (genetIC's default, ic.hpp:80, 606-614), by `threads` host threads: positions
+ * and velocities as float triples (Coordinate<float> of pos and vel), ids = the
+ * particle's index in the map (the mapper iterator's getIndex), masses as floats (the
+ * variable-mass block; map->mass per level).  NULL outputs are skipped; the map's
+ * eps and factors are not used.  Failures: gic_last_error(NULL). */
+GIC_API int gic_gadget_pack_host(const gic_particle_map *map, const double *const *pos, const double *const *vel,
+                                 unsigned long long first, unsigned long long count, float *pos_out, float *vel_out,
+                                 unsigned long long *ids, float *mass_out, int threads);
 
 /* Forward (dir=-1) or inverse (dir=+1) normalised 3-D real FFT of a level field
  * in place on the device (testing).  Replaces FieldFourierManager<T,T>::performTransform

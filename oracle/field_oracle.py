@@ -1091,3 +1091,20 @@ def tipsy_records(order, pos, vel, mass, eps, pos_factor, vel_factor, mass_facto
         out[sel, 4:7] = (vel[l][c] * vel_factor).astype(np.float32)
         out[sel, 7] = np.float32(eps[l] * pos_factor)
     return out
+
+
+def gadget_blocks(order, pos, vel, mass):
+    """Position, velocity and mass blocks of a gadget file whose particles are all of
+    one type (io/gadget.hpp:481-520): Coordinate<float> of pos and vel, float masses, in
+    mapper order."""
+    lev, cells = order
+    n = len(cells)
+    p = np.zeros((n, 3), dtype=np.float32)
+    v = np.zeros((n, 3), dtype=np.float32)
+    m = np.zeros(n, dtype=np.float32)
+    for l in range(len(pos)):
+        sel = lev == l
+        p[sel] = pos[l][cells[sel]].astype(np.float32)
+        v[sel] = vel[l][cells[sel]].astype(np.float32)
+        m[sel] = np.float32(mass[l])
+    return p, v, m

@@ -325,6 +325,36 @@ def tipsy_goldens():
         np.savez_compressed(os.path.join(HERE, 'tipsy_zoom2.npz'), scalefactor=np.float64(t), header=header, dark=dark)
 
 
+def read_fortran_records(path):
+    """The records of a Fortran-framed binary file (int32 length before and after each)."""
+    raw = open(path, 'rb').read()
+    recs, off = [], 0
+    while off < len(raw):
+        n = int(np.frombuffer(raw[off:off + 4], '<i4')[0])
+        recs.append(raw[off + 4:off + 4 + n])
+        assert int(np.frombuffer(raw[off + 4 + n:off + 8 + n], '<i4')[0]) == n
+        off += n + 8
+    return recs
+
+
+def gadget_goldens():
+    """The reference's gadget2 file of the zoom2 case: positions, velocities and masses
+    (every level is gadget type 1; the id block is checked to hold 0..n-1)."""
+    with tempfile.TemporaryDirectory() as d:
+        write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+        params = ZOOM_PARAMS.format(seedcmd='random_seed', zooms='\n'.join(ZOOMS['zoom2']), dumps='')
+        open(os.path.join(d, 'paramfile.txt'), 'w').write(params.replace('outformat tipsy', 'outformat gadget2'))
+        subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True)
+        header, pos, vel, ids, mass = read_fortran_records(os.path.join(d, 'out.gadget2'))
+        npart = np.frombuffer(header[:24], '<i4')
+        ids = np.frombuffer(ids, '<u8')
+        assert np.array_equal(ids, np.arange(len(ids)))
+        np.savez_compressed(os.path.join(HERE, 'gadget_zoom2.npz'), npart=npart.copy(),
+                            header_mass=np.frombuffer(header[24:72], '<f8').copy(),
+                            pos=np.frombuffer(pos, '<f4').reshape(-1, 3), vel=np.frombuffer(vel, '<f4').reshape(-1, 3),
+                            mass=np.frombuffer(mass, '<f4'))
+
+
 def main():
     for mode, cmd in (('serial', 'random_seed_serial'), ('parallel', 'random_seed'), ('real', 'random_seed_real_space')):
         with tempfile.TemporaryDirectory() as d:
@@ -349,3 +379,4 @@ if __name__ == '__main__':
     mod_more_goldens()
     splice_goldens()
     tipsy_goldens()
+    gadget_goldens()

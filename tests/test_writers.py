@@ -17,9 +17,9 @@ ORIGIN = (8, 8, 8)
 
 
 def make_map(levels, replaced, factors, ratio=2, origin=ORIGIN):
-    from genetic_gb300._lib import GicTipsyMap
+    from genetic_gb300._lib import GicParticleMap
     mass, eps, pf, vf, mf = factors
-    m = GicTipsyMap()
+    m = GicParticleMap()
     m.nlevels = len(levels)
     for l, (_, n, _) in enumerate(levels):
         m.n[l] = n
@@ -136,3 +136,36 @@ def test_tipsy_map_errors(built):
     rc, _ = pack_host(lib, m, pos, pos, first=60, count=5)
     assert rc == _lib.GIC_ERR_INVALID_ARG
     assert lib.gic_tipsy_count(ctypes.byref(m), ctypes.byref(cnt)) == 0 and cnt.value == 64
+
+
+def test_gadget_blocks_match_reference_file_and_oracle(built, zoom2_particles):
+    from genetic_gb300 import _lib
+    lib = _lib.load()
+    g = np.load(os.path.join(GOLDEN, 'gadget_zoom2.npz'))
+    z = zoom2_particles
+    n = len(z['order'][1])
+    assert int(g['npart'][1]) == n
+    want_pos, want_vel, want_mass = fo.gadget_blocks(z['order'], z['pos'], z['vel'], z['factors'][0])
+    # the oracle against the reference's file: masses exact, positions (Mpc/h, < 50) and
+    # velocities to one float rounding step
+    assert np.array_equal(want_mass, g['mass'])
+    assert np.abs(want_pos - g['pos']).max() <= 4e-6
+    assert np.abs(want_vel - g['vel']).max() <= 1e-6 * np.abs(g['vel']).max()
+    # the C ABI's host packer against the oracle, bit for bit
+    m = make_map(ZOOM2, z['replaced'], z['factors'])
+    pos = np.zeros((n, 3), np.float32)
+    vel = np.zeros((n, 3), np.float32)
+    ids = np.zeros(n, np.uint64)
+    mass = np.zeros(n, np.float32)
+    P = ctypes.POINTER(ctypes.c_double)
+    pp = (P * 2)(*[np.ascontiguousarray(p).ctypes.data_as(P) for p in z['pos']])
+    vv = (P * 2)(*[np.ascontiguousarray(v).ctypes.data_as(P) for v in z['vel']])
+    ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    assert lib.gic_gadget_pack_host(ctypes.byref(m), pp, vv, 0, n, ptr(pos), ptr(vel), ptr(ids), ptr(mass), 3) == 0
+    assert np.array_equal(pos.view(np.uint32), want_pos.view(np.uint32))
+    assert np.array_equal(vel.view(np.uint32), want_vel.view(np.uint32))
+    assert np.array_equal(mass, want_mass) and np.array_equal(ids, np.arange(n, dtype=np.uint64))
+    # ids alone, for a window
+    ids2 = np.zeros(10, np.uint64)
+    assert lib.gic_gadget_pack_host(ctypes.byref(m), None, None, 500, 10, None, None, ptr(ids2), None, 1) == 0
+    assert np.array_equal(ids2, np.arange(500, 510, dtype=np.uint64))
