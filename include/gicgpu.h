@@ -3,8 +3,10 @@
  * The library replaces genetIC's field-realisation hot path: white-noise drawing,
  * multiplication by sqrt(P(k)), inter-level filtering and zoom combination, the
  * modification (constraint) projections and Zel'dovich displacements/velocities.
- * genetIC's host (paramfile parser, grid geometry, particle mappers and the
- * Gadget/grafIC/tipsy writers) stays as it is and calls these entry points.
+ * genetIC's host (paramfile parser, grid geometry, particle mappers, file
+ * headers and the grafIC writer) stays as it is and calls these entry points;
+ * the tipsy and gadget writers' particle loops can use gic_tipsy_pack* and
+ * gic_gadget_pack_host.
  *
  * Conventions (same as genetIC):
  *   - real-space index (x*N + y)*N + z, z fastest (genetIC/src/simulation/grid/grid.hpp:610-626);
