@@ -131,38 +131,26 @@ def tipsy_map(wl):
     _, L, n0 = levels[0]
     if len(levels) > 2 or n0 > 1024:
         return None, None
-    m = GicParticleMap()
-    m.nlevels = len(levels)
-    m.n[0] = n0
+    lv = [(n0, 1, (0, 0, 0))]
     dx = [L / n0]
     counts = [n0 ** 3]
-    m.ratio = 1
     rep = np.zeros(0, dtype=np.uint64)
     if len(levels) == 2:
         _, ox, oy, oz, factor, n1 = levels[1]
         span = n0 // factor
-        m.n[1] = n1
-        m.ratio = factor * n1 // n0
-        m.origin[0], m.origin[1], m.origin[2] = ox, oy, oz
+        ratio = factor * n1 // n0
+        lv.append((n1, ratio, (ox, oy, oz)))
         ax = [(o + np.arange(span)) % n0 for o in (ox, oy, oz)]
         rep = np.sort(((ax[0][:, None, None] * n0 + ax[1][None, :, None]) * n0 + ax[2][None, None, :]).ravel())
-        rep = rep.astype(np.uint64)
         dx.append(L / factor / n1)
-        counts = [n0 ** 3 - len(rep), len(rep) * m.ratio ** 3]
+        counts = [n0 ** 3 - len(rep), len(rep) * ratio ** 3]
     om, h = COSMO['omega_m'], COSMO['hubble']
     a = 1.0 / (1.0 + COSMO['redshift'])
     mass = [27.744948 * om * L ** 3 * (d / L) ** 3 for d in dx]
     tot = sum(c * ms for c, ms in zip(counts, mass))
-    m.mass_factor = om / tot
-    m.pos_factor = 1.0 / L
-    kms = np.sqrt(4.3022682e-6 * (1e10 / h / m.mass_factor) / (L * 1000 / h))
-    m.vel_factor = a ** -0.5 / kms
-    for l, d in enumerate(dx):
-        m.mass[l] = mass[l]
-        m.eps[l] = d * 0.01075
-    m._rep = rep  # keep alive
-    m.replaced = rep.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong))
-    m.n_replaced = len(rep)
+    mass_factor = om / tot
+    kms = np.sqrt(4.3022682e-6 * (1e10 / h / mass_factor) / (L * 1000 / h))
+    m = GicParticleMap.of(lv, [rep], mass, [d * 0.01075 for d in dx], 1.0 / L, a ** -0.5 / kms, mass_factor)
     return m, sum(counts)
 
 
@@ -589,7 +577,7 @@ def main():
             t_tipsy = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
             n0 = wl['levels'][0][2]
             e2e_tipsy = {'value': round(ntot * world / t_tipsy / 1e6, 3), 'unit': 'Mparticles/s',
-                         'h2d_bytes_per_step': int(8 * tmap.n_replaced + 16 * n0 * n0 + 8),
+                         'h2d_bytes_per_step': int(8 * tmap.n_replaced[0] + 16 * n0 * n0 + 8),
                          'd2h_bytes_per_step': int(recs.nbytes)}
             del recs
     except Exception as e:  # reported, never fatal to the benchmark line

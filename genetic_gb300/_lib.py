@@ -61,12 +61,39 @@ _D = ctypes.POINTER(ctypes.c_double)
 _I = ctypes.c_int
 
 
+GIC_MAP_MAX_LEVELS = 8
+
+
 class GicParticleMap(ctypes.Structure):
-    """gic_particle_map: the particles of one level or a two-level zoom in genetIC's mapper order."""
-    _fields_ = [('nlevels', ctypes.c_int), ('n', ctypes.c_int * 2), ('ratio', ctypes.c_int),
-                ('origin', ctypes.c_int * 3), ('replaced', ctypes.POINTER(ctypes.c_ulonglong)),
-                ('n_replaced', ctypes.c_ulonglong), ('mass', ctypes.c_double * 2), ('eps', ctypes.c_double * 2),
+    """gic_particle_map: the particles of a multi-level context in genetIC's mapper order."""
+    _fields_ = [('nlevels', ctypes.c_int), ('n', ctypes.c_int * GIC_MAP_MAX_LEVELS),
+                ('ratio', ctypes.c_int * GIC_MAP_MAX_LEVELS), ('origin', (ctypes.c_int * 3) * GIC_MAP_MAX_LEVELS),
+                ('replaced', ctypes.POINTER(ctypes.c_ulonglong) * GIC_MAP_MAX_LEVELS),
+                ('n_replaced', ctypes.c_ulonglong * GIC_MAP_MAX_LEVELS),
+                ('mass', ctypes.c_double * GIC_MAP_MAX_LEVELS), ('eps', ctypes.c_double * GIC_MAP_MAX_LEVELS),
                 ('pos_factor', ctypes.c_double), ('vel_factor', ctypes.c_double), ('mass_factor', ctypes.c_double)]
+
+    @classmethod
+    def of(cls, levels, replaced, mass, eps, pos_factor, vel_factor, mass_factor):
+        """levels: [(n, ratio, (ox, oy, oz))] (ratio and origin unused on level 0);
+        replaced: one array of ascending cell ids per level (the finest empty)."""
+        import numpy as np
+        m = cls()
+        m.nlevels = len(levels)
+        m._keep = []
+        for l, (n, ratio, origin) in enumerate(levels):
+            m.n[l] = n
+            m.ratio[l] = ratio
+            for a in range(3):
+                m.origin[l][a] = origin[a]
+            rep = np.ascontiguousarray(replaced[l] if l < len(replaced) else [], dtype=np.uint64)
+            m._keep.append(rep)
+            m.replaced[l] = rep.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong))
+            m.n_replaced[l] = len(rep)
+            m.mass[l] = mass[l]
+            m.eps[l] = eps[l]
+        m.pos_factor, m.vel_factor, m.mass_factor = pos_factor, vel_factor, mass_factor
+        return m
 # symbol -> argument types (all return int unless noted)
 SIGNATURES = {
     'gic_create': [ctypes.POINTER(_P), ctypes.POINTER(GicDeviceOpts)],

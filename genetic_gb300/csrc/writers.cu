@@ -21,6 +21,7 @@ namespace gic {
 namespace {
 
 constexpr int kRowWords = 32;  // a row of at most 1024 cells as a bit mask
+constexpr int kMaxLevels = GIC_MAP_MAX_LEVELS;
 
 // the map as the kernels and the host loops read it
 struct MapView {
@@ -30,7 +31,7 @@ struct MapView {
 };
 
 struct TipsyConst {
-  double mass[2], eps[2], pf, vf, mf;
+  double mass[kMaxLevels], eps[kMaxLevels], pf, vf, mf;
 };
 
 __host__ __device__ inline int popc32(unsigned v) {
@@ -66,21 +67,27 @@ __host__ __device__ inline int row_rank(const unsigned *w, const int *pre, int z
   return z - pre[k] - popc32(w[k] & (bit - 1u));
 }
 
-// level-1 cell of the j-th fine particle (j < n_replaced * ratio^3)
-__host__ __device__ inline unsigned long long fine_cell(const MapView &m, unsigned long long j) {
-  const unsigned long long parent = m.replaced[j / m.per_block];
-  const unsigned s = (unsigned)(j % m.per_block), r = (unsigned)m.ratio;
-  const long long n0 = m.n0;
+// cell s (x, y, z ascending) of the ratio^3 block that parent cell `parent` of a grid of
+// np cells per side covers on a grid of nc cells whose corner is parent cell `org`
+__host__ __device__ inline unsigned long long block_cell(int np, int nc, int ratio, const int *org,
+                                                        unsigned long long parent, unsigned s) {
+  const unsigned r = (unsigned)ratio;
+  const long long n0 = np;
   long long p[3] = {(long long)(parent / (unsigned long long)(n0 * n0)), (long long)((parent / n0) % n0),
                     (long long)(parent % n0)};
   for (int a = 0; a < 3; ++a) {
-    p[a] -= m.org[a];
+    p[a] -= org[a];
     if (p[a] < 0) p[a] += n0;
   }
   const unsigned long long fx = (unsigned long long)p[0] * r + s / (r * r);
   const unsigned long long fy = (unsigned long long)p[1] * r + (s / r) % r;
   const unsigned long long fz = (unsigned long long)p[2] * r + s % r;
-  return (fx * m.n1 + fy) * m.n1 + fz;
+  return (fx * (unsigned long long)nc + fy) * (unsigned long long)nc + fz;
+}
+
+// level-1 cell of the j-th fine particle (j < n_replaced * ratio^3)
+__host__ __device__ inline unsigned long long fine_cell(const MapView &m, unsigned long long j) {
+  return block_cell(m.n0, m.n1, m.ratio, m.org, m.replaced[j / m.per_block], (unsigned)(j % m.per_block));
 }
 
 template <typename V>
@@ -99,55 +106,116 @@ __host__ __device__ inline void tipsy_record(gic_tipsy_dark &o, const double *po
   o.phi = 0.f;
 }
 
-// the map's view, checked; replaced cells must lie under the level-1 grid, as
-// TwoLevelParticleMapper requires (calculateHiresParticleList throws otherwise)
-MapView check_map(const gic_particle_map *m) {
+// every level of a map, checked: replaced cells ascending, each under the next level's
+// grid (TwoLevelParticleMapper's calculateHiresParticleList throws otherwise) and under a
+// replaced cell of the level above (its consistency assertion, twolevelmapper.hpp:287-302)
+struct LevelMap {
+  int n, ratio, org[3];
+  const unsigned long long *rep;
+  unsigned long long nrep;
+};
+struct MapFull {
+  int nlevels;
+  LevelMap lv[kMaxLevels];
+  unsigned long long total;
+};
+
+bool contains(const unsigned long long *a, unsigned long long n, unsigned long long v) {
+  return std::binary_search(a, a + n, v);
+}
+
+MapFull check_full(const gic_particle_map *m) {
   if (!m) fail(GIC_ERR_INVALID_ARG, "null map");
-  MapView v{};
-  v.nlevels = m->nlevels;
-  if (v.nlevels != 1 && v.nlevels != 2) fail(GIC_ERR_INVALID_ARG, "a tipsy map has one or two levels");
-  v.n0 = m->n[0];
-  if (v.n0 < 1 || v.n0 > 32 * kRowWords) fail(GIC_ERR_INVALID_ARG, "level 0 needs 1 to 1024 cells per side");
-  const unsigned long long n03 = (unsigned long long)v.n0 * v.n0 * v.n0;
-  v.ratio = 1;
-  v.per_block = 1;
-  if (v.nlevels == 1) {
-    if (m->n_replaced) fail(GIC_ERR_INVALID_ARG, "a single level replaces no cells");
-    v.n_kept = n03;
-    return v;
+  MapFull f{};
+  f.nlevels = m->nlevels;
+  if (f.nlevels < 1 || f.nlevels > kMaxLevels) fail(GIC_ERR_INVALID_ARG, "a particle map has 1 to 8 levels");
+  for (int l = 0; l < f.nlevels; ++l) {
+    LevelMap &L = f.lv[l];
+    L.n = m->n[l];
+    if (L.n < 1 || (l == 0 && L.n > 32 * kRowWords)) fail(GIC_ERR_INVALID_ARG, "level 0 needs 1 to 1024 cells per side");
+    L.ratio = l ? m->ratio[l] : 1;
+    if (l) {
+      const LevelMap &P = f.lv[l - 1];
+      if (L.ratio < 1 || L.n < L.ratio || L.n % L.ratio)
+        fail(GIC_ERR_INVALID_ARG, "each zoom level needs a multiple of its ratio cells per side");
+      for (int a = 0; a < 3; ++a) {
+        L.org[a] = m->origin[l][a];
+        if (L.org[a] < 0 || L.org[a] >= P.n) fail(GIC_ERR_INVALID_ARG, "a level's origin is a cell coordinate of the level above");
+      }
+    }
+    L.nrep = m->n_replaced[l];
+    L.rep = m->replaced[l];
+    const unsigned long long n3 = (unsigned long long)L.n * L.n * L.n;
+    if (L.nrep && (l == f.nlevels - 1)) fail(GIC_ERR_INVALID_ARG, "the finest level replaces no cells");
+    if (L.nrep > n3 || (L.nrep && !L.rep)) fail(GIC_ERR_INVALID_ARG, "bad list of replaced cells");
   }
-  v.n1 = m->n[1];
-  v.ratio = m->ratio;
-  if (v.ratio < 1 || v.n1 < v.ratio || v.n1 % v.ratio) fail(GIC_ERR_INVALID_ARG, "level 1 needs a multiple of ratio cells per side");
-  for (int a = 0; a < 3; ++a) {
-    v.org[a] = m->origin[a];
-    if (v.org[a] < 0 || v.org[a] >= v.n0) fail(GIC_ERR_INVALID_ARG, "the level-1 origin is a level-0 cell coordinate");
-  }
-  v.n_replaced = m->n_replaced;
-  if (v.n_replaced > n03 || (v.n_replaced && !m->replaced)) fail(GIC_ERR_INVALID_ARG, "bad list of replaced cells");
-  v.replaced = m->replaced;
-  const long long span = v.n1 / v.ratio, n0 = v.n0;
-  for (unsigned long long k = 0; k < v.n_replaced; ++k) {
-    const unsigned long long c = v.replaced[k];
-    if (c >= n03 || (k && c <= v.replaced[k - 1]))
-      fail(GIC_ERR_INVALID_ARG, "replaced cells must be ascending level-0 cell ids");
-    const long long p[3] = {(long long)(c / (unsigned long long)(n0 * n0)), (long long)((c / n0) % n0), (long long)(c % n0)};
-    for (int a = 0; a < 3; ++a) {
-      long long d = p[a] - v.org[a];
-      if (d < 0) d += n0;
-      if (d >= span) fail(GIC_ERR_INVALID_ARG, "Requested zoom region falls outside high resolution grid");
+  for (int l = 0; l + 1 < f.nlevels; ++l) {
+    const LevelMap &L = f.lv[l], &C = f.lv[l + 1];
+    const unsigned long long n3 = (unsigned long long)L.n * L.n * L.n;
+    const long long span = C.n / C.ratio, n0 = L.n;
+    for (unsigned long long k = 0; k < L.nrep; ++k) {
+      const unsigned long long c = L.rep[k];
+      if (c >= n3 || (k && c <= L.rep[k - 1])) fail(GIC_ERR_INVALID_ARG, "replaced cells must be ascending cell ids");
+      const long long p[3] = {(long long)(c / (unsigned long long)(n0 * n0)), (long long)((c / n0) % n0), (long long)(c % n0)};
+      for (int a = 0; a < 3; ++a) {
+        long long d = p[a] - C.org[a];
+        if (d < 0) d += n0;
+        if (d >= span) fail(GIC_ERR_INVALID_ARG, "Requested zoom region falls outside high resolution grid");
+      }
+      if (l) {
+        // the parent on level l-1 must itself be replaced: the cell is a particle of the mapper
+        const LevelMap &P = f.lv[l - 1];
+        const long long q[3] = {(p[0] / L.ratio + L.org[0]) % P.n, (p[1] / L.ratio + L.org[1]) % P.n,
+                                (p[2] / L.ratio + L.org[2]) % P.n};
+        const unsigned long long parent = ((unsigned long long)q[0] * P.n + q[1]) * P.n + q[2];
+        if (!contains(P.rep, P.nrep, parent))
+          fail(GIC_ERR_INVALID_ARG, "a replaced cell is not a particle of the level above's zoom");
+      }
     }
   }
-  v.n_kept = n03 - v.n_replaced;
-  v.per_block = (unsigned long long)v.ratio * v.ratio * v.ratio;
+  // particles per level: level 0's cells, or the blocks of the level above, less those replaced
+  f.total = 0;
+  for (int l = 0; l < f.nlevels; ++l) {
+    const LevelMap &L = f.lv[l];
+    const unsigned long long have =
+        l ? f.lv[l - 1].nrep * (unsigned long long)L.ratio * L.ratio * L.ratio : (unsigned long long)L.n * L.n * L.n;
+    f.total += have - L.nrep;
+  }
+  return f;
+}
+
+// the one- or two-level view the streaming host loop and the kernels use
+MapView view2(const MapFull &f) {
+  MapView v{};
+  v.nlevels = f.nlevels;
+  v.n0 = f.lv[0].n;
+  v.ratio = 1;
+  v.per_block = 1;
+  const unsigned long long n03 = (unsigned long long)v.n0 * v.n0 * v.n0;
+  v.n_kept = n03;
+  if (f.nlevels == 2) {
+    v.n1 = f.lv[1].n;
+    v.ratio = f.lv[1].ratio;
+    for (int a = 0; a < 3; ++a) v.org[a] = f.lv[1].org[a];
+    v.n_replaced = f.lv[0].nrep;
+    v.replaced = f.lv[0].rep;
+    v.n_kept = n03 - v.n_replaced;
+    v.per_block = (unsigned long long)v.ratio * v.ratio * v.ratio;
+  }
   return v;
+}
+
+MapView check_map(const gic_particle_map *m) {
+  const MapFull f = check_full(m);
+  if (f.nlevels > 2) fail(GIC_ERR_INVALID_ARG, "the device packer takes maps of one or two levels");
+  return view2(f);
 }
 
 unsigned long long map_size(const MapView &v) { return v.n_kept + v.n_replaced * v.per_block; }
 
 TipsyConst tipsy_const(const gic_particle_map *m) {
   TipsyConst c{};
-  for (int l = 0; l < 2; ++l) {
+  for (int l = 0; l < kMaxLevels; ++l) {
     c.mass[l] = m->mass[l];
     c.eps[l] = m->eps[l];
   }
@@ -223,6 +291,54 @@ void for_each_particle(const MapView &v, unsigned long long first, unsigned long
   for (auto &th : pool) th.join();
 }
 
+// the mapper order of three or more levels, written out: level 0's cells, then per zoom
+// level the order so far without the replaced cells of the level above, followed by
+// the blocks of those cells in ascending id
+void build_order(const MapFull &f, std::vector<unsigned char> &lev, std::vector<unsigned long long> &cell) {
+  const unsigned long long n3 = (unsigned long long)f.lv[0].n * f.lv[0].n * f.lv[0].n;
+  lev.assign(n3, 0);
+  cell.resize(n3);
+  for (unsigned long long c = 0; c < n3; ++c) cell[c] = c;
+  for (int l = 1; l < f.nlevels; ++l) {
+    const LevelMap &P = f.lv[l - 1], &L = f.lv[l];
+    size_t w = 0;
+    for (size_t i = 0; i < cell.size(); ++i)
+      if (!(lev[i] == l - 1 && contains(P.rep, P.nrep, cell[i]))) {
+        lev[w] = lev[i];
+        cell[w] = cell[i];
+        ++w;
+      }
+    lev.resize(w);
+    cell.resize(w);
+    const unsigned per = (unsigned)(L.ratio * L.ratio * L.ratio);
+    for (unsigned long long k = 0; k < P.nrep; ++k)
+      for (unsigned s = 0; s < per; ++s) {
+        lev.push_back((unsigned char)l);
+        cell.push_back(block_cell(P.n, L.n, L.ratio, L.org, P.rep[k], s));
+      }
+  }
+}
+
+// every particle of [first, first + count) of any map in mapper order: f(o, level, cell)
+template <typename F>
+void for_each_particle_full(const MapFull &mf, unsigned long long first, unsigned long long count, int threads,
+                            const F &f) {
+  if (mf.nlevels <= 2) {
+    for_each_particle(view2(mf), first, count, threads, f);
+    return;
+  }
+  std::vector<unsigned char> lev;
+  std::vector<unsigned long long> cell;
+  build_order(mf, lev, cell);
+  int nt = threads > 0 ? threads : (int)std::max(1u, std::thread::hardware_concurrency());
+  std::vector<std::thread> pool;
+  for (int t = 0; t < nt; ++t)
+    pool.emplace_back([&, t] {
+      for (unsigned long long o = first + count * t / nt; o < first + count * (t + 1) / nt; ++o) f(o, lev[o], cell[o]);
+    });
+  for (auto &th : pool) th.join();
+}
+
 template <typename V>
 __global__ void k_tipsy_kept(gic_tipsy_dark *out, unsigned long long first, unsigned long long count, MapView v,
                              const unsigned long long *rep_begin, const unsigned long long *kept_before, const double *pos,
@@ -267,23 +383,23 @@ __global__ void k_tipsy_fine(gic_tipsy_dark *out, unsigned long long first, unsi
 
 }  // namespace
 
-unsigned long long tipsy_count(const gic_particle_map *m) { return map_size(check_map(m)); }
+unsigned long long tipsy_count(const gic_particle_map *m) { return check_full(m).total; }
 
-static void check_window(const MapView &v, unsigned long long first, unsigned long long count, const void *out) {
-  const unsigned long long total = map_size(v);
+static void check_window(unsigned long long total, unsigned long long first, unsigned long long count, const void *out) {
   if (first > total || count > total - first) fail(GIC_ERR_INVALID_ARG, "records outside the map");
   if (count && !out) fail(GIC_ERR_INVALID_ARG, "null output");
 }
 
 void tipsy_pack_host(const gic_particle_map *m, const double *const *pos, const double *const *vel, unsigned long long first,
                      unsigned long long count, gic_tipsy_dark *out, int threads) {
-  const MapView v = check_map(m);
-  check_window(v, first, count, out);
-  if (!pos || !vel || !pos[0] || !vel[0] || (v.nlevels == 2 && (!pos[1] || !vel[1])))
-    fail(GIC_ERR_INVALID_ARG, "null particle arrays");
+  const MapFull f = check_full(m);
+  check_window(f.total, first, count, out);
+  bool ok = pos && vel;
+  for (int l = 0; ok && l < f.nlevels; ++l) ok = pos[l] && vel[l];
+  if (!ok) fail(GIC_ERR_INVALID_ARG, "null particle arrays");
   if (!count) return;
   const TipsyConst c = tipsy_const(m);
-  for_each_particle(v, first, count, threads, [&](unsigned long long o, int l, unsigned long long cell) {
+  for_each_particle_full(f, first, count, threads, [&](unsigned long long o, int l, unsigned long long cell) {
     tipsy_record(out[o - first], pos[l], vel[l], cell, l, c);
   });
 }
@@ -291,15 +407,20 @@ void tipsy_pack_host(const gic_particle_map *m, const double *const *pos, const 
 void gadget_pack_host(const gic_particle_map *m, const double *const *pos, const double *const *vel,
                       unsigned long long first, unsigned long long count, float *pos_out, float *vel_out,
                       unsigned long long *ids, float *mass_out, int threads) {
-  const MapView v = check_map(m);
+  const MapFull f = check_full(m);
   const void *any = pos_out ? (const void *)pos_out : vel_out ? (const void *)vel_out : ids ? (const void *)ids
                                                                                          : (const void *)mass_out;
-  check_window(v, first, count, any);
-  auto arrays_ok = [&](const double *const *a) { return a && a[0] && (v.nlevels == 1 || a[1]); };
+  check_window(f.total, first, count, any);
+  auto arrays_ok = [&](const double *const *a) {
+    bool ok = a != nullptr;
+    for (int l = 0; ok && l < f.nlevels; ++l) ok = a[l] != nullptr;
+    return ok;
+  };
   if ((pos_out && !arrays_ok(pos)) || (vel_out && !arrays_ok(vel))) fail(GIC_ERR_INVALID_ARG, "null particle arrays");
   if (!count) return;
-  const float mass[2] = {(float)m->mass[0], (float)m->mass[1]};
-  for_each_particle(v, first, count, threads, [&](unsigned long long o, int l, unsigned long long cell) {
+  float mass[kMaxLevels];
+  for (int l = 0; l < kMaxLevels; ++l) mass[l] = (float)m->mass[l];
+  for_each_particle_full(f, first, count, threads, [&](unsigned long long o, int l, unsigned long long cell) {
     const unsigned long long k = o - first;
     for (int a = 0; a < 3; ++a) {
       if (pos_out) pos_out[3 * k + a] = (float)pos[l][3 * cell + a];
@@ -331,7 +452,7 @@ static void launch_tipsy(Context &C, const MapView &dv, const TipsyConst &c, uns
 void tipsy_pack_device(Context &C, const gic_particle_map *m, unsigned long long first, unsigned long long count,
                        gic_tipsy_dark *host_out) {
   const MapView v = check_map(m);
-  check_window(v, first, count, host_out);
+  check_window(map_size(v), first, count, host_out);
   if ((int)C.levels.size() < v.nlevels) fail(GIC_ERR_NOT_READY, "the map has more levels than the context");
   for (int l = 0; l < v.nlevels; ++l) {
     const Level &L = *C.levels[l];

@@ -153,24 +153,28 @@ typedef struct {
   float mass, x, y, z, vx, vy, vz, eps, phi;
 } gic_tipsy_dark;
 
-/* The particles of one level, or of a two-level zoom, in genetIC's mapper order
- * (OneLevelParticleMapper; TwoLevelParticleMapper, particles/mapper/twolevelmapper.hpp:262-320):
- * the level-0 cells not in `replaced`, in cell order, then for every replaced
- * level-0 cell (ascending ids, as ICGenerator's zoom mask holds them, ic.hpp:480-569)
- * the ratio^3 level-1 cells it covers, x, y, z ascending (grid.hpp:704-729).
- * origin: the level-1 grid's lower corner in level-0 cells.  mass and eps are the
- * levels' particle mass and softening (ZeldovichParticleEvaluator::getMass/getEps),
- * and the factors TipsyOutput's (tipsy.hpp:217-239): a record holds
+/* The particles of a multi-level context in genetIC's mapper order
+ * (OneLevelParticleMapper; TwoLevelParticleMapper nested once per zoom level, ic.hpp:1150-1185,
+ * particles/mapper/twolevelmapper.hpp:262-320, 869-893): level 0's cells in cell order;
+ * then for each level l >= 1, the order so far less the level-(l-1) cells in
+ * replaced[l-1], followed by, for every cell of replaced[l-1] in ascending id, the
+ * ratio[l]^3 level-l cells it covers, x, y, z ascending (grid.hpp:704-729).
+ * replaced[l] are ascending level-l cell ids (ICGenerator's zoom masks, ic.hpp:480-569),
+ * each under a replaced level-(l-1) cell; the finest level replaces none.
+ * origin[l]: level l's lower corner in level-(l-1) cells.  mass and eps are each
+ * level's particle mass and softening (ZeldovichParticleEvaluator::getMass/getEps),
+ * and the factors TipsyOutput's (tipsy.hpp:217-239): a tipsy record holds
  * mass*mass_factor, pos*pos_factor - 0.5, vel*vel_factor, eps*pos_factor, phi = 0,
  * each product and difference rounded in double, then to float. */
+#define GIC_MAP_MAX_LEVELS 8
 typedef struct {
-  int nlevels;  /* 1 or 2 */
-  int n[2];     /* cells per side of each level (level 0 at most 1024) */
-  int ratio;    /* level-0 cell size / level-1 cell size */
-  int origin[3];
-  const unsigned long long *replaced;
-  unsigned long long n_replaced;
-  double mass[2], eps[2];
+  int nlevels;                        /* 1 to GIC_MAP_MAX_LEVELS */
+  int n[GIC_MAP_MAX_LEVELS];          /* cells per side (level 0 at most 1024) */
+  int ratio[GIC_MAP_MAX_LEVELS];      /* ratio[l]: level-(l-1) cell size / level-l cell size */
+  int origin[GIC_MAP_MAX_LEVELS][3];
+  const unsigned long long *replaced[GIC_MAP_MAX_LEVELS];
+  unsigned long long n_replaced[GIC_MAP_MAX_LEVELS];
+  double mass[GIC_MAP_MAX_LEVELS], eps[GIC_MAP_MAX_LEVELS];
   double pos_factor, vel_factor, mass_factor;
 } gic_particle_map;
 
@@ -178,15 +182,15 @@ typedef struct {
  * context: a failure's message is gic_last_error(NULL). */
 GIC_API int gic_tipsy_count(const gic_particle_map *map, unsigned long long *count);
 
-/* Records [first, first + count) of the map from host particles (pos[l], vel[l]:
- * 3 doubles per cell of level l in cell order, as gic_fetch_particles writes them),
+/* Records [first, first + count) of the map from host particles (pos[l], vel[l] for
+ * every level: 3 doubles per cell in cell order, as gic_fetch_particles writes them),
  * packed by `threads` host threads (0: all cores).  Replaces the packing loop of
  * TipsyOutput::saveNextBlockOfTipsyParticles (tipsy.hpp:109-145). */
 GIC_API int gic_tipsy_pack_host(const gic_particle_map *map, const double *const *pos, const double *const *vel,
                                 unsigned long long first, unsigned long long count, gic_tipsy_dark *out, int threads);
 
 /* The same records packed on the device from the context's particles (after
- * gic_zeldovich; levels 0 and 1 of the context) and copied to host_out: 36 bytes
+ * gic_zeldovich) and copied to host_out, for maps of one or two levels: 36 bytes
  * per particle cross to the host instead of the 48 of gic_fetch_particles. */
 GIC_API int gic_tipsy_pack(gic_ctx *ctx, const gic_particle_map *map, unsigned long long first, unsigned long long count,
                            gic_tipsy_dark *host_out);

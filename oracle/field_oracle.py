@@ -1031,29 +1031,48 @@ def splice_levels(levels, original, new, power, flagged):
 
 # --- tipsy output (genetIC/src/io/tipsy.hpp:109-145, 200-262) ---------------------------
 
+def block_cells(parents, np_, nc, ratio, origin):
+    """For every parent cell (ids on a grid of np_ per side), the ratio^3 cells it covers on
+    the grid of nc per side whose corner is parent cell `origin`, x, y, z ascending
+    (Grid::insertCubeIdsIntoVector, grid.hpp:704-729; iterateOverCube, coordinate.hpp:197-208)."""
+    parents = np.asarray(parents, dtype=np.int64)
+    px, py, pz = parents // (np_ * np_), (parents // np_) % np_, parents % np_
+    px, py, pz = ((px - origin[0]) % np_, (py - origin[1]) % np_, (pz - origin[2]) % np_)
+    s = np.arange(ratio ** 3)
+    sx, sy, sz = s // (ratio * ratio), (s // ratio) % ratio, s % ratio
+    fx = px[:, None] * ratio + sx[None, :]
+    fy = py[:, None] * ratio + sy[None, :]
+    fz = pz[:, None] * ratio + sz[None, :]
+    return ((fx * nc + fy) * nc + fz).ravel()
+
+
+def mapper_order_levels(levels, replaced):
+    """(level, cell) of every particle in genetIC's mapper order for any number of levels:
+    a OneLevelParticleMapper of level 0 wrapped in one TwoLevelParticleMapper per zoom level
+    (ic.hpp:1150-1185; particles/mapper/twolevelmapper.hpp:262-320, 869-893).  Each wrapping
+    drops the replaced cells of the level above from the order so far, then appends the
+    blocks of those cells in ascending cell id.  levels: [(n, ratio, origin)];
+    replaced[l]: level-l cell ids replaced by level l+1."""
+    n0 = levels[0][0]
+    lev = np.zeros(n0 ** 3, dtype=np.int64)
+    cells = np.arange(n0 ** 3, dtype=np.int64)
+    for l in range(1, len(levels)):
+        pn = levels[l - 1][0]
+        n, ratio, origin = levels[l]
+        rep = np.sort(np.asarray(replaced[l - 1], dtype=np.int64))
+        drop = (lev == l - 1) & np.isin(cells, rep)
+        lev, cells = lev[~drop], cells[~drop]
+        fine = block_cells(rep, pn, n, ratio, origin)
+        lev = np.concatenate([lev, np.full(len(fine), l, dtype=np.int64)])
+        cells = np.concatenate([cells, fine])
+    return lev, cells
+
+
 def mapper_order(n0, replaced=(), n1=0, ratio=1, origin=(0, 0, 0)):
-    """(level, cell) of every particle in genetIC's mapper order: the level-0 cells
-    not replaced, in cell order, then for every replaced level-0 cell (ascending) the
-    ratio^3 level-1 cells under it, x, y, z ascending (OneLevelParticleMapper;
-    TwoLevelParticleMapper, particles/mapper/twolevelmapper.hpp:262-320, 869-893;
-    Grid::insertCubeIdsIntoVector, grid.hpp:704-729; iterateOverCube, coordinate.hpp:197-208)."""
-    replaced = np.sort(np.asarray(replaced, dtype=np.int64))
-    keep = np.ones(n0 ** 3, dtype=bool)
-    keep[replaced] = False
-    lev = [np.zeros(int(keep.sum()), dtype=np.int64)]
-    cells = [np.flatnonzero(keep)]
-    if len(replaced):
-        px, py, pz = replaced // (n0 * n0), (replaced // n0) % n0, replaced % n0
-        px, py, pz = ((px - origin[0]) % n0, (py - origin[1]) % n0, (pz - origin[2]) % n0)
-        s = np.arange(ratio ** 3)
-        sx, sy, sz = s // (ratio * ratio), (s // ratio) % ratio, s % ratio
-        fx = px[:, None] * ratio + sx[None, :]
-        fy = py[:, None] * ratio + sy[None, :]
-        fz = pz[:, None] * ratio + sz[None, :]
-        fine = ((fx * n1 + fy) * n1 + fz).ravel()
-        lev.append(np.ones(len(fine), dtype=np.int64))
-        cells.append(fine)
-    return np.concatenate(lev), np.concatenate(cells)
+    """The mapper order of one level, or of two when `replaced` level-0 cells are given."""
+    if len(replaced) == 0:
+        return mapper_order_levels([(n0, 1, (0, 0, 0))], [])
+    return mapper_order_levels([(n0, 1, (0, 0, 0)), (n1, ratio, origin)], [replaced])
 
 
 def tipsy_factors(levels, cosmo, order_levels):

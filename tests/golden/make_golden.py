@@ -325,6 +325,23 @@ def tipsy_goldens():
         np.savez_compressed(os.path.join(HERE, 'tipsy_zoom2.npz'), scalefactor=np.float64(t), header=header, dark=dark)
 
 
+def tipsy3_goldens():
+    """The reference's tipsy file of the three-level zoom3 case: its header and the records
+    of the finest level (the level-1 particles are all replaced), which follow the level-1
+    cell ids of their parents."""
+    with tempfile.TemporaryDirectory() as d:
+        write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+        open(os.path.join(d, 'paramfile.txt'), 'w').write(
+            ZOOM_PARAMS.format(seedcmd='random_seed', zooms='\n'.join(ZOOMS['zoom3']), dumps=''))
+        subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True)
+        raw = open(os.path.join(d, 'out.tipsy'), 'rb').read()
+        header = np.frombuffer(raw[8:28], '<i4').copy()
+        _, _, dark = read_tipsy(os.path.join(d, 'out.tipsy'))
+        first = 32 ** 3 - 216
+        np.savez_compressed(os.path.join(HERE, 'tipsy_zoom3.npz'), header=header, first=np.int64(first),
+                            head=dark[:64].copy(), tail=dark[first:].copy())
+
+
 def read_fortran_records(path):
     """The records of a Fortran-framed binary file (int32 length before and after each)."""
     raw = open(path, 'rb').read()
@@ -380,3 +397,4 @@ if __name__ == '__main__':
     splice_goldens()
     tipsy_goldens()
     gadget_goldens()
+    tipsy3_goldens()

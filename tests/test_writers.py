@@ -17,23 +17,10 @@ ORIGIN = (8, 8, 8)
 
 
 def make_map(levels, replaced, factors, ratio=2, origin=ORIGIN):
+    """A map of one level, or of two with `replaced` level-0 cells."""
     from genetic_gb300._lib import GicParticleMap
-    mass, eps, pf, vf, mf = factors
-    m = GicParticleMap()
-    m.nlevels = len(levels)
-    for l, (_, n, _) in enumerate(levels):
-        m.n[l] = n
-        m.mass[l] = mass[l]
-        m.eps[l] = eps[l]
-    m.ratio = ratio
-    for a in range(3):
-        m.origin[a] = origin[a]
-    rep = np.ascontiguousarray(replaced, dtype=np.uint64)
-    m._rep = rep  # keep alive
-    m.replaced = rep.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong))
-    m.n_replaced = len(rep)
-    m.pos_factor, m.vel_factor, m.mass_factor = pf, vf, mf
-    return m
+    lv = [(n, ratio if l else 1, origin if l else (0, 0, 0)) for l, (_, n, _) in enumerate(levels)]
+    return GicParticleMap.of(lv, [replaced], *factors)
 
 
 def pack_host(lib, m, pos, vel, first=0, count=None, threads=4):
@@ -43,8 +30,8 @@ def pack_host(lib, m, pos, vel, first=0, count=None, threads=4):
         count = total.value - first
     out = np.zeros((count, 9), dtype=np.float32)
     P = ctypes.POINTER(ctypes.c_double)
-    pp = (P * 2)(*[np.ascontiguousarray(p).ctypes.data_as(P) for p in pos] + [None] * (2 - len(pos)))
-    vv = (P * 2)(*[np.ascontiguousarray(v).ctypes.data_as(P) for v in vel] + [None] * (2 - len(vel)))
+    pp = (P * len(pos))(*[np.ascontiguousarray(p).ctypes.data_as(P) for p in pos])
+    vv = (P * len(vel))(*[np.ascontiguousarray(v).ctypes.data_as(P) for v in vel])
     rc = lib.gic_tipsy_pack_host(ctypes.byref(m), pp, vv, first, count, out.ctypes.data_as(ctypes.c_void_p), threads)
     return rc, out
 
@@ -169,3 +156,44 @@ def test_gadget_blocks_match_reference_file_and_oracle(built, zoom2_particles):
     ids2 = np.zeros(10, np.uint64)
     assert lib.gic_gadget_pack_host(ctypes.byref(m), None, None, 500, 10, None, None, ptr(ids2), None, 1) == 0
     assert np.array_equal(ids2, np.arange(500, 510, dtype=np.uint64))
+
+
+ZOOM3 = ZOOM2 + [(12.5, 32, (18.75, 18.75, 18.75))]
+
+
+def test_three_level_tipsy_matches_reference_and_oracle(built, bbks):
+    """Nested mappers: the finest level's blocks follow the level-1 cell ids of their parents."""
+    from conftest import COSMO
+    from genetic_gb300 import _lib
+    from genetic_gb300._lib import GicParticleMap
+    lib = _lib.load()
+    g = np.load(os.path.join(GOLDEN, 'tipsy_zoom3.npz'))
+    w = fo.white_noise_levels([l[1] for l in ZOOM3], 8896131, 2)
+    out = fo.zoom_realisation(w, ZOOM3, fo.CambPower(bbks, COSMO))
+    ratio = fo.velocity_to_offset_ratio(COSMO)
+    pv = [fo.particles(out[l][1:4], b, off, ZOOM3[0][0], ratio) for l, (b, n, off) in enumerate(ZOOM3)]
+    levels = [(32, 1, (0, 0, 0)), (32, 2, (8, 8, 8)), (32, 2, (8, 8, 8))]
+    # level 0's flagged cube, and its cells' blocks on level 1 (genetIC carries the flags down)
+    rep0 = fo.flag_cells(fo.Levels(ZOOM3), 0, (25., 25., 25.), 'cube', 10)
+    rep1 = np.sort(fo.block_cells(rep0, 32, 32, 2, (8, 8, 8)))
+    order = fo.mapper_order_levels(levels, [rep0, rep1])
+    factors = fo.tipsy_factors(ZOOM3, COSMO, order[0])
+    want = fo.tipsy_records(order, [p for p, _ in pv], [v for _, v in pv], *factors)
+    assert len(want) == int(g['header'][0])
+    first = int(g['first'])
+    ref = np.concatenate([g['head'], g['tail']])
+    mine = np.concatenate([want[:len(g['head'])], want[first:]])
+    assert np.array_equal(mine[:, 0], ref[:, 0]) and np.array_equal(mine[:, 7:], ref[:, 7:])
+    assert np.abs(mine[:, 1:4] - ref[:, 1:4]).max() <= 6e-8
+    assert np.abs(mine[:, 4:7] - ref[:, 4:7]).max() <= 2e-7 * np.abs(ref[:, 4:7]).max()
+    # the host packer against the oracle, bit for bit
+    m = GicParticleMap.of(levels, [rep0, rep1, []], *factors)
+    cnt = ctypes.c_ulonglong()
+    assert lib.gic_tipsy_count(ctypes.byref(m), ctypes.byref(cnt)) == 0 and cnt.value == len(want)
+    rc, got = pack_host(lib, m, [p for p, _ in pv], [v for _, v in pv])
+    assert rc == 0 and np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    rc, part = pack_host(lib, m, [p for p, _ in pv], [v for _, v in pv], first=first - 7, count=1000, threads=3)
+    assert rc == 0 and np.array_equal(part.view(np.uint32), want[first - 7:first + 993].view(np.uint32))
+    # a level-1 cell that is not under a replaced level-0 cell is refused
+    bad = GicParticleMap.of(levels, [rep0, np.array([0])], *factors)
+    assert lib.gic_tipsy_count(ctypes.byref(bad), ctypes.byref(cnt)) == _lib.GIC_ERR_INVALID_ARG
