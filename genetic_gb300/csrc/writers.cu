@@ -1,16 +1,20 @@
-// Tipsy particle records of one level or a two-level zoom, in genetIC's particle-mapper
-// order, packed on the host (threads) or on the device.
+// Particle output in genetIC's particle-mapper order: tipsy records packed on the device
+// (one level or a two-level zoom) or by host threads (any depth), and gadget blocks packed
+// by host threads.
 //
-// The records are TipsyParticle::dark (genetIC/src/io/tipsy.hpp:61-63) as
+// The tipsy records are TipsyParticle::dark (genetIC/src/io/tipsy.hpp:61-63) as
 // TipsyOutput::saveNextBlockOfTipsyParticles fills them (tipsy.hpp:109-145):
 //   mass = m * mass_factor, (x, y, z) = pos * pos_factor - 0.5, eps = soft * pos_factor,
 //   (vx, vy, vz) = vel * vel_factor, phi = 0,
 // each product and difference rounded in double (no fused multiply-add) and then to float.
-// The order is that of OneLevelParticleMapper (cell order) and TwoLevelParticleMapper
+// The gadget blocks are GadgetOutput's (io/gadget.hpp:481-520) for one particle type:
+// Coordinate<float> of positions and velocities, the map index as id, float masses.
+// The order is that of OneLevelParticleMapper (cell order) and of TwoLevelParticleMapper
 // (genetIC/src/simulation/particles/mapper/twolevelmapper.hpp:262-320, 869-893): the
 // level-0 cells that are not replaced, in cell order, then for every replaced level-0
 // cell in ascending order the r^3 level-1 cells it covers, x, y, z ascending
 // (Grid::insertCubeIdsIntoVector, grid.hpp:704-729, iterateOverCube, coordinate.hpp:197-208).
+// Deeper zooms nest one TwoLevelParticleMapper per level (ic.hpp:1150-1185).
 #include "gic_internal.h"
 
 #include <algorithm>
