@@ -387,6 +387,13 @@ int gic_tipsy_count(const gic_particle_map *map, unsigned long long *count) {
   HOST_END
 }
 
+int gic_tipsy_factors(const gic_particle_map *map, double omega_m, double hubble, double scalefactor, double box,
+                      double *pos_factor, double *vel_factor, double *mass_factor) {
+  HOST_BEGIN
+  gic::tipsy_factors(map, omega_m, hubble, scalefactor, box, pos_factor, vel_factor, mass_factor);
+  HOST_END
+}
+
 int gic_tipsy_pack_host(const gic_particle_map *map, const double *const *pos, const double *const *vel,
                         unsigned long long first, unsigned long long count, gic_tipsy_dark *out, int threads) {
   HOST_BEGIN

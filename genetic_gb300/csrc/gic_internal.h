@@ -378,6 +378,8 @@ void make_particles(Context &ctx, Level &L, int order = 1);
 namespace gic {
 // tipsy records (writers.cu)
 unsigned long long tipsy_count(const gic_particle_map *m);
+void tipsy_factors(const gic_particle_map *m, double omega_m, double hubble, double scalefactor, double box,
+                   double *pos_factor, double *vel_factor, double *mass_factor);
 void tipsy_pack_host(const gic_particle_map *m, const double *const *pos, const double *const *vel, unsigned long long first,
                      unsigned long long count, gic_tipsy_dark *out, int threads);
 void gadget_pack_host(const gic_particle_map *m, const double *const *pos, const double *const *vel,

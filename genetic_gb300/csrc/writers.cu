@@ -389,6 +389,30 @@ __global__ void k_tipsy_fine(gic_tipsy_dark *out, unsigned long long first, unsi
 
 unsigned long long tipsy_count(const gic_particle_map *m) { return check_full(m).total; }
 
+// TipsyOutput's factors (tipsy.hpp:200-239): the particle masses summed one by one in
+// mapper order (where each level's particles form one run, in level order), then
+// mass_factor = Om / sum, pos_factor = 1 / box, vel_factor = a^-1/2 / dKmsUnit
+void tipsy_factors(const gic_particle_map *m, double omega_m, double hubble, double scalefactor, double box,
+                   double *pos_factor, double *vel_factor, double *mass_factor) {
+  const MapFull f = check_full(m);
+  if (!(box > 0) || !(hubble > 0) || !(scalefactor > 0)) fail(GIC_ERR_INVALID_ARG, "box, hubble and a must be positive");
+  double tot = 0;
+  for (int l = 0; l < f.nlevels; ++l) {
+    const LevelMap &L = f.lv[l];
+    const unsigned long long have =
+        l ? f.lv[l - 1].nrep * (unsigned long long)L.ratio * L.ratio * L.ratio : (unsigned long long)L.n * L.n * L.n;
+    const double ml = m->mass[l];
+    for (unsigned long long i = 0; i < have - L.nrep; ++i) tot += ml;
+  }
+  const double mf = omega_m / tot;
+  const double kpc = box * 1000 / hubble;
+  const double msol = 1e10 / hubble / mf;
+  const double kms = std::sqrt(4.3022682e-6 * msol / kpc);
+  if (mass_factor) *mass_factor = mf;
+  if (pos_factor) *pos_factor = 1. / box;
+  if (vel_factor) *vel_factor = std::pow(scalefactor, -0.5) / kms;
+}
+
 static void check_window(unsigned long long total, unsigned long long first, unsigned long long count, const void *out) {
   if (first > total || count > total - first) fail(GIC_ERR_INVALID_ARG, "records outside the map");
   if (count && !out) fail(GIC_ERR_INVALID_ARG, "null output");

@@ -182,6 +182,14 @@ typedef struct {
  * context: a failure's message is gic_last_error(NULL). */
 GIC_API int gic_tipsy_count(const gic_particle_map *map, unsigned long long *count);
 
+/* TipsyOutput's factors for the map (tipsy.hpp:200-239), ignoring the map's own factor
+ * fields: the levels' masses summed one by one in mapper order, mass_factor = omega_m /
+ * sum, pos_factor = 1 / box (level 0's side), vel_factor = scalefactor^-1/2 / dKmsUnit
+ * with dKmsUnit = sqrt(4.3022682e-6 dMsolUnit / dKpcUnit), dKpcUnit = box 1000 / hubble,
+ * dMsolUnit = 1e10 / hubble / mass_factor.  Failures: gic_last_error(NULL). */
+GIC_API int gic_tipsy_factors(const gic_particle_map *map, double omega_m, double hubble, double scalefactor,
+                              double box, double *pos_factor, double *vel_factor, double *mass_factor);
+
 /* Records [first, first + count) of the map from host particles (pos[l], vel[l] for
  * every level: 3 doubles per cell in cell order, as gic_fetch_particles writes them),
  * packed by `threads` host threads (0: all cores).  Replaces the packing loop of

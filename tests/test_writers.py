@@ -197,3 +197,18 @@ def test_three_level_tipsy_matches_reference_and_oracle(built, bbks):
     # a level-1 cell that is not under a replaced level-0 cell is refused
     bad = GicParticleMap.of(levels, [rep0, np.array([0])], *factors)
     assert lib.gic_tipsy_count(ctypes.byref(bad), ctypes.byref(cnt)) == _lib.GIC_ERR_INVALID_ARG
+
+
+def test_tipsy_factors_match_oracle(built, zoom2_particles):
+    """TipsyOutput's factors, the masses summed one by one in mapper order: exactly the oracle's."""
+    from conftest import COSMO
+    from genetic_gb300 import _lib
+    lib = _lib.load()
+    z = zoom2_particles
+    mass, eps, pf, vf, mf = z['factors']
+    m = make_map(ZOOM2, z['replaced'], (mass, eps, 0.0, 0.0, 0.0))
+    got = [ctypes.c_double() for _ in range(3)]
+    a = 1.0 / (1.0 + COSMO['redshift'])
+    assert lib.gic_tipsy_factors(ctypes.byref(m), COSMO['omega_m'], COSMO['hubble'], a, ZOOM2[0][0],
+                                 *[ctypes.byref(g) for g in got]) == 0
+    assert (got[0].value, got[1].value, got[2].value) == (pf, vf, mf)
