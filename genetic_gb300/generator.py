@@ -11,7 +11,7 @@ import os
 
 import numpy as np
 
-from . import _lib
+from . import _lib, writers
 from ._lib import check
 from .transfer import read_camb
 
@@ -48,6 +48,7 @@ class ICGenerator:
         self._done = False
         self.centre_point = (0.0, 0.0, 0.0)
         self.flagged = None  # flagged cells of the finest level (linear indices)
+        self.zoom_masks = []  # per zoom level: (replaced cells of the level above, ratio, origin)
 
     # -- lifetime --------------------------------------------------------------
     def close(self):
@@ -124,7 +125,16 @@ class ICGenerator:
         if int(x0) < 0 or int(y0) < 0 or int(z0) < 0:
             raise ValueError('The newly initialised zoom level is not fully contained within the previous level')
         offset = tuple(off0[i] + int(c) * dx0 for i, c in enumerate((x0, y0, z0)))
+        # the zoom mask and the flags carried to the new level (ic.hpp:480-596)
+        flags = getattr(self, 'flagged_levels', [])
+        above = flags[-1] if len(flags) == len(self.levels) else np.zeros(0, dtype=np.uint64)
+        origin = (int(x0), int(y0), int(z0))
+        mask, ratio, new_flags = writers.zoom_mask(above, n0, origin, int(zoomfac), int(n))
         self._add_level(box0 / int(zoomfac), int(n), offset)
+        self.zoom_masks.append((mask, ratio, origin))
+        if len(flags) == len(self.levels) - 1:
+            self.flagged_levels = list(flags) + [new_flags]
+            self.flagged = new_flags
 
     zoomgrid_with_origin_at = zoom_grid_with_origin_at
 
@@ -348,6 +358,59 @@ class ICGenerator:
         vel = np.empty((n ** 3, 3), dtype=np.float64)
         self._call('gic_fetch_particles', level, _ptr(pos), _ptr(vel))
         return pos, vel
+
+    # -- particle files (io/tipsy.hpp, io/gadget.hpp) ------------------------------------
+    def particle_map(self):
+        """The gic_particle_map of this context: genetIC's particle-mapper order over the zoom masks."""
+        return writers.particle_map(self.levels, self.zoom_masks, self.cosmo)
+
+    def _host_particles(self, nlevels):
+        parts = [self.particles(l) for l in range(nlevels)]
+        P = ctypes.POINTER(ctypes.c_double)
+        pos = (P * nlevels)(*[p.ctypes.data_as(P) for p, _ in parts])
+        vel = (P * nlevels)(*[v.ctypes.data_as(P) for _, v in parts])
+        return parts, pos, vel
+
+    def tipsy_records(self):
+        """The tipsy dark-matter records (n x 9 float32) in mapper order, packed on the device
+        for one or two levels and by host threads for more."""
+        m = self.particle_map()
+        n = ctypes.c_ulonglong()
+        check(None, self._lib.gic_tipsy_count(ctypes.byref(m), ctypes.byref(n)))
+        out = np.empty((n.value, 9), dtype=np.float32)
+        if m.nlevels <= 2:
+            self._call('gic_tipsy_pack', ctypes.byref(m), 0, n.value, out.ctypes.data_as(ctypes.c_void_p))
+        else:
+            keep, pos, vel = self._host_particles(m.nlevels)
+            check(None, self._lib.gic_tipsy_pack_host(ctypes.byref(m), pos, vel, 0, n.value,
+                                                      out.ctypes.data_as(ctypes.c_void_p), 0))
+        return out
+
+    def write_tipsy(self, path):
+        """The particles as genetIC's tipsy file (TipsyOutput, tipsy.hpp:200-262)."""
+        writers.write_tipsy(path, 1.0 / (1.0 + self.cosmo['redshift']), self.tipsy_records())
+
+    def write_gadget(self, path, version=2):
+        """The particles as genetIC's single-file gadget snapshot, every level of particle
+        type 1 (GadgetOutput, gadget.hpp:481-520): float positions and velocities, ids, and
+        the mass block when the levels' masses differ."""
+        m = self.particle_map()
+        n = ctypes.c_ulonglong()
+        check(None, self._lib.gic_tipsy_count(ctypes.byref(m), ctypes.byref(n)))
+        keep, pos, vel = self._host_particles(m.nlevels)
+        pos3 = np.empty((n.value, 3), dtype=np.float32)
+        vel3 = np.empty((n.value, 3), dtype=np.float32)
+        ids = np.empty(n.value, dtype=np.uint64)
+        mass = np.empty(n.value, dtype=np.float32)
+        ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        check(None, self._lib.gic_gadget_pack_host(ctypes.byref(m), pos, vel, 0, n.value, ptr(pos3), ptr(vel3),
+                                                   ptr(ids), ptr(mass), 0))
+        variable = len(set(m.mass[l] for l in range(m.nlevels))) > 1
+        masses = [0.0] * 6 if variable else [0.0, m.mass[0], 0.0, 0.0, 0.0, 0.0]
+        c = self.cosmo
+        h = writers.gadget_header(version, [0, n.value, 0, 0, 0, 0], masses, 1.0 / (1.0 + c['redshift']), c['redshift'],
+                                  self.levels[0][0], c['omega_m'], c['omega_lambda'], c['hubble'])
+        writers.write_gadget(path, h, pos3, vel3, ids, mass if variable else None)
 
     def gaussian_stream(self, seed, count):
         out = np.empty(int(count), dtype=np.float64)

@@ -322,7 +322,8 @@ def tipsy_goldens():
         raw = open(os.path.join(d, 'out.tipsy'), 'rb').read()
         header = np.frombuffer(raw[8:28], '<i4').copy()
         t, _, dark = read_tipsy(os.path.join(d, 'out.tipsy'))
-        np.savez_compressed(os.path.join(HERE, 'tipsy_zoom2.npz'), scalefactor=np.float64(t), header=header, dark=dark)
+        np.savez_compressed(os.path.join(HERE, 'tipsy_zoom2.npz'), scalefactor=np.float64(t), header=header, dark=dark,
+                            header_bytes=np.frombuffer(raw[:28], np.uint8).copy())
 
 
 def tipsy3_goldens():
@@ -367,6 +368,7 @@ def gadget_goldens():
         ids = np.frombuffer(ids, '<u8')
         assert np.array_equal(ids, np.arange(len(ids)))
         np.savez_compressed(os.path.join(HERE, 'gadget_zoom2.npz'), npart=npart.copy(),
+                            header_bytes=np.frombuffer(header, np.uint8).copy(),
                             header_mass=np.frombuffer(header[24:72], '<f8').copy(),
                             pos=np.frombuffer(pos, '<f4').reshape(-1, 3), vel=np.frombuffer(vel, '<f4').reshape(-1, 3),
                             mass=np.frombuffer(mass, '<f4'))

@@ -212,3 +212,99 @@ def test_tipsy_factors_match_oracle(built, zoom2_particles):
     assert lib.gic_tipsy_factors(ctypes.byref(m), COSMO['omega_m'], COSMO['hubble'], a, ZOOM2[0][0],
                                  *[ctypes.byref(g) for g in got]) == 0
     assert (got[0].value, got[1].value, got[2].value) == (pf, vf, mf)
+
+
+def test_file_headers_match_reference_bytes():
+    """The tipsy and gadget2 headers of the zoom2 files, byte for byte (the tipsy header's
+    trailing padding excepted: the reference leaves it unset)."""
+    from conftest import COSMO
+    from genetic_gb300 import writers
+    a = 1.0 / (1.0 + COSMO['redshift'])
+    t = np.load(os.path.join(GOLDEN, 'tipsy_zoom2.npz'))
+    n = int(t['header'][0])
+    assert writers.tipsy_header(a, n)[:28] == bytes(t['header_bytes'])
+    g = np.load(os.path.join(GOLDEN, 'gadget_zoom2.npz'))
+    h = writers.gadget_header(2, [0, n, 0, 0, 0, 0], [0.0] * 6, a, COSMO['redshift'], ZOOM2[0][0], COSMO['omega_m'],
+                              COSMO['omega_lambda'], COSMO['hubble'])
+    assert h == bytes(g['header_bytes'])
+
+
+def test_gadget_file_round_trip(tmp_path):
+    from genetic_gb300 import writers
+    rng = np.random.default_rng(3)
+    pos, vel = rng.random((10, 3)).astype(np.float32), rng.random((10, 3)).astype(np.float32)
+    ids, mass = np.arange(10, dtype=np.uint64), np.full(10, 2.5, np.float32)
+    h = writers.gadget_header(3, [0, 10, 0, 0, 0, 0], [0.0] * 6, 0.01, 99.0, 50.0, 0.31, 0.69, 0.68)
+    writers.write_gadget(tmp_path / 'g', h, pos, vel, ids, mass)
+    rec = writers.read_fortran_records(tmp_path / 'g')
+    assert rec[0] == h and len(rec) == 5
+    assert np.array_equal(np.frombuffer(rec[1], np.float32).reshape(-1, 3), pos)
+    assert np.array_equal(np.frombuffer(rec[3], np.uint64), ids)
+    assert np.frombuffer(h[196:208], '<i4', 2).tolist() == [0, 1]
+
+
+def test_zoom_masks_and_map_follow_genetic(built):
+    """The generator's zoom bookkeeping: the flagged cube becomes the zoom mask, its cells'
+    blocks the new level's flags and the next zoom's mask; the map's count and factors are
+    the oracle's for the zoom2 and zoom3 cases."""
+    from conftest import COSMO
+    from genetic_gb300 import _lib, writers
+    lib = _lib.load()
+    flags0 = fo.flag_cells(fo.Levels(ZOOM3), 0, (25., 25., 25.), 'cube', 10)
+    mask0, r0, flags1 = writers.zoom_mask(flags0, 32, (8, 8, 8), 2, 32)
+    assert r0 == 2 and np.array_equal(mask0, np.sort(flags0))
+    assert np.array_equal(flags1, np.sort(fo.block_cells(flags0, 32, 32, 2, (8, 8, 8))))
+    mask1, r1, _ = writers.zoom_mask(flags1, 32, (8, 8, 8), 2, 32)
+    assert r1 == 2 and np.array_equal(mask1, flags1)
+    cnt = ctypes.c_ulonglong()
+    for levels, masks, n in ((ZOOM2, [(mask0, 2, (8, 8, 8))], 34280),
+                             (ZOOM3, [(mask0, 2, (8, 8, 8)), (mask1, 2, (8, 8, 8))], 46376)):
+        m = writers.particle_map(levels, masks, COSMO)
+        assert lib.gic_tipsy_count(ctypes.byref(m), ctypes.byref(cnt)) == 0 and cnt.value == n
+        geo = [(32, 1, (0, 0, 0))] + [(32, 2, (8, 8, 8))] * (len(levels) - 1)
+        order = fo.mapper_order_levels(geo, [mask0, mask1][:len(levels) - 1])
+        mass, eps, pf, vf, mf = fo.tipsy_factors(levels, COSMO, order[0])
+        assert (m.pos_factor, m.vel_factor, m.mass_factor) == (pf, vf, mf)
+        assert [m.mass[l] for l in range(len(levels))] == mass and [m.eps[l] for l in range(len(levels))] == eps
+    # cells outside the zoom window are dropped from the mask, as genetIC trims them
+    mask, _, _ = writers.zoom_mask(np.array([0, 8 * 32 * 32 + 8 * 32 + 8]), 32, (8, 8, 8), 2, 32)
+    assert mask.tolist() == [8 * 32 * 32 + 8 * 32 + 8]
+
+
+def test_generator_writes_reference_files(built, zoom2_particles, tmp_path):
+    """ICGenerator.write_tipsy / write_gadget on the zoom2 case, with the oracle's particles
+    standing in for the device's (and the host packer for the device packer, which the GPU
+    tests show to be bit-identical): the files match the reference's."""
+    from conftest import COSMO
+    from genetic_gb300 import _lib, writers
+    from genetic_gb300.generator import ICGenerator
+    lib = _lib.load()
+    z = zoom2_particles
+    gen = ICGenerator.__new__(ICGenerator)
+    gen._lib, gen._ctx = lib, None
+    gen.levels = ZOOM2
+    gen.cosmo = dict(COSMO)
+    mask, ratio, _ = writers.zoom_mask(z['replaced'], 32, ORIGIN, 2, 32)
+    gen.zoom_masks = [(mask, ratio, ORIGIN)]
+    gen.particles = lambda l: (z['pos'][l], z['vel'][l])
+
+    def fake_call(name, m, first, count, out):
+        assert name == 'gic_tipsy_pack'
+        P = ctypes.POINTER(ctypes.c_double)
+        pp = (P * 2)(*[p.ctypes.data_as(P) for p in z['pos']])
+        vv = (P * 2)(*[v.ctypes.data_as(P) for v in z['vel']])
+        assert lib.gic_tipsy_pack_host(m, pp, vv, first, count, out, 2) == 0
+    gen._call = fake_call
+    gen.write_tipsy(tmp_path / 'out.tipsy')
+    gen.write_gadget(tmp_path / 'out.gadget2')
+    t = np.load(os.path.join(GOLDEN, 'tipsy_zoom2.npz'))
+    raw = open(tmp_path / 'out.tipsy', 'rb').read()
+    assert raw[:28] == bytes(t['header_bytes'])
+    dark = np.frombuffer(raw[32:], np.float32).reshape(-1, 9)
+    assert np.array_equal(dark[:, 0], t['dark'][:, 0]) and np.abs(dark[:, 1:4] - t['dark'][:, 1:4]).max() <= 6e-8
+    g = np.load(os.path.join(GOLDEN, 'gadget_zoom2.npz'))
+    rec = writers.read_fortran_records(tmp_path / 'out.gadget2')
+    assert rec[0] == bytes(g['header_bytes']) and len(rec) == 5
+    assert np.abs(np.frombuffer(rec[1], np.float32).reshape(-1, 3) - g['pos']).max() <= 4e-6
+    assert np.array_equal(np.frombuffer(rec[4], np.float32), g['mass'])
+    assert np.array_equal(np.frombuffer(rec[3], np.uint64), np.arange(len(g['mass']), dtype=np.uint64))
