@@ -49,6 +49,7 @@ class ICGenerator:
         self.centre_point = (0.0, 0.0, 0.0)
         self.flagged = None  # flagged cells of the finest level (linear indices)
         self.zoom_masks = []  # per zoom level: (replaced cells of the level above, ratio, origin)
+        self.output_dir, self.output_name, self.output_format = './', '', None
 
     # -- lifetime --------------------------------------------------------------
     def close(self):
@@ -319,13 +320,53 @@ class ICGenerator:
     def done(self, apply_modifications=True, order=1):
         """Draw the noise if needed, apply the queued modifications, then P(k), the
         Zel'dovich fields and particles (ic.hpp:1633-1648); order=2 adds the
-        second-order (2LPT) displacements, an extension genetIC does not have."""
+        second-order (2LPT) displacements, an extension genetIC does not have.  With an
+        output format set (outformat), the particle file is written, as genetIC's done does."""
         self.draw()
         self._modified = False
         if apply_modifications and self._has_modifications():
             self.apply_modifications()
         self._call('gic_zeldovich', int(order))
         self._done = True
+        if self.output_format is not None:
+            self.write()
+
+    # -- output (ic.hpp:735-760, 1275-1331; io.hpp:35-90) ----------------------------------
+    _FORMATS = {'gadget2': 2, 'gadget3': 3, 'tipsy': 4, 'grafic': 5, 'gadgethdf': 6, 'swift': 7}
+
+    def outdir(self, path):
+        self.output_dir = str(path)
+
+    def outname(self, name):
+        self.output_name = str(name)
+
+    def outformat(self, fmt):
+        """A format by number (2-7) or name, as genetIC's OutputFormat reads it (io.hpp:66-90)."""
+        s = str(fmt).strip().lower()
+        v = int(s) if s.isdigit() else self._FORMATS.get(s)
+        if v not in self._FORMATS.values():
+            raise ValueError('Unknown output format %r' % fmt)
+        self.output_format = v
+
+    def output_path(self):
+        """ICGenerator::getOutputPath (ic.hpp:753-760), relative to the paramfile's directory."""
+        folder = os.path.join(self.base_dir, self.output_dir)
+        if self.output_name:
+            return os.path.join(folder, self.output_name)
+        return os.path.join(folder, 'IC_%s_z%g_%d' % ('float' if self.precision == 'mixed' else 'doub',
+                                                      self.cosmo['redshift'], self.levels[0][1]))
+
+    def write(self):
+        """The particle file in the chosen format (ICGenerator::write, ic.hpp:1275-1331): tipsy and
+        gadget 2/3 are written here; the other formats are genetIC's own writers."""
+        path = self.output_path()
+        if self.output_format == 4:
+            self.write_tipsy(path + '.tipsy')
+        elif self.output_format in (2, 3):
+            self.write_gadget(path + '.gadget%d' % self.output_format, self.output_format)
+        else:
+            name = {v: k for k, v in self._FORMATS.items()}[self.output_format]
+            raise NotImplementedError('outformat %s is written by genetIC\'s own writer' % name)
 
     def _has_modifications(self):
         return getattr(self, '_nmods', 0) > 0
@@ -433,9 +474,10 @@ _COMMANDS = {
     'exact_power_spectrum_enforcement': 'fix_power', 'reverse': 'reverse', 'reverse_small_k': 'reverse_small_k',
     'splice': 'splice',
     'apply_modifications': 'apply_modifications',
+    'outname': 'outname', 'outdir': 'outdir', 'outformat': 'outformat',
 }
 # output-side commands handled by genetIC's own writers; accepted and ignored here
-_IGNORED = {'outname', 'outdir', 'outformat', 'dump_grid', 'dump_ps', 'idfile', 'dump_idfile'}
+_IGNORED = {'dump_grid', 'dump_ps', 'idfile', 'dump_idfile'}
 
 
 def parse_paramfile(path):

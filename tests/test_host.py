@@ -135,7 +135,7 @@ def test_paramfile_parser(tmp_path):
     p = tmp_path / 'p.txt'
     p.write_text('Om 0.3\n# comment\nbasegrid 50 32 # trailing\noutformat tipsy\nrandom_seed 5\ndone\n')
     cmds = generator.parse_paramfile(str(p))
-    assert [c[1] for c in cmds] == ['Om', 'base_grid', 'random_seed', 'done']
+    assert [c[1] for c in cmds] == ['Om', 'base_grid', 'outformat', 'random_seed', 'done']
     assert cmds[1][2] == ['50', '32']
     p.write_text('supersample 2\n')
     with pytest.raises(ValueError, match='not on the GPU realisation path'):

@@ -308,3 +308,27 @@ def test_generator_writes_reference_files(built, zoom2_particles, tmp_path):
     assert np.abs(np.frombuffer(rec[1], np.float32).reshape(-1, 3) - g['pos']).max() <= 4e-6
     assert np.array_equal(np.frombuffer(rec[4], np.float32), g['mass'])
     assert np.array_equal(np.frombuffer(rec[3], np.uint64), np.arange(len(g['mass']), dtype=np.uint64))
+
+
+def test_outformat_commands_name_files_like_genetic(built, tmp_path):
+    from genetic_gb300.generator import ICGenerator
+    gen = ICGenerator.__new__(ICGenerator)
+    gen._ctx = None
+    gen.base_dir, gen.output_dir, gen.output_name, gen.output_format = str(tmp_path), './', '', None
+    gen.precision, gen.cosmo, gen.levels = 'fp64', {'redshift': 99.0}, [(50.0, 32, (0, 0, 0))]
+    written = []
+    gen.write_tipsy = lambda p: written.append(p)
+    gen.write_gadget = lambda p, v=2: written.append((p, v))
+    gen.outformat('tipsy')
+    gen.write()
+    assert written[-1] == os.path.join(str(tmp_path), './', 'IC_doub_z99_32') + '.tipsy'
+    gen.outdir('sub')
+    gen.outname('out')
+    gen.outformat('3')
+    gen.write()
+    assert written[-1] == (os.path.join(str(tmp_path), 'sub', 'out') + '.gadget3', 3)
+    gen.outformat('grafic')
+    with pytest.raises(NotImplementedError):
+        gen.write()
+    with pytest.raises(ValueError):
+        gen.outformat('fits')
