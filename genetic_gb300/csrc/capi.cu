@@ -402,10 +402,10 @@ int gic_tipsy_pack_host(const gic_particle_map *map, const double *const *pos, c
 }
 
 int gic_gadget_pack_host(const gic_particle_map *map, const double *const *pos, const double *const *vel,
-                         unsigned long long first, unsigned long long count, float *pos_out, float *vel_out,
-                         unsigned long long *ids, float *mass_out, int threads) {
+                         const int *level_types, unsigned long long first, unsigned long long count, float *pos_out,
+                         float *vel_out, unsigned long long *ids, float *mass_out, int threads) {
   HOST_BEGIN
-  gic::gadget_pack_host(map, pos, vel, first, count, pos_out, vel_out, ids, mass_out, threads);
+  gic::gadget_pack_host(map, pos, vel, level_types, first, count, pos_out, vel_out, ids, mass_out, threads);
   HOST_END
 }
 

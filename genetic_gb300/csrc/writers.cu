@@ -432,10 +432,26 @@ void tipsy_pack_host(const gic_particle_map *m, const double *const *pos, const 
   });
 }
 
+// each level's particles in mapper order: one run per level, in level order
+static void level_runs(const MapFull &f, unsigned long long *start, unsigned long long *len) {
+  unsigned long long at = 0;
+  for (int l = 0; l < f.nlevels; ++l) {
+    const LevelMap &L = f.lv[l];
+    const unsigned long long have =
+        l ? f.lv[l - 1].nrep * (unsigned long long)L.ratio * L.ratio * L.ratio : (unsigned long long)L.n * L.n * L.n;
+    start[l] = at;
+    len[l] = have - L.nrep;
+    at += len[l];
+  }
+}
+
 void gadget_pack_host(const gic_particle_map *m, const double *const *pos, const double *const *vel,
-                      unsigned long long first, unsigned long long count, float *pos_out, float *vel_out,
-                      unsigned long long *ids, float *mass_out, int threads) {
+                      const int *level_types, unsigned long long first, unsigned long long count, float *pos_out,
+                      float *vel_out, unsigned long long *ids, float *mass_out, int threads) {
   const MapFull f = check_full(m);
+  if (level_types)
+    for (int l = 0; l < f.nlevels; ++l)
+      if (level_types[l] < 0 || level_types[l] > 5) fail(GIC_ERR_INVALID_ARG, "gadget particle types are 0 to 5");
   const void *any = pos_out ? (const void *)pos_out : vel_out ? (const void *)vel_out : ids ? (const void *)ids
                                                                                          : (const void *)mass_out;
   check_window(f.total, first, count, any);
@@ -448,15 +464,33 @@ void gadget_pack_host(const gic_particle_map *m, const double *const *pos, const
   if (!count) return;
   float mass[kMaxLevels];
   for (int l = 0; l < kMaxLevels; ++l) mass[l] = (float)m->mass[l];
-  for_each_particle_full(f, first, count, threads, [&](unsigned long long o, int l, unsigned long long cell) {
-    const unsigned long long k = o - first;
-    for (int a = 0; a < 3; ++a) {
-      if (pos_out) pos_out[3 * k + a] = (float)pos[l][3 * cell + a];
-      if (vel_out) vel_out[3 * k + a] = (float)vel[l][3 * cell + a];
-    }
-    if (ids) ids[k] = o;
-    if (mass_out) mass_out[k] = mass[l];
-  });
+  // the file holds the types in order 0..5, each type's particles in mapper order
+  // (GadgetOutput::genericSaveBlock, gadget.hpp:285-312); a level's particles are one
+  // run in mapper order, so a file range of a level is a mapper range
+  unsigned long long start[kMaxLevels], len[kMaxLevels], file_at[kMaxLevels];
+  level_runs(f, start, len);
+  unsigned long long at = 0;
+  for (int t = 0; t < 6; ++t)
+    for (int l = 0; l < f.nlevels; ++l)
+      if ((level_types ? level_types[l] : 1) == t) {
+        file_at[l] = at;
+        at += len[l];
+      }
+  const unsigned long long end = first + count;
+  for (int l = 0; l < f.nlevels; ++l) {
+    const unsigned long long a = std::max(first, file_at[l]), b = std::min(end, file_at[l] + len[l]);
+    if (b <= a) continue;
+    const unsigned long long shift = file_at[l] - start[l];  // file index = mapper index + shift
+    for_each_particle_full(f, a - shift, b - a, threads, [&](unsigned long long o, int lv, unsigned long long cell) {
+      const unsigned long long k = o + shift - first;
+      for (int c = 0; c < 3; ++c) {
+        if (pos_out) pos_out[3 * k + c] = (float)pos[lv][3 * cell + c];
+        if (vel_out) vel_out[3 * k + c] = (float)vel[lv][3 * cell + c];
+      }
+      if (ids) ids[k] = o;
+      if (mass_out) mass_out[k] = mass[lv];
+    });
+  }
 }
 
 template <typename V>

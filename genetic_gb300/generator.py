@@ -50,6 +50,8 @@ class ICGenerator:
         self.flagged = None  # flagged cells of the finest level (linear indices)
         self.zoom_masks = []  # per zoom level: (replaced cells of the level above, ratio, origin)
         self.output_dir, self.output_name, self.output_format = './', '', None
+        # gadget particle type per level (ic.hpp:80, 606-614, 680-700)
+        self.gadget_types, self._mru_gadget_type, self._used_gadget_types = [], 1, set()
 
     # -- lifetime --------------------------------------------------------------
     def close(self):
@@ -143,6 +145,23 @@ class ICGenerator:
         lid = ctypes.c_int()
         self._call('gic_level_add', box, n, offset[0], offset[1], offset[2], ctypes.byref(lid))
         self.levels.append((box, n, offset))
+        self.gadget_types.append(self._mru_gadget_type)
+        if len(self.gadget_types) > 1:  # the type selected before is now in use (ic.hpp:611-613)
+            self._used_gadget_types.add(self._mru_gadget_type)
+
+    def gadget_particle_type(self, t):
+        """ICGenerator::setGadgetParticleType (ic.hpp:690-701): the gadget type of the deepest level."""
+        t = int(t)
+        if not 0 <= t < 6:
+            raise ValueError('Gadget particle type must be between 0 and 5')
+        if t != self._mru_gadget_type:
+            if t in self._used_gadget_types:
+                raise ValueError('Cannot reuse a gadget particle type; this type was already used in a different '
+                                 'section of the ICs')
+            self._mru_gadget_type = t
+        if not self.levels:
+            raise RuntimeError("Can't set a gadget particle type until a level has been initialised to set it for")
+        self.gadget_types[-1] = t
 
     # -- seeding (main.cpp:44-52) ----------------------------------------------------
     def _seed(self, seed, mode):
@@ -444,13 +463,15 @@ class ICGenerator:
         ids = np.empty(n.value, dtype=np.uint64)
         mass = np.empty(n.value, dtype=np.float32)
         ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
-        check(None, self._lib.gic_gadget_pack_host(ctypes.byref(m), pos, vel, 0, n.value, ptr(pos3), ptr(vel3),
+        types = list(getattr(self, 'gadget_types', [])) or [1] * m.nlevels
+        tarr = (ctypes.c_int * m.nlevels)(*types)
+        check(None, self._lib.gic_gadget_pack_host(ctypes.byref(m), pos, vel, tarr, 0, n.value, ptr(pos3), ptr(vel3),
                                                    ptr(ids), ptr(mass), 0))
-        variable = len(set(m.mass[l] for l in range(m.nlevels))) > 1
-        masses = [0.0] * 6 if variable else [0.0, m.mass[0], 0.0, 0.0, 0.0, 0.0]
+        npart, masses = writers.gadget_type_counts(m, types)
+        variable = masses is None
         c = self.cosmo
-        h = writers.gadget_header(version, [0, n.value, 0, 0, 0, 0], masses, 1.0 / (1.0 + c['redshift']), c['redshift'],
-                                  self.levels[0][0], c['omega_m'], c['omega_lambda'], c['hubble'])
+        h = writers.gadget_header(version, npart, [0.0] * 6 if variable else masses, 1.0 / (1.0 + c['redshift']),
+                                  c['redshift'], self.levels[0][0], c['omega_m'], c['omega_lambda'], c['hubble'])
         writers.write_gadget(path, h, pos3, vel3, ids, mass if variable else None)
 
     def gaussian_stream(self, seed, count):
@@ -475,6 +496,7 @@ _COMMANDS = {
     'splice': 'splice',
     'apply_modifications': 'apply_modifications',
     'outname': 'outname', 'outdir': 'outdir', 'outformat': 'outformat',
+    'gadget_particle_type': 'gadget_particle_type',
 }
 # output-side commands handled by genetIC's own writers; accepted and ignored here
 _IGNORED = {'dump_grid', 'dump_ps', 'idfile', 'dump_idfile'}

@@ -146,3 +146,22 @@ def particle_map(levels, zoom_masks, cosmo):
     _lib.check(None, lib.gic_tipsy_factors(ctypes.byref(m), om, cosmo['hubble'], a, L, *[ctypes.byref(v) for v in f]))
     m.pos_factor, m.vel_factor, m.mass_factor = f[0].value, f[1].value, f[2].value
     return m
+
+
+def gadget_type_counts(m, level_types):
+    """Particles per gadget type and the header's per-type masses, as
+    GadgetOutput::preScanForMassesAndParticleNumbers finds them (gadget.hpp:325-372): a
+    type's mass is its particles' mass when they all share one; if any type mixes
+    masses, the file stores every mass (None is returned for the masses)."""
+    runs = []
+    for l in range(m.nlevels):
+        have = m.n[0] ** 3 if l == 0 else m.n_replaced[l - 1] * m.ratio[l] ** 3
+        runs.append(have - m.n_replaced[l])
+    npart, per_type = [0] * 6, [set() for _ in range(6)]
+    for l, t in enumerate(level_types[:m.nlevels]):
+        npart[t] += runs[l]
+        if runs[l]:
+            per_type[t].add(m.mass[l])
+    if any(len(s) > 1 for s in per_type):
+        return npart, None
+    return npart, [min(s) if s else 0.0 for s in per_type]

@@ -204,15 +204,18 @@ GIC_API int gic_tipsy_pack(gic_ctx *ctx, const gic_particle_map *map, unsigned l
                            gic_tipsy_dark *host_out);
 
 /* Gadget blocks (io::gadget::GadgetOutput, genetIC/src/io/gadget.hpp:481-520) of the map's
- * particles [first, first + count) from host particles, every level of gadget particle
- * type 1 (genetIC's default, ic.hpp:80, 606-614), by `threads` host threads: positions
- * and velocities as float triples (Coordinate<float> of pos and vel), ids = the
- * particle's index in the map (the mapper iterator's getIndex), masses as floats (the
- * variable-mass block; map->mass per level).  NULL outputs are skipped; the map's
- * eps and factors are not used.  Failures: gic_last_error(NULL). */
+ * particles from host particles, by `threads` host threads.  level_types[l] is level l's
+ * gadget particle type (0-5; gadget_particle_type, ic.hpp:606-614, 691-700); NULL means
+ * type 1 for every level, genetIC's default.  The file holds the types in order, each
+ * type's particles in mapper order (genericSaveBlock, gadget.hpp:285-312); [first,
+ * first + count) indexes that file order.  Positions and velocities as float triples
+ * (Coordinate<float> of pos and vel), ids = the particle's index in the map (the mapper
+ * iterator's getIndex), masses as floats (the variable-mass block; map->mass per level).
+ * NULL outputs are skipped; the map's eps and factors are not used.  Failures:
+ * gic_last_error(NULL). */
 GIC_API int gic_gadget_pack_host(const gic_particle_map *map, const double *const *pos, const double *const *vel,
-                                 unsigned long long first, unsigned long long count, float *pos_out, float *vel_out,
-                                 unsigned long long *ids, float *mass_out, int threads);
+                                 const int *level_types, unsigned long long first, unsigned long long count,
+                                 float *pos_out, float *vel_out, unsigned long long *ids, float *mass_out, int threads);
 
 /* Forward (dir=-1) or inverse (dir=+1) normalised 3-D real FFT of a level field
  * in place on the device (testing).  Replaces FieldFourierManager<T,T>::performTransform

@@ -326,6 +326,22 @@ def tipsy_goldens():
                             header_bytes=np.frombuffer(raw[:28], np.uint8).copy())
 
 
+def gadget_types_goldens():
+    """The reference's gadget2 file of the zoom2 case with gadget particle types: level 0 of
+    type 3, the zoom level of type 1, so the file holds the zoom's particles first: header
+    bytes, ids and every 97th position."""
+    with tempfile.TemporaryDirectory() as d:
+        write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+        params = ZOOM_PARAMS.format(seedcmd='random_seed', zooms='gadget_particle_type 3\n' + '\n'.join(ZOOMS['zoom2'])
+                                    + '\ngadget_particle_type 1', dumps='')
+        open(os.path.join(d, 'paramfile.txt'), 'w').write(params.replace('outformat tipsy', 'outformat gadget2'))
+        subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True)
+        # one mass per type: the masses are in the header and there is no mass block
+        header, pos, vel, ids = read_fortran_records(os.path.join(d, 'out.gadget2'))
+        np.savez_compressed(os.path.join(HERE, 'gadget_types_zoom2.npz'), header_bytes=np.frombuffer(header, np.uint8).copy(),
+                            ids=np.frombuffer(ids, '<u8').copy(), pos97=np.frombuffer(pos, '<f4').reshape(-1, 3)[::97].copy())
+
+
 def tipsy3_goldens():
     """The reference's tipsy file of the three-level zoom3 case: its header and the records
     of the finest level (the level-1 particles are all replaced), which follow the level-1
@@ -400,3 +416,4 @@ if __name__ == '__main__':
     tipsy_goldens()
     gadget_goldens()
     tipsy3_goldens()
+    gadget_types_goldens()

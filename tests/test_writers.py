@@ -148,13 +148,13 @@ def test_gadget_blocks_match_reference_file_and_oracle(built, zoom2_particles):
     pp = (P * 2)(*[np.ascontiguousarray(p).ctypes.data_as(P) for p in z['pos']])
     vv = (P * 2)(*[np.ascontiguousarray(v).ctypes.data_as(P) for v in z['vel']])
     ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
-    assert lib.gic_gadget_pack_host(ctypes.byref(m), pp, vv, 0, n, ptr(pos), ptr(vel), ptr(ids), ptr(mass), 3) == 0
+    assert lib.gic_gadget_pack_host(ctypes.byref(m), pp, vv, None, 0, n, ptr(pos), ptr(vel), ptr(ids), ptr(mass), 3) == 0
     assert np.array_equal(pos.view(np.uint32), want_pos.view(np.uint32))
     assert np.array_equal(vel.view(np.uint32), want_vel.view(np.uint32))
     assert np.array_equal(mass, want_mass) and np.array_equal(ids, np.arange(n, dtype=np.uint64))
     # ids alone, for a window
     ids2 = np.zeros(10, np.uint64)
-    assert lib.gic_gadget_pack_host(ctypes.byref(m), None, None, 500, 10, None, None, ptr(ids2), None, 1) == 0
+    assert lib.gic_gadget_pack_host(ctypes.byref(m), None, None, None, 500, 10, None, None, ptr(ids2), None, 1) == 0
     assert np.array_equal(ids2, np.arange(500, 510, dtype=np.uint64))
 
 
@@ -286,6 +286,7 @@ def test_generator_writes_reference_files(built, zoom2_particles, tmp_path):
     gen.cosmo = dict(COSMO)
     mask, ratio, _ = writers.zoom_mask(z['replaced'], 32, ORIGIN, 2, 32)
     gen.zoom_masks = [(mask, ratio, ORIGIN)]
+    gen.gadget_types = [1, 1]
     gen.particles = lambda l: (z['pos'][l], z['vel'][l])
 
     def fake_call(name, m, first, count, out):
@@ -332,3 +333,34 @@ def test_outformat_commands_name_files_like_genetic(built, tmp_path):
         gen.write()
     with pytest.raises(ValueError):
         gen.outformat('fits')
+
+
+def test_gadget_particle_types_match_reference_file(built, zoom2_particles, tmp_path):
+    """gadget_particle_type 3 on the base level and 1 on the zoom: the file holds type 1 (the
+    zoom's particles) first, ids keep the mapper index, and one mass per type goes to the
+    header with no mass block, as in the reference's file."""
+    from conftest import COSMO
+    from genetic_gb300 import writers
+    from genetic_gb300.generator import ICGenerator
+    z = zoom2_particles
+    g = np.load(os.path.join(GOLDEN, 'gadget_types_zoom2.npz'))
+    gen = ICGenerator.__new__(ICGenerator)
+    from genetic_gb300 import _lib
+    gen._lib, gen._ctx = _lib.load(), None
+    gen.levels, gen.cosmo = ZOOM2, dict(COSMO)
+    mask, ratio, _ = writers.zoom_mask(z['replaced'], 32, ORIGIN, 2, 32)
+    gen.zoom_masks = [(mask, ratio, ORIGIN)]
+    gen.gadget_types, gen._mru_gadget_type, gen._used_gadget_types = [1], 1, set()
+    gen.gadget_particle_type(3)
+    gen.gadget_types.append(gen._mru_gadget_type)  # the zoom level, as _add_level records it
+    gen._used_gadget_types.add(gen._mru_gadget_type)
+    gen.gadget_particle_type(1)
+    assert gen.gadget_types == [3, 1]
+    with pytest.raises(ValueError, match='reuse'):
+        gen.gadget_particle_type(3)
+    gen.particles = lambda l: (z['pos'][l], z['vel'][l])
+    gen.write_gadget(tmp_path / 'out.gadget2')
+    rec = writers.read_fortran_records(tmp_path / 'out.gadget2')
+    assert len(rec) == 4 and rec[0] == bytes(g['header_bytes'])
+    assert np.array_equal(np.frombuffer(rec[3], np.uint64), g['ids'])
+    assert np.abs(np.frombuffer(rec[1], np.float32).reshape(-1, 3)[::97] - g['pos97']).max() <= 4e-6
