@@ -52,6 +52,9 @@ class ICGenerator:
         self.output_dir, self.output_name, self.output_format = './', '', None
         # gadget particle type per level (ic.hpp:80, 606-614, 680-700)
         self.gadget_types, self._mru_gadget_type, self._used_gadget_types = [], 1, set()
+        # gadget_flagged_particle_type: the type and the finest level's flags at genetIC's
+        # last particle-mapper rebuild (ic.hpp:705-714, 1176-1185)
+        self._flagged_type, self._flagged_snapshot = None, None
 
     # -- lifetime --------------------------------------------------------------
     def close(self):
@@ -138,6 +141,29 @@ class ICGenerator:
         if len(flags) == len(self.levels) - 1:
             self.flagged_levels = list(flags) + [new_flags]
             self.flagged = new_flags
+        self._update_mapper()
+
+    def _update_mapper(self):
+        """ICGenerator::updateParticleMapper's part that reads state: the finest level's
+        flagged cells, kept for the flagged particles' own gadget type."""
+        if getattr(self, '_flagged_type', None) is None:
+            return
+        flags = getattr(self, 'flagged_levels', [])
+        cells = flags[-1] if len(flags) == len(self.levels) and len(flags) else np.zeros(0, dtype=np.uint64)
+        self._flagged_snapshot = np.sort(np.asarray(cells, dtype=np.uint64))
+
+    def gadget_flagged_particle_type(self, t):
+        """ICGenerator::setFlaggedGadgetParticleType (ic.hpp:705-714): the finest level's
+        flagged cells become particles of type t, at the end of the particle order."""
+        t = int(t)
+        if not 0 <= t < 6:
+            raise ValueError('Gadget particle type must be between 0 and 5')
+        if t in self._used_gadget_types:
+            raise ValueError('Cannot reuse a gadget particle type; this type was already used in a different '
+                             'section of the ICs')
+        self._flagged_type = t
+        self._used_gadget_types.add(t)
+        self._update_mapper()
 
     zoomgrid_with_origin_at = zoom_grid_with_origin_at
 
@@ -162,6 +188,7 @@ class ICGenerator:
         if not self.levels:
             raise RuntimeError("Can't set a gadget particle type until a level has been initialised to set it for")
         self.gadget_types[-1] = t
+        self._update_mapper()
 
     # -- seeding (main.cpp:44-52) ----------------------------------------------------
     def _seed(self, seed, mode):
@@ -366,6 +393,7 @@ class ICGenerator:
         if v not in self._FORMATS.values():
             raise ValueError('Unknown output format %r' % fmt)
         self.output_format = v
+        self._update_mapper()
 
     def output_path(self):
         """ICGenerator::getOutputPath (ic.hpp:753-760), relative to the paramfile's directory."""
@@ -421,11 +449,14 @@ class ICGenerator:
 
     # -- particle files (io/tipsy.hpp, io/gadget.hpp) ------------------------------------
     def particle_map(self):
-        """The gic_particle_map of this context: genetIC's particle-mapper order over the zoom masks."""
-        return writers.particle_map(self.levels, self.zoom_masks, self.cosmo)
+        """The gic_particle_map of this context: genetIC's particle-mapper order over the zoom
+        masks, with the flagged particles' own gadget type as one more level when it is set."""
+        flagged = self._flagged_snapshot if getattr(self, '_flagged_type', None) is not None else None
+        return writers.particle_map(self.levels, self.zoom_masks, self.cosmo, flagged)
 
     def _host_particles(self, nlevels):
-        parts = [self.particles(l) for l in range(nlevels)]
+        # a map level past the context's levels is the flagged particles of the finest level
+        parts = [self.particles(min(l, len(self.levels) - 1)) for l in range(nlevels)]
         P = ctypes.POINTER(ctypes.c_double)
         pos = (P * nlevels)(*[p.ctypes.data_as(P) for p, _ in parts])
         vel = (P * nlevels)(*[v.ctypes.data_as(P) for _, v in parts])
@@ -463,7 +494,9 @@ class ICGenerator:
         ids = np.empty(n.value, dtype=np.uint64)
         mass = np.empty(n.value, dtype=np.float32)
         ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
-        types = list(getattr(self, 'gadget_types', [])) or [1] * m.nlevels
+        types = list(getattr(self, 'gadget_types', [])) or [1] * len(self.levels)
+        if getattr(self, '_flagged_type', None) is not None:
+            types.append(self._flagged_type)
         tarr = (ctypes.c_int * m.nlevels)(*types)
         check(None, self._lib.gic_gadget_pack_host(ctypes.byref(m), pos, vel, tarr, 0, n.value, ptr(pos3), ptr(vel3),
                                                    ptr(ids), ptr(mass), 0))
@@ -496,7 +529,7 @@ _COMMANDS = {
     'splice': 'splice',
     'apply_modifications': 'apply_modifications',
     'outname': 'outname', 'outdir': 'outdir', 'outformat': 'outformat',
-    'gadget_particle_type': 'gadget_particle_type',
+    'gadget_particle_type': 'gadget_particle_type', 'gadget_flagged_particle_type': 'gadget_flagged_particle_type',
 }
 # output-side commands handled by genetIC's own writers; accepted and ignored here
 _IGNORED = {'dump_grid', 'dump_ps', 'idfile', 'dump_idfile'}

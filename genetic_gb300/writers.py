@@ -118,11 +118,14 @@ def zoom_mask(flags_above, n_above, origin, zoomfac, n_new):
     return mask, ratio, new_flags
 
 
-def particle_map(levels, zoom_masks, cosmo):
+def particle_map(levels, zoom_masks, cosmo, flagged=None):
     """The gic_particle_map of a context: levels [(box, n, offset)]; zoom_masks[l - 1] =
     (mask, ratio, origin) of zoom level l; each level's particle mass and softening as
     ZeldovichParticleEvaluator gives them (27.744948 Om L^3 (dx/L)^3 and 0.01075 dx,
-    zeldovich.hpp:55-62, 112-121); TipsyOutput's factors from gic_tipsy_factors."""
+    zeldovich.hpp:55-62, 112-121); TipsyOutput's factors from gic_tipsy_factors.
+    flagged: cells of the finest level given their own gadget type, which genetIC moves
+    to the end of the order with one more TwoLevelParticleMapper on the finest grid
+    (ic.hpp:1176-1185); the map then has one more level, of ratio 1, over the finest."""
     import ctypes
 
     from . import _lib
@@ -134,9 +137,15 @@ def particle_map(levels, zoom_masks, cosmo):
             raise ValueError('a zoom level needs flagged cells on the level above and an integer cell-size ratio')
         lv.append((n, ratio, tuple(int(o) for o in origin)))
         replaced.append(mask)
+    dx = [box / n for box, n, _ in levels]
+    if flagged is not None:
+        if len(flagged) == 0:
+            raise ValueError('no cells are flagged on the finest level for their own gadget type')
+        replaced.append(np.sort(np.asarray(flagged, dtype=np.uint64)))
+        lv.append((levels[-1][1], 1, (0, 0, 0)))
+        dx.append(dx[-1])
     replaced.append([])
     om = cosmo['omega_m']
-    dx = [box / n for box, n, _ in levels]
     mass = [27.744948 * om * pow(L, 3.0) * pow(d / L, 3.0) for d in dx]
     eps = [d * 1.0 * 0.01075 for d in dx]
     m = _lib.GicParticleMap.of(lv, replaced, mass, eps, 0.0, 0.0, 0.0)

@@ -342,6 +342,33 @@ def gadget_types_goldens():
                             ids=np.frombuffer(ids, '<u8').copy(), pos97=np.frombuffer(pos, '<f4').reshape(-1, 3)[::97].copy())
 
 
+def flagged_type_goldens():
+    """The zoom2 case with the finest level's cells in a 3 Mpc/h sphere given gadget type 4:
+    genetIC moves them to the end of the particle order.  The gadget2 file (header bytes,
+    ids, every 97th position) and the tipsy file (header bytes, every 37th record, the last
+    400 records)."""
+    out = {}
+    for fmt in ('gadget2', 'tipsy'):
+        with tempfile.TemporaryDirectory() as d:
+            write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+            zooms = '\n'.join(ZOOMS['zoom2']) + '\ncentre 25 25 25\nselect_sphere 3\ngadget_flagged_particle_type 4'
+            params = ZOOM_PARAMS.format(seedcmd='random_seed', zooms=zooms, dumps='')
+            open(os.path.join(d, 'paramfile.txt'), 'w').write(params.replace('outformat tipsy', 'outformat ' + fmt))
+            subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True)
+            if fmt == 'tipsy':
+                raw = open(os.path.join(d, 'out.tipsy'), 'rb').read()
+                _, _, dark = read_tipsy(os.path.join(d, 'out.tipsy'))
+                out.update(tipsy_header=np.frombuffer(raw[:28], np.uint8).copy(), tipsy37=dark[::37].copy(),
+                           tipsy_tail=dark[-400:].copy())
+            else:
+                rec = read_fortran_records(os.path.join(d, 'out.gadget2'))
+                out.update(gadget_header=np.frombuffer(rec[0], np.uint8).copy(), gadget_ids=np.frombuffer(rec[3], '<u8').copy(),
+                           gadget_pos97=np.frombuffer(rec[1], '<f4').reshape(-1, 3)[::97].copy(), gadget_nrec=np.int64(len(rec)))
+                if len(rec) > 4:
+                    out['gadget_mass'] = np.frombuffer(rec[4], '<f4').copy()
+    np.savez_compressed(os.path.join(HERE, 'flagged_type_zoom2.npz'), **out)
+
+
 def tipsy3_goldens():
     """The reference's tipsy file of the three-level zoom3 case: its header and the records
     of the finest level (the level-1 particles are all replaced), which follow the level-1
@@ -417,3 +444,4 @@ if __name__ == '__main__':
     gadget_goldens()
     tipsy3_goldens()
     gadget_types_goldens()
+    flagged_type_goldens()

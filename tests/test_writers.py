@@ -364,3 +364,37 @@ def test_gadget_particle_types_match_reference_file(built, zoom2_particles, tmp_
     assert len(rec) == 4 and rec[0] == bytes(g['header_bytes'])
     assert np.array_equal(np.frombuffer(rec[3], np.uint64), g['ids'])
     assert np.abs(np.frombuffer(rec[1], np.float32).reshape(-1, 3)[::97] - g['pos97']).max() <= 4e-6
+
+
+def test_flagged_particle_type_matches_reference_files(built, zoom2_particles, tmp_path):
+    """gadget_flagged_particle_type 4 after flagging a 3 Mpc/h sphere on the zoom level: the
+    flagged particles move to the end, in the gadget file (as type 4) and in the tipsy file."""
+    from conftest import COSMO
+    from genetic_gb300 import _lib, writers
+    from genetic_gb300.generator import ICGenerator
+    z = zoom2_particles
+    g = np.load(os.path.join(GOLDEN, 'flagged_type_zoom2.npz'))
+    gen = ICGenerator.__new__(ICGenerator)
+    gen._lib, gen._ctx = _lib.load(), None
+    gen.levels, gen.cosmo = ZOOM2, dict(COSMO)
+    mask, ratio, _ = writers.zoom_mask(z['replaced'], 32, ORIGIN, 2, 32)
+    gen.zoom_masks = [(mask, ratio, ORIGIN)]
+    gen.gadget_types, gen._mru_gadget_type, gen._used_gadget_types = [1, 1], 1, {1}
+    gen.flagged_levels = [fo.flag_cells(fo.Levels(ZOOM2), l, (25., 25., 25.), 'sphere', 3) for l in range(2)]
+    gen._flagged_type = None
+    gen.gadget_flagged_particle_type(4)
+    assert len(gen._flagged_snapshot) == 208
+    gen.particles = lambda l: (z['pos'][l], z['vel'][l])
+    gen.write_gadget(tmp_path / 'out.gadget2')
+    rec = writers.read_fortran_records(tmp_path / 'out.gadget2')
+    assert len(rec) == int(g['gadget_nrec']) and rec[0] == bytes(g['gadget_header'])
+    assert np.array_equal(np.frombuffer(rec[3], np.uint64), g['gadget_ids'])
+    assert np.array_equal(np.frombuffer(rec[4], np.float32), g['gadget_mass'])
+    assert np.abs(np.frombuffer(rec[1], np.float32).reshape(-1, 3)[::97] - g['gadget_pos97']).max() <= 4e-6
+    gen.write_tipsy(tmp_path / 'out.tipsy')
+    raw = open(tmp_path / 'out.tipsy', 'rb').read()
+    assert raw[:28] == bytes(g['tipsy_header'])
+    dark = np.frombuffer(raw[32:], np.float32).reshape(-1, 9)
+    for mine, ref in ((dark[::37], g['tipsy37']), (dark[-400:], g['tipsy_tail'])):
+        assert np.array_equal(mine[:, 0], ref[:, 0]) and np.array_equal(mine[:, 7:], ref[:, 7:])
+        assert np.abs(mine[:, 1:4] - ref[:, 1:4]).max() <= 6e-8
