@@ -123,35 +123,27 @@ def n_particles(wl):
 
 def tipsy_map(wl):
     """The gic_particle_map of a one- or two-level workload: the zoom replaces the base cells it
-    covers; particle masses, softenings and TipsyOutput's factors as genetIC forms them
-    (genetIC/src/io/tipsy.hpp:200-239, simulation/particles/zeldovich.hpp:55-62, 112-121),
-    the masses summed as a product per level.  None for other workloads."""
-    from genetic_gb300._lib import GicParticleMap
+    covers; masses, softenings and TipsyOutput's factors as genetIC forms them
+    (genetic_gb300.writers.particle_map).  None for other workloads."""
+    from genetic_gb300 import writers
     levels = wl['levels']
     _, L, n0 = levels[0]
     if len(levels) > 2 or n0 > 1024:
         return None, None
-    lv = [(n0, 1, (0, 0, 0))]
-    dx = [L / n0]
-    counts = [n0 ** 3]
-    rep = np.zeros(0, dtype=np.uint64)
+    geo = [(L, n0, (0.0, 0.0, 0.0))]
+    masks = []
+    total = n0 ** 3
     if len(levels) == 2:
         _, ox, oy, oz, factor, n1 = levels[1]
         span = n0 // factor
         ratio = factor * n1 // n0
-        lv.append((n1, ratio, (ox, oy, oz)))
+        dx0 = L / n0
+        geo.append((L / factor, n1, (ox * dx0, oy * dx0, oz * dx0)))
         ax = [(o + np.arange(span)) % n0 for o in (ox, oy, oz)]
         rep = np.sort(((ax[0][:, None, None] * n0 + ax[1][None, :, None]) * n0 + ax[2][None, None, :]).ravel())
-        dx.append(L / factor / n1)
-        counts = [n0 ** 3 - len(rep), len(rep) * ratio ** 3]
-    om, h = COSMO['omega_m'], COSMO['hubble']
-    a = 1.0 / (1.0 + COSMO['redshift'])
-    mass = [27.744948 * om * L ** 3 * (d / L) ** 3 for d in dx]
-    tot = sum(c * ms for c, ms in zip(counts, mass))
-    mass_factor = om / tot
-    kms = np.sqrt(4.3022682e-6 * (1e10 / h / mass_factor) / (L * 1000 / h))
-    m = GicParticleMap.of(lv, [rep], mass, [d * 0.01075 for d in dx], 1.0 / L, a ** -0.5 / kms, mass_factor)
-    return m, sum(counts)
+        masks.append((rep.astype(np.uint64), ratio, (ox, oy, oz)))
+        total += len(rep) * (ratio ** 3 - 1)
+    return writers.particle_map(geo, masks, COSMO), total
 
 
 class Clocks:
