@@ -407,11 +407,16 @@ def gadget_goldens():
         open(os.path.join(d, 'paramfile.txt'), 'w').write(params.replace('outformat tipsy', 'outformat gadget2'))
         subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True)
         header, pos, vel, ids, mass = read_fortran_records(os.path.join(d, 'out.gadget2'))
+        # the same run written as gadget3: its header
+        open(os.path.join(d, 'paramfile.txt'), 'w').write(params.replace('outformat tipsy', 'outformat gadget3'))
+        subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True)
+        header3 = read_fortran_records(os.path.join(d, 'out.gadget3'))[0]
         npart = np.frombuffer(header[:24], '<i4')
         ids = np.frombuffer(ids, '<u8')
         assert np.array_equal(ids, np.arange(len(ids)))
         np.savez_compressed(os.path.join(HERE, 'gadget_zoom2.npz'), npart=npart.copy(),
                             header_bytes=np.frombuffer(header, np.uint8).copy(),
+                            header3_bytes=np.frombuffer(header3, np.uint8).copy(),
                             header_mass=np.frombuffer(header[24:72], '<f8').copy(),
                             pos=np.frombuffer(pos, '<f4').reshape(-1, 3), vel=np.frombuffer(vel, '<f4').reshape(-1, 3),
                             mass=np.frombuffer(mass, '<f4'))

@@ -227,6 +227,9 @@ def test_file_headers_match_reference_bytes():
     h = writers.gadget_header(2, [0, n, 0, 0, 0, 0], [0.0] * 6, a, COSMO['redshift'], ZOOM2[0][0], COSMO['omega_m'],
                               COSMO['omega_lambda'], COSMO['hubble'])
     assert h == bytes(g['header_bytes'])
+    h3 = writers.gadget_header(3, [0, n, 0, 0, 0, 0], [0.0] * 6, a, COSMO['redshift'], ZOOM2[0][0], COSMO['omega_m'],
+                               COSMO['omega_lambda'], COSMO['hubble'])
+    assert h3 == bytes(g['header3_bytes'])
 
 
 def test_gadget_file_round_trip(tmp_path):
