@@ -11,7 +11,7 @@ import os
 
 import numpy as np
 
-from . import _lib, writers
+from . import _lib, geometry, writers
 from ._lib import check
 from .transfer import read_camb
 
@@ -34,6 +34,10 @@ class ICGenerator:
         if st != _lib.GIC_OK:
             raise _lib.GicError(st, lib.gic_last_error(None).decode())
         self._ctx = ctx
+        self._init_state(precision, device)
+
+    def _init_state(self, precision, device):
+        """The host-side state of a new context (no device call)."""
         self.precision = precision
         self.device = device
         # genetIC's defaults for Om, Ob, h, ns (genetIC/src/ic.hpp:200-210); Ol, s8
@@ -166,6 +170,19 @@ class ICGenerator:
         self._update_mapper()
 
     zoomgrid_with_origin_at = zoom_grid_with_origin_at
+
+    def zoom_grid(self, zoomfac, n):
+        """ICGenerator::initZoomGrid (ic.hpp:398-476): a zoom level of n cells per side and
+        1/zoomfac of the finest level's size, placed around that level's flagged cells."""
+        if not self.levels:
+            raise RuntimeError('Cannot initialise a zoom grid before initialising the base grid')
+        flags = getattr(self, 'flagged_levels', [])
+        above = flags[-1] if len(flags) == len(self.levels) else np.zeros(0, dtype=np.uint64)
+        box, na, off = self.levels[-1]
+        x0, y0, z0 = geometry.zoom_corner(above, na, box, off, self.levels[0][0], int(zoomfac))
+        self.zoom_grid_with_origin_at(x0, y0, z0, zoomfac, n)
+
+    zoomgrid = zoom_grid
 
     def _add_level(self, box, n, offset):
         lid = ctypes.c_int()
@@ -517,6 +534,7 @@ _COMMANDS = {
     'Om': 'Om', 'Ol': 'Ol', 'Ob': 'Ob', 'hubble': 'hubble', 's8': 's8', 'ns': 'ns', 'zin': 'zin',
     'camb': 'camb', 'basegrid': 'base_grid', 'base_grid': 'base_grid',
     'zoomgrid_with_origin_at': 'zoom_grid_with_origin_at', 'zoom_grid_with_origin_at': 'zoom_grid_with_origin_at',
+    'zoomgrid': 'zoom_grid', 'zoom_grid': 'zoom_grid',
     'random_seed': 'random_seed', 'seedfourier_parallel': 'random_seed',
     'random_seed_serial': 'random_seed_serial', 'seedfourier': 'random_seed_serial',
     'random_seed_real_space': 'random_seed_real_space', 'seed': 'random_seed_real_space',

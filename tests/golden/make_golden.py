@@ -369,6 +369,32 @@ def flagged_type_goldens():
     np.savez_compressed(os.path.join(HERE, 'flagged_type_zoom2.npz'), **out)
 
 
+ZOOM_GRID_CASES = {
+    # flagged cube at the centre, one zoom
+    'centre': 'centre 25 25 25\nselect_cube 10\nzoom_grid 2 32',
+    # a sphere across the periodic corner: the window wraps
+    'wrap': 'centre 2 2 48\nselect_sphere 5\nzoom_grid 4 32',
+    # two nested zooms; the second is moved inside the first
+    'nested': 'centre 30 28 25\nselect_sphere 6\nzoom_grid 2 32\ncentre 32 27 25\nselect_sphere 2\nzoom_grid 2 32',
+}
+
+
+def zoom_grid_goldens():
+    """The lower corners genetIC's zoom_grid chooses (its log's "Low-left corner in parent
+    grid"), for ZOOM_GRID_CASES on a 32^3, 50 Mpc/h base."""
+    import re
+    out = {}
+    for name, cmds in ZOOM_GRID_CASES.items():
+        with tempfile.TemporaryDirectory() as d:
+            write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+            params = PARAMS.format(seedcmd='random_seed').replace('done\ndump_grid 0\n', cmds + '\n')
+            open(os.path.join(d, 'paramfile.txt'), 'w').write(params)
+            r = subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True, text=True)
+            corners = re.findall(r'Low-left corner in parent grid = \((-?\d+), (-?\d+), (-?\d+)\)', r.stdout + r.stderr)
+            out[name] = np.array([[int(v) for v in c] for c in corners])
+    np.savez_compressed(os.path.join(HERE, 'zoom_grid_corners.npz'), **out)
+
+
 def tipsy3_goldens():
     """The reference's tipsy file of the three-level zoom3 case: its header and the records
     of the finest level (the level-1 particles are all replaced), which follow the level-1
@@ -450,3 +476,4 @@ if __name__ == '__main__':
     tipsy3_goldens()
     gadget_types_goldens()
     flagged_type_goldens()
+    zoom_grid_goldens()

@@ -401,3 +401,34 @@ def test_flagged_particle_type_matches_reference_files(built, zoom2_particles, t
     for mine, ref in ((dark[::37], g['tipsy37']), (dark[-400:], g['tipsy_tail'])):
         assert np.array_equal(mine[:, 0], ref[:, 0]) and np.array_equal(mine[:, 7:], ref[:, 7:])
         assert np.abs(mine[:, 1:4] - ref[:, 1:4]).max() <= 6e-8
+
+
+def _host_only_generator():
+    """An ICGenerator whose level bookkeeping runs without a device (gic_level_add skipped)."""
+    from genetic_gb300 import _lib
+    from genetic_gb300.generator import ICGenerator
+    gen = ICGenerator.__new__(ICGenerator)
+    gen._lib, gen._ctx = _lib.load(), None
+    gen._init_state('fp64', 0)
+    gen._call = lambda name, *args: None
+    return gen
+
+
+@pytest.mark.parametrize('case', ['centre', 'wrap', 'nested'])
+def test_zoom_grid_places_zooms_like_genetic(built, case):
+    """zoom_grid's lower corners against those genetIC logs for the same commands
+    (tests/golden/make_golden.py: ZOOM_GRID_CASES)."""
+    import sys
+    sys.path.insert(0, GOLDEN)
+    from make_golden import ZOOM_GRID_CASES
+    want = np.load(os.path.join(GOLDEN, 'zoom_grid_corners.npz'))[case].tolist()
+    gen = _host_only_generator()
+    gen.base_grid(50.0, 32)
+    got = []
+    for line in ZOOM_GRID_CASES[case].split('\n'):
+        cmd, *args = line.split()
+        getattr(gen, cmd)(*args)
+        if cmd == 'zoom_grid':
+            (box_a, n_a, off_a), (_, _, off) = gen.levels[-2], gen.levels[-1]
+            got.append([int(round((o - oa) / (box_a / n_a))) for o, oa in zip(off, off_a)])
+    assert got == want
