@@ -259,6 +259,24 @@ class ICGenerator:
             self.flagged_levels.append(np.ascontiguousarray(flat, dtype=np.uint64))
         self.flagged = self.flagged_levels[-1]
 
+    def select_nearest(self):
+        """ICGenerator::selectNearest (ic.hpp:1447-1455): every flag is cleared, then the finest
+        level's cell holding the centre is flagged (Grid::getIndexFromPoint, grid.hpp:672-677:
+        floor of the wrapped offset from the level's corner over the cell size)."""
+        period = self.levels[0][0]
+        box, n, off = self.levels[-1]
+        dx = box / n
+        idx = []
+        for a in range(3):
+            d = (self.centre_point[a] - off[a]) % period
+            idx.append(int(np.floor(d / dx)))
+        if any(i < 0 or i >= n for i in idx):
+            raise ValueError('the centre is not on the finest level')
+        cell = (idx[0] * n + idx[1]) * n + idx[2]
+        self.flagged_levels = [np.zeros(0, dtype=np.uint64) for _ in self.levels[:-1]]
+        self.flagged_levels.append(np.array([cell], dtype=np.uint64))
+        self.flagged = self.flagged_levels[-1]
+
     def select_sphere(self, radius):
         r2 = float(np.float32(radius) * np.float32(radius))
         self._select(lambda X, Y, Z: X * X + Y * Y + Z * Z < r2)
@@ -540,7 +558,7 @@ _COMMANDS = {
     'random_seed_real_space': 'random_seed_real_space', 'seed': 'random_seed_real_space',
     'seedfourier_reverse': 'seedfourier_reverse', 'done': 'done', 'chi2': 'chi2',
     'centre': 'centre', 'center': 'centre', 'select_sphere': 'select_sphere', 'select_cube': 'select_cube',
-    'select_ellipse': 'select_ellipse',
+    'select_ellipse': 'select_ellipse', 'select_nearest': 'select_nearest',
     'calculate': 'calculate', 'modify': 'modify', 'clear_modifications': 'clear_modifications',
     'filtering_scale': 'filtering_scale', 'fix_power': 'fix_power',
     'exact_power_spectrum_enforcement': 'fix_power', 'reverse': 'reverse', 'reverse_small_k': 'reverse_small_k',

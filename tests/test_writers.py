@@ -432,3 +432,19 @@ def test_zoom_grid_places_zooms_like_genetic(built, case):
             (box_a, n_a, off_a), (_, _, off) = gen.levels[-2], gen.levels[-1]
             got.append([int(round((o - oa) / (box_a / n_a))) for o, oa in zip(off, off_a)])
     assert got == want
+
+
+def test_select_nearest_flags_the_finest_cell_at_the_centre(built):
+    gen = _host_only_generator()
+    gen.base_grid(50.0, 32)
+    gen.centre(25.0, 25.0, 25.0)
+    gen.select_cube(10)
+    gen.zoom_grid_with_origin_at(8, 8, 8, 2, 32)
+    gen.centre(49.9, 20.1, 12.6)  # outside the zoom in x: refused
+    with pytest.raises(ValueError):
+        gen.select_nearest()
+    gen.centre(20.1, 12.6, 36.0)
+    gen.select_nearest()
+    dx = 25.0 / 32
+    want = ((int((20.1 - 12.5) // dx)) * 32 + int((12.6 - 12.5) // dx)) * 32 + int((36.0 - 12.5) // dx)
+    assert gen.flagged.tolist() == [want] and len(gen.flagged_levels[0]) == 0
