@@ -388,6 +388,19 @@ class ICGenerator:
         self._call('gic_splice', int(new_seed), ptrs, counts, its)
         return list(its)
 
+    def zerolevel(self, level):
+        """ICGenerator::zeroLevel (ic.hpp:787-802, a testing command): the drawn white noise of
+        one level set to zero."""
+        self.draw()
+        level = int(level)
+        if not 0 <= level < len(self.levels):
+            raise ValueError('level %d does not exist' % level)
+        n = self.levels[level][1]
+        zeros = np.zeros(n * n * (n // 2 + 1) * 2, dtype=np.float64)
+        self._call('gic_set_noise', level, _ptr(zeros))
+
+    zero_level = zerolevel
+
     def reverse(self):
         """ICGenerator::reverse (ic.hpp:1652-1655): the white noise changes sign."""
         self.draw()
@@ -559,6 +572,7 @@ _COMMANDS = {
     'seedfourier_reverse': 'seedfourier_reverse', 'done': 'done', 'chi2': 'chi2',
     'centre': 'centre', 'center': 'centre', 'select_sphere': 'select_sphere', 'select_cube': 'select_cube',
     'select_ellipse': 'select_ellipse', 'select_nearest': 'select_nearest',
+    'zerolevel': 'zerolevel', 'zero_level': 'zerolevel',
     'calculate': 'calculate', 'modify': 'modify', 'clear_modifications': 'clear_modifications',
     'filtering_scale': 'filtering_scale', 'fix_power': 'fix_power',
     'exact_power_spectrum_enforcement': 'fix_power', 'reverse': 'reverse', 'reverse_small_k': 'reverse_small_k',
