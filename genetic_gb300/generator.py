@@ -277,6 +277,95 @@ class ICGenerator:
         self.flagged_levels.append(np.array([cell], dtype=np.uint64))
         self.flagged = self.flagged_levels[-1]
 
+    # -- particle ID files (ic.hpp:1374-1439; io/input.hpp:33-39, 99-106) ---------------
+    def _order(self):
+        flagged = self._flagged_snapshot if getattr(self, '_flagged_type', None) is not None else None
+        return writers.mapper_order(self.levels, self.zoom_masks, flagged)
+
+    def _flags(self):
+        flags = getattr(self, 'flagged_levels', [])
+        if len(flags) != len(self.levels):
+            return [np.zeros(0, dtype=np.uint64) for _ in self.levels]
+        return [np.asarray(f, dtype=np.uint64) for f in flags]
+
+    def dump_id_file(self, fname):
+        """ICGenerator::dumpID: the map indices of the flagged cells that are particles,
+        ascending, one per line (ParticleMapper::getFlaggedParticles)."""
+        lev, cells = self._order()
+        flags = self._flags()
+        keep = np.zeros(len(cells), dtype=bool)
+        for l in range(int(lev.max()) + 1):
+            sel = lev == l
+            keep[sel] = np.isin(cells[sel], flags[min(l, len(flags) - 1)].astype(np.int64))
+        with open(os.path.join(self.base_dir, fname), 'w') as f:
+            f.writelines('%d\n' % i for i in np.flatnonzero(keep))
+
+    def merge_id_file(self, fname):
+        """ICGenerator::appendID: flags the cells of the particles listed in the file, and the
+        replaced cells above them (TwoLevelParticleMapper::flagParticles flags a zoom
+        particle's parent on the level above), then centres on the deepest flagged level."""
+        with open(os.path.join(self.base_dir, fname)) as f:
+            ids = np.unique(np.array(f.read().split(), dtype=np.int64))
+        lev, cells = self._order()
+        if len(ids) and (ids[0] < 0 or ids[-1] >= len(cells)):
+            raise ValueError('Particle ID out of range')
+        nl = len(self.levels)
+        add = [[] for _ in range(nl)]
+        for l, c in zip(lev[ids], cells[ids]):
+            l = min(int(l), nl - 1)  # the flagged-type level lies on the finest grid
+            c = int(c)
+            while True:
+                add[l].append(c)
+                if l == 0:
+                    break
+                mask, ratio, origin = self.zoom_masks[l - 1]
+                n, na = self.levels[l][1], self.levels[l - 1][1]
+                p = [c // (n * n), (c // n) % n, c % n]
+                q = [(p[a] // ratio + origin[a]) % na for a in range(3)]
+                c, l = (q[0] * na + q[1]) * na + q[2], l - 1
+        flags = self._flags()
+        self.flagged_levels = [np.union1d(flags[l].astype(np.int64), np.array(add[l], dtype=np.int64)).astype(np.uint64)
+                               for l in range(nl)]
+        self.flagged = self.flagged_levels[-1]
+        self._centre_on_flags()
+
+    def id_file(self, fname):
+        """ICGenerator::loadID: every flag cleared, then merge_id_file."""
+        self.flagged_levels = [np.zeros(0, dtype=np.uint64) for _ in self.levels]
+        self.merge_id_file(fname)
+
+    IDfile = id_file
+    append_IDfile = merge_id_file
+    dump_IDfile = dump_id_file
+
+    def _centre_on_flags(self):
+        """ICGenerator::getCentre (ic.hpp:1374-1385) with Grid::getCentreWrapped (grid.hpp:466-494):
+        on the deepest level with flags, the mean of the wrapped offsets from its first flagged
+        cell's centroid, added back and wrapped into the box."""
+        period = self.levels[0][0]
+        deep = [l for l, f in enumerate(self.flagged_levels) if len(f)]
+        if not deep:
+            return
+        l = deep[-1]
+        box, n, off = self.levels[l]
+        dx = box / n
+        c = np.asarray(self.flagged_levels[l], dtype=np.int64)
+        idx = (c // (n * n), (c // n) % n, c % n)
+        centre = []
+        for a in range(3):
+            x = idx[a] * dx + off[a] + dx / 2
+            run = 0.0
+            for v in x[1:] - x[0]:
+                if v > period / 2:
+                    v -= period
+                if v < -period / 2:
+                    v += period
+                run += v
+            v = run / len(x) + x[0]
+            v = float(np.fmod(v, period))
+            centre.append(v + period if v < 0 else v)
+        self.centre_point = tuple(centre)
+
     def select_sphere(self, radius):
         r2 = float(np.float32(radius) * np.float32(radius))
         self._select(lambda X, Y, Z: X * X + Y * Y + Z * Z < r2)
@@ -573,6 +662,8 @@ _COMMANDS = {
     'centre': 'centre', 'center': 'centre', 'select_sphere': 'select_sphere', 'select_cube': 'select_cube',
     'select_ellipse': 'select_ellipse', 'select_nearest': 'select_nearest',
     'zerolevel': 'zerolevel', 'zero_level': 'zerolevel',
+    'IDfile': 'id_file', 'id_file': 'id_file', 'append_IDfile': 'merge_id_file', 'merge_id_file': 'merge_id_file',
+    'dump_IDfile': 'dump_id_file', 'dump_id_file': 'dump_id_file',
     'calculate': 'calculate', 'modify': 'modify', 'clear_modifications': 'clear_modifications',
     'filtering_scale': 'filtering_scale', 'fix_power': 'fix_power',
     'exact_power_spectrum_enforcement': 'fix_power', 'reverse': 'reverse', 'reverse_small_k': 'reverse_small_k',
@@ -582,7 +673,7 @@ _COMMANDS = {
     'gadget_particle_type': 'gadget_particle_type', 'gadget_flagged_particle_type': 'gadget_flagged_particle_type',
 }
 # output-side commands handled by genetIC's own writers; accepted and ignored here
-_IGNORED = {'dump_grid', 'dump_ps', 'idfile', 'dump_idfile'}
+_IGNORED = {'dump_grid', 'dump_ps'}
 
 
 def parse_paramfile(path):

@@ -174,3 +174,27 @@ def gadget_type_counts(m, level_types):
     if any(len(s) > 1 for s in per_type):
         return npart, None
     return npart, [min(s) if s else 0.0 for s in per_type]
+
+
+def mapper_order(levels, zoom_masks, flagged=None):
+    """(level, cell) of every particle in genetIC's mapper order (one TwoLevelParticleMapper
+    per zoom level, ic.hpp:1150-1185; twolevelmapper.hpp:262-320, 869-893): each zoom drops
+    its mask's cells from the order so far and appends their blocks in ascending cell id.
+    levels: [(box, n, offset)]; zoom_masks[l - 1] = (mask, ratio, origin); flagged: the
+    finest level's cells moved to the end as their own gadget type (map level len(levels))."""
+    n0 = levels[0][1]
+    lev = np.zeros(n0 ** 3, dtype=np.int64)
+    cells = np.arange(n0 ** 3, dtype=np.int64)
+    steps = [(l, mask, ratio, origin) for l, (mask, ratio, origin) in enumerate(zoom_masks, 1)]
+    if flagged is not None:
+        steps.append((len(levels), flagged, 1, (0, 0, 0)))
+    for l, mask, ratio, origin in steps:
+        n_parent = levels[l - 1][1]
+        n_child = levels[min(l, len(levels) - 1)][1]
+        rep = np.sort(np.asarray(mask, dtype=np.int64))
+        drop = (lev == l - 1) & np.isin(cells, rep)
+        lev, cells = lev[~drop], cells[~drop]
+        fine = block_cells(rep, n_parent, n_child, ratio, origin)
+        lev = np.concatenate([lev, np.full(len(fine), l, dtype=np.int64)])
+        cells = np.concatenate([cells, fine])
+    return lev, cells

@@ -395,6 +395,30 @@ def zoom_grid_goldens():
     np.savez_compressed(os.path.join(HERE, 'zoom_grid_corners.npz'), **out)
 
 
+ID_FILE_IN = [0, 5, 100, 32552 + 3, 32552 + 1000, 34000]
+
+
+def id_file_goldens():
+    """genetIC's particle ID files on the zoom2 case: the ids it dumps for a 3 Mpc/h sphere,
+    and, after loading ID_FILE_IN, the ids it dumps back and the centre it logs."""
+    import re
+    out = {}
+    cases = {'dump': 'centre 25 25 25\nselect_sphere 3\ndump_IDfile ids.txt',
+             'load': 'IDfile in.txt\ndump_IDfile ids.txt'}
+    for name, cmds in cases.items():
+        with tempfile.TemporaryDirectory() as d:
+            write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+            open(os.path.join(d, 'in.txt'), 'w').write(''.join('%d\n' % i for i in ID_FILE_IN))
+            params = ZOOM_PARAMS.format(seedcmd='random_seed', zooms='\n'.join(ZOOMS['zoom2']) + '\n' + cmds, dumps='')
+            open(os.path.join(d, 'paramfile.txt'), 'w').write(params)
+            r = subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True, text=True)
+            out[name + '_ids'] = np.loadtxt(os.path.join(d, 'ids.txt'), dtype=np.int64, ndmin=1)
+            centres = re.findall(r'Centre of region is (\S+) (\S+) (\S+)', r.stdout + r.stderr)
+            if centres:
+                out[name + '_centre'] = np.array([float(v) for v in centres[-1]])
+    np.savez_compressed(os.path.join(HERE, 'id_files_zoom2.npz'), **out)
+
+
 def tipsy3_goldens():
     """The reference's tipsy file of the three-level zoom3 case: its header and the records
     of the finest level (the level-1 particles are all replaced), which follow the level-1
@@ -477,3 +501,4 @@ if __name__ == '__main__':
     gadget_types_goldens()
     flagged_type_goldens()
     zoom_grid_goldens()
+    id_file_goldens()

@@ -448,3 +448,34 @@ def test_select_nearest_flags_the_finest_cell_at_the_centre(built):
     dx = 25.0 / 32
     want = ((int((20.1 - 12.5) // dx)) * 32 + int((12.6 - 12.5) // dx)) * 32 + int((36.0 - 12.5) // dx)
     assert gen.flagged.tolist() == [want] and len(gen.flagged_levels[0]) == 0
+
+
+def _zoom2_host_generator(tmp_path):
+    gen = _host_only_generator()
+    gen.base_dir = str(tmp_path)
+    gen.base_grid(50.0, 32)
+    gen.centre(25, 25, 25)
+    gen.select_cube(10)
+    gen.zoom_grid_with_origin_at(8, 8, 8, 2, 32)
+    return gen
+
+
+def test_id_files_match_genetic(built, tmp_path):
+    """dump_IDfile after flagging a sphere, and IDfile + dump_IDfile of a list mixing coarse
+    and zoom particles, against genetIC's files and logged centre (zoom2 case)."""
+    import sys
+    sys.path.insert(0, GOLDEN)
+    from make_golden import ID_FILE_IN
+    g = np.load(os.path.join(GOLDEN, 'id_files_zoom2.npz'))
+    gen = _zoom2_host_generator(tmp_path)
+    gen.centre(25, 25, 25)
+    gen.select_sphere(3)
+    gen.dump_id_file('a.txt')
+    assert np.loadtxt(tmp_path / 'a.txt', dtype=np.int64).tolist() == g['dump_ids'].tolist()
+    gen = _zoom2_host_generator(tmp_path)
+    (tmp_path / 'in.txt').write_text(''.join('%d\n' % i for i in ID_FILE_IN))
+    gen.id_file('in.txt')
+    gen.dump_id_file('b.txt')
+    assert np.loadtxt(tmp_path / 'b.txt', dtype=np.int64).tolist() == g['load_ids'].tolist()
+    # the centre genetIC logs to 12 significant digits
+    assert np.allclose(gen.centre_point, g['load_centre'], rtol=0, atol=1e-9)
