@@ -676,6 +676,10 @@ _COMMANDS = {
 _IGNORED = {'dump_grid', 'dump_ps'}
 
 
+_COMMANDS_LOWER = {k.lower(): v for k, v in _COMMANDS.items()}
+_IGNORED_LOWER = {k.lower() for k in _IGNORED}
+
+
 def parse_paramfile(path):
     """(line number, method, args) for each realisation command of a paramfile."""
     out = []
@@ -685,12 +689,13 @@ def parse_paramfile(path):
             if not line:
                 continue
             parts = line.split()
-            cmd, args = parts[0], parts[1:]
-            if cmd in _IGNORED:
+            # genetIC matches command names case-insensitively (tools/parser.hpp:171, 243)
+            cmd, args = parts[0].lower(), parts[1:]
+            if cmd in _IGNORED_LOWER:
                 continue
-            if cmd not in _COMMANDS:
-                raise ValueError('%s:%d: command %r is not on the GPU realisation path' % (path, lineno, cmd))
-            out.append((lineno, _COMMANDS[cmd], args))
+            if cmd not in _COMMANDS_LOWER:
+                raise ValueError('%s:%d: command %r is not on the GPU realisation path' % (path, lineno, parts[0]))
+            out.append((lineno, _COMMANDS_LOWER[cmd], args))
     return out
 
 
