@@ -338,6 +338,20 @@ class ICGenerator:
     append_IDfile = merge_id_file
     dump_IDfile = dump_id_file
 
+    def dump_tipsy(self, fname):
+        """ICGenerator::saveTipsyArray (ic.hpp:891-899, io/tipsy.hpp:39-52): the overdensity at
+        every particle in mapper order, as floats after a 4-byte count."""
+        lev, cells = self._order()
+        nl = len(self.levels)
+        deltas = [self.field(l, 'delta').ravel() for l in range(nl)]
+        vals = np.empty(len(cells), dtype=np.float32)
+        for l in np.unique(lev):
+            sel = lev == l
+            vals[sel] = deltas[min(int(l), nl - 1)][cells[sel]]
+        with open(os.path.join(self.base_dir, fname), 'wb') as f:
+            f.write(np.array([len(cells) & 0xffffffff], dtype='<u4').tobytes())
+            f.write(vals.astype('<f4').tobytes())
+
     def _centre_on_flags(self):
         """ICGenerator::getCentre (ic.hpp:1374-1385) with Grid::getCentreWrapped (grid.hpp:466-494):
         on the deepest level with flags, the mean of the wrapped offsets from its first flagged
@@ -663,7 +677,7 @@ _COMMANDS = {
     'select_ellipse': 'select_ellipse', 'select_nearest': 'select_nearest',
     'zerolevel': 'zerolevel', 'zero_level': 'zerolevel',
     'IDfile': 'id_file', 'id_file': 'id_file', 'append_IDfile': 'merge_id_file', 'merge_id_file': 'merge_id_file',
-    'dump_IDfile': 'dump_id_file', 'dump_id_file': 'dump_id_file',
+    'dump_IDfile': 'dump_id_file', 'dump_id_file': 'dump_id_file', 'dump_tipsy': 'dump_tipsy',
     'calculate': 'calculate', 'modify': 'modify', 'clear_modifications': 'clear_modifications',
     'filtering_scale': 'filtering_scale', 'fix_power': 'fix_power',
     'exact_power_spectrum_enforcement': 'fix_power', 'reverse': 'reverse', 'reverse_small_k': 'reverse_small_k',

@@ -419,6 +419,18 @@ def id_file_goldens():
     np.savez_compressed(os.path.join(HERE, 'id_files_zoom2.npz'), **out)
 
 
+def dump_tipsy_goldens():
+    """genetIC's dump_tipsy of the zoom2 case after done: the overdensity of every particle in
+    mapper order (a 4-byte count, then floats)."""
+    with tempfile.TemporaryDirectory() as d:
+        write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+        params = ZOOM_PARAMS.format(seedcmd='random_seed', zooms='\n'.join(ZOOMS['zoom2']), dumps='dump_tipsy field.tipsy')
+        open(os.path.join(d, 'paramfile.txt'), 'w').write(params)
+        subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True)
+        raw = open(os.path.join(d, 'field.tipsy'), 'rb').read()
+        np.savez_compressed(os.path.join(HERE, 'dump_tipsy_zoom2.npz'), raw=np.frombuffer(raw, np.uint8).copy())
+
+
 def tipsy3_goldens():
     """The reference's tipsy file of the three-level zoom3 case: its header and the records
     of the finest level (the level-1 particles are all replaced), which follow the level-1
@@ -502,3 +514,4 @@ if __name__ == '__main__':
     flagged_type_goldens()
     zoom_grid_goldens()
     id_file_goldens()
+    dump_tipsy_goldens()

@@ -479,3 +479,16 @@ def test_id_files_match_genetic(built, tmp_path):
     assert np.loadtxt(tmp_path / 'b.txt', dtype=np.int64).tolist() == g['load_ids'].tolist()
     # the centre genetIC logs to 12 significant digits
     assert np.allclose(gen.centre_point, g['load_centre'], rtol=0, atol=1e-9)
+
+
+def test_dump_tipsy_matches_genetic_file(built, bbks, tmp_path):
+    """dump_tipsy after done: the combined overdensity at every particle in mapper order,
+    byte for byte the reference's file (the oracle's delta standing in for the device's)."""
+    from conftest import COSMO
+    g = np.load(os.path.join(GOLDEN, 'dump_tipsy_zoom2.npz'))
+    w = fo.white_noise_levels([32, 32], 8896131, 2)
+    out = fo.zoom_realisation(w, ZOOM2, fo.CambPower(bbks, COSMO))
+    gen = _zoom2_host_generator(tmp_path)
+    gen.field = lambda l, name: out[l][0]
+    gen.dump_tipsy('field.tipsy')
+    assert open(tmp_path / 'field.tipsy', 'rb').read() == bytes(g['raw'])
