@@ -59,6 +59,7 @@ class ICGenerator:
         # gadget_flagged_particle_type: the type and the finest level's flags at genetIC's
         # last particle-mapper rebuild (ic.hpp:705-714, 1176-1185)
         self._flagged_type, self._flagged_snapshot = None, None
+        self.gadget_files = 1
 
     # -- lifetime --------------------------------------------------------------
     def close(self):
@@ -155,6 +156,13 @@ class ICGenerator:
         flags = getattr(self, 'flagged_levels', [])
         cells = flags[-1] if len(flags) == len(self.levels) and len(flags) else np.zeros(0, dtype=np.uint64)
         self._flagged_snapshot = np.sort(np.asarray(cells, dtype=np.uint64))
+
+    def gadget_num_files(self, n):
+        """ICGenerator::setGadgetNumFiles (ic.hpp:674-676): gadget output over n files."""
+        n = int(n)
+        if n < 1:
+            raise ValueError('the number of gadget files must be positive')
+        self.gadget_files = n
 
     def gadget_flagged_particle_type(self, t):
         """ICGenerator::setFlaggedGadgetParticleType (ic.hpp:705-714): the finest level's
@@ -654,9 +662,19 @@ class ICGenerator:
         npart, masses = writers.gadget_type_counts(m, types)
         variable = masses is None
         c = self.cosmo
-        h = writers.gadget_header(version, npart, [0.0] * 6 if variable else masses, 1.0 / (1.0 + c['redshift']),
-                                  c['redshift'], self.levels[0][0], c['omega_m'], c['omega_lambda'], c['hubble'])
-        writers.write_gadget(path, h, pos3, vel3, ids, mass if variable else None)
+        nfiles = getattr(self, 'gadget_files', 1)
+        per_file, per_type = writers.gadget_file_split(npart, nfiles)
+        at = 0
+        for i, (nf, counts) in enumerate(zip(per_file, per_type)):
+            # the header's counts are this file's; the totals and the file count are the run's
+            h = bytearray(writers.gadget_header(version, npart, [0.0] * 6 if variable else masses,
+                                                1.0 / (1.0 + c['redshift']), c['redshift'], self.levels[0][0],
+                                                c['omega_m'], c['omega_lambda'], c['hubble'], num_files=nfiles))
+            h[0:24] = np.array(counts, dtype='<u4').tobytes()
+            s = slice(at, at + nf)
+            writers.write_gadget(path if nfiles == 1 else '%s.%d' % (path, i), bytes(h), pos3[s], vel3[s], ids[s],
+                                 mass[s] if variable else None)
+            at += nf
 
     def gaussian_stream(self, seed, count):
         out = np.empty(int(count), dtype=np.float64)
@@ -684,7 +702,7 @@ _COMMANDS = {
     'splice': 'splice',
     'apply_modifications': 'apply_modifications',
     'outname': 'outname', 'outdir': 'outdir', 'outformat': 'outformat',
-    'gadget_particle_type': 'gadget_particle_type', 'gadget_flagged_particle_type': 'gadget_flagged_particle_type',
+    'gadget_particle_type': 'gadget_particle_type', 'gadget_num_files': 'gadget_num_files', 'gadget_flagged_particle_type': 'gadget_flagged_particle_type',
 }
 # output-side commands handled by genetIC's own writers; accepted and ignored here
 _IGNORED = {'dump_grid', 'dump_ps'}

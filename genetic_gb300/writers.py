@@ -198,3 +198,22 @@ def mapper_order(levels, zoom_masks, flagged=None):
         lev = np.concatenate([lev, np.full(len(fine), l, dtype=np.int64)])
         cells = np.concatenate([cells, fine])
     return lev, cells
+
+
+def gadget_file_split(npart, nfiles):
+    """How GadgetOutput spreads the particles over `nfiles` files (gadget.hpp:355-420):
+    nTotal / nFiles particles per file, the last file taking the rest, and each file's
+    particles taken from the types in order.  Returns (particles per file, per-file counts
+    per type)."""
+    total = sum(npart)
+    per_file = [total // nfiles] * (nfiles - 1) + [total - (total // nfiles) * (nfiles - 1)]
+    left = list(npart)
+    per_type = []
+    for nf in per_file:
+        room, this = nf, [0] * 6
+        for t in range(6):
+            this[t] = min(left[t], room)
+            room -= this[t]
+            left[t] -= this[t]
+        per_type.append(this)
+    return per_file, per_type

@@ -431,6 +431,22 @@ def dump_tipsy_goldens():
         np.savez_compressed(os.path.join(HERE, 'dump_tipsy_zoom2.npz'), raw=np.frombuffer(raw, np.uint8).copy())
 
 
+def gadget_files_goldens():
+    """The zoom2 case written over 3 gadget2 files: each file's header bytes and ids."""
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+        params = ZOOM_PARAMS.format(seedcmd='random_seed', zooms='\n'.join(ZOOMS['zoom2']) + '\ngadget_num_files 3', dumps='')
+        open(os.path.join(d, 'paramfile.txt'), 'w').write(params.replace('outformat tipsy', 'outformat gadget2'))
+        subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True)
+        for i in range(3):
+            rec = read_fortran_records(os.path.join(d, 'out.gadget2.%d' % i))
+            out['header%d' % i] = np.frombuffer(rec[0], np.uint8).copy()
+            out['ids%d' % i] = np.frombuffer(rec[3], '<u8').copy()
+            out['nrec%d' % i] = np.int64(len(rec))
+    np.savez_compressed(os.path.join(HERE, 'gadget_files_zoom2.npz'), **out)
+
+
 def tipsy3_goldens():
     """The reference's tipsy file of the three-level zoom3 case: its header and the records
     of the finest level (the level-1 particles are all replaced), which follow the level-1
@@ -515,3 +531,4 @@ if __name__ == '__main__':
     zoom_grid_goldens()
     id_file_goldens()
     dump_tipsy_goldens()
+    gadget_files_goldens()

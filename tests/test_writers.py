@@ -492,3 +492,19 @@ def test_dump_tipsy_matches_genetic_file(built, bbks, tmp_path):
     gen.field = lambda l, name: out[l][0]
     gen.dump_tipsy('field.tipsy')
     assert open(tmp_path / 'field.tipsy', 'rb').read() == bytes(g['raw'])
+
+
+def test_gadget_num_files_matches_genetic(built, zoom2_particles, tmp_path):
+    """gadget_num_files 3: each file's header and ids as genetIC splits them."""
+    from genetic_gb300 import writers
+    z = zoom2_particles
+    g = np.load(os.path.join(GOLDEN, 'gadget_files_zoom2.npz'))
+    gen = _zoom2_host_generator(tmp_path)
+    gen.particles = lambda l: (z['pos'][l], z['vel'][l])
+    gen.gadget_num_files(3)
+    gen.cosmo.update(dict(omega_m=0.31, omega_lambda=0.69, hubble=0.68, redshift=99.0))
+    gen.write_gadget(str(tmp_path / 'out.gadget2'))
+    for i in range(3):
+        rec = writers.read_fortran_records(tmp_path / ('out.gadget2.%d' % i))
+        assert len(rec) == int(g['nrec%d' % i]) and rec[0] == bytes(g['header%d' % i])
+        assert np.array_equal(np.frombuffer(rec[3], np.uint64), g['ids%d' % i])
