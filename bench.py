@@ -19,6 +19,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -152,11 +153,10 @@ class Clocks:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, 'gpurun_out', 'bench_clocks.csv')
+        self.path = os.path.join(tempfile.gettempdir(), 'gic_bench_clocks_%d.csv' % os.getpid())
 
     def __enter__(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, 'w')
             self.proc = subprocess.Popen(
                 ['nvidia-smi', '-i', str(self.index),

@@ -13,8 +13,9 @@ CSRC = os.path.join(HERE, 'csrc')
 BUILD = os.path.join(HERE, '_build')
 LIB = os.path.join(HERE, 'libgicgpu.so')
 SOURCES = ['capi.cu', 'rng.cu', 'fft.cu', 'kspace.cu', 'particles.cu', 'zoom.cu', 'modify.cu', 'batch.cu', 'writers.cu']
-# the host packer rounds every product and difference separately, as genetIC's host build does
-SOURCE_FLAGS = {'writers.cu': ['-Xcompiler', '-ffp-contract=off']}
+# the host packer rounds every product and difference separately, as genetIC's host build does;
+# the transfer spline's host solve gives the same bits on every host architecture
+SOURCE_FLAGS = {'writers.cu': ['-Xcompiler', '-ffp-contract=off'], 'kspace.cu': ['-Xcompiler', '-ffp-contract=off']}
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-Xcompiler', '-fvisibility=hidden',
          '--expt-relaxed-constexpr']

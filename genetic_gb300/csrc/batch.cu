@@ -61,6 +61,7 @@ void append_signature(const Context &C, std::vector<uintptr_t> &sig) {
 }
 
 void field_maps(Context &C, int order) {
+  AccountScope scope(C.account);
   const int nl = (int)C.levels.size();
   for (int l = 0; l < nl; ++l) za_fields(C, l);
   for (int l = 1; l < nl; ++l) zoom_combine(C, l);
@@ -190,6 +191,7 @@ GIC_API int gic_batch_realise(gic_batch *b, const unsigned long *seeds, const in
       if (i >= n) return;
       gic::Context &C = b->ctxs[i]->impl;
       try {
+        gic::AccountScope scope(C.account);
         gic::cuda_check(cudaSetDevice(C.device), "cudaSetDevice");
         if (C.levels.empty()) gic::fail(GIC_ERR_NOT_READY, "a context of the batch has no grid levels");
         gic::cuda_check(cudaStreamWaitEvent(C.stream, b->start, 0), "cudaStreamWaitEvent");
@@ -246,7 +248,7 @@ GIC_API int gic_batch_realise(gic_batch *b, const unsigned long *seeds, const in
     }
     gic::cuda_check(cudaStreamSynchronize(b->origin), "cudaStreamSynchronize");
     for (auto *c : b->ctxs)
-      if (gic::take_fft_wait_error(c->impl)) gic::fail(GIC_ERR_CUDA, c->impl.last_error);
+      if (gic::take_fft_wait_error(c->impl)) gic::fail(GIC_ERR_TIMEOUT, c->impl.last_error);
     for (auto *c : b->ctxs)
       for (auto &L : c->impl.levels) {
         L->have_fields = true;

@@ -154,6 +154,8 @@ thread_local std::string g_create_error;
 }  // namespace
 
 std::string &host_error() { return g_create_error; }
+
+thread_local MemAccount *t_account = nullptr;
 }  // namespace gic
 
 using gic::Error;
@@ -162,6 +164,7 @@ using gic::Error;
   if (!(ctxp)) return GIC_ERR_INVALID_ARG;                 \
   gic::Context &C = (ctxp)->impl;                          \
   try {                                                    \
+    gic::AccountScope account_scope_(C.account);           \
     gic::use_device(C);
 #define API_END                                            \
   }                                                        \
@@ -177,7 +180,7 @@ using gic::Error;
     C.last_error = e.what();                               \
     return GIC_ERR_INTERNAL;                               \
   }                                                        \
-  if (gic::take_fft_wait_error(C)) return GIC_ERR_CUDA;   \
+  if (gic::take_fft_wait_error(C)) return GIC_ERR_TIMEOUT; \
   C.last_error.clear();                                    \
   return GIC_OK;
 
@@ -206,6 +209,7 @@ int gic_create(gic_ctx **out, const gic_device_opts *opts) {
   if (!c) return GIC_ERR_OOM;
   c->impl.device = device;
   c->impl.precision = precision;
+  c->impl.account.limit = opts ? opts->mem_limit : 0;
   if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->impl.stream, cudaStreamNonBlocking) != cudaSuccess) {
     gic::g_create_error = cudaGetErrorString(cudaGetLastError());
     delete c;
@@ -232,6 +236,20 @@ int gic_create(gic_ctx **out, const gic_device_opts *opts) {
 int gic_launch_count(unsigned long long *count) {
   if (!count) return GIC_ERR_INVALID_ARG;
   *count = gic::g_launches.load();
+  return GIC_OK;
+}
+
+int gic_set_fft_wait(gic_ctx *ctx, unsigned spin_limit, int unreachable) {
+  if (!ctx) return GIC_ERR_INVALID_ARG;
+  ctx->impl.fft.plane_spin_limit = spin_limit ? spin_limit : (1u << 22);
+  ctx->impl.fft.plane_wait_extra = unreachable ? 1u : 0u;
+  return GIC_OK;
+}
+
+int gic_memory_use(gic_ctx *ctx, size_t *in_use, size_t *limit) {
+  if (!ctx) return GIC_ERR_INVALID_ARG;
+  if (in_use) *in_use = ctx->impl.account.used.load();
+  if (limit) *limit = ctx->impl.account.limit;
   return GIC_OK;
 }
 

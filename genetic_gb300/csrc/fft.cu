@@ -957,8 +957,9 @@ __global__ void __launch_bounds__(NT) k_fft_rows_r2c_fixed(typename Cx<T>::type 
 //   c2r (INV): first kind = y transform of TC columns (sign +1), second = RPC rows c2r
 //   r2c:       first kind = RPC rows r2c, second = y transform of TC columns (sign -1)
 // sync: N plane counters and the ticket, zeroed before the launch; wait_flag is set
-// when a wait gives up (the host reports it).
-constexpr unsigned kPlaneSpinLimit = 1u << 22;
+// when a wait gives up (the host reports it).  A wait polls at most spin_limit times
+// (100 ns apart) for `need` finished first-kind tasks of its plane: the plane's count
+// of them, unless a test raises it to make every wait give up.
 
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p) {
   unsigned v;
@@ -977,7 +978,8 @@ struct PlaneTasks {
 template <typename T, int N, int TC, int RPC, int NT, bool INV>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_fft_planes(typename Cx<T>::type *data,
                                                                const typename Cx<T>::type *tw, T scale, int group,
-                                                               int lag, unsigned *sync, int *wait_flag) {
+                                                               int lag, unsigned *sync, int *wait_flag,
+                                                               unsigned spin_limit, unsigned need) {
   using C = typename Cx<T>::type;
   using PT = PlaneTasks<N, TC, RPC>;
   constexpr int H = N / 2, S = PT::S;
@@ -1017,8 +1019,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_fft_planes(typename Cx<T>::ty
     if (!first) {
       if (threadIdx.x == 0) {
         unsigned spins = 0;
-        while (ld_acquire_gpu(plane_done + plane) < (unsigned)P1) {
-          if (++spins > kPlaneSpinLimit) {
+        while (ld_acquire_gpu(plane_done + plane) < need) {
+          if (++spins > spin_limit) {
             atomicExch(wait_flag, 1);
             break;
           }
@@ -1230,7 +1232,8 @@ struct FixedFft {
       ctx.fft.plane_sync.ensure((size_t)(N + 1) * sizeof(unsigned));
       GIC_CUDA(cudaMemsetAsync(ctx.fft.plane_sync.ptr, 0, (size_t)(N + 1) * sizeof(unsigned), ctx.stream));
       k_fft_planes<T, N, PTC, PRPC, PNT, INV><<<std::min(ctas, total), PNT, smem, ctx.stream>>>(
-          d, tw, scale, group, lag, ctx.fft.plane_sync.template as<unsigned>(), ctx.fft.wait_flag());
+          d, tw, scale, group, lag, ctx.fft.plane_sync.template as<unsigned>(), ctx.fft.wait_flag(),
+          ctx.fft.plane_spin_limit, (unsigned)(INV ? PT::NY : PT::NZ) + ctx.fft.plane_wait_extra);
       launched();
     }
   }

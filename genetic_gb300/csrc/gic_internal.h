@@ -6,6 +6,7 @@
 #include <cmath>
 #include <vector>
 #include <memory>
+#include <atomic>
 #include "../../include/gicgpu.h"
 
 namespace gic {
@@ -23,16 +24,36 @@ void count_launches(unsigned long long kernels);  // kernels run by a graph laun
 void cuda_check(cudaError_t e, const char *what);
 #define GIC_CUDA(call) ::gic::cuda_check((call), #call)
 
+// Device memory charged to a context, against its gic_device_opts.mem_limit.  A
+// context's API calls (and a batch's workers) make its account the thread's current
+// one; a DevBuf is charged to the account current when it grows and credited back
+// when it is released.
+struct MemAccount {
+  std::atomic<size_t> used{0};
+  size_t limit = 0;  // bytes; 0 = no limit
+};
+extern thread_local MemAccount *t_account;
+struct AccountScope {
+  MemAccount *prev;
+  explicit AccountScope(MemAccount &a) : prev(t_account) { t_account = &a; }
+  ~AccountScope() { t_account = prev; }
+  AccountScope(const AccountScope &) = delete;
+  AccountScope &operator=(const AccountScope &) = delete;
+};
+
 // Owning device allocation.
 struct DevBuf {
   void *ptr = nullptr;
   size_t bytes = 0;
+  MemAccount *acct = nullptr;
   DevBuf() = default;
   DevBuf(const DevBuf &) = delete;
   DevBuf &operator=(const DevBuf &) = delete;
   ~DevBuf() { release(); }
   void release() {
     if (ptr) cudaFree(ptr);
+    if (acct) acct->used -= bytes;
+    acct = nullptr;
     ptr = nullptr;
     bytes = 0;
   }
@@ -40,6 +61,10 @@ struct DevBuf {
     if (nbytes <= bytes && ptr) return;
     release();
     if (nbytes == 0) return;
+    MemAccount *a = t_account;
+    if (a && a->limit && a->used.load() + nbytes > a->limit)
+      fail(GIC_ERR_OOM, "device allocation of " + std::to_string(nbytes) + " bytes would exceed the context's mem_limit of " +
+                            std::to_string(a->limit) + " bytes (" + std::to_string(a->used.load()) + " in use)");
     cudaError_t e = cudaMalloc(&ptr, nbytes);
     if (e != cudaSuccess) {
       cudaGetLastError();
@@ -47,6 +72,10 @@ struct DevBuf {
       fail(GIC_ERR_OOM, "cudaMalloc of " + std::to_string(nbytes) + " bytes failed");
     }
     bytes = nbytes;
+    if (a) {
+      a->used += nbytes;
+      acct = a;
+    }
   }
   template <typename T> T *as() const { return static_cast<T *>(ptr); }
 };
@@ -126,6 +155,9 @@ struct Transfer {
   double amplitude = 0;  // (sigma8/sigma8_pre * D(a)/D(1))^2
   double sigma8_pre = 0;
   bool ready = false;
+  // FNV-1a hash of the table and the cosmology it was normalised with: a repeated
+  // gic_set_transfer with the same inputs finds the state already built
+  uint64_t inputs_hash = 0;
 };
 
 struct FftTables {
@@ -151,6 +183,10 @@ struct FftTables {
   // mapped host memory the kernel sets when one of its waits gives up
   DevBuf plane_sync;
   int *wait_flag_host = nullptr, *wait_flag_dev = nullptr;
+  // polls per wait before it gives up (100 ns apart: about 0.4 s), and a count added to
+  // each wait's target (0; tests set 1 so that no wait can finish)
+  unsigned plane_spin_limit = 1u << 22;
+  unsigned plane_wait_extra = 0;
   int *wait_flag();
   FftTables() = default;
   FftTables(const FftTables &) = delete;
@@ -228,6 +264,7 @@ struct CachedTable {
 };
 
 struct Context {
+  MemAccount account;  // first: destroyed after every buffer charged to it
   int device = 0;
   int precision = GIC_FP64;
   cudaStream_t stream = nullptr;

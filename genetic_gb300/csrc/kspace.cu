@@ -20,13 +20,14 @@
 namespace gic {
 namespace {
 
-// natural cubic spline (second-derivative form) solved by one thread; n ~ 10^3
-__global__ void k_spline_solve(const double *x, const double *y, double *c, int n, double *work) {
-  if (blockIdx.x != 0 || threadIdx.x != 0) return;
-  for (int i = 0; i < n; ++i) c[i] = 0.0;
+// Natural cubic spline (second-derivative form): c[i] (= y''/2) at the knots from the
+// tridiagonal system, solved on the host (n ~ 10^3: microseconds) and uploaded.
+void spline_solve_host(const std::vector<double> &x, const std::vector<double> &y, std::vector<double> &c) {
+  const int n = (int)x.size();
+  c.assign(n, 0.0);
   if (n < 3) return;
-  int m = n - 2;
-  double *diag = work, *off = work + m, *rhs = work + 2 * m;
+  const int m = n - 2;
+  std::vector<double> diag(m), off(m), rhs(m);
   for (int i = 0; i < m; ++i) {
     double h0 = x[i + 1] - x[i], h1 = x[i + 2] - x[i + 1];
     double g0 = h0 != 0.0 ? 1.0 / h0 : 0.0, g1 = h1 != 0.0 ? 1.0 / h1 : 0.0;
@@ -41,6 +42,15 @@ __global__ void k_spline_solve(const double *x, const double *y, double *c, int 
   }
   c[m] = rhs[m - 1] / diag[m - 1];
   for (int i = m - 1; i-- > 0;) c[i + 1] = (rhs[i] - off[i] * c[i + 2]) / diag[i];
+}
+
+uint64_t fnv1a(uint64_t h, const void *data, size_t bytes) {
+  const unsigned char *p = static_cast<const unsigned char *>(data);
+  for (size_t i = 0; i < bytes; ++i) {
+    h ^= p[i];
+    h *= 1099511628211ull;
+  }
+  return h;
 }
 
 __device__ double spline_eval(const double *x, const double *y, const double *c, int n, double v) {
@@ -66,18 +76,10 @@ __device__ double transfer_at(const double *lx, const double *ly, const double *
   return exp(spline_eval(lx, ly, c, n, l));
 }
 
-// k_i of `for (k = kmin; k < kmax; k += dk)`, accumulated exactly as written
-__global__ void k_sigma8_ks(double kmin, double kmax, double dk, double *ks, int cap, int *count) {
-  if (blockIdx.x != 0 || threadIdx.x != 0) return;
-  int i = 0;
-  for (double k = kmin; k < kmax && i < cap; k += dk) ks[i++] = k;
-  *count = i;
-}
-
-__global__ void k_sigma8_terms(const double *ks, const int *count, double ns, double radius, const double *lx,
+// terms of calculateLinearVarianceInSphere's sum (camb.hpp:300-328) at the host-accumulated k_i
+__global__ void k_sigma8_terms(const double *ks, int cnt, double ns, double radius, const double *lx,
                                const double *ly, const double *c, int n, double *partial) {
   __shared__ double red[256];
-  int cnt = *count;
   double acc = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
     double k = ks[i];
@@ -265,6 +267,16 @@ void transfer_setup(Context &ctx, const double *table, int nrows, int ncols) {
   if (!ctx.have_cosmo) fail(GIC_ERR_NOT_READY, "set the cosmology before the transfer function");
   if (ncols != 7 && ncols != 13) fail(GIC_ERR_INVALID_ARG, "CAMB transfer file doesn't have a sensible number of columns");
   if (nrows < 2) fail(GIC_ERR_INVALID_ARG, "transfer table too short");
+  Transfer &T = ctx.transfer;
+  // an unchanged table and cosmology leave the state as it is (callers re-upload the
+  // same table once per realisation)
+  uint64_t h = 1469598103934665603ull;
+  h = fnv1a(h, &nrows, sizeof nrows);
+  h = fnv1a(h, &ncols, sizeof ncols);
+  h = fnv1a(h, table, (size_t)nrows * ncols * sizeof(double));
+  h = fnv1a(h, &ctx.cosmo, sizeof ctx.cosmo);
+  if (T.ready && T.inputs_hash == h) return;
+  T.ready = false;
   // species columns: dm -> 1, all -> 6; normalised by the first row's column 1
   double tnorm = table[1];
   std::vector<double> k, tall, tdm;
@@ -291,10 +303,13 @@ void transfer_setup(Context &ctx, const double *table, int nrows, int ncols) {
   if (lx_all.size() < 2 || lx_dm.size() < 2)
     fail(GIC_ERR_INVALID_ARG, "Could not find enough valid values in the transfer function");
   if (lx_all.size() != lx_dm.size()) fail(GIC_ERR_INVALID_ARG, "transfer columns with invalid entries are not supported");
-  Transfer &T = ctx.transfer;
   int n = (int)lx_all.size();
   T.nrows = n;
   cudaStream_t s = ctx.stream;
+  // the spline's second derivatives: a serial recurrence, solved on the host
+  std::vector<double> c_all, c_dm;
+  spline_solve_host(lx_all, ly_all, c_all);
+  spline_solve_host(lx_dm, ly_dm, c_dm);
   T.lnk.ensure(n * sizeof(double));
   T.lnT_all.ensure(n * sizeof(double));
   T.c_all.ensure(n * sizeof(double));
@@ -303,29 +318,29 @@ void transfer_setup(Context &ctx, const double *table, int nrows, int ncols) {
   GIC_CUDA(cudaMemcpyAsync(T.lnk.ptr, lx_all.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
   GIC_CUDA(cudaMemcpyAsync(T.lnT_all.ptr, ly_all.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
   GIC_CUDA(cudaMemcpyAsync(T.lnT_dm.ptr, ly_dm.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
-  DevBuf work;
-  work.ensure(3 * (size_t)n * sizeof(double));
-  k_spline_solve<<<1, 1, 0, s>>>(T.lnk.as<double>(), T.lnT_all.as<double>(), T.c_all.as<double>(), n,
-                                 work.as<double>());
-  k_spline_solve<<<1, 1, 0, s>>>(T.lnk.as<double>(), T.lnT_dm.as<double>(), T.c_dm.as<double>(), n,
-                                 work.as<double>());
-  launched(2);
+  GIC_CUDA(cudaMemcpyAsync(T.c_all.ptr, c_all.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+  GIC_CUDA(cudaMemcpyAsync(T.c_dm.ptr, c_dm.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
 
-  // sigma8 before normalisation, radius 8 Mpc/h, species "all"
+  // sigma8 before normalisation, radius 8 Mpc/h, species "all".  The k_i of
+  // `for (k = kmin; k < kmax; k += dk)` are accumulated on the host exactly as written
+  // (a serial recurrence); the terms are summed on the device.
   const double radius = 8.0;
   double kmax = std::min(k.back(), 200.0 / radius) * 0.999999;
   double kmin = k[0] * 1.000001;
   double dk = (kmax - kmin) / 50000.;
   const int cap = 50100;
-  DevBuf ks, cnt, partial;
-  ks.ensure(cap * sizeof(double));
-  cnt.ensure(sizeof(int));
+  std::vector<double> hks;
+  hks.reserve(cap);
+  for (double kk = kmin; kk < kmax && (int)hks.size() < cap; kk += dk) hks.push_back(kk);
+  const int count = (int)hks.size();
+  DevBuf ks, partial;
+  ks.ensure(std::max(count, 1) * sizeof(double));
   const int blocks = 64;
   partial.ensure(blocks * sizeof(double));
-  k_sigma8_ks<<<1, 1, 0, s>>>(kmin, kmax, dk, ks.as<double>(), cap, cnt.as<int>());
-  k_sigma8_terms<<<blocks, 256, 0, s>>>(ks.as<double>(), cnt.as<int>(), ctx.cosmo.ns, radius, T.lnk.as<double>(),
+  if (count) GIC_CUDA(cudaMemcpyAsync(ks.ptr, hks.data(), count * sizeof(double), cudaMemcpyHostToDevice, s));
+  k_sigma8_terms<<<blocks, 256, 0, s>>>(ks.as<double>(), count, ctx.cosmo.ns, radius, T.lnk.as<double>(),
                                         T.lnT_all.as<double>(), T.c_all.as<double>(), n, partial.as<double>());
-  launched(2);
+  launched(1);
   std::vector<double> hp(blocks);
   GIC_CUDA(cudaMemcpyAsync(hp.data(), partial.ptr, blocks * sizeof(double), cudaMemcpyDeviceToHost, s));
   GIC_CUDA(cudaStreamSynchronize(s));
@@ -342,6 +357,7 @@ void transfer_setup(Context &ctx, const double *table, int nrows, int ncols) {
   T.lnk_min = lx_all.front();
   T.lnk_max = lx_all.back();
   T.ready = true;
+  T.inputs_hash = h;
   ctx.table_cache.clear();
   for (auto &L : ctx.levels) {
     L->sqrtp.release();

@@ -17,6 +17,7 @@
 //     kz<0 and of modes with a zero component) the later draw wins, found with
 //     an atomicMax over draw indices, then one write per winning draw.
 #include "gic_internal.h"
+#include <cuda.h>
 #include "bigint576.h"
 #include "ddlog.h"
 #include "zig_tables.h"
@@ -887,16 +888,17 @@ void draw_noise_all(Context &ctx, unsigned long long seed, int mode) {
 // ---- allocation-free gaussian stream ------------------------------------------------
 //
 // For callers that cannot allocate device memory themselves -- code running
-// inside another runtime's memory pool or budget, or under a stream capture,
-// where a cudaMalloc is not permitted -- this variant of the gaussian-stream
-// pipeline keeps all its scratch (the raw RANLUX numbers, the chunk jump
-// multipliers, the segment walk tables, the stream descriptor and the underrun
-// flag) in one file-scope device array.  The array is NoallocScratchBytes
-// bytes on every device that loads the library, for the lifetime of the
-// process, and every call shares it: calls that overlap on the GPU (different
-// streams or host threads) race on it and must be serialised by the caller.
-// Every region a call reads is written by that same call first (the flag is
-// cleared), so no state carries over from an earlier call.
+// inside another runtime's memory pool or budget, where a cudaMalloc of its
+// own is not permitted -- this variant of the gaussian-stream pipeline keeps
+// all its scratch (the raw RANLUX numbers, the chunk jump multipliers, the
+// segment walk tables, the stream descriptor and the underrun flag) in one
+// file-scope device array.  The array is NoallocScratchBytes bytes on every
+// device that loads the library, for the lifetime of the process, and every
+// call shares it: calls that overlap on the GPU (different streams or host
+// threads) race on it and must be serialised by the caller.  Every region a
+// call reads is written by that same call first (the flag is cleared), so no
+// state carries over from an earlier call.  A call reads the underrun flag
+// back and synchronises the caller's stream before it returns.
 
 constexpr unsigned long long kNoallocMaxGauss = GIC_NOALLOC_MAX_GAUSSIANS;
 constexpr size_t NoallocScratchBytes = 24ull << 20;
@@ -952,9 +954,43 @@ NoallocLayout noalloc_layout(unsigned long long raw_count, unsigned long long nc
   return L;
 }
 
-// device address of the scratch array, looked up once per device
+// Device address of the scratch array, looked up once per device and CUDA
+// context: a context made after cudaDeviceReset loads the module again, so the
+// address is looked up again when the current context's id changes.
 std::mutex g_noalloc_mutex;
-void *g_noalloc_base[64];
+struct NoallocSlot {
+  unsigned long long ctx_id;
+  void *base;
+};
+NoallocSlot g_noalloc_slot[64];
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+
+// id of the current CUDA context (0 when it cannot be read); the driver calls
+// are reached through the runtime, so the library does not link libcuda
+unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+    cudaGetLastError();
+    looked_up = true;
+  }
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&c) == CUDA_SUCCESS && c && get_id(c, &id) == CUDA_SUCCESS) return id;
+  return 0;
+}
 
 }  // namespace
 
@@ -965,16 +1001,19 @@ static int noalloc_scratch(void **base) {
     return GIC_ERR_CUDA;
   }
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_base[dev]) {
+  const unsigned long long id = current_context_id();
+  NoallocSlot &slot = g_noalloc_slot[dev];
+  if (!slot.base || id == 0 || slot.ctx_id != id) {
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, gNoallocScratch);
     if (e != cudaSuccess || !p) {
       cudaGetLastError();
       return GIC_ERR_CUDA;
     }
-    g_noalloc_base[dev] = p;
+    slot.base = p;
+    slot.ctx_id = current_context_id();  // the lookup makes the device's context current
   }
-  *base = g_noalloc_base[dev];
+  *base = slot.base;
   return GIC_OK;
 }
 
@@ -983,6 +1022,8 @@ static int noalloc_run(unsigned long long seed, unsigned long long n, double *ou
   void *base = nullptr;
   int st = noalloc_scratch(&base);
   if (st != GIC_OK) return st;
+  // an error left by the caller's own earlier launches is not this call's
+  cudaGetLastError();
   Stream s{};
   s.seed = seed;
   s.raw_off = 0;
@@ -998,7 +1039,7 @@ static int noalloc_run(unsigned long long seed, unsigned long long n, double *ou
   int npow = 1;
   while ((1ull << npow) < s.nchunk) ++npow;
   NoallocLayout L = noalloc_layout(s.raw_count, s.nchunk, s.nseg, s.nblk, npow);
-  if (L.end > NoallocScratchBytes) return GIC_ERR_INVALID_ARG;
+  if (L.end > NoallocScratchBytes) return GIC_ERR_NOT_READY;
   unsigned char *b = static_cast<unsigned char *>(base);
   uint32_t *raw = reinterpret_cast<uint32_t *>(b + L.raw);
   U576 *pow2 = reinterpret_cast<U576 *>(b + L.pow2);
@@ -1043,12 +1084,16 @@ extern "C" GIC_API int gic_gaussian_stream_noalloc(unsigned long seed, size_t n,
   if (n == 0) return GIC_OK;
   if (!device_out || n > gic::kNoallocMaxGauss) return GIC_ERR_INVALID_ARG;
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
-  bool underrun = false;
-  int st = gic::noalloc_run(seed, n, device_out, cs, 1.0, &underrun);
-  if (st == GIC_OK && underrun) st = gic::noalloc_run(seed, n, device_out, cs, 1.5, &underrun);
-  if (st == GIC_OK && underrun) st = GIC_ERR_INTERNAL;
-  return st;
+  // The stream is drawn with a margin of raw numbers over the expected count;
+  // on the (rare) underrun the margin grows by 1.5, through the same margins
+  // as gic_gaussian_stream's (1, 1.5, 2.25, 3.375, 5.0625), for as long as the
+  // longer stream still fits the scratch array.
+  bool underrun = true;
+  int st = GIC_OK;
+  for (double margin = 1.0; underrun && margin < 6.0; margin *= 1.5) {
+    st = gic::noalloc_run(seed, n, device_out, cs, margin, &underrun);
+    if (st == GIC_ERR_NOT_READY) return GIC_ERR_INTERNAL;  // the longer stream does not fit
+    if (st != GIC_OK) return st;
+  }
+  return underrun ? GIC_ERR_INTERNAL : GIC_OK;
 }
-
-namespace gic {
-}  // namespace gic

@@ -25,10 +25,12 @@ def _ptr(a):
 class ICGenerator:
     """The realisation state of one set of initial conditions on one GPU."""
 
-    def __init__(self, precision='fp64', device=0):
+    def __init__(self, precision='fp64', device=0, mem_limit=0):
+        """mem_limit: bytes of device memory the context may hold (0: no limit); a call
+        that would allocate past it fails with GIC_ERR_OOM and the context stays usable."""
         lib = _lib.load()
         self._lib = lib
-        opts = _lib.GicDeviceOpts(_lib.GIC_FP64 if precision == 'fp64' else _lib.GIC_MIXED, device, 0)
+        opts = _lib.GicDeviceOpts(_lib.GIC_FP64 if precision == 'fp64' else _lib.GIC_MIXED, device, int(mem_limit))
         ctx = ctypes.c_void_p()
         st = lib.gic_create(ctypes.byref(ctx), ctypes.byref(opts))
         if st != _lib.GIC_OK:
@@ -81,6 +83,12 @@ class ICGenerator:
 
     def _call(self, name, *args):
         check(self._ctx, getattr(self._lib, name)(self._ctx, *args))
+
+    def memory_use(self):
+        """(bytes of device memory the context holds, its mem_limit)."""
+        used, limit = ctypes.c_size_t(), ctypes.c_size_t()
+        self._call('gic_memory_use', ctypes.byref(used), ctypes.byref(limit))
+        return used.value, limit.value
 
     # -- cosmology (main.cpp:31-37) ------------------------------------------------
     def Om(self, v):

@@ -68,7 +68,7 @@ typedef struct gic_ctx gic_ctx;
 typedef struct {
   int precision;     /* GIC_FP64 or GIC_MIXED */
   int device;        /* CUDA device ordinal */
-  size_t mem_limit;  /* 0 = no limit */
+  size_t mem_limit;  /* bytes of device memory the context may hold; 0 = no limit */
 } gic_device_opts;
 
 /* Cosmological parameters, as set by the paramfile commands Om, Ol, Ob, hubble,
@@ -329,14 +329,16 @@ GIC_API int gic_apply_modifications(gic_ctx *ctx, double *chi2_before, double *c
  * code that must stay inside another runtime's device-memory pool or budget).
  * Writes the first n unit gaussians of the stream of `seed` to the caller's
  * device buffer `device_out` (n doubles) on the caller's CUDA stream `stream`
- * (a cudaStream_t, NULL = legacy default stream), and returns when they are
- * there.  It allocates nothing: its scratch is one file-scope device array of
- * 24 MiB that every device loading the library holds until the process exits.
- * n may be at most GIC_NOALLOC_MAX_GAUSSIANS; larger n returns
- * GIC_ERR_INVALID_ARG without touching the GPU.  The first call on each device
- * looks up the array's device address (make it before any stream capture).
- * All calls share the array: calls that overlap on the GPU race and must be
- * serialised by the caller.  Errors are status codes only (no message). */
+ * (a cudaStream_t, NULL = legacy default stream).  The call reads a status
+ * flag back and synchronises `stream` before it returns.  It allocates
+ * nothing: its scratch is one file-scope device array of 24 MiB that every
+ * device loading the library holds until the process exits.  n may be at most
+ * GIC_NOALLOC_MAX_GAUSSIANS; larger n returns GIC_ERR_INVALID_ARG without
+ * touching the GPU.  The first call on each device (and in each new CUDA
+ * context of it) looks up the array's device address, so make that call before
+ * any stream capture.  All calls share the array: calls that overlap on the GPU
+ * race and must be serialised by the caller.  Errors are status codes only (no
+ * message). */
 #define GIC_NOALLOC_MAX_GAUSSIANS (1ull << 20)
 GIC_API int gic_gaussian_stream_noalloc(unsigned long seed, size_t n, double *device_out, void *stream);
 
@@ -360,6 +362,23 @@ GIC_API int gic_batch_get_stream(gic_batch *batch, void **stream);
 
 /* Number of kernels this library has launched in the process so far. */
 GIC_API int gic_launch_count(unsigned long long *count);
+
+/* The bounded waits of the FFT plane pass (a persistent kernel whose CTAs wait, one
+ * thread each, for tiles other CTAs of the launch write: the L2-resident fusion of a
+ * transform's y and z passes).  Each wait polls at most spin_limit times, 100 ns apart
+ * (0 = the default, 2^22: about 0.4 s), then gives up, flags it and carries on, so the
+ * kernel always ends; the call then returns GIC_ERR_TIMEOUT and the transform's
+ * results are invalid.  unreachable != 0 (tests only) sets every wait a target no
+ * task can reach, so each one gives up after spin_limit polls.  No counterpart in
+ * genetIC (its FFTW transforms have no waits). */
+GIC_API int gic_set_fft_wait(gic_ctx *ctx, unsigned spin_limit, int unreachable);
+
+/* Device memory the context holds now, in bytes, and its mem_limit (0 = none).
+ * Every device allocation a call makes for the context is checked against the limit
+ * first: one that would pass it fails the call with GIC_ERR_OOM (the message names
+ * the sizes) and allocates nothing; the context stays usable, and later calls that
+ * fit run normally.  genetIC has no counterpart: its fields live in host memory. */
+GIC_API int gic_memory_use(gic_ctx *ctx, size_t *in_use, size_t *limit);
 
 /* The context's CUDA stream (a cudaStream_t), for callers that order their own
  * work or timing events after the library's. */

@@ -500,6 +500,81 @@ def gadget_goldens():
                             mass=np.frombuffer(mass, '<f4'))
 
 
+# The headline's geometry at sizes the reference build finishes in seconds: zoom factor 4
+# (the compiled ratio-4 block means and interpolation), factor 3 with an integer number of
+# coarse cells under the zoom (the generic-ratio block means; a 72 Mpc/h, 48^3 base) and factor 3 over a fractional
+# number of them (genetIC's test_01c geometry: 32 fine cells over 10 2/3 coarse ones), with
+# the headline's four modifications in a 2 Mpc/h sphere and the variance modification of the
+# differentiation configuration (3 Mpc/h filter, 5 Mpc/h sphere, variance x 1.3).
+GEOMETRY = {
+    'zoom4': ('basegrid 50.0 32', 'centre 25 25 25\nselect_cube 10\nzoom_grid_with_origin_at 12 12 12 4 32', 2, ''),
+    'zoom3f': ('basegrid 50.0 32', 'centre 25 25 25\nselect_cube 10\nzoom_grid_with_origin_at 11 11 11 3 32', 2, ''),
+    'mod4': ('basegrid 50.0 32', 'centre 25 25 25\nselect_cube 10\nzoom_grid_with_origin_at 12 12 12 4 32', 2,
+             """centre 25 25 25
+select_sphere 2
+calculate overdensity
+calculate vx
+calculate vy
+calculate vz
+modify overdensity absolute 1.5
+modify vx absolute 0
+modify vy absolute 0
+modify vz absolute 0
+"""),
+    # dx = 1.5 and 0.5 Mpc/h, exact in binary: with thirds of a cell (50 Mpc/h over 48 cells)
+    # the reference build's own grid containment assertion fails
+    'mod3': ('basegrid 72.0 48', 'centre 36 36 36\nselect_cube 10\nzoom_grid_with_origin_at 16 16 16 3 48', 2,
+             """centre 36 36 36
+select_sphere 2
+calculate overdensity
+calculate vx
+calculate vy
+calculate vz
+modify overdensity absolute 1.5
+modify vx absolute 0
+modify vy absolute 0
+modify vz absolute 0
+"""),
+    'var4': ('basegrid 50.0 32', 'centre 25 25 25\nselect_cube 10\nzoom_grid_with_origin_at 12 12 12 4 32', 2,
+             """centre 25 25 25
+select_sphere 5
+filtering_scale 3
+calculate variance
+calculate overdensity
+modify overdensity relative 1
+modify variance relative 1.3
+"""),
+}
+
+
+def geometry_goldens():
+    """Reference-build grids (float64), logged calculated values, chi^2 change and quadratic
+    step counts of the GEOMETRY cases (random_seed 8896131)."""
+    import re
+    for name, (base, zoom, nlev, mods) in GEOMETRY.items():
+        with tempfile.TemporaryDirectory() as d:
+            write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+            body = MOD_BASE.replace('basegrid 50.0 32', base) + zoom + '\n' + mods + 'done\n' + ''.join(
+                'dump_grid %d\n' % l for l in range(nlev))
+            open(os.path.join(d, 'paramfile.txt'), 'w').write(body)
+            r = subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True, text=True)
+            log = r.stdout + r.stderr
+            vals = {}
+            for key in ('overdensity', 'vx', 'vy', 'vz', 'variance'):
+                m = re.search(r'%s: calculated value = (\S+)' % key, log)
+                if m:
+                    vals[key] = float(m.group(1))
+            m = re.search(r'Modification Delta chi\^2 = (\S+)', log)
+            if m:
+                vals['delta_chi2'] = float(m.group(1))
+            m = re.search(r'(\d+) steps are required for the quadratic algorithm', log)
+            if 'variance' in mods:
+                vals['steps'] = int(m.group(1)) if m else 10
+            grids = {'delta%d' % l: np.load(os.path.join(d, 'grid-%d.npy' % l)) for l in range(nlev)}
+            np.savez_compressed(os.path.join(HERE, 'geom_%s.npz' % name), **grids,
+                                **{k: np.array(v) for k, v in vals.items()})
+
+
 def main():
     for mode, cmd in (('serial', 'random_seed_serial'), ('parallel', 'random_seed'), ('real', 'random_seed_real_space')):
         with tempfile.TemporaryDirectory() as d:
@@ -516,7 +591,12 @@ def main():
 
 
 if __name__ == '__main__':
+    if len(sys.argv) > 1:  # named generators only, e.g. geometry_goldens
+        for fn in sys.argv[1:]:
+            globals()[fn]()
+        sys.exit(0)
     main()
+    geometry_goldens()
     zoom_goldens()
     mod_goldens()
     var_goldens()

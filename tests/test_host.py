@@ -140,3 +140,21 @@ def test_paramfile_parser(tmp_path):
     p.write_text('supersample 2\n')
     with pytest.raises(ValueError, match='not on the GPU realisation path'):
         generator.parse_paramfile(str(p))
+
+
+def test_c_program_compiles_and_links_against_the_library(built, tmp_path):
+    """tests/capi/realise32.c, a plain C caller, builds against include/gicgpu.h and links libgicgpu.so."""
+    from test_gpu_capi import build_c_program
+    assert os.path.exists(build_c_program(tmp_path))
+
+
+def test_genetic_side_hook_compiles_against_genetic_headers():
+    """include/gicgpu_genetic.hpp (DeviceRealisation, DeviceBackedParticleEvaluator) compiled
+    against genetIC's own headers by oracle/Makefile's `hook` target, where they are present."""
+    import subprocess
+    oracle = os.path.join(ROOT, 'oracle')
+    ref = subprocess.run(['make', '-s', '-C', oracle, 'print-ref'], capture_output=True, text=True).stdout.strip()
+    if not os.path.isdir(os.path.join(ref, 'src')):
+        pytest.skip('genetIC sources not present')
+    r = subprocess.run(['make', '-s', '-C', oracle, '-B', '_ref/hook_check.o'], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]

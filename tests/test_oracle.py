@@ -9,7 +9,8 @@ import pytest
 import field_oracle as fo
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_TESTS = '/root/reference/genetIC/tests'
+REF_TESTS = os.path.join(subprocess.run(['make', '-s', '-C', os.path.join(ROOT, 'oracle'), 'print-ref'],
+                                        capture_output=True, text=True).stdout.strip(), 'tests')
 REF_BIN = os.path.join(ROOT, 'oracle', '_ref', 'genetIC')
 GOLDEN = os.path.join(ROOT, 'tests', 'golden')
 
@@ -132,6 +133,14 @@ MOD_CASES = {
                  mods=[('overdensity', 0, 0.05), ('vx', 0, 0.0)]),
     'mod2': dict(levels=[(50.0, 32, (0.0, 0.0, 0.0)), (25.0, 32, (12.5, 12.5, 12.5))], radius=3,
                  mods=[('overdensity', 0, 0.05), ('vx', 0, 0.0), ('vy', 1, 0.0), ('vz', 2, 0.0)]),
+    # the headline's zoom factor 4 and its four modifications (mean overdensity +1.5 and the
+    # three mean velocities 0 in a 2 Mpc/h sphere at the zoom centre), at 32^3 + 32^3
+    'mod4': dict(levels=[(50.0, 32, (0.0, 0.0, 0.0)), (12.5, 32, (18.75, 18.75, 18.75))], radius=2,
+                 mods=[('overdensity', 0, 1.5), ('vx', 0, 0.0), ('vy', 1, 0.0), ('vz', 2, 0.0)]),
+    # zoom factor 3 (generic-ratio block means) on a 72 Mpc/h, 48^3 base
+    'mod3': dict(levels=[(72.0, 48, (0.0, 0.0, 0.0)), (24.0, 48, (24.0, 24.0, 24.0))], radius=2,
+                 centre=(36., 36., 36.),
+                 mods=[('overdensity', 0, 1.5), ('vx', 0, 0.0), ('vy', 1, 0.0), ('vz', 2, 0.0)]),
 }
 
 
@@ -145,7 +154,7 @@ def oracle_modified(bbks, case, cr_log=False):
     fo.set_cr_log(False)
     p_dm = fo.CambPower(bbks, COSMO, column=1)
     vs = fo.velocity_to_offset_ratio(COSMO)
-    flagged = fo.flag_cells(L, len(c['levels']) - 1, (25., 25., 25.), 'sphere', c['radius'])
+    flagged = fo.flag_cells(L, len(c['levels']) - 1, c.get('centre', (25., 25., 25.)), 'sphere', c['radius'])
     covs, targets, values = [], [], {}
     for name, d, t in c['mods']:
         loc = fo.localisation_covector(L, flagged, 'overdensity' if name == 'overdensity' else 'velocity', d)
@@ -232,6 +241,10 @@ VAR_CASES = {
     'var1': dict(levels=[(50.0, 32, (0.0, 0.0, 0.0))], select=('sphere', 8), scale=4.0, rel=3.0),
     'var2': dict(levels=[(50.0, 32, (0.0, 0.0, 0.0)), (25.0, 32, (12.5, 12.5, 12.5))], select=('sphere', 4),
                  scale=3.0, rel=1.5),
+    # the differentiation configuration's variance modification (3 Mpc/h filter, 5 Mpc/h sphere,
+    # variance x 1.3, overdensity held) on the factor-4 zoom, at 32^3 + 32^3
+    'var4': dict(levels=[(50.0, 32, (0.0, 0.0, 0.0)), (12.5, 32, (18.75, 18.75, 18.75))], select=('sphere', 5),
+                 scale=3.0, rel=1.3),
 }
 
 
@@ -438,3 +451,54 @@ def test_splice_oracle_matches_goldens(bbks, case):
     for l in range(len(levels)):
         ref = g['delta%d' % l]
         assert np.abs(fields[l][0] - ref).max() <= 1e-12 * np.abs(ref).max(), l
+
+
+# --- the headline's geometry: zoom factors 4 and 3 (tests/golden/geom_*.npz) ---------------
+
+GEOM_LEVELS = {
+    'zoom4': [(50.0, 32, (0.0, 0.0, 0.0)), (12.5, 32, (18.75, 18.75, 18.75))],
+    # factor 3 over 10 2/3 coarse cells (genetIC's test_01c geometry at 32^3)
+    'zoom3f': [(50.0, 32, (0.0, 0.0, 0.0)), (50.0 / 3, 32, (17.1875, 17.1875, 17.1875))],
+}
+
+
+@pytest.mark.parametrize('name', ['zoom4', 'zoom3f'])
+def test_geometry_oracle_matches_reference_grids(bbks, name):
+    from conftest import COSMO
+    g = _load_golden('geom_%s.npz' % name)
+    levels = GEOM_LEVELS[name]
+    fo.set_cr_log(False)
+    w = fo.white_noise_levels([l[1] for l in levels], 8896131, 2)
+    out = fo.zoom_realisation(w, levels, fo.CambPower(bbks, COSMO))
+    for l in range(len(levels)):
+        ref = g['delta%d' % l]
+        assert np.abs(out[l][0] - ref).max() <= 1e-12 * np.abs(ref).max(), l
+
+
+@pytest.mark.parametrize('case', ['mod4', 'mod3'])
+def test_geometry_modification_oracle_matches_reference(bbks, case):
+    from conftest import COSMO
+    g = _load_golden('geom_%s.npz' % case)
+    r = oracle_modified(bbks, case)
+    for name in ('overdensity', 'vx', 'vy', 'vz'):
+        assert '%.6g' % r['values'][name] == '%.6g' % float(g[name]), name
+    assert '%.6g' % (r['chi2'][1] - r['chi2'][0]) == '%.6g' % float(g['delta_chi2'])
+    levels = MOD_CASES[case]['levels']
+    out = fo.zoom_realisation(r['modified'], levels, fo.CambPower(bbks, COSMO))
+    for l in range(len(levels)):
+        ref = g['delta%d' % l]
+        assert np.abs(out[l][0] - ref).max() <= 1e-11 * np.abs(ref).max(), l
+
+
+def test_geometry_variance_oracle_matches_reference(bbks):
+    from conftest import COSMO
+    g = _load_golden('geom_var4.npz')
+    r = oracle_variance(bbks, 'var4')
+    assert '%.6g' % r['variance'] == '%.6g' % float(g['variance'])
+    assert '%.6g' % r['overdensity'] == '%.6g' % float(g['overdensity'])
+    assert r['steps'] == int(g['steps'])
+    assert '%.6g' % (r['chi2'][1] - r['chi2'][0]) == '%.6g' % float(g['delta_chi2'])
+    out = fo.zoom_realisation(r['modified'], VAR_CASES['var4']['levels'], fo.CambPower(bbks, COSMO))
+    for l in range(2):
+        ref = g['delta%d' % l]
+        assert np.abs(out[l][0] - ref).max() <= 1e-11 * np.abs(ref).max(), l
