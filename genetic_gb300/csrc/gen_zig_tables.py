@@ -12,6 +12,7 @@ in which the published tables are distributed.
 Run:  python genetic_gb300/csrc/gen_zig_tables.py > genetic_gb300/csrc/zig_tables.h
 """
 import mpmath as mp
+import numpy as np
 
 mp.mp.dps = 50
 
@@ -31,6 +32,11 @@ def g12(t):
     return float('%.12g' % float(mp.nstr(t, 20)))
 
 
+def f32(v):
+    """The double v rounded to the nearest float (ties to even), as a C float literal."""
+    return float.hex(float(np.float32(v))) + 'f'
+
+
 if __name__ == '__main__':
     R = mp.findroot(lambda r: layers(r)[1][0] - 1, mp.mpf('3.4442864767'))
     xs, ys = layers(R)
@@ -42,5 +48,8 @@ if __name__ == '__main__':
            '#define GIC_ZIG_PARAM_R %r' % g12(R),
            '#define GIC_ZIG_Y_INIT {' + ', '.join(float.hex(g12(t)) for t in y) + '}',
            '#define GIC_ZIG_W_INIT {' + ', '.join(float.hex(g12(t)) for t in w) + '}',
-           '#define GIC_ZIG_K_INIT {' + ', '.join('%du' % v for v in k) + '}']
+           '#define GIC_ZIG_K_INIT {' + ', '.join('%du' % v for v in k) + '}',
+           # the same values rounded to float, for the single-precision slow-path decisions
+           '#define GIC_ZIG_YF_INIT {' + ', '.join(f32(g12(t)) for t in y) + '}',
+           '#define GIC_ZIG_WF_INIT {' + ', '.join(f32(g12(t)) for t in w) + '}']
     print('\n'.join(out))

@@ -759,80 +759,78 @@ __global__ void k_subsample_add(const T *fine, int nf, int r, int sx, int sy, in
 // the fine half spectrum, completed by Hermitian symmetry; on the kz = 0 and N/2 planes
 // the conjugate halves are taken from their partners, as the inverse transform's mirror
 // does.  out: the (N/r)^3 half spectrum G.  btab: b(k), k < N.
-// R > 0: the ratio r known at compile time; each (kx, ky) column's R coefficients are
-// loaded together before their sums (which run in the same order)
-template <typename T, int R>
-__global__ void k_fold_block_means(typename V2m<T>::type *out, const typename V2m<T>::type *in, int N, int r_rt,
-                                   const T *tab, const typename V2m<T>::type *btab, T fac) {
+// The r^2 (m_x, m_y) alias pairs of an output coefficient are spread over the warps of
+// a CTA: a CTA owns 32 consecutive output coefficients (one per lane),
+// warp w sums the pairs w, w + NW, ... over m_z, and the NW partial sums are added in
+// shared memory: r^2 times the loads in flight of one thread per output coefficient, for
+// a pass bound by its loads' latency.  R > 0: r known at compile time.
+template <typename T, int R, int NW>
+__global__ void __launch_bounds__(32 * NW) k_fold_block_means(typename V2m<T>::type *out,
+                                                                    const typename V2m<T>::type *in, int N,
+                                                                    int r_rt, const T *tab,
+                                                                    const typename V2m<T>::type *btab, T fac) {
   using C = typename V2m<T>::type;
+  __shared__ C part[NW][32];
   const int r = R > 0 ? R : r_rt;
   const int nc = N / r, Sc = nc / 2 + 1, H = N / 2, S = H + 1;
-  const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (id >= (size_t)nc * nc * Sc) return;
-  const int KZ = (int)(id % Sc);
-  const size_t rr = id / Sc;
-  const int KY = (int)(rr % nc), KX = (int)(rr / nc);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const size_t id = (size_t)blockIdx.x * 32 + lane;
+  const bool valid = id < (size_t)nc * nc * Sc;
   T ar = 0, ai = 0;
-  for (int mx = 0; mx < r; ++mx) {
-    const int kx = KX + mx * nc;
-    const C bx = btab[kx];
-    for (int my = 0; my < r; ++my) {
-      const int ky = KY + my * nc;
-      const C by = btab[ky];
-      // bxy = bx by
+  if (valid) {
+    const int KZ = (int)(id % Sc);
+    const size_t rr = id / Sc;
+    const int KY = (int)(rr % nc), KX = (int)(rr / nc);
+    for (int pr = w; pr < r * r; pr += NW) {
+      const int mx = pr / r, my = pr - mx * r;
+      const int kx = KX + mx * nc, ky = KY + my * nc;
+      const C bx = btab[kx], by = btab[ky];
       const T bxy_r = bx.x * by.x - bx.y * by.y, bxy_i = bx.x * by.y + bx.y * by.x;
-      if constexpr (R > 0) {
-        C f[R];
-        T t[R];
+      const long long sxk = kx > H ? kx - N : kx, syk = ky > H ? ky - N : ky;
+      const long long qxy = sxk * sxk + syk * syk;
+      constexpr int RU = R > 0 ? R : 1;
 #pragma unroll
-        for (int mz = 0; mz < R; ++mz) {
-          const int kz = KZ + mz * nc;
+      for (int mz0 = 0; mz0 < (R > 0 ? R : r); mz0 += RU) {
+        C f[RU];
+        T t[RU];
+#pragma unroll
+        for (int u = 0; u < RU; ++u) {
+          const int kz = KZ + (mz0 + u) * nc;
           // the stored coefficient, or the conjugate of its Hermitian partner
           const bool mir = kz > H || ((kz == 0 || kz == H) && (kx > H || ((kx == 0 || kx == H) && ky > H)));
           const int qx = mir ? (N - kx) % N : kx, qy = mir ? (N - ky) % N : ky, qz = kz > H ? N - kz : kz;
-          f[mz] = in[((size_t)qx * N + qy) * S + qz];
-          if (mir) f[mz].y = -f[mz].y;
-          const long long sxk = kx > H ? kx - N : kx, syk = ky > H ? ky - N : ky;
-          t[mz] = tab[sxk * sxk + syk * syk + (long long)qz * qz];
+          f[u] = in[((size_t)qx * N + qy) * S + qz];
+          if (mir) f[u].y = -f[u].y;
+          t[u] = tab[qxy + (long long)qz * qz];
         }
 #pragma unroll
-        for (int mz = 0; mz < R; ++mz) {
-          const C bz = btab[KZ + mz * nc];
+        for (int u = 0; u < RU; ++u) {
+          const C bz = btab[KZ + (mz0 + u) * nc];
           const T b_r = bxy_r * bz.x - bxy_i * bz.y, b_i = bxy_r * bz.y + bxy_i * bz.x;
-          const T fr = f[mz].x * t[mz], fi = f[mz].y * t[mz];
+          const T fr = f[u].x * t[u], fi = f[u].y * t[u];
           ar += fr * b_r - fi * b_i;
           ai += fr * b_i + fi * b_r;
         }
-      } else {
-      for (int mz = 0; mz < r; ++mz) {
-        const int kz = KZ + mz * nc;
-        C f;
-        if (kz > H) {
-          const C g = in[((size_t)((N - kx) % N) * N + (N - ky) % N) * S + (N - kz)];
-          f.x = g.x;
-          f.y = -g.y;
-        } else if ((kz == 0 || kz == H) && (kx > H || ((kx == 0 || kx == H) && ky > H))) {
-          const C g = in[((size_t)((N - kx) % N) * N + (N - ky) % N) * S + kz];
-          f.x = g.x;
-          f.y = -g.y;
-        } else {
-          f = in[((size_t)kx * N + ky) * S + kz];
-        }
-        const long long sxk = kx > H ? kx - N : kx, syk = ky > H ? ky - N : ky, szk = kz > H ? N - kz : kz;
-        const T t = tab[sxk * sxk + syk * syk + szk * szk];
-        const C bz = btab[kz];
-        const T b_r = bxy_r * bz.x - bxy_i * bz.y, b_i = bxy_r * bz.y + bxy_i * bz.x;
-        const T fr = f.x * t, fi = f.y * t;
-        ar += fr * b_r - fi * b_i;
-        ai += fr * b_i + fi * b_r;
-      }
       }
     }
   }
-  C o;
-  o.x = ar * fac;
-  o.y = ai * fac;
-  out[id] = o;
+  C v;
+  v.x = ar;
+  v.y = ai;
+  part[w][lane] = v;
+  __syncthreads();
+  if (w == 0 && valid) {
+    T sr = 0, si = 0;
+#pragma unroll
+    for (int k = 0; k < NW; ++k) {
+      sr += part[k][lane].x;
+      si += part[k][lane].y;
+    }
+    C o;
+    o.x = sr * fac;
+    o.y = si * fac;
+    out[id] = o;
+  }
 }
 
 // coarse[(s + X) mod nc] += means[X] for X in [0, m)^3 (means: padded real layout of m^3)
@@ -1382,10 +1380,12 @@ struct ModEngine {
     const T fac = (T)std::pow((double)r, -1.5);
     const C *src = reinterpret_cast<const C *>(source_k);
     const C *bt = S.btab.template as<C>();
-    if (r == 2) k_fold_block_means<T, 2><<<nblk(ncomplex), 256, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac);
-    else if (r == 4) k_fold_block_means<T, 4><<<nblk(ncomplex), 256, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac);
-    else if (r == 8) k_fold_block_means<T, 8><<<nblk(ncomplex), 256, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac);
-    else k_fold_block_means<T, 0><<<nblk(ncomplex), 256, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac);
+    // 32 coefficients per CTA, the r^2 alias pairs over its warps
+    const unsigned ctas = nblk(ncomplex, 32);
+    if (r == 2) k_fold_block_means<T, 2, 4><<<ctas, 128, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac);
+    else if (r == 4) k_fold_block_means<T, 4, 16><<<ctas, 512, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac);
+    else if (r == 8) k_fold_block_means<T, 8, 16><<<ctas, 512, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac);
+    else k_fold_block_means<T, 0, 8><<<ctas, 256, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac);
     launched();
     fft_c2r_3d<T>(ctx, reinterpret_cast<T *>(g), nc, std::pow((double)nc, -1.5));
     const int sx = (int)std::lround((F.x0[0] - Cl.x0[0]) / Cl.dx), sy = (int)std::lround((F.x0[1] - Cl.x0[1]) / Cl.dx),

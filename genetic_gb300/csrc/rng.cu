@@ -36,22 +36,23 @@ constexpr int kSpecThreads = 128;  // segments per CTA of the speculative walk
 constexpr int kBlockSegs = 64;     // segments per block of the two-level chain
 constexpr uint32_t kUnderrun = 0xFFFFFFFFu;
 
-// Ziggurat tables: doubles for the values, floats for the slow-path decision,
-// copied into shared memory by the kernels that walk the stream.
+// Ziggurat tables: doubles for the values, floats (the doubles rounded to nearest)
+// for the slow-path decision.  Kernels that walk many segments copy them into shared
+// memory; the occasional walk of step_segment reads them here.
 struct ZigTab {
   unsigned int K[128];
   float Wf[128], Yf[129];
   double W[128], Y[129];
 };
-__device__ const ZigTab gZig = {GIC_ZIG_K_INIT, {}, {}, GIC_ZIG_W_INIT, GIC_ZIG_Y_INIT};
+__device__ const ZigTab gZig = {GIC_ZIG_K_INIT, GIC_ZIG_WF_INIT, GIC_ZIG_YF_INIT, GIC_ZIG_W_INIT, GIC_ZIG_Y_INIT};
 
 __device__ __forceinline__ void load_zig(ZigTab &t) {
   for (int i = threadIdx.x; i < 128; i += blockDim.x) {
     t.K[i] = gZig.K[i];
     t.W[i] = gZig.W[i];
     t.Y[i] = gZig.Y[i];
-    t.Wf[i] = (float)gZig.W[i];
-    t.Yf[i] = (float)gZig.Y[i];
+    t.Wf[i] = gZig.Wf[i];
+    t.Yf[i] = gZig.Yf[i];
   }
   if (threadIdx.x == 0) {
     t.Y[128] = 0.0;
@@ -165,9 +166,17 @@ __global__ void __launch_bounds__(128) k_generate(const Stream *st, int nstreams
     for (int k = 0; k < 22; ++k) y[k] = y[k + 2];
     y[22] = t0;
     y[23] = t1;
+    if (base + 24 <= count) {
+      // a block of 24 numbers starts 96 bytes into its stream (raw_off and base are
+      // multiples of 24), so it is six aligned 16-byte stores
+      uint4 *v = reinterpret_cast<uint4 *>(dst + base);
 #pragma unroll
-    for (int k = 0; k < 24; ++k)
-      if (base + k < count) dst[base + k] = y[k];
+      for (int k = 0; k < 6; ++k) v[k] = make_uint4(y[4 * k], y[4 * k + 1], y[4 * k + 2], y[4 * k + 3]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 24; ++k)
+        if (base + k < count) dst[base + k] = y[k];
+    }
   }
 }
 
@@ -588,18 +597,21 @@ __host__ __device__ __forceinline__ unsigned long long shell_offset(long long ks
   return ks <= 1 ? 0ull : (unsigned long long)(2 * (ks - 1) * ks * (2 * ks - 1));
 }
 
+// Draw index Q -> mode.  shell_offset(ks) ~ 4 ks^3, so ks starts from the cube root of
+// Q / 4 and is corrected exactly by at most a step or two; the rest fits 32 bits
+// (Q < 2^31: draw_noise_all checks the grid size).
 __device__ __forceinline__ void decode_mode(unsigned long long Q, int half, int &k1, int &k2, int &k3) {
-  int lo = 1, hi = half - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (shell_offset(mid) <= Q) lo = mid; else hi = mid - 1;
-  }
-  int ks = lo;
-  unsigned long long q = Q - shell_offset(ks);
-  int which = (int)(q % 3ull);
-  unsigned long long t = q / 3ull;
-  int a = (int)(t / (unsigned long long)(2 * ks)) - ks;
-  int b = (int)(t % (unsigned long long)(2 * ks)) - ks;
+  int ks = (int)cbrtf((float)Q * 0.25f);
+  ks = max(1, min(ks, half - 1));
+  while (ks < half - 1 && shell_offset(ks + 1) <= Q) ++ks;
+  while (ks > 1 && shell_offset(ks) > Q) --ks;
+  const unsigned q = (unsigned)(Q - shell_offset(ks));
+  const unsigned t = q / 3u;
+  const int which = (int)(q - 3u * t);
+  const unsigned side = 2u * (unsigned)ks;
+  const unsigned ta = t / side;
+  const int a = (int)ta - ks;
+  const int b = (int)(t - ta * side) - ks;
   if (which == 0) { k1 = ks; k2 = a; k3 = b; }
   else if (which == 1) { k1 = a; k2 = ks; k3 = b; }
   else { k1 = a; k2 = b; k3 = ks; }

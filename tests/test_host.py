@@ -43,9 +43,17 @@ def test_create_without_gpu_fails_cleanly(built):
 def test_ziggurat_tables_agree_with_oracle():
     a = open(os.path.join(ROOT, 'oracle', 'rng', 'zig_tables.h')).read()
     b = open(os.path.join(CSRC, 'zig_tables.h')).read()
-    hx = lambda s: re.findall(r'0x[0-9a-f.]+p[+-]\d+', s)
-    assert hx(a) == hx(b) and len(hx(a)) == 256
+    hx = lambda s: re.findall(r'0x[0-9a-f.]+p[+-]\d+(?!f)\b', s)
+    line = lambda s, name: re.search(r'#define %s \{([^}]*)\}' % name, s).group(1)
+    oracle_doubles = hx(a)
+    doubles = hx(line(b, 'GIC_ZIG_Y_INIT')) + hx(line(b, 'GIC_ZIG_W_INIT'))
+    assert oracle_doubles == doubles and len(doubles) == 256
     assert re.findall(r'(\d+)u', a) == re.findall(r'(\d+)u', b)
+    # the device's single-precision decision tables are those doubles rounded to nearest
+    for dname, fname in (('GIC_ZIG_Y_INIT', 'GIC_ZIG_YF_INIT'), ('GIC_ZIG_W_INIT', 'GIC_ZIG_WF_INIT')):
+        d = [float.fromhex(v) for v in hx(line(b, dname))]
+        f = [float.fromhex(v[:-1]) for v in re.findall(r'0x[0-9a-f.]+p[+-]\d+f', line(b, fname))]
+        assert len(f) == len(d) and all(float(np.float32(x)) == y for x, y in zip(d, f))
 
 
 HOST_TEST = r'''
