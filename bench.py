@@ -7,7 +7,8 @@ workload has zoom levels, and particle positions/velocities -- with the transfer
 table already on the device
 (`value`), or end to end through the C ABI from host memory (`e2e`: the
 transfer table uploaded and the sigma8 normalisation recomputed every step,
-particles copied back to pinned host memory every step).
+particles copied back to pinned host memory every step: positions as doubles, velocities
+in the context's precision).
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
 Under torchrun each rank runs an independent replica on its own GPU
@@ -523,12 +524,15 @@ def main():
     t = max_over_ranks(start.elapsed_time(end) * 1e-3 / args.steps, world)
     value = npart * world / t / 1e6
 
-    # end to end through the C ABI, host buffers (pinned), copies inside the timed region
+    # end to end through the C ABI, host buffers (pinned), copies inside the timed region:
+    # positions as doubles, velocities in the precision the context computes them
+    # (gic_fetch_particles_native: float32 in the mixed form)
+    vel_dtype = torch.float64 if wl['precision'] == 'fp64' else torch.float32
     pinned = []
     for lev in range(len(wl['levels'])):
         n = gen.levels[lev][1]
         pos = torch.empty((n ** 3, 3), dtype=torch.float64, pin_memory=True).numpy()
-        vel = torch.empty((n ** 3, 3), dtype=torch.float64, pin_memory=True).numpy()
+        vel = torch.empty((n ** 3, 3), dtype=vel_dtype, pin_memory=True).numpy()
         pinned.append((pos, vel))
     table_pinned = torch.empty(table.shape, dtype=torch.float64, pin_memory=True).numpy()
     table_pinned[...] = table
@@ -538,7 +542,7 @@ def main():
         gen._call('gic_set_transfer', _ptr(table_pinned), table.shape[0], table.shape[1])
         step(i)
         for lev, (pos, vel) in enumerate(pinned):
-            gen._call('gic_fetch_particles', lev, _ptr(pos), _ptr(vel))
+            gen._call('gic_fetch_particles_native', lev, _ptr(pos), ctypes.c_void_p(vel.ctypes.data))
 
     e2e_step(0)
     barrier(world)

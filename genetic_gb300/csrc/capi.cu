@@ -455,6 +455,19 @@ int gic_fetch_particles(gic_ctx *ctx, int level, double *pos, double *vel) {
   API_END
 }
 
+int gic_fetch_particles_native(gic_ctx *ctx, int level, double *pos, void *vel) {
+  API_BEGIN(ctx)
+  gic::Level &L = gic::level_at(C, level);
+  if (!L.pos.ptr) gic::fail(GIC_ERR_NOT_READY, "particles have not been generated");
+  size_t m = L.ncells();
+  if (pos) GIC_CUDA(cudaMemcpyAsync(pos, L.pos.ptr, 3 * m * sizeof(double), cudaMemcpyDeviceToHost, C.stream));
+  if (vel)
+    GIC_CUDA(cudaMemcpyAsync(vel, L.vel.ptr, 3 * m * (C.dbl() ? sizeof(double) : sizeof(float)),
+                             cudaMemcpyDeviceToHost, C.stream));
+  GIC_CUDA(cudaStreamSynchronize(C.stream));
+  API_END
+}
+
 int gic_fft(gic_ctx *ctx, int level, int what, int dir) {
   API_BEGIN(ctx)
   gic::Level &L = gic::level_at(C, level);

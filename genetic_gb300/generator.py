@@ -614,6 +614,15 @@ class ICGenerator:
         self._call('gic_fetch_particles', level, _ptr(pos), _ptr(vel))
         return pos, vel
 
+    def particles_native(self, level=0):
+        """Positions (doubles) and velocities in the context's precision (float32 in the
+        mixed form), as the device holds them."""
+        n = self.levels[level][1]
+        pos = np.empty((n ** 3, 3), dtype=np.float64)
+        vel = np.empty((n ** 3, 3), dtype=np.float64 if self.precision == 'fp64' else np.float32)
+        self._call('gic_fetch_particles_native', level, _ptr(pos), ctypes.c_void_p(vel.ctypes.data))
+        return pos, vel
+
     # -- particle files (io/tipsy.hpp, io/gadget.hpp) ------------------------------------
     def particle_map(self):
         """The gic_particle_map of this context: genetIC's particle-mapper order over the zoom

@@ -146,6 +146,12 @@ GIC_API int gic_fetch_level(gic_ctx *ctx, int level, int what, double *host_dst)
  * (km/s a^1/2), as ZeldovichParticleEvaluator::getParticle evaluates them
  * (zeldovich.hpp:87-124, genetIC/src/simulation/particles/generator.hpp:49-53). */
 GIC_API int gic_fetch_particles(gic_ctx *ctx, int level, double *pos, double *vel);
+/* The same particles with the velocities in the precision the context computes them:
+ * n^3 x 3 floats in GIC_MIXED, doubles in GIC_FP64 (positions are always doubles).
+ * For callers that keep float particle arrays (genetIC's single-precision build, whose
+ * ParticleEvaluator yields Particle<float>): the velocities cross the host link in half
+ * the bytes, with no rounding beyond the device's own. */
+GIC_API int gic_fetch_particles_native(gic_ctx *ctx, int level, double *pos, void *vel);
 
 /* ---- Tipsy particle records (io::tipsy::TipsyOutput, genetIC/src/io/tipsy.hpp) ----
  * One dark-matter record, TipsyParticle::dark (tipsy.hpp:61-63). */

@@ -67,3 +67,18 @@ def test_grid_fixture_from_reference(built, bbks):
     assert _rel(got['delta'], g['delta']) < 1e-10
     disp = (got['pos'] - g['pos'].astype(np.float64) + 25.0) % 50.0 - 25.0
     assert np.abs(disp).max() < 5e-6
+
+
+@pytest.mark.parametrize('precision', ['mixed', 'fp64'])
+def test_native_fetch_matches_double_fetch(built, bbks, precision):
+    """gic_fetch_particles_native: the same positions, and velocities in the context's own
+    precision (float32 in the mixed form) that widen exactly to gic_fetch_particles' doubles."""
+    from conftest import make_generator
+    gen = make_generator(precision, bbks, [('base', 50.0, 32)], 8896131, 'random_seed')
+    gen.done()
+    pos, vel = gen.particles(0)
+    pos_n, vel_n = gen.particles_native(0)
+    gen.close()
+    assert vel_n.dtype == (np.float32 if precision == 'mixed' else np.float64)
+    assert np.array_equal(pos, pos_n)
+    assert np.array_equal(vel, vel_n.astype(np.float64))
