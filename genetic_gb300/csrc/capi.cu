@@ -468,6 +468,19 @@ int gic_fetch_particles_native(gic_ctx *ctx, int level, double *pos, void *vel) 
   API_END
 }
 
+int gic_fetch_particles_resampled(gic_ctx *ctx, int level, int factor, double *pos, double *vel) {
+  API_BEGIN(ctx)
+  gic::Level &L = gic::level_at(C, level);
+  if (!pos || !vel) gic::fail(GIC_ERR_INVALID_ARG, "null buffer");
+  if (factor > -2 && factor < 2) gic::fail(GIC_ERR_INVALID_ARG, "factor must be >= 2 (supersample) or <= -2 (subsample)");
+  const int s = factor > 0 ? factor : -factor;
+  const long long nv = factor > 0 ? (long long)L.n * s : L.n / s;
+  if (factor < 0 && L.n % s) gic::fail(GIC_ERR_INVALID_ARG, "subsampling factor must divide the level's cells per side");
+  if (nv < 2 || nv % 2 || nv > 2048) gic::fail(GIC_ERR_INVALID_ARG, "resampled grid needs an even number of cells per side <= 2048");
+  gic::resampled_particles(C, L, factor, pos, vel);
+  API_END
+}
+
 int gic_fft(gic_ctx *ctx, int level, int what, int dir) {
   API_BEGIN(ctx)
   gic::Level &L = gic::level_at(C, level);

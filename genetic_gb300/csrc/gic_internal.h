@@ -408,6 +408,8 @@ void noise_real(Context &ctx, int level, void *out);
 // particles.cu
 double velocity_to_offset_ratio(const Cosmo &c);
 void make_particles(Context &ctx, Level &L, int order = 1);
+// particles of a virtual grid over L's region: factor > 1 supersampled, < -1 subsampled
+void resampled_particles(Context &ctx, const Level &L, int factor, double *host_pos, double *host_vel);
 
 }  // namespace gic
 

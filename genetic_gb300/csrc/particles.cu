@@ -116,6 +116,31 @@ __global__ void __launch_bounds__(256) k_particles(const T *__restrict__ px, con
   }
 }
 
+// The mean of each s^3 block of a level's real field (SubSampleEvaluator,
+// genetIC/src/simulation/field/evaluator.hpp:180-207 with SubSampleGrid::forEachSubcell,
+// genetIC/src/simulation/grid/virtualgrid.hpp:576-605: the sum over x, then y, then z,
+// divided by the count) into an (n/s)^3 field; both in the padded real layout.
+template <typename T>
+__global__ void k_block_average(const T *__restrict__ src, int n, int s, T *__restrict__ dst, int nv) {
+  const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= (size_t)nv * nv * nv) return;
+  const int z = (int)(id % nv);
+  const size_t r = id / nv;
+  const int y = (int)(r % nv), x = (int)(r / nv);
+  const size_t srow = 2 * (size_t)(n / 2 + 1);
+  T acc = 0;
+  for (int i = 0; i < s; ++i)
+    for (int j = 0; j < s; ++j)
+      for (int k = 0; k < s; ++k) acc += src[((size_t)(x * s + i) * n + (y * s + j)) * srow + (size_t)(z * s + k)];
+  dst[((size_t)x * nv + y) * (2 * (size_t)(nv / 2 + 1)) + z] = acc / (T)(s * s * s);
+}
+
+template <typename T>
+__global__ void k_widen(const T *src, double *dst, size_t count) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) dst[i] = to_double(src[i]);
+}
+
 }  // namespace
 
 double velocity_to_offset_ratio(const Cosmo &c) {
@@ -142,6 +167,68 @@ static void particles_typed(Context &ctx, Level &L, int order) {
                                                         nullptr, nullptr, nullptr, L.n, cen, L.periodic, ratio,
                                                         L.pos.as<double>(), L.vel.as<T>());
   launched(2);
+}
+
+// Particles of a virtual grid over level L's region (genetIC's supersample / subsample):
+// factor > 1, (n factor)^3 cells whose displacements are the level's interpolated at
+// their centroids (SuperSampleEvaluator, evaluator.hpp:96-130: the tricubic of
+// field.hpp:483-509, wrapped on the periodic base level, clamped on a zoom level);
+// factor < -1, (n / |factor|)^3 cells averaging |factor|^3 cells each.  Positions
+// (centroid + displacement, wrapped) and velocities go to host_pos / host_vel (doubles).
+template <typename T>
+static void resampled_typed(Context &ctx, const Level &L, int factor, double *host_pos, double *host_vel) {
+  const bool super = factor > 1;
+  const int s = super ? factor : -factor;
+  Level V;
+  V.n = super ? L.n * s : L.n / s;
+  V.box = L.box;
+  V.dx = L.box / V.n;
+  for (int a = 0; a < 3; ++a) V.x0[a] = L.x0[a];
+  V.periodic = L.periodic;
+  const size_t real = (size_t)V.n * V.n * 2 * (size_t)(V.n / 2 + 1), m = V.ncells();
+  std::unique_ptr<DevBuf> f[3] = {ctx.pool.take(real * sizeof(T)), ctx.pool.take(real * sizeof(T)),
+                                  ctx.pool.take(real * sizeof(T))};
+  T *dst[3] = {f[0]->as<T>(), f[1]->as<T>(), f[2]->as<T>()};
+  if (super) {
+    const T *src[3] = {L.field[1].as<T>(), L.field[2].as<T>(), L.field[3].as<T>()};
+    interp_add<T, 3>(ctx, L, src, V, dst, true);
+  } else {
+    for (int a = 0; a < 3; ++a)
+      k_block_average<T><<<(unsigned)((m + 255) / 256), 256, 0, ctx.stream>>>(L.field[1 + a].as<T>(), L.n, s, dst[a],
+                                                                             V.n);
+    launched(3);
+  }
+  auto pos = ctx.pool.take(3 * m * sizeof(double));
+  auto vel = ctx.pool.take(3 * m * sizeof(T));
+  auto cen = ctx.pool.take(3 * (size_t)V.n * sizeof(double));
+  k_centroids<<<(3 * V.n + 127) / 128, 128, 0, ctx.stream>>>(V.n, V.dx, V.x0[0], V.x0[1], V.x0[2], cen->as<double>());
+  k_particles<T, false><<<(unsigned)((size_t)V.n * V.n), 256, 0, ctx.stream>>>(
+      dst[0], dst[1], dst[2], nullptr, nullptr, nullptr, V.n, cen->as<double>(), V.periodic,
+      (T)velocity_to_offset_ratio(ctx.cosmo), pos->as<double>(), vel->as<T>());
+  launched(2);
+  GIC_CUDA(cudaMemcpyAsync(host_pos, pos->ptr, 3 * m * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+  if (sizeof(T) == sizeof(double)) {
+    GIC_CUDA(cudaMemcpyAsync(host_vel, vel->ptr, 3 * m * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+  } else {
+    // widen in the positions' buffer, once they are on the host
+    GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+    k_widen<T><<<(unsigned)((3 * m + 255) / 256), 256, 0, ctx.stream>>>(vel->as<T>(), pos->as<double>(), 3 * m);
+    launched();
+    GIC_CUDA(cudaMemcpyAsync(host_vel, pos->ptr, 3 * m * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+  }
+  GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+  for (auto &b : f) ctx.pool.give(std::move(b));
+  ctx.pool.give(std::move(pos));
+  ctx.pool.give(std::move(vel));
+  ctx.pool.give(std::move(cen));
+}
+
+void resampled_particles(Context &ctx, const Level &L, int factor, double *host_pos, double *host_vel) {
+  if (!L.have_fields) fail(GIC_ERR_NOT_READY, "displacement fields not computed");
+  if (ctx.dbl())
+    resampled_typed<double>(ctx, L, factor, host_pos, host_vel);
+  else
+    resampled_typed<float>(ctx, L, factor, host_pos, host_vel);
 }
 
 void make_particles(Context &ctx, Level &L, int order) {

@@ -363,5 +363,7 @@ template void interp_add_fields<float>(Context &, const Level &, float *const[4]
 template void interp_add_fields<double>(Context &, const Level &, double *const[4], Level &, unsigned);
 template void interp_add<float, 1>(Context &, const Level &, const float *const *, const Level &, float *const *, bool);
 template void interp_add<double, 1>(Context &, const Level &, const double *const *, const Level &, double *const *, bool);
+template void interp_add<float, 3>(Context &, const Level &, const float *const *, const Level &, float *const *, bool);
+template void interp_add<double, 3>(Context &, const Level &, const double *const *, const Level &, double *const *, bool);
 
 }  // namespace gic

@@ -623,6 +623,16 @@ class ICGenerator:
         self._call('gic_fetch_particles_native', level, _ptr(pos), ctypes.c_void_p(vel.ctypes.data))
         return pos, vel
 
+    def particles_resampled(self, level, factor):
+        """Particles of `level` on genetIC's supersampled (factor >= 2) or subsampled
+        (factor <= -2) virtual grid of the same region: (positions, velocities)."""
+        n = self.levels[level][1]
+        nv = n * factor if factor > 0 else n // -factor
+        pos = np.empty((nv ** 3, 3), dtype=np.float64)
+        vel = np.empty((nv ** 3, 3), dtype=np.float64)
+        self._call('gic_fetch_particles_resampled', level, int(factor), _ptr(pos), _ptr(vel))
+        return pos, vel
+
     # -- particle files (io/tipsy.hpp, io/gadget.hpp) ------------------------------------
     def particle_map(self):
         """The gic_particle_map of this context: genetIC's particle-mapper order over the zoom

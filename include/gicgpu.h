@@ -152,6 +152,17 @@ GIC_API int gic_fetch_particles(gic_ctx *ctx, int level, double *pos, double *ve
  * ParticleEvaluator yields Particle<float>): the velocities cross the host link in half
  * the bytes, with no rounding beyond the device's own. */
 GIC_API int gic_fetch_particles_native(gic_ctx *ctx, int level, double *pos, void *vel);
+/* Particles of a level evaluated on a virtual grid over its region, as genetIC's
+ * supersample / subsample commands produce them (SuperSampleEvaluator and
+ * SubSampleEvaluator, genetIC/src/simulation/field/evaluator.hpp:96-207, over the
+ * virtual grids of simulation/grid/virtualgrid.hpp:126-160, 528-605).  factor >= 2:
+ * (n factor)^3 particles whose displacements are the level's, tricubic-interpolated at
+ * the virtual cells' centroids (wrapped on the periodic base level, clamped on a zoom
+ * level); factor <= -2: (n / |factor|)^3 particles whose displacements average each
+ * block of |factor|^3 cells (|factor| must divide n).  pos, vel: (cells x 3) doubles in
+ * the virtual grid's cell order, positions = centroid + displacement wrapped into the
+ * box, velocities as gic_fetch_particles.  First-order (Zel'dovich) displacements. */
+GIC_API int gic_fetch_particles_resampled(gic_ctx *ctx, int level, int factor, double *pos, double *vel);
 
 /* ---- Tipsy particle records (io::tipsy::TipsyOutput, genetIC/src/io/tipsy.hpp) ----
  * One dark-matter record, TipsyParticle::dark (tipsy.hpp:61-63). */

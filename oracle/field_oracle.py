@@ -1075,16 +1075,19 @@ def mapper_order(n0, replaced=(), n1=0, ratio=1, origin=(0, 0, 0)):
     return mapper_order_levels([(n0, 1, (0, 0, 0)), (n1, ratio, origin)], [replaced])
 
 
-def tipsy_factors(levels, cosmo, order_levels):
+def tipsy_factors(levels, cosmo, order_levels, soft_scale=None):
     """Per-level particle mass and softening (zeldovich.hpp:55-62, 112-121, grid.hpp:112)
     and TipsyOutput's factors (tipsy.hpp:200-239): mass_factor = Om / (masses summed in
-    mapper order), pos_factor = 1 / box, vel_factor = a^-1/2 / dKmsUnit."""
+    mapper order), pos_factor = 1 / box, vel_factor = a^-1/2 / dKmsUnit.  soft_scale: per
+    level the grid's cellSofteningScale (1; a supersampled virtual grid's is its factor,
+    virtualgrid.hpp:139-146)."""
     L = levels[0][0]
     om, h = cosmo['omega_m'], cosmo['hubble']
     a = 1.0 / (1.0 + cosmo['redshift'])
     box_mass = 27.744948 * om * pow(L, 3.0)
     mass = [box_mass * pow((b / n) / L, 3.0) for b, n, _ in levels]
-    eps = [(b / n) * 1.0 * 0.01075 for b, n, _ in levels]
+    soft_scale = soft_scale or [1.0] * len(levels)
+    eps = [(b / n) * float(sc) * 0.01075 for (b, n, _), sc in zip(levels, soft_scale)]
     tot = 0.0
     for lv in order_levels:  # the reference's running double sum
         tot += mass[lv]
@@ -1095,6 +1098,20 @@ def tipsy_factors(levels, cosmo, order_levels):
     kms = np.sqrt(4.3022682e-6 * msol / kpc)
     vel_factor = pow(a, -0.5) / kms
     return mass, eps, pos_factor, vel_factor, mass_factor
+
+
+def resample_displacements(psi, box, n, offset, periodic, factor):
+    """A level's displacement fields on genetIC's supersampled (factor >= 2) or subsampled
+    (factor <= -2) virtual grid of the same region (SuperSampleEvaluator / SubSampleEvaluator,
+    evaluator.hpp:96-207; virtualgrid.hpp:126-160, 528-605): the tricubic of the level's
+    fields at the virtual centroids (wrapped on the periodic base level, clamped on a zoom
+    level), or the mean of each block of |factor|^3 cells.  Returns (fields, cells per side)."""
+    if factor > 1:
+        nv = n * factor
+        return [interpolate_to(p, box, offset, periodic, box, nv, offset) for p in psi], nv
+    s = -factor
+    nv = n // s
+    return [p.reshape(nv, s, nv, s, nv, s).sum(axis=(1, 3, 5)) / float(s ** 3) for p in psi], nv
 
 
 def tipsy_records(order, pos, vel, mass, eps, pos_factor, vel_factor, mass_factor):

@@ -575,6 +575,33 @@ def geometry_goldens():
                                 **{k: np.array(v) for k, v in vals.items()})
 
 
+# genetIC's supersample / subsample: particles of virtual grids (tipsy records).  A 16^3 base
+# supersampled x2, a 32^3 base subsampled x2, and the zoom2 geometry with its zoom level
+# supersampled x2 (the finest level is the one genetIC supersamples).
+RESAMPLE = {
+    'super1': ('basegrid 50.0 16', 'supersample 2', 3),
+    'sub1': ('basegrid 50.0 32', 'subsample 2', 1),
+    'superzoom': ('basegrid 50.0 32\ncentre 25 25 25\nselect_cube 10\nzoom_grid_with_origin_at 8 8 8 2 32', 'supersample 2',
+                  37),
+}
+
+
+def resample_goldens():
+    """Header bytes and dark records (every `stride`-th, plus the last 400) of the reference's
+    tipsy files with supersampling or subsampling."""
+    for name, (grids, cmd, stride) in RESAMPLE.items():
+        with tempfile.TemporaryDirectory() as d:
+            write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+            body = MOD_BASE.replace('basegrid 50.0 32', grids) + cmd + '\ndone\n'
+            open(os.path.join(d, 'paramfile.txt'), 'w').write(body)
+            subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True)
+            raw = open(os.path.join(d, 'out.tipsy'), 'rb').read()
+            _, _, dark = read_tipsy(os.path.join(d, 'out.tipsy'))
+            np.savez_compressed(os.path.join(HERE, 'resample_%s.npz' % name), header_bytes=np.frombuffer(raw[:28], np.uint8).copy(),
+                                nrec=np.int64(len(dark)), stride=np.int64(stride), every=dark[::stride].copy(),
+                                tail=dark[-400:].copy())
+
+
 def main():
     for mode, cmd in (('serial', 'random_seed_serial'), ('parallel', 'random_seed'), ('real', 'random_seed_real_space')):
         with tempfile.TemporaryDirectory() as d:
@@ -597,6 +624,7 @@ if __name__ == '__main__':
         sys.exit(0)
     main()
     geometry_goldens()
+    resample_goldens()
     zoom_goldens()
     mod_goldens()
     var_goldens()

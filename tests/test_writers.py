@@ -508,3 +508,58 @@ def test_gadget_num_files_matches_genetic(built, zoom2_particles, tmp_path):
         rec = writers.read_fortran_records(tmp_path / ('out.gadget2.%d' % i))
         assert len(rec) == int(g['nrec%d' % i]) and rec[0] == bytes(g['header%d' % i])
         assert np.array_equal(np.frombuffer(rec[3], np.uint64), g['ids%d' % i])
+
+
+# --- genetIC's supersample / subsample (tests/golden/resample_*.npz) -------------------------
+
+RESAMPLE = {
+    # name: (levels, resampled level, factor, replaced-cell selection)
+    'super1': ([(50.0, 16, (0.0, 0.0, 0.0))], 0, 2, None),
+    'sub1': ([(50.0, 32, (0.0, 0.0, 0.0))], 0, -2, None),
+    'superzoom': (ZOOM2, 1, 2, ('cube', 10)),
+}
+
+
+def resampled_oracle(bbks, name):
+    """The oracle's particles of RESAMPLE[name] with the resampled level on its virtual grid:
+    positions and velocities per level, the mapper order and the tipsy factors."""
+    from conftest import COSMO
+    levels, lev, factor, sel = RESAMPLE[name]
+    fo.set_cr_log(False)
+    w = fo.white_noise_levels([l[1] for l in levels], 8896131, 2)
+    fields = fo.zoom_realisation(w, levels, fo.CambPower(bbks, COSMO))
+    ratio = fo.velocity_to_offset_ratio(COSMO)
+    periodic = levels[0][0]
+    pos, vel, vlevels, soft = [], [], [], []
+    for l, (b, n, off) in enumerate(levels):
+        psi = fields[l][1:4]
+        nv, sc = n, 1.0
+        if l == lev:
+            psi, nv = fo.resample_displacements(psi, b, n, off, periodic, factor)
+            sc = float(factor) if factor > 1 else 1.0
+        p, v = fo.particles(psi, b, off, periodic, ratio)
+        pos.append(p)
+        vel.append(v)
+        vlevels.append((b, nv, off))
+        soft.append(sc)
+    if sel is None:
+        order = (np.zeros(vlevels[0][1] ** 3, dtype=int), np.arange(vlevels[0][1] ** 3))
+    else:
+        replaced = fo.flag_cells(fo.Levels(levels), 0, (25., 25., 25.), *sel)
+        n0, n1 = vlevels[0][1], vlevels[1][1]
+        order = fo.mapper_order(n0, replaced, n1, n1 // (n0 // 2), ORIGIN)
+    factors = fo.tipsy_factors(vlevels, COSMO, order[0], soft)
+    return dict(pos=pos, vel=vel, order=order, factors=factors)
+
+
+@pytest.mark.parametrize('name', sorted(RESAMPLE))
+def test_resampled_oracle_matches_reference_file(bbks, name):
+    g = np.load(os.path.join(GOLDEN, 'resample_%s.npz' % name))
+    r = resampled_oracle(bbks, name)
+    assert len(r['order'][1]) == int(g['nrec'])
+    got = fo.tipsy_records(r['order'], r['pos'], r['vel'], *r['factors'])
+    stride = int(g['stride'])
+    for mine, ref in ((got[::stride], g['every']), (got[-400:], g['tail'])):
+        assert np.array_equal(mine[:, 0], ref[:, 0]) and np.array_equal(mine[:, 7:], ref[:, 7:])
+        assert np.abs(mine[:, 1:4] - ref[:, 1:4]).max() <= 6e-8
+        assert np.abs(mine[:, 4:7] - ref[:, 4:7]).max() <= 2e-7 * np.abs(ref[:, 4:7]).max()
