@@ -109,6 +109,7 @@ SIGNATURES = {
     'gic_gaussian_stream_noalloc': [ctypes.c_ulong, ctypes.c_size_t, _P, _P],
     'gic_fetch_particles_native': [_P, _I, _D, _P],
     'gic_fetch_particles_resampled': [_P, _I, _I, _D, _D],
+    'gic_fetch_particles_matched': [_P, _I, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_size_t, _D, _D],
     'gic_memory_use': [_P, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)],
     'gic_set_fft_wait': [_P, ctypes.c_uint, _I],
     'gic_set_noise': [_P, _I, _D],

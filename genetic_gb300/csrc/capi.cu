@@ -481,6 +481,16 @@ int gic_fetch_particles_resampled(gic_ctx *ctx, int level, int factor, double *p
   API_END
 }
 
+int gic_fetch_particles_matched(gic_ctx *ctx, int level, const unsigned long long *cells, size_t n, double *pos,
+                                double *vel) {
+  API_BEGIN(ctx)
+  gic::level_at(C, level);
+  if (level < 1) gic::fail(GIC_ERR_INVALID_ARG, "a resolution-matching grid belongs to a zoom level (level >= 1)");
+  if (n && (!cells || !pos || !vel)) gic::fail(GIC_ERR_INVALID_ARG, "null buffer");
+  gic::matched_particles(C, level, cells, n, pos, vel);
+  API_END
+}
+
 int gic_fft(gic_ctx *ctx, int level, int what, int dir) {
   API_BEGIN(ctx)
   gic::Level &L = gic::level_at(C, level);

@@ -410,6 +410,9 @@ double velocity_to_offset_ratio(const Cosmo &c);
 void make_particles(Context &ctx, Level &L, int order = 1);
 // particles of a virtual grid over L's region: factor > 1 supersampled, < -1 subsampled
 void resampled_particles(Context &ctx, const Level &L, int factor, double *host_pos, double *host_vel);
+// particles of listed cells of a zoom level's resolution-matching grid (strays)
+void matched_particles(Context &ctx, int level, const unsigned long long *cells, size_t count, double *pos,
+                       double *vel);
 
 }  // namespace gic
 

@@ -135,6 +135,88 @@ __global__ void k_block_average(const T *__restrict__ src, int n, int s, T *__re
   dst[((size_t)x * nv + y) * (2 * (size_t)(nv / 2 + 1)) + z] = acc / (T)(s * s * s);
 }
 
+// Geometry of a resolution-matching grid (strays): V is level l's resolution over the
+// region of level l-1 (nv cells per side from vx0), the zoom window starts at cell w0 of V
+// (cyclic in V, nw cells per side); the coarse level has nc cells of dxc from cx0.
+struct Matched {
+  int nv, nw, nc, wrap_coarse;
+  int w0[3];
+  double dxv, vx0[3], dxc, cx0[3], period;
+};
+
+__device__ __forceinline__ void catmull_rom_w(double t, double (&w)[4]) {
+  const double t2 = t * t, t3 = t2 * t;
+  w[0] = -(t - 1) * (t - 1) * t / 2;
+  w[1] = (2 - 5 * t2 + 3 * t3) / 2;
+  w[2] = t * (1 + 4 * t - 3 * t2) / 2;
+  w[3] = (t - 1) * t2 / 2;
+}
+
+// genetIC's ResolutionMatchingEvaluator (evaluator.hpp:208-256) per requested cell of the
+// resolution-matching grid: inside the zoom window the level's own displacement, outside it
+// the coarse level's displacement tricubic-interpolated at the cell's centroid (the
+// supersampled low-resolution grid, virtualgrid.hpp:250-255; wrapped when the coarse level
+// is the periodic base, clamped otherwise).  Position = centroid + displacement, wrapped.
+template <typename T>
+__global__ void k_matched_particles(const unsigned long long *cells, size_t count, Matched g, const T *fx, const T *fy,
+                                    const T *fz, const T *cxf, const T *cyf, const T *czf, T ratio, double *pos,
+                                    T *vel) {
+  const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= count) return;
+  const unsigned long long c = cells[id];
+  const int v[3] = {(int)(c / ((unsigned long long)g.nv * g.nv)), (int)((c / g.nv) % g.nv), (int)(c % g.nv)};
+  int w[3];
+  bool inside = true;
+  double cen[3];
+  for (int a = 0; a < 3; ++a) {
+    w[a] = ((v[a] - g.w0[a]) % g.nv + g.nv) % g.nv;
+    inside = inside && w[a] < g.nw;
+    cen[a] = (double)v[a] * g.dxv + g.vx0[a] + g.dxv / 2;
+  }
+  T d[3];
+  if (inside) {
+    const size_t at = ((size_t)w[0] * g.nw + w[1]) * (size_t)(2 * (g.nw / 2 + 1)) + w[2];
+    d[0] = fx[at];
+    d[1] = fy[at];
+    d[2] = fz[at];
+  } else {
+    int base[3];
+    double wt[3][4];
+    for (int a = 0; a < 3; ++a) {
+      double l = fmod(cen[a] - g.cx0[a], g.period);
+      if (l < 0) l += g.period;
+      const double u = l / g.dxc - 0.5, f = floor(u);
+      base[a] = (int)f - 1;
+      catmull_rom_w(u - f, wt[a]);
+    }
+    const size_t crow = 2 * (size_t)(g.nc / 2 + 1);
+    double acc[3] = {0, 0, 0};
+    for (int i = 0; i < 4; ++i) {
+      int ix = base[0] + i;
+      ix = g.wrap_coarse ? ((ix % g.nc) + g.nc) % g.nc : min(max(ix, 0), g.nc - 1);
+      for (int j = 0; j < 4; ++j) {
+        int iy = base[1] + j;
+        iy = g.wrap_coarse ? ((iy % g.nc) + g.nc) % g.nc : min(max(iy, 0), g.nc - 1);
+        const double wij = wt[0][i] * wt[1][j];
+        for (int k = 0; k < 4; ++k) {
+          int iz = base[2] + k;
+          iz = g.wrap_coarse ? ((iz % g.nc) + g.nc) % g.nc : min(max(iz, 0), g.nc - 1);
+          const size_t at = ((size_t)ix * g.nc + iy) * crow + iz;
+          const double ww = wij * wt[2][k];
+          acc[0] += ww * (double)cxf[at];
+          acc[1] += ww * (double)cyf[at];
+          acc[2] += ww * (double)czf[at];
+        }
+      }
+    }
+    for (int a = 0; a < 3; ++a) d[a] = (T)acc[a];
+  }
+  for (int a = 0; a < 3; ++a) {
+    pos[3 * id + a] = wrap_coord((double)d[a] + cen[a], g.period);
+    vel[3 * id + a] = d[a] * ratio;
+  }
+}
+
 template <typename T>
 __global__ void k_widen(const T *src, double *dst, size_t count) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -229,6 +311,64 @@ void resampled_particles(Context &ctx, const Level &L, int factor, double *host_
     resampled_typed<double>(ctx, L, factor, host_pos, host_vel);
   else
     resampled_typed<float>(ctx, L, factor, host_pos, host_vel);
+}
+
+template <typename T>
+static void matched_typed(Context &ctx, const Level &F, const Level &Cl, const unsigned long long *host_cells,
+                          size_t count, double *host_pos, double *host_vel) {
+  Matched g{};
+  const int r = (int)std::lround(Cl.dx / F.dx);
+  g.nv = Cl.n * r;
+  g.nw = F.n;
+  g.nc = Cl.n;
+  g.wrap_coarse = Cl.box == Cl.periodic ? 1 : 0;
+  g.dxv = F.dx;
+  g.dxc = Cl.dx;
+  g.period = F.periodic;
+  for (int a = 0; a < 3; ++a) {
+    g.vx0[a] = Cl.x0[a];
+    g.cx0[a] = Cl.x0[a];
+    // the window's lower corner in cells of the matching grid (virtualgrid.hpp:257-259)
+    g.w0[a] = (int)std::lround((F.x0[a] - Cl.x0[a]) / F.dx);
+  }
+  auto cells = ctx.pool.take(count * sizeof(unsigned long long));
+  auto pos = ctx.pool.take(3 * count * sizeof(double));
+  auto vel = ctx.pool.take(3 * count * sizeof(T));
+  GIC_CUDA(cudaMemcpyAsync(cells->ptr, host_cells, count * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                           ctx.stream));
+  k_matched_particles<T><<<(unsigned)((count + 255) / 256), 256, 0, ctx.stream>>>(
+      cells->as<unsigned long long>(), count, g, F.field[1].as<T>(), F.field[2].as<T>(), F.field[3].as<T>(),
+      Cl.field[1].as<T>(), Cl.field[2].as<T>(), Cl.field[3].as<T>(), (T)velocity_to_offset_ratio(ctx.cosmo),
+      pos->as<double>(), vel->as<T>());
+  launched();
+  GIC_CUDA(cudaMemcpyAsync(host_pos, pos->ptr, 3 * count * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+  if (sizeof(T) == sizeof(double)) {
+    GIC_CUDA(cudaMemcpyAsync(host_vel, vel->ptr, 3 * count * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+  } else {
+    GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+    k_widen<T><<<(unsigned)((3 * count + 255) / 256), 256, 0, ctx.stream>>>(vel->as<T>(), pos->as<double>(), 3 * count);
+    launched();
+    GIC_CUDA(cudaMemcpyAsync(host_vel, pos->ptr, 3 * count * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+  }
+  GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+  ctx.pool.give(std::move(cells));
+  ctx.pool.give(std::move(pos));
+  ctx.pool.give(std::move(vel));
+}
+
+void matched_particles(Context &ctx, int level, const unsigned long long *cells, size_t count, double *pos,
+                       double *vel) {
+  const Level &F = *ctx.levels[level], &Cl = *ctx.levels[level - 1];
+  if (!F.have_fields || !Cl.have_fields) fail(GIC_ERR_NOT_READY, "displacement fields not computed");
+  const unsigned long long nv = (unsigned long long)Cl.n * (unsigned long long)std::lround(Cl.dx / F.dx);
+  const unsigned long long total = nv * nv * nv;
+  for (size_t i = 0; i < count; ++i)
+    if (cells[i] >= total) fail(GIC_ERR_INVALID_ARG, "cell index beyond the resolution-matching grid");
+  if (count == 0) return;
+  if (ctx.dbl())
+    matched_typed<double>(ctx, F, Cl, cells, count, pos, vel);
+  else
+    matched_typed<float>(ctx, F, Cl, cells, count, pos, vel);
 }
 
 void make_particles(Context &ctx, Level &L, int order) {

@@ -633,6 +633,16 @@ class ICGenerator:
         self._call('gic_fetch_particles_resampled', level, int(factor), _ptr(pos), _ptr(vel))
         return pos, vel
 
+    def particles_matched(self, level, cells):
+        """Particles of the listed cells of `level`'s resolution-matching grid (genetIC's
+        output grid of a zoom level with strays on): (positions, velocities)."""
+        cells = np.ascontiguousarray(cells, dtype=np.uint64)
+        pos = np.empty((len(cells), 3), dtype=np.float64)
+        vel = np.empty((len(cells), 3), dtype=np.float64)
+        self._call('gic_fetch_particles_matched', level, cells.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong)),
+                   len(cells), _ptr(pos), _ptr(vel))
+        return pos, vel
+
     # -- particle files (io/tipsy.hpp, io/gadget.hpp) ------------------------------------
     def particle_map(self):
         """The gic_particle_map of this context: genetIC's particle-mapper order over the zoom

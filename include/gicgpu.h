@@ -163,6 +163,18 @@ GIC_API int gic_fetch_particles_native(gic_ctx *ctx, int level, double *pos, voi
  * the virtual grid's cell order, positions = centroid + displacement wrapped into the
  * box, velocities as gic_fetch_particles.  First-order (Zel'dovich) displacements. */
 GIC_API int gic_fetch_particles_resampled(gic_ctx *ctx, int level, int factor, double *pos, double *vel);
+/* Particles of listed cells of a zoom level's resolution-matching grid: the output grid
+ * genetIC gives a zoom level when stray particles are on (strays_on; MultiLevelGrid::addLevel,
+ * genetIC/src/simulation/multilevelgrid/multilevelgrid.hpp:130-137; ResolutionMatchingGrid
+ * and ResolutionMatchingEvaluator, simulation/grid/virtualgrid.hpp:217-300 and
+ * simulation/field/evaluator.hpp:208-256).  That grid has the level's resolution over the
+ * whole region of the level above: (n_{l-1} r)^3 cells, r the cell-size ratio, cell index
+ * (x m + y) m + z with m = n_{l-1} r.  Inside the zoom window a cell's particle is the
+ * level's own; outside it (a stray particle) its displacement is the level above's,
+ * tricubic-interpolated at the cell's centroid.  cells: n indices; pos, vel: n x 3 doubles
+ * (positions wrapped into the box).  level >= 1. */
+GIC_API int gic_fetch_particles_matched(gic_ctx *ctx, int level, const unsigned long long *cells, size_t n,
+                                        double *pos, double *vel);
 
 /* ---- Tipsy particle records (io::tipsy::TipsyOutput, genetIC/src/io/tipsy.hpp) ----
  * One dark-matter record, TipsyParticle::dark (tipsy.hpp:61-63). */

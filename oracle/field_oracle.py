@@ -1114,6 +1114,25 @@ def resample_displacements(psi, box, n, offset, periodic, factor):
     return [p.reshape(nv, s, nv, s, nv, s).sum(axis=(1, 3, 5)) / float(s ** 3) for p in psi], nv
 
 
+def matched_displacements(psi_fine, fine, psi_coarse, coarse, periodic):
+    """A zoom level's displacements on its resolution-matching grid, the output grid of a
+    zoom level with stray particles on (ResolutionMatchingGrid / ResolutionMatchingEvaluator,
+    virtualgrid.hpp:217-300, evaluator.hpp:208-256): the zoom's resolution over the whole
+    region of the level above; the coarse level's fields supersampled (tricubic at the fine
+    centroids), overwritten by the zoom's own inside its window.  fine, coarse: (box, n, offset).
+    Returns (fields, cells per side, the matching grid's (box, n, offset))."""
+    fbox, fn, foff = fine
+    cbox, cn, coff = coarse
+    r = int(round((cbox / cn) / (fbox / fn)))
+    nv = cn * r
+    out = [interpolate_to(p, cbox, coff, periodic, cbox, nv, coff) for p in psi_coarse]
+    w0 = [int(round((foff[a] - coff[a]) / (fbox / fn))) for a in range(3)]
+    ix = [(w0[a] + np.arange(fn)) % nv for a in range(3)]
+    for o, p in zip(out, psi_fine):
+        o[np.ix_(ix[0], ix[1], ix[2])] = p
+    return out, nv, (cbox, nv, coff)
+
+
 def tipsy_records(order, pos, vel, mass, eps, pos_factor, vel_factor, mass_factor):
     """Dark records (mass, x, y, z, vx, vy, vz, eps, phi) as float32 (tipsy.hpp:61-63,
     123-131): products and differences in double, then rounded to float."""

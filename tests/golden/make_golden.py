@@ -602,6 +602,21 @@ def resample_goldens():
                                 tail=dark[-400:].copy())
 
 
+def strays_goldens():
+    """genetIC with stray particles on: a factor-4 zoom at cell (15, 15, 12) of a 32^3 base
+    whose flagged 3 Mpc/h sphere reaches outside the zoom window (genetIC's test_06a
+    geometry, Fourier seeding).  Header bytes and dark records (every 7th and the last 400)."""
+    with tempfile.TemporaryDirectory() as d:
+        write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+        body = 'strays_on\n' + MOD_BASE + 'centre 25 25 25\nselect_sphere 3.0\nzoom_grid_with_origin_at 15 15 12 4 32\ndone\n'
+        open(os.path.join(d, 'paramfile.txt'), 'w').write(body)
+        subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True)
+        raw = open(os.path.join(d, 'out.tipsy'), 'rb').read()
+        _, _, dark = read_tipsy(os.path.join(d, 'out.tipsy'))
+        np.savez_compressed(os.path.join(HERE, 'strays_zoom4.npz'), header_bytes=np.frombuffer(raw[:28], np.uint8).copy(),
+                            nrec=np.int64(len(dark)), stride=np.int64(7), every=dark[::7].copy(), tail=dark[-400:].copy())
+
+
 def main():
     for mode, cmd in (('serial', 'random_seed_serial'), ('parallel', 'random_seed'), ('real', 'random_seed_real_space')):
         with tempfile.TemporaryDirectory() as d:
@@ -625,6 +640,7 @@ if __name__ == '__main__':
     main()
     geometry_goldens()
     resample_goldens()
+    strays_goldens()
     zoom_goldens()
     mod_goldens()
     var_goldens()

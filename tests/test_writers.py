@@ -563,3 +563,38 @@ def test_resampled_oracle_matches_reference_file(bbks, name):
         assert np.array_equal(mine[:, 0], ref[:, 0]) and np.array_equal(mine[:, 7:], ref[:, 7:])
         assert np.abs(mine[:, 1:4] - ref[:, 1:4]).max() <= 6e-8
         assert np.abs(mine[:, 4:7] - ref[:, 4:7]).max() <= 2e-7 * np.abs(ref[:, 4:7]).max()
+
+
+# --- stray particles (genetIC's strays_on; tests/golden/strays_zoom4.npz) ----------------------
+
+STRAYS = [(50.0, 32, (0.0, 0.0, 0.0)), (12.5, 32, (23.4375, 23.4375, 18.75))]  # zoom at cell (15, 15, 12)
+STRAYS_ORIGIN = (15, 15, 12)
+
+
+def strays_oracle(bbks):
+    """The oracle's particles of the strays case: level 0 as usual, the zoom level on its
+    resolution-matching grid (128^3 over the whole box), mapper order and tipsy factors."""
+    from conftest import COSMO
+    fo.set_cr_log(False)
+    w = fo.white_noise_levels([32, 32], 8896131, 2)
+    fields = fo.zoom_realisation(w, STRAYS, fo.CambPower(bbks, COSMO))
+    ratio = fo.velocity_to_offset_ratio(COSMO)
+    psi, nv, vgeom = fo.matched_displacements(fields[1][1:4], STRAYS[1], fields[0][1:4], STRAYS[0], 50.0)
+    pv0 = fo.particles(fields[0][1:4], 50.0, (0.0, 0.0, 0.0), 50.0, ratio)
+    pv1 = fo.particles(psi, vgeom[0], vgeom[2], 50.0, ratio)
+    replaced = fo.flag_cells(fo.Levels(STRAYS), 0, (25., 25., 25.), 'sphere', 3.0)
+    order = fo.mapper_order(32, replaced, nv, nv // 32, (0, 0, 0))
+    factors = fo.tipsy_factors([STRAYS[0], vgeom], COSMO, order[0])
+    return dict(pos=[pv0[0], pv1[0]], vel=[pv0[1], pv1[1]], order=order, factors=factors, replaced=replaced, nv=nv)
+
+
+def test_strays_oracle_matches_reference_file(bbks):
+    g = np.load(os.path.join(GOLDEN, 'strays_zoom4.npz'))
+    r = strays_oracle(bbks)
+    assert len(r['order'][1]) == int(g['nrec'])
+    got = fo.tipsy_records(r['order'], r['pos'], r['vel'], *r['factors'])
+    stride = int(g['stride'])
+    for mine, ref in ((got[::stride], g['every']), (got[-400:], g['tail'])):
+        assert np.array_equal(mine[:, 0], ref[:, 0]) and np.array_equal(mine[:, 7:], ref[:, 7:])
+        assert np.abs(mine[:, 1:4] - ref[:, 1:4]).max() <= 6e-8
+        assert np.abs(mine[:, 4:7] - ref[:, 4:7]).max() <= 2e-7 * np.abs(ref[:, 4:7]).max()
