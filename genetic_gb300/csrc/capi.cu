@@ -419,6 +419,13 @@ int gic_tipsy_pack_host(const gic_particle_map *map, const double *const *pos, c
   HOST_END
 }
 
+int gic_gadget_pack(gic_ctx *ctx, const gic_particle_map *map, const int *level_types, unsigned long long first,
+                    unsigned long long count, float *pos_out, float *vel_out, unsigned long long *ids, float *mass_out) {
+  API_BEGIN(ctx)
+  gic::gadget_pack_device(C, map, level_types, first, count, pos_out, vel_out, ids, mass_out);
+  API_END
+}
+
 int gic_gadget_pack_host(const gic_particle_map *map, const double *const *pos, const double *const *vel,
                          const int *level_types, unsigned long long first, unsigned long long count, float *pos_out,
                          float *vel_out, unsigned long long *ids, float *mass_out, int threads) {

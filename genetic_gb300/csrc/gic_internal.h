@@ -427,6 +427,9 @@ void tipsy_pack_host(const gic_particle_map *m, const double *const *pos, const 
 void gadget_pack_host(const gic_particle_map *m, const double *const *pos, const double *const *vel,
                       const int *level_types, unsigned long long first, unsigned long long count, float *pos_out,
                       float *vel_out, unsigned long long *ids, float *mass_out, int threads);
+void gadget_pack_device(Context &C, const gic_particle_map *m, const int *level_types, unsigned long long first,
+                        unsigned long long count, float *pos_out, float *vel_out, unsigned long long *ids,
+                        float *mass_out);
 void tipsy_pack_device(Context &C, const gic_particle_map *m, unsigned long long first, unsigned long long count,
                        gic_tipsy_dark *host_out);
 // the message of the last failure of a call without a context (this thread)

@@ -385,6 +385,68 @@ __global__ void k_tipsy_fine(gic_tipsy_dark *out, unsigned long long first, unsi
   tipsy_record(out[o - first], pos, vel, fine_cell(v, o - v.n_kept), 1, c);
 }
 
+// Gadget blocks on the device.  File index = mapper index + shift (each level's particles
+// are one run of the mapper order; the file holds them by gadget type).  Outputs for file
+// indices [first, first + count); a level's part of that window is mapper range [lo, hi).
+struct GadgetOut {
+  float *pos, *vel, *mass;
+  unsigned long long *ids;
+  unsigned long long first;
+};
+
+template <typename V>
+__device__ __forceinline__ void gadget_emit(const GadgetOut &g, unsigned long long k, unsigned long long o,
+                                            const double *pos, const V *vel, unsigned long long cell, float mass) {
+  for (int c = 0; c < 3; ++c) {
+    if (g.pos) g.pos[3 * k + c] = (float)pos[3 * cell + c];
+    if (g.vel) g.vel[3 * k + c] = (float)vel[3 * cell + c];
+  }
+  if (g.ids) g.ids[k] = o;
+  if (g.mass) g.mass[k] = mass;
+}
+
+template <typename V>
+__global__ void k_gadget_kept(GadgetOut g, unsigned long long lo, unsigned long long hi, unsigned long long shift,
+                              MapView v, const unsigned long long *rep_begin, const unsigned long long *kept_before,
+                              const double *pos, const V *vel, float mass) {
+  // a CTA per level-0 row, as k_tipsy_kept
+  const unsigned long long row = blockIdx.x;
+  __shared__ unsigned w[kRowWords];
+  __shared__ int pre[kRowWords];
+  if (threadIdx.x < kRowWords) w[threadIdx.x] = 0;
+  __syncthreads();
+  const unsigned long long rb = rep_begin[row], re = rep_begin[row + 1];
+  for (unsigned long long k = rb + threadIdx.x; k < re; k += blockDim.x) {
+    const int z = (int)(v.replaced[k] - row * v.n0);
+    atomicOr(&w[z >> 5], 1u << (z & 31));
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int q = 0; q < kRowWords; ++q) {
+      pre[q] = s;
+      s += __popc(w[q]);
+    }
+  }
+  __syncthreads();
+  const unsigned long long kb = kept_before[row];
+  for (int z = threadIdx.x; z < v.n0; z += blockDim.x) {
+    const int rk = row_rank(w, pre, z);
+    if (rk < 0) continue;
+    const unsigned long long o = kb + (unsigned long long)rk;
+    if (o < lo || o >= hi) continue;
+    gadget_emit(g, o + shift - g.first, o, pos, vel, row * v.n0 + z, mass);
+  }
+}
+
+template <typename V>
+__global__ void k_gadget_fine(GadgetOut g, unsigned long long lo, unsigned long long hi, unsigned long long shift,
+                              MapView v, const double *pos, const V *vel, float mass) {
+  const unsigned long long o = lo + (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= hi) return;
+  gadget_emit(g, o + shift - g.first, o, pos, vel, fine_cell(v, o - v.n_kept), mass);
+}
+
 }  // namespace
 
 unsigned long long tipsy_count(const gic_particle_map *m) { return check_full(m).total; }
@@ -509,6 +571,88 @@ static void launch_tipsy(Context &C, const MapView &dv, const TipsyConst &c, uns
                                                                              L1.vel.as<V>(), c);
     launched();
   }
+}
+
+template <typename V>
+static void launch_gadget(Context &C, const MapView &dv, const GadgetOut &g, const unsigned long long *lo,
+                          const unsigned long long *hi, const unsigned long long *shift, const float *mass,
+                          const unsigned long long *rep_begin, const unsigned long long *kept_before) {
+  if (hi[0] > lo[0]) {
+    const Level &L0 = *C.levels[0];
+    k_gadget_kept<V><<<(unsigned)((unsigned long long)dv.n0 * dv.n0), 256, 0, C.stream>>>(
+        g, lo[0], hi[0], shift[0], dv, rep_begin, kept_before, L0.pos.as<double>(), L0.vel.as<V>(), mass[0]);
+    launched();
+  }
+  if (dv.nlevels == 2 && hi[1] > lo[1]) {
+    const Level &L1 = *C.levels[1];
+    k_gadget_fine<V><<<(unsigned)((hi[1] - lo[1] + 255) / 256), 256, 0, C.stream>>>(g, lo[1], hi[1], shift[1], dv,
+                                                                                    L1.pos.as<double>(), L1.vel.as<V>(),
+                                                                                    mass[1]);
+    launched();
+  }
+}
+
+void gadget_pack_device(Context &C, const gic_particle_map *m, const int *level_types, unsigned long long first,
+                        unsigned long long count, float *pos_out, float *vel_out, unsigned long long *ids,
+                        float *mass_out) {
+  const MapView v = check_map(m);
+  if (level_types)
+    for (int l = 0; l < v.nlevels; ++l)
+      if (level_types[l] < 0 || level_types[l] > 5) fail(GIC_ERR_INVALID_ARG, "gadget particle types are 0 to 5");
+  const void *any = pos_out ? (const void *)pos_out : vel_out ? (const void *)vel_out : ids ? (const void *)ids
+                                                                                         : (const void *)mass_out;
+  check_window(map_size(v), first, count, any);
+  if ((int)C.levels.size() < v.nlevels) fail(GIC_ERR_NOT_READY, "the map has more levels than the context");
+  for (int l = 0; l < v.nlevels; ++l) {
+    const Level &L = *C.levels[l];
+    if (L.n != m->n[l]) fail(GIC_ERR_INVALID_ARG, "map and level sizes differ");
+    if (!L.pos.ptr || !L.vel.ptr) fail(GIC_ERR_NOT_READY, "particles have not been generated");
+  }
+  if (!count) return;
+  // mapper runs of the levels, their file positions by type, the window per level
+  const unsigned long long start[2] = {0, v.n_kept}, len[2] = {v.n_kept, v.n_replaced * v.per_block};
+  unsigned long long file_at[2] = {0, 0}, at = 0, lo[2] = {0, 0}, hi[2] = {0, 0}, shift[2] = {0, 0};
+  for (int t = 0; t < 6; ++t)
+    for (int l = 0; l < v.nlevels; ++l)
+      if ((level_types ? level_types[l] : 1) == t) {
+        file_at[l] = at;
+        at += len[l];
+      }
+  const unsigned long long end = first + count;
+  for (int l = 0; l < v.nlevels; ++l) {
+    const unsigned long long a = std::max(first, file_at[l]), b = std::min(end, file_at[l] + len[l]);
+    shift[l] = file_at[l] - start[l];
+    if (b > a) {
+      lo[l] = a - shift[l];
+      hi[l] = b - shift[l];
+    }
+  }
+  float mass[2] = {(float)m->mass[0], (float)m->mass[1]};
+  std::vector<unsigned long long> rep_begin, kept_before;
+  row_tables(v, rep_begin, kept_before);
+  const size_t rows = (size_t)v.n0 * v.n0, u = sizeof(unsigned long long);
+  auto drep = C.pool.take(std::max<size_t>(1, v.n_replaced) * u), dbeg = C.pool.take((rows + 1) * u),
+       dkept = C.pool.take(rows * u);
+  auto dpos = C.pool.take(pos_out ? 3 * count * sizeof(float) : 1), dvel = C.pool.take(vel_out ? 3 * count * sizeof(float) : 1),
+       dids = C.pool.take(ids ? count * u : 1), dmass = C.pool.take(mass_out ? count * sizeof(float) : 1);
+  if (v.n_replaced)
+    GIC_CUDA(cudaMemcpyAsync(drep->ptr, v.replaced, v.n_replaced * u, cudaMemcpyHostToDevice, C.stream));
+  GIC_CUDA(cudaMemcpyAsync(dbeg->ptr, rep_begin.data(), (rows + 1) * u, cudaMemcpyHostToDevice, C.stream));
+  GIC_CUDA(cudaMemcpyAsync(dkept->ptr, kept_before.data(), rows * u, cudaMemcpyHostToDevice, C.stream));
+  MapView dv = v;
+  dv.replaced = drep->as<unsigned long long>();
+  GadgetOut g{pos_out ? dpos->as<float>() : nullptr, vel_out ? dvel->as<float>() : nullptr,
+              mass_out ? dmass->as<float>() : nullptr, ids ? dids->as<unsigned long long>() : nullptr, first};
+  if (C.dbl())
+    launch_gadget<double>(C, dv, g, lo, hi, shift, mass, dbeg->as<unsigned long long>(), dkept->as<unsigned long long>());
+  else
+    launch_gadget<float>(C, dv, g, lo, hi, shift, mass, dbeg->as<unsigned long long>(), dkept->as<unsigned long long>());
+  if (pos_out) GIC_CUDA(cudaMemcpyAsync(pos_out, g.pos, 3 * count * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
+  if (vel_out) GIC_CUDA(cudaMemcpyAsync(vel_out, g.vel, 3 * count * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
+  if (ids) GIC_CUDA(cudaMemcpyAsync(ids, g.ids, count * u, cudaMemcpyDeviceToHost, C.stream));
+  if (mass_out) GIC_CUDA(cudaMemcpyAsync(mass_out, g.mass, count * sizeof(float), cudaMemcpyDeviceToHost, C.stream));
+  GIC_CUDA(cudaStreamSynchronize(C.stream));
+  for (auto *b : {&drep, &dbeg, &dkept, &dpos, &dvel, &dids, &dmass}) C.pool.give(std::move(*b));
 }
 
 void tipsy_pack_device(Context &C, const gic_particle_map *m, unsigned long long first, unsigned long long count,

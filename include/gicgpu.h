@@ -246,6 +246,15 @@ GIC_API int gic_gadget_pack_host(const gic_particle_map *map, const double *cons
                                  const int *level_types, unsigned long long first, unsigned long long count,
                                  float *pos_out, float *vel_out, unsigned long long *ids, float *mass_out, int threads);
 
+/* The same gadget blocks packed on the device from the context's particles (after
+ * gic_zeldovich) and copied to the host outputs, for maps of one or two levels: 40 bytes
+ * per particle (all four blocks) cross to the host instead of the 48 of
+ * gic_fetch_particles, and no host thread walks the mapper order.  Bit for bit the blocks
+ * of gic_gadget_pack_host given the fetched particles. */
+GIC_API int gic_gadget_pack(gic_ctx *ctx, const gic_particle_map *map, const int *level_types, unsigned long long first,
+                            unsigned long long count, float *pos_out, float *vel_out, unsigned long long *ids,
+                            float *mass_out);
+
 /* Forward (dir=-1) or inverse (dir=+1) normalised 3-D real FFT of a level field
  * in place on the device (testing).  Replaces FieldFourierManager<T,T>::performTransform
  * (fourier.hpp:479-518). */

@@ -37,3 +37,62 @@ def test_device_tipsy_matches_host_packer(built, bbks, precision):
         gen._call('gic_tipsy_pack', ctypes.byref(m), first, 500, part.ctypes.data_as(ctypes.c_void_p))
         assert np.array_equal(part.view(np.uint32), want[first:first + 500].view(np.uint32))
     gen.close()
+
+
+def _gadget_host(lib, m, pos, vel, types, first, count):
+    P = ctypes.POINTER(ctypes.c_double)
+    pp = (P * len(pos))(*[np.ascontiguousarray(p).ctypes.data_as(P) for p in pos])
+    vv = (P * len(vel))(*[np.ascontiguousarray(v).ctypes.data_as(P) for v in vel])
+    t = (ctypes.c_int * len(types))(*types) if types else None
+    out = (np.zeros((count, 3), np.float32), np.zeros((count, 3), np.float32), np.zeros(count, np.uint64),
+           np.zeros(count, np.float32))
+    rc = lib.gic_gadget_pack_host(ctypes.byref(m), pp, vv, t, first, count, *[o.ctypes.data_as(ctypes.c_void_p) for o in out],
+                                  4)
+    return rc, out
+
+
+def _gadget_device(gen, m, types, first, count):
+    t = (ctypes.c_int * len(types))(*types) if types else None
+    out = (np.zeros((count, 3), np.float32), np.zeros((count, 3), np.float32), np.zeros(count, np.uint64),
+           np.zeros(count, np.float32))
+    gen._call('gic_gadget_pack', ctypes.byref(m), t, first, count, *[o.ctypes.data_as(ctypes.c_void_p) for o in out])
+    return out
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'mixed'])
+@pytest.mark.parametrize('types', [None, (3, 1), (1, 1)])
+def test_device_gadget_matches_host_packer(built, bbks, precision, types):
+    """gic_gadget_pack (the four blocks on the device) against gic_gadget_pack_host given the
+    fetched particles, bit for bit: the whole file, and windows across the level boundary."""
+    from genetic_gb300 import _lib
+    lib = _lib.load()
+    gen = make_generator(precision, bbks, LEVELS, 8896131, 'random_seed')
+    gen.done()
+    parts = [gen.particles(l) for l in range(2)]
+    replaced = fo.flag_cells(fo.Levels(ZOOM2), 0, (25., 25., 25.), 'cube', 10)
+    lev, _ = fo.mapper_order(32, replaced, 32, 2, ORIGIN)
+    m = make_map(ZOOM2, replaced, fo.tipsy_factors(ZOOM2, COSMO, lev))
+    n = len(lev)
+    for first, count in ((0, n), (n - 5000, 4000), (27000, 3000)):
+        rc, want = _gadget_host(lib, m, [p for p, _ in parts], [v for _, v in parts], types, first, count)
+        assert rc == 0
+        got = _gadget_device(gen, m, types, first, count)
+        for a, b in zip(got, want):
+            assert np.array_equal(a.view(np.uint8), b.view(np.uint8)), (first, count)
+    gen.close()
+
+
+def test_device_gadget_one_level(built, bbks):
+    from genetic_gb300 import _lib
+    lib = _lib.load()
+    gen = make_generator('mixed', bbks, [('base', 50.0, 32)], 8896131, 'random_seed')
+    gen.done()
+    pos, vel = gen.particles(0)
+    one = [ZOOM2[0]]
+    m = make_map(one, np.zeros(0, np.uint64), fo.tipsy_factors(one, COSMO, np.zeros(32 ** 3, int)))
+    rc, want = _gadget_host(lib, m, [pos], [vel], None, 0, 32 ** 3)
+    assert rc == 0
+    got = _gadget_device(gen, m, None, 0, 32 ** 3)
+    for a, b in zip(got, want):
+        assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
+    gen.close()
