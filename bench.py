@@ -59,12 +59,13 @@ WORKLOADS = {
 }
 # 64 independent realisations in one batch (mixed precision, seeds 1..64): 32 single-level
 # 128^3 boxes (50 Mpc/h), 24 single-level 192^3 boxes (75 Mpc/h) and 8 two-level zooms of a
-# 256^3 base (100 Mpc/h) plus a 128^3 zoom of side 25 Mpc/h centred at (50, 50, 50), each zoom
+# 256^3 base (100 Mpc/h) plus a 128^3 zoom of side 25 Mpc/h centred at (50, 50, 50) (genetIC zoom
+# factor 4, cells half the base cells), each zoom
 # with 2 modifications: overdensity +1.0 in a 1.5 Mpc/h sphere at the centre and -0.5 in a
 # 3 Mpc/h sphere 5 Mpc/h along x
 BATCH64 = ([dict(levels=[('base', 50.0, 128)], mods=[])] * 32 +
            [dict(levels=[('base', 75.0, 192)], mods=[])] * 24 +
-           [dict(levels=[('base', 100.0, 256), ('zoom', 96, 96, 96, 2, 128)], replaced=64 ** 3,
+           [dict(levels=[('base', 100.0, 256), ('zoom', 96, 96, 96, 4, 128)], replaced=64 ** 3,
                  mods=[((50.0, 50.0, 50.0), 1.5, 1.0), ((55.0, 50.0, 50.0), 3.0, -0.5)])] * 8)
 WORKLOADS['batch64'] = dict(batch=BATCH64, precision='mixed', seed_cmd='random_seed', levels=[])
 DEFAULT_WORKLOAD = 'zoom512'

@@ -130,6 +130,8 @@ SIGNATURES = {
     'gic_batch_realise': [_P, ctypes.POINTER(ctypes.c_ulong), ctypes.POINTER(_I), _I, _I],
     'gic_batch_last_error': [_P],
     'gic_batch_get_stream': [_P, ctypes.POINTER(_P)],
+    'gic_batch_graph_info': [_P, ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(_I),
+                             ctypes.POINTER(ctypes.c_char_p)],
     'gic_noise_real': [_P, _I, _P],
     'gic_field_from_noise': [_P, _I, _I, ctypes.POINTER(_P), _P],
     'gic_field_from_noise_adjoint': [_P, _I, _I, _P, ctypes.POINTER(_P)],

@@ -1,6 +1,7 @@
 """Many independent realisations on one GPU through the batch entry points of the
-C ABI (gic_batch_*): noise and modifications from a pool of host threads, each
-context on its own stream, and the field maps of all contexts as one CUDA graph.
+C ABI (gic_batch_*): the whole realisation of every context (noise, linear
+modifications, fields, particles) as one CUDA graph, each context on its own stream;
+contexts with a variance modification from a pool of host threads beside it.
 
   gens = [ICGenerator(precision='mixed') for _ in range(64)]   # set up like any generator
   with Batch(gens) as b:
@@ -36,6 +37,14 @@ class Batch:
             raise _lib.GicError(st, self._lib.gic_batch_last_error(self._handle).decode())
         for g in self.generators:
             g._drawn = True
+
+    def graph_info(self):
+        """(contexts in the graph, kernels per replay, replays since capture, why
+        capturing stopped or '')."""
+        c, k, r, why = ctypes.c_int(), ctypes.c_ulonglong(), ctypes.c_int(), ctypes.c_char_p()
+        self._lib.gic_batch_graph_info(self._handle, ctypes.byref(c), ctypes.byref(k), ctypes.byref(r),
+                                       ctypes.byref(why))
+        return c.value, k.value, r.value, (why.value or b'').decode()
 
     def stream(self):
         s = ctypes.c_void_p()

@@ -1,20 +1,23 @@
 // Batches of independent realisations on one GPU (no genetIC counterpart: the
 // reference realises one set of initial conditions per process).
 //
-// Each context of a batch keeps its own stream and buffers.  One call of
-// gic_batch_realise draws every context's white noise and applies its queued
-// modifications from a pool of host threads (these steps take host decisions:
-// the RNG's segment retries, the Gram-Schmidt scalars), then runs the field maps
-// of every context -- Zel'dovich spectra, inverse FFTs, zoom combination and
-// particles -- as one CUDA graph: captured once, with a fork from an origin stream
-// to each context's stream and a join back, and replayed on later calls.  Small
-// realisations then overlap on the GPU instead of queueing behind one another,
-// and the ~10^2 kernel launches of each are one graph launch.  The graph holds the
-// contexts' device pointers; a signature of those pointers is checked before
-// every replay and the graph is captured again when any changed.  Second-order
-// (2LPT) fields use pooled scratch and run eagerly from the worker threads.
+// Each context of a batch keeps its own stream and buffers.  The whole realisation of
+// every context -- white noise, linear modifications, Zel'dovich (or 2LPT) spectra,
+// inverse FFTs, zoom combination and particles -- is one CUDA graph, captured on the
+// first call (after one eager realisation, which allocates every buffer, tunes the FFTs
+// and caches the geometry) with a fork from an origin stream to each context's stream
+// and a join back, and replayed on later calls.  Nothing in it goes to the host: the
+// Gram-Schmidt of the modifications runs on the device, the noise streams' descriptors
+// (which carry the seeds) are copied to the device before each replay, and the RNG's
+// underrun flag is read after it (a context whose stream ran short is realised again
+// eagerly, with a longer stream).  The graph holds device pointers: a signature of
+// them, of the seeding modes, the order, the modifications and of every buffer the
+// contexts have freed since is checked before each replay, and the graph is captured
+// again when any changed.  Contexts with a quadratic (variance) modification, whose
+// iteration count is a host decision, are realised eagerly by host threads beside it.
 #include "gic_internal.h"
 #include <atomic>
+#include <cstring>
 #include <mutex>
 #include <thread>
 
@@ -26,7 +29,11 @@ struct gic_batch {
   std::vector<cudaEvent_t> done;
   cudaGraphExec_t exec = nullptr;
   std::vector<uintptr_t> signature;
+  std::vector<int> in_graph;  // the contexts the graph realises
   unsigned long long graph_kernels = 0;
+  int replays = 0;         // graph launches since the last capture
+  int failed_captures = 0;
+  std::string graph_off;   // why the batch stopped capturing (a capture that failed)
   std::string last_error;
 };
 
@@ -58,6 +65,16 @@ void append_signature(const Context &C, std::vector<uintptr_t> &sig) {
   for (auto &t : C.fft.tuned) sig.push_back((uintptr_t)(t.n * 64 + t.cols * 8 + t.rows) * 16 + (uintptr_t)(t.planes + 1));
   sig.push_back((uintptr_t)C.fft.plane_sync.ptr);
   sig.push_back((uintptr_t)C.fft.wait_flag_dev);
+  // a buffer that existed when the graph was captured, freed since (a regrowth or a
+  // release), may be one the graph uses
+  sig.push_back((uintptr_t)C.account.frees.load());
+  sig.push_back((uintptr_t)C.mods.size());
+  for (auto &m : C.mods) {
+    uintptr_t bits;
+    static_assert(sizeof(bits) >= sizeof(double), "pointer-sized signature entries");
+    std::memcpy(&bits, &m.target, sizeof(double));
+    sig.push_back(bits);
+  }
 }
 
 void field_maps(Context &C, int order) {
@@ -69,39 +86,91 @@ void field_maps(Context &C, int order) {
   for (int l = 0; l < nl; ++l) make_particles(C, *C.levels[l], order);
 }
 
-void capture(gic_batch &b) {
+// one realisation: noise, modifications, fields and particles
+void realise_one(Context &C, unsigned long long seed, int mode, int order) {
+  AccountScope scope(C.account);
+  cuda_check(cudaSetDevice(C.device), "cudaSetDevice");
+  if (C.levels.empty()) fail(GIC_ERR_NOT_READY, "a context of the batch has no grid levels");
+  draw_noise_all(C, seed, mode);
+  for (auto &L : C.levels) L->have_fields = L->have_lpt2 = false;
+  if (!C.mods.empty() || !C.quads.empty()) apply_modifications(C, nullptr, nullptr);
+  field_maps(C, order);
+}
+
+// whether a context's realisation can be captured: linear modifications only (their
+// coefficients are formed on the device)
+bool capturable(const Context &C) { return C.quads.empty() && C.mods.size() <= 16; }
+
+// Captures the realisations of b.in_graph; false (and no graph) when a buffer was freed
+// during the capture (a scratch buffer that grew): the graph could hold its pointer.
+bool capture(gic_batch &b, const std::vector<int> &modes, int order) {
   release_graph(b);
+  std::vector<unsigned long long> frees0;
+  for (int i : b.in_graph) {
+    MemAccount &a = b.ctxs[i]->impl.account;
+    a.graph_serial = ~0ull;  // during the capture every free counts
+    frees0.push_back(a.frees.load());
+  }
   cudaEvent_t fork;
   GIC_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
   const unsigned long long k0 = launch_count();
   GIC_CUDA(cudaStreamBeginCapture(b.origin, cudaStreamCaptureModeRelaxed));
   try {
     GIC_CUDA(cudaEventRecord(fork, b.origin));
-    for (size_t i = 0; i < b.ctxs.size(); ++i) {
+    for (int i : b.in_graph) {
       Context &C = b.ctxs[i]->impl;
       GIC_CUDA(cudaStreamWaitEvent(C.stream, fork, 0));
-      field_maps(C, 1);
+      C.defer_checks = true;
+      // the seed does not matter here: the streams' descriptors are copied before each replay
+      realise_one(C, 0, modes[i], order);
+      C.defer_checks = false;
       GIC_CUDA(cudaEventRecord(b.done[i], C.stream));
       GIC_CUDA(cudaStreamWaitEvent(b.origin, b.done[i], 0));
     }
   } catch (...) {
+    for (auto *c : b.ctxs) c->impl.defer_checks = false;
     cudaGraph_t g = nullptr;
     cudaStreamEndCapture(b.origin, &g);
     if (g) cudaGraphDestroy(g);
     cudaGetLastError();
     cudaEventDestroy(fork);
+    count_launches(0ull - (launch_count() - k0));
     throw;
   }
   cudaGraph_t g = nullptr;
   GIC_CUDA(cudaStreamEndCapture(b.origin, &g));
+  bool stable = true;
+  for (size_t k = 0; k < b.in_graph.size(); ++k)
+    stable = stable && b.ctxs[b.in_graph[k]]->impl.account.frees.load() == frees0[k];
+  if (!stable) {
+    cudaGraphDestroy(g);
+    cudaEventDestroy(fork);
+    count_launches(0ull - (launch_count() - k0));
+    return false;
+  }
   cudaError_t e = cudaGraphInstantiate(&b.exec, g, 0);
   cudaGraphDestroy(g);
   cudaEventDestroy(fork);
   GIC_CUDA(e);
+  // from now on only buffers that existed during the capture can invalidate the graph
+  for (int i : b.in_graph) {
+    MemAccount &a = b.ctxs[i]->impl.account;
+    a.graph_serial = a.serial.load();
+  }
   // the launches recorded during capture ran nothing yet
   b.graph_kernels = launch_count() - k0;
   count_launches(0ull - b.graph_kernels);
-  for (auto *c : b.ctxs) append_signature(c->impl, b.signature);
+  return true;
+}
+
+std::vector<uintptr_t> batch_signature(const gic_batch &b, const std::vector<int> &modes, int order) {
+  std::vector<uintptr_t> sig{(uintptr_t)order};
+  for (int i : b.in_graph) {
+    sig.push_back((uintptr_t)i);
+    sig.push_back((uintptr_t)modes[i]);
+    append_signature(b.ctxs[i]->impl, sig);
+  }
+  return sig;
 }
 
 }  // namespace
@@ -158,6 +227,16 @@ GIC_API int gic_batch_destroy(gic_batch *b) {
 
 GIC_API const char *gic_batch_last_error(const gic_batch *b) { return b ? b->last_error.c_str() : "null batch"; }
 
+GIC_API int gic_batch_graph_info(const gic_batch *b, int *contexts, unsigned long long *kernels, int *replays,
+                                 const char **off_reason) {
+  if (!b) return GIC_ERR_INVALID_ARG;
+  if (contexts) *contexts = b->exec ? (int)b->in_graph.size() : 0;
+  if (kernels) *kernels = b->exec ? b->graph_kernels : 0;
+  if (replays) *replays = b->replays;
+  if (off_reason) *off_reason = b->graph_off.c_str();
+  return GIC_OK;
+}
+
 GIC_API int gic_batch_get_stream(gic_batch *b, void **stream) {
   if (!b || !stream) return GIC_ERR_INVALID_ARG;
   *stream = (void *)b->origin;
@@ -171,82 +250,102 @@ GIC_API int gic_batch_realise(gic_batch *b, const unsigned long *seeds, const in
     return GIC_ERR_INVALID_ARG;
   }
   const int n = (int)b->ctxs.size();
-  threads = std::max(1, std::min(threads, n));
-  std::atomic<int> next{0};
+  std::vector<int> mode(n);
+  for (int i = 0; i < n; ++i) {
+    mode[i] = modes ? modes[i] : GIC_SEED_FOURIER_PARALLEL;
+    if (mode[i] < 0 || mode[i] > 3) {
+      b->last_error = "unknown seeding mode";
+      return GIC_ERR_INVALID_ARG;
+    }
+  }
+  std::vector<int> in_graph, eager;
+  for (int i = 0; i < n; ++i)
+    (b->graph_off.empty() && gic::capturable(b->ctxs[i]->impl) ? in_graph : eager).push_back(i);
   std::mutex err_mutex;
   int err_code = GIC_OK;
   std::string err_msg;
-  try {
-    gic::cuda_check(cudaSetDevice(b->device), "cudaSetDevice");
-    gic::cuda_check(cudaEventRecord(b->start, b->origin), "cudaEventRecord");
-  } catch (const gic::Error &e) {
-    b->last_error = e.msg;
-    return e.code;
-  }
-  const bool use_graph = order == 1;
-  // noise and modifications, one context at a time per worker, on the context's stream
-  auto worker = [&]() {
-    for (;;) {
-      int i = next.fetch_add(1);
-      if (i >= n) return;
-      gic::Context &C = b->ctxs[i]->impl;
-      try {
-        gic::AccountScope scope(C.account);
-        gic::cuda_check(cudaSetDevice(C.device), "cudaSetDevice");
-        if (C.levels.empty()) gic::fail(GIC_ERR_NOT_READY, "a context of the batch has no grid levels");
-        gic::cuda_check(cudaStreamWaitEvent(C.stream, b->start, 0), "cudaStreamWaitEvent");
-        gic::draw_noise_all(C, seeds[i], modes ? modes[i] : GIC_SEED_FOURIER_PARALLEL);
-        for (auto &L : C.levels) L->have_fields = L->have_lpt2 = false;
-        if (!C.mods.empty() || !C.quads.empty()) gic::apply_modifications(C, nullptr, nullptr);
-        if (!use_graph) gic::field_maps(C, order);
-        gic::cuda_check(cudaEventRecord(b->done[i], C.stream), "cudaEventRecord");
-      } catch (const gic::Error &e) {
-        std::lock_guard<std::mutex> lock(err_mutex);
-        if (err_code == GIC_OK) {
-          err_code = e.code;
-          err_msg = e.msg;
-        }
-      } catch (const std::exception &e) {
-        std::lock_guard<std::mutex> lock(err_mutex);
-        if (err_code == GIC_OK) {
-          err_code = GIC_ERR_CUDA;
-          err_msg = e.what();
-        }
-      }
+  auto record = [&](int code, const std::string &msg) {
+    std::lock_guard<std::mutex> lock(err_mutex);
+    if (err_code == GIC_OK) {
+      err_code = code;
+      err_msg = msg;
     }
   };
-  std::vector<std::thread> pool;
-  for (int t = 1; t < threads; ++t) pool.emplace_back(worker);
-  worker();
-  for (auto &t : pool) t.join();
-  if (err_code != GIC_OK) {
-    for (auto *c : b->ctxs) cudaStreamSynchronize(c->impl.stream);
-    b->last_error = err_msg;
-    return err_code;
-  }
-  try {
-    for (int i = 0; i < n; ++i) gic::cuda_check(cudaStreamWaitEvent(b->origin, b->done[i], 0), "cudaStreamWaitEvent");
-    if (use_graph) {
-      std::vector<uintptr_t> sig;
-      for (auto *c : b->ctxs) gic::append_signature(c->impl, sig);
-      if (!b->exec || sig != b->signature) {
-        // the first realisation of a context allocates its buffers and tunes its
-        // FFTs: run the maps once outside the graph, then capture
-        gic::cuda_check(cudaStreamSynchronize(b->origin), "cudaStreamSynchronize");
-        for (auto *c : b->ctxs) {
-          gic::field_maps(c->impl, 1);
-          gic::cuda_check(cudaStreamSynchronize(c->impl.stream), "cudaStreamSynchronize");
+  // realisations one context at a time per host thread, each on its context's stream
+  auto run_eager = [&](const std::vector<int> &which) {
+    std::atomic<int> next{0};
+    auto worker = [&]() {
+      for (;;) {
+        const int k = next.fetch_add(1);
+        if (k >= (int)which.size()) return;
+        const int i = which[k];
+        gic::Context &C = b->ctxs[i]->impl;
+        try {
+          gic::realise_one(C, seeds[i], mode[i], order);
+        } catch (const gic::Error &e) {
+          record(e.code, e.msg);
+        } catch (const std::exception &e) {
+          record(GIC_ERR_CUDA, e.what());
         }
-        gic::capture(*b);
       }
-      gic::cuda_check(cudaGraphLaunch(b->exec, b->origin), "cudaGraphLaunch");
-      gic::count_launches(b->graph_kernels);
-      for (int i = 0; i < n; ++i) {
-        gic::cuda_check(cudaEventRecord(b->done[i], b->origin), "cudaEventRecord");
-        gic::cuda_check(cudaStreamWaitEvent(b->ctxs[i]->impl.stream, b->done[i], 0), "cudaStreamWaitEvent");
+    };
+    const int nt = std::max(1, std::min(threads, (int)which.size()));
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; ++t) pool.emplace_back(worker);
+    worker();
+    for (auto &t : pool) t.join();
+  };
+  try {
+    gic::cuda_check(cudaSetDevice(b->device), "cudaSetDevice");
+    bool replay = false;
+    if (!in_graph.empty()) {
+      b->in_graph = in_graph;
+      const std::vector<uintptr_t> sig = gic::batch_signature(*b, mode, order);
+      replay = b->exec && sig == b->signature;
+      if (replay) {
+        for (int i : in_graph) {
+          gic::Context &C = b->ctxs[i]->impl;
+          gic::AccountScope scope(C.account);
+          gic::upload_noise_streams(C, seeds[i], mode[i]);
+        }
+        gic::cuda_check(cudaGraphLaunch(b->exec, b->origin), "cudaGraphLaunch");
+        gic::count_launches(b->graph_kernels);
+        ++b->replays;
       }
     }
+    // contexts outside the graph (and, before the first capture, all of them) eagerly
+    run_eager(replay ? eager : [&] {
+      std::vector<int> all(n);
+      for (int i = 0; i < n; ++i) all[i] = i;
+      return all;
+    }());
+    if (err_code != GIC_OK) {
+      for (auto *c : b->ctxs) cudaStreamSynchronize(c->impl.stream);
+      cudaStreamSynchronize(b->origin);
+      b->last_error = err_msg;
+      return err_code;
+    }
     gic::cuda_check(cudaStreamSynchronize(b->origin), "cudaStreamSynchronize");
+    for (auto *c : b->ctxs) gic::cuda_check(cudaStreamSynchronize(c->impl.stream), "cudaStreamSynchronize");
+    if (replay) {
+      // a stream that ran short of raw numbers: that realisation again, with a longer stream
+      for (int i : in_graph)
+        if (gic::noise_underrun(b->ctxs[i]->impl)) gic::realise_one(b->ctxs[i]->impl, seeds[i], mode[i], order);
+    } else if (!in_graph.empty()) {
+      // every buffer now exists: capture the realisations of the graph's contexts.  The
+      // realisations are already complete, so a capture that fails only ends capturing.
+      try {
+        if (gic::capture(*b, mode, order)) {
+          b->signature = gic::batch_signature(*b, mode, order);
+          b->replays = 0;
+        } else if (++b->failed_captures >= 3) {
+          b->graph_off = "scratch buffers were reallocated during three captures";
+        }
+      } catch (const gic::Error &e) {
+        gic::release_graph(*b);
+        b->graph_off = e.msg.empty() ? "stream capture failed" : e.msg;
+      }
+    }
     for (auto *c : b->ctxs)
       if (gic::take_fft_wait_error(c->impl)) gic::fail(GIC_ERR_TIMEOUT, c->impl.last_error);
     for (auto *c : b->ctxs)

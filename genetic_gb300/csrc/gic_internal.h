@@ -31,6 +31,13 @@ void cuda_check(cudaError_t e, const char *what);
 struct MemAccount {
   std::atomic<size_t> used{0};
   size_t limit = 0;  // bytes; 0 = no limit
+  // A captured CUDA graph holds device pointers: every allocation gets a serial number,
+  // and `frees` counts the releases (or regrowths) of buffers whose serial is at most
+  // graph_serial, the last serial when the context's realisation was captured (all
+  // buffers before any capture).  Buffers made after a capture cannot be in its graph.
+  std::atomic<unsigned long long> serial{0};
+  std::atomic<unsigned long long> graph_serial{~0ull};
+  std::atomic<unsigned long long> frees{0};
 };
 extern thread_local MemAccount *t_account;
 struct AccountScope {
@@ -46,12 +53,16 @@ struct DevBuf {
   void *ptr = nullptr;
   size_t bytes = 0;
   MemAccount *acct = nullptr;
+  unsigned long long serial = 0;  // allocation number in acct
   DevBuf() = default;
   DevBuf(const DevBuf &) = delete;
   DevBuf &operator=(const DevBuf &) = delete;
   ~DevBuf() { release(); }
   void release() {
-    if (ptr) cudaFree(ptr);
+    if (ptr) {
+      cudaFree(ptr);
+      if (acct && serial <= acct->graph_serial.load()) acct->frees++;
+    }
     if (acct) acct->used -= bytes;
     acct = nullptr;
     ptr = nullptr;
@@ -75,6 +86,7 @@ struct DevBuf {
     if (a) {
       a->used += nbytes;
       acct = a;
+      serial = ++a->serial;
     }
   }
   template <typename T> T *as() const { return static_cast<T *>(ptr); }
@@ -112,6 +124,7 @@ struct BufPool {
 struct GeomEntry;
 struct ModScratch {
   DevBuf tab, tabf, conv, masks, tmp_src, win, cells, geom, t1, t2, t3, reduce, compact, csum, fold, btab;
+  DevBuf gram;  // the correction's coefficients, formed on the device
   int btab_n = 0, btab_r = 0;  // the (N, r) btab holds the block filter of
   std::vector<std::unique_ptr<GeomEntry>> geom_cache;
   const unsigned char *cur_masks = nullptr;  // the masks of the last window setup (in geom_cache)
@@ -266,6 +279,10 @@ struct CachedTable {
 struct Context {
   MemAccount account;  // first: destroyed after every buffer charged to it
   int device = 0;
+  // set while a batch captures this context's realisation into a CUDA graph: no host
+  // synchronisation or host-memory copies; the noise draw's stream descriptors are
+  // uploaded (upload_noise_streams) before each replay and its underrun flag read after
+  bool defer_checks = false;
   int precision = GIC_FP64;
   cudaStream_t stream = nullptr;
   std::string last_error;
@@ -278,6 +295,7 @@ struct Context {
   DevBuf reduce;  // small scratch for reductions
   DevBuf zoom_scratch[4];  // low-passed coarse fields during zoom combination
   DevBuf geom;             // per-axis interpolation / centroid tables
+  DevBuf lpt2_tab, lpt2_tabt;  // the 2LPT multiplier table (double) and its typed copy
   std::vector<ModRequest> mods;
   std::vector<QuadRequest> quads;
   BufPool pool;
@@ -408,6 +426,11 @@ void noise_real(Context &ctx, int level, void *out);
 // particles.cu
 double velocity_to_offset_ratio(const Cosmo &c);
 void make_particles(Context &ctx, Level &L, int order = 1);
+// the descriptors of the noise streams of (seed, mode) for the context's levels, in the
+// layout a deferred draw was captured with, copied to the device on the context's stream
+void upload_noise_streams(Context &ctx, unsigned long long seed, int mode);
+// after a deferred draw: whether a stream ran short of raw numbers (the draw must be redone)
+bool noise_underrun(Context &ctx);
 // particles of a virtual grid over L's region: factor > 1 supersampled, < -1 subsampled
 void resampled_particles(Context &ctx, const Level &L, int factor, double *host_pos, double *host_vel);
 // particles of listed cells of a zoom level's resolution-matching grid (strays)

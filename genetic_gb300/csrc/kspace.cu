@@ -167,9 +167,13 @@ __global__ void k_za_fields(const typename V2<T>::type *noise, const T *tab, int
 // Second derivatives of the potential (nabla^2 phi = delta): phi_ab = k_a k_b delta / k^2
 // for ab = xx, yy, zz, xy, xz, yz, delta = src * tab[q]; zero at k = 0, and the
 // mixed ones where either component is the Nyquist mode.
+template <typename C>
+struct SixFields {
+  C *p[6];
+};
 template <typename T>
 __global__ void k_hessian_fields(const typename V2<T>::type *src, const T *tab, int n, T kmin,
-                                 typename V2<T>::type *const *out) {
+                                 SixFields<typename V2<T>::type> out) {
   using C = typename V2<T>::type;
   const int H = n / 2, S = H + 1;
   unsigned row;
@@ -192,7 +196,7 @@ __global__ void k_hessian_fields(const typename V2<T>::type *src, const T *tab, 
     C o;
     o.x = w.x * m;
     o.y = w.y * m;
-    out[c][id] = o;
+    out.p[c][id] = o;
   }
 }
 
@@ -558,24 +562,24 @@ static void lpt2_typed(Context &ctx) {
   const int nl = (int)ctx.levels.size();
   std::vector<std::vector<std::unique_ptr<DevBuf>>> hess(nl);
   std::vector<std::unique_ptr<DevBuf>> source(nl);
-  DevBuf ptrs, tab, tabt;
+  // the psi2 multiplier tables are kept by the context: nothing is allocated or freed
+  // per call once they have grown (a batch captures this in a CUDA graph that holds
+  // the pointers)
+  DevBuf &tab = ctx.lpt2_tab, &tabt = ctx.lpt2_tabt;
   // combined Hessian and the source S of every level
   for (int li = 0; li < nl; ++li) {
     Level &L = *ctx.levels[li];
     const size_t bytes = L.ncomplex() * sizeof(C);
     const double scale = 1.0 / std::pow((double)L.n, 1.5);
     build_level_tables(ctx, li);
-    C *hp[6];
+    SixFields<C> hp{};
     for (int c = 0; c < 6; ++c) {
       hess[li].push_back(ctx.pool.take(bytes));
-      hp[c] = hess[li][c]->as<C>();
+      hp.p[c] = hess[li][c]->as<C>();
     }
-    ptrs.ensure(sizeof(hp));
-    GIC_CUDA(cudaMemcpyAsync(ptrs.ptr, hp, sizeof(hp), cudaMemcpyHostToDevice, ctx.stream));
     k_hessian_fields<T><<<hs_grid(L.n), hs_block(), 0, ctx.stream>>>(L.noise.as<C>(), tab_main<T>(L), L.n,
-                                                                     (T)L.kmin(), ptrs.as<C *>());
+                                                                     (T)L.kmin(), hp);
     launched();
-    GIC_CUDA(cudaStreamSynchronize(ctx.stream));  // ptrs is reused
     T *real[6];
     for (int c = 0; c < 6; ++c) {
       real[c] = hess[li][c]->as<T>();
@@ -625,7 +629,7 @@ static void lpt2_typed(Context &ctx) {
     }
     L.have_lpt2 = true;
   }
-  GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+  if (!ctx.defer_checks) GIC_CUDA(cudaStreamSynchronize(ctx.stream));
   for (auto &b : source) ctx.pool.give(std::move(b));
 }
 

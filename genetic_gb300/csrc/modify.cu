@@ -128,13 +128,14 @@ struct AxpySources {
   T c[kMaxAxpy];  // rounded to the field precision on the host (a per-element double->float
                   // conversion would occupy the FP64 pipe)
   int nb;
+  const T *cdev;  // or, when set, the coefficients in device memory (already rounded)
 };
 template <typename T>
 __global__ void k_axpy_multi(T *a, AxpySources<T> src, size_t n) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   T v = a[i];
-  for (int k = 0; k < src.nb; ++k) v += src.c[k] * src.b[k][i];
+  for (int k = 0; k < src.nb; ++k) v += (src.cdev ? src.cdev[k] : src.c[k]) * src.b[k][i];
   a[i] = v;
 }
 // the same with NB sources known at compile time and 16-byte vectors (4 floats or 2
@@ -157,10 +158,60 @@ __global__ void k_axpy_multi_vec(T *a, AxpySources<T> src, size_t nvec) {
 #pragma unroll
   for (int k = 0; k < NB; ++k) {
     const T *pb = reinterpret_cast<const T *>(&b[k]);
+    const T ck = src.cdev ? src.cdev[k] : src.c[k];
 #pragma unroll
-    for (int w = 0; w < W; ++w) pv[w] += src.c[k] * pb[w];
+    for (int w = 0; w < W; ++w) pv[w] += ck * pb[w];
   }
   reinterpret_cast<V *>(a)[i] = v;
+}
+
+// Gram-Schmidt of n covectors through their Gram matrix, in the order of
+// modificationmanager.hpp:288-312, and the correction's coefficients on the covectors
+// converted to vectors (applyLinearModif, :199-217), as the host form in apply_mods:
+// one thread, so that a realisation needs no host round trip (a batch captures it in a
+// CUDA graph).  M: n x (n + 1) doubles, M[i][0] = <a_i|W>, M[i][1 + j] = <a_i|C a_j>.
+constexpr int kDevGramMax = 16;
+struct GramTargets {
+  int n;
+  double t[kDevGramMax];
+};
+template <typename T>
+__global__ void k_gram_coefficients(const double *M, GramTargets tg, T *coef) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int n = tg.n;
+  double L[kDevGramMax * kDevGramMax], t[kDevGramMax], c[kDevGramMax];
+  auto G = [&](int i, int j) { return M[(size_t)i * (n + 1) + 1 + j]; };
+  auto ip = [&](const double *x, const double *y) {
+    double s = 0;
+    for (int k = 0; k < n; ++k)
+      for (int m = 0; m < n; ++m) s += x[k] * y[m] * G(k, m);
+    return s;
+  };
+  for (int i = 0; i < n; ++i) {
+    t[i] = tg.t[i];
+    c[i] = 0;
+    for (int k = 0; k < n; ++k) L[i * kDevGramMax + k] = 0;
+  }
+  for (int i = 0; i < n; ++i) {
+    double *li = &L[i * kDevGramMax];
+    li[i] = 1.0;
+    for (int j = 0; j < i; ++j) {
+      const double *lj = &L[j * kDevGramMax];
+      const double r = ip(li, lj);
+      for (int k = 0; k < n; ++k) li[k] -= r * lj[k];
+      t[i] -= r * t[j];
+    }
+    const double nrm = sqrt(ip(li, li));
+    for (int k = 0; k < n; ++k) li[k] /= nrm;
+    t[i] /= nrm;
+  }
+  for (int i = 0; i < n; ++i) {
+    double existing = 0;
+    for (int k = 0; k < n; ++k) existing += L[i * kDevGramMax + k] * M[(size_t)k * (n + 1)];
+    const double d = t[i] - existing;
+    for (int k = 0; k < n; ++k) c[k] += d * L[i * kDevGramMax + k];
+  }
+  for (int k = 0; k < n; ++k) coef[k] = (T)c[k];
 }
 
 // all products <a_i|b_j> (i < na <= 4, j < nb <= 5) of half spectra in one pass over the
@@ -1170,8 +1221,8 @@ struct ModEngine {
   double inner(Field &a, Field &b) { return inner_many({{&a, &b}})[0]; }
 
   // M[i][j] = <A_i|B_j> summed over levels (Fourier), each field read once per level
-  // for every 4 x 5 block of products; one read-back for the whole matrix
-  std::vector<double> inner_block(const std::vector<Field *> &A, const std::vector<Field *> &B) {
+  // for every 4 x 5 block of products, left in device scratch (inner_block reads it back)
+  const double *inner_block_dev(const std::vector<Field *> &A, const std::vector<Field *> &B) {
     // one wave of resident CTAs
     static std::atomic<int> per_sm{0};
     if (per_sm.load() == 0) {
@@ -1190,7 +1241,7 @@ struct ModEngine {
     const int nb_row = per_sm.load() * nsm, blocks_flat = per_sm_flat.load() * nsm;
     const int blocks = std::max(nb_row, blocks_flat);
     const int L = nl(), na = (int)A.size(), nbt = (int)B.size(), np = na * nbt;
-    if (np == 0) return {};
+    if (np == 0) return nullptr;
     const size_t pstride = (size_t)L * blocks;
     S.reduce.ensure((pstride * np + np) * sizeof(double));
     double *part = S.reduce.template as<double>();
@@ -1227,20 +1278,29 @@ struct ModEngine {
         }
     k_sum<<<np, 256, 0, ctx.stream>>>(part, (int)pstride, part + pstride * np);
     launched();
+    return part + pstride * np;
+  }
+  std::vector<double> inner_block(const std::vector<Field *> &A, const std::vector<Field *> &B) {
+    const size_t np = A.size() * B.size();
+    if (np == 0) return {};
+    const double *d = inner_block_dev(A, B);
     std::vector<double> out(np);
-    GIC_CUDA(cudaMemcpyAsync(out.data(), part + pstride * np, np * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+    GIC_CUDA(cudaMemcpyAsync(out.data(), d, np * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
     GIC_CUDA(cudaStreamSynchronize(ctx.stream));
     return out;
   }
 
-  // a += sum_k c[k] b[k] over a level's half spectrum, up to kMaxAxpy sources per pass
-  void axpy_many(T *a, const std::vector<const T *> &b, const std::vector<double> &c, int l) {
+  // a += sum_k c[k] b[k] over a level's half spectrum, up to kMaxAxpy sources per pass;
+  // the coefficients from c (host) or, when cdev is set, from device memory
+  void axpy_many(T *a, const std::vector<const T *> &b, const std::vector<double> &c, int l,
+                 const T *cdev = nullptr) {
     for (size_t k0 = 0; k0 < b.size(); k0 += kMaxAxpy) {
       AxpySources<T> src{};
       src.nb = (int)std::min<size_t>(kMaxAxpy, b.size() - k0);
+      src.cdev = cdev ? cdev + k0 : nullptr;
       for (int k = 0; k < src.nb; ++k) {
         src.b[k] = b[k0 + k];
-        src.c[k] = (T)c[k0 + k];
+        src.c[k] = cdev ? (T)0 : (T)c[k0 + k];
       }
       constexpr int W = Vec16<T>::W;
       const size_t n = elems(l);
@@ -2442,6 +2502,25 @@ static void apply_mods(Context &ctx, double *chi2_before, double *chi2_after) {
   std::vector<F *> As, Bs{&W};
   for (int i = 0; i < n; ++i) As.push_back(&alpha[i]);
   for (int j = 0; j < n; ++j) Bs.push_back(&vec[j]);
+  if (ctx.quads.empty() && n <= kDevGramMax) {
+    // the Gram block stays on the device; one thread forms the coefficients, and the
+    // correction reads them there: no host round trip
+    const double *Md = E.inner_block_dev(As, Bs);
+    if (n > 0) {
+      GramTargets tg{};
+      tg.n = n;
+      for (int i = 0; i < n; ++i) tg.t[i] = t[i];
+      E.S.gram.ensure(kDevGramMax * sizeof(T));
+      k_gram_coefficients<T><<<1, 1, 0, ctx.stream>>>(Md, tg, E.S.gram.template as<T>());
+      launched();
+      const std::vector<double> none(n, 0.0);
+      for (int l = 0; l < E.nl(); ++l) {
+        std::vector<const T *> srcs;
+        for (int k = 0; k < n; ++k) srcs.push_back(E.ptr(vec[k], l));
+        E.axpy_many(E.ptr(W, l), srcs, none, l, E.S.gram.template as<T>());
+      }
+    }
+  } else {
   std::vector<double> M = E.inner_block(As, Bs);  // M[i][0] = <a_i|W>, M[i][1 + j] = G_ij
   std::vector<double> b(n), G((size_t)n * n);
   for (int i = 0; i < n; ++i) {
@@ -2498,8 +2577,9 @@ static void apply_mods(Context &ctx, double *chi2_before, double *chi2_after) {
     for (auto &q : ctx.quads) apply_quadratic<T>(E, W, lin, q);
   }
   }
+  }
   for (int l = 0; l < E.nl(); ++l) E.lev(l).have_fields = E.lev(l).have_lpt2 = false;
-  GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+  if (!ctx.defer_checks) GIC_CUDA(cudaStreamSynchronize(ctx.stream));
   if (chi2_after) *chi2_after = chi2_of_noise<T>(ctx);
 }
 

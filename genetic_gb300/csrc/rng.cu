@@ -689,12 +689,16 @@ unsigned long long raw_needed(unsigned long long g) {
 
 }  // namespace
 
-// Generate `streams` gaussians into ctx.rng.gauss (layout given by gauss_off).
-static void generate_gaussians(Context &ctx, std::vector<Stream> &streams, unsigned long long total_gauss,
-                               double margin) {
-  cudaStream_t cs = ctx.stream;
-  int ns = (int)streams.size();
-  unsigned long long raw_total = 0, seg_total = 0, chunk_total = 0, max_chunks = 0, blk_total = 0;
+struct StreamTotals {
+  unsigned long long raw = 0, seg = 0, chunk = 0, max_chunks = 0, blk = 0;
+};
+
+// raw-number, segment, chunk and block ranges of every stream (a function of the
+// gaussian counts and the margin only, not of the seeds)
+static StreamTotals layout_streams(std::vector<Stream> &streams, double margin) {
+  StreamTotals t;
+  unsigned long long &raw_total = t.raw, &seg_total = t.seg, &chunk_total = t.chunk, &max_chunks = t.max_chunks,
+                     &blk_total = t.blk;
   for (auto &s : streams) {
     s.raw_off = raw_total;
     s.raw_count = (unsigned long long)(raw_needed(s.gauss_count) * margin);
@@ -712,6 +716,19 @@ static void generate_gaussians(Context &ctx, std::vector<Stream> &streams, unsig
     chunk_total += s.nchunk;
     max_chunks = std::max<unsigned long long>(max_chunks, s.nchunk);
   }
+  return t;
+}
+
+// Generate `streams` gaussians into ctx.rng.gauss (layout given by gauss_off).  With
+// ctx.defer_checks the descriptors are not uploaded (upload_noise_streams did) and the
+// underrun flag is left on the device (noise_underrun reads it).
+static void generate_gaussians(Context &ctx, std::vector<Stream> &streams, unsigned long long total_gauss,
+                               double margin) {
+  cudaStream_t cs = ctx.stream;
+  int ns = (int)streams.size();
+  const StreamTotals tot = layout_streams(streams, margin);
+  const unsigned long long raw_total = tot.raw, seg_total = tot.seg, chunk_total = tot.chunk,
+                           max_chunks = tot.max_chunks, blk_total = tot.blk;
   RngScratch &R = ctx.rng;
   R.raw.ensure(raw_total * sizeof(uint32_t));
   R.gauss.ensure(total_gauss * sizeof(double));
@@ -747,7 +764,8 @@ static void generate_gaussians(Context &ctx, std::vector<Stream> &streams, unsig
   }
 
   Stream *dst = R.streams.as<Stream>();
-  GIC_CUDA(cudaMemcpyAsync(dst, streams.data(), streams.size() * sizeof(Stream), cudaMemcpyHostToDevice, cs));
+  if (!ctx.defer_checks)
+    GIC_CUDA(cudaMemcpyAsync(dst, streams.data(), streams.size() * sizeof(Stream), cudaMemcpyHostToDevice, cs));
   GIC_CUDA(cudaMemsetAsync(R.flags.ptr, 0, sizeof(int) * 4, cs));
   k_seed<<<(ns + 127) / 128, 128, 0, cs>>>(dst, ns);
   launched();
@@ -779,6 +797,7 @@ static void generate_gaussians(Context &ctx, std::vector<Stream> &streams, unsig
       R.gauss.as<double>(), R.flags.as<int>(), q);
   k_tail_values<<<(tail_cap + 255) / 256, 256, 0, cs>>>(q);
   launched(2);
+  if (ctx.defer_checks) return;
   int flag = 0;
   GIC_CUDA(cudaMemcpyAsync(&flag, R.flags.ptr, sizeof(int), cudaMemcpyDeviceToHost, cs));
   GIC_CUDA(cudaStreamSynchronize(cs));
@@ -825,10 +844,14 @@ static void place_level(Context &ctx, Level &L, const double *gauss, int mode) {
 // serial and real-space modes keep consuming one stream across levels, the
 // parallel mode reseeds every shell with seed + ks on every level, so all
 // levels share the shell streams of the largest one.
-template <typename T>
-static void draw_all_typed(Context &ctx, unsigned long long seed, int mode) {
+// The streams genetIC draws the levels' noise from: per shell seed + ks in the parallel
+// mode (every level reseeds each shell), one stream of `seed` across the levels otherwise.
+// offset: each level's first gaussian; total: the gaussians drawn.
+static std::vector<Stream> noise_streams(const Context &ctx, unsigned long long seed, int mode,
+                                         std::vector<unsigned long long> &offset, unsigned long long &total) {
   std::vector<Stream> streams;
-  std::vector<unsigned long long> offset(ctx.levels.size(), 0);
+  offset.assign(ctx.levels.size(), 0);
+  total = 0;
   if (mode == GIC_SEED_FOURIER_PARALLEL) {
     int half = 0;
     for (auto &L : ctx.levels) half = std::max(half, L->n / 2);
@@ -839,9 +862,8 @@ static void draw_all_typed(Context &ctx, unsigned long long seed, int mode) {
       s.gauss_count = 2 * (shell_offset(ks + 1) - shell_offset(ks));
       streams.push_back(s);
     }
-    if (!streams.empty()) generate_gaussians(ctx, streams, 2 * shell_offset(half), 1.0);
+    if (!streams.empty()) total = 2 * shell_offset(half);
   } else {
-    unsigned long long total = 0;
     for (size_t l = 0; l < ctx.levels.size(); ++l) {
       offset[l] = total;
       const Level &L = *ctx.levels[l];
@@ -851,9 +873,17 @@ static void draw_all_typed(Context &ctx, unsigned long long seed, int mode) {
     s.seed = seed;
     s.gauss_off = 0;
     s.gauss_count = total;
-    streams.push_back(s);
-    if (total > 0) generate_gaussians(ctx, streams, total, 1.0);
+    if (total > 0) streams.push_back(s);
   }
+  return streams;
+}
+
+template <typename T>
+static void draw_all_typed(Context &ctx, unsigned long long seed, int mode) {
+  std::vector<unsigned long long> offset;
+  unsigned long long total = 0;
+  std::vector<Stream> streams = noise_streams(ctx, seed, mode, offset, total);
+  if (!streams.empty()) generate_gaussians(ctx, streams, total, 1.0);
   for (size_t l = 0; l < ctx.levels.size(); ++l) {
     Level &L = *ctx.levels[l];
     if (mode == GIC_SEED_FOURIER_PARALLEL) {
@@ -872,7 +902,28 @@ static void draw_all_typed(Context &ctx, unsigned long long seed, int mode) {
     }
     place_level<T>(ctx, L, ctx.rng.gauss.as<double>() + offset[l], mode);
   }
+  if (!ctx.defer_checks) GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+}
+
+void upload_noise_streams(Context &ctx, unsigned long long seed, int mode) {
+  std::vector<unsigned long long> offset;
+  unsigned long long total = 0;
+  std::vector<Stream> streams = noise_streams(ctx, seed, mode, offset, total);
+  if (streams.empty()) return;
+  layout_streams(streams, 1.0);
+  if (ctx.rng.streams.bytes < streams.size() * sizeof(Stream))
+    fail(GIC_ERR_INTERNAL, "the noise streams were not laid out by an earlier draw");
+  GIC_CUDA(cudaMemcpyAsync(ctx.rng.streams.ptr, streams.data(), streams.size() * sizeof(Stream), cudaMemcpyHostToDevice,
+                           ctx.stream));
+  GIC_CUDA(cudaStreamSynchronize(ctx.stream));  // the host vector goes out of scope
+}
+
+bool noise_underrun(Context &ctx) {
+  if (!ctx.rng.flags.ptr) return false;
+  int flag = 0;
+  GIC_CUDA(cudaMemcpyAsync(&flag, ctx.rng.flags.ptr, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
   GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+  return flag != 0;
 }
 
 void gaussian_stream(Context &ctx, unsigned long long seed, size_t n, double *host) {

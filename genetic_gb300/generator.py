@@ -627,7 +627,9 @@ class ICGenerator:
         """Particles of `level` on genetIC's supersampled (factor >= 2) or subsampled
         (factor <= -2) virtual grid of the same region: (positions, velocities)."""
         n = self.levels[level][1]
-        nv = n * factor if factor > 0 else n // -factor
+        # sizes the library refuses get a one-particle buffer: the call reports the error
+        nv = n * factor if factor > 1 else (n // -factor if factor < -1 else 1)
+        nv = nv if nv <= 2048 else 1
         pos = np.empty((nv ** 3, 3), dtype=np.float64)
         vel = np.empty((nv ** 3, 3), dtype=np.float64)
         self._call('gic_fetch_particles_resampled', level, int(factor), _ptr(pos), _ptr(vel))

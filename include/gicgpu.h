@@ -382,13 +382,16 @@ GIC_API int gic_gaussian_stream_noalloc(unsigned long seed, size_t n, double *de
 
 /* ---- Batches of independent realisations on one GPU (no genetIC counterpart) ----
  * A batch groups contexts of one device (any sizes, levels and modifications).
- * gic_batch_realise draws every context's white noise (seeds[i], seeding mode
- * modes[i], or the parallel Fourier mode when modes is NULL) and applies its
- * queued modifications from `threads` host threads, each context on its own
- * stream; then it runs every context's field maps and particles (order 1 or 2).
- * For order 1 those maps run as one CUDA graph over all contexts, captured on the
- * first call and replayed while the contexts' buffers stay the same.  Returns
- * when all realisations are complete; results are then read per context. */
+ * gic_batch_realise realises every context: white noise (seeds[i], seeding mode
+ * modes[i], or the parallel Fourier mode when modes is NULL), its queued
+ * modifications, fields and particles (order 1 or 2), each context on its own
+ * stream.  Contexts whose modifications are all linear (at most 16) are realised
+ * by one CUDA graph over all of them, captured on the first call (after an eager
+ * realisation) and replayed on later calls while the contexts' buffers, seeding
+ * modes, order and modification targets stay the same; it is captured again when
+ * any changed.  Contexts with a variance modification are realised from `threads`
+ * host threads beside it.  Returns when all realisations are complete; results
+ * are then read per context. */
 typedef struct gic_batch gic_batch;
 GIC_API int gic_batch_create(gic_batch **out, gic_ctx *const *ctxs, int n);
 GIC_API int gic_batch_destroy(gic_batch *batch);
@@ -397,6 +400,11 @@ GIC_API const char *gic_batch_last_error(const gic_batch *batch);
 /* The stream a batch's graph runs on; every realisation of gic_batch_realise is
  * ordered between work queued on it before the call and work queued after. */
 GIC_API int gic_batch_get_stream(gic_batch *batch, void **stream);
+/* The batch's graph: the contexts it realises, the kernels of one replay, the
+ * replays since it was captured, and (empty unless) why the batch stopped
+ * capturing.  Any pointer may be NULL. */
+GIC_API int gic_batch_graph_info(const gic_batch *batch, int *contexts, unsigned long long *kernels, int *replays,
+                                 const char **off_reason);
 
 /* Number of kernels this library has launched in the process so far. */
 GIC_API int gic_launch_count(unsigned long long *count);

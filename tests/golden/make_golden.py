@@ -617,6 +617,43 @@ def strays_goldens():
                             nrec=np.int64(len(dark)), stride=np.int64(7), every=dark[::7].copy(), tail=dark[-400:].copy())
 
 
+# The batch workload's zoom class at 64^3: a 100 Mpc/h base of 64 cells and a zoom of a quarter
+# of its side (zoom factor 4) with 32 cells, so the zoom cells are half the base cells (ratio 2,
+# fewer zoom cells than the window's base cells x 4), centred at (50, 50, 50); overdensity +1.0
+# in a 1.5 Mpc/h sphere at the centre and -0.5 in a 3 Mpc/h sphere 5 Mpc/h along x.
+RATIO2 = """centre 50 50 50
+select_cube 10
+zoom_grid_with_origin_at 24 24 24 4 32
+centre 50 50 50
+select_sphere 1.5
+calculate overdensity
+modify overdensity absolute 1.0
+centre 55 50 50
+select_sphere 3
+calculate overdensity
+modify overdensity absolute -0.5
+done
+dump_grid 0
+dump_grid 1
+"""
+
+
+def ratio2_golden():
+    """Reference-build grids, the two logged overdensities and the chi^2 change of RATIO2."""
+    import re
+    with tempfile.TemporaryDirectory() as d:
+        write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+        open(os.path.join(d, 'paramfile.txt'), 'w').write(MOD_BASE.replace('basegrid 50.0 32', 'basegrid 100.0 64') +
+                                                           RATIO2)
+        r = subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True, text=True)
+        log = r.stdout + r.stderr
+        values = [float(v) for v in re.findall(r'overdensity: calculated value = (\S+)', log)]
+        dchi2 = float(re.search(r'Modification Delta chi\^2 = (\S+)', log).group(1))
+        grids = {'delta%d' % l: np.load(os.path.join(d, 'grid-%d.npy' % l)) for l in range(2)}
+        np.savez_compressed(os.path.join(HERE, 'geom_ratio2.npz'), **grids, overdensity=np.array(values),
+                            delta_chi2=np.array(dchi2))
+
+
 def main():
     for mode, cmd in (('serial', 'random_seed_serial'), ('parallel', 'random_seed'), ('real', 'random_seed_real_space')):
         with tempfile.TemporaryDirectory() as d:
@@ -639,6 +676,7 @@ if __name__ == '__main__':
         sys.exit(0)
     main()
     geometry_goldens()
+    ratio2_golden()
     resample_goldens()
     strays_goldens()
     zoom_goldens()

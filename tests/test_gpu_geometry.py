@@ -4,7 +4,9 @@ Zoom factor 4 (the ratio-4 block means, interpolation and deinterpolation the he
 runs), factor 3 over an integer number of coarse cells (the generic-ratio block means),
 and factor 3 over a fractional number of them (genetIC's test_01c geometry), with the
 headline's four modifications (mean overdensity +1.5 and mean velocities 0 in a 2 Mpc/h
-sphere at the zoom centre) and the differentiation configuration's variance modification.
+sphere at the zoom centre) and the differentiation configuration's variance modification;
+and the batch workload's zoom class (zoom factor 4 with half as many zoom cells: cell
+ratio 2) with its two overdensity modifications.
 The oracle reproduces the reference build's grids of these cases to 1e-11
 (tests/golden/geom_*.npz, test_oracle.py).  FP64: 1e-10 relative; mixed: 1e-5.
 """
@@ -15,7 +17,8 @@ import pytest
 
 import field_oracle as fo
 from conftest import COSMO, make_generator
-from test_oracle import GEOM_LEVELS, MOD_CASES, VAR_CASES, oracle_modified, oracle_variance
+from test_oracle import (GEOM_LEVELS, MOD_CASES, RATIO2_LEVELS, RATIO2_MODS, VAR_CASES, oracle_modified,
+                         oracle_ratio2, oracle_variance)
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), 'golden')
@@ -190,3 +193,30 @@ def test_geometry_variance_mixed(built, bbks, variance4):
     for l, w2 in enumerate(want['modified']):
         assert np.abs(got['noise'][l] - w2).max() < 1e-5 * np.abs(w2).max(), l
     assert abs(got['final'] / want['final'] - 1) < 1e-5
+
+
+RATIO2_GPU = [('base', 100.0, 64), ('zoom', 24, 24, 24, 4, 32)]
+
+
+@pytest.mark.parametrize('precision,tol', [('fp64', 1e-10), ('mixed', 1e-5)])
+def test_ratio2_zoom_with_modifications(built, bbks, precision, tol):
+    want = oracle_ratio2(bbks, cr_log=True)
+    gen = make_generator(precision, bbks, RATIO2_GPU, 8896131, 'random_seed')
+    values = []
+    for centre, radius, target in RATIO2_MODS:
+        gen.centre(*centre)
+        gen.select_sphere(radius)
+        values.append(gen.calculate('overdensity'))
+        gen.modify('overdensity', 'absolute', target)
+    chi2 = gen.apply_modifications()
+    fields, parts = _realise(gen, 2)
+    gen.close()
+    for v, w in zip(values, want['values']):
+        assert abs(v - w) <= tol * max(abs(w), 1e-3)
+    d_got, d_want = chi2[1] - chi2[0], want['chi2'][1] - want['chi2'][0]
+    assert abs(d_got - d_want) < 10 * tol * abs(d_want)
+    ref = fo.zoom_realisation(want['modified'], RATIO2_LEVELS, fo.CambPower(bbks, COSMO))
+    _check_fields(fields, parts, ref, RATIO2_LEVELS, tol)
+    g = np.load(os.path.join(GOLDEN, 'geom_ratio2.npz'))
+    for l in range(2):
+        assert _rel(fields[l]['delta'], g['delta%d' % l]) < tol, l

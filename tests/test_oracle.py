@@ -490,6 +490,43 @@ def test_geometry_modification_oracle_matches_reference(bbks, case):
         assert np.abs(out[l][0] - ref).max() <= 1e-11 * np.abs(ref).max(), l
 
 
+# The batch workload's zoom class at 64^3 (tests/golden/geom_ratio2.npz): a zoom of a quarter of
+# a 100 Mpc/h base's side (zoom factor 4) with 32 cells, half the base's cell size, and two
+# overdensity modifications on different spheres
+RATIO2_LEVELS = [(100.0, 64, (0.0, 0.0, 0.0)), (25.0, 32, (37.5, 37.5, 37.5))]
+RATIO2_MODS = [((50.0, 50.0, 50.0), 1.5, 1.0), ((55.0, 50.0, 50.0), 3.0, -0.5)]
+
+
+def oracle_ratio2(bbks, cr_log=False):
+    from conftest import COSMO
+    L = fo.Levels(RATIO2_LEVELS)
+    fo.set_cr_log(cr_log)
+    w = fo.white_noise_levels([64, 32], 8896131, 2)
+    fo.set_cr_log(False)
+    p_dm = fo.CambPower(bbks, COSMO, column=1)
+    covs, values = [], []
+    for centre, radius, _ in RATIO2_MODS:
+        flagged = fo.flag_cells(L, 1, centre, 'sphere', radius)
+        cv = fo.multilevel_covector(L, fo.localisation_covector(L, flagged, 'overdensity', 0), p_dm, None)
+        values.append(fo.inner(cv, w))
+        covs.append(cv)
+    before = fo.chi2_levels(L, w)
+    w2 = fo.apply_linear_modifications(L, w, covs, [t for _, _, t in RATIO2_MODS])
+    return dict(values=values, chi2=(before, fo.chi2_levels(L, w2)), modified=w2)
+
+
+def test_ratio2_zoom_oracle_matches_reference(bbks):
+    from conftest import COSMO
+    g = _load_golden('geom_ratio2.npz')
+    r = oracle_ratio2(bbks)
+    assert ['%.6g' % v for v in r['values']] == ['%.6g' % v for v in g['overdensity']]
+    assert '%.6g' % (r['chi2'][1] - r['chi2'][0]) == '%.6g' % float(g['delta_chi2'])
+    out = fo.zoom_realisation(r['modified'], RATIO2_LEVELS, fo.CambPower(bbks, COSMO))
+    for l in range(2):
+        ref = g['delta%d' % l]
+        assert np.abs(out[l][0] - ref).max() <= 1e-11 * np.abs(ref).max(), l
+
+
 def test_geometry_variance_oracle_matches_reference(bbks):
     from conftest import COSMO
     g = _load_golden('geom_var4.npz')
