@@ -2,6 +2,7 @@
 // runs on the context's CUDA stream, synchronises before returning and turns
 // every failure into a status code plus a message.
 #include "gic_internal.h"
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -573,7 +574,10 @@ static gic::ModRequest make_request(gic::Context &C, int kind, const unsigned lo
     if (cells[i] >= m) gic::fail(GIC_ERR_INVALID_ARG, "flagged cell outside the finest grid");
   gic::ModRequest r;
   r.kind = kind;
+  // genetIC keeps its flagged cells sorted and unique; the covectors follow that order
   r.cells.assign(cells, cells + n);
+  std::sort(r.cells.begin(), r.cells.end());
+  r.cells.erase(std::unique(r.cells.begin(), r.cells.end()), r.cells.end());
   r.target = 0;
   return r;
 }

@@ -16,6 +16,7 @@
 // Twiddles are computed in long double on the host once per size and stored
 // in the working precision.
 #include "gic_internal.h"
+#include <cuda.h>
 #include <cmath>
 #include <algorithm>
 #include <atomic>
@@ -1049,6 +1050,202 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_fft_planes(typename Cx<T>::ty
   }
 }
 
+
+// ---- TMA-staged strided pass (persistent) ------------------------------------------
+// Each CTA walks its share of the column tiles with a ring of two shared-memory slots
+// filled by bulk tensor copies (cp.async.bulk.tensor, completion counted on an mbarrier
+// per slot).  The threads read a tile's first-stage inputs from its slot and, once all
+// of them have, one thread issues the copy of the tile two ahead into that slot; the
+// tile's remaining Stockham stages run in an exchange tile meanwhile, and the last
+// stage stores straight to HBM.  So a copy is always in flight behind the arithmetic.
+// Twiddles are copied to shared memory once per CTA.  The arithmetic (radix schedule,
+// twiddle indices, explicit fused multiply-adds) is the fused pass's: the same bits.
+// Plain passes and inverse passes with a store window (EXT) only: with one 16-warp CTA
+// per SM the per-|k|^2 table gathers of the x passes' multipliers and epilogues are
+// latency-bound here (measured 2-4x slower), so those passes stay with the fused pass.
+//
+// Tile layouts in a slot, matching the tensor map the host builds:
+//   rows  (PAIRS = false): rows of B complex whose byte stride is a multiple of 16 (the
+//         x pass, and the y pass in FP64): boxes (TC, <= 256 rows) of one plane, slot [L][TC];
+//   pairs (PAIRS = true): FP32 rows of odd length B (the y pass; a row is not 16-byte
+//         aligned): two rows seen as one of 2B, a box of TC + 2 values for the even rows
+//         at column b0 and one for the odd rows at B - 1 + b0 (16-byte aligned starts),
+//         slot [2][L/2][TC + 2], odd rows' values one place in.
+// A wait for a copy is bounded (about a second of clock cycles); one that gives up sets
+// *err (the FFT wait flag the host reads) and the CTA stops after the copies it issued
+// have landed (again bounded).
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *b, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// waits for the phase of the given parity to complete; false after `cycles` clocks
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *b, unsigned parity, long long cycles) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(b, parity))
+    if (clock64() - t0 > cycles) return false;
+  return true;
+}
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+          smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+template <typename T>
+struct TmaColsArgs {
+  typename Cx<T>::type *data;  // the array (A planes of L x B complex)
+  long long B;
+  int A, a0, ntb, ntiles;      // planes (a0 + i) mod A; ntb column tiles per plane
+  const typename Cx<T>::type *tw;
+  T scale;
+  int sm0, smn;                // inverse: positions (sm0 + i) mod L, i < smn, stored
+  int *err;
+  long long wait_cycles;
+};
+
+template <int L, int TC, bool PAIRS>
+struct TmaColsShape {
+  static constexpr int SLOT = PAIRS ? L * (TC + 2) : L * TC;  // complex values per slot
+  static constexpr int ROWS = PAIRS ? L / 2 : L;              // rows of the tensor per tile
+  static constexpr int BOXR = ROWS < 256 ? ROWS : 256;       // rows per bulk copy
+  static constexpr int W = PAIRS ? TC + 2 : TC;              // values per row of a box
+};
+
+template <typename T, int L, int TC, int NCW, int SIGN, bool EXT, bool PAIRS>
+__global__ void __launch_bounds__(NCW * 32, L >= 512 ? 1 : 2) k_fft_cols_tma(const __grid_constant__ CUtensorMap map,
+                                                                            const TmaColsArgs<T> a) {
+  using C = typename Cx<T>::type;
+  using SH = TmaColsShape<L, TC, PAIRS>;
+  constexpr int NC = NCW * 32, SLOT = SH::SLOT, NBOX = SH::ROWS / SH::BOXR;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const unsigned pad = (1024u - (smem_u32(smraw) & 1023u)) & 1023u;  // bulk-copy destinations: 1024-byte aligned
+  C *slots = reinterpret_cast<C *>(smraw + pad);
+  C *xt = slots + 2 * SLOT;
+  C *stw = xt + L * TC;
+  uint64_t *full = reinterpret_cast<uint64_t *>(stw + L);
+  __shared__ int s_stop;
+  const int ct = threadIdx.x;
+  const int nt = (int)gridDim.x, mine = a.ntiles > (int)blockIdx.x ? (a.ntiles - (int)blockIdx.x + nt - 1) / nt : 0;
+  // the copy of this CTA's k-th tile into slot k & 1 (one thread)
+  auto issue = [&](int k) {
+    const int s = k & 1;
+    const int t = (int)blockIdx.x + k * nt;
+    const int plane = (a.a0 + t / a.ntb) % a.A, b0 = (t % a.ntb) * TC;
+    mbar_expect_tx(&full[s], SLOT * (unsigned)sizeof(C));
+    C *dst = slots + s * SLOT;
+    // tensor coordinates count scalars (two per complex value) along the rows
+#pragma unroll
+    for (int r = 0; r < NBOX; ++r) {
+      tma_load_3d(dst + r * SH::BOXR * SH::W, &map, 2 * b0, r * SH::BOXR, plane, &full[s]);
+      if (PAIRS)
+        tma_load_3d(dst + (SH::ROWS + r * SH::BOXR) * SH::W, &map, (int)(2 * (a.B - 1 + b0)), r * SH::BOXR, plane,
+                    &full[s]);
+    }
+  };
+  if (ct == 0) {
+    mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
+    s_stop = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if (mine > 0) issue(0);
+    if (mine > 1) issue(1);
+  }
+  for (int i = ct; i < L; i += NC) stw[i] = a.tw[i];
+  __syncthreads();
+  constexpr int R = next_radix(L, 1), LR = L / R, NB = LR * TC, PER = (NB + NC - 1) / NC;
+  constexpr int NSL = last_stage_ns(L), RL = L / NSL, LRL = L / RL, NBL = LRL * TC, PERL = (NBL + NC - 1) / NC;
+  for (int k = 0; k < mine; ++k) {
+    const int s = k & 1;
+    const unsigned ph = (unsigned)(k >> 1) & 1u;
+    if (ct == 0 && !mbar_wait_bounded(&full[s], ph, a.wait_cycles)) {
+      s_stop = 1;
+      atomicExch(a.err, 3);
+      // the copies issued and not yet waited for: this tile's and, if issued, the next one's
+      if (k + 1 < mine) mbar_wait_bounded(&full[s ^ 1], ((unsigned)((k + 1) >> 1)) & 1u, a.wait_cycles);
+      mbar_wait_bounded(&full[s], ph, a.wait_cycles);
+    }
+    // also orders this tile's exchange-tile writes after the last tile's final reads
+    __syncthreads();
+    if (s_stop) return;
+    const int t = (int)blockIdx.x + k * nt;
+    const int plane = (a.a0 + t / a.ntb) % a.A;
+    const long long b0 = (long long)(t % a.ntb) * TC;
+    const int tcv = (int)min((long long)TC, a.B - b0);
+    const size_t off = (size_t)plane * (size_t)L * (size_t)a.B + (size_t)b0;
+    const C *in = slots + s * SLOT;
+    C v[PER][R];
+#pragma unroll
+    for (int p = 0; p < PER; ++p) {
+      const int b = ct + p * NC;
+      if (NB % NC == 0 || b < NB) {
+        const int c = b % TC, j = b / TC;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const int m = j + r * LR;
+          C x;
+          if (PAIRS) x = in[(m & 1) * SH::ROWS * SH::W + (m >> 1) * SH::W + c + (m & 1)];
+          else x = in[m * TC + c];
+          if (c >= tcv) x = czero<C>();
+          v[p][r] = x;
+        }
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < PER; ++p) {
+      const int b = ct + p * NC;
+      if (NB % NC == 0 || b < NB) {
+        const int c = b % TC, j = b / TC;
+        Dft<T, C, R>::run(v[p], SIGN);
+#pragma unroll
+        for (int r = 0; r < R; ++r) xt[(j * R + r) * TC + c] = v[p][r];
+      }
+    }
+    __syncthreads();
+    // every thread has read slot s: refill it with the tile two ahead
+    if (ct == 0 && k + 2 < mine) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(k + 2);
+    }
+    TileStagesUntil<T, L, TC, TC, NC, R, NSL, SIGN, 1>::run(xt, stw);
+    C *base = a.data + off;
+#pragma unroll
+    for (int p = 0; p < PERL; ++p) {
+      const int b = ct + p * NC;
+      if (NBL % NC == 0 || b < NBL) {
+        const int c = b % TC, j = b / TC;
+        C w[RL];
+#pragma unroll
+        for (int r = 0; r < RL; ++r) w[r] = xt[(j + r * LRL) * TC + c];
+#pragma unroll
+        for (int r = 1; r < RL; ++r) w[r] = cmul(w[r], twid(stw, r * j * (L / (NSL * RL)), SIGN));
+        Dft<T, C, RL>::run(w, SIGN);
+        if (c < tcv) {
+#pragma unroll
+          for (int r = 0; r < RL; ++r) {
+            const int m = j + r * NSL;
+            if (EXT && (m - a.sm0 + L) % L >= a.smn) continue;
+            base[(size_t)m * (size_t)a.B + c] = cscale(w[r], a.scale);
+          }
+        }
+      }
+    }
+  }
+}
+
 template <typename T>
 void set_smem(const void *fn, size_t bytes) {
   GIC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
@@ -1056,11 +1253,32 @@ void set_smem(const void *fn, size_t bytes) {
 
 // launchers of the fixed-length passes; candidate tile widths per precision:
 //   strided: (TC, threads) = FP32 (8, 256) | (16, 512) | fused (8, 512) | fused (16, 512),
-//            FP64 (4, 256) | (8, 256) | fused (4, 256) | fused (8, 128)
+//            FP64 (4, 256) | (8, 256) | fused (4, 256) | fused (8, 128);
+//            then fused 8 (FP64: 4) columns with 3 or 4 CTAs per SM, and (256 <= N <= 512)
+//            the TMA-staged pass: 16 (FP64: 8) columns, 16 consumer warps at N = 512, 8 below
 //   rows:    (RPC, threads) = FP32 (8, 256) | (16, 256) | fused (16, 256) | (32, 512),
 //            FP64 (4, 256) | (8, 256) | fused (8, 256) | (16, 512)
 constexpr int kFixedCandidates = 4;  // row-pass candidates
-constexpr int kColsCandidates = 6;   // strided-pass candidates (the last two: fused, 8 columns, 3 or 4 CTAs per SM)
+constexpr int kColsCandidates = 7;   // strided-pass candidates (4, 5: fused, 8 columns, 3 or 4 CTAs per SM; 6: TMA-staged)
+
+// cuTensorMapEncodeTiled, looked up once through the runtime (no link-time dependency on
+// the driver library); null when the driver does not provide it
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled_fn() {
+  static EncodeTiledFn fn = [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return (EncodeTiledFn) nullptr;
+    }
+    return reinterpret_cast<EncodeTiledFn>(f);
+  }();
+  return fn;
+}
 
 // the dynamic shared-memory limit of a kernel, set once per device (any host thread)
 inline void set_smem_once(const void *fn, size_t bytes, std::atomic<int> &done_mask) {
@@ -1150,6 +1368,94 @@ struct FixedFft {
     }
     launched();
   }
+  // the TMA-staged strided pass (k_fft_cols_tma) for 256 <= N <= 512; false where it does
+  // not apply, and the caller runs a fused pass: a forward pass that reads a window of
+  // positions only (the fused pass loads just the window), an x pass with a multiplier,
+  // an out-of-place source or an epilogue, or no tensor-map encoder
+  static constexpr bool kTma = N >= 256 && N <= 512;
+  template <int SIGN, bool EXT, bool PAIRS>
+  static void launch_tma(Context &ctx, const CUtensorMap &map, const TmaColsArgs<T> &args) {
+    constexpr int TC = F32 ? 16 : 8, NCW = N >= 512 ? 16 : 8;
+    using SH = TmaColsShape<N, TC, PAIRS>;
+    const void *fn = (const void *)k_fft_cols_tma<T, N, TC, NCW, SIGN, EXT, PAIRS>;
+    const size_t smem = 1024 + (2 * (size_t)SH::SLOT + (size_t)N * TC + N) * sizeof(C) + 2 * sizeof(uint64_t);
+    static std::atomic<int> mask{0}, resident{0};
+    set_smem_once(fn, smem, mask);
+    if (resident.load() == 0) {
+      int nb = 0;
+      GIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, NCW * 32, smem));
+      resident.store(std::max(nb, 1));
+    }
+    int dev = 0, nsm = 0;
+    GIC_CUDA(cudaGetDevice(&dev));
+    GIC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const int grid = std::min(args.ntiles, resident.load() * nsm);
+    k_fft_cols_tma<T, N, TC, NCW, SIGN, EXT, PAIRS><<<grid, NCW * 32, smem, ctx.stream>>>(map, args);
+    launched();
+  }
+  static bool cols_tma(Context &ctx, int sign, C *d, int A, long long B, const C *tw, T scale, const T *tab, int a0,
+                       int na, int m0, int mn, const C *src, C *dst, const C *xsrc, const T *xtab) {
+    if constexpr (!kTma) {
+      return false;
+    } else {
+      if ((sign < 0 && mn < N) || tab || src || dst || xsrc || xtab) return false;
+      constexpr int TC = F32 ? 16 : 8;
+      const bool pairs = ((size_t)B * sizeof(C)) % 16 != 0;
+      if (pairs && !(F32 && B % 2 == 1)) return false;
+      EncodeTiledFn enc = encode_tiled_fn();
+      if (!enc) return false;
+      if (reinterpret_cast<uintptr_t>(d) % 16) return false;
+      // the tensor: scalars along a row (two per complex value), rows (or row pairs), planes
+      cuuint64_t dims[3], strides[2];
+      cuuint32_t box[3], es[3] = {1, 1, 1};
+      if (!pairs) {
+        dims[0] = (cuuint64_t)(2 * B);
+        dims[1] = (cuuint64_t)N;
+        strides[0] = (cuuint64_t)(B * (long long)sizeof(C));
+        box[0] = 2 * TC;
+        box[1] = (cuuint32_t)std::min(N, 256);
+      } else {
+        dims[0] = (cuuint64_t)(4 * B);
+        dims[1] = (cuuint64_t)(N / 2);
+        strides[0] = (cuuint64_t)(2 * B * (long long)sizeof(C));
+        box[0] = 2 * (TC + 2);
+        box[1] = (cuuint32_t)std::min(N / 2, 256);
+      }
+      dims[2] = (cuuint64_t)A;
+      strides[1] = (cuuint64_t)((long long)N * B * (long long)sizeof(C));
+      box[2] = 1;
+      CUtensorMap map;
+      if (enc(&map, F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, d, dims,
+              strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+      TmaColsArgs<T> args{};
+      args.data = d;
+      args.B = B;
+      args.A = A;
+      args.a0 = a0;
+      args.ntb = (int)((B + TC - 1) / TC);
+      args.ntiles = args.ntb * na;
+      args.tw = tw;
+      args.scale = scale;
+      args.sm0 = m0;
+      args.smn = mn;
+      args.err = ctx.fft.wait_flag();
+      args.wait_cycles = 1ll << 31;
+      if (args.ntiles <= 0) return true;
+      const bool ext = sign > 0 && mn < N;
+      if (pairs) {
+        if constexpr (F32) {
+          if (sign > 0) ext ? launch_tma<+1, true, true>(ctx, map, args) : launch_tma<+1, false, true>(ctx, map, args);
+          else ext ? launch_tma<-1, true, true>(ctx, map, args) : launch_tma<-1, false, true>(ctx, map, args);
+        }
+      } else {
+        if (sign > 0) ext ? launch_tma<+1, true, false>(ctx, map, args) : launch_tma<+1, false, false>(ctx, map, args);
+        else ext ? launch_tma<-1, true, false>(ctx, map, args) : launch_tma<-1, false, false>(ctx, map, args);
+      }
+      return true;
+    }
+  }
   // a0, na: the planes (a0 + i) mod A, i < na, of the strided pass (na < 0: all A);
   // m0, mn: the positions along the transform read (forward) or written (inverse)
   // src: an out-of-place inverse x pass reads the columns other than kz = 0, N/2 from src
@@ -1158,6 +1464,11 @@ struct FixedFft {
                        const T *tab = nullptr, int a0 = 0, int na = -1, int m0 = 0, int mn = N,
                        const C *src = nullptr, C *dst = nullptr, const C *xsrc = nullptr, const T *xtab = nullptr) {
     if (na < 0) na = A;
+    if (cfg == 6) {
+      // TMA-staged, else the fused 16- (FP64: 8-) column pass
+      if (cols_tma(ctx, sign, d, A, B, tw, scale, tab, a0, na, m0, mn, src, dst, xsrc, xtab)) return;
+      cfg = 3;
+    }
     if (cfg == 4) {
       // fused, 8 columns, registers capped for 3 CTAs of 512 threads per SM (48 warps)
       if (sign > 0) cols_fused<F32 ? 8 : 4, 512, +1, 3>(ctx, d, A, B, tw, scale, tab, a0, na, m0, mn, src, dst, xsrc, xtab);
@@ -1284,8 +1595,12 @@ struct FixedFft {
       return ms;
     };
     float bc = 1e30f, br = 1e30f;
+    // a strided candidate is timed on both of its passes (x, then y over every plane)
     for (int c = 0; c < kColsCandidates; ++c) {
-      float t = time_it([&] { cols_cfg(ctx, c, +1, d, 1, (long long)N * S, tw, (T)1); });
+      float t = time_it([&] {
+        cols_cfg(ctx, c, +1, d, 1, (long long)N * S, tw, (T)1);
+        cols_cfg(ctx, c, +1, d, N, S, tw, (T)1);
+      });
       if (t < bc) { bc = t; best_cols = c; }
     }
     for (int r = 0; r < kFixedCandidates; ++r) {
@@ -1498,8 +1813,10 @@ bool fft_prunes(const Context &ctx, int n) {
 bool take_fft_wait_error(Context &ctx) {
   volatile int *f = ctx.fft.wait_flag_host;
   if (!f || *f == 0) return false;
+  ctx.last_error = *f >= 3 ? "FFT TMA-staged strided pass: a wait for a tile's bulk copy gave up; results of the transform "
+                             "are invalid"
+                           : "FFT plane pass: a wait for another CTA's tiles gave up; results of the transform are invalid";
   *f = 0;
-  ctx.last_error = "FFT plane pass: a wait for another CTA's tiles gave up; results of the transform are invalid";
   return true;
 }
 

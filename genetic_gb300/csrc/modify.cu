@@ -628,74 +628,137 @@ __global__ void k_center_cells(T *v, size_t count) {
   for (size_t i = threadIdx.x; i < count; i += blockDim.x) v[i] = (v[i] - m) / c;
 }
 
-// localisation covector on the finest grid (padded real layout)
+// Localisation covectors on the finest grid (padded real layout).  genetIC builds them
+// cell by cell in the order of its sorted flagged-cell list, adding the stencil values
+// into the output (linearmodification.hpp:223-233, 344-374); where stencils overlap, a
+// cell's value is a sum whose rounding depends on that order.  Each kernel here writes
+// every reached cell once, from the thread of the contribution that comes first, as the
+// double sum of all its contributions in the reference's order, so the FP64 covector has
+// the reference's bits (the mixed form rounds that sum once) and nothing depends on
+// thread scheduling.  cells: sorted, unique.
+
+// the list position of cell id, or -1
+__device__ __forceinline__ long long find_flagged(const unsigned long long *cells, size_t count,
+                                                  unsigned long long id) {
+  size_t lo = 0, hi = count;
+  while (lo < hi) {
+    const size_t mid = (lo + hi) / 2;
+    if (cells[mid] < id) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo < count && cells[lo] == id ? (long long)lo : -1;
+}
+// the cell `step` cells from id along axis ax, periodically
+__device__ __forceinline__ unsigned long long step_cell(unsigned long long id, int n, int ax, int step) {
+  int p[3] = {(int)(id / ((unsigned long long)n * n)), (int)((id / n) % n), (int)(id % n)};
+  p[ax] = ((p[ax] + step) % n + n) % n;
+  return ((unsigned long long)p[0] * n + p[1]) * n + p[2];
+}
+__device__ __forceinline__ size_t padded_at(unsigned long long id, int n) {
+  const unsigned long long z = id % n, r = id / n;
+  return (size_t)r * (size_t)(2 * (n / 2 + 1)) + (size_t)z;
+}
+
+// kind 0: w on every flagged cell (OverdensityModification); kind 1: the 4th-order
+// gradient stencil along dir with values a, b, -b, -a at -2, -1, +1, +2 (VelocityModification)
 template <typename T>
 __global__ void k_localise(T *real, int n, const unsigned long long *cells, size_t count, int kind, int dir,
                            double w, double a, double b) {
-  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
-  unsigned long long c = cells[i];
-  int z = (int)(c % n);
-  unsigned long long r = c / n;
-  int y = (int)(r % n), x = (int)(r / n);
-  const size_t rs = (size_t)(2 * (n / 2 + 1));
-  auto at = [&](int dx, int dy, int dz) -> T * {
-    int xx = ((x + dx) % n + n) % n, yy = ((y + dy) % n + n) % n, zz = ((z + dz) % n + n) % n;
-    return real + ((size_t)xx * n + yy) * rs + zz;
-  };
+  const unsigned long long q = cells[i];
   if (kind == 0) {
-    atomicAdd(at(0, 0, 0), (T)w);
+    real[padded_at(q, n)] = (T)w;
     return;
   }
-  int s[3] = {0, 0, 0};
-  s[dir] = 1;
-  atomicAdd(at(-2 * s[0], -2 * s[1], -2 * s[2]), (T)a);
-  atomicAdd(at(-s[0], -s[1], -s[2]), (T)b);
-  atomicAdd(at(s[0], s[1], s[2]), (T)(-b));
-  atomicAdd(at(2 * s[0], 2 * s[1], 2 * s[2]), (T)(-a));
+  const int off[4] = {-2, -1, 1, 2};
+  const double val[4] = {a, b, -b, -a};
+  for (int k = 0; k < 4; ++k) {
+    const unsigned long long t = step_cell(q, n, dir, off[k]);
+    // every contribution to t: the flagged cell -off[k2] away, its stencil value k2
+    long long ci[4];
+    int ck[4], nc = 0;
+    bool first = true;
+    for (int k2 = 0; k2 < 4 && first; ++k2) {
+      const long long i2 = find_flagged(cells, count, step_cell(t, n, dir, -off[k2]));
+      if (i2 < 0) continue;
+      if (i2 < (long long)i || (i2 == (long long)i && k2 < k)) first = false;
+      ci[nc] = i2;
+      ck[nc++] = k2;
+    }
+    if (!first) continue;
+    for (int u = 1; u < nc; ++u)  // by (list position, stencil position)
+      for (int v = u; v > 0 && (ci[v] < ci[v - 1] || (ci[v] == ci[v - 1] && ck[v] < ck[v - 1])); --v) {
+        const long long ti = ci[v]; ci[v] = ci[v - 1]; ci[v - 1] = ti;
+        const int tk = ck[v]; ck[v] = ck[v - 1]; ck[v - 1] = tk;
+      }
+    double acc = 0;  // the reference's double sum; rounded once in the mixed form
+    for (int u = 0; u < nc; ++u) acc += val[ck[u]];
+    real[padded_at(t, n)] = (T)acc;
+  }
 }
 
 // angular-momentum localisation covector (AngMomentumModification::calculateLocalisationCovector,
 // linearmodification.hpp:333-383): per flagged cell at centroid q, with dq = centre - q
 // (wrapped), coefficients c[dir+2] = dq[dir+1], c[dir+1] = -dq[dir+2], and along each
-// other axis the 4th-order gradient stencil a, b scaled by that coefficient
+// other axis (ascending) the 4th-order gradient stencil a, b, -b, -a scaled by that
+// coefficient, summed in the reference's order (cell, axis, stencil position)
 template <typename T>
 __global__ void k_localise_am(T *real, int n, const unsigned long long *cells, size_t count, int dir, double dx,
                               double x0, double y0, double z0, double cx, double cy, double cz, double period,
                               double a, double b) {
-  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
-  unsigned long long c = cells[i];
-  int pz = (int)(c % n);
-  unsigned long long r = c / n;
-  int py = (int)(r % n), px = (int)(r / n);
-  const int p[3] = {px, py, pz};
-  const double q[3] = {px * dx + x0 + dx / 2, py * dx + y0 + dx / 2, pz * dx + z0 + dx / 2};
-  const double cen[3] = {cx, cy, cz};
-  double dq[3];
-  for (int k = 0; k < 3; ++k) {
-    double v = cen[k] - q[k];
-    if (v > period / 2) v -= period;
-    if (v < -period / 2) v += period;
-    dq[k] = v;
-  }
   const int d1 = (dir + 1) % 3, d2 = (dir + 2) % 3;
-  double coeff[3];
-  coeff[dir] = 0;
-  coeff[d2] = dq[d1];
-  coeff[d1] = -dq[d2];
-  const size_t rs = (size_t)(2 * (n / 2 + 1));
-  for (int ax = 0; ax < 3; ++ax) {
-    if (ax == dir) continue;
-    auto at = [&](int step) -> T * {
-      int s[3] = {p[0], p[1], p[2]};
-      s[ax] = ((s[ax] + step) % n + n) % n;
-      return real + ((size_t)s[0] * n + s[1]) * rs + s[2];
-    };
-    atomicAdd(at(-2), (T)(coeff[ax] * a));
-    atomicAdd(at(-1), (T)(coeff[ax] * b));
-    atomicAdd(at(1), (T)(-(coeff[ax] * b)));
-    atomicAdd(at(2), (T)(-(coeff[ax] * a)));
+  const int axes[2] = {d1 < d2 ? d1 : d2, d1 < d2 ? d2 : d1};
+  const double org[3] = {x0, y0, z0}, cen[3] = {cx, cy, cz};
+  // the stencil coefficient of a flagged cell along axis ax
+  auto coeff = [&](unsigned long long id, int ax) {
+    const int p[3] = {(int)(id / ((unsigned long long)n * n)), (int)((id / n) % n), (int)(id % n)};
+    double dq[3];
+    for (int k = 0; k < 3; ++k) {
+      double v = cen[k] - (p[k] * dx + org[k] + dx / 2);
+      if (v > period / 2) v -= period;
+      if (v < -period / 2) v += period;
+      dq[k] = v;
+    }
+    return ax == d2 ? dq[d1] : (ax == d1 ? -dq[d2] : 0.0);
+  };
+  const int off[4] = {-2, -1, 1, 2};
+  const unsigned long long q = cells[i];
+  for (int xa = 0; xa < 2; ++xa) {
+    const int ax = axes[xa];
+    for (int k = 0; k < 4; ++k) {
+      const unsigned long long t = step_cell(q, n, ax, off[k]);
+      long long ci[8];
+      int cx2[8], ck[8], nc = 0;
+      bool first = true;
+      for (int xb = 0; xb < 2 && first; ++xb)
+        for (int k2 = 0; k2 < 4 && first; ++k2) {
+          const long long i2 = find_flagged(cells, count, step_cell(t, n, axes[xb], -off[k2]));
+          if (i2 < 0) continue;
+          if (i2 < (long long)i || (i2 == (long long)i && (xb < xa || (xb == xa && k2 < k)))) first = false;
+          ci[nc] = i2;
+          cx2[nc] = xb;
+          ck[nc++] = k2;
+        }
+      if (!first) continue;
+      for (int u = 1; u < nc; ++u)  // by (list position, axis, stencil position)
+        for (int v = u; v > 0; --v) {
+          const bool before = ci[v] < ci[v - 1] || (ci[v] == ci[v - 1] && (cx2[v] < cx2[v - 1] ||
+                                                                          (cx2[v] == cx2[v - 1] && ck[v] < ck[v - 1])));
+          if (!before) break;
+          const long long ti = ci[v]; ci[v] = ci[v - 1]; ci[v - 1] = ti;
+          const int tx = cx2[v]; cx2[v] = cx2[v - 1]; cx2[v - 1] = tx;
+          const int tk = ck[v]; ck[v] = ck[v - 1]; ck[v - 1] = tk;
+        }
+      double acc = 0;  // the reference's double sum; rounded once in the mixed form
+      for (int u = 0; u < nc; ++u) {
+        const double c = coeff(cells[ci[u]], axes[cx2[u]]);
+        acc += ck[u] == 0 ? c * a : ck[u] == 1 ? c * b : ck[u] == 2 ? -(c * b) : -(c * a);
+      }
+      real[padded_at(t, n)] = (T)acc;
+    }
   }
 }
 

@@ -51,7 +51,8 @@ def test_fft_passes_bit_identical_across_tiles(built, bbks, precision, n, monkey
     schedule, the twiddles and the rounding of every operation (complex products
     are explicit fused multiply-adds)."""
     out = {}
-    for tile in ('generic', '0,0', '1,1', '2,2', '3,3', '0,2', '2,0', '1,3', '3,3,0', '1,2,1', '0,1,2', '4,1', '5,3'):
+    for tile in ('generic', '0,0', '1,1', '2,2', '3,3', '0,2', '2,0', '1,3', '3,3,0', '1,2,1', '0,1,2', '4,1', '5,3',
+                 '6,3', '6,0', '6,2,1'):
         monkeypatch.setenv('GIC_FFT_TILE', tile)
         _, reals, back = _noise_roundtrip(precision, n, bbks)
         out[tile] = (reals, back)
@@ -91,7 +92,7 @@ def test_plane_pass_bit_identical_512(built, bbks, precision, monkeypatch):
     in every lag variant, for 512^3 in both precisions."""
     monkeypatch.setenv('GIC_FFT_TILE', '3,3')
     ref = _roundtrip_raw(precision, 512, bbks, 11)
-    for tile in ('1,0', '3,3,0', '3,3,1', '3,3,2', '4,1', '5,1'):
+    for tile in ('1,0', '3,3,0', '3,3,1', '3,3,2', '4,1', '5,1', '6,1', '6,3', '6,3,0'):
         monkeypatch.setenv('GIC_FFT_TILE', tile)
         raw, back = _roundtrip_raw(precision, 512, bbks, 11)
         assert np.array_equal(raw, ref[0]), tile
@@ -103,13 +104,16 @@ BOXES = [((3, 5, 0), (9, 17, 1)), ((60, 50, 7), (10, 20, 3)), ((0, 0, 0), (64, 1
 
 
 @pytest.mark.parametrize('precision', ['fp64', 'mixed'])
-@pytest.mark.parametrize('n', [64, 256])
-def test_box_transforms_match_whole(built, bbks, precision, n):
+@pytest.mark.parametrize('n,tile', [(64, None), (256, None), (256, '6,3')])
+def test_box_transforms_match_whole(built, bbks, precision, n, tile, monkeypatch):
     """Transforms restricted to a box of cells (the rows and planes outside skipped)
     give the whole transform's bits: forward transforms of fields zero outside the
     box (padding words of every row left non-zero, which the transform must not
-    read), inverse transforms inside the box; boxes wrap around the grid."""
+    read), inverse transforms inside the box; boxes wrap around the grid.  With the
+    tuner's passes, and with the TMA-staged strided pass pinned."""
     from genetic_gb300.generator import _ptr
+    if tile:
+        monkeypatch.setenv('GIC_FFT_TILE', tile)
     gen = make_generator(precision, bbks, [('base', 50.0, n)], 7, 'random_seed')
     rng = np.random.default_rng(5)
     sx = n // 64
@@ -143,3 +147,31 @@ def test_box_transforms_match_whole(built, bbks, precision, n):
             out[kind] = np.stack([raw.real, raw.imag], -1).reshape(n, n, -1)[:, :, :n]
         assert np.array_equal(out['whole'][mask], out['box'][mask]), (start, length)
     gen.close()
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'mixed'])
+def test_tma_pass_bit_identical_in_the_modification_algebra(built, bbks, precision, monkeypatch):
+    """The TMA-staged strided pass (its plain and store-windowed passes; the others fall
+    back to the fused pass) against the fused pass everywhere, through the whole
+    two-level realisation at 256^3 + 256^3 (zoom factor 4) with the four modifications:
+    every field and particle is the same bits (in FP64 too: the path is deterministic)."""
+    levels = [('base', 100.0, 256), ('zoom', 96, 96, 96, 4, 256)]
+    out = {}
+    for tile in ('3,3', '6,3'):
+        monkeypatch.setenv('GIC_FFT_TILE', tile)
+        gen = make_generator(precision, bbks, levels, 8896131, 'random_seed')
+        gen.centre(50, 50, 50)
+        gen.select_sphere(2.0)
+        for name, t in (('overdensity', 1.5), ('vx', 0.0), ('vy', 0.0), ('vz', 0.0)):
+            gen.modify(name, 'absolute', t)
+        chi2 = gen.apply_modifications()
+        gen.done(apply_modifications=False)
+        out[tile] = (chi2, [gen.field(l, f) for l in range(2) for f in ('delta', 'psi_x', 'psi_y', 'psi_z')],
+                     [gen.particles(l) for l in range(2)])
+        gen.close()
+    a, b = out['3,3'], out['6,3']
+    assert a[0] == b[0]
+    for x, y in zip(a[1], b[1]):
+        assert np.array_equal(x, y)
+    for (p, v), (p2, v2) in zip(a[2], b[2]):
+        assert np.array_equal(p, p2) and np.array_equal(v, v2)
