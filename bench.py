@@ -218,24 +218,26 @@ def profiled_traffic(kernel):
     return None
 
 
-def fft_roofline(gen, wl, stream, reps=20):
-    """Average device time of one inverse 3-D FFT of the finest level's x displacement field."""
+def fft_roofline(gen, wl, stream, reps=20, field=None):
+    """Average device time of one inverse 3-D FFT of the finest level's x displacement field
+    (or of `field`)."""
     import torch
     from genetic_gb300 import _lib
     level = len(wl['levels']) - 1
     n = gen.levels[level][1]
     s = 4 if wl['precision'] == 'mixed' else 8
     nc = n * n * (n // 2 + 1)
+    what = _lib.GIC_FIELD_PSI_X if field is None else field
     # the field is in real space after a realisation: forward then inverse keeps it meaningful
     for _ in range(3):
-        gen._call('gic_fft', level, _lib.GIC_FIELD_PSI_X, -1)
-        gen._call('gic_fft', level, _lib.GIC_FIELD_PSI_X, +1)
+        gen._call('gic_fft', level, what, -1)
+        gen._call('gic_fft', level, what, +1)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * reps + 1)]
     times = []
     for r in range(reps):
-        gen._call('gic_fft', level, _lib.GIC_FIELD_PSI_X, -1)
+        gen._call('gic_fft', level, what, -1)
         ev[2 * r].record(stream)
-        gen._call('gic_fft', level, _lib.GIC_FIELD_PSI_X, +1)
+        gen._call('gic_fft', level, what, +1)
         ev[2 * r + 1].record(stream)
     torch.cuda.synchronize()
     for r in range(reps):
@@ -248,6 +250,37 @@ def fft_roofline(gen, wl, stream, reps=20):
     return {'bound': 'hbm', 'achieved': round(achieved, 1), 'peak': peak, 'unit': 'GB/s',
             'frac': round(achieved / peak, 4), 'traffic': profiled_traffic(kernel), 'kernel': kernel,
             'ms_per_launch': round(t * 1e3, 4), 'peak_source': kind}
+
+
+def fft_choice(gen):
+    """The FFT passes the tuner chose per transform size: {n: "<cols>,<rows>,<planes>"}
+    (the GIC_FFT_TILE value that pins them, e.g. for a profiler run)."""
+    out = {}
+    for _, n, _ in gen.levels:
+        c, r, p = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        if gen._lib.gic_fft_choice(gen._ctx, n, ctypes.byref(c), ctypes.byref(r), ctypes.byref(p)) == 0:
+            out[str(n)] = '%d,%d,%d' % (c.value, r.value, p.value)
+    return out
+
+
+def fft_only(n, precision, table, device):
+    """One single-level n^3 context whose white noise is set from the host (a seeded
+    Gaussian half spectrum), then the FFT roofline of its field: the transform passes
+    alone, on a small device footprint."""
+    import torch
+    from genetic_gb300 import _lib
+    from genetic_gb300.generator import _ptr
+    wl = dict(levels=[('base', 100.0, n)], seed_cmd='random_seed', precision=precision)
+    gen = make_gen(wl, table, device)
+    rng = np.random.default_rng(SEED)
+    gen._call('gic_set_noise', 0, _ptr(np.ascontiguousarray(rng.standard_normal((n, n, n // 2 + 1, 2)))))
+    sptr = ctypes.c_void_p()
+    _lib.check(gen._ctx, gen._lib.gic_get_stream(gen._ctx, ctypes.byref(sptr)))
+    stream = torch.cuda.ExternalStream(sptr.value, device=torch.device('cuda', device))
+    roof = fft_roofline(gen, wl, stream, field=_lib.GIC_FIELD_NOISE)
+    passes = fft_choice(gen)
+    gen.close()
+    print(json.dumps({'fft_only': n, 'precision': precision, 'roofline': roof, 'fft_passes': passes}))
 
 
 def cpu_baseline_port(n=192, box=75.0, threads=None):
@@ -464,6 +497,10 @@ def main():
                     help='bracket the timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off)')
     ap.add_argument('--accuracy', action='store_true',
                     help='print the per-field error of the mixed form against FP64 instead of timing')
+    ap.add_argument('--fft-only', type=int, default=0, metavar='N',
+                    help='time the inverse + forward 3-D FFT of one N^3 field (set from the host, no realisation; '
+                         'about 2 N^3 x 8 bytes on the device in the mixed form) and print its roofline: a small case '
+                         'for profiling the transform passes')
     args = ap.parse_args()
     rank, world, local = dist_env()
     if world > 1:
@@ -481,6 +518,9 @@ def main():
     table = np.ascontiguousarray(bbks_table())
     if args.accuracy:
         accuracy(args.workload, wl, table, local)
+        return
+    if args.fft_only:
+        fft_only(args.fft_only, wl['precision'], table, local)
         return
     if wl.get('batch'):
         run_batch(args, wl, table, local, rank, world)
@@ -580,6 +620,7 @@ def main():
     except Exception as e:  # reported, never fatal to the benchmark line
         e2e_tipsy = {'error': str(e)[:200]}
     roof = fft_roofline(gen, wl, stream)
+    fft_passes = fft_choice(gen)
     gen.close()
 
     if rank != 0:
@@ -595,7 +636,7 @@ def main():
                    'precision': wl['precision'], 'seeding': wl['seed_cmd'], 'transfer': 'BBKS table, 2000 rows',
                    'lpt_order': wl.get('order', 1),
                    'particles_per_step': npart, 'l2': 'inputs larger than L2 (fields >= 0.5 GB)',
-                   'parallelism': 'replicas' if world > 1 else 'single GPU'},
+                   'parallelism': 'replicas' if world > 1 else 'single GPU', 'fft_passes': fft_passes},
         'e2e': {'value': round(npart * world / t_e2e / 1e6, 3), 'unit': 'Mparticles/s',
                 'h2d_bytes_per_step': int(table.nbytes), 'd2h_bytes_per_step': int(d2h)},
         'e2e_tipsy': e2e_tipsy,

@@ -247,6 +247,26 @@ int gic_set_fft_wait(gic_ctx *ctx, unsigned spin_limit, int unreachable) {
   return GIC_OK;
 }
 
+int gic_fft_choice(gic_ctx *ctx, int n, int *cols, int *rows, int *planes) {
+  if (!ctx) return GIC_ERR_INVALID_ARG;
+  const gic::FftTables &F = ctx->impl.fft;
+  const bool dbl = ctx->impl.dbl();
+  if (F.force_cols >= 0 && F.force_rows >= 0) {  // pinned by GIC_FFT_TILE
+    if (cols) *cols = F.force_cols;
+    if (rows) *rows = F.force_rows;
+    if (planes) *planes = F.force_planes >= -1 ? F.force_planes : -1;
+    return GIC_OK;
+  }
+  for (const auto &t : F.tuned)
+    if (t.n == n && t.dbl == dbl) {
+      if (cols) *cols = F.force_cols >= 0 ? F.force_cols : t.cols;
+      if (rows) *rows = F.force_rows >= 0 ? F.force_rows : t.rows;
+      if (planes) *planes = F.force_planes >= -1 ? F.force_planes : t.planes;
+      return GIC_OK;
+    }
+  return GIC_ERR_NOT_READY;
+}
+
 int gic_memory_use(gic_ctx *ctx, size_t *in_use, size_t *limit) {
   if (!ctx) return GIC_ERR_INVALID_ARG;
   if (in_use) *in_use = ctx->impl.account.used.load();

@@ -1188,20 +1188,19 @@ __global__ void __launch_bounds__(NCW * 32, L >= 512 ? 1 : 2) k_fft_cols_tma(con
     const size_t off = (size_t)plane * (size_t)L * (size_t)a.B + (size_t)b0;
     const C *in = slots + s * SLOT;
     C v[PER][R];
+    // positions j + r LR of column c; LR is even, so in the pairs layout a thread's rows
+    // share one parity and step LR / 2 rows of the box
+    static_assert(!PAIRS || LR % 2 == 0, "row pairs need an even stride");
+    constexpr int RSTEP = PAIRS ? (LR / 2) * SH::W : LR * TC;
 #pragma unroll
     for (int p = 0; p < PER; ++p) {
       const int b = ct + p * NC;
       if (NB % NC == 0 || b < NB) {
         const int c = b % TC, j = b / TC;
+        const C *src = in + (PAIRS ? (j & 1) * (SH::ROWS * SH::W + 1) + (j >> 1) * SH::W + c : j * TC + c);
+        const bool valid = c < tcv;
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const int m = j + r * LR;
-          C x;
-          if (PAIRS) x = in[(m & 1) * SH::ROWS * SH::W + (m >> 1) * SH::W + c + (m & 1)];
-          else x = in[m * TC + c];
-          if (c >= tcv) x = czero<C>();
-          v[p][r] = x;
-        }
+        for (int r = 0; r < R; ++r) v[p][r] = valid ? src[r * RSTEP] : czero<C>();
       }
     }
 #pragma unroll
@@ -1234,11 +1233,12 @@ __global__ void __launch_bounds__(NCW * 32, L >= 512 ? 1 : 2) k_fft_cols_tma(con
         for (int r = 1; r < RL; ++r) w[r] = cmul(w[r], twid(stw, r * j * (L / (NSL * RL)), SIGN));
         Dft<T, C, RL>::run(w, SIGN);
         if (c < tcv) {
+          C *out = base + (size_t)j * (size_t)a.B + c;
+          const size_t ostep = (size_t)NSL * (size_t)a.B;
 #pragma unroll
           for (int r = 0; r < RL; ++r) {
-            const int m = j + r * NSL;
-            if (EXT && (m - a.sm0 + L) % L >= a.smn) continue;
-            base[(size_t)m * (size_t)a.B + c] = cscale(w[r], a.scale);
+            if (EXT && (j + r * NSL - a.sm0 + L) % L >= a.smn) continue;
+            out[r * ostep] = cscale(w[r], a.scale);
           }
         }
       }

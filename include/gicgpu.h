@@ -419,6 +419,13 @@ GIC_API int gic_launch_count(unsigned long long *count);
  * genetIC (its FFTW transforms have no waits). */
 GIC_API int gic_set_fft_wait(gic_ctx *ctx, unsigned spin_limit, int unreachable);
 
+/* The FFT passes the context uses for n^3 transforms in its precision (chosen by timing
+ * the candidates on first use, or pinned by GIC_FFT_TILE=<cols>,<rows>[,<plane variant>]):
+ * strided-pass candidate (6: TMA-staged), row-pass candidate and plane-pass variant (-1:
+ * separate y and z passes).  GIC_ERR_NOT_READY before the first n^3 transform, or when
+ * n^3 uses the runtime-length passes.  The choice never changes a result. */
+GIC_API int gic_fft_choice(gic_ctx *ctx, int n, int *cols, int *rows, int *planes);
+
 /* Device memory the context holds now, in bytes, and its mem_limit (0 = none).
  * Every device allocation a call makes for the context is checked against the limit
  * first: one that would pass it fails the call with GIC_ERR_OOM (the message names
