@@ -125,6 +125,8 @@ SIGNATURES = {
     'gic_clear_modifications': [_P],
     'gic_noise_op': [_P, _I, ctypes.c_double],
     'gic_splice': [_P, ctypes.c_ulong, ctypes.POINTER(_P), ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(_I)],
+    'gic_fetch_particles_async': [_P, _I, _D, _P],
+    'gic_fetch_wait': [_P],
     'gic_fft_choice': [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)],
     'gic_batch_create': [ctypes.POINTER(_P), ctypes.POINTER(_P), _I],
     'gic_batch_destroy': [_P],

@@ -297,6 +297,11 @@ GIC_API int gic_batch_realise(gic_batch *b, const unsigned long *seeds, const in
   };
   try {
     gic::cuda_check(cudaSetDevice(b->device), "cudaSetDevice");
+    // asynchronous particle fetches end first: the realisations write the particle buffers
+    for (auto *c : b->ctxs) {
+      gic::AccountScope scope(c->impl.account);
+      gic::finish_fetches(c->impl);
+    }
     bool replay = false;
     if (!in_graph.empty()) {
       b->in_graph = in_graph;

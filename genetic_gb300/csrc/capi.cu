@@ -138,13 +138,11 @@ void set_noise_typed(Context &c, Level &L, const double *host) {
 template <typename T>
 double chi2_typed(Context &c, Level &L) {
   const int blocks = 256;
-  DevBuf partial;
-  partial.ensure(blocks * sizeof(double));
-  k_chi2_partial<T><<<blocks, 256, 0, c.stream>>>(L.noise.as<T>(), L.n, partial.as<double>());
+  c.small.ensure(blocks * sizeof(double));
+  k_chi2_partial<T><<<blocks, 256, 0, c.stream>>>(L.noise.as<T>(), L.n, c.small.as<double>());
   launched();
   std::vector<double> h(blocks);
-  GIC_CUDA(cudaMemcpyAsync(h.data(), partial.ptr, blocks * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-  GIC_CUDA(cudaStreamSynchronize(c.stream));
+  read_small(c, c.small.ptr, blocks * sizeof(double), h.data());
   double s = 0;
   for (double v : h) s += v;
   return s;
@@ -284,9 +282,13 @@ int gic_destroy(gic_ctx *ctx) {
   if (!ctx) return GIC_OK;
   cudaSetDevice(ctx->impl.device);
   cudaStreamSynchronize(ctx->impl.stream);
-  cudaStream_t s = ctx->impl.stream;
+  cudaStream_t s = ctx->impl.stream, cs = ctx->impl.copy_stream;
+  cudaEvent_t ready = ctx->impl.copy_ready;
+  if (cs) cudaStreamSynchronize(cs);
   delete ctx;  // frees device buffers
   cudaStreamDestroy(s);
+  if (cs) cudaStreamDestroy(cs);
+  if (ready) cudaEventDestroy(ready);
   return GIC_OK;
 }
 
@@ -493,6 +495,18 @@ int gic_fetch_particles_native(gic_ctx *ctx, int level, double *pos, void *vel) 
     GIC_CUDA(cudaMemcpyAsync(vel, L.vel.ptr, 3 * m * (C.dbl() ? sizeof(double) : sizeof(float)),
                              cudaMemcpyDeviceToHost, C.stream));
   GIC_CUDA(cudaStreamSynchronize(C.stream));
+  API_END
+}
+
+int gic_fetch_particles_async(gic_ctx *ctx, int level, double *pos, void *vel) {
+  API_BEGIN(ctx)
+  gic::fetch_particles_async(C, gic::level_at(C, level), pos, vel);
+  API_END
+}
+
+int gic_fetch_wait(gic_ctx *ctx) {
+  API_BEGIN(ctx)
+  gic::finish_fetches(C);
   API_END
 }
 

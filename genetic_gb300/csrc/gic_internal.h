@@ -7,6 +7,7 @@
 #include <vector>
 #include <memory>
 #include <atomic>
+#include <utility>
 #include "../../include/gicgpu.h"
 
 namespace gic {
@@ -90,6 +91,12 @@ struct DevBuf {
     }
   }
   template <typename T> T *as() const { return static_cast<T *>(ptr); }
+  void swap(DevBuf &o) {
+    std::swap(ptr, o.ptr);
+    std::swap(bytes, o.bytes);
+    std::swap(acct, o.acct);
+    std::swap(serial, o.serial);
+  }
 };
 
 // Device buffers kept between calls: the fields of the modification algebra take
@@ -150,10 +157,23 @@ struct Level {
   DevBuf tab_main_f, tab_lp_src_f, tab_lp_f;  // float copies of the three (float fields)
   DevBuf field2[3];      // second-order displacements psi2_x, psi2_y, psi2_z (real)
   DevBuf pos, vel;       // particles: pos double[3M], vel (precision)[3M]
+  // asynchronous fetches (gic_fetch_particles_async): while one may still be reading pos/vel,
+  // the next particles go to the other pair (swapped in); `fetched` is recorded on the copy
+  // stream after a fetch of the current pair, fetched_alt likewise for the other pair
+  DevBuf pos_alt, vel_alt;
+  cudaEvent_t fetched = nullptr, fetched_alt = nullptr;
+  bool fetching = false, fetching_alt = false;
   bool have_noise = false;
   bool have_fields = false;  // displacements in real space
   bool have_delta = false;   // delta in real space (made on demand)
   bool have_lpt2 = false;
+  Level() = default;
+  Level(const Level &) = delete;
+  Level &operator=(const Level &) = delete;
+  ~Level() {
+    if (fetched) cudaEventDestroy(fetched);
+    if (fetched_alt) cudaEventDestroy(fetched_alt);
+  }
 };
 
 struct Cosmo {
@@ -285,6 +305,21 @@ struct Context {
   bool defer_checks = false;
   int precision = GIC_FP64;
   cudaStream_t stream = nullptr;
+  // copies of gic_fetch_particles_async, ordered after `stream` by copy_ready
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_ready = nullptr;
+  // small results (flags, inner products) come back through mapped pinned host memory that a
+  // kernel writes: a cudaMemcpy would queue behind a large transfer on the copy engine
+  struct Mapped {
+    void *host = nullptr, *dev = nullptr;
+    Mapped() = default;
+    Mapped(const Mapped &) = delete;
+    Mapped &operator=(const Mapped &) = delete;
+    ~Mapped() {
+      if (host) cudaFreeHost(host);
+    }
+  } readback;
+  DevBuf small;  // scratch of reductions whose partial sums are read back
   std::string last_error;
   std::vector<std::unique_ptr<Level>> levels;
   Cosmo cosmo{};
@@ -426,6 +461,15 @@ void noise_real(Context &ctx, int level, void *out);
 // particles.cu
 double velocity_to_offset_ratio(const Cosmo &c);
 void make_particles(Context &ctx, Level &L, int order = 1);
+// asynchronous particle fetches: enqueue the copies of a level's particles on the copy
+// stream; finish_fetches waits for every one and releases the buffer pairs
+void fetch_particles_async(Context &ctx, Level &L, double *host_pos, void *host_vel);
+void finish_fetches(Context &ctx);
+// copies `bytes` (a multiple of 4, at most kReadbackBytes) of device memory to host memory
+// through the mapped readback buffer, after the work queued on ctx.stream; synchronises
+// ctx.stream.  Larger or unaligned reads use a plain copy.
+constexpr size_t kReadbackBytes = 64 * 1024;
+void read_small(Context &ctx, const void *dev, size_t bytes, void *host);
 // the descriptors of the noise streams of (seed, mode) for the context's levels, in the
 // layout a deferred draw was captured with, copied to the device on the context's stream
 void upload_noise_streams(Context &ctx, unsigned long long seed, int mode);

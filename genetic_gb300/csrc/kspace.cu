@@ -346,8 +346,7 @@ void transfer_setup(Context &ctx, const double *table, int nrows, int ncols) {
                                         T.lnT_all.as<double>(), T.c_all.as<double>(), n, partial.as<double>());
   launched(1);
   std::vector<double> hp(blocks);
-  GIC_CUDA(cudaMemcpyAsync(hp.data(), partial.ptr, blocks * sizeof(double), cudaMemcpyDeviceToHost, s));
-  GIC_CUDA(cudaStreamSynchronize(s));
+  read_small(ctx, partial.ptr, blocks * sizeof(double), hp.data());
   double sum = 0;
   for (double v : hp) sum += v;
   double amp = 9. / 2. / M_PI / M_PI;

@@ -1263,8 +1263,7 @@ struct ModEngine {
     k_sum<<<np, 256, 0, ctx.stream>>>(part, (int)per, part + per * np);
     launched();
     std::vector<double> out(np);
-    GIC_CUDA(cudaMemcpyAsync(out.data(), part + per * np, np * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
-    GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+    read_small(ctx, part + per * np, np * sizeof(double), out.data());
     return out;
   }
   // <a_i|b_i> for every pair, summed over levels, in Fourier space
@@ -1348,8 +1347,7 @@ struct ModEngine {
     if (np == 0) return {};
     const double *d = inner_block_dev(A, B);
     std::vector<double> out(np);
-    GIC_CUDA(cudaMemcpyAsync(out.data(), d, np * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
-    GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+    read_small(ctx, d, np * sizeof(double), out.data());
     return out;
   }
 

@@ -8,6 +8,7 @@
 // real-space displacement fields: positions in double, velocities in the
 // working precision.
 #include "gic_internal.h"
+#include <cstring>
 #include <cmath>
 
 namespace gic {
@@ -233,6 +234,18 @@ double velocity_to_offset_ratio(const Cosmo &c) {
 template <typename T>
 static void particles_typed(Context &ctx, Level &L, int order) {
   size_t m = L.ncells();
+  // an asynchronous fetch may still be reading the current pair: write the other one, after
+  // (on the device) any fetch still reading that
+  if (L.fetching) {
+    L.pos.swap(L.pos_alt);
+    L.vel.swap(L.vel_alt);
+    std::swap(L.fetched, L.fetched_alt);
+    std::swap(L.fetching, L.fetching_alt);
+    if (L.fetching) {
+      GIC_CUDA(cudaStreamWaitEvent(ctx.stream, L.fetched, 0));
+      L.fetching = false;
+    }
+  }
   L.pos.ensure(3 * m * sizeof(double));
   L.vel.ensure(3 * m * sizeof(T));
   T ratio = (T)velocity_to_offset_ratio(ctx.cosmo);
@@ -249,6 +262,60 @@ static void particles_typed(Context &ctx, Level &L, int order) {
                                                         nullptr, nullptr, nullptr, L.n, cen, L.periodic, ratio,
                                                         L.pos.as<double>(), L.vel.as<T>());
   launched(2);
+}
+
+void fetch_particles_async(Context &ctx, Level &L, double *host_pos, void *host_vel) {
+  if (!L.pos.ptr || !L.vel.ptr) fail(GIC_ERR_NOT_READY, "particles have not been generated");
+  if (!ctx.copy_stream) {
+    GIC_CUDA(cudaStreamCreateWithFlags(&ctx.copy_stream, cudaStreamNonBlocking));
+    GIC_CUDA(cudaEventCreateWithFlags(&ctx.copy_ready, cudaEventDisableTiming));
+  }
+  if (!L.fetched) {
+    GIC_CUDA(cudaEventCreateWithFlags(&L.fetched, cudaEventDisableTiming));
+    GIC_CUDA(cudaEventCreateWithFlags(&L.fetched_alt, cudaEventDisableTiming));
+  }
+  const size_t m = L.ncells();
+  GIC_CUDA(cudaEventRecord(ctx.copy_ready, ctx.stream));
+  GIC_CUDA(cudaStreamWaitEvent(ctx.copy_stream, ctx.copy_ready, 0));
+  if (host_pos)
+    GIC_CUDA(cudaMemcpyAsync(host_pos, L.pos.ptr, 3 * m * sizeof(double), cudaMemcpyDeviceToHost, ctx.copy_stream));
+  if (host_vel)
+    GIC_CUDA(cudaMemcpyAsync(host_vel, L.vel.ptr, 3 * m * (ctx.dbl() ? sizeof(double) : sizeof(float)),
+                             cudaMemcpyDeviceToHost, ctx.copy_stream));
+  GIC_CUDA(cudaEventRecord(L.fetched, ctx.copy_stream));
+  L.fetching = true;
+}
+
+__global__ void k_copy_words(const unsigned *__restrict__ src, unsigned *__restrict__ dst, size_t n) {
+  for (size_t i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+
+void read_small(Context &ctx, const void *dev, size_t bytes, void *host) {
+  if (bytes == 0) return;
+  if (bytes > kReadbackBytes || bytes % 4 || reinterpret_cast<uintptr_t>(dev) % 4) {
+    GIC_CUDA(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, ctx.stream));
+    GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+    return;
+  }
+  Context::Mapped &m = ctx.readback;
+  if (!m.host) {
+    GIC_CUDA(cudaHostAlloc(&m.host, kReadbackBytes, cudaHostAllocMapped));
+    if (cudaHostGetDevicePointer(&m.dev, m.host, 0) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFreeHost(m.host);
+      m.host = nullptr;
+      fail(GIC_ERR_CUDA, "cudaHostGetDevicePointer failed");
+    }
+  }
+  k_copy_words<<<1, 256, 0, ctx.stream>>>(static_cast<const unsigned *>(dev), static_cast<unsigned *>(m.dev), bytes / 4);
+  launched();
+  GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+  std::memcpy(host, m.host, bytes);
+}
+
+void finish_fetches(Context &ctx) {
+  if (ctx.copy_stream) GIC_CUDA(cudaStreamSynchronize(ctx.copy_stream));
+  for (auto &L : ctx.levels) L->fetching = L->fetching_alt = false;
 }
 
 // Particles of a virtual grid over level L's region (genetIC's supersample / subsample):

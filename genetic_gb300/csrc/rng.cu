@@ -799,8 +799,7 @@ static void generate_gaussians(Context &ctx, std::vector<Stream> &streams, unsig
   launched(2);
   if (ctx.defer_checks) return;
   int flag = 0;
-  GIC_CUDA(cudaMemcpyAsync(&flag, R.flags.ptr, sizeof(int), cudaMemcpyDeviceToHost, cs));
-  GIC_CUDA(cudaStreamSynchronize(cs));
+  read_small(ctx, R.flags.ptr, sizeof(int), &flag);
   if (flag) {
     if (margin > 4.0) fail(GIC_ERR_INTERNAL, "random stream shorter than the gaussians it must supply");
     generate_gaussians(ctx, streams, total_gauss, margin * 1.5);
@@ -921,8 +920,7 @@ void upload_noise_streams(Context &ctx, unsigned long long seed, int mode) {
 bool noise_underrun(Context &ctx) {
   if (!ctx.rng.flags.ptr) return false;
   int flag = 0;
-  GIC_CUDA(cudaMemcpyAsync(&flag, ctx.rng.flags.ptr, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
-  GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+  read_small(ctx, ctx.rng.flags.ptr, sizeof(int), &flag);
   return flag != 0;
 }
 

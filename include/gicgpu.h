@@ -152,6 +152,17 @@ GIC_API int gic_fetch_particles(gic_ctx *ctx, int level, double *pos, double *ve
  * ParticleEvaluator yields Particle<float>): the velocities cross the host link in half
  * the bytes, with no rounding beyond the device's own. */
 GIC_API int gic_fetch_particles_native(gic_ctx *ctx, int level, double *pos, void *vel);
+
+/* gic_fetch_particles_native without waiting: the copies are queued on the context's copy
+ * stream after the work queued so far and the call returns.  pos, vel must be pinned host
+ * memory and stay valid until gic_fetch_wait returns.  The next realisation of the level
+ * writes its particles to a second device buffer pair while a fetch of the first may still
+ * be running (a third realisation waits, on the device, for the fetch of the pair it
+ * reuses), so a caller can overlap the copies of one realisation with the next one's
+ * computation.  No genetIC counterpart (genetIC's evaluators return particles on demand). */
+GIC_API int gic_fetch_particles_async(gic_ctx *ctx, int level, double *pos, void *vel);
+/* Waits for every asynchronous fetch of the context and reports their errors. */
+GIC_API int gic_fetch_wait(gic_ctx *ctx);
 /* Particles of a level evaluated on a virtual grid over its region, as genetIC's
  * supersample / subsample commands produce them (SuperSampleEvaluator and
  * SubSampleEvaluator, genetIC/src/simulation/field/evaluator.hpp:96-207, over the

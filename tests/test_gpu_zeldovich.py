@@ -82,3 +82,38 @@ def test_native_fetch_matches_double_fetch(built, bbks, precision):
     assert vel_n.dtype == (np.float32 if precision == 'mixed' else np.float64)
     assert np.array_equal(pos, pos_n)
     assert np.array_equal(vel, vel_n.astype(np.float64))
+
+
+@pytest.mark.parametrize('precision', ['mixed', 'fp64'])
+def test_async_fetch_overlapping_realisations(built, bbks, precision):
+    """gic_fetch_particles_async: three realisations in a row, each fetched without waiting
+    while the next one computes (the level alternates between two device buffer pairs; the
+    third waits on the device for the first fetch), give the particles of each realisation,
+    the same bits as a synchronous fetch of it."""
+    import ctypes
+    torch = pytest.importorskip('torch')
+    from conftest import make_generator
+    from genetic_gb300.generator import _ptr
+    levels = [('base', 50.0, 32), ('zoom', 8, 8, 8, 2, 32)]
+    seeds = [11, 12, 13]
+    want = []
+    for seed in seeds:
+        g = make_generator(precision, bbks, levels, seed, 'random_seed')
+        g.done()
+        want.append([g.particles_native(l) for l in range(2)])
+        g.close()
+    gen = make_generator(precision, bbks, levels, seeds[0], 'random_seed')
+    vdt = torch.float32 if precision == 'mixed' else torch.float64
+    bufs = [[(torch.empty((32 ** 3, 3), dtype=torch.float64, pin_memory=True).numpy(),
+              torch.empty((32 ** 3, 3), dtype=vdt, pin_memory=True).numpy()) for _ in range(2)] for _ in seeds]
+    for k, seed in enumerate(seeds):
+        gen._call('gic_draw_noise', seed, 2)
+        gen._call('gic_zeldovich', 1)
+        for l, (pos, vel) in enumerate(bufs[k]):
+            gen._call('gic_fetch_particles_async', l, _ptr(pos), ctypes.c_void_p(vel.ctypes.data))
+    gen._call('gic_fetch_wait')
+    gen.close()
+    for k in range(len(seeds)):
+        for l in range(2):
+            assert np.array_equal(bufs[k][l][0], want[k][l][0]), (k, l)
+            assert np.array_equal(bufs[k][l][1], want[k][l][1]), (k, l)
