@@ -149,6 +149,7 @@ SIGNATURES = {
     'gic_tipsy_factors': [_P, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, _D, _D, _D],
     'gic_tipsy_pack_host': [_P, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.c_ulonglong, ctypes.c_ulonglong, _P, _I],
     'gic_tipsy_pack': [_P, _P, ctypes.c_ulonglong, ctypes.c_ulonglong, _P],
+    'gic_tipsy_pack_async': [_P, _P, ctypes.c_ulonglong, ctypes.c_ulonglong, _P],
     'gic_gadget_pack': [_P, _P, ctypes.POINTER(_I), ctypes.c_ulonglong, ctypes.c_ulonglong, _P, _P, _P, _P],
     'gic_gadget_pack_host': [_P, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_I), ctypes.c_ulonglong,
                              ctypes.c_ulonglong, _P, _P, _P, _P, _I],

@@ -284,11 +284,14 @@ int gic_destroy(gic_ctx *ctx) {
   cudaStreamSynchronize(ctx->impl.stream);
   cudaStream_t s = ctx->impl.stream, cs = ctx->impl.copy_stream;
   cudaEvent_t ready = ctx->impl.copy_ready;
+  cudaEvent_t rec[2] = {ctx->impl.records_read[0], ctx->impl.records_read[1]};
   if (cs) cudaStreamSynchronize(cs);
   delete ctx;  // frees device buffers
   cudaStreamDestroy(s);
   if (cs) cudaStreamDestroy(cs);
   if (ready) cudaEventDestroy(ready);
+  for (cudaEvent_t e : rec)
+    if (e) cudaEventDestroy(e);
   return GIC_OK;
 }
 
@@ -461,6 +464,13 @@ int gic_tipsy_pack(gic_ctx *ctx, const gic_particle_map *map, unsigned long long
                    gic_tipsy_dark *host_out) {
   API_BEGIN(ctx)
   gic::tipsy_pack_device(C, map, first, count, host_out);
+  API_END
+}
+
+int gic_tipsy_pack_async(gic_ctx *ctx, const gic_particle_map *map, unsigned long long first, unsigned long long count,
+                         gic_tipsy_dark *host_out) {
+  API_BEGIN(ctx)
+  gic::tipsy_pack_device(C, map, first, count, host_out, true);
   API_END
 }
 

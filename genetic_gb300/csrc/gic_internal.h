@@ -320,6 +320,11 @@ struct Context {
     }
   } readback;
   DevBuf small;  // scratch of reductions whose partial sums are read back
+  // the device record buffers of asynchronous tipsy packs, and the copy that last read each
+  DevBuf records[2];
+  cudaEvent_t records_read[2] = {nullptr, nullptr};
+  bool records_pending[2] = {false, false};
+  int records_next = 0;
   std::string last_error;
   std::vector<std::unique_ptr<Level>> levels;
   Cosmo cosmo{};
@@ -497,8 +502,11 @@ void gadget_pack_host(const gic_particle_map *m, const double *const *pos, const
 void gadget_pack_device(Context &C, const gic_particle_map *m, const int *level_types, unsigned long long first,
                         unsigned long long count, float *pos_out, float *vel_out, unsigned long long *ids,
                         float *mass_out);
+// async: the copy to host_out is queued on the copy stream (pinned host_out, valid until
+// finish_fetches); the records are packed into one of two device buffers, the next pack
+// into the other (after, on the device, any copy still reading it)
 void tipsy_pack_device(Context &C, const gic_particle_map *m, unsigned long long first, unsigned long long count,
-                       gic_tipsy_dark *host_out);
+                       gic_tipsy_dark *host_out, bool async = false);
 // the message of the last failure of a call without a context (this thread)
 std::string &host_error();
 }  // namespace gic

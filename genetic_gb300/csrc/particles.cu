@@ -316,6 +316,7 @@ void read_small(Context &ctx, const void *dev, size_t bytes, void *host) {
 void finish_fetches(Context &ctx) {
   if (ctx.copy_stream) GIC_CUDA(cudaStreamSynchronize(ctx.copy_stream));
   for (auto &L : ctx.levels) L->fetching = L->fetching_alt = false;
+  ctx.records_pending[0] = ctx.records_pending[1] = false;
 }
 
 // Particles of a virtual grid over level L's region (genetIC's supersample / subsample):

@@ -656,7 +656,7 @@ void gadget_pack_device(Context &C, const gic_particle_map *m, const int *level_
 }
 
 void tipsy_pack_device(Context &C, const gic_particle_map *m, unsigned long long first, unsigned long long count,
-                       gic_tipsy_dark *host_out) {
+                       gic_tipsy_dark *host_out, bool async) {
   const MapView v = check_map(m);
   check_window(map_size(v), first, count, host_out);
   if ((int)C.levels.size() < v.nlevels) fail(GIC_ERR_NOT_READY, "the map has more levels than the context");
@@ -670,7 +670,23 @@ void tipsy_pack_device(Context &C, const gic_particle_map *m, unsigned long long
   row_tables(v, rep_begin, kept_before);
   const size_t rows = (size_t)v.n0 * v.n0, u = sizeof(unsigned long long);
   auto drep = C.pool.take(std::max<size_t>(1, v.n_replaced) * u), dbeg = C.pool.take((rows + 1) * u),
-       dkept = C.pool.take(rows * u), dout = C.pool.take((size_t)count * sizeof(gic_tipsy_dark));
+       dkept = C.pool.take(rows * u);
+  std::unique_ptr<DevBuf> dout;
+  int slot = -1;
+  if (async) {
+    // alternate two record buffers; one a copy may still be reading is waited for on the device
+    slot = C.records_next;
+    C.records_next ^= 1;
+    if (!C.copy_stream) {
+      GIC_CUDA(cudaStreamCreateWithFlags(&C.copy_stream, cudaStreamNonBlocking));
+      GIC_CUDA(cudaEventCreateWithFlags(&C.copy_ready, cudaEventDisableTiming));
+    }
+    if (!C.records_read[slot]) GIC_CUDA(cudaEventCreateWithFlags(&C.records_read[slot], cudaEventDisableTiming));
+    if (C.records_pending[slot]) GIC_CUDA(cudaStreamWaitEvent(C.stream, C.records_read[slot], 0));
+    C.records[slot].ensure((size_t)count * sizeof(gic_tipsy_dark));
+  } else {
+    dout = C.pool.take((size_t)count * sizeof(gic_tipsy_dark));
+  }
   if (v.n_replaced)
     GIC_CUDA(cudaMemcpyAsync(drep->ptr, v.replaced, v.n_replaced * u, cudaMemcpyHostToDevice, C.stream));
   GIC_CUDA(cudaMemcpyAsync(dbeg->ptr, rep_begin.data(), (rows + 1) * u, cudaMemcpyHostToDevice, C.stream));
@@ -678,11 +694,22 @@ void tipsy_pack_device(Context &C, const gic_particle_map *m, unsigned long long
   MapView dv = v;
   dv.replaced = drep->as<unsigned long long>();
   const TipsyConst c = tipsy_const(m);
-  gic_tipsy_dark *out = dout->as<gic_tipsy_dark>();
+  gic_tipsy_dark *out = async ? C.records[slot].as<gic_tipsy_dark>() : dout->as<gic_tipsy_dark>();
   if (C.dbl())
     launch_tipsy<double>(C, dv, c, first, count, dbeg->as<unsigned long long>(), dkept->as<unsigned long long>(), out);
   else
     launch_tipsy<float>(C, dv, c, first, count, dbeg->as<unsigned long long>(), dkept->as<unsigned long long>(), out);
+  if (async) {
+    GIC_CUDA(cudaEventRecord(C.copy_ready, C.stream));
+    GIC_CUDA(cudaStreamWaitEvent(C.copy_stream, C.copy_ready, 0));
+    GIC_CUDA(cudaMemcpyAsync(host_out, out, (size_t)count * sizeof(gic_tipsy_dark), cudaMemcpyDeviceToHost,
+                             C.copy_stream));
+    GIC_CUDA(cudaEventRecord(C.records_read[slot], C.copy_stream));
+    C.records_pending[slot] = true;
+    // the tables are read by kernels on C.stream only: later users of the pool are ordered after them
+    for (auto *b : {&drep, &dbeg, &dkept}) C.pool.give(std::move(*b));
+    return;
+  }
   GIC_CUDA(cudaMemcpyAsync(host_out, out, (size_t)count * sizeof(gic_tipsy_dark), cudaMemcpyDeviceToHost, C.stream));
   GIC_CUDA(cudaStreamSynchronize(C.stream));
   for (auto *b : {&drep, &dbeg, &dkept, &dout}) C.pool.give(std::move(*b));

@@ -242,6 +242,12 @@ GIC_API int gic_tipsy_pack_host(const gic_particle_map *map, const double *const
  * per particle cross to the host instead of the 48 of gic_fetch_particles. */
 GIC_API int gic_tipsy_pack(gic_ctx *ctx, const gic_particle_map *map, unsigned long long first, unsigned long long count,
                            gic_tipsy_dark *host_out);
+/* gic_tipsy_pack without waiting for the copy: the records are packed on the device and
+ * their copy to host_out (pinned, valid until gic_fetch_wait returns) is queued on the
+ * context's copy stream, as gic_fetch_particles_async's are; consecutive packs alternate
+ * two device record buffers. */
+GIC_API int gic_tipsy_pack_async(gic_ctx *ctx, const gic_particle_map *map, unsigned long long first,
+                                 unsigned long long count, gic_tipsy_dark *host_out);
 
 /* Gadget blocks (io::gadget::GadgetOutput, genetIC/src/io/gadget.hpp:481-520) of the map's
  * particles from host particles, by `threads` host threads.  level_types[l] is level l's

@@ -39,6 +39,37 @@ def test_device_tipsy_matches_host_packer(built, bbks, precision):
     gen.close()
 
 
+@pytest.mark.parametrize('precision', ['mixed'])
+def test_async_tipsy_pack_overlapping_realisations(built, bbks, precision):
+    """gic_tipsy_pack_async after each of three realisations in a row, without waiting
+    (two device record buffers alternate; the copies run on the copy stream): each
+    pinned buffer holds its own realisation's records, the same bits as gic_tipsy_pack."""
+    torch = pytest.importorskip('torch')
+    replaced = fo.flag_cells(fo.Levels(ZOOM2), 0, (25., 25., 25.), 'cube', 10)
+    lev, _ = fo.mapper_order(32, replaced, 32, 2, ORIGIN)
+    m = make_map(ZOOM2, replaced, fo.tipsy_factors(ZOOM2, COSMO, lev))
+    seeds = [21, 22, 23]
+    want = []
+    for seed in seeds:
+        g = make_generator(precision, bbks, LEVELS, seed, 'random_seed')
+        g.done()
+        n = 32 ** 3 + 7 * len(replaced)  # coarse cells kept + 8 fine particles per replaced cell
+        rec = np.zeros((n, 9), dtype=np.float32)
+        g._call('gic_tipsy_pack', ctypes.byref(m), 0, n, rec.ctypes.data_as(ctypes.c_void_p))
+        want.append(rec)
+        g.close()
+    gen = make_generator(precision, bbks, LEVELS, seeds[0], 'random_seed')
+    bufs = [torch.zeros((n * 9,), dtype=torch.float32, pin_memory=True).numpy() for _ in seeds]
+    for k, seed in enumerate(seeds):
+        gen._call('gic_draw_noise', seed, 2)
+        gen._call('gic_zeldovich', 1)
+        gen._call('gic_tipsy_pack_async', ctypes.byref(m), 0, n, bufs[k].ctypes.data_as(ctypes.c_void_p))
+    gen._call('gic_fetch_wait')
+    gen.close()
+    for k in range(len(seeds)):
+        assert np.array_equal(bufs[k].view(np.uint32), want[k].reshape(-1).view(np.uint32)), k
+
+
 def _gadget_host(lib, m, pos, vel, types, first, count):
     P = ctypes.POINTER(ctypes.c_double)
     pp = (P * len(pos))(*[np.ascontiguousarray(p).ctypes.data_as(P) for p in pos])
