@@ -127,6 +127,7 @@ SIGNATURES = {
     'gic_splice': [_P, ctypes.c_ulong, ctypes.POINTER(_P), ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(_I)],
     'gic_fetch_particles_async': [_P, _I, _D, _P],
     'gic_fetch_wait': [_P],
+    'gic_grafic_pack': [_P, _P, _I, _I, _P, _P, _P, _P],
     'gic_fft_choice': [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)],
     'gic_batch_create': [ctypes.POINTER(_P), ctypes.POINTER(_P), _I],
     'gic_batch_destroy': [_P],
@@ -172,6 +173,12 @@ def load():
         fn.restype = ctypes.c_char_p if name in ('gic_last_error', 'gic_batch_last_error') else ctypes.c_int
     _lib = lib
     return lib
+
+
+class GraficGrid(ctypes.Structure):
+    """gic_grafic_grid: one grid of genetIC's grafic stack (include/gicgpu.h)."""
+    _fields_ = [('level', ctypes.c_int), ('factor', ctypes.c_int), ('roll', ctypes.c_int * 3),
+                ('vel_factor', ctypes.c_double), ('pos_factor', ctypes.c_double), ('id_offset', ctypes.c_ulonglong)]
 
 
 class GicError(RuntimeError):

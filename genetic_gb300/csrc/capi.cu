@@ -467,6 +467,14 @@ int gic_tipsy_pack(gic_ctx *ctx, const gic_particle_map *map, unsigned long long
   API_END
 }
 
+int gic_grafic_pack(gic_ctx *ctx, const gic_grafic_grid *grid, int z0, int nz, float *vel, float *pos, float *delta,
+                    unsigned long long *ids) {
+  API_BEGIN(ctx)
+  if (!grid) gic::fail(GIC_ERR_INVALID_ARG, "null grid");
+  gic::grafic_pack(C, *grid, z0, nz, vel, pos, delta, ids);
+  API_END
+}
+
 int gic_tipsy_pack_async(gic_ctx *ctx, const gic_particle_map *map, unsigned long long first, unsigned long long count,
                          gic_tipsy_dark *host_out) {
   API_BEGIN(ctx)

@@ -482,6 +482,9 @@ void upload_noise_streams(Context &ctx, unsigned long long seed, int mode);
 bool noise_underrun(Context &ctx);
 // particles of a virtual grid over L's region: factor > 1 supersampled, < -1 subsampled
 void resampled_particles(Context &ctx, const Level &L, int factor, double *host_pos, double *host_vel);
+// the grafic writer's per-cell floats of one grid of its stack (see gic_grafic_pack)
+void grafic_pack(Context &ctx, const gic_grafic_grid &g, int z0, int nz, float *host_vel, float *host_pos,
+                 float *host_delta, unsigned long long *host_ids);
 // particles of listed cells of a zoom level's resolution-matching grid (strays)
 void matched_particles(Context &ctx, int level, const unsigned long long *cells, size_t count, double *pos,
                        double *vel);

@@ -319,6 +319,46 @@ void finish_fetches(Context &ctx) {
   ctx.records_pending[0] = ctx.records_pending[1] = false;
 }
 
+
+// genetIC's grafic writer (io/grafic.hpp:160-200, GraficOutput::writeGrid) on one grid of the
+// grafic stack: for every cell (x, y, z) of the z-slabs [z0, z0 + nz), the particle of cell
+// (x, y, z) - roll of the (virtual) level (CenteredGrid's index map; roll = 0 for the other
+// grids), as the writer's floats: velocity * vel_factor, displacement * pos_factor
+// (getParticleNoOffset: the displacement, vel = displacement * velocityToOffsetRatio, in
+// double), the overdensity, and the cell's id + id_offset; every output [nz][n][n] with x
+// fastest, the order of a slab's record.  Sources: padded real fields of n^3.
+template <typename T, bool LPT2>
+__global__ void k_grafic_slabs(const T *__restrict__ px, const T *__restrict__ py, const T *__restrict__ pz,
+                               const T *__restrict__ qx, const T *__restrict__ qy, const T *__restrict__ qz,
+                               const T *__restrict__ delta, int n, int z0, int nz, int rx, int ry, int rz, double ratio,
+                               double vel_factor, double pos_factor, float *vel, float *pos, float *dlt,
+                               unsigned long long *ids, unsigned long long id_offset) {
+  const size_t m = (size_t)nz * n * n;
+  const size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= m) return;
+  const int x = (int)(o % n);
+  const size_t r = o / n;
+  const int y = (int)(r % n), z = z0 + (int)(r / n);
+  const int ux = ((x - rx) % n + n) % n, uy = ((y - ry) % n + n) % n, uz = ((z - rz) % n + n) % n;
+  const size_t src = ((size_t)ux * n + uy) * (size_t)(2 * (n / 2 + 1)) + uz;
+  if (vel || pos) {
+    const T *p[3] = {px, py, pz};
+    const T *q[3] = {qx, qy, qz};
+    for (int a = 0; a < 3; ++a) {
+      T d = p[a][src], v = d;
+      if (LPT2) {
+        const T e = q[a][src];
+        v = d + 2 * e;  // as the particle kernel forms the second-order velocity
+        d += e;
+      }
+      if (vel) vel[a * m + o] = (float)(((double)v * ratio) * vel_factor);
+      if (pos) pos[a * m + o] = (float)((double)d * pos_factor);
+    }
+  }
+  if (dlt) dlt[o] = (float)delta[src];
+  if (ids) ids[o] = id_offset + ((unsigned long long)ux * n + uy) * (unsigned long long)n + (unsigned long long)uz;
+}
+
 // Particles of a virtual grid over level L's region (genetIC's supersample / subsample):
 // factor > 1, (n factor)^3 cells whose displacements are the level's interpolated at
 // their centroids (SuperSampleEvaluator, evaluator.hpp:96-130: the tricubic of
@@ -371,6 +411,93 @@ static void resampled_typed(Context &ctx, const Level &L, int factor, double *ho
   ctx.pool.give(std::move(pos));
   ctx.pool.give(std::move(vel));
   ctx.pool.give(std::move(cen));
+}
+
+
+template <typename T>
+static void grafic_typed(Context &ctx, int level, const gic_grafic_grid &g, int z0, int nz, float *host_vel,
+                         float *host_pos, float *host_delta, unsigned long long *host_ids) {
+  Level &L = *ctx.levels[level];
+  if (host_delta) ensure_delta(ctx);
+  const bool lpt2 = L.have_lpt2;
+  const int f = g.factor, s = f > 1 ? f : (f < -1 ? -f : 1);
+  const bool super = f > 1, sub = f < -1;
+  const int n = super ? L.n * s : (sub ? L.n / s : L.n);
+  // the (virtual) grid's padded real fields: delta, psi (and psi2) of level L, interpolated
+  // tricubically (supersampled) or averaged over blocks (subsampled) as in particles of those grids
+  const int nsrc = lpt2 ? 7 : 4;
+  const T *src[7] = {L.field[0].as<T>(), L.field[1].as<T>(), L.field[2].as<T>(), L.field[3].as<T>(),
+                     L.field2[0].as<T>(), L.field2[1].as<T>(), L.field2[2].as<T>()};
+  std::unique_ptr<DevBuf> virt[7];
+  if (super || sub) {
+    Level V;
+    V.n = n;
+    V.box = L.box;
+    V.dx = L.box / n;
+    for (int a = 0; a < 3; ++a) V.x0[a] = L.x0[a];
+    V.periodic = L.periodic;
+    const size_t real = (size_t)n * n * 2 * (size_t)(n / 2 + 1), m = V.ncells();
+    T *dst[7];
+    for (int k = 0; k < nsrc; ++k) {
+      virt[k] = ctx.pool.take(real * sizeof(T));
+      dst[k] = virt[k]->as<T>();
+    }
+    for (int k = 0; k < nsrc; ++k) {
+      if (k == 0 && !host_delta) continue;
+      if (super) {
+        const T *one[1] = {src[k]};
+        T *out[1] = {dst[k]};
+        interp_add<T, 1>(ctx, L, one, V, out, true);
+      } else {
+        k_block_average<T><<<(unsigned)((m + 255) / 256), 256, 0, ctx.stream>>>(src[k], L.n, s, dst[k], n);
+        launched();
+      }
+    }
+    for (int k = 0; k < nsrc; ++k) src[k] = dst[k];
+  }
+  const size_t m = (size_t)nz * n * n;
+  auto dv = ctx.pool.take(std::max<size_t>(1, 7 * m) * sizeof(float));
+  auto di = ctx.pool.take(std::max<size_t>(1, m) * sizeof(unsigned long long));
+  float *vel = host_vel ? dv->as<float>() : nullptr, *pos = host_pos ? dv->as<float>() + 3 * m : nullptr,
+        *dl = host_delta ? dv->as<float>() + 6 * m : nullptr;
+  unsigned long long *id = host_ids ? di->as<unsigned long long>() : nullptr;
+  const double ratio = velocity_to_offset_ratio(ctx.cosmo);
+  const unsigned blocks = (unsigned)((m + 255) / 256);
+  if (lpt2)
+    k_grafic_slabs<T, true><<<blocks, 256, 0, ctx.stream>>>(src[1], src[2], src[3], src[4], src[5], src[6], src[0], n,
+                                                           z0, nz, g.roll[0], g.roll[1], g.roll[2], ratio, g.vel_factor,
+                                                           g.pos_factor, vel, pos, dl, id, g.id_offset);
+  else
+    k_grafic_slabs<T, false><<<blocks, 256, 0, ctx.stream>>>(src[1], src[2], src[3], nullptr, nullptr, nullptr, src[0],
+                                                            n, z0, nz, g.roll[0], g.roll[1], g.roll[2], ratio,
+                                                            g.vel_factor, g.pos_factor, vel, pos, dl, id, g.id_offset);
+  launched();
+  if (host_vel) GIC_CUDA(cudaMemcpyAsync(host_vel, vel, 3 * m * sizeof(float), cudaMemcpyDeviceToHost, ctx.stream));
+  if (host_pos) GIC_CUDA(cudaMemcpyAsync(host_pos, pos, 3 * m * sizeof(float), cudaMemcpyDeviceToHost, ctx.stream));
+  if (host_delta) GIC_CUDA(cudaMemcpyAsync(host_delta, dl, m * sizeof(float), cudaMemcpyDeviceToHost, ctx.stream));
+  if (host_ids)
+    GIC_CUDA(cudaMemcpyAsync(host_ids, id, m * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx.stream));
+  GIC_CUDA(cudaStreamSynchronize(ctx.stream));
+  for (auto &b : virt)
+    if (b) ctx.pool.give(std::move(b));
+  ctx.pool.give(std::move(dv));
+  ctx.pool.give(std::move(di));
+}
+
+void grafic_pack(Context &ctx, const gic_grafic_grid &g, int z0, int nz, float *host_vel, float *host_pos,
+                 float *host_delta, unsigned long long *host_ids) {
+  if (g.level < 0 || g.level >= (int)ctx.levels.size()) fail(GIC_ERR_INVALID_ARG, "no such level");
+  const Level &L = *ctx.levels[g.level];
+  if (!L.have_fields) fail(GIC_ERR_NOT_READY, "fields have not been computed");
+  const int f = g.factor;
+  if (f == 0 || f == -1 || (f < -1 && L.n % (-f)) || (f > 1 && (long long)L.n * f > 2048))
+    fail(GIC_ERR_INVALID_ARG, "factor must be 1, >= 2 (supersampled, at most 2048 cells per side) or <= -2 "
+                              "dividing the level's cells per side (subsampled)");
+  const int n = f > 1 ? L.n * f : (f < -1 ? L.n / -f : L.n);
+  if (z0 < 0 || nz < 0 || z0 + nz > n) fail(GIC_ERR_INVALID_ARG, "slab range outside the grid");
+  if (nz == 0) return;
+  if (ctx.dbl()) grafic_typed<double>(ctx, g.level, g, z0, nz, host_vel, host_pos, host_delta, host_ids);
+  else grafic_typed<float>(ctx, g.level, g, z0, nz, host_vel, host_pos, host_delta, host_ids);
 }
 
 void resampled_particles(Context &ctx, const Level &L, int factor, double *host_pos, double *host_vel) {

@@ -272,6 +272,30 @@ GIC_API int gic_gadget_pack(gic_ctx *ctx, const gic_particle_map *map, const int
                             unsigned long long count, float *pos_out, float *vel_out, unsigned long long *ids,
                             float *mass_out);
 
+/* ---- Grafic output (io::grafic::GraficOutput, genetIC/src/io/grafic.hpp:109-200) ----
+ * One grid of the grafic writer's stack (copyContextWithCenteredIntermediate): a level of
+ * the context (factor 1), its supersampled (factor >= 2) or subsampled (factor <= -2)
+ * virtual grid, seen through a CenteredGrid when roll is non-zero: output cell (x, y, z)
+ * is the grid's cell (x, y, z) - roll, periodically (roll = the CenteredGrid's integer
+ * offset; 0 for the OffsetGrid-wrapped finer levels, whose cells are not moved). */
+typedef struct gic_grafic_grid {
+  int level;
+  int factor;
+  int roll[3];
+  double vel_factor;            /* GraficOutput::velFactor, sqrt(a) */
+  double pos_factor;            /* GraficOutput::lengthFactorDisplacements, 1 */
+  unsigned long long id_offset; /* GraficOutput::iordOffset: cells of the grids written before */
+} gic_grafic_grid;
+/* writeGrid's per-cell values for the z-slabs [z0, z0 + nz) of that grid, as the file's
+ * records hold them (each slab [y][x], x fastest): vel = 3 arrays of nz n^2 floats
+ * (ic_velcx/y/z: velocity * vel_factor), pos = 3 such arrays (ic_poscx/y/z: displacement *
+ * pos_factor), delta (ic_deltab: the overdensity), ids (ic_particle_ids: cell id +
+ * id_offset).  NULL outputs are skipped.  The refinement mask and passive variable
+ * (ic_refmap, ic_pvar_*) stay genetIC's (GraficMask).  Fields must have been computed
+ * (gic_zeldovich); a virtual grid is evaluated per call, so pass all slabs at once. */
+GIC_API int gic_grafic_pack(gic_ctx *ctx, const gic_grafic_grid *grid, int z0, int nz, float *vel, float *pos,
+                            float *delta, unsigned long long *ids);
+
 /* Forward (dir=-1) or inverse (dir=+1) normalised 3-D real FFT of a level field
  * in place on the device (testing).  Replaces FieldFourierManager<T,T>::performTransform
  * (fourier.hpp:479-518). */

@@ -1133,6 +1133,28 @@ def matched_displacements(psi_fine, fine, psi_coarse, coarse, periodic):
     return out, nv, (cbox, nv, coff)
 
 
+def grafic_slabs(fields, box, n, offset, periodic, factor, roll, ratio, vel_factor, pos_factor, id_offset):
+    """genetIC's grafic writer on one grid of its stack (GraficOutput::writeGrid,
+    io/grafic.hpp:160-200): the level's fields (delta, psi_x, psi_y, psi_z) on the grid
+    (the level itself, or its supersampled / subsampled virtual grid), seen through a
+    CenteredGrid (virtualgrid.hpp:680-800: output cell (x, y, z) is the grid's cell
+    (x, y, z) - roll, periodically).  Per cell as the files hold them, each [z][y][x]:
+    velocities (psi * ratio * vel_factor, in double, then float), displacements
+    (psi * pos_factor), the overdensity, and ids (the grid cell's index + id_offset)."""
+    if factor == 1:
+        f, nv = list(fields), n
+    else:
+        f, nv = resample_displacements(fields, box, n, offset, periodic, factor)
+    idx = [(np.arange(nv) - roll[a]) % nv for a in range(3)]
+    # out[z][y][x] = field[ux][uy][uz]
+    pick = lambda a: a[np.ix_(idx[0], idx[1], idx[2])].transpose(2, 1, 0)
+    ux, uy, uz = np.meshgrid(idx[0], idx[1], idx[2], indexing='ij')
+    ids = (((ux.astype(np.uint64) * nv + uy) * nv + uz) + np.uint64(id_offset)).transpose(2, 1, 0)
+    vel = [(pick(p).astype(np.float64) * ratio * vel_factor).astype(np.float32) for p in f[1:]]
+    pos = [(pick(p).astype(np.float64) * pos_factor).astype(np.float32) for p in f[1:]]
+    return vel, pos, pick(f[0]).astype(np.float32), ids
+
+
 def tipsy_records(order, pos, vel, mass, eps, pos_factor, vel_factor, mass_factor):
     """Dark records (mass, x, y, z, vx, vy, vz, eps, phi) as float32 (tipsy.hpp:61-63,
     123-131): products and differences in double, then rounded to float."""

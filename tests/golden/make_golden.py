@@ -654,6 +654,58 @@ def ratio2_golden():
                             delta_chi2=np.array(dchi2))
 
 
+# genetIC's grafic writer: a 16^3 base of 50 Mpc/h written with one subsampled level below it
+# (`subsample 2`), a factor-4 zoom of 16 cells around a 5 Mpc/h sphere at the centre with its
+# intermediate factor-2 subsampled grid,
+# and the output centred on (30, 20, 25) (`center_output`: the coarse grids are rolled by whole
+# cells, the finer ones keep their cells); the geometry of genetIC's test_12_grafic at 16^3.
+GRAFIC = """subsample 2
+centre 25 25 25
+select_sphere 5
+zoomgrid 4 16
+centre 30 20 25
+center_output
+done
+"""
+GRAFIC_FILES = ('ic_velcx', 'ic_velcy', 'ic_velcz', 'ic_poscx', 'ic_poscy', 'ic_poscz', 'ic_deltab', 'ic_refmap',
+                'ic_particle_ids')
+
+
+def read_grafic(path, n, ids=False):
+    """A grafic file: the 44-byte header record, then n slabs of n^2 values (Fortran records)."""
+    raw = open(path, 'rb').read()
+    header = np.frombuffer(raw[4:48], np.uint8).copy()
+    item = 8 if ids else 4
+    rec = 8 + n * n * item
+    out = np.empty((n, n * n), dtype=np.uint64 if ids else np.float32)
+    for z in range(n):
+        o = 52 + z * rec
+        out[z] = np.frombuffer(raw[o + 4:o + 4 + n * n * item], np.uint64 if ids else np.float32)
+    return header, out.reshape(n, n, n)
+
+
+def grafic_goldens():
+    """The reference build's grafic files of the GRAFIC case (Fourier seeding): per grid of the
+    stack, its header and every record of each field, and the zoom's origin from the log."""
+    import re
+    with tempfile.TemporaryDirectory() as d:
+        write_camb(os.path.join(d, 'bbks.dat'), bbks_table())
+        body = MOD_BASE.replace('basegrid 50.0 32', 'basegrid 50.0 16').replace('outformat tipsy', 'outformat grafic')
+        open(os.path.join(d, 'paramfile.txt'), 'w').write(body + GRAFIC)
+        r = subprocess.run([REF_BIN, 'paramfile.txt'], cwd=d, check=True, capture_output=True, text=True)
+        log = r.stdout + r.stderr
+        origin = [int(v) for v in re.search(r'Low-left corner in parent grid = \((\d+), (\d+), (\d+)\)', log).groups()]
+        out = {'origin': np.array(origin)}
+        for eff in sorted(int(x.split('_')[-1]) for x in os.listdir(d) if x.startswith('out.grafic_')):
+            gd = os.path.join(d, 'out.grafic_%d' % eff)
+            n = int(np.frombuffer(open(os.path.join(gd, 'ic_velcx'), 'rb').read()[4:8], np.int32)[0])
+            for f in GRAFIC_FILES:
+                header, arr = read_grafic(os.path.join(gd, f), n, ids=f == 'ic_particle_ids')
+                out['g%d_%s' % (eff, f)] = arr
+            out['g%d_header' % eff] = header
+        np.savez_compressed(os.path.join(HERE, 'grafic_zoom.npz'), **out)
+
+
 def main():
     for mode, cmd in (('serial', 'random_seed_serial'), ('parallel', 'random_seed'), ('real', 'random_seed_real_space')):
         with tempfile.TemporaryDirectory() as d:
@@ -677,6 +729,7 @@ if __name__ == '__main__':
     main()
     geometry_goldens()
     ratio2_golden()
+    grafic_goldens()
     resample_goldens()
     strays_goldens()
     zoom_goldens()

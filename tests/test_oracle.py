@@ -539,3 +539,51 @@ def test_geometry_variance_oracle_matches_reference(bbks):
     for l in range(2):
         ref = g['delta%d' % l]
         assert np.abs(out[l][0] - ref).max() <= 1e-11 * np.abs(ref).max(), l
+
+
+# --- grafic output (io/grafic.hpp) -----------------------------------------------------
+
+@needs_reference
+def test_reference_build_reproduces_test_12_grafic(tmp_path):
+    """genetIC's own grafic fixture (test_12_grafic: subsampled base, intermediate and zoom
+    grids): the reference build here writes every file byte for byte."""
+    dst, _ = _run_reference(tmp_path, 'test_12_grafic')
+    ref = os.path.join(REF_TESTS, 'test_12_grafic', 'reference_grafic')
+    for d in sorted(os.listdir(ref)):
+        for f in sorted(os.listdir(os.path.join(ref, d))):
+            assert open(os.path.join(dst, d, f), 'rb').read() == open(os.path.join(ref, d, f), 'rb').read(), (d, f)
+
+
+# the grafic stack of tests/golden/grafic_zoom.npz (make_golden.py GRAFIC): effective resolution,
+# level, factor, CenteredGrid roll, first id
+GRAFIC_GRIDS = [(8, 0, -2, (0, 0, 0), 0), (16, 0, 1, (-1, 1, 0), 512), (32, 1, -2, (0, 0, 0), 4608),
+                (64, 1, 1, (0, 0, 0), 5120)]
+
+
+def grafic_oracle(bbks, cr_log=False):
+    from conftest import COSMO
+    g = _load_golden('grafic_zoom.npz')
+    o = [int(v) for v in g['origin']]
+    levels = [(50.0, 16, (0., 0., 0.)), (12.5, 16, tuple(o[a] * 50.0 / 16 for a in range(3)))]
+    fo.set_cr_log(cr_log)
+    w = fo.white_noise_levels([16, 16], 8896131, 2)
+    fo.set_cr_log(False)
+    fields = fo.zoom_realisation(w, levels, fo.CambPower(bbks, COSMO))
+    ratio = fo.velocity_to_offset_ratio(COSMO)
+    vf = np.sqrt(1.0 / (1.0 + COSMO['redshift']))
+    out = {}
+    for eff, l, fac, roll, off in GRAFIC_GRIDS:
+        box, n, offs = levels[l]
+        out[eff] = fo.grafic_slabs(fields[l], box, n, offs, 50.0, fac, roll, ratio, vf, 1.0, off)
+    return g, out
+
+
+def test_grafic_oracle_matches_reference_files(bbks):
+    """The writer's restatement (grafic_slabs) against the reference build's grafic files: the
+    centred and subsampled base grids, the intermediate and the zoom grid, every velocity,
+    displacement and overdensity record and every id, exactly."""
+    g, out = grafic_oracle(bbks)
+    for eff, (vel, pos, dl, ids) in out.items():
+        for k, arr in zip(('velcx', 'velcy', 'velcz', 'poscx', 'poscy', 'poscz', 'deltab'), vel + pos + [dl]):
+            assert np.array_equal(arr, g['g%d_ic_%s' % (eff, k)]), (eff, k)
+        assert np.array_equal(ids, g['g%d_ic_particle_ids' % eff]), eff
