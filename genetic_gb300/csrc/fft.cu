@@ -1125,7 +1125,15 @@ struct TmaColsShape {
   static constexpr int W = PAIRS ? TC + 2 : TC;              // values per row of a box
 };
 
-template <typename T, int L, int TC, int NCW, int SIGN, bool EXT, bool PAIRS>
+// SHUF (L = 512, 16 columns, 16 warps): the middle and last radix-8 stages run in registers,
+// exchanging through warp shuffles instead of the exchange tile.  Each group of 8 lanes holds
+// one column's butterflies 8q + s (q = lane in the group) of the middle stage; the last stage
+// needs output t of butterflies 8r + s in lane t, an 8 x 8 transpose done by three rounds of
+// pairwise swaps (__shfl_xor_sync 4, 2, 1).  The first stage writes the exchange tile with
+// its columns permuted by row / 8 (c ^ (row / 8 mod 16)), so that the middle stage's reads of
+// 8 rows 8 apart fall in different banks.  The arithmetic is the other variants' (same
+// radix schedule, twiddle indices and fused multiply-adds): the same bits.
+template <typename T, int L, int TC, int NCW, int SIGN, bool EXT, bool PAIRS, bool SHUF = false>
 __global__ void __launch_bounds__(NCW * 32, L >= 512 ? 1 : 2) k_fft_cols_tma(const __grid_constant__ CUtensorMap map,
                                                                             const TmaColsArgs<T> a) {
   using C = typename Cx<T>::type;
@@ -1210,7 +1218,10 @@ __global__ void __launch_bounds__(NCW * 32, L >= 512 ? 1 : 2) k_fft_cols_tma(con
         const int c = b % TC, j = b / TC;
         Dft<T, C, R>::run(v[p], SIGN);
 #pragma unroll
-        for (int r = 0; r < R; ++r) xt[(j * R + r) * TC + c] = v[p][r];
+        for (int r = 0; r < R; ++r) {
+          const int row = j * R + r;
+          xt[row * TC + (SHUF ? (c ^ ((row >> 3) & (TC - 1))) : c)] = v[p][r];
+        }
       }
     }
     __syncthreads();
@@ -1219,8 +1230,58 @@ __global__ void __launch_bounds__(NCW * 32, L >= 512 ? 1 : 2) k_fft_cols_tma(con
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       issue(k + 2);
     }
-    TileStagesUntil<T, L, TC, TC, NC, R, NSL, SIGN, 1>::run(xt, stw);
     C *base = a.data + off;
+    if constexpr (SHUF) {
+      static_assert(L == 512 && TC == 16 && NC == 512 && R == 8 && NSL == 64 && RL == 8,
+                    "the shuffle stages are laid out for 512-point columns, 16 per tile, 512 threads");
+      const int lane = ct & 31, w = ct >> 5, g = lane >> 3, q = lane & 7;
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {
+        const int u = p * 64 + w * 4 + g, c = u & 15, sm = u >> 4;
+        // middle stage (NS = 8): butterfly 8q + sm, positions 8q + sm + 64r
+        C v[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+          const int row = 8 * q + sm + 64 * r;
+          v[r] = xt[row * 16 + (c ^ ((row >> 3) & 15))];
+        }
+#pragma unroll
+        for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], twid(stw, r * sm * 8, SIGN));
+        Dft<T, C, 8>::run(v, SIGN);
+        // output r' of butterfly 8q + sm is position 64q + sm + 8r'; the last stage's butterfly
+        // sm + 8t reads positions sm + 8t + 64r: output t of butterfly 8r + sm
+#pragma unroll
+        for (int kb = 4; kb >= 1; kb >>= 1) {
+          const bool up = (q & kb) != 0;
+#pragma unroll
+          for (int e = 0; e < 8; ++e) {
+            if (e & kb) continue;
+            const C send = up ? v[e] : v[e | kb];
+            C recv;
+            recv.x = __shfl_xor_sync(0xffffffffu, send.x, kb);
+            recv.y = __shfl_xor_sync(0xffffffffu, send.y, kb);
+            if (up) v[e] = recv;
+            else v[e | kb] = recv;
+          }
+        }
+        // last stage (NS = 64): butterfly j = sm + 8q, positions j + 64r
+        const int j = sm + 8 * q;
+#pragma unroll
+        for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], twid(stw, r * j, SIGN));
+        Dft<T, C, 8>::run(v, SIGN);
+        if (c < tcv) {
+          C *out = base + (size_t)j * (size_t)a.B + c;
+          const size_t ostep = (size_t)64 * (size_t)a.B;
+#pragma unroll
+          for (int r = 0; r < 8; ++r) {
+            if (EXT && (j + r * 64 - a.sm0 + L) % L >= a.smn) continue;
+            out[r * ostep] = cscale(v[r], a.scale);
+          }
+        }
+      }
+      continue;
+    }
+    TileStagesUntil<T, L, TC, TC, NC, R, NSL, SIGN, 1>::run(xt, stw);
 #pragma unroll
     for (int p = 0; p < PERL; ++p) {
       const int b = ct + p * NC;
@@ -1255,11 +1316,13 @@ void set_smem(const void *fn, size_t bytes) {
 //   strided: (TC, threads) = FP32 (8, 256) | (16, 512) | fused (8, 512) | fused (16, 512),
 //            FP64 (4, 256) | (8, 256) | fused (4, 256) | fused (8, 128);
 //            then fused 8 (FP64: 4) columns with 3 or 4 CTAs per SM, and (256 <= N <= 512)
-//            the TMA-staged pass: 16 (FP64: 8) columns, 16 consumer warps at N = 512, 8 below
+//            the TMA-staged pass: 16 (FP64: 8) columns, 16 warps at N = 512, 8 below; the same
+//            with warp-shuffle middle and last stages (FP32, N = 512; else as candidate 6)
 //   rows:    (RPC, threads) = FP32 (8, 256) | (16, 256) | fused (16, 256) | (32, 512),
 //            FP64 (4, 256) | (8, 256) | fused (8, 256) | (16, 512)
 constexpr int kFixedCandidates = 4;  // row-pass candidates
-constexpr int kColsCandidates = 7;   // strided-pass candidates (4, 5: fused, 8 columns, 3 or 4 CTAs per SM; 6: TMA-staged)
+constexpr int kColsCandidates = 8;   // strided-pass candidates (4, 5: fused, 8 columns, 3 or 4 CTAs per SM; 6: TMA-staged;
+                                     // 7: TMA-staged with warp-shuffle stages)
 
 // cuTensorMapEncodeTiled, looked up once through the runtime (no link-time dependency on
 // the driver library); null when the driver does not provide it
@@ -1373,11 +1436,11 @@ struct FixedFft {
   // positions only (the fused pass loads just the window), an x pass with a multiplier,
   // an out-of-place source or an epilogue, or no tensor-map encoder
   static constexpr bool kTma = N >= 256 && N <= 512;
-  template <int SIGN, bool EXT, bool PAIRS>
+  template <int SIGN, bool EXT, bool PAIRS, bool SHUF = false>
   static void launch_tma(Context &ctx, const CUtensorMap &map, const TmaColsArgs<T> &args) {
     constexpr int TC = F32 ? 16 : 8, NCW = N >= 512 ? 16 : 8;
     using SH = TmaColsShape<N, TC, PAIRS>;
-    const void *fn = (const void *)k_fft_cols_tma<T, N, TC, NCW, SIGN, EXT, PAIRS>;
+    const void *fn = (const void *)k_fft_cols_tma<T, N, TC, NCW, SIGN, EXT, PAIRS, SHUF>;
     const size_t smem = 1024 + (2 * (size_t)SH::SLOT + (size_t)N * TC + N) * sizeof(C) + 2 * sizeof(uint64_t);
     static std::atomic<int> mask{0}, resident{0};
     set_smem_once(fn, smem, mask);
@@ -1390,11 +1453,13 @@ struct FixedFft {
     GIC_CUDA(cudaGetDevice(&dev));
     GIC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     const int grid = std::min(args.ntiles, resident.load() * nsm);
-    k_fft_cols_tma<T, N, TC, NCW, SIGN, EXT, PAIRS><<<grid, NCW * 32, smem, ctx.stream>>>(map, args);
+    k_fft_cols_tma<T, N, TC, NCW, SIGN, EXT, PAIRS, SHUF><<<grid, NCW * 32, smem, ctx.stream>>>(map, args);
     launched();
   }
+  // SHUF: the variant with warp-shuffle middle and last stages (FP32, N = 512)
+  static constexpr bool kShuf = F32 && N == 512;
   static bool cols_tma(Context &ctx, int sign, C *d, int A, long long B, const C *tw, T scale, const T *tab, int a0,
-                       int na, int m0, int mn, const C *src, C *dst, const C *xsrc, const T *xtab) {
+                       int na, int m0, int mn, const C *src, C *dst, const C *xsrc, const T *xtab, bool shuf = false) {
     if constexpr (!kTma) {
       return false;
     } else {
@@ -1444,6 +1509,18 @@ struct FixedFft {
       args.wait_cycles = 1ll << 31;
       if (args.ntiles <= 0) return true;
       const bool ext = sign > 0 && mn < N;
+      if constexpr (kShuf) {
+        if (shuf) {
+          if (pairs) {
+            if (sign > 0) ext ? launch_tma<+1, true, true, true>(ctx, map, args) : launch_tma<+1, false, true, true>(ctx, map, args);
+            else ext ? launch_tma<-1, true, true, true>(ctx, map, args) : launch_tma<-1, false, true, true>(ctx, map, args);
+          } else {
+            if (sign > 0) ext ? launch_tma<+1, true, false, true>(ctx, map, args) : launch_tma<+1, false, false, true>(ctx, map, args);
+            else ext ? launch_tma<-1, true, false, true>(ctx, map, args) : launch_tma<-1, false, false, true>(ctx, map, args);
+          }
+          return true;
+        }
+      }
       if (pairs) {
         if constexpr (F32) {
           if (sign > 0) ext ? launch_tma<+1, true, true>(ctx, map, args) : launch_tma<+1, false, true>(ctx, map, args);
@@ -1464,9 +1541,10 @@ struct FixedFft {
                        const T *tab = nullptr, int a0 = 0, int na = -1, int m0 = 0, int mn = N,
                        const C *src = nullptr, C *dst = nullptr, const C *xsrc = nullptr, const T *xtab = nullptr) {
     if (na < 0) na = A;
-    if (cfg == 6) {
-      // TMA-staged, else the fused 16- (FP64: 8-) column pass
-      if (cols_tma(ctx, sign, d, A, B, tw, scale, tab, a0, na, m0, mn, src, dst, xsrc, xtab)) return;
+    if (cfg == 6 || cfg == 7) {
+      // TMA-staged (7: with warp-shuffle middle and last stages where built), else the fused
+      // 16- (FP64: 8-) column pass
+      if (cols_tma(ctx, sign, d, A, B, tw, scale, tab, a0, na, m0, mn, src, dst, xsrc, xtab, cfg == 7)) return;
       cfg = 3;
     }
     if (cfg == 4) {

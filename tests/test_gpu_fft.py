@@ -52,7 +52,7 @@ def test_fft_passes_bit_identical_across_tiles(built, bbks, precision, n, monkey
     are explicit fused multiply-adds)."""
     out = {}
     for tile in ('generic', '0,0', '1,1', '2,2', '3,3', '0,2', '2,0', '1,3', '3,3,0', '1,2,1', '0,1,2', '4,1', '5,3',
-                 '6,3', '6,0', '6,2,1'):
+                 '6,3', '6,0', '6,2,1', '7,1'):
         monkeypatch.setenv('GIC_FFT_TILE', tile)
         _, reals, back = _noise_roundtrip(precision, n, bbks)
         out[tile] = (reals, back)
@@ -92,7 +92,7 @@ def test_plane_pass_bit_identical_512(built, bbks, precision, monkeypatch):
     in every lag variant, for 512^3 in both precisions."""
     monkeypatch.setenv('GIC_FFT_TILE', '3,3')
     ref = _roundtrip_raw(precision, 512, bbks, 11)
-    for tile in ('1,0', '3,3,0', '3,3,1', '3,3,2', '4,1', '5,1', '6,1', '6,3', '6,3,0'):
+    for tile in ('1,0', '3,3,0', '3,3,1', '3,3,2', '4,1', '5,1', '6,1', '6,3', '6,3,0', '7,1', '7,3', '7,3,1'):
         monkeypatch.setenv('GIC_FFT_TILE', tile)
         raw, back = _roundtrip_raw(precision, 512, bbks, 11)
         assert np.array_equal(raw, ref[0]), tile
@@ -175,3 +175,27 @@ def test_tma_pass_bit_identical_in_the_modification_algebra(built, bbks, precisi
         assert np.array_equal(x, y)
     for (p, v), (p2, v2) in zip(a[2], b[2]):
         assert np.array_equal(p, p2) and np.array_equal(v, v2)
+
+
+@pytest.mark.parametrize('precision', ['mixed'])
+def test_shuffle_pass_box_inverse_512(built, bbks, precision, monkeypatch):
+    """The TMA-staged pass with warp-shuffle stages (candidate 7, 512^3 FP32) on a box-restricted
+    inverse transform (store windows on x and y) gives the fused pass's bits inside the box."""
+    from genetic_gb300.generator import _ptr
+    n = 512
+    rng = np.random.default_rng(3)
+    spec = np.ascontiguousarray(rng.standard_normal((n, n, n // 2 + 1, 2)))
+    start = np.array([500, 37, 5], dtype=np.int32)
+    length = np.array([40, 100, 512], dtype=np.int32)
+    out = {}
+    for tile in ('3,3', '7,3'):
+        monkeypatch.setenv('GIC_FFT_TILE', tile)
+        gen = make_generator(precision, bbks, [('base', 100.0, n)], 7, 'random_seed')
+        gen._call('gic_set_noise', 0, _ptr(spec))
+        gen._call('gic_fft_box', 0, 0, +1, _ptr(start), _ptr(length))
+        raw = gen.noise(0)
+        gen.close()
+        real = np.stack([raw.real, raw.imag], -1).reshape(n, n, -1)[:, :, :n]
+        ix = [(start[a] + np.arange(length[a])) % n for a in range(3)]
+        out[tile] = real[np.ix_(ix[0], ix[1], ix[2])]
+    assert np.array_equal(out['3,3'], out['7,3'])
