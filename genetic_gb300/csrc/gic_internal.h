@@ -276,6 +276,9 @@ struct ModRequest {
   std::shared_ptr<DevBuf> dcells;
   CellBox box;
   bool have_box = false;
+  // the list position of every cell of `box` (-1 where not flagged), when the box is small
+  // enough to hold one: the localisation kernels' lookups
+  std::shared_ptr<DevBuf> dmap;
   double centre[3] = {0, 0, 0};
   bool have_centre = false;
 };

@@ -637,6 +637,38 @@ __global__ void k_center_cells(T *v, size_t count) {
 // the reference's bits (the mixed form rounds that sum once) and nothing depends on
 // thread scheduling.  cells: sorted, unique.
 
+// The list position of a cell: from a dense map of the flagged cells' box (start, len per
+// axis, cyclic on n cells; -1 = not flagged, and every cell outside the box is unflagged),
+// or, without a map, by binary search of the sorted list.
+struct FlagLookup {
+  const int *map;
+  int n, start[3], len[3];
+};
+__device__ __forceinline__ long long find_flagged(const unsigned long long *cells, size_t count,
+                                                  unsigned long long id);
+__device__ __forceinline__ long long find_flagged(const FlagLookup &fl, const unsigned long long *cells, size_t count,
+                                                  unsigned long long id) {
+  if (!fl.map) return find_flagged(cells, count, id);
+  const int n = fl.n;
+  const int p[3] = {(int)(id / ((unsigned long long)n * n)), (int)((id / n) % n), (int)(id % n)};
+  int o[3];
+  for (int a = 0; a < 3; ++a) {
+    o[a] = ((p[a] - fl.start[a]) % n + n) % n;
+    if (o[a] >= fl.len[a]) return -1;
+  }
+  return fl.map[((size_t)o[0] * fl.len[1] + o[1]) * fl.len[2] + o[2]];
+}
+__global__ void k_flag_map(const unsigned long long *cells, size_t count, FlagLookup fl, int *map) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const unsigned long long id = cells[i];
+  const int n = fl.n;
+  const int p[3] = {(int)(id / ((unsigned long long)n * n)), (int)((id / n) % n), (int)(id % n)};
+  int o[3];
+  for (int a = 0; a < 3; ++a) o[a] = ((p[a] - fl.start[a]) % n + n) % n;
+  map[((size_t)o[0] * fl.len[1] + o[1]) * fl.len[2] + o[2]] = (int)i;
+}
+
 // the list position of cell id, or -1
 __device__ __forceinline__ long long find_flagged(const unsigned long long *cells, size_t count,
                                                   unsigned long long id) {
@@ -663,39 +695,38 @@ __device__ __forceinline__ size_t padded_at(unsigned long long id, int n) {
 // gradient stencil along dir with values a, b, -b, -a at -2, -1, +1, +2 (VelocityModification)
 template <typename T>
 __global__ void k_localise(T *real, int n, const unsigned long long *cells, size_t count, int kind, int dir,
-                           double w, double a, double b) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= count) return;
-  const unsigned long long q = cells[i];
+                           double w, double a, double b, FlagLookup fl) {
+  // kind 0: a thread per flagged cell; kind 1: a thread per (flagged cell, stencil position)
+  const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (kind == 0) {
-    real[padded_at(q, n)] = (T)w;
+    if (tid < count) real[padded_at(cells[tid], n)] = (T)w;
     return;
   }
+  const size_t i = tid >> 2;
+  const int k = (int)(tid & 3);
+  if (i >= count) return;
+  const unsigned long long q = cells[i];
   const int off[4] = {-2, -1, 1, 2};
   const double val[4] = {a, b, -b, -a};
-  for (int k = 0; k < 4; ++k) {
-    const unsigned long long t = step_cell(q, n, dir, off[k]);
-    // every contribution to t: the flagged cell -off[k2] away, its stencil value k2
-    long long ci[4];
-    int ck[4], nc = 0;
-    bool first = true;
-    for (int k2 = 0; k2 < 4 && first; ++k2) {
-      const long long i2 = find_flagged(cells, count, step_cell(t, n, dir, -off[k2]));
-      if (i2 < 0) continue;
-      if (i2 < (long long)i || (i2 == (long long)i && k2 < k)) first = false;
-      ci[nc] = i2;
-      ck[nc++] = k2;
-    }
-    if (!first) continue;
-    for (int u = 1; u < nc; ++u)  // by (list position, stencil position)
-      for (int v = u; v > 0 && (ci[v] < ci[v - 1] || (ci[v] == ci[v - 1] && ck[v] < ck[v - 1])); --v) {
-        const long long ti = ci[v]; ci[v] = ci[v - 1]; ci[v - 1] = ti;
-        const int tk = ck[v]; ck[v] = ck[v - 1]; ck[v - 1] = tk;
-      }
-    double acc = 0;  // the reference's double sum; rounded once in the mixed form
-    for (int u = 0; u < nc; ++u) acc += val[ck[u]];
-    real[padded_at(t, n)] = (T)acc;
+  const unsigned long long t = step_cell(q, n, dir, off[k]);
+  // every contribution to t: the flagged cell -off[k2] away, its stencil value k2
+  long long ci[4];
+  int ck[4], nc = 0;
+  for (int k2 = 0; k2 < 4; ++k2) {
+    const long long i2 = find_flagged(fl, cells, count, step_cell(t, n, dir, -off[k2]));
+    if (i2 < 0) continue;
+    if (i2 < (long long)i || (i2 == (long long)i && k2 < k)) return;  // an earlier contribution writes t
+    ci[nc] = i2;
+    ck[nc++] = k2;
   }
+  for (int u = 1; u < nc; ++u)  // by (list position, stencil position)
+    for (int v = u; v > 0 && (ci[v] < ci[v - 1] || (ci[v] == ci[v - 1] && ck[v] < ck[v - 1])); --v) {
+      const long long ti = ci[v]; ci[v] = ci[v - 1]; ci[v - 1] = ti;
+      const int tk = ck[v]; ck[v] = ck[v - 1]; ck[v - 1] = tk;
+    }
+  double acc = 0;  // the reference's double sum; rounded once in the mixed form
+  for (int u = 0; u < nc; ++u) acc += val[ck[u]];
+  real[padded_at(t, n)] = (T)acc;
 }
 
 // angular-momentum localisation covector (AngMomentumModification::calculateLocalisationCovector,
@@ -706,8 +737,10 @@ __global__ void k_localise(T *real, int n, const unsigned long long *cells, size
 template <typename T>
 __global__ void k_localise_am(T *real, int n, const unsigned long long *cells, size_t count, int dir, double dx,
                               double x0, double y0, double z0, double cx, double cy, double cz, double period,
-                              double a, double b) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+                              double a, double b, FlagLookup fl) {
+  // a thread per (flagged cell, axis, stencil position)
+  const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t i = tid >> 3;
   if (i >= count) return;
   const int d1 = (dir + 1) % 3, d2 = (dir + 2) % 3;
   const int axes[2] = {d1 < d2 ? d1 : d2, d1 < d2 ? d2 : d1};
@@ -726,40 +759,35 @@ __global__ void k_localise_am(T *real, int n, const unsigned long long *cells, s
   };
   const int off[4] = {-2, -1, 1, 2};
   const unsigned long long q = cells[i];
-  for (int xa = 0; xa < 2; ++xa) {
-    const int ax = axes[xa];
-    for (int k = 0; k < 4; ++k) {
-      const unsigned long long t = step_cell(q, n, ax, off[k]);
-      long long ci[8];
-      int cx2[8], ck[8], nc = 0;
-      bool first = true;
-      for (int xb = 0; xb < 2 && first; ++xb)
-        for (int k2 = 0; k2 < 4 && first; ++k2) {
-          const long long i2 = find_flagged(cells, count, step_cell(t, n, axes[xb], -off[k2]));
-          if (i2 < 0) continue;
-          if (i2 < (long long)i || (i2 == (long long)i && (xb < xa || (xb == xa && k2 < k)))) first = false;
-          ci[nc] = i2;
-          cx2[nc] = xb;
-          ck[nc++] = k2;
-        }
-      if (!first) continue;
-      for (int u = 1; u < nc; ++u)  // by (list position, axis, stencil position)
-        for (int v = u; v > 0; --v) {
-          const bool before = ci[v] < ci[v - 1] || (ci[v] == ci[v - 1] && (cx2[v] < cx2[v - 1] ||
-                                                                          (cx2[v] == cx2[v - 1] && ck[v] < ck[v - 1])));
-          if (!before) break;
-          const long long ti = ci[v]; ci[v] = ci[v - 1]; ci[v - 1] = ti;
-          const int tx = cx2[v]; cx2[v] = cx2[v - 1]; cx2[v - 1] = tx;
-          const int tk = ck[v]; ck[v] = ck[v - 1]; ck[v - 1] = tk;
-        }
-      double acc = 0;  // the reference's double sum; rounded once in the mixed form
-      for (int u = 0; u < nc; ++u) {
-        const double c = coeff(cells[ci[u]], axes[cx2[u]]);
-        acc += ck[u] == 0 ? c * a : ck[u] == 1 ? c * b : ck[u] == 2 ? -(c * b) : -(c * a);
-      }
-      real[padded_at(t, n)] = (T)acc;
+  const int xa = (int)((tid >> 2) & 1), k = (int)(tid & 3);
+  const unsigned long long t = step_cell(q, n, axes[xa], off[k]);
+  // every contribution to t, unless an earlier one (in the reference's order) writes it
+  long long ci[8];
+  int cx2[8], ck[8], nc = 0;
+  for (int xb = 0; xb < 2; ++xb)
+    for (int k2 = 0; k2 < 4; ++k2) {
+      const long long i2 = find_flagged(fl, cells, count, step_cell(t, n, axes[xb], -off[k2]));
+      if (i2 < 0) continue;
+      if (i2 < (long long)i || (i2 == (long long)i && (xb < xa || (xb == xa && k2 < k)))) return;
+      ci[nc] = i2;
+      cx2[nc] = xb;
+      ck[nc++] = k2;
     }
+  for (int u = 1; u < nc; ++u)  // by (list position, axis, stencil position)
+    for (int v = u; v > 0; --v) {
+      const bool before = ci[v] < ci[v - 1] ||
+                          (ci[v] == ci[v - 1] && (cx2[v] < cx2[v - 1] || (cx2[v] == cx2[v - 1] && ck[v] < ck[v - 1])));
+      if (!before) break;
+      const long long ti = ci[v]; ci[v] = ci[v - 1]; ci[v - 1] = ti;
+      const int tx = cx2[v]; cx2[v] = cx2[v - 1]; cx2[v - 1] = tx;
+      const int tk = ck[v]; ck[v] = ck[v - 1]; ck[v - 1] = tk;
+    }
+  double acc = 0;  // the reference's double sum; rounded once in the mixed form
+  for (int u = 0; u < nc; ++u) {
+    const double c = coeff(cells[ci[u]], axes[cx2[u]]);
+    acc += ck[u] == 0 ? c * a : ck[u] == 1 ? c * b : ck[u] == 2 ? -(c * b) : -(c * a);
   }
+  real[padded_at(t, n)] = (T)acc;
 }
 
 // cosmology::densityToPotential (cosmology/parameters.hpp:209-225): times -prefac / k^2.
@@ -2193,6 +2221,24 @@ struct ModEngine {
       m.box = cells_box(flagged, count, lev(F).n, 2);
       m.have_box = true;
     }
+    FlagLookup fl{};
+    fl.n = lev(F).n;
+    for (int a = 0; a < 3; ++a) {
+      fl.start[a] = m.box.start[a];
+      fl.len[a] = m.box.len[a];
+    }
+    const size_t box_cells = (size_t)fl.len[0] * fl.len[1] * fl.len[2];
+    if (kind != 0 && box_cells <= (size_t)1 << 26) {
+      if (!m.dmap) {
+        m.dmap = std::make_shared<DevBuf>();
+        m.dmap->ensure(box_cells * sizeof(int));
+        GIC_CUDA(cudaMemsetAsync(m.dmap->ptr, 0xff, box_cells * sizeof(int), ctx.stream));
+        k_flag_map<<<nblk(count), 256, 0, ctx.stream>>>(m.dcells->template as<unsigned long long>(), count, fl,
+                                                        m.dmap->template as<int>());
+        launched();
+      }
+      fl.map = m.dmap->template as<int>();
+    }
     // a level's real covector is read inside its support only when its transform is
     // box-restricted: then only the support's x planes are zeroed
     if (fft_prunes(ctx, lev(F).n)) zero_planes(ptr(out, F), F, m.box);
@@ -2227,14 +2273,15 @@ struct ModEngine {
       }
       const double *cen = m.centre;
       const double norm = (double)count * Lf.dx;
-      k_localise_am<T><<<nblk(count), 256, 0, ctx.stream>>>(ptr(out, F), Lf.n, dcells,
+      k_localise_am<T><<<nblk(8 * count), 256, 0, ctx.stream>>>(ptr(out, F), Lf.n, dcells,
                                                            count, kind - GIC_MOD_LX, Lf.dx, Lf.x0[0], Lf.x0[1], Lf.x0[2],
-                                                           cen[0], cen[1], cen[2], P, 1. / 12. / norm, -2. / 3. / norm);
+                                                           cen[0], cen[1], cen[2], P, 1. / 12. / norm, -2. / 3. / norm,
+                                                           fl);
     } else {
       const bool vel = kind >= GIC_MOD_VX && kind <= GIC_MOD_VZ;
       double a = -w / 12. / lev(F).dx, b = w * 2. / 3. / lev(F).dx;
-      k_localise<T><<<nblk(count), 256, 0, ctx.stream>>>(ptr(out, F), lev(F).n, dcells,
-                                                        count, vel ? 1 : 0, vel ? kind - GIC_MOD_VX : 0, w, a, b);
+      k_localise<T><<<nblk(vel ? 4 * count : count), 256, 0, ctx.stream>>>(ptr(out, F), lev(F).n, dcells,
+                                                        count, vel ? 1 : 0, vel ? kind - GIC_MOD_VX : 0, w, a, b, fl);
     }
     launched();
     // the reference transforms the localisation covector to Fourier space and back
