@@ -19,6 +19,7 @@
 #include <atomic>
 #include <cstring>
 #include <mutex>
+#include <new>
 #include <thread>
 
 struct gic_batch {
@@ -349,6 +350,9 @@ GIC_API int gic_batch_realise(gic_batch *b, const unsigned long *seeds, const in
       } catch (const gic::Error &e) {
         gic::release_graph(*b);
         b->graph_off = e.msg.empty() ? "stream capture failed" : e.msg;
+      } catch (const std::exception &e) {
+        gic::release_graph(*b);
+        b->graph_off = e.what();
       }
     }
     for (auto *c : b->ctxs)
@@ -362,6 +366,12 @@ GIC_API int gic_batch_realise(gic_batch *b, const unsigned long *seeds, const in
   } catch (const gic::Error &e) {
     b->last_error = e.msg;
     return e.code;
+  } catch (const std::bad_alloc &) {
+    b->last_error = "host allocation failed";
+    return GIC_ERR_OOM;
+  } catch (const std::exception &e) {
+    b->last_error = e.what();
+    return GIC_ERR_INTERNAL;
   }
   return GIC_OK;
 }
