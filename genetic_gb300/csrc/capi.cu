@@ -228,6 +228,9 @@ int gic_create(gic_ctx **out, const gic_device_opts *opts) {
       c->impl.fft.force_planes = got == 3 && p >= 0 ? p : -1;
     }
   }
+  // GIC_FFT_COLTAB=0: the x passes read their per-|k|^2 multipliers from the tables
+  // themselves instead of the per-coefficient layouts (the same values)
+  if (const char *t = std::getenv("GIC_FFT_COLTAB")) c->impl.fft.col_tables = std::strcmp(t, "0") != 0;
   *out = c;
   return GIC_OK;
 }
@@ -314,7 +317,7 @@ int gic_level_add(gic_ctx *ctx, double box, int n, double x0, double y0, double 
   L->dx = box / n;
   L->periodic = C.levels.empty() ? box : C.levels[0]->periodic;
   C.levels.push_back(std::move(L));
-  C.table_cache.clear();
+  C.clear_table_cache();
   if (level_id) *level_id = (int)C.levels.size() - 1;
   API_END
 }
@@ -331,7 +334,7 @@ int gic_set_cosmology(gic_ctx *ctx, const gic_cosmo *cosmo) {
   C.cosmo.z = cosmo->redshift;
   C.cosmo.a = 1. / (cosmo->redshift + 1.);
   C.have_cosmo = true;
-  C.table_cache.clear();
+  C.clear_table_cache();
   API_END
 }
 

@@ -17,6 +17,7 @@
 // in the working precision.
 #include "gic_internal.h"
 #include <cuda.h>
+#include <type_traits>
 #include <cmath>
 #include <algorithm>
 #include <atomic>
@@ -70,6 +71,25 @@ __device__ __forceinline__ TT qtab(const TT *tab, int N, int kx, long long col) 
   const long long a = kx > H ? kx - N : kx, b = ky > H ? ky - N : ky;
   return tab[a * a + b * b + (long long)kz * kz];
 }
+
+// The multiplier of a fixed-length x pass: the per-|k|^2 table q, and optionally the
+// same values laid out per coefficient, col[f][c] = q[|k|^2] for kx = f or N - f
+// (f <= N/2) and half-spectrum column c = ky (N/2 + 1) + kz.  Along a tile's columns
+// the per-coefficient values are contiguous, where the per-|k|^2 ones are a gather
+// (the index steps by 2 kz + 1, a 32-byte sector per value).
+template <typename TT>
+struct XTab {
+  const TT *q = nullptr;
+  const TT *col = nullptr;
+  __host__ __device__ explicit operator bool() const { return q != nullptr; }
+  __device__ __forceinline__ TT at(int N, int kx, long long c) const {
+    if (col) {
+      const int f = kx > N / 2 ? N - kx : kx;
+      return col[(size_t)f * (size_t)N * (size_t)(N / 2 + 1) + (size_t)c];
+    }
+    return qtab(q, N, kx, c);
+  }
+};
 
 template <typename T, typename C, int R> struct Dft;
 template <typename T, typename C> struct Dft<T, C, 2> {
@@ -522,10 +542,10 @@ struct TileStages<T, L, TC, TCP, NT, NS, SIGN, TWM, true> {
 // the inputs when SIGN > 0 (c2r) and to the scaled outputs when SIGN < 0 (r2c)
 template <typename T, int L, int TC, int NT, int SIGN>
 __global__ void __launch_bounds__(NT) k_fft_cols(typename Cx<T>::type *data, long long B,
-                                                 const typename Cx<T>::type *tw, T scale, const T *tab, int a0,
+                                                 const typename Cx<T>::type *tw, T scale, XTab<T> tab, int a0,
                                                  int A, int m0, int mn, const typename Cx<T>::type *src,
                                                  typename Cx<T>::type *dst, const typename Cx<T>::type *xsrc,
-                                                 const T *xtab) {
+                                                 XTab<T> xtab) {
   using C = typename Cx<T>::type;
   constexpr int TCP = TC + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -554,7 +574,7 @@ __global__ void __launch_bounds__(NT) k_fft_cols(typename Cx<T>::type *data, lon
   if (SIGN > 0 && tab) {
     for (int e = threadIdx.x; e < L * tcv; e += NT) {
       const int i = e / tcv, c = e % tcv;
-      tile[i * TCP + c] = cscale(tile[i * TCP + c], qtab(tab, L, i, b0 + c));
+      tile[i * TCP + c] = cscale(tile[i * TCP + c], tab.at(L, i, b0 + c));
     }
     __syncthreads();
   }
@@ -563,11 +583,11 @@ __global__ void __launch_bounds__(NT) k_fft_cols(typename Cx<T>::type *data, lon
     const int i = e / TC, c = e % TC;
     if (c < tcv && (i - sm0 + L) % L < smn) {
       C v = cscale(tile[i * TCP + c], scale);
-      if (SIGN < 0 && tab) v = cscale(v, qtab(tab, L, i, b0 + c));
+      if (SIGN < 0 && tab) v = cscale(v, tab.at(L, i, b0 + c));
       const size_t at = (size_t)i * (size_t)B + c;
       if (dst) {
         const size_t off = (size_t)(base - data);
-        dst[off + at] = cadd(cscale(xsrc[off + at], qtab(xtab, L, i, b0 + c)), v);
+        dst[off + at] = cadd(cscale(xsrc[off + at], xtab.at(L, i, b0 + c)), v);
       } else {
         base[at] = v;
       }
@@ -611,9 +631,21 @@ struct TileStagesUntil<T, L, TC, TCP, NT, NS, STOP, SIGN, TWM, true> {
   static __device__ __forceinline__ void run(typename Cx<T>::type *, const typename Cx<T>::type *) {}
 };
 
-// first stage (NS = 1, no twiddles): inputs from `in(c, position)`, outputs to the tile
-template <typename T, int L, int TC, int NT, int SIGN, class In>
-__device__ __forceinline__ void first_stage_from(typename Cx<T>::type *tile, const In &in) {
+// no multiplier between a first stage's loads and its butterflies
+struct NoMid {
+  static constexpr bool kActive = false;
+  __device__ __forceinline__ void wait() const {}
+  template <typename C>
+  __device__ __forceinline__ C operator()(int, int, C v) const {
+    return v;
+  }
+};
+
+// first stage (NS = 1, no twiddles): inputs from `in(c, position)`, outputs to the tile.
+// With an active `mid`, every thread's loads are issued first, then mid.wait() (a block
+// barrier: all threads reach it), then each input becomes mid(c, position, value).
+template <typename T, int L, int TC, int NT, int SIGN, class In, class Mid = NoMid>
+__device__ __forceinline__ void first_stage_from(typename Cx<T>::type *tile, const In &in, const Mid &mid = Mid{}) {
   using C = typename Cx<T>::type;
   constexpr int R = next_radix(L, 1), LR = L / R, NB = LR * TC, PER = (NB + NT - 1) / NT;
   C v[PER][R];
@@ -624,6 +656,18 @@ __device__ __forceinline__ void first_stage_from(typename Cx<T>::type *tile, con
       const int c = b % TC, j = b / TC;
 #pragma unroll
       for (int r = 0; r < R; ++r) v[p][r] = in(c, j + r * LR);
+    }
+  }
+  if constexpr (Mid::kActive) {
+    mid.wait();
+#pragma unroll
+    for (int p = 0; p < PER; ++p) {
+      const int b = threadIdx.x + p * NT;
+      if (NB % NT == 0 || b < NB) {
+        const int c = b % TC, j = b / TC;
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[p][r] = mid(c, j + r * LR, v[p][r]);
+      }
     }
   }
 #pragma unroll
@@ -639,6 +683,18 @@ __device__ __forceinline__ void first_stage_from(typename Cx<T>::type *tile, con
   __syncthreads();
 }
 
+// An output functor with `kPrefetch` reads a value per output (`prefetch(c, position)`)
+// that `put(c, position, value, prefetched)` combines with the result: the last stage
+// issues those loads before its butterflies, so no store waits on a load behind it.
+template <class O, class = void>
+struct HasPrefetch {
+  static constexpr bool value = false;
+};
+template <class O>
+struct HasPrefetch<O, std::void_t<decltype(O::kPrefetch)>> {
+  static constexpr bool value = O::kPrefetch;
+};
+
 // last stage: inputs from the tile, outputs to `out(c, position, value)`
 template <typename T, int L, int TC, int NT, int SIGN, int TWM, class Out>
 __device__ __forceinline__ void last_stage_to(const typename Cx<T>::type *tile, const typename Cx<T>::type *tw,
@@ -651,13 +707,26 @@ __device__ __forceinline__ void last_stage_to(const typename Cx<T>::type *tile, 
     const int b = threadIdx.x + p * NT;
     if (NB % NT == 0 || b < NB) {
       const int c = b % TC, j = b / TC;
+      if constexpr (HasPrefetch<Out>::value) {
+        C x[R];
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[p][r] = tile[(j + r * LR) * TC + c];
+        for (int r = 0; r < R; ++r) x[r] = out.prefetch(c, j + r * NS);
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[p][r] = cmul(v[p][r], twid(tw, TWM * r * j * (L / (NS * R)), SIGN));
-      Dft<T, C, R>::run(v[p], SIGN);
+        for (int r = 0; r < R; ++r) v[p][r] = tile[(j + r * LR) * TC + c];
 #pragma unroll
-      for (int r = 0; r < R; ++r) out(c, j + r * NS, v[p][r]);
+        for (int r = 1; r < R; ++r) v[p][r] = cmul(v[p][r], twid(tw, TWM * r * j * (L / (NS * R)), SIGN));
+        Dft<T, C, R>::run(v[p], SIGN);
+#pragma unroll
+        for (int r = 0; r < R; ++r) out.put(c, j + r * NS, v[p][r], x[r]);
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[p][r] = tile[(j + r * LR) * TC + c];
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[p][r] = cmul(v[p][r], twid(tw, TWM * r * j * (L / (NS * R)), SIGN));
+        Dft<T, C, R>::run(v[p], SIGN);
+#pragma unroll
+        for (int r = 0; r < R; ++r) out(c, j + r * NS, v[p][r]);
+      }
     }
   }
 }
@@ -680,7 +749,7 @@ struct ColsIn {
   const C *base;
   long long B;
   int tcv;
-  const decltype(C::x) *tab;  // optional multiplier (x pass of an L^3 grid), field precision
+  XTab<decltype(C::x)> tab;  // optional multiplier (x pass of an L^3 grid), field precision
   int L;
   long long b0;
   int m0 = 0, mn = 1 << 30;
@@ -695,16 +764,17 @@ struct ColsIn {
     }
     const C *p = from + (size_t)m * (size_t)B + c;
     C v = CG ? __ldcg(p) : *p;
-    return tab ? cscale(v, qtab(tab, L, m, b0 + c)) : v;
+    return tab ? cscale(v, tab.at(L, m, b0 + c)) : v;
   }
 };
-template <typename C, typename T>
+// PF: the epilogue's source values are prefetched by the last stage (kPrefetch)
+template <typename C, typename T, bool PF = false>
 struct ColsOut {
   C *base;
   long long B;
   int tcv;
   T scale;
-  const T *tab;
+  XTab<T> tab;
   int L;
   long long b0;
   int m0 = 0, mn = 1 << 30;
@@ -712,17 +782,61 @@ struct ColsOut {
   // xtab[q] * xsrc + result
   C *obase = nullptr;
   const C *xsrc = nullptr;
-  const T *xtab = nullptr;
-  __device__ __forceinline__ void operator()(int c, int m, C v) const {
+  XTab<T> xtab = {};
+  // the multipliers staged in shared memory ([L/2 + 1][tcs] by folded kx), where they are
+  const T *stab = nullptr, *sxtab = nullptr;
+  int tcs = 0;
+  static constexpr bool kPrefetch = PF;
+  // the epilogue's source value at (c, m) (zero without an epilogue)
+  __device__ __forceinline__ C prefetch(int c, int m) const {
+    if (!obase || c >= tcv || (m - m0 + L) % L >= mn) return czero<C>();
+    return xsrc[(size_t)m * (size_t)B + c];
+  }
+  __device__ __forceinline__ void put(int c, int m, C v, C x) const {
     if (c >= tcv || (m - m0 + L) % L >= mn) return;
     v = cscale(v, scale);
-    if (tab) v = cscale(v, qtab(tab, L, m, b0 + c));
+    const int f = m > L / 2 ? L - m : m;
+    if (stab) v = cscale(v, stab[f * tcs + c]);
+    else if (tab) v = cscale(v, tab.at(L, m, b0 + c));
     const size_t at = (size_t)m * (size_t)B + c;
     if (obase) {
-      obase[at] = cadd(cscale(xsrc[at], qtab(xtab, L, m, b0 + c)), v);
+      obase[at] = cadd(cscale(x, sxtab ? sxtab[f * tcs + c] : xtab.at(L, m, b0 + c)), v);
       return;
     }
     base[at] = v;
+  }
+  __device__ __forceinline__ void operator()(int c, int m, C v) const { put(c, m, v, prefetch(c, m)); }
+};
+
+// The x pass's multipliers for a tile of TC columns from b0, in per-coefficient layout
+// (XTab::col), copied to shared memory dst[f][TC], f <= L/2, by 16-byte cp.async.  The
+// caller waits (cp_async_wait_all, then a block barrier) before reading them.
+template <typename T, int L, int TC, int NT>
+__device__ __forceinline__ void stage_col_rows(T *dst, const T *col, long long b0) {
+  constexpr int VEC = 16 / (int)sizeof(T), ROWV = TC / VEC, HP = L / 2 + 1;
+  static_assert(TC % VEC == 0, "a tile row of multipliers is whole 16-byte chunks");
+  for (int e = threadIdx.x; e < HP * ROWV; e += NT) {
+    const int f = e / ROWV, k = e - f * ROWV;
+    cp_async<16>(dst + f * TC + k * VEC, col + (size_t)f * (size_t)L * HP + (size_t)b0 + (size_t)(k * VEC));
+  }
+}
+
+// first-stage multiplier of an inverse x pass from the staged values (none: stab null,
+// the same for the whole block)
+template <typename T, int TC>
+struct StagedMid {
+  static constexpr bool kActive = true;
+  const T *stab;
+  int L;
+  __device__ __forceinline__ void wait() const {
+    if (stab) {
+      cp_async_wait_all();
+      __syncthreads();
+    }
+  }
+  template <typename C>
+  __device__ __forceinline__ C operator()(int c, int m, C v) const {
+    return stab ? cscale(v, stab[(m > L / 2 ? L - m : m) * TC + c]) : v;
   }
 };
 // c2r packing on the fly: Z[m] = (X[m] + conj X[H-m]) + i (X[m] - conj X[H-m]) e^{+2 pi i m / N}
@@ -765,10 +879,10 @@ struct RowsIn {
 // without them keeps fewer registers)
 template <typename T, int L, int TC, int NT, int SIGN, int MINB = 1024 / NT, bool EXT = true>
 __global__ void __launch_bounds__(NT, MINB) k_fft_cols_fused(typename Cx<T>::type *data, long long B,
-                                                       const typename Cx<T>::type *tw, T scale, const T *tab,
+                                                       const typename Cx<T>::type *tw, T scale, XTab<T> tab,
                                                        int a0, int A, int m0, int mn,
                                                        const typename Cx<T>::type *src, typename Cx<T>::type *dst,
-                                                       const typename Cx<T>::type *xsrc, const T *xtab) {
+                                                       const typename Cx<T>::type *xsrc, XTab<T> xtab, bool stage) {
   using C = typename Cx<T>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
   C *tile = reinterpret_cast<C *>(smraw);
@@ -779,14 +893,42 @@ __global__ void __launch_bounds__(NT, MINB) k_fft_cols_fused(typename Cx<T>::typ
   const int lm0 = EXT && SIGN < 0 ? m0 : 0, lmn = EXT && SIGN < 0 ? mn : (1 << 30);
   const int sm0 = EXT && SIGN > 0 ? m0 : 0, smn = EXT && SIGN > 0 ? mn : (1 << 30);
   const C *alt = EXT && src ? src + (base - data) : nullptr;
-  first_stage_from<T, L, TC, NT, SIGN>(tile, ColsIn<C>{base, B, tcv, SIGN > 0 ? tab : nullptr, L, b0, lm0, lmn, alt});
+  // stage: the multipliers of this tile (per-coefficient layout) go to shared memory after
+  // the tile, by cp.async issued before the tile's loads, so no load waits on a table value
+  T *stab = nullptr, *sxtab = nullptr;
+  if (stage && tcv == TC) {
+    T *area = reinterpret_cast<T *>(tile + L * TC);
+    if (tab.col) {
+      stab = area;
+      stage_col_rows<T, L, TC, NT>(stab, tab.col, b0);
+      area += (L / 2 + 1) * TC;
+    }
+    if (EXT && SIGN < 0 && dst && xtab.col) {
+      sxtab = area;
+      stage_col_rows<T, L, TC, NT>(sxtab, xtab.col, b0);
+    }
+  }
+  const XTab<T> in_tab = SIGN > 0 && !stab ? tab : XTab<T>{};
+  if constexpr (SIGN > 0)
+    first_stage_from<T, L, TC, NT, SIGN>(tile, ColsIn<C>{base, B, tcv, in_tab, L, b0, lm0, lmn, alt},
+                                         StagedMid<T, TC>{stab, L});
+  else
+    first_stage_from<T, L, TC, NT, SIGN>(tile, ColsIn<C>{base, B, tcv, in_tab, L, b0, lm0, lmn, alt});
   constexpr int R0 = next_radix(L, 1), NSL = last_stage_ns(L);
   TileStagesUntil<T, L, TC, TC, NT, R0, NSL, SIGN, 1>::run(tile, tw);
+  if (SIGN < 0 && (stab || sxtab)) {  // the same for the whole block
+    cp_async_wait_all();
+    __syncthreads();
+  }
   const size_t off = (size_t)(base - data);
-  last_stage_to<T, L, TC, NT, SIGN, 1>(tile, tw,
-                                       ColsOut<C, T>{base, B, tcv, scale, SIGN < 0 ? tab : nullptr, L, b0, sm0, smn,
-                                                     EXT && dst ? dst + off : nullptr, EXT && xsrc ? xsrc + off : nullptr,
-                                                     xtab});
+  if (EXT && SIGN < 0 && dst)
+    last_stage_to<T, L, TC, NT, SIGN, 1>(tile, tw,
+                                         ColsOut<C, T, true>{base, B, tcv, scale, tab, L, b0, sm0, smn, dst + off,
+                                                             xsrc + off, xtab, stab, sxtab, TC});
+  else
+    last_stage_to<T, L, TC, NT, SIGN, 1>(tile, tw,
+                                         ColsOut<C, T>{base, B, tcv, scale, SIGN < 0 ? tab : XTab<T>{}, L, b0, sm0, smn,
+                                                       nullptr, nullptr, {}, SIGN < 0 ? stab : nullptr, nullptr, TC});
 }
 
 template <typename T, int H, int RPC, int NT>
@@ -1040,10 +1182,10 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_fft_planes(typename Cx<T>::ty
       const long long b0 = (long long)sub * TC;
       const int tcv = (int)min((long long)TC, (long long)S - b0);
       C *base = pbase + b0;
-      first_stage_from<T, N, TC, NT, SIGN>(tile, ColsIn<C, true>{base, S, tcv, nullptr, N, b0});
+      first_stage_from<T, N, TC, NT, SIGN>(tile, ColsIn<C, true>{base, S, tcv, {}, N, b0});
       constexpr int R0 = next_radix(N, 1), NSL = last_stage_ns(N);
       TileStagesUntil<T, N, TC, TC, NT, R0, NSL, SIGN, 1>::run(tile, tw);
-      last_stage_to<T, N, TC, NT, SIGN, 1>(tile, tw, ColsOut<C, T>{base, S, tcv, (T)1, nullptr, N, b0});
+      last_stage_to<T, N, TC, NT, SIGN, 1>(tile, tw, ColsOut<C, T>{base, S, tcv, (T)1, {}, N, b0});
     }
     __syncthreads();
     if (first && threadIdx.x == 0) red_release_gpu(plane_done + plane, 1u);
@@ -1366,8 +1508,8 @@ struct FixedFft {
   static Sel whole_sel() { return Sel{0, N, 0, N}; }
 
   template <int TC, int NT, int SIGN>
-  static void cols(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const T *tab, int a0, int na,
-                   int m0, int mn, const C *src, C *dst, const C *xsrc, const T *xtab) {
+  static void cols(Context &ctx, C *d, int A, long long B, const C *tw, T scale, XTab<T> tab, int a0, int na,
+                   int m0, int mn, const C *src, C *dst, const C *xsrc, XTab<T> xtab) {
     static std::atomic<int> mask{0};
     const size_t smem = (size_t)N * (TC + 1) * sizeof(C);
     set_smem_once((const void *)k_fft_cols<T, N, TC, NT, SIGN>, smem, mask);
@@ -1377,19 +1519,24 @@ struct FixedFft {
     launched();
   }
   template <int TC, int NT, int SIGN, int MINB = 1024 / NT>
-  static void cols_fused(Context &ctx, C *d, int A, long long B, const C *tw, T scale, const T *tab, int a0,
-                         int na, int m0, int mn, const C *src, C *dst, const C *xsrc, const T *xtab) {
+  static void cols_fused(Context &ctx, C *d, int A, long long B, const C *tw, T scale, XTab<T> tab, int a0,
+                         int na, int m0, int mn, const C *src, C *dst, const C *xsrc, XTab<T> xtab) {
     static std::atomic<int> mask{0}, mask_plain{0};
-    const size_t smem = (size_t)N * TC * sizeof(C);
+    // FP32 x passes stage their multipliers' per-coefficient layouts in shared memory
+    // (FP64 would lose a resident CTA per SM to the extra shared memory)
+    const size_t rows = (size_t)(N / 2 + 1) * TC * sizeof(T);
+    const bool stage = F32 && B == (long long)N * S && (tab.col || (dst && xtab.col));
+    const size_t smem_max = (size_t)N * TC * sizeof(C) + (F32 ? 2 * rows : 0);
+    const size_t smem = (size_t)N * TC * sizeof(C) + (stage ? ((tab.col ? rows : 0) + (dst && xtab.col ? rows : 0)) : 0);
     dim3 grid((unsigned)((B + TC - 1) / TC), (unsigned)na);
     if (src || dst || m0 != 0 || mn < N) {
-      set_smem_once((const void *)k_fft_cols_fused<T, N, TC, NT, SIGN, MINB, true>, smem, mask);
+      set_smem_once((const void *)k_fft_cols_fused<T, N, TC, NT, SIGN, MINB, true>, smem_max, mask);
       k_fft_cols_fused<T, N, TC, NT, SIGN, MINB, true><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A, m0, mn,
-                                                                                       src, dst, xsrc, xtab);
+                                                                                       src, dst, xsrc, xtab, stage);
     } else {
-      set_smem_once((const void *)k_fft_cols_fused<T, N, TC, NT, SIGN, MINB, false>, smem, mask_plain);
+      set_smem_once((const void *)k_fft_cols_fused<T, N, TC, NT, SIGN, MINB, false>, smem_max, mask_plain);
       k_fft_cols_fused<T, N, TC, NT, SIGN, MINB, false><<<grid, NT, smem, ctx.stream>>>(d, B, tw, scale, tab, a0, A, m0,
-                                                                                        mn, src, dst, xsrc, xtab);
+                                                                                        mn, src, dst, xsrc, xtab, stage);
     }
     launched();
   }
@@ -1458,8 +1605,8 @@ struct FixedFft {
   }
   // SHUF: the variant with warp-shuffle middle and last stages (FP32, N = 512)
   static constexpr bool kShuf = F32 && N == 512;
-  static bool cols_tma(Context &ctx, int sign, C *d, int A, long long B, const C *tw, T scale, const T *tab, int a0,
-                       int na, int m0, int mn, const C *src, C *dst, const C *xsrc, const T *xtab, bool shuf = false) {
+  static bool cols_tma(Context &ctx, int sign, C *d, int A, long long B, const C *tw, T scale, XTab<T> tab, int a0,
+                       int na, int m0, int mn, const C *src, C *dst, const C *xsrc, XTab<T> xtab, bool shuf = false) {
     if constexpr (!kTma) {
       return false;
     } else {
@@ -1538,8 +1685,8 @@ struct FixedFft {
   // src: an out-of-place inverse x pass reads the columns other than kz = 0, N/2 from src
   // dst, xsrc, xtab: a forward x pass writes xtab[q] xsrc + result to dst instead of in place
   static void cols_cfg(Context &ctx, int cfg, int sign, C *d, int A, long long B, const C *tw, T scale,
-                       const T *tab = nullptr, int a0 = 0, int na = -1, int m0 = 0, int mn = N,
-                       const C *src = nullptr, C *dst = nullptr, const C *xsrc = nullptr, const T *xtab = nullptr) {
+                       XTab<T> tab = {}, int a0 = 0, int na = -1, int m0 = 0, int mn = N,
+                       const C *src = nullptr, C *dst = nullptr, const C *xsrc = nullptr, XTab<T> xtab = {}) {
     if (na < 0) na = A;
     if (cfg == 6 || cfg == 7) {
       // TMA-staged (7: with warp-shuffle middle and last stages where built), else the fused
@@ -1628,7 +1775,7 @@ struct FixedFft {
   }
   // inverse: the x pass over every column, then the y transforms of the selected
   // planes and the real transforms of the selected rows (output valid there)
-  static void c2r(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, int pv, const T *tab,
+  static void c2r(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, int pv, XTab<T> tab,
                   const Sel &sel, const C *src = nullptr) {
     // the x pass stores the selected planes only, the y pass the selected rows only
     cols_cfg(ctx, ccfg, +1, c, 1, (long long)N * S, tw, (T)1, tab, 0, -1, sel.x0, sel.nx, src);
@@ -1636,19 +1783,19 @@ struct FixedFft {
       planes<true>(ctx, c, tw, scale, pv);
       return;
     }
-    cols_cfg(ctx, ccfg, +1, c, N, S, tw, (T)1, nullptr, sel.x0, sel.nx, sel.y0, sel.ny);
+    cols_cfg(ctx, ccfg, +1, c, N, S, tw, (T)1, {}, sel.x0, sel.nx, sel.y0, sel.ny);
     rows_cfg(ctx, rcfg, true, c, tw, scale, sel);
   }
   // forward, input zero outside the selection: the selected rows, the selected
   // planes' y transforms, then the x pass over every column
-  static void r2c(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, int pv, const T *tab,
-                  const Sel &sel, C *dst = nullptr, const C *xsrc = nullptr, const T *xtab = nullptr) {
+  static void r2c(Context &ctx, C *c, const C *tw, T scale, int ccfg, int rcfg, int pv, XTab<T> tab,
+                  const Sel &sel, C *dst = nullptr, const C *xsrc = nullptr, XTab<T> xtab = {}) {
     if (kPlanes && pv >= 0 && sel.whole()) {
       planes<false>(ctx, c, tw, (T)1, pv);
     } else {
       rows_cfg(ctx, rcfg, false, c, tw, (T)1, sel);
       // rows outside the selection are zero: the y pass does not read them
-      cols_cfg(ctx, ccfg, -1, c, N, S, tw, (T)1, nullptr, sel.x0, sel.nx, sel.y0, sel.ny);
+      cols_cfg(ctx, ccfg, -1, c, N, S, tw, (T)1, {}, sel.x0, sel.nx, sel.y0, sel.ny);
     }
     // planes outside the selection are zero: the x pass does not read them
     cols_cfg(ctx, ccfg, -1, c, 1, (long long)N * S, tw, scale, tab, 0, -1, sel.x0, sel.nx, nullptr, dst, xsrc, xtab);
@@ -1712,6 +1859,54 @@ struct SharedTune {
 std::mutex g_tune_mutex;
 std::vector<SharedTune> g_tuned;
 
+// out[f][c] = q[f^2 + ky^2 + kz^2], f <= n/2, c = ky (n/2 + 1) + kz (ky signed)
+template <typename T>
+__global__ void k_col_table(T *out, const T *q, int n) {
+  const int S = n / 2 + 1, H = n / 2, per = n * S;
+  const int c = (int)(blockIdx.x * blockDim.x + threadIdx.x), f = (int)blockIdx.y;
+  if (c >= per) return;
+  const int ky = c / S, kz = c - ky * S, b = ky > H ? ky - n : ky;
+  out[(size_t)f * (size_t)per + (size_t)c] = q[(long long)f * f + (long long)b * b + (long long)kz * kz];
+}
+
+// Layouts of all registered tables together stay below this many bytes.
+constexpr size_t kColTableBytes = size_t(8) << 30;
+
+// The per-coefficient layout of the registered per-|k|^2 table q of an n^3 grid, built
+// on first use; nullptr where q is not registered, the layout does not fit, or the
+// stream is being captured (the x pass then gathers from q: the same values).
+template <typename T>
+const T *col_table(Context &ctx, const T *q, int n) {
+  if (!q || !ctx.fft.col_tables) return nullptr;
+  for (auto &e : ctx.col_tables) {
+    if (e->q != (const void *)q || e->n != n || e->elem != (int)sizeof(T)) continue;
+    if (e->col.ptr) return e->col.template as<T>();
+    if (e->failed) return nullptr;
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    GIC_CUDA(cudaStreamIsCapturing(ctx.stream, &st));
+    if (st != cudaStreamCaptureStatusNone) return nullptr;
+    const size_t per = (size_t)n * (size_t)(n / 2 + 1), bytes = (size_t)(n / 2 + 1) * per * sizeof(T);
+    size_t held = 0;
+    for (auto &o : ctx.col_tables) held += o->col.bytes;
+    const MemAccount *a = t_account;
+    if (held + bytes > kColTableBytes || (a && a->limit && a->used.load() + bytes > a->limit)) {
+      e->failed = true;
+      return nullptr;
+    }
+    try {
+      e->col.ensure(bytes);
+    } catch (const Error &) {
+      e->failed = true;
+      return nullptr;
+    }
+    k_col_table<T><<<dim3((unsigned)((per + 255) / 256), (unsigned)(n / 2 + 1)), 256, 0, ctx.stream>>>(
+        e->col.template as<T>(), q, n);
+    launched();
+    return e->col.template as<T>();
+  }
+  return nullptr;
+}
+
 template <typename T, int N>
 void fixed_transform(Context &ctx, typename Cx<T>::type *c, const typename Cx<T>::type *tw, double scale, bool inverse,
                      const T *tab, const CellBox *box, const typename Cx<T>::type *src, typename Cx<T>::type *dst,
@@ -1760,8 +1955,9 @@ void fixed_transform(Context &ctx, typename Cx<T>::type *c, const typename Cx<T>
     sel.y0 = ((box->start[1] % N) + N) % N;
     sel.ny = box->len[1];
   }
-  if (inverse) FixedFft<T, N>::c2r(ctx, c, tw, (T)scale, cc, rc, pv, tab, sel, src);
-  else FixedFft<T, N>::r2c(ctx, c, tw, (T)scale, cc, rc, pv, tab, sel, dst, xsrc, xtab);
+  const XTab<T> t{tab, col_table<T>(ctx, tab, N)}, xt{xtab, col_table<T>(ctx, xtab, N)};
+  if (inverse) FixedFft<T, N>::c2r(ctx, c, tw, (T)scale, cc, rc, pv, t, sel, src);
+  else FixedFft<T, N>::r2c(ctx, c, tw, (T)scale, cc, rc, pv, t, sel, dst, xsrc, xt);
 }
 
 // power-of-two sizes 32..1024 use the fixed-length passes

@@ -212,6 +212,7 @@ struct FftTables {
   std::vector<Tuned> tuned;
   int force_cols = -1, force_rows = -1;  // >= 0: use this candidate (tests)
   int force_planes = -2;                 // -2: tuned, -1: separate y and z passes, >= 0: this variant
+  bool col_tables = true;                // false: x passes gather their multipliers by |k|^2
   // plane pass: N plane counters and a ticket, zeroed before each launch; a word of
   // mapped host memory the kernel sets when one of its waits gives up
   DevBuf plane_sync;
@@ -344,6 +345,39 @@ struct Context {
   BufPool pool;
   ModScratch modscratch;
   std::vector<std::unique_ptr<CachedTable>> table_cache;
+  // Per-coefficient layouts of per-|k|^2 tables for the x passes of power-of-two
+  // transforms (n >= 256), built on first use by col_table (fft.cu).  The owner of a
+  // registered table keeps it unchanged at its address until drop_col_tables drops the
+  // registrations of its kind (`cache`: the modification algebra's cached tables).
+  struct ColTable {
+    const void *q = nullptr;
+    int n = 0, elem = 0;
+    bool cache = false;
+    bool failed = false;  // no room for the layout: the x pass gathers from q
+    DevBuf col;
+  };
+  std::vector<std::unique_ptr<ColTable>> col_tables;
+  void register_col_table(const void *q, int n, int elem, bool cache) {
+    if (!q || n < 256 || (n & (n - 1))) return;
+    for (auto &e : col_tables)
+      if (e->q == q && e->n == n && e->elem == elem) return;
+    auto e = std::make_unique<ColTable>();
+    e->q = q;
+    e->n = n;
+    e->elem = elem;
+    e->cache = cache;
+    col_tables.push_back(std::move(e));
+  }
+  void drop_col_tables(bool cache_only) {
+    std::vector<std::unique_ptr<ColTable>> keep;
+    for (auto &e : col_tables)
+      if (cache_only && !e->cache) keep.push_back(std::move(e));
+    col_tables.swap(keep);
+  }
+  void clear_table_cache() {
+    drop_col_tables(true);
+    table_cache.clear();
+  }
   bool dbl() const { return precision == GIC_FP64; }
 };
 

@@ -361,6 +361,7 @@ void transfer_setup(Context &ctx, const double *table, int nrows, int ncols) {
   T.lnk_max = lx_all.back();
   T.ready = true;
   T.inputs_hash = h;
+  ctx.drop_col_tables(false);
   ctx.table_cache.clear();
   for (auto &L : ctx.levels) {
     L->sqrtp.release();
@@ -429,6 +430,9 @@ static void build_lowpass_tables(Context &ctx, int coarse_index) {
   k_table_to_float<<<blocks, 256, 0, ctx.stream>>>(C.tab_lp_src_f.as<float>(), C.tab_lp_src.as<double>(), nq);
   k_table_to_float<<<blocks, 256, 0, ctx.stream>>>(C.tab_lp_f.as<float>(), C.tab_lp.as<double>(), nq);
   launched(4);
+  // the low-pass multiplies the coarse level's x passes (zoom combination)
+  ctx.register_col_table(C.tab_lp.ptr, C.n, (int)sizeof(double), false);
+  ctx.register_col_table(C.tab_lp_f.ptr, C.n, (int)sizeof(float), false);
 }
 
 template <>

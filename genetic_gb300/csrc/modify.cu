@@ -1217,7 +1217,7 @@ struct ModEngine {
         cur_tab = e.get();
         return;
       }
-    if (ctx.table_cache.size() >= 128) ctx.table_cache.clear();
+    if (ctx.table_cache.size() >= 128) ctx.clear_table_cache();
     auto e = std::make_unique<CachedTable>();
     e->key = std::move(key);
     e->d.ensure(nq * sizeof(double));
@@ -1226,6 +1226,7 @@ struct ModEngine {
                                                  sizeof(T) == 4 ? e->f.template as<float>() : nullptr, nq, sp);
     launched();
     cur_tab = e.get();
+    ctx.register_col_table(tabT(), lev(g).n, (int)sizeof(T), true);
     ctx.table_cache.push_back(std::move(e));
   }
   CachedTable *cur_tab = nullptr;

@@ -199,3 +199,33 @@ def test_shuffle_pass_box_inverse_512(built, bbks, precision, monkeypatch):
         ix = [(start[a] + np.arange(length[a])) % n for a in range(3)]
         out[tile] = real[np.ix_(ix[0], ix[1], ix[2])]
     assert np.array_equal(out['3,3'], out['7,3'])
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'mixed'])
+def test_column_tables_bit_identical_in_the_modification_algebra(built, bbks, precision, monkeypatch):
+    """The x passes' per-|k|^2 multipliers read from the per-coefficient layouts (the
+    default from 256^3 up) against the gathers from the tables by |k|^2 (GIC_FFT_COLTAB=0),
+    through the two-level realisation at 256^3 + 256^3 with the four modifications: the
+    zoom combination's low-pass, the modification algebra's filters and the metric's
+    epilogue all see the same values, so every field and particle is the same bits."""
+    levels = [('base', 100.0, 256), ('zoom', 96, 96, 96, 4, 256)]
+    out = {}
+    for flag in ('0', '1'):
+        monkeypatch.setenv('GIC_FFT_COLTAB', flag)
+        gen = make_generator(precision, bbks, levels, 8896131, 'random_seed')
+        gen.centre(50, 50, 50)
+        gen.select_sphere(2.0)
+        for name, t in (('overdensity', 1.5), ('vx', 0.0), ('vy', 0.0), ('vz', 0.0)):
+            gen.modify(name, 'absolute', t)
+        chi2 = gen.apply_modifications()
+        gen.done(apply_modifications=False)
+        out[flag] = (chi2, [gen.field(l, f) for l in range(2) for f in ('delta', 'psi_x', 'psi_y', 'psi_z')],
+                     [gen.particles(l) for l in range(2)])
+        gen.close()
+    monkeypatch.delenv('GIC_FFT_COLTAB')
+    a, b = out['0'], out['1']
+    assert a[0] == b[0]
+    for x, y in zip(a[1], b[1]):
+        assert np.array_equal(x, y)
+    for (p, v), (p2, v2) in zip(a[2], b[2]):
+        assert np.array_equal(p, p2) and np.array_equal(v, v2)
