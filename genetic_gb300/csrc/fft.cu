@@ -1998,6 +1998,13 @@ int rows_per_cta(int N) {
 
 }  // namespace
 
+template <typename T>
+const T *coefficient_table(Context &ctx, const T *q, int n) {
+  return col_table<T>(ctx, q, n);
+}
+template const float *coefficient_table<float>(Context &, const float *, int);
+template const double *coefficient_table<double>(Context &, const double *, int);
+
 int *FftTables::wait_flag() {
   if (!wait_flag_host) {
     void *h = nullptr, *d = nullptr;
@@ -2087,9 +2094,12 @@ bool fft_prunes(const Context &ctx, int n) {
 bool take_fft_wait_error(Context &ctx) {
   volatile int *f = ctx.fft.wait_flag_host;
   if (!f || *f == 0) return false;
-  ctx.last_error = *f >= 3 ? "FFT TMA-staged strided pass: a wait for a tile's bulk copy gave up; results of the transform "
-                             "are invalid"
-                           : "FFT plane pass: a wait for another CTA's tiles gave up; results of the transform are invalid";
+  ctx.last_error = *f == 4   ? "block means (k_fold_rows): a wait for the fine rows' bulk copies gave up; the coarse "
+                               "field is invalid"
+                  : *f >= 3 ? "FFT TMA-staged strided pass: a wait for a tile's bulk copy gave up; results of the "
+                              "transform are invalid"
+                            : "FFT plane pass: a wait for another CTA's tiles gave up; results of the transform are "
+                              "invalid";
   *f = 0;
   return true;
 }

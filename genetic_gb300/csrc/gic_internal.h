@@ -410,6 +410,11 @@ inline unsigned long long hs_elements(int n) { return (unsigned long long)n * n 
 template <typename T>
 const T *typed_table(Context &ctx, DevBuf &shadow, const double *tab, size_t nq);
 // the level tables in the fields' precision (their float copies are made with them)
+// The per-coefficient layout col[f][ky (n/2 + 1) + kz] = q[|k|^2] (f = |kx| <= n/2) of a
+// per-|k|^2 table q of an n^3 grid registered with Context::register_col_table, built on
+// first use; nullptr where q is not registered or the layout has no room.
+template <typename T>
+const T *coefficient_table(Context &ctx, const T *q, int n);
 template <typename T>
 const T *tab_main(const Level &L);
 template <typename T>

@@ -910,7 +910,8 @@ template <typename T, int R, int NW>
 __global__ void __launch_bounds__(32 * NW) k_fold_block_means(typename V2m<T>::type *out,
                                                                     const typename V2m<T>::type *in, int N,
                                                                     int r_rt, const T *tab,
-                                                                    const typename V2m<T>::type *btab, T fac) {
+                                                                    const typename V2m<T>::type *btab, T fac,
+                                                                    const T *tcol) {
   using C = typename V2m<T>::type;
   __shared__ C part[NW][32];
   const int r = R > 0 ? R : r_rt;
@@ -943,7 +944,8 @@ __global__ void __launch_bounds__(32 * NW) k_fold_block_means(typename V2m<T>::t
           const int qx = mir ? (N - kx) % N : kx, qy = mir ? (N - ky) % N : ky, qz = kz > H ? N - kz : kz;
           f[u] = in[((size_t)qx * N + qy) * S + qz];
           if (mir) f[u].y = -f[u].y;
-          t[u] = tab[qxy + (long long)qz * qz];
+          // the filter from its per-coefficient layout (contiguous along a warp's kz) where there is one
+          t[u] = tcol ? tcol[((size_t)(qx > H ? N - qx : qx) * N + qy) * S + qz] : tab[qxy + (long long)qz * qz];
         }
 #pragma unroll
         for (int u = 0; u < RU; ++u) {
@@ -972,6 +974,257 @@ __global__ void __launch_bounds__(32 * NW) k_fold_block_means(typename V2m<T>::t
     o.x = sr * fac;
     o.y = si * fac;
     out[id] = o;
+  }
+}
+
+// mbarrier and bulk-copy helpers of k_fold_rows
+__device__ __forceinline__ unsigned fold_smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ bool fold_mbar_wait(uint64_t *b, long long cycles) {
+  const long long t0 = clock64();
+  for (;;) {
+    unsigned done = 0;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(fold_smem_u32(b)), "r"(0u)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > cycles) return false;
+  }
+}
+// one bulk copy of `bytes` (a multiple of 16; both addresses 16-byte aligned) completing on bar
+__device__ __forceinline__ void fold_bulk(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   fold_smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(fold_smem_u32(bar))
+               : "memory");
+}
+template <int BYTES>
+__device__ __forceinline__ void fold_cp_async(void *smem, const void *gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(fold_smem_u32(smem)), "l"(gmem), "n"(BYTES));
+}
+
+// Row geometry of k_fold_rows for N: a staged row of the half spectrum (N/2 + 1 complex) or
+// of the filter's per-coefficient layout (N/2 + 1 real) starts on the 16-byte boundary at or
+// below the row and covers it: the shared-memory row is that many bytes, the element at
+// kz is at (row start mod 16) / element size + kz.
+template <typename T>
+struct FoldRowGeom {
+  // bytes of a copy of `bytes` starting `shift` bytes after a 16-byte boundary
+  __host__ __device__ static size_t span(size_t shift, size_t bytes) { return (shift + bytes + 15) & ~(size_t)15; }
+  // the largest such copy: row starts are multiples of the element size
+  __host__ __device__ static size_t data_bytes(int N) {
+    const size_t e = 2 * sizeof(T);
+    return span(e < 16 ? 16 - e : 0, (size_t)(N / 2 + 1) * e);
+  }
+  __host__ __device__ static size_t tab_bytes(int N) {
+    const size_t e = sizeof(T);
+    return span(e < 16 ? 16 - e : 0, (size_t)(N / 2 + 1) * e);
+  }
+  // shared memory: an mbarrier (16 bytes), 2 r^2 data rows, 2 r^2 filter rows, b(k) for k < N,
+  // and the partial sums of up to 4 groups of alias pairs for the 2 (N/r/2 + 1) outputs
+  static size_t smem(int r, int N) {
+    return 16 + 2 * (size_t)r * r * (data_bytes(N) + tab_bytes(N)) + (size_t)N * 2 * sizeof(T) +
+           4 * 2 * (size_t)(N / r / 2 + 1) * 2 * sizeof(T);
+  }
+};
+constexpr size_t kFoldRowsSmem = 220 * 1024;
+
+// per alias row of k_fold_rows: the staged rows' element offsets and b(kx) b(ky)
+template <typename T>
+struct FoldPair {
+  int own, town, mir, tmir;  // the row and its Hermitian partner row (elements of g, tv)
+  int noncanon;              // (kx, ky) takes the kz = 0, N/2 coefficients from its partner
+  T bxy_r, bxy_i;
+};
+
+// The same G by fine rows.  A CTA owns a pair of coarse columns {K, K'} with
+// K' = (-K_x, -K_y) mod N/r (a column equal to its partner alone): the r^2 fine rows
+// (K_x + m_x N/r, K_y + m_y N/r) of each, the ones whose Hermitian partners the other
+// column's mirrored aliases read, are copied once into shared memory with their filter
+// values and b(k), by one bulk copy (cp.async.bulk) per row, all in flight together.  Then
+// each output coefficient (side, K_z) sums its r^3 aliases from there with the products of
+// k_fold_block_means: the alias pairs (m_x, m_y) fall in up to 4 equal groups in order,
+// a thread sums a group (each pair's m_z terms first, then the pairs in order), and the
+// groups' sums are added in order.  tcol: the filter's per-coefficient layout, or nullptr
+// (tab by |k|^2, a gather of 4- or 8-byte cp.async).  The CTAs cover the columns with K <= K' (ids K_x nc + K_y):
+// K_x in [1, nc/2) with every K_y, then K_x = 0 and nc/2 with K_y in [0, nc/2].
+// err, wait_cycles: a wait for the bulk copies that gives up sets *err = 4 and the CTA
+// returns after its copies have landed (or a second wait has given up).  N % 4 == 0.
+template <typename T, int R, int NT>
+__global__ void __launch_bounds__(NT) k_fold_rows(typename V2m<T>::type *out, const typename V2m<T>::type *in, int N,
+                                                  const T *tab, const T *tcol, const typename V2m<T>::type *btab,
+                                                  T fac, int *err, long long wait_cycles) {
+  using C = typename V2m<T>::type;
+  using G = FoldRowGeom<T>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ FoldPair<T> pairs[2 * R * R];
+  __shared__ int s_stop;
+  constexpr int R2 = R * R;
+  const int nc = N / R, Sc = nc / 2 + 1, H = N / 2, S = H + 1;
+  int KX, KY;
+  {
+    const int p = (int)blockIdx.x, head = (nc / 2 - 1) * nc;
+    if (p < head) {
+      KX = 1 + p / nc;
+      KY = p - (KX - 1) * nc;
+    } else {
+      const int q = p - head;
+      KX = q < nc / 2 + 1 ? 0 : nc / 2;
+      KY = q % (nc / 2 + 1);
+    }
+  }
+  const int PX = (nc - KX) % nc, PY = (nc - KY) % nc;
+  const int sides = (PX == KX && PY == KY) ? 1 : 2;
+  const size_t DB = G::data_bytes(N), TB = G::tab_bytes(N);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smraw);
+  unsigned char *drows = smraw + 16;
+  unsigned char *trows = drows + 2 * R2 * DB;
+  C *bt = reinterpret_cast<C *>(trows + 2 * R2 * TB);
+  const int nrow = sides * R2;
+  if (threadIdx.x == 0) {
+    s_stop = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(fold_smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // the bulk copies, spread over the first warp's lanes: each lane announces its bytes
+  // before it issues them, and lane 0 arrives after the whole warp has announced, so the
+  // phase completes only when every copy has landed.  A row's copy starts on the 16-byte
+  // boundary at or below the row and ends on the one at or above its end: for the array
+  // of N^2 rows (N % 4 == 0) and the per-coefficient layout of a power-of-two N, the
+  // bytes before and after a row belong to its neighbouring rows, inside the buffer.
+  if (threadIdx.x < 32) {
+    unsigned mine = 0;
+    for (int row = (int)threadIdx.x; row < nrow; row += 32) {
+      const int sd = row / R2, pr = row - sd * R2;
+      const int kx = (sd ? PX : KX) + (pr / R) * nc, ky = (sd ? PY : KY) + (pr % R) * nc;
+      const uintptr_t a = (uintptr_t)(in + ((size_t)kx * N + ky) * S);
+      mine += (unsigned)G::span(a & 15, (size_t)S * sizeof(C));
+      if (tcol) {
+        const uintptr_t b = (uintptr_t)(tcol + ((size_t)(kx > H ? N - kx : kx) * N + ky) * S);
+        mine += (unsigned)G::span(b & 15, (size_t)S * sizeof(T));
+      }
+    }
+    if (threadIdx.x == 0) mine += (unsigned)(N * sizeof(C));
+    if (mine)
+      asm volatile("mbarrier.expect_tx.shared::cta.b64 [%0], %1;" ::"r"(fold_smem_u32(bar)), "r"(mine) : "memory");
+    __syncwarp();
+    if (threadIdx.x == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(fold_smem_u32(bar)) : "memory");
+    for (int row = (int)threadIdx.x; row < nrow; row += 32) {
+      const int sd = row / R2, pr = row - sd * R2;
+      const int kx = (sd ? PX : KX) + (pr / R) * nc, ky = (sd ? PY : KY) + (pr % R) * nc;
+      const uintptr_t a = (uintptr_t)(in + ((size_t)kx * N + ky) * S);
+      fold_bulk(drows + row * DB, (const void *)(a & ~(uintptr_t)15), (unsigned)G::span(a & 15, (size_t)S * sizeof(C)),
+                bar);
+      if (tcol) {
+        const uintptr_t b = (uintptr_t)(tcol + ((size_t)(kx > H ? N - kx : kx) * N + ky) * S);
+        fold_bulk(trows + row * TB, (const void *)(b & ~(uintptr_t)15),
+                  (unsigned)G::span(b & 15, (size_t)S * sizeof(T)), bar);
+      }
+    }
+    if (threadIdx.x == 0) fold_bulk(bt, btab, (unsigned)(N * sizeof(C)), bar);
+  }
+  if (!tcol) {
+    // the filter by |k|^2: a gather, element by element (no shift: rows start aligned)
+    const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+    for (int row = warp; row < nrow; row += NT / 32) {
+      const int sd = row / R2, pr = row - sd * R2;
+      const int kx = (sd ? PX : KX) + (pr / R) * nc, ky = (sd ? PY : KY) + (pr % R) * nc;
+      const long long sx = kx > H ? kx - N : kx, sy = ky > H ? ky - N : ky, qxy = sx * sx + sy * sy;
+      T *dst = reinterpret_cast<T *>(trows + row * TB);
+      for (int kz = lane; kz < S; kz += 32) fold_cp_async<sizeof(T)>(dst + kz, tab + qxy + (long long)kz * kz);
+    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+  }
+  if (threadIdx.x == 0 && !fold_mbar_wait(bar, wait_cycles)) {
+    s_stop = 1;
+    atomicExch(err, 4);
+    fold_mbar_wait(bar, wait_cycles);  // the copies still in flight write this CTA's shared memory
+  }
+  __syncthreads();
+  if (s_stop) return;
+  // per alias row: offsets of the row and of its partner, in elements
+  if ((int)threadIdx.x < nrow) {
+    const int row = (int)threadIdx.x, sd = row / R2, pr = row - sd * R2;
+    const int kx = (sd ? PX : KX) + (pr / R) * nc, ky = (sd ? PY : KY) + (pr % R) * nc;
+    const int qx = (N - kx) % N, qy = (N - ky) % N;
+    const int prow = (sides == 2 ? 1 - sd : 0) * R2 + (qx / nc) * R + qy / nc;
+    auto dshift = [&](int x, int y) {
+      return (int)(((uintptr_t)(in + ((size_t)x * N + y) * S) & 15) / sizeof(C));
+    };
+    auto tshift = [&](int x, int y) {
+      return tcol ? (int)(((uintptr_t)(tcol + ((size_t)(x > H ? N - x : x) * N + y) * S) & 15) / sizeof(T)) : 0;
+    };
+    FoldPair<T> fp;
+    fp.own = (int)(row * (DB / sizeof(C))) + dshift(kx, ky);
+    fp.town = (int)(row * (TB / sizeof(T))) + tshift(kx, ky);
+    fp.mir = (int)(prow * (DB / sizeof(C))) + dshift(qx, qy);
+    fp.tmir = (int)(prow * (TB / sizeof(T))) + tshift(qx, qy);
+    fp.noncanon = kx > H || ((kx == 0 || kx == H) && ky > H);
+    const C bx = bt[kx], by = bt[ky];
+    fp.bxy_r = bx.x * by.x - bx.y * by.y;
+    fp.bxy_i = bx.x * by.y + bx.y * by.x;
+    pairs[row] = fp;
+  }
+  __syncthreads();
+  const C *g = reinterpret_cast<const C *>(drows);
+  const T *tv = reinterpret_cast<const T *>(trows);
+  // the alias pairs in NQ groups of PQ: a work item sums one group for one output
+  // coefficient into part[group][output]
+  constexpr int NQ = R2 < 4 ? R2 : 4, PQ = R2 / NQ;
+  static_assert(R2 % NQ == 0, "equal groups of alias pairs");
+  const int nout = sides * Sc;
+  C *part = bt + N;
+  for (int item = threadIdx.x; item < NQ * nout; item += NT) {
+    const int q = item / nout, o = item - q * nout;
+    const int side = o / Sc, KZ = o - side * Sc;
+    T sr = 0, si = 0;
+    for (int pr = q * PQ; pr < (q + 1) * PQ; ++pr) {
+      const FoldPair<T> P = pairs[side * R2 + pr];
+      T ar = 0, ai = 0;
+#pragma unroll
+      for (int mz = 0; mz < R; ++mz) {
+        const int kz = KZ + mz * nc;
+        const bool mir = kz > H || ((kz == 0 || kz == H) && P.noncanon);
+        C f;
+        T t;
+        if (mir) {
+          const int at = kz > H ? N - kz : kz;
+          f = g[P.mir + at];
+          f.y = -f.y;
+          t = tv[P.tmir + at];
+        } else {
+          f = g[P.own + kz];
+          t = tv[P.town + kz];
+        }
+        const C bz = bt[kz];
+        const T b_r = P.bxy_r * bz.x - P.bxy_i * bz.y, b_i = P.bxy_r * bz.y + P.bxy_i * bz.x;
+        const T fr = f.x * t, fi = f.y * t;
+        ar += fr * b_r - fi * b_i;
+        ai += fr * b_i + fi * b_r;
+      }
+      sr += ar;
+      si += ai;
+    }
+    C v;
+    v.x = sr;
+    v.y = si;
+    part[q * nout + o] = v;
+  }
+  __syncthreads();
+  for (int o = threadIdx.x; o < nout; o += NT) {
+    const int side = o / Sc, KZ = o - side * Sc;
+    T sr = 0, si = 0;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      sr += part[q * nout + o].x;
+      si += part[q * nout + o].y;
+    }
+    C res;
+    res.x = sr * fac;
+    res.y = si * fac;
+    out[((size_t)(side ? PX : KX) * nc + (side ? PY : KY)) * Sc + KZ] = res;
   }
 }
 
@@ -1532,10 +1785,30 @@ struct ModEngine {
     const C *bt = S.btab.template as<C>();
     // 32 coefficients per CTA, the r^2 alias pairs over its warps
     const unsigned ctas = nblk(ncomplex, 32);
-    if (r == 2) k_fold_block_means<T, 2, 4><<<ctas, 128, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac);
-    else if (r == 4) k_fold_block_means<T, 4, 16><<<ctas, 512, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac);
-    else if (r == 8) k_fold_block_means<T, 8, 16><<<ctas, 512, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac);
-    else k_fold_block_means<T, 0, 8><<<ctas, 256, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac);
+    const T *tc = coefficient_table<T>(ctx, tabT(), F.n);
+    // by fine rows where a CTA's 2 r^2 rows, their filter values and b(k) fit in shared memory
+    const size_t rows_smem = FoldRowGeom<T>::smem(r, F.n);
+    const bool aligned = (((uintptr_t)src | (uintptr_t)tc | (uintptr_t)bt) & 15) == 0;
+    if ((r == 2 || r == 4) && F.n % 4 == 0 && aligned && rows_smem <= kFoldRowsSmem) {
+      static std::atomic<int> done2{0}, done4{0};
+      const void *fn = r == 2 ? (const void *)k_fold_rows<T, 2, 256> : (const void *)k_fold_rows<T, 4, 256>;
+      std::atomic<int> &done = r == 2 ? done2 : done4;
+      if (!(done.load() & (1 << (ctx.device & 31)))) {
+        GIC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFoldRowsSmem));
+        done.fetch_or(1 << (ctx.device & 31));
+      }
+      // the column pairs: K_x in [1, nc/2) with every K_y, K_x = 0 and nc/2 with K_y <= nc/2
+      const unsigned cols = (unsigned)((nc / 2 - 1) * nc + 2 * (nc / 2 + 1));
+      int *err = ctx.fft.wait_flag();
+      const long long wait_cycles = 1ll << 31;
+      if (r == 2)
+        k_fold_rows<T, 2, 256><<<cols, 256, rows_smem, ctx.stream>>>(g, src, F.n, tabT(), tc, bt, fac, err, wait_cycles);
+      else
+        k_fold_rows<T, 4, 256><<<cols, 256, rows_smem, ctx.stream>>>(g, src, F.n, tabT(), tc, bt, fac, err, wait_cycles);
+    } else if (r == 2) k_fold_block_means<T, 2, 4><<<ctas, 128, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac, tc);
+    else if (r == 4) k_fold_block_means<T, 4, 16><<<ctas, 512, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac, tc);
+    else if (r == 8) k_fold_block_means<T, 8, 16><<<ctas, 512, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac, tc);
+    else k_fold_block_means<T, 0, 8><<<ctas, 256, 0, ctx.stream>>>(g, src, F.n, r, tabT(), bt, fac, tc);
     launched();
     fft_c2r_3d<T>(ctx, reinterpret_cast<T *>(g), nc, std::pow((double)nc, -1.5));
     const int sx = (int)std::lround((F.x0[0] - Cl.x0[0]) / Cl.dx), sy = (int)std::lround((F.x0[1] - Cl.x0[1]) / Cl.dx),
